@@ -1,0 +1,344 @@
+"""Python binding of the GB300 block-DDA C ABI (``include/bdda.h``).
+
+Thin ctypes layer over ``block-dda_gb300/_lib/libbdda.so`` used by the tests,
+the benchmark and ``__graft_entry__``.  There is no CPU fallback: if the
+library is missing, :func:`lib` raises.  Host matrices are numpy complex128
+arrays in column-major (Fortran) order, exactly the reference's Eigen layout
+(column l = right-hand side, row 3*m + c = component c of dipole m).
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_BREAKDOWN, ERR_NOT_CONVERGED = 0, 1, 2, 3, 4, 5
+PREC_FP64, PREC_FP32 = 1, 2
+SOLVER_COCG_RQ, SOLVER_BICGSTAB, SOLVER_BICGGR = 0, 1, 2
+SOLVE_FP64, SOLVE_MIXED = 0, 1
+SOLVERS = {"cocg_rq": SOLVER_COCG_RQ, "bicgstab": SOLVER_BICGSTAB, "bicggr": SOLVER_BICGGR}
+KERNEL_NAMES = ["passA", "passB", "passC", "passD", "passE", "gram", "update", "small", "other"]
+
+# every symbol include/bdda.h declares
+EXPORTS = [
+    "bdda_op_create", "bdda_op_destroy", "bdda_op_set_dipoles", "bdda_op_info", "bdda_mbt_fft_mvp",
+    "bdda_op_mvp_device", "bdda_solve_opts_default", "bdda_solve_device", "bdda_solve", "bdda_qr_reduced",
+    "bdda_mie_a1b1", "bdda_aggregate", "bdda_incident_fields", "bdda_cross_sections", "bdda_op_set_timing",
+    "bdda_op_kernel_stats", "bdda_last_error",
+]
+
+
+class BddaError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"bdda error {code}: {msg}")
+        self.code = code
+
+
+class SolveOpts(ct.Structure):
+    _fields_ = [("solver", ct.c_int), ("jacobi", ct.c_int), ("precision", ct.c_int), ("tol", ct.c_double),
+                ("itermax", ct.c_int), ("true_tol", ct.c_double), ("inner_tol", ct.c_double),
+                ("max_refine", ct.c_int), ("check_every", ct.c_int)]
+
+
+class SolveStats(ct.Structure):
+    _fields_ = [("status", ct.c_int), ("iterations", ct.c_int), ("refinements", ct.c_int), ("mvps", ct.c_int),
+                ("final_err", ct.c_double), ("true_res_max", ct.c_double), ("ms_solve", ct.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = False):
+    """Load libbdda.so (raises if it was not built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"CUDA library not built: {path} (run __graft_entry__.build())")
+        _build.build()
+    L = ct.CDLL(path)
+    vp, ip, dp = ct.c_void_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_double)
+    L.bdda_op_create.argtypes = [ct.POINTER(vp), ip, ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_int]
+    L.bdda_op_destroy.argtypes = [vp]
+    L.bdda_op_set_dipoles.argtypes = [vp, ip, ct.c_int]
+    L.bdda_op_info.argtypes = [vp, ip, ip, ip]
+    L.bdda_mbt_fft_mvp.argtypes = [vp, dp, dp]
+    L.bdda_op_mvp_device.argtypes = [vp, ct.c_int, vp, ct.c_int, vp, ct.c_int, ct.c_int, vp, vp, vp]
+    L.bdda_solve_opts_default.argtypes = [ct.POINTER(SolveOpts)]
+    L.bdda_solve_opts_default.restype = None
+    L.bdda_solve_device.argtypes = [vp, ct.POINTER(SolveOpts), vp, vp, ct.c_int, vp, ct.c_int, ct.c_int,
+                                    ct.POINTER(SolveStats), vp]
+    L.bdda_solve.argtypes = [vp, ct.POINTER(SolveOpts), dp, dp, ct.c_int, dp, ct.c_int, ct.c_int,
+                             ct.POINTER(SolveStats)]
+    L.bdda_qr_reduced.argtypes = [dp, ct.c_int, ct.c_int, ct.c_int, dp, ct.c_int, dp]
+    L.bdda_mie_a1b1.argtypes = [ct.c_double, ct.c_double, dp, dp, dp, dp, dp, dp]
+    L.bdda_aggregate.argtypes = [ct.c_int, ct.c_double, ct.c_double, ct.c_ulonglong, ip, ip]
+    L.bdda_incident_fields.argtypes = [ip, ct.c_double, ip, ct.c_int, ct.c_double, ct.c_int, dp, dp, dp, ct.c_int]
+    L.bdda_cross_sections.argtypes = [ct.c_double, dp, dp, ct.c_int, dp, ct.c_int, ct.c_int, ct.c_int, dp]
+    L.bdda_op_set_timing.argtypes = [vp, ct.c_int]
+    L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
+    L.bdda_last_error.restype = ct.c_char_p
+    L.bdda_host_fft_line.argtypes = [ct.c_int, ct.c_int, ct.c_int, dp, ip]
+    _LIB = L
+    return L
+
+
+def _check(rc, allow=()):
+    if rc != OK and rc not in allow:
+        raise BddaError(rc, lib().bdda_last_error().decode())
+    return rc
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ct.POINTER(ct.c_double))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(ct.POINTER(ct.c_int))
+
+
+def _cmat(a, rows=None):
+    """complex128 column-major copy (or view) of a matrix / vector."""
+    a = np.asarray(a, dtype=np.complex128)
+    if a.ndim == 1:
+        a = a[:, None]
+    return np.asfortranarray(a)
+
+
+# ---------------------------------------------------------------------------
+# operator
+# ---------------------------------------------------------------------------
+
+class Operator:
+    """Green-tensor operator of one lattice box (``bdda_op``)."""
+
+    def __init__(self, n, lf, k, prec=PREC_FP64 | PREC_FP32, f=3):
+        self._h = ct.c_void_p()
+        n3 = np.ascontiguousarray(n, dtype=np.int32)
+        k = complex(k)
+        _check(lib().bdda_op_create(ct.byref(self._h), _iptr(n3), f, float(lf), k.real, k.imag, prec))
+        self.n = tuple(int(v) for v in n3)
+        self.lf = float(lf)
+        self.k = k
+        self.nocc = 0
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().bdda_op_destroy(self._h)
+            self._h = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_dipoles(self, address):
+        a = np.ascontiguousarray(address, dtype=np.int32)
+        _check(lib().bdda_op_set_dipoles(self._h, _iptr(a), int(a.size)))
+        self.nocc = int(a.size)
+
+    def info(self):
+        P = np.zeros(3, np.int32)
+        nocc, nl = ct.c_int(), ct.c_int()
+        _check(lib().bdda_op_info(self._h, _iptr(P), ct.byref(nocc), ct.byref(nl)))
+        return tuple(int(v) for v in P), nocc.value, nl.value
+
+    def mbt_fft_mvp(self, p_hat):
+        """Reference ``MBT_fft_mvp`` on a full cuboid vector (host, complex128)."""
+        x = np.ascontiguousarray(p_hat, dtype=np.complex128)
+        y = np.empty_like(x)
+        _check(lib().bdda_mbt_fft_mvp(self._h, _dptr(x), _dptr(y)))
+        return y
+
+    def mvp_device(self, x, y, L, ldx, ldy, prec=PREC_FP64, diag=None, jpre=None, stream=None):
+        """Block MVP on device pointers (ints, e.g. ``torch.Tensor.data_ptr()``)."""
+        _check(lib().bdda_op_mvp_device(self._h, prec, ct.c_void_p(x), ldx, ct.c_void_p(y), ldy, L,
+                                        ct.c_void_p(diag) if diag else None, ct.c_void_p(jpre) if jpre else None,
+                                        ct.c_void_p(stream) if stream else None))
+
+    def set_timing(self, on=True):
+        _check(lib().bdda_op_set_timing(self._h, 1 if on else 0))
+
+    def kernel_stats(self, reset=False):
+        n = len(KERNEL_NAMES)
+        ms = (ct.c_double * n)()
+        la = (ct.c_longlong * n)()
+        m = lib().bdda_op_kernel_stats(self._h, ms, la, n, 1 if reset else 0)
+        return {KERNEL_NAMES[i]: {"ms": ms[i], "launches": la[i]} for i in range(m)}
+
+
+def solve_opts(solver="cocg_rq", jacobi=True, precision=SOLVE_FP64, tol=1e-2, itermax=300, true_tol=0.0,
+               inner_tol=0.0, max_refine=8, check_every=4) -> SolveOpts:
+    o = SolveOpts()
+    lib().bdda_solve_opts_default(ct.byref(o))
+    o.solver = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+    o.jacobi = 1 if jacobi else 0
+    o.precision = int(precision)
+    o.tol = float(tol)
+    o.itermax = int(itermax)
+    o.true_tol = float(true_tol)
+    o.inner_tol = float(inner_tol)
+    o.max_refine = int(max_refine)
+    o.check_every = int(check_every)
+    return o
+
+
+def solve(op: Operator, diag, B, opts: SolveOpts, allow_not_converged=True):
+    """Host-buffer solve (``bdda_solve``).  Returns (X, stats dict)."""
+    d = np.ascontiguousarray(diag, dtype=np.complex128)
+    Bm = _cmat(B)
+    n, L = Bm.shape
+    X = np.zeros((n, L), dtype=np.complex128, order="F")
+    st = SolveStats()
+    allow = (ERR_NOT_CONVERGED,) if allow_not_converged else ()
+    _check(lib().bdda_solve(op.handle, ct.byref(opts), _dptr(d), _dptr(Bm), n,
+                            _dptr(X), n, L, ct.byref(st)), allow)
+    return X, st.as_dict()
+
+
+def solve_device(op: Operator, diag_ptr, B_ptr, ldb, X_ptr, ldx, L, opts: SolveOpts, stream=None,
+                 allow_not_converged=True):
+    st = SolveStats()
+    allow = (ERR_NOT_CONVERGED,) if allow_not_converged else ()
+    _check(lib().bdda_solve_device(op.handle, ct.byref(opts), ct.c_void_p(diag_ptr), ct.c_void_p(B_ptr), ldb,
+                                   ct.c_void_p(X_ptr), ldx, L, ct.byref(st), ct.c_void_p(stream) if stream else None),
+           allow)
+    return st.as_dict()
+
+
+def qr_reduced(A):
+    a = _cmat(A)
+    m, n = a.shape
+    Q = np.zeros((m, n), dtype=np.complex128, order="F")
+    R = np.zeros((n, n), dtype=np.complex128, order="F")
+    _check(lib().bdda_qr_reduced(_dptr(a), m, n, m, _dptr(Q), m,
+                                 _dptr(R)))
+    return Q, R
+
+
+# ---------------------------------------------------------------------------
+# host physics (C++)
+# ---------------------------------------------------------------------------
+
+def mie_a1b1(wl0, r_p, eps_p, mu_p=1 + 0j, eps_m=1 + 0j, mu_m=1 + 0j):
+    vals = [np.array([complex(v).real, complex(v).imag]) for v in (eps_p, mu_p, eps_m, mu_m)]
+    a1 = np.zeros(2)
+    b1 = np.zeros(2)
+    _check(lib().bdda_mie_a1b1(float(wl0), float(r_p), *[_dptr(v) for v in vals], _dptr(a1), _dptr(b1)))
+    return complex(a1[0], a1[1]), complex(b1[0], b1[1])
+
+
+def polarizability(wl0, r_p, eps_p, k, mu_p=1 + 0j):
+    """alpha = 3 i a1 / (2 k^3) (Target_manager.cpp:232)."""
+    a1, _ = mie_a1b1(wl0, r_p, eps_p, mu_p)
+    return 3j * a1 / (2.0 * k ** 3)
+
+
+def aggregate(nocc, kf=1.0, Df=2.8, seed=1):
+    n = np.zeros(3, np.int32)
+    addr = np.zeros(nocc, np.int32)
+    _check(lib().bdda_aggregate(int(nocc), float(kf), float(Df), int(seed), _iptr(n), _iptr(addr)))
+    return tuple(int(v) for v in n), addr
+
+
+def incident_fields(n, lf, address, k, uinc, einc):
+    n3 = np.ascontiguousarray(n, dtype=np.int32)
+    a = np.ascontiguousarray(address, dtype=np.int32)
+    u = np.ascontiguousarray(uinc, dtype=np.float64).reshape(-1, 3)
+    e = np.ascontiguousarray(einc, dtype=np.complex128).reshape(-1, 3)
+    L = u.shape[0]
+    B = np.zeros((3 * a.size, L), dtype=np.complex128, order="F")
+    _check(lib().bdda_incident_fields(_iptr(n3), float(lf), _iptr(a), int(a.size), float(k), L, _dptr(u),
+                                      _dptr(e), _dptr(B), 3 * a.size))
+    return B
+
+
+def cross_sections(k, alpha0, E, P):
+    Em = _cmat(E)
+    Pm = _cmat(P)
+    n, L = Em.shape
+    out = np.zeros(3 * L)
+    a0 = np.array([complex(alpha0).real, complex(alpha0).imag])
+    _check(lib().bdda_cross_sections(float(k), _dptr(a0), _dptr(Em), n, _dptr(Pm),
+                                     n, n, L, _dptr(out)))
+    out = out.reshape(L, 3)
+    return out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy()
+
+
+def host_fft_line(x, inverse=False, prec=1):
+    """Run the device FFT core on the CPU (unit tests).  Returns (y, radices)."""
+    a = np.ascontiguousarray(x, dtype=np.complex128).copy()
+    rad = np.zeros(16, np.int32)
+    nst = lib().bdda_host_fft_line(int(a.size), 1 if inverse else 0, int(prec), _dptr(a), _iptr(rad))
+    if nst < 0:
+        raise BddaError(ERR_INVALID, "unsupported FFT length")
+    return a, [int(v) for v in rad[:nst]]
+
+
+@dataclass
+class Problem:
+    """A DDA problem on a lattice aggregate (f=3, vacuum medium)."""
+    n: tuple
+    lf: float
+    address: np.ndarray
+    k: float
+    alpha: np.ndarray   # per dipole
+    diag: np.ndarray    # 3*nocc (1/alpha)
+    B: np.ndarray       # 3*nocc x L, column-major
+
+    @property
+    def nocc(self):
+        return int(self.address.size)
+
+
+def directions(n_dirs, seed):
+    """Seeded propagation directions, uniform on the sphere, with two
+    orthonormal polarisations each: returns (uinc, einc) for L = 2*n_dirs."""
+    rng = np.random.default_rng(seed)
+    us, es = [], []
+    for i in range(n_dirs):
+        if i == 0:
+            u = np.array([0.0, 0.0, 1.0])
+        else:
+            v = rng.standard_normal(3)
+            u = v / np.linalg.norm(v)
+        a = np.array([1.0, 0.0, 0.0]) if abs(u[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+        e1 = a - np.dot(a, u) * u
+        e1 /= np.linalg.norm(e1)
+        e2 = np.cross(u, e1)
+        us += [u, u]
+        es += [e1.astype(np.complex128), e2.astype(np.complex128)]
+    return np.array(us), np.array(es)
+
+
+def make_problem(nocc, m, wl0=0.55, kf=1.0, Df=2.8, seed=1, n_dirs=1, mkd=0.5):
+    """Synthetic aggregate problem: |m| k d = mkd, dipole volume d^3,
+    alpha from the Mie a1 of the volume-equivalent sphere."""
+    n, addr = aggregate(nocc, kf, Df, seed)
+    k = 2 * np.pi / wl0
+    m = complex(m)
+    d = mkd / (abs(m) * k)
+    r_eq = d * (3.0 / (4.0 * np.pi)) ** (1.0 / 3.0)
+    alpha0 = polarizability(wl0, r_eq, m * m, k)
+    alpha = np.full(nocc, alpha0, dtype=np.complex128)
+    diag = np.repeat(1.0 / alpha, 3)
+    u, e = directions(n_dirs, seed + 1000)
+    B = incident_fields(n, d, addr, k, u, e)
+    return Problem(n=n, lf=d, address=addr, k=k, alpha=alpha, diag=diag, B=B)

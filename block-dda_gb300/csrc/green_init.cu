@@ -1,0 +1,178 @@
+// Green-tensor spectrum Ghat on the padded grid, built on the device in FP64.
+//
+// Replaces application_function + BT_fft + MBT_fft_init
+// (mvp_fft/application_function.cpp:21-40, mvp_fft/BT_fft.cpp:8-53,
+// mvp_fft/MBT_fft_init.cpp:22-35): instead of the length f^2 prod(2n_i-1) 1-D
+// MBT projection, the 3x3 block A(d) = -G(d lf) is evaluated on the 2x-padded
+// circulant grid (index j -> offset j for j < n, j - P for j > P - n, zero in
+// the gap and at d = 0), its 6 distinct components are transformed with a full
+// 3-D FFT in FP64, divided by Px*Py*Pz and re-tiled for the fused x pass.
+#include <vector>
+
+#include "fft_core.cuh"
+#include "mvp.hpp"
+
+namespace bdda {
+
+namespace {
+
+__device__ __forceinline__ bool circ_offset(int j, int n, int P, int* d) {
+  if (j < n) { *d = j; return true; }
+  if (j > P - n) { *d = j - P; return true; }
+  return false;
+}
+
+// g[comp][jx][jy][jz], comp = xx, xy, xz, yy, yz, zz of A = -G.
+__global__ void k_green_eval(double2* __restrict__ g, int nx, int ny, int nz, int Px, int Py, int Pz,
+                             double lf, double kr, double ki) {
+  const size_t ng = (size_t)Px * Py * Pz;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < ng; idx += (size_t)gridDim.x * blockDim.x) {
+    const int jz = (int)(idx % Pz);
+    const int jy = (int)((idx / Pz) % Py);
+    const int jx = (int)(idx / ((size_t)Pz * Py));
+    int dx, dy, dz;
+    double2 out[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) out[c] = make_double2(0.0, 0.0);
+    if (circ_offset(jx, nx, Px, &dx) && circ_offset(jy, ny, Py, &dy) && circ_offset(jz, nz, Pz, &dz) &&
+        (dx | dy | dz) != 0) {
+      const double rx = dx * lf, ry = dy * lf, rz = dz * lf;
+      const double r2 = rx * rx + ry * ry + rz * rz;
+      const double r = sqrt(r2);
+      // e = exp(i k r) / r with complex k = kr + i ki
+      double sn, cs;
+      sincos(kr * r, &sn, &cs);
+      const double damp = exp(-ki * r) / r;
+      const double2 e = make_double2(damp * cs, damp * sn);
+      // c1 = k^2 ; c2 = (1 - i k r) / r^2
+      const double2 c1 = make_double2(kr * kr - ki * ki, 2.0 * kr * ki);
+      const double2 c2 = make_double2((1.0 + ki * r) / r2, (-kr * r) / r2);
+      const double u[3] = {rx, ry, rz};
+      int c = 0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int b = a; b < 3; ++b) {
+          const double rr = u[a] * u[b] / r2;
+          const double dl = (a == b) ? 1.0 : 0.0;
+          // G_ab = (c1 (d - rr) - c2 (d - 3 rr)) e ; A = -G
+          const double p = dl - rr, q = dl - 3.0 * rr;
+          const double2 t = make_double2(c1.x * p - c2.x * q, c1.y * p - c2.y * q);
+          const double2 gab = cmul(t, e);
+          out[c++] = make_double2(-gab.x, -gab.y);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) g[(size_t)c * ng + idx] = out[c];
+  }
+}
+
+// In-place FFT of contiguous lines (length p.N), one warp per line.
+template <bool INV>
+__global__ void __launch_bounds__(kLineWarps * 32)
+k_fft_contig(double2* __restrict__ data, size_t nlines, AxisPlan p, const double2* __restrict__ tw) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t line = (size_t)blockIdx.x * kLineWarps + warp;
+  if (line >= nlines) return;
+  double2* s = smem + warp * p.N;
+  double2* d = data + line * p.N;
+  for (int i = lane; i < p.N; i += 32) s[i] = d[i];
+  __syncwarp();
+  warp_fft<INV>(s, tw, p, lane);
+  for (int i = lane; i < p.N; i += 32) d[i] = s[i];
+}
+
+// In-place FFT along the middle index of data[A][N][Cc], tiles of TS columns.
+constexpr int kStridedTile = 8;
+template <bool INV>
+__global__ void __launch_bounds__(kStridedTile * 32)
+k_fft_strided(double2* __restrict__ data, int N, size_t Cc, AxisPlan p, const double2* __restrict__ tw) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* smem = reinterpret_cast<double2*>(smem_raw);
+  const int lds = N | 1;
+  const size_t c0 = (size_t)blockIdx.x * kStridedTile;
+  double2* base = data + (size_t)blockIdx.y * N * Cc;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < N * kStridedTile; idx += kStridedTile * 32) {
+    const int w = idx % kStridedTile, i = idx / kStridedTile;
+    const size_t c = c0 + w;
+    smem[w * lds + i] = (c < Cc) ? base[(size_t)i * Cc + c] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  warp_fft<INV>(smem + (tid >> 5) * lds, tw, p, tid & 31);
+  __syncthreads();
+  for (int idx = tid; idx < N * kStridedTile; idx += kStridedTile * 32) {
+    const int w = idx % kStridedTile, i = idx / kStridedTile;
+    const size_t c = c0 + w;
+    if (c < Cc) base[(size_t)i * Cc + c] = smem[w * lds + i];
+  }
+}
+
+// g[comp][qx][y][z] / Ng  ->  ghat[y][zt][comp][qx][w]   (TZ-wide z tiles)
+template <typename C, int TZ>
+__global__ void k_green_tile(const double2* __restrict__ g, C* __restrict__ out, int Px, int Py, int Pz, double scale) {
+  const int nzt = (Pz + TZ - 1) / TZ;
+  const size_t total = (size_t)Py * nzt * 6 * Px * TZ;
+  const size_t ng = (size_t)Px * Py * Pz;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const int w = (int)(idx % TZ);
+    size_t t = idx / TZ;
+    const int qx = (int)(t % Px); t /= Px;
+    const int comp = (int)(t % 6); t /= 6;
+    const int zt = (int)(t % nzt);
+    const int y = (int)(t / nzt);
+    const int z = zt * TZ + w;
+    double2 v = make_double2(0.0, 0.0);
+    if (z < Pz) {
+      v = g[(size_t)comp * ng + ((size_t)qx * Py + y) * Pz + z];
+      v.x *= scale;
+      v.y *= scale;
+    }
+    out[idx] = cmake((decltype(C::x))v.x, (decltype(C::x))v.y);
+  }
+}
+
+}  // namespace
+
+cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_im,
+                            const double2* twx, const double2* twy, const double2* twz,
+                            double2* work, double2* ghat_d, float2* ghat_f, cudaStream_t st) {
+  const int Px = g.Px, Py = g.Py, Pz = g.Pz;
+  const size_t ng = (size_t)Px * Py * Pz;
+  cudaError_t e;
+  k_green_eval<<<1216, 256, 0, st>>>(work, g.nx, g.ny, g.nz, Px, Py, Pz, lf, k_re, k_im);
+  // z lines (contiguous)
+  {
+    size_t nlines = 6 * (size_t)Px * Py;
+    int sm = kLineWarps * Pz * (int)sizeof(double2);
+    e = cudaFuncSetAttribute(k_fft_contig<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kLineWarps * kMaxLine * (int)sizeof(double2));
+    if (e != cudaSuccess) return e;
+    k_fft_contig<false><<<(unsigned)((nlines + kLineWarps - 1) / kLineWarps), kLineWarps * 32, sm, st>>>(work, nlines, g.pz, twz);
+  }
+  e = cudaFuncSetAttribute(k_fft_strided<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kStridedTile * (kMaxLine | 1) * (int)sizeof(double2));
+  if (e != cudaSuccess) return e;
+  // y lines: data[6*Px][Py][Pz]
+  {
+    dim3 grid((unsigned)((Pz + kStridedTile - 1) / kStridedTile), 6 * Px);
+    int sm = kStridedTile * (Py | 1) * (int)sizeof(double2);
+    k_fft_strided<false><<<grid, kStridedTile * 32, sm, st>>>(work, Py, (size_t)Pz, g.py, twy);
+  }
+  // x lines: data[6][Px][Py*Pz]
+  {
+    size_t cc = (size_t)Py * Pz;
+    dim3 grid((unsigned)((cc + kStridedTile - 1) / kStridedTile), 6);
+    int sm = kStridedTile * (Px | 1) * (int)sizeof(double2);
+    k_fft_strided<false><<<grid, kStridedTile * 32, sm, st>>>(work, Px, cc, g.px, twx);
+  }
+  const double scale = 1.0 / (double)ng;
+  if (ghat_d) k_green_tile<double2, TileCfg<double>::TZ><<<2432, 256, 0, st>>>(work, ghat_d, Px, Py, Pz, scale);
+  if (ghat_f) k_green_tile<float2, TileCfg<float>::TZ><<<2432, 256, 0, st>>>(work, ghat_f, Px, Py, Pz, scale);
+  return cudaGetLastError();
+}
+
+}  // namespace bdda

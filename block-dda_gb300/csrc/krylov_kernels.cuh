@@ -1,0 +1,272 @@
+// Tall-skinny block kernels for the block Krylov solvers (included by solver.cu only).
+//
+// Blocks are n x L column-major (the reference's Eigen layout of B, X, S, AS,
+// Q ...; rows 3*m + c).  Coefficient matrices (L x L) are complex FP64,
+// column-major, in global memory.  All reductions run in a fixed order (per
+// CTA partials, then an ordered sum), so results are bitwise reproducible.
+#pragma once
+
+#include "common.cuh"
+
+namespace bdda {
+
+constexpr int kMaxL = 32;          // largest block width (nrhs) supported
+constexpr int kGramThreads = 256;
+constexpr int kGramRows = 32;      // rows per shared-memory sub-tile
+constexpr int kRowThreads = 64;    // rows per CTA of the row-transform kernels
+
+// Device-side solver control block (lives in device memory).
+struct SolverCtl {
+  int done;         // 1 once the stopping test passed (all later kernels return)
+  int status;       // 0 ok, 4 breakdown (singular L x L / non-finite / Cholesky)
+  int iter;         // iterations completed
+  int flags;
+  double err;       // last recurrence error (the value the reference prints)
+  double bnorm;     // ||B||_F of the (preconditioned) right-hand side
+};
+
+__device__ __forceinline__ bool ctl_skip(const SolverCtl* ctl) {
+  return ctl != nullptr && *(volatile const int*)&ctl->done != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Gram partials: partials[blk][i + j*L] = sum_{r in chunk} op(A[r,i]) B[r,j]
+// Each CTA owns a contiguous row chunk; FP32 data is multiplied in FP32 and
+// summed in FP32 over one 32-row sub-tile, then added to FP64 accumulators.
+// ---------------------------------------------------------------------------
+template <typename T, bool CONJ>
+__global__ void __launch_bounds__(kGramThreads)
+k_gram(const typename cplx<T>::type* __restrict__ A, int lda,
+       const typename cplx<T>::type* __restrict__ B, int ldb,
+       int n, int L, double2* __restrict__ partials, const SolverCtl* ctl) {
+  using C = typename cplx<T>::type;
+  if (ctl_skip(ctl)) return;
+  __shared__ C sa[kMaxL][kGramRows + 1];
+  __shared__ C sb[kMaxL][kGramRows + 1];
+  const int tid = threadIdx.x;
+  const int LL = L * L;
+  // entries owned by this thread: e = tid + k*256, k < 4  (L <= 32 -> LL <= 1024)
+  double2 acc[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) acc[k] = make_double2(0.0, 0.0);
+  const long long rows_per = ((long long)n + gridDim.x - 1) / gridDim.x;
+  const long long r0 = (long long)blockIdx.x * rows_per;
+  const long long r1 = min((long long)n, r0 + rows_per);
+  for (long long rb = r0; rb < r1; rb += kGramRows) {
+    const int nr = (int)min((long long)kGramRows, r1 - rb);
+    __syncthreads();
+    for (int idx = tid; idx < L * kGramRows; idx += kGramThreads) {
+      const int rr = idx % kGramRows, col = idx / kGramRows;
+      C va = czero<C>(), vb = czero<C>();
+      if (rr < nr) {
+        va = A[(size_t)col * lda + rb + rr];
+        vb = B[(size_t)col * ldb + rb + rr];
+      }
+      sa[col][rr] = va;
+      sb[col][rr] = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int e = tid + k * kGramThreads;
+      if (e < LL) {
+        const int i = e % L, j = e / L;
+        C s = czero<C>();
+        for (int rr = 0; rr < nr; ++rr) {
+          const C a = sa[i][rr], b = sb[j][rr];
+          s = CONJ ? cadd(s, cconjmul(a, b)) : cadd(s, cmul(a, b));
+        }
+        acc[k].x += (double)s.x;
+        acc[k].y += (double)s.y;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int e = tid + k * kGramThreads;
+    if (e < LL) partials[(size_t)blockIdx.x * LL + e] = acc[k];
+  }
+}
+
+// Column sums of |A[r,l]|^2 (squared column norms) -> partials[blk][l] (double)
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_colnorm2(const typename cplx<T>::type* __restrict__ A, int lda, int n, int L, double* __restrict__ partials) {
+  using C = typename cplx<T>::type;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long rows_per = ((long long)n + gridDim.x - 1) / gridDim.x;
+  const long long r0 = (long long)blockIdx.x * rows_per;
+  const long long r1 = min((long long)n, r0 + rows_per);
+  for (int l = warp; l < L; l += 8) {
+    double s = 0.0;
+    for (long long r = r0 + lane; r < r1; r += 32) {
+      const C v = A[(size_t)l * lda + r];
+      s += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) partials[(size_t)blockIdx.x * L + l] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Row transform: Out = A*Ma [+ B*Mb] [+ Cadd]
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kRowThreads)
+k_rowmm(int n, int L, const typename cplx<T>::type* A, int lda, const double2* __restrict__ Ma,
+        const typename cplx<T>::type* B, int ldb, const double2* __restrict__ Mb,
+        const typename cplx<T>::type* Cadd, int ldc,
+        typename cplx<T>::type* Out, int ldo, const SolverCtl* ctl) {
+  // Out may alias A, B or Cadd: every row is read completely before it is written.
+  using C = typename cplx<T>::type;
+  if (ctl_skip(ctl)) return;
+  // dynamic smem: ta[L][kRowThreads], tb[L][kRowThreads], ma[L*L], mb[L*L]
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* ta = reinterpret_cast<C*>(smem_raw);
+  C* tb = ta + L * kRowThreads;
+  C* ma = tb + (B ? L * kRowThreads : 0);
+  C* mb = ma + L * L;
+  const int tid = threadIdx.x;
+  const int LL = L * L;
+  for (int e = tid; e < LL; e += kRowThreads) {
+    const double2 v = Ma[e];
+    ma[e] = cmake((T)v.x, (T)v.y);
+    if (Mb) { const double2 w = Mb[e]; mb[e] = cmake((T)w.x, (T)w.y); }
+  }
+  const long long r = (long long)blockIdx.x * kRowThreads + tid;
+  const bool ok = r < n;
+  for (int l = 0; l < L; ++l) {
+    ta[l * kRowThreads + tid] = ok ? A[(size_t)l * lda + r] : czero<C>();
+    if (B) tb[l * kRowThreads + tid] = ok ? B[(size_t)l * ldb + r] : czero<C>();
+  }
+  __syncthreads();
+  if (!ok) return;
+  for (int j = 0; j < L; ++j) {
+    C acc = Cadd ? Cadd[(size_t)j * ldc + r] : czero<C>();
+    for (int l = 0; l < L; ++l) acc = cadd(acc, cmul(ta[l * kRowThreads + tid], ma[l + j * L]));
+    if (B)
+      for (int l = 0; l < L; ++l) acc = cadd(acc, cmul(tb[l * kRowThreads + tid], mb[l + j * L]));
+    Out[(size_t)j * ldo + r] = acc;
+  }
+}
+
+template <typename T>
+inline int rowmm_smem(int L, bool two) {
+  return (int)sizeof(typename cplx<T>::type) * ((two ? 2 : 1) * L * kRowThreads + 2 * L * L);
+}
+
+// Out = a*A + b*B (a, b complex FP64 scalars in device memory; null a -> 1; null B -> no term)
+template <typename T>
+__global__ void k_axpby(int n, int L, const double2* __restrict__ a, const typename cplx<T>::type* A, int lda,
+                        const double2* __restrict__ b, const typename cplx<T>::type* B, int ldb,
+                        typename cplx<T>::type* Out, int ldo, const SolverCtl* ctl) {
+  using C = typename cplx<T>::type;
+  if (ctl_skip(ctl)) return;
+  const C ca = a ? cmake((T)a->x, (T)a->y) : cmake((T)1, (T)0);
+  const C cb = b ? cmake((T)b->x, (T)b->y) : cmake((T)1, (T)0);
+  const size_t total = (size_t)n * L;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = idx / n, r = idx - l * n;
+    C v = cmul(ca, A[l * lda + r]);
+    if (B) v = cadd(v, cmul(cb, B[l * ldb + r]));
+    Out[l * ldo + r] = v;
+  }
+}
+
+// Complex dot partials over a whole block: partials[blk] = sum conj(A) * B  (FP64)
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_dotc(int n, int L, const typename cplx<T>::type* __restrict__ A, int lda,
+       const typename cplx<T>::type* __restrict__ B, int ldb, double2* __restrict__ partials, const SolverCtl* ctl) {
+  using C = typename cplx<T>::type;
+  if (ctl_skip(ctl)) return;
+  __shared__ double2 red[8];
+  const size_t total = (size_t)n * L;
+  double2 s = make_double2(0.0, 0.0);
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = idx / n, r = idx - l * n;
+    const C a = A[l * lda + r], b = B[l * ldb + r];
+    s.x += (double)a.x * (double)b.x + (double)a.y * (double)b.y;
+    s.y += (double)a.x * (double)b.y - (double)a.y * (double)b.x;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s.x += __shfl_down_sync(0xffffffffu, s.x, o);
+    s.y += __shfl_down_sync(0xffffffffu, s.y, o);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) red[warp] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t.x += red[w].x; t.y += red[w].y; }
+    partials[blockIdx.x] = t;
+  }
+}
+
+// Precision conversion / copy of an n x L block.
+template <typename TO, typename TI>
+__global__ void k_convert(int n, int L, const typename cplx<TI>::type* __restrict__ in, int ldi,
+                          typename cplx<TO>::type* __restrict__ out, int ldo) {
+  const size_t total = (size_t)n * L;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = idx / n, r = idx - l * n;
+    const auto v = in[l * ldi + r];
+    out[l * ldo + r] = cmake((TO)v.x, (TO)v.y);
+  }
+}
+
+// X64 += D (D in T precision)
+template <typename T>
+__global__ void k_accumulate(int n, int L, const typename cplx<T>::type* __restrict__ D, int ldd,
+                             double2* __restrict__ X, int ldx) {
+  const size_t total = (size_t)n * L;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = idx / n, r = idx - l * n;
+    const auto d = D[l * ldd + r];
+    double2 x = X[l * ldx + r];
+    x.x += (double)d.x;
+    x.y += (double)d.y;
+    X[l * ldx + r] = x;
+  }
+}
+
+// R = B - Y (FP64)
+__global__ void k_residual(int n, int L, const double2* __restrict__ B, int ldb, const double2* __restrict__ Y, int ldy,
+                           double2* __restrict__ R, int ldr) {
+  const size_t total = (size_t)n * L;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = idx / n, r = idx - l * n;
+    R[l * ldr + r] = csub(B[l * ldb + r], Y[l * ldy + r]);
+  }
+}
+
+// Out = v o In   (per-row complex scaling, e.g. B_pre = jpre o B)
+template <typename TO, typename TI>
+__global__ void k_rowscale(int n, int L, const double2* __restrict__ v, const typename cplx<TI>::type* __restrict__ In, int ldi,
+                           typename cplx<TO>::type* __restrict__ Out, int ldo) {
+  const size_t total = (size_t)n * L;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = idx / n, r = idx - l * n;
+    const auto a = In[l * ldi + r];
+    const double2 s = v[r];
+    const double2 p = cmul(make_double2((double)a.x, (double)a.y), s);
+    Out[l * ldo + r] = cmake((TO)p.x, (TO)p.y);
+  }
+}
+
+// d -> 1/d (FP64) and its FP32 copies
+__global__ void k_diag_prep(int n, const double2* __restrict__ diag, double2* __restrict__ jpre64,
+                            float2* __restrict__ diag32, float2* __restrict__ jpre32) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 d = diag[i];
+    const double den = d.x * d.x + d.y * d.y;
+    const double2 j = make_double2(d.x / den, -d.y / den);
+    if (jpre64) jpre64[i] = j;
+    if (diag32) diag32[i] = make_float2((float)d.x, (float)d.y);
+    if (jpre32) jpre32[i] = make_float2((float)j.x, (float)j.y);
+  }
+}
+
+}  // namespace bdda

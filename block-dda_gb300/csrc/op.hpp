@@ -1,0 +1,99 @@
+// The operator object behind the C ABI (one lattice box + wavenumber).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "mvp.hpp"
+
+namespace bdda {
+
+// Thread-local last error text (bdda_last_error).
+void set_error(const std::string& msg);
+const char* last_error();
+
+// RAII device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b; else p = nullptr;
+    return e;
+  }
+  template <typename X> X* as() const { return static_cast<X*>(p); }
+};
+
+// Occupancy of the lattice by dipoles, on the device.
+struct Occupancy {
+  int nocc = 0;
+  int nlines = 0;
+  DevBuf occ, lines, lmask, address;
+};
+
+struct SolverWork;  // solver.cu
+
+struct Op {
+  int n[3] = {0, 0, 0};
+  int P[3] = {0, 0, 0};
+  int f = 3;
+  double lf = 0, kr = 0, ki = 0;
+  int prec = 0;  // bit mask BDDA_PREC_FP64 | BDDA_PREC_FP32
+  AxisPlan plan[3];
+  DevBuf tw64[3], tw32[3];
+  DevBuf ghat64, ghat32;
+  Occupancy dip;    // dipole occupancy (set_dipoles)
+  Occupancy cub;    // every cuboid site (the reference's MBT_fft_mvp vector)
+  DevBuf t1[2], t2[2];   // MVP workspace per precision (0 = FP64, 1 = FP32)
+  cudaStream_t stream = nullptr;
+  KernelTimer timer;
+  std::mutex mu;
+  std::shared_ptr<SolverWork> solver;   // cached Krylov workspace (solver.cu)
+  long long kernel_launches = 0;
+
+  MvpGeom geom(const Occupancy& o) const {
+    MvpGeom g;
+    g.nx = n[0]; g.ny = n[1]; g.nz = n[2];
+    g.Px = P[0]; g.Py = P[1]; g.Pz = P[2];
+    g.px = plan[0]; g.py = plan[1]; g.pz = plan[2];
+    g.nlines = o.nlines;
+    g.occ = o.occ.as<int>();
+    g.lines = o.lines.as<int>();
+    g.lmask = o.lmask.as<unsigned char>();
+    return g;
+  }
+  template <typename T> MvpPrec<T> tables() const;
+  ~Op();
+};
+
+template <> inline MvpPrec<double> Op::tables<double>() const {
+  return {tw64[0].as<double2>(), tw64[1].as<double2>(), tw64[2].as<double2>(), ghat64.as<double2>()};
+}
+template <> inline MvpPrec<float> Op::tables<float>() const {
+  return {tw32[0].as<float2>(), tw32[1].as<float2>(), tw32[2].as<float2>(), ghat32.as<float2>()};
+}
+
+// Build the occupancy tables from a host list of lattice addresses (null -> all sites).
+int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o);
+
+// y = [diag o x +] A_off x [o jpre] for L columns (device pointers, op->stream or st).
+template <typename T>
+int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, int ldx, typename cplx<T>::type* y, int ldy,
+                 int L, const typename cplx<T>::type* diag, const typename cplx<T>::type* jpre, cudaStream_t st,
+                 const int* done = nullptr);
+
+}  // namespace bdda
+
+// The opaque handle of the C ABI.
+struct bdda_op : public bdda::Op {};

@@ -1,0 +1,86 @@
+// FFT radix schedules and FP64 twiddle tables (host), plus a host entry point
+// that runs the exact device FFT core on the CPU for unit tests.
+#include <cmath>
+#include <vector>
+
+#include "../../include/bdda.h"
+#include "fft_core.cuh"
+#include "mvp.hpp"
+
+namespace bdda {
+
+bool make_axis_plan(int N, AxisPlan* p) {
+  if (N < 1 || N > kMaxLine) return false;
+  int a = 0, b = 0, c = 0, t = N;
+  while (t % 2 == 0) { t /= 2; ++a; }
+  while (t % 3 == 0) { t /= 3; ++b; }
+  while (t % 5 == 0) { t /= 5; ++c; }
+  if (t != 1) return false;
+  p->N = N;
+  p->nst = 0;
+  auto push = [&](int r) { p->radix[p->nst++] = r; };
+  while (a >= 3) { push(8); a -= 3; }
+  if (a == 2) push(4);
+  if (a == 1) push(2);
+  for (int i = 0; i < c; ++i) push(5);
+  for (int i = 0; i < b; ++i) push(3);
+  if (p->nst == 0) push(2);  // N == 1 is rejected by callers; keep the plan well formed
+  return p->nst <= kMaxStages;
+}
+
+void make_twiddles(int N, std::vector<double2>* out) {
+  out->resize(N);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int t = 0; t < N; ++t) {
+    // angle reduced to the first octant-friendly form through exact integer symmetry
+    long long num = t;  // exp(-2 pi i t / N)
+    double c, s;
+    if (4 * num == N) { c = 0.0; s = 1.0; }
+    else if (2 * num == N) { c = -1.0; s = 0.0; }
+    else if (4 * num == 3LL * N) { c = 0.0; s = -1.0; }
+    else if (num == 0) { c = 1.0; s = 0.0; }
+    else {
+      const double ang = two_pi * (double)num / (double)N;
+      c = std::cos(ang);
+      s = std::sin(ang);
+    }
+    (*out)[t] = make_double2(c, -s);
+  }
+}
+
+}  // namespace bdda
+
+extern "C" {
+
+// Runs the device FFT core (one "lane") on a host line: forward (natural ->
+// digit-reversed) or inverse (digit-reversed -> natural, unnormalised).
+// data: N interleaved complex values; prec 1 = FP64, 2 = FP32 arithmetic
+// (values are rounded to float and back).  Returns the number of stages, or
+// a negative value for an unsupported N.  Radices are written to radix (<= 16).
+int bdda_host_fft_line(int N, int inverse, int prec, double* data, int* radix) {
+  bdda::AxisPlan p;
+  if (!bdda::make_axis_plan(N, &p)) return -1;
+  std::vector<double2> tw;
+  bdda::make_twiddles(N, &tw);
+  if (prec == 1) {
+    std::vector<double2> s(N);
+    for (int i = 0; i < N; ++i) s[i] = make_double2(data[2 * i], data[2 * i + 1]);
+    if (inverse) bdda::warp_fft<true>(s.data(), tw.data(), p, 0, 1);
+    else bdda::warp_fft<false>(s.data(), tw.data(), p, 0, 1);
+    for (int i = 0; i < N; ++i) { data[2 * i] = s[i].x; data[2 * i + 1] = s[i].y; }
+  } else {
+    std::vector<float2> s(N), t(N);
+    for (int i = 0; i < N; ++i) {
+      s[i] = make_float2((float)data[2 * i], (float)data[2 * i + 1]);
+      t[i] = make_float2((float)tw[i].x, (float)tw[i].y);
+    }
+    if (inverse) bdda::warp_fft<true>(s.data(), t.data(), p, 0, 1);
+    else bdda::warp_fft<false>(s.data(), t.data(), p, 0, 1);
+    for (int i = 0; i < N; ++i) { data[2 * i] = s[i].x; data[2 * i + 1] = s[i].y; }
+  }
+  if (radix)
+    for (int i = 0; i < p.nst; ++i) radix[i] = p.radix[i];
+  return p.nst;
+}
+
+}  // extern "C"

@@ -1,0 +1,235 @@
+// Single-CTA complex-FP64 L x L algebra for the block Krylov solvers
+// (included by solver.cu only).  Matrices are column-major in shared memory,
+// M[i + j*L].  Every routine is called by all kSmallThreads threads of the CTA
+// and ends with a barrier.
+//
+// Replaces Eigen's partialPivLu / fullPivLu solves
+// (bl_krylov_mvp_fft/bl_cocg_rq_mvp_fft.cpp:56,66, bl_cocg_rq_jacobi_mvp_fft.cpp:63,73,
+// bl_bicgstab_mvp_fft.cpp:58-59,93, bl_bicggr_mvp_fft.cpp:51,110) and the L x L
+// part of qr_reduced (qr_reduced.cpp:9-31, here as the Cholesky factors of
+// CholQR2), so a whole Krylov iteration runs without a host round trip.
+#pragma once
+
+#include "common.cuh"
+#include "krylov_kernels.cuh"
+
+namespace bdda {
+
+constexpr int kSmallThreads = 256;
+
+__device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  // Smith-free plain division; operands are O(1) pivots.
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+
+// dst[e] = sum_p partials[p*LL + e] in order p = 0..nparts-1
+__device__ void sm_reduce(double2* dst, const double2* __restrict__ partials, int nparts, int LL) {
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int p = 0; p < nparts; ++p) {
+      const double2 v = partials[(size_t)p * LL + e];
+      s.x += v.x;
+      s.y += v.y;
+    }
+    dst[e] = s;
+  }
+  __syncthreads();
+}
+
+__device__ void sm_copy(double2* dst, const double2* src, int LL) {
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) dst[e] = src[e];
+  __syncthreads();
+}
+
+// C = op(A) * B with op = transpose (TA=1) or identity (TA=0); C must not alias.
+__device__ void sm_matmul(double2* Cm, const double2* A, const double2* B, int L, bool TA, double2 scale = make_double2(1.0, 0.0)) {
+  for (int e = threadIdx.x; e < L * L; e += blockDim.x) {
+    const int i = e % L, j = e / L;
+    double2 s = make_double2(0.0, 0.0);
+    for (int k = 0; k < L; ++k) {
+      const double2 a = TA ? A[k + i * L] : A[i + k * L];
+      s = cadd(s, cmul(a, B[k + j * L]));
+    }
+    Cm[e] = cmul(s, scale);
+  }
+  __syncthreads();
+}
+
+// Solve A X = B (L x L, nrhs columns) by LU; A and B are overwritten (B <- X).
+// full=false: partial (row) pivoting on the largest |a| in the column (first
+// max); full=true: complete pivoting on the largest |a| of the trailing block,
+// first max in column-major order.  Returns false on a zero / non-finite pivot.
+__device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, int* colperm /*smem[L]*/,
+                            int* piv /*smem[2]*/, double* red_v /*smem[kSmallThreads]*/, int* red_i /*smem[kSmallThreads]*/) {
+  const int tid = threadIdx.x;
+  for (int i = tid; i < L; i += blockDim.x) colperm[i] = i;
+  __shared__ int bad;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < L; ++k) {
+    // ---- pivot search
+    const int m = L - k;
+    const int cnt = full ? m * m : m;
+    double best = -1.0;
+    int bidx = 0x7fffffff;
+    for (int t = tid; t < cnt; t += blockDim.x) {
+      const int ii = k + (t % m);
+      const int jj = full ? k + t / m : k;
+      const double v = sqrt(cabs2(A[ii + jj * L]));
+      const int lin = ii + jj * L;  // column-major order
+      if (v > best || (v == best && lin < bidx)) { best = v; bidx = lin; }
+    }
+    red_v[tid] = best;
+    red_i[tid] = bidx;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (tid < s) {
+        const double v2 = red_v[tid + s];
+        const int i2 = red_i[tid + s];
+        if (v2 > red_v[tid] || (v2 == red_v[tid] && i2 < red_i[tid])) { red_v[tid] = v2; red_i[tid] = i2; }
+      }
+      __syncthreads();
+    }
+    if (tid == 0) {
+      piv[0] = red_i[0] % L;
+      piv[1] = red_i[0] / L;
+      if (!(red_v[0] > 0.0) || !isfinite(red_v[0])) bad = 1;
+    }
+    __syncthreads();
+    const int pr = piv[0], pc = piv[1];
+    // ---- row swap k <-> pr (A and B)
+    if (pr != k) {
+      for (int j = tid; j < L + nrhs; j += blockDim.x) {
+        double2* M = j < L ? A : B;
+        const int jc = j < L ? j : j - L;
+        const double2 t = M[k + jc * L];
+        M[k + jc * L] = M[pr + jc * L];
+        M[pr + jc * L] = t;
+      }
+    }
+    __syncthreads();
+    // ---- column swap k <-> pc (A only, record permutation)
+    if (full && pc != k) {
+      for (int i = tid; i < L; i += blockDim.x) {
+        const double2 t = A[i + k * L];
+        A[i + k * L] = A[i + pc * L];
+        A[i + pc * L] = t;
+      }
+      if (tid == 0) { const int t = colperm[k]; colperm[k] = colperm[pc]; colperm[pc] = t; }
+    }
+    __syncthreads();
+    if (bad) continue;
+    // ---- eliminate below the pivot
+    const double2 p = A[k + k * L];
+    const int rows = L - k - 1;
+    for (int t = tid; t < rows * (L - k - 1 + nrhs); t += blockDim.x) {
+      const int i = k + 1 + t % rows;
+      const int jj = t / rows;  // 0..(L-k-2) -> A columns k+1.., then B columns
+      const double2 f = cdiv(A[i + k * L], p);
+      if (jj < L - k - 1) {
+        const int j = k + 1 + jj;
+        A[i + j * L] = csub(A[i + j * L], cmul(f, A[k + j * L]));
+      } else {
+        const int j = jj - (L - k - 1);
+        B[i + j * L] = csub(B[i + j * L], cmul(f, B[k + j * L]));
+      }
+    }
+    __syncthreads();
+    for (int i = k + 1 + tid; i < L; i += blockDim.x) A[i + k * L] = cdiv(A[i + k * L], p);  // store multipliers
+    __syncthreads();
+  }
+  // ---- back substitution, one thread per right-hand side
+  for (int j = tid; j < nrhs; j += blockDim.x) {
+    for (int k = L - 1; k >= 0; --k) {
+      double2 s = B[k + j * L];
+      for (int c = k + 1; c < L; ++c) s = csub(s, cmul(A[k + c * L], B[c + j * L]));
+      B[k + j * L] = cdiv(s, A[k + k * L]);
+    }
+  }
+  __syncthreads();
+  if (full) {
+    // x[colperm[k]] = y[k]; use A's first column block as scratch (A no longer needed)
+    for (int e = tid; e < L * nrhs; e += blockDim.x) A[e] = B[e];
+    __syncthreads();
+    for (int e = tid; e < L * nrhs; e += blockDim.x) {
+      const int k = e % L, j = e / L;
+      B[colperm[k] + j * L] = A[e];
+    }
+    __syncthreads();
+  }
+  bool ok = !bad;
+  for (int e = tid; e < L * nrhs; e += blockDim.x)
+    if (!cfinite(B[e])) bad = 1;
+  __syncthreads();
+  ok = !bad;
+  __syncthreads();
+  return ok;
+}
+
+// H = R^H R with R upper triangular, real positive diagonal.  R may alias H.
+__device__ bool sm_cholesky(double2* R, const double2* H, int L) {
+  __shared__ int bad;
+  const int tid = threadIdx.x;
+  if (tid == 0) bad = 0;
+  if (R != H) for (int e = tid; e < L * L; e += blockDim.x) R[e] = H[e];
+  __syncthreads();
+  for (int k = 0; k < L; ++k) {
+    // diagonal
+    if (tid == 0) {
+      double d = R[k + k * L].x;
+      for (int i = 0; i < k; ++i) d -= cabs2(R[i + k * L]);
+      if (!(d > 0.0) || !isfinite(d)) { bad = 1; d = 1.0; }
+      R[k + k * L] = make_double2(sqrt(d), 0.0);
+    }
+    __syncthreads();
+    const double rkk = R[k + k * L].x;
+    for (int j = k + 1 + tid; j < L; j += blockDim.x) {
+      double2 s = R[k + j * L];
+      for (int i = 0; i < k; ++i) s = csub(s, cconjmul(R[i + k * L], R[i + j * L]));
+      R[k + j * L] = make_double2(s.x / rkk, s.y / rkk);
+    }
+    __syncthreads();
+  }
+  // zero the strictly lower part
+  for (int e = tid; e < L * L; e += blockDim.x) {
+    const int i = e % L, j = e / L;
+    if (i > j) R[e] = make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  const bool ok = !bad;
+  __syncthreads();
+  return ok;
+}
+
+// Inverse of an upper triangular matrix (one thread per column).
+__device__ void sm_tri_inv(double2* Ri, const double2* R, int L) {
+  for (int j = threadIdx.x; j < L; j += blockDim.x) {
+    for (int i = L - 1; i >= 0; --i) {
+      if (i > j) { Ri[i + j * L] = make_double2(0.0, 0.0); continue; }
+      double2 s = make_double2(i == j ? 1.0 : 0.0, 0.0);
+      for (int k = i + 1; k <= j; ++k) s = csub(s, cmul(R[i + k * L], Ri[k + j * L]));
+      Ri[i + j * L] = cdiv(s, R[i + i * L]);
+    }
+  }
+  __syncthreads();
+}
+
+// Frobenius norm (thread 0 result broadcast through smem)
+__device__ double sm_fro(const double2* M, int LL) {
+  __shared__ double r;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int e = 0; e < LL; ++e) s += cabs2(M[e]);
+    r = sqrt(s);
+  }
+  __syncthreads();
+  const double v = r;
+  __syncthreads();
+  return v;
+}
+
+}  // namespace bdda

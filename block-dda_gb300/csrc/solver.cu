@@ -1,0 +1,798 @@
+// Block Krylov solvers on the device, FP64 refinement loop and qr_reduced.
+//
+// Every Krylov iteration is a fixed sequence of kernel launches with no host
+// round trip: block MVP passes, tall-skinny Gram reductions, one-CTA FP64
+// L x L steps (LU solves, Cholesky factors of CholQR2, stopping test) and row
+// transforms.  The stopping test runs on the device and raises
+// SolverCtl::done; every later kernel of the solve returns at entry, so the
+// host only polls the control block every few iterations.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/bdda.h"
+#include "krylov_kernels.cuh"
+#include "op.hpp"
+#include "small.cuh"
+
+namespace bdda {
+
+// ---------------------------------------------------------------------------
+// small-state slots (each L x L complex FP64, column-major)
+// ---------------------------------------------------------------------------
+enum Slot {
+  kXi = 0, kAlpha, kNAlpha, kAXi, kR1, kR1Inv, kR2Inv, kTau, kQtQ, kBeta, kM, kM2, kZetaI, kNZetaI, kIdent, kNIdent,
+  kNumSlots
+};
+
+struct SolverWork {
+  int n = 0, L = 0;
+  DevBuf blk64[10], blk32[10];   // 0-7 Krylov blocks, 8 right-hand side, 9 solution
+  DevBuf X64, R64, Y64;
+  DevBuf jpre64, diag32, jpre32;
+  DevBuf partials, partials2;   // Gram partials (c128) [G][L*L]
+  DevBuf vpart;                 // dot / norm partials
+  DevBuf small;                 // c128 [kNumSlots][L*L] + scalars
+  DevBuf ctl;                   // SolverCtl
+  DevBuf hist;                  // double[itermax]
+  SolverCtl* ctl_host = nullptr;
+  ~SolverWork() { if (ctl_host) cudaFreeHost(ctl_host); }
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* where) {
+  set_error(std::string(where) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? BDDA_ERR_NOMEM : BDDA_ERR_CUDA;
+}
+#define BDDA_CUDA(call)                                   \
+  do {                                                    \
+    cudaError_t _e = (call);                              \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call);   \
+  } while (0)
+#define BDDA_TRY(call)           \
+  do {                           \
+    int _rc = (call);            \
+    if (_rc != BDDA_OK) return _rc; \
+  } while (0)
+
+inline int gram_grid(int n) { return std::max(1, std::min(296, (n + 127) / 128)); }
+inline int vec_grid(size_t total) { return (int)std::max<size_t>(1, std::min<size_t>(608, (total + 255) / 256)); }
+
+__device__ __forceinline__ double2* slot(double2* st, int s, int L) { return st + (size_t)s * L * L; }
+
+// ---------------------------------------------------------------------------
+// one-CTA steps
+// ---------------------------------------------------------------------------
+struct SmallSmem {
+  // dynamic smem carve-up: 6 matrices + reduction scratch
+  static size_t bytes(int L) { return 6 * (size_t)L * L * sizeof(double2) + kSmallThreads * (sizeof(double) + sizeof(int)) + (2 + kMaxL) * sizeof(int); }
+};
+
+#define SMALL_PROLOGUE                                                               \
+  extern __shared__ __align__(16) unsigned char smem_raw[];                          \
+  double2* m0 = reinterpret_cast<double2*>(smem_raw);                                \
+  double2* m1 = m0 + L * L;                                                          \
+  double2* m2 = m1 + L * L;                                                          \
+  double2* m3 = m2 + L * L;                                                          \
+  double2* m4 = m3 + L * L;                                                          \
+  double2* m5 = m4 + L * L;                                                          \
+  double* red_v = reinterpret_cast<double*>(m5 + L * L);                             \
+  int* red_i = reinterpret_cast<int*>(red_v + kSmallThreads);                        \
+  int* piv = red_i + kSmallThreads;                                                  \
+  int* colperm = piv + 2;                                                            \
+  const int LL = L * L;
+
+__device__ void fail(SolverCtl* ctl) {
+  if (threadIdx.x == 0) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; }
+}
+
+// Identity helpers and ||B|| from column-norm partials.
+__global__ void k_small_init(const double* __restrict__ vpart, int nparts, int L, double2* st, SolverCtl* ctl) {
+  const int LL = L * L;
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) {
+    const int i = e % L, j = e / L;
+    slot(st, kIdent, L)[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    slot(st, kNIdent, L)[e] = make_double2(i == j ? -1.0 : 0.0, 0.0);
+  }
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int p = 0; p < nparts; ++p)
+      for (int l = 0; l < L; ++l) s += vpart[(size_t)p * L + l];
+    ctl->bnorm = sqrt(s);
+    ctl->done = 0;
+    ctl->status = 0;
+    ctl->iter = 0;
+    ctl->err = 1.0;
+    if (!(s > 0.0) || !isfinite(s)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; }
+  }
+}
+
+// QR step 1: H = W^H W ; R1 = chol(H) ; R1inv
+__global__ void __launch_bounds__(kSmallThreads)
+k_small_chol1(const double2* __restrict__ part, int nparts, int L, double2* st, SolverCtl* ctl) {
+  if (ctl_skip(ctl)) return;
+  SMALL_PROLOGUE
+  sm_reduce(m0, part, nparts, LL);
+  if (!sm_cholesky(m1, m0, L)) { fail(ctl); return; }
+  sm_tri_inv(m2, m1, L);
+  sm_copy(slot(st, kR1, L), m1, LL);
+  sm_copy(slot(st, kR1Inv, L), m2, LL);
+}
+
+// QR step 2: H2 = W1^H W1 ; R2 = chol ; R2inv ; tau = R2 R1.
+// mode 0: xi = tau (initial QR of the right-hand side)
+// mode 1: xi = tau xi ; err = ||xi|| / bnorm ; stopping test
+// mode 2: like mode 0 but R = tau returned in kXi only (qr_reduced)
+__global__ void __launch_bounds__(kSmallThreads)
+k_small_chol2(const double2* __restrict__ part, int nparts, int L, double2* st, SolverCtl* ctl, double tol,
+              double* hist, int k, int mode) {
+  if (ctl_skip(ctl)) return;
+  SMALL_PROLOGUE
+  sm_reduce(m0, part, nparts, LL);
+  if (!sm_cholesky(m1, m0, L)) { fail(ctl); return; }
+  sm_tri_inv(m2, m1, L);
+  sm_copy(slot(st, kR2Inv, L), m2, LL);
+  sm_copy(m3, slot(st, kR1, L), LL);
+  sm_matmul(m4, m1, m3, L, false);  // tau = R2 R1
+  sm_copy(slot(st, kTau, L), m4, LL);
+  if (mode != 1) {
+    sm_copy(slot(st, kXi, L), m4, LL);
+    return;
+  }
+  sm_copy(m5, slot(st, kXi, L), LL);
+  sm_matmul(m0, m4, m5, L, false);  // xi = tau xi
+  sm_copy(slot(st, kXi, L), m0, LL);
+  const double nrm = sm_fro(m0, LL);
+  if (threadIdx.x == 0) {
+    const double err = nrm / ctl->bnorm;
+    ctl->err = err;
+    if (hist) hist[k] = err;
+    ctl->iter = k + 1;
+    if (!isfinite(err)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; }
+    else if (err < tol) ctl->done = 1;
+  }
+}
+
+// COCG-RQ alpha: alpha = (S^T AS)^-1 (Q^T Q) ; A_xi = alpha xi ; -alpha
+__global__ void __launch_bounds__(kSmallThreads)
+k_small_cocg_alpha(const double2* __restrict__ pSAS, const double2* __restrict__ pQQ, int nparts, int L, double2* st,
+                   SolverCtl* ctl, int full) {
+  if (ctl_skip(ctl)) return;
+  SMALL_PROLOGUE
+  sm_reduce(m0, pSAS, nparts, LL);
+  if (pQQ) {
+    sm_reduce(m1, pQQ, nparts, LL);
+    sm_copy(slot(st, kQtQ, L), m1, LL);
+  } else {
+    sm_copy(m1, slot(st, kQtQ, L), LL);
+  }
+  if (!sm_lu_solve(m0, m1, L, L, full != 0, colperm, piv, red_v, red_i)) { fail(ctl); return; }
+  sm_copy(slot(st, kAlpha, L), m1, LL);
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) slot(st, kNAlpha, L)[e] = make_double2(-m1[e].x, -m1[e].y);
+  sm_copy(m2, slot(st, kXi, L), LL);
+  sm_matmul(m3, m1, m2, L, false);
+  sm_copy(slot(st, kAXi, L), m3, LL);
+}
+
+// COCG-RQ beta: beta = (Q^T Q)^-1 (tau^T Q'^T Q') ; Q^T Q <- Q'^T Q'
+__global__ void __launch_bounds__(kSmallThreads)
+k_small_cocg_beta(const double2* __restrict__ pQQn, int nparts, int L, double2* st, SolverCtl* ctl, int full) {
+  if (ctl_skip(ctl)) return;
+  SMALL_PROLOGUE
+  sm_reduce(m0, pQQn, nparts, LL);           // Q'^T Q'
+  sm_copy(m1, slot(st, kTau, L), LL);
+  sm_matmul(m2, m1, m0, L, true);            // tau^T Q'^T Q'
+  sm_copy(m3, slot(st, kQtQ, L), LL);
+  if (!sm_lu_solve(m3, m2, L, L, full != 0, colperm, piv, red_v, red_i)) { fail(ctl); return; }
+  sm_copy(slot(st, kBeta, L), m2, LL);
+  sm_copy(slot(st, kQtQ, L), m0, LL);
+}
+
+// BiCG*: X = M^-1 RHS with M = reduce(pM) (stored in kM), RHS = scale * reduce(pR).
+// out slots: x -> so, -x -> sno (optional)
+__global__ void __launch_bounds__(kSmallThreads)
+k_small_solve(const double2* __restrict__ pM, const double2* __restrict__ pR, int nparts, int L, double2* st,
+              SolverCtl* ctl, int mslot_in, int mslot_store, double rhs_scale, const double2* scal_div, int so, int sno) {
+  if (ctl_skip(ctl)) return;
+  SMALL_PROLOGUE
+  if (pM) sm_reduce(m0, pM, nparts, LL);
+  else sm_copy(m0, slot(st, mslot_in, L), LL);
+  if (mslot_store >= 0) sm_copy(slot(st, mslot_store, L), m0, LL);
+  sm_reduce(m1, pR, nparts, LL);
+  double2 sc = make_double2(rhs_scale, 0.0);
+  if (scal_div) sc = cdiv(sc, *scal_div);
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) m1[e] = cmul(m1[e], sc);
+  __syncthreads();
+  if (!sm_lu_solve(m0, m1, L, L, false, colperm, piv, red_v, red_i)) { fail(ctl); return; }
+  sm_copy(slot(st, so, L), m1, LL);
+  if (sno >= 0)
+    for (int e = threadIdx.x; e < LL; e += blockDim.x) slot(st, sno, L)[e] = make_double2(-m1[e].x, -m1[e].y);
+}
+
+// zeta = sum(p1) / sum(p2) ; kZetaI = zeta I ; kNZetaI = -zeta I ; scal[0] = zeta, scal[1] = -zeta
+__global__ void k_small_zeta(const double2* __restrict__ p1, const double2* __restrict__ p2, int nparts, int L, double2* st,
+                             double2* scal, SolverCtl* ctl) {
+  if (ctl_skip(ctl)) return;
+  __shared__ double2 z;
+  if (threadIdx.x == 0) {
+    double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
+    for (int p = 0; p < nparts; ++p) {
+      a.x += p1[p].x; a.y += p1[p].y;
+      b.x += p2[p].x; b.y += p2[p].y;
+    }
+    z = cdiv(a, b);
+    if (!cfinite(z)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; }
+    scal[0] = z;
+    scal[1] = make_double2(-z.x, -z.y);
+  }
+  __syncthreads();
+  const int LL = L * L;
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) {
+    const int i = e % L, j = e / L;
+    slot(st, kZetaI, L)[e] = i == j ? z : make_double2(0.0, 0.0);
+    slot(st, kNZetaI, L)[e] = i == j ? make_double2(-z.x, -z.y) : make_double2(0.0, 0.0);
+  }
+}
+
+// err = sqrt(sum of column-norm partials) / bnorm ; stopping test
+__global__ void k_small_err(const double* __restrict__ vpart, int nparts, int L, SolverCtl* ctl, double tol, double* hist, int k) {
+  if (ctl_skip(ctl)) return;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int p = 0; p < nparts; ++p)
+      for (int l = 0; l < L; ++l) s += vpart[(size_t)p * L + l];
+    const double err = sqrt(s) / ctl->bnorm;
+    ctl->err = err;
+    if (hist) hist[k] = err;
+    ctl->iter = k + 1;
+    if (!isfinite(err)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; }
+    else if (err < tol) ctl->done = 1;
+  }
+}
+
+// st[s] = reduce(partials)
+__global__ void __launch_bounds__(kSmallThreads)
+k_small_store_reduce(const double2* __restrict__ part, int nparts, int L, double2* st, SolverCtl* ctl, int s) {
+  if (ctl_skip(ctl)) return;
+  sm_reduce(slot(st, s, L), part, nparts, L * L);
+}
+
+// ---------------------------------------------------------------------------
+// host-side runner for one precision
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Krylov {
+  using C = typename cplx<T>::type;
+  Op* op;
+  SolverWork* w;
+  cudaStream_t st;
+  int n, L;
+  const C* diag;
+  const C* jpre;
+  int check_every;
+  int mvps = 0;
+
+  SolverCtl* ctl() const { return w->ctl.as<SolverCtl>(); }
+  double2* small() const { return w->small.as<double2>(); }
+  double2* sl(int s) const { return small() + (size_t)s * L * L; }
+  C* blk(int i) const { return (std::is_same<T, double>::value ? w->blk64[i] : w->blk32[i]).template as<C>(); }
+  int G() const { return gram_grid(n); }
+
+  int mvp(const C* x, C* y) {
+    ++mvps;
+    return op_block_mvp<T>(op, op->dip, x, n, y, n, L, diag, jpre, st, &ctl()->done);
+  }
+  template <bool CONJ> void gram(const C* A, const C* B, double2* part) {
+    op->timer.begin(kGram, st);
+    k_gram<T, CONJ><<<G(), kGramThreads, 0, st>>>(A, n, B, n, n, L, part, ctl());
+    op->timer.end(kGram, st);
+    ++op->kernel_launches;
+  }
+  void rowmm(const C* A, const double2* Ma, const C* B, const double2* Mb, const C* Cadd, C* Out) {
+    op->timer.begin(kUpdate, st);
+    k_rowmm<T><<<(n + kRowThreads - 1) / kRowThreads, kRowThreads, rowmm_smem<T>(L, B != nullptr), st>>>(
+        n, L, A, n, Ma, B, n, Mb, Cadd, n, Out, n, ctl());
+    op->timer.end(kUpdate, st);
+    ++op->kernel_launches;
+  }
+  void axpby(const double2* a, const C* A, const double2* b, const C* B, C* Out) {
+    op->timer.begin(kUpdate, st);
+    k_axpby<T><<<vec_grid((size_t)n * L), 256, 0, st>>>(n, L, a, A, n, b, B, n, Out, n, ctl());
+    op->timer.end(kUpdate, st);
+    ++op->kernel_launches;
+  }
+  void dotc(const C* A, const C* B, double2* part) {
+    op->timer.begin(kGram, st);
+    k_dotc<T><<<vec_grid((size_t)n * L), 256, 0, st>>>(n, L, A, n, B, n, part, ctl());
+    op->timer.end(kGram, st);
+    ++op->kernel_launches;
+  }
+  void colnorm(const C* A, double* part) {
+    op->timer.begin(kGram, st);
+    k_colnorm2<T><<<vec_grid((size_t)n * L), 256, 0, st>>>(A, n, n, L, part);
+    op->timer.end(kGram, st);
+    ++op->kernel_launches;
+  }
+  template <typename K, typename... Args> void small_launch(K kern, Args... args) {
+    op->timer.begin(kSmall, st);
+    kern<<<1, kSmallThreads, SmallSmem::bytes(L), st>>>(args...);
+    op->timer.end(kSmall, st);
+    ++op->kernel_launches;
+  }
+
+  // poll the control block; returns 1 when the device signalled done
+  int poll(bool* done, bool wait = true) {
+    BDDA_CUDA(cudaMemcpyAsync(w->ctl_host, ctl(), sizeof(SolverCtl), cudaMemcpyDeviceToHost, st));
+    if (wait) BDDA_CUDA(cudaStreamSynchronize(st));
+    *done = w->ctl_host->done != 0;
+    return BDDA_OK;
+  }
+
+  // ||Bp||_F -> ctl->bnorm, identity slots, control reset
+  int init(const C* Bp) {
+    double* vp = w->vpart.as<double>();
+    const int g = vec_grid((size_t)n * L);
+    k_colnorm2<T><<<g, 256, 0, st>>>(Bp, n, n, L, vp);
+    k_small_init<<<1, 256, 0, st>>>(vp, g, L, small(), ctl());
+    op->kernel_launches += 2;
+    return cudaGetLastError() == cudaSuccess ? BDDA_OK : cuda_fail(cudaGetLastError(), "init");
+  }
+
+  // [Q, R] = qr(A) by CholQR2 ; R -> kXi (mode 0/2).  W is scratch (may equal Q).
+  void cholqr2(const C* A, C* W, C* Q, int mode) {
+    double2* p = w->partials.template as<double2>();
+    gram<true>(A, A, p);
+    small_launch(k_small_chol1, (const double2*)p, G(), L, small(), ctl());
+    rowmm(A, sl(kR1Inv), nullptr, nullptr, nullptr, W);
+    gram<true>(W, W, p);
+    small_launch(k_small_chol2, (const double2*)p, G(), L, small(), ctl(), 0.0, (double*)nullptr, 0, mode);
+    rowmm(W, sl(kR2Inv), nullptr, nullptr, nullptr, Q);
+  }
+
+  // Block COCG-RQ (bl_cocg_rq_mvp_fft.cpp:22-71 / bl_cocg_rq_jacobi_mvp_fft.cpp:22-78)
+  int cocg_rq(const C* Bp, C* X, bool full, double tol, int itermax, int* iters, double* err, int* status) {
+    C* Q = blk(0); C* Qn = blk(1); C* S = blk(2); C* AS = blk(3); C* W = blk(4);
+    double2* p = w->partials.template as<double2>();
+    double2* p2 = w->partials2.template as<double2>();
+    BDDA_CUDA(cudaMemsetAsync(X, 0, sizeof(C) * (size_t)n * L, st));
+    BDDA_TRY(init(Bp));
+    cholqr2(Bp, W, Q, 0);
+    BDDA_CUDA(cudaMemcpyAsync(S, Q, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+    bool done = false;
+    int k = 0;
+    for (; k < itermax; ++k) {
+      BDDA_TRY(mvp(S, AS));
+      gram<false>(S, AS, p);
+      if (k == 0) gram<false>(Q, Q, p2);
+      small_launch(k_small_cocg_alpha, (const double2*)p, (const double2*)(k == 0 ? p2 : nullptr), G(), L, small(), ctl(),
+                   (int)full);
+      rowmm(S, sl(kAXi), nullptr, nullptr, X, X);           // X += S alpha xi
+      rowmm(AS, sl(kNAlpha), nullptr, nullptr, Q, W);       // W = Q - AS alpha
+      gram<true>(W, W, p);
+      small_launch(k_small_chol1, (const double2*)p, G(), L, small(), ctl());
+      rowmm(W, sl(kR1Inv), nullptr, nullptr, nullptr, W);
+      gram<true>(W, W, p);
+      small_launch(k_small_chol2, (const double2*)p, G(), L, small(), ctl(), tol, w->hist.as<double>(), k, 1);
+      rowmm(W, sl(kR2Inv), nullptr, nullptr, nullptr, Qn);  // Q'
+      gram<false>(Qn, Qn, p);
+      small_launch(k_small_cocg_beta, (const double2*)p, G(), L, small(), ctl(), (int)full);
+      rowmm(S, sl(kBeta), nullptr, nullptr, Qn, S);         // S = Q' + S beta
+      std::swap(Q, Qn);
+      if ((k + 1) % check_every == 0 || k + 1 == itermax) {
+        BDDA_TRY(poll(&done));
+        if (done) break;
+      }
+    }
+    if (!done) BDDA_TRY(poll(&done));
+    *iters = w->ctl_host->iter;
+    *err = w->ctl_host->err;
+    *status = w->ctl_host->status;
+    return cudaGetLastError() == cudaSuccess ? BDDA_OK : cuda_fail(cudaGetLastError(), "cocg_rq");
+  }
+
+  // Block BiCGSTAB (bl_bicgstab_mvp_fft.cpp:21-98 / bl_bicgstab_jacobi_mvp_fft.cpp:21-96)
+  int bicgstab(const C* Bp, C* X, double tol, int itermax, int* iters, double* err, int* status) {
+    C* R = blk(0); C* P = blk(1); C* R0 = blk(2); C* V = blk(3); C* Tm = blk(4); C* Z = blk(5); C* Pt = blk(6);
+    double2* p = w->partials.template as<double2>();
+    double2* p2 = w->partials2.template as<double2>();
+    double2* vp = w->vpart.as<double2>();
+    double2* scal = sl(kNumSlots);  // 2 scalars after the matrix slots
+    BDDA_CUDA(cudaMemsetAsync(X, 0, sizeof(C) * (size_t)n * L, st));
+    BDDA_TRY(init(Bp));
+    BDDA_CUDA(cudaMemcpyAsync(R, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+    BDDA_CUDA(cudaMemcpyAsync(P, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+    BDDA_CUDA(cudaMemcpyAsync(R0, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+    const int gv = vec_grid((size_t)n * L);
+    bool done = false;
+    int k = 0;
+    for (; k < itermax; ++k) {
+      BDDA_TRY(mvp(P, V));                                   // V = A P
+      gram<true>(R0, V, p);
+      gram<true>(R0, R, p2);
+      small_launch(k_small_solve, (const double2*)p, (const double2*)p2, G(), L, small(), ctl(), 0, (int)kM, 1.0,
+                   (const double2*)nullptr, (int)kAlpha, (int)kNAlpha);
+      rowmm(V, sl(kNAlpha), nullptr, nullptr, R, Tm);        // T = R - V alpha
+      BDDA_TRY(mvp(Tm, Z));                                  // Z = A T
+      dotc(Z, Tm, vp);
+      dotc(Z, Z, vp + gv);
+      op->timer.begin(kSmall, st);
+      k_small_zeta<<<1, 256, 0, st>>>(vp, vp + gv, gv, L, small(), scal, ctl());
+      op->timer.end(kSmall, st);
+      ++op->kernel_launches;
+      rowmm(P, sl(kAlpha), Tm, sl(kZetaI), X, X);            // X = X + P alpha + zeta T
+      axpby(nullptr, Tm, scal + 1, Z, R);                    // R = T - zeta Z
+      colnorm(R, w->vpart.as<double>());
+      op->timer.begin(kSmall, st);
+      k_small_err<<<1, 32, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
+      op->timer.end(kSmall, st);
+      ++op->kernel_launches;
+      gram<true>(R0, Z, p);
+      small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, G(), L, small(), ctl(), (int)kM, -1, -1.0,
+                   (const double2*)nullptr, (int)kBeta, -1);  // beta = M^-1 (-R0^H Z)
+      axpby(nullptr, P, scal + 1, V, Pt);                    // Pt = P - zeta V
+      rowmm(Pt, sl(kBeta), nullptr, nullptr, R, P);          // P = R + Pt beta
+      if ((k + 1) % check_every == 0 || k + 1 == itermax) {
+        BDDA_TRY(poll(&done));
+        if (done) break;
+      }
+    }
+    if (!done) BDDA_TRY(poll(&done));
+    *iters = w->ctl_host->iter;
+    *err = w->ctl_host->err;
+    *status = w->ctl_host->status;
+    return cudaGetLastError() == cudaSuccess ? BDDA_OK : cuda_fail(cudaGetLastError(), "bicgstab");
+  }
+
+  // Block BiCGGR (bl_bicggr_mvp_fft.cpp:18-116 / bl_bicggr_jacobi_mvp_fft.cpp:18-117)
+  int bicggr(const C* Bp, C* X, double tol, int itermax, int* iters, double* err, int* status) {
+    C* R = blk(0); C* P = blk(1); C* R0 = blk(2); C* V = blk(3); C* Wm = blk(4); C* U = blk(5); C* Y = blk(6); C* Rn = blk(7);
+    double2* p = w->partials.template as<double2>();
+    double2* p2 = w->partials2.template as<double2>();
+    double2* vp = w->vpart.as<double2>();
+    double2* scal = sl(kNumSlots);
+    BDDA_CUDA(cudaMemsetAsync(X, 0, sizeof(C) * (size_t)n * L, st));
+    BDDA_TRY(init(Bp));
+    BDDA_CUDA(cudaMemcpyAsync(R, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+    BDDA_CUDA(cudaMemcpyAsync(P, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+    BDDA_CUDA(cudaMemcpyAsync(R0, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+    BDDA_TRY(mvp(R, V));                                     // V = A R
+    BDDA_CUDA(cudaMemcpyAsync(Wm, V, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+    const int gv = vec_grid((size_t)n * L);
+    bool done = false;
+    int k = 0;
+    for (; k < itermax; ++k) {
+      gram<true>(R0, V, p);
+      gram<true>(R0, R, p2);
+      small_launch(k_small_solve, (const double2*)p, (const double2*)p2, G(), L, small(), ctl(), 0, -1, 1.0,
+                   (const double2*)nullptr, (int)kAlpha, -1);
+      // keep R0^H R (old R) for gamma
+      small_launch(k_small_store_reduce, (const double2*)p2, G(), L, small(), ctl(), (int)kM2);
+      dotc(Wm, R, vp);
+      dotc(Wm, Wm, vp + gv);
+      op->timer.begin(kSmall, st);
+      k_small_zeta<<<1, 256, 0, st>>>(vp, vp + gv, gv, L, small(), scal, ctl());
+      op->timer.end(kSmall, st);
+      ++op->kernel_launches;
+      axpby(nullptr, P, scal + 1, V, Rn);                    // S = P - zeta V   (Rn as scratch)
+      rowmm(Rn, sl(kAlpha), nullptr, nullptr, nullptr, U);   // U = S alpha
+      BDDA_TRY(mvp(U, Y));                                   // Y = A U
+      rowmm(R, sl(kZetaI), U, sl(kIdent), X, X);             // X = X + zeta R + U
+      rowmm(Wm, sl(kNZetaI), Y, sl(kNIdent), R, Rn);         // Rn = R - zeta W - Y
+      colnorm(Rn, w->vpart.as<double>());
+      op->timer.begin(kSmall, st);
+      k_small_err<<<1, 32, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
+      op->timer.end(kSmall, st);
+      ++op->kernel_launches;
+      BDDA_TRY(mvp(Rn, Wm));                                 // W = A Rnew
+      gram<true>(R0, Rn, p);
+      small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, G(), L, small(), ctl(), (int)kM2, -1, 1.0,
+                   (const double2*)scal, (int)kBeta, -1);    // gamma = (R0^H R)^-1 (R0^H Rnew / zeta)
+      std::swap(R, Rn);
+      rowmm(U, sl(kBeta), nullptr, nullptr, R, P);           // P = R + U gamma
+      rowmm(Y, sl(kBeta), nullptr, nullptr, Wm, V);          // V = W + Y gamma
+      if ((k + 1) % check_every == 0 || k + 1 == itermax) {
+        BDDA_TRY(poll(&done));
+        if (done) break;
+      }
+    }
+    if (!done) BDDA_TRY(poll(&done));
+    // R/Rn swapping above only changes which buffer holds the residual; X is final.
+    *iters = w->ctl_host->iter;
+    *err = w->ctl_host->err;
+    *status = w->ctl_host->status;
+    return cudaGetLastError() == cudaSuccess ? BDDA_OK : cuda_fail(cudaGetLastError(), "bicggr");
+  }
+
+  int run(int solver, const C* Bp, C* X, bool full, double tol, int itermax, int* iters, double* err, int* status) {
+    switch (solver) {
+      case BDDA_SOLVER_COCG_RQ: return cocg_rq(Bp, X, full, tol, itermax, iters, err, status);
+      case BDDA_SOLVER_BICGSTAB: return bicgstab(Bp, X, tol, itermax, iters, err, status);
+      case BDDA_SOLVER_BICGGR: return bicggr(Bp, X, tol, itermax, iters, err, status);
+      default: set_error("unknown solver id"); return BDDA_ERR_INVALID;
+    }
+  }
+
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// workspace
+// ---------------------------------------------------------------------------
+static int ensure_work(Op* op, int n, int L, int itermax, bool need64, bool need32) {
+  if (!op->solver) op->solver = std::make_shared<SolverWork>();
+  SolverWork* w = op->solver.get();
+  const size_t b64 = sizeof(double2) * (size_t)n * L, b32 = sizeof(float2) * (size_t)n * L;
+  for (int i = 0; i < 10; ++i) {
+    if (need64) BDDA_CUDA(w->blk64[i].ensure(b64));
+    if (need32) BDDA_CUDA(w->blk32[i].ensure(b32));
+  }
+  BDDA_CUDA(w->X64.ensure(b64));
+  BDDA_CUDA(w->R64.ensure(b64));
+  BDDA_CUDA(w->Y64.ensure(b64));
+  BDDA_CUDA(w->jpre64.ensure(sizeof(double2) * (size_t)n));
+  BDDA_CUDA(w->diag32.ensure(sizeof(float2) * (size_t)n));
+  BDDA_CUDA(w->jpre32.ensure(sizeof(float2) * (size_t)n));
+  const size_t LL = (size_t)L * L;
+  BDDA_CUDA(w->partials.ensure(sizeof(double2) * LL * gram_grid(n)));
+  BDDA_CUDA(w->partials2.ensure(sizeof(double2) * LL * gram_grid(n)));
+  BDDA_CUDA(w->vpart.ensure(sizeof(double2) * 2 * (size_t)std::max(vec_grid((size_t)n * L) * L, 2 * 608)));
+  BDDA_CUDA(w->small.ensure(sizeof(double2) * (LL * kNumSlots + 8)));
+  BDDA_CUDA(w->ctl.ensure(sizeof(SolverCtl)));
+  BDDA_CUDA(w->hist.ensure(sizeof(double) * (size_t)std::max(1, itermax)));
+  if (!w->ctl_host) BDDA_CUDA(cudaMallocHost(&w->ctl_host, sizeof(SolverCtl)));
+  w->n = n;
+  w->L = L;
+  static bool attr_done = false;
+  if (!attr_done) {
+    const int mx = (int)SmallSmem::bytes(kMaxL);
+    BDDA_CUDA(cudaFuncSetAttribute(k_small_chol1, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    BDDA_CUDA(cudaFuncSetAttribute(k_small_chol2, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    BDDA_CUDA(cudaFuncSetAttribute(k_small_cocg_alpha, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    BDDA_CUDA(cudaFuncSetAttribute(k_small_cocg_beta, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    BDDA_CUDA(cudaFuncSetAttribute(k_small_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    BDDA_CUDA(cudaFuncSetAttribute(k_small_store_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    const int r64 = rowmm_smem<double>(kMaxL, true), r32 = rowmm_smem<float>(kMaxL, true);
+    BDDA_CUDA(cudaFuncSetAttribute(k_rowmm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, r64));
+    BDDA_CUDA(cudaFuncSetAttribute(k_rowmm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, r32));
+    attr_done = true;
+  }
+  return BDDA_OK;
+}
+
+// column norms of an FP64 block -> host (squared)
+static int host_colnorm2(Op* op, cudaStream_t st, const double2* A, int n, int L, std::vector<double>* out) {
+  SolverWork* w = op->solver.get();
+  const int g = vec_grid((size_t)n * L);
+  double* vp = w->vpart.as<double>();
+  k_colnorm2<double><<<g, 256, 0, st>>>(A, n, n, L, vp);
+  ++op->kernel_launches;
+  std::vector<double> h((size_t)g * L);
+  BDDA_CUDA(cudaMemcpyAsync(h.data(), vp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+  BDDA_CUDA(cudaStreamSynchronize(st));
+  out->assign(L, 0.0);
+  for (int p = 0; p < g; ++p)
+    for (int l = 0; l < L; ++l) (*out)[l] += h[(size_t)p * L + l];
+  return BDDA_OK;
+}
+
+// R = B - (diag o X + A_off X) in FP64; returns max_l ||r_l|| / ||b_l||
+static int true_residual(Op* op, cudaStream_t st, const double2* diag, const double2* B, int ldb, const double2* X, int n,
+                         int L, const std::vector<double>& bn2, double* resmax, int* mvps) {
+  SolverWork* w = op->solver.get();
+  BDDA_TRY(op_block_mvp<double>(op, op->dip, X, n, w->Y64.as<double2>(), n, L, diag, nullptr, st));
+  ++*mvps;
+  k_residual<<<vec_grid((size_t)n * L), 256, 0, st>>>(n, L, B, ldb, w->Y64.as<double2>(), n, w->R64.as<double2>(), n);
+  ++op->kernel_launches;
+  std::vector<double> rn2;
+  BDDA_TRY(host_colnorm2(op, st, w->R64.as<double2>(), n, L, &rn2));
+  double mx = 0.0;
+  for (int l = 0; l < L; ++l) {
+    const double r = std::sqrt(rn2[l] / bn2[l]);
+    if (!(r <= mx)) mx = r;  // NaN propagates as the maximum
+  }
+  *resmax = mx;
+  return BDDA_OK;
+}
+
+static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, const double2* B, int ldb, double2* X,
+                      int ldx, int L, bdda_solve_stats* stats, cudaStream_t st) {
+  const int n = 3 * op->dip.nocc;
+  if (n == 0) { set_error("no dipoles set on the operator"); return BDDA_ERR_INVALID; }
+  if (L < 1 || L > kMaxL) { set_error("nrhs must be 1..32"); return BDDA_ERR_INVALID; }
+  if (ldb < n || ldx < n) { set_error("leading dimension smaller than 3*nocc"); return BDDA_ERR_INVALID; }
+  const bool mixed = o->precision == BDDA_SOLVE_MIXED;
+  if (mixed && !(op->prec & BDDA_PREC_FP32)) { set_error("mixed precision needs BDDA_PREC_FP32 tables"); return BDDA_ERR_INVALID; }
+  if (!(op->prec & BDDA_PREC_FP64) && (!mixed || o->true_tol > 0)) {
+    set_error("this solve needs BDDA_PREC_FP64 tables");
+    return BDDA_ERR_INVALID;
+  }
+  const bool refine = o->true_tol > 0;
+  const int itermax = o->itermax > 0 ? o->itermax : 300;
+  BDDA_TRY(ensure_work(op, n, L, itermax, !mixed, mixed));
+  SolverWork* w = op->solver.get();
+  const int check_every = o->check_every > 0 ? o->check_every : 4;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, st);
+  k_diag_prep<<<vec_grid(n), 256, 0, st>>>(n, diag, w->jpre64.as<double2>(), w->diag32.as<float2>(), w->jpre32.as<float2>());
+  ++op->kernel_launches;
+  const double2* jpre64 = o->jacobi ? w->jpre64.as<double2>() : nullptr;
+  const float2* jpre32 = o->jacobi ? w->jpre32.as<float2>() : nullptr;
+  const bool full = !o->jacobi && o->solver == BDDA_SOLVER_COCG_RQ;  // fullPivLu only in bl_cocg_rq_mvp_fft
+
+  Krylov<double> k64{op, w, st, n, L, diag, jpre64, check_every};
+  Krylov<float> k32{op, w, st, n, L, w->diag32.as<float2>(), jpre32, check_every};
+  int total_iters = 0, refinements = 0, status = BDDA_OK, mvps = 0;
+  double last_err = 0.0, resmax = -1.0;
+
+  // inner solve on RHS R (FP64, leading dim ldr): the correction D is solved in
+  // the inner precision into block 9 (right-hand side in block 8), then added
+  // to (accumulate) or written into Dst.
+  auto inner = [&](const double2* R, int ldr, double tol, double2* Dst, int ldd, bool accumulate) -> int {
+    int it = 0, stt = 0;
+    double er = 0.0;
+    const int gv = vec_grid((size_t)n * L);
+    if (!mixed) {
+      double2* Bp = w->blk64[8].as<double2>();
+      double2* D = w->blk64[9].as<double2>();
+      if (o->jacobi) k_rowscale<double, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n);
+      else k_convert<double, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n);
+      ++op->kernel_launches;
+      BDDA_TRY(k64.run(o->solver, Bp, D, full, tol, itermax, &it, &er, &stt));
+      if (accumulate) k_accumulate<double><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
+      else k_convert<double, double><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
+      ++op->kernel_launches;
+    } else {
+      float2* Bp = w->blk32[8].as<float2>();
+      float2* D = w->blk32[9].as<float2>();
+      if (o->jacobi) k_rowscale<float, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n);
+      else k_convert<float, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n);
+      ++op->kernel_launches;
+      BDDA_TRY(k32.run(o->solver, Bp, D, full, tol, itermax, &it, &er, &stt));
+      if (accumulate) k_accumulate<float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
+      else k_convert<double, float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
+      ++op->kernel_launches;
+    }
+    total_iters += it;
+    last_err = er;
+    ++refinements;
+    if (stt != 0) status = stt;
+    return BDDA_OK;
+  };
+
+  if (!refine) {
+    BDDA_TRY(inner(B, ldb, o->tol, X, ldx, false));
+    if (status == BDDA_OK && last_err >= o->tol) status = BDDA_ERR_NOT_CONVERGED;
+  } else {
+    std::vector<double> bn2;
+    BDDA_TRY(host_colnorm2(op, st, B, n, L, &bn2));
+    for (int l = 0; l < L; ++l)
+      if (!(bn2[l] > 0.0)) { set_error("zero right-hand side column"); return BDDA_ERR_INVALID; }
+    BDDA_CUDA(cudaMemset2DAsync(X, sizeof(double2) * (size_t)ldx, 0, sizeof(double2) * (size_t)n, L, st));
+    const int max_refine = o->max_refine > 0 ? o->max_refine : 8;
+    const double itol = o->inner_tol > 0 ? o->inner_tol : (mixed ? 2e-5 : 0.3 * o->true_tol);
+    const double2* R = B;
+    int ldr = ldb;
+    bool converged = false;
+    for (int r = 0; r < max_refine; ++r) {
+      BDDA_TRY(inner(R, ldr, itol, X, ldx, true));
+      if (status == BDDA_ERR_BREAKDOWN) break;
+      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, n, L, bn2, &resmax, &mvps));
+      R = w->R64.as<double2>();
+      ldr = n;
+      if (resmax <= o->true_tol) { converged = true; break; }
+    }
+    if (status == BDDA_OK && !converged) status = BDDA_ERR_NOT_CONVERGED;
+  }
+  cudaEventRecord(e1, st);
+  BDDA_CUDA(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (stats) {
+    stats->status = status;
+    stats->iterations = total_iters;
+    stats->refinements = refinements;
+    stats->mvps = mvps + k64.mvps + k32.mvps;
+    stats->final_err = last_err;
+    stats->true_res_max = resmax;
+    stats->ms_solve = ms;
+  }
+  BDDA_CUDA(cudaGetLastError());
+  if (status == BDDA_ERR_BREAKDOWN) set_error("breakdown: singular L x L system, failed Cholesky or non-finite value");
+  if (status == BDDA_ERR_NOT_CONVERGED) set_error("tolerance not reached within itermax / max_refine");
+  return status;
+}
+
+}  // namespace bdda
+
+using namespace bdda;
+
+extern "C" {
+
+void bdda_solve_opts_default(bdda_solve_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->solver = BDDA_SOLVER_COCG_RQ;
+  o->jacobi = 1;
+  o->precision = BDDA_SOLVE_FP64;
+  o->tol = 1e-2;
+  o->itermax = 300;
+  o->true_tol = 0.0;
+  o->inner_tol = 0.0;
+  o->max_refine = 8;
+  o->check_every = 4;
+}
+
+int bdda_solve_device(bdda_op* op, const bdda_solve_opts* opts, const double* diag, const double* B, int ldb, double* X,
+                      int ldx, int L, bdda_solve_stats* stats, void* stream) {
+  if (!op || !opts || !diag || !B || !X) { set_error("null argument"); return BDDA_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(op->mu);
+  cudaStream_t st = stream ? (cudaStream_t)stream : op->stream;
+  return solve_impl(op, opts, (const double2*)diag, (const double2*)B, ldb, (double2*)X, ldx, L, stats, st);
+}
+
+int bdda_solve(bdda_op* op, const bdda_solve_opts* opts, const double* diag, const double* B, int ldb, double* X, int ldx,
+               int L, bdda_solve_stats* stats) {
+  if (!op || !opts || !diag || !B || !X) { set_error("null argument"); return BDDA_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(op->mu);
+  const int n = 3 * op->dip.nocc;
+  if (n == 0) { set_error("no dipoles set on the operator"); return BDDA_ERR_INVALID; }
+  if (ldb < n || ldx < n || L < 1) { set_error("bad leading dimension or nrhs"); return BDDA_ERR_INVALID; }
+  cudaStream_t st = op->stream;
+  DevBuf d, b, x;
+  BDDA_CUDA(d.ensure(sizeof(double2) * (size_t)n));
+  BDDA_CUDA(b.ensure(sizeof(double2) * (size_t)n * L));
+  BDDA_CUDA(x.ensure(sizeof(double2) * (size_t)n * L));
+  BDDA_CUDA(cudaMemcpyAsync(d.p, diag, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
+  BDDA_CUDA(cudaMemcpy2DAsync(b.p, sizeof(double2) * n, B, sizeof(double2) * (size_t)ldb, sizeof(double2) * n, L,
+                              cudaMemcpyHostToDevice, st));
+  const int rc = solve_impl(op, opts, d.as<double2>(), b.as<double2>(), n, x.as<double2>(), n, L, stats, st);
+  if (rc == BDDA_OK || rc == BDDA_ERR_NOT_CONVERGED) {
+    BDDA_CUDA(cudaMemcpy2DAsync(X, sizeof(double2) * (size_t)ldx, x.p, sizeof(double2) * n, sizeof(double2) * n, L,
+                                cudaMemcpyDeviceToHost, st));
+    BDDA_CUDA(cudaStreamSynchronize(st));
+  }
+  return rc;
+}
+
+int bdda_qr_reduced(const double* A, int m, int nc, int lda, double* Q, int ldq, double* R) {
+  if (!A || !Q || !R || m < 1 || nc < 1 || nc > kMaxL || lda < m || ldq < m) {
+    set_error("bad qr_reduced arguments");
+    return BDDA_ERR_INVALID;
+  }
+  cudaStream_t st;
+  BDDA_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  Op tmp;  // bookkeeping only (timer, workspace); no tables
+  int rc = ensure_work(&tmp, m, nc, 1, true, false);
+  if (rc) { cudaStreamDestroy(st); return rc; }
+  SolverWork* w = tmp.solver.get();
+  Krylov<double> kr{&tmp, w, st, m, nc, nullptr, nullptr, 4};
+  double2* a = w->blk64[0].as<double2>();
+  double2* q = w->blk64[1].as<double2>();
+  double2* s = w->blk64[2].as<double2>();
+  cudaMemcpy2DAsync(a, sizeof(double2) * m, A, sizeof(double2) * (size_t)lda, sizeof(double2) * m, nc, cudaMemcpyHostToDevice, st);
+  // ctl reset with a unit norm so the init kernel does not flag a zero block
+  rc = kr.init(a);
+  if (rc == BDDA_OK) {
+    kr.cholqr2(a, s, q, 2);
+    std::vector<double2> hr((size_t)nc * nc);
+    cudaMemcpy2DAsync(Q, sizeof(double2) * (size_t)ldq, q, sizeof(double2) * m, sizeof(double2) * m, nc, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(hr.data(), kr.sl(kXi), sizeof(double2) * hr.size(), cudaMemcpyDeviceToHost, st);
+    bool done = false;
+    kr.poll(&done);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "qr_reduced");
+    else if (w->ctl_host->status != 0) { set_error("qr_reduced: rank-deficient block (Cholesky failed)"); rc = BDDA_ERR_BREAKDOWN; }
+    std::memcpy(R, hr.data(), sizeof(double2) * hr.size());
+  }
+  cudaStreamDestroy(st);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,210 @@
+/*
+ * bdda.h -- C ABI of the GB300 block-DDA solve path.
+ *
+ * Drop-in boundary for the reference's fast operator and block solvers
+ * (nmoteki/block-DDA).  Plain C types only: complex numbers are interleaved
+ * {re, im} doubles (or floats for FP32 device buffers); matrices are
+ * column-major with an explicit leading dimension, exactly like the Eigen
+ * MatrixXcd the reference passes around (column l = right-hand side l,
+ * row 3*m + c = component c of occupied dipole m).
+ *
+ * Every function returns BDDA_OK (0) or an error code; bdda_last_error()
+ * gives the message of the calling thread's last failure.  Nothing in this
+ * library calls exit(); a CUDA error is reported, not fatal.
+ *
+ * Thread safety: calls on one bdda_op are serialised by a lock inside the
+ * operator, so host threads may call bdda_mbt_fft_mvp concurrently on a shared
+ * operator (the reference calls MBT_fft_mvp from OpenMP threads on shared
+ * plans, bl_krylov_mvp_fft/bl_cocg_rq_mvp_fft.cpp:38-51).
+ */
+#ifndef BDDA_H
+#define BDDA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define BDDA_OK 0
+#define BDDA_ERR_INVALID 1      /* bad argument (size, f, pointer, box too large) */
+#define BDDA_ERR_CUDA 2         /* CUDA runtime error */
+#define BDDA_ERR_NOMEM 3        /* device allocation failed */
+#define BDDA_ERR_BREAKDOWN 4    /* singular L x L system, failed Cholesky or NaN in a solve */
+#define BDDA_ERR_NOT_CONVERGED 5 /* itermax / refinement limit reached before the tolerance */
+
+/* ---- precision bits of an operator ----------------------------------- */
+#define BDDA_PREC_FP64 1        /* complex FP64 tables (plain FP64 path, true residuals) */
+#define BDDA_PREC_FP32 2        /* complex FP32 tables (mixed-precision inner solves)   */
+
+/* ---- solvers (bl_*_mvp_fft in bl_krylov_mvp_fft/DDA_linear_solvers.hpp:1-6) */
+#define BDDA_SOLVER_COCG_RQ 0   /* block COCG-RQ, complex-symmetric systems  */
+#define BDDA_SOLVER_BICGSTAB 1  /* block BiCGSTAB                            */
+#define BDDA_SOLVER_BICGGR 2    /* block BiCGGR                              */
+
+/* ---- solve precision -------------------------------------------------- */
+#define BDDA_SOLVE_FP64 0       /* everything in complex FP64                                  */
+#define BDDA_SOLVE_MIXED 1      /* complex FP32 Krylov + FFT-MVP inside FP64 iterative refinement */
+
+typedef struct bdda_op bdda_op;
+
+/*
+ * Operator creation.  Replaces MBT_fft_init (mvp_fft/MBT_fft_init.cpp:10-42,
+ * declared in MBT_utils.hpp:5): instead of returning the FFT of the 1-D MBT
+ * projection Au_til, the Green-tensor spectrum on the 2x-padded 5-smooth grid
+ * is built on the device and kept in the handle.
+ *   n[3]        lattice box (nx, ny, nz), each 1..256
+ *   f           3 (electric dipoles, the reference's CED)
+ *   lf          lattice spacing (physical length)
+ *   k_re, k_im  wavenumber in the medium
+ *   prec        BDDA_PREC_FP64 and/or BDDA_PREC_FP32
+ */
+int bdda_op_create(bdda_op** op, const int n[3], int f, double lf, double k_re, double k_im, int prec);
+
+/* Release an operator (null is accepted). */
+int bdda_op_destroy(bdda_op* op);
+
+/*
+ * Occupied lattice sites (host array of 0-based addresses
+ * ny*nz*ix + nz*iy + iz, Target_manager.cpp:98,167-169, in the caller's dipole
+ * order).  Required before bdda_op_mvp_device / bdda_solve*.
+ */
+int bdda_op_set_dipoles(bdda_op* op, const int* address, int nocc);
+
+/* Padded grid, dipole count and number of occupied (x, y) lattice lines. */
+int bdda_op_info(const bdda_op* op, int P[3], int* nocc, int* nlines);
+
+/*
+ * Reference MBT_fft_mvp (mvp_fft/MBT_fft_mvp.cpp:8-43, MBT_utils.hpp:6):
+ * q_hat = A_off p_hat on the full cuboid vector of length f*nx*ny*nz (host
+ * buffers, interleaved complex FP64, site-major xyz).  No diagonal.
+ */
+int bdda_mbt_fft_mvp(bdda_op* op, const double* p_hat, double* q_hat);
+
+/*
+ * Block MVP over the dipoles set with bdda_op_set_dipoles, device buffers,
+ * all L right-hand sides in one pass:
+ *   y = [diag o x +] A_off x [o jpre]
+ * This is the inline block-MVP wrapper of every reference solver
+ * (e.g. bl_krylov_mvp_fft/bl_cocg_rq_jacobi_mvp_fft.cpp:43-60).
+ *   prec      BDDA_PREC_FP64 (double2 buffers) or BDDA_PREC_FP32 (float2 buffers)
+ *   x, y      3*nocc x L column-major, leading dimensions ldx, ldy (>= 3*nocc)
+ *   diag      3*nocc complex or null (off-diagonal part only)
+ *   jpre      3*nocc complex or null (no Jacobi scaling)
+ *   stream    cudaStream_t or null (the operator's stream)
+ */
+int bdda_op_mvp_device(bdda_op* op, int prec, const void* x, int ldx, void* y, int ldy, int L,
+                       const void* diag, const void* jpre, void* stream);
+
+/* ---- block solvers ----------------------------------------------------- */
+typedef struct {
+  int solver;         /* BDDA_SOLVER_* */
+  int jacobi;         /* 1: left Jacobi scaling by 1/DIAG_A (the *_jacobi_mvp_fft variants) */
+  int precision;      /* BDDA_SOLVE_FP64 or BDDA_SOLVE_MIXED */
+  double tol;         /* reference stopping test on the recurrence error (Solver.hpp:27 default 1e-2) */
+  int itermax;        /* reference iteration limit per Krylov solve (Solver.hpp:28 default 300) */
+  double true_tol;    /* >0: iterate until every column's true residual ||b-Ax||/||b|| <= true_tol
+                         (FP64 residuals, iterative refinement); <=0: one reference-semantics solve */
+  double inner_tol;   /* tolerance of each inner Krylov solve in refinement mode (0 -> automatic) */
+  int max_refine;     /* refinement steps limit (0 -> 8) */
+  int check_every;    /* host convergence poll period in iterations (0 -> 4) */
+} bdda_solve_opts;
+
+typedef struct {
+  int status;             /* BDDA_OK / BDDA_ERR_BREAKDOWN / BDDA_ERR_NOT_CONVERGED */
+  int iterations;         /* Krylov iterations, summed over refinement steps */
+  int refinements;        /* inner solves performed */
+  int mvps;               /* block MVPs performed (all precisions) */
+  double final_err;       /* last recurrence error (the reference's printed value) */
+  double true_res_max;    /* max over columns of ||b_l - A x_l|| / ||b_l|| (FP64), -1 if not computed */
+  double ms_solve;        /* device time of the whole solve (CUDA events) */
+} bdda_solve_stats;
+
+/* Fill opts with the reference defaults (COCG-RQ-Jacobi, FP64, tol 1e-2, itermax 300). */
+void bdda_solve_opts_default(bdda_solve_opts* opts);
+
+/*
+ * Solve (DIAG_A + A_off) X = B for L right-hand sides.  Replaces
+ * bl_cocg_rq_mvp_fft, bl_cocg_rq_jacobi_mvp_fft, bl_bicgstab_mvp_fft,
+ * bl_bicgstab_jacobi_mvp_fft, bl_bicggr_mvp_fft, bl_bicggr_jacobi_mvp_fft
+ * (bl_krylov_mvp_fft/DDA_linear_solvers.hpp:1-6).
+ * Device buffers, complex FP64: diag[3*nocc], B (ldb), X (ldx), X is overwritten.
+ */
+int bdda_solve_device(bdda_op* op, const bdda_solve_opts* opts, const double* diag, const double* B, int ldb,
+                      double* X, int ldx, int L, bdda_solve_stats* stats, void* stream);
+
+/* Same with host buffers (copies in and out inside the call). */
+int bdda_solve(bdda_op* op, const bdda_solve_opts* opts, const double* diag, const double* B, int ldb,
+               double* X, int ldx, int L, bdda_solve_stats* stats);
+
+/*
+ * Thin QR with R real-positive on the diagonal (qr_reduced,
+ * bl_krylov_mvp_fft/qr_reduced.cpp:9-31, linear_algebra_addon.hpp:1), complex
+ * FP64 host buffers: A (m x n, lda) -> Q (m x n, ldq), R (n x n, column-major).
+ * Computed on the device by CholQR2.  n <= 32.
+ */
+int bdda_qr_reduced(const double* A, int m, int n, int lda, double* Q, int ldq, double* R);
+
+/* ---- target, fields and cross sections (host) --------------------------- */
+
+/*
+ * Polarizability alpha = 3 i a1 / (2 k^3) of a sphere of radius r_p
+ * (Target_manager.cpp:215-233), a1 the first Mie coefficient (BH83).  Also
+ * returns b1 (for magnetic dipoles).  eps/mu as {re, im}.
+ */
+int bdda_mie_a1b1(double wl0, double r_p, const double eps_p[2], const double mu_p[2], const double eps_m[2],
+                  const double mu_m[2], double a1[2], double b1[2]);
+
+/*
+ * Seeded lattice particle-cluster aggregate of exactly nocc sites with
+ * radius of gyration Rg(N) = a (N/kf)^(1/Df) (a = 1 lattice spacing).
+ * Output: box n[3] and 0-based addresses (address must hold nocc ints).
+ */
+int bdda_aggregate(int nocc, double kf, double Df, unsigned long long seed, int n[3], int* address);
+
+/*
+ * Incident fields for f=3 (Target_manager.cpp:262-279): B[3m+c, l] =
+ * e_l[c] exp(i k u_l . r_m), r_m = (ix, iy, iz) lf.  uinc, einc: L x 3
+ * (einc complex interleaved).  B has leading dimension ldb.
+ */
+int bdda_incident_fields(const int n[3], double lf, const int* address, int nocc, double k, int L,
+                         const double* uinc, const double* einc, double* B, int ldb);
+
+/*
+ * Cext, Cabs, Csca per column (Result_manager.cpp:132-143): out[3*l + {0,1,2}].
+ * Host buffers.  alpha0 = polarizability of dipole 0 (the reference uses it
+ * for every dipole).
+ */
+int bdda_cross_sections(double k, const double alpha0[2], const double* E, int lde, const double* P, int ldp,
+                        int nrows, int L, double* out);
+
+/* ---- instrumentation ------------------------------------------------------ */
+
+/* Enable (1) / disable (0) per-kernel CUDA-event timing on the operator. */
+int bdda_op_set_timing(bdda_op* op, int enable);
+
+/*
+ * Per-kernel totals since the last reset: ms[i], launches[i] for
+ * i = 0..n-1 in the order passA, passB, passC, passD, passE, gram, update,
+ * small, other.  Returns the number of entries written (<= n).  reset=1 zeroes
+ * the counters after reading.
+ */
+int bdda_op_kernel_stats(bdda_op* op, double* ms, long long* launches, int n, int reset);
+
+/* Message of the calling thread's last error (empty string if none). */
+const char* bdda_last_error(void);
+
+/*
+ * Test hook: run the device FFT core (the same source the kernels inline) on
+ * the CPU for one line of length N (5-smooth, <= 512).  inverse = 0: natural
+ * order in, digit-reversed spectrum out; inverse = 1: digit-reversed in,
+ * natural out, unnormalised.  prec 1 = FP64, 2 = FP32 arithmetic.  data holds
+ * N interleaved complex doubles, overwritten.  Returns the number of radix
+ * stages (radices written to radix[0..16)) or -1 for an unsupported N.
+ */
+int bdda_host_fft_line(int N, int inverse, int prec, double* data, int* radix);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BDDA_H */

@@ -1,0 +1,133 @@
+"""Oracle: targets, incident fields, DIAG_A and cross sections (numpy, FP64).
+
+Test infrastructure only (see ``oracle/__init__.py``).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+# --------------------------------------------------------------------------
+# libstdc++ default_random_engine + uniform_real_distribution<double>(0,1)
+# --------------------------------------------------------------------------
+
+class MinstdUniform:
+    """``std::default_random_engine`` (minstd_rand0, seed 1) feeding
+    ``uniform_real_distribution<double>{0,1}`` as libstdc++ implements it
+    (``generate_canonical<double,53>``: two draws, sum/(r*r) with r = 2^31-2).
+
+    Used by ``Incident_Wave::set_random_incident_directions``
+    (``Incident_Wave.cpp:32-40``).
+    """
+
+    A = 16807
+    M = 2147483647
+
+    def __init__(self, seed: int = 1):
+        self.state = seed % self.M or 1
+
+    def _next(self) -> int:
+        self.state = (self.A * self.state) % self.M
+        return self.state
+
+    def __call__(self) -> float:
+        r = float(self.M - 1)          # max - min + 1 = 2147483646
+        s = float(self._next() - 1)
+        s = s + float(self._next() - 1) * r
+        tmp = float(np.float64(r) * np.float64(r))
+        ret = s / tmp
+        if ret >= 1.0:
+            ret = np.nextafter(1.0, 0.0)
+        return ret
+
+
+def angle_axis(psi: float, axis) -> np.ndarray:
+    """Rotation matrix of ``Eigen::AngleAxisd(psi, axis)`` (Rodrigues)."""
+    u = np.asarray(axis, dtype=np.float64)
+    c, s = math.cos(psi), math.sin(psi)
+    ux = np.array([[0.0, -u[2], u[1]], [u[2], 0.0, -u[0]], [-u[1], u[0], 0.0]])
+    return c * np.eye(3) + (1.0 - c) * np.outer(u, u) + s * ux
+
+
+def reference_incident_waves(n_inc: int, eper_m=1.0 + 0j, mper_m=1.0 + 0j):
+    """Propagation, E and H polarisation vectors of ``Incident_Wave``.
+
+    Default wave +z, x-polarised (``Incident_Wave.cpp:14-25``) followed by
+    ``n_inc - 1`` random axis-angle rotations of it (``:29-49``).
+    """
+    u0 = np.array([0.0, 0.0, 1.0])
+    e0 = np.array([1.0, 0.0, 0.0], dtype=np.complex128)
+    h0 = np.array([0.0, np.sqrt(eper_m / mper_m), 0.0], dtype=np.complex128)
+    us, es, hs = [u0], [e0], [h0]
+    urf = MinstdUniform(1)
+    for _i in range(1, n_inc):
+        theta = math.acos(2.0 * urf() - 1.0)
+        phi = 2 * math.pi * urf()
+        nvec = np.array([math.sin(theta) * math.cos(phi), math.sin(theta) * math.sin(phi), math.cos(theta)])
+        psi = 2 * math.pi * urf()
+        rot = angle_axis(psi, nvec)
+        us.append(rot @ u0)
+        es.append(rot @ e0)
+        hs.append(rot @ h0)
+    return np.array(us), np.array(es), np.array(hs)
+
+
+# --------------------------------------------------------------------------
+# targets
+# --------------------------------------------------------------------------
+
+def read_target_file(path: str, scale_factor: float):
+    """Parse a ``DDA_target_*.out`` file (``Target_manager.cpp:142-201``).
+
+    Header: pp_radius, aggregate volume, coating volume, ``nx ny nz``, lf; then
+    rows ``address vol material_index``.  lf and vol are scaled by
+    scale_factor and scale_factor^3 (``:157,172``).
+    """
+    with open(path) as fh:
+        lines = fh.read().splitlines()
+    n = tuple(int(v) for v in lines[3].split())
+    lf = float(lines[4]) * scale_factor
+    rows = [ln.split() for ln in lines[5:] if ln.strip()]
+    address = np.array([int(r[0]) for r in rows], dtype=np.int64)
+    vol = np.array([float(r[1]) for r in rows]) * scale_factor ** 3
+    mat = np.array([int(r[2]) for r in rows], dtype=np.int64)
+    return n, lf, address, vol, mat
+
+
+def positions(n, lf, address):
+    """Physical coordinates (ix, iy, iz) * lf (``Target_manager.cpp:167-171``)."""
+    nx, ny, nz = n
+    address = np.asarray(address)
+    ix = address // (ny * nz)
+    iy = (address - ny * nz * ix) // nz
+    iz = address - ny * nz * ix - nz * iy
+    return np.stack([ix, iy, iz], axis=1).astype(np.float64) * lf
+
+
+def incident_fields(pos, k, einc, uinc):
+    """EHinc for f=3: ``einc_l exp(i k u_l . r_m)`` (``Target_manager.cpp:267-277``)."""
+    nocc = pos.shape[0]
+    L = len(einc)
+    out = np.zeros((3 * nocc, L), dtype=np.complex128)
+    for l in range(L):
+        ph = np.exp(1j * k * (pos @ np.asarray(uinc[l])))
+        out[:, l] = (ph[:, None] * np.asarray(einc[l])[None, :]).reshape(-1)
+    return out
+
+
+def diag_a(alpha_e):
+    """DIAG_A = 1/alpha_E repeated over the 3 components (``Solver.cpp:33-36``)."""
+    return np.repeat(1.0 / np.asarray(alpha_e, dtype=np.complex128), 3)
+
+
+def cross_sections(k: float, ehinc, pm, alpha0):
+    """Cext, Cabs, Csca per incident wave, f=3 (``Result_manager.cpp:132-143``).
+
+    Cext = 4 pi k Im(E^H P); Cabs = 4 pi k (Im(conj(1/alpha_0)) - 2k^3/3) ||P||^2
+    with the polarizability of dipole 0 used for every dipole (``:135``).
+    """
+    cext = 4 * math.pi * k * np.imag(np.sum(np.conj(ehinc) * pm, axis=0))
+    cabs = 4 * math.pi * k * (np.imag(np.conj(1.0 / alpha0)) - 2.0 * k ** 3 / 3.0) * np.sum(np.abs(pm) ** 2, axis=0)
+    return cext, cabs, cext - cabs

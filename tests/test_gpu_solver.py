@@ -1,0 +1,132 @@
+"""Block Krylov solvers on the GPU against the oracle (parity tests, -m gpu).
+
+* reference semantics (one solve, the reference's recurrence error and tol):
+  same iteration count as the oracle restatement, per-iteration errors within
+  1e-6 relative, solution within 1e-6 relative;
+* the recorded run result.dat (f=3 block COCG-RQ-Jacobi, N512 target, tol 1e-2)
+  reproduced through the C ABI to its printed digits;
+* refinement mode: every column's true residual <= 1e-8, FP64 and mixed
+  precision, cross sections of the two within 1e-6 relative.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import bdda
+from conftest import golden
+from oracle import krylov, mbt, physics
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_problem(nocc=150, L=4, seed=21, m=1.7 + 0.3j):
+    prob = bdda.make_problem(nocc, m, seed=seed, n_dirs=max(1, L // 2))
+    rng = np.random.default_rng(seed)
+    B = prob.B[:, :L]
+    if B.shape[1] < L:
+        B = np.concatenate([B, rng.standard_normal((B.shape[0], L - B.shape[1]))], axis=1)
+    return prob, np.asfortranarray(B)
+
+
+def _oracle_amul(prob):
+    gh, P = mbt.green_hat(prob.n, 3, prob.lf, prob.k)
+    return lambda S: mbt.block_mvp(prob.n, 3, gh, P, prob.address, prob.diag, S)
+
+
+def test_qr_reduced_matches_oracle():
+    rng = np.random.default_rng(2)
+    for m, n in ((40, 1), (300, 7), (1000, 32)):
+        a = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+        q, r = bdda.qr_reduced(a)
+        qo, ro = krylov.qr_reduced(a)
+        assert np.max(np.abs(q - qo)) < 1e-12
+        assert np.max(np.abs(r - ro)) / np.max(np.abs(ro)) < 1e-13
+
+
+@pytest.mark.parametrize("solver", ["cocg_rq", "bicgstab", "bicggr"])
+@pytest.mark.parametrize("jacobi", [False, True])
+def test_solver_reference_semantics_vs_oracle(solver, jacobi):
+    prob, B = _small_problem()
+    amul = _oracle_amul(prob)
+    Xo, hist = krylov.SOLVERS[solver](amul, B, 1e-6, 300, diag=prob.diag, jacobi=jacobi)
+    op = bdda.Operator(prob.n, prob.lf, prob.k)
+    op.set_dipoles(prob.address)
+    opts = bdda.solve_opts(solver=solver, jacobi=jacobi, tol=1e-6, itermax=300)
+    X, st = bdda.solve(op, prob.diag, B, opts)
+    assert st["status"] == 0
+    assert st["iterations"] == len(hist), (st["iterations"], len(hist))
+    assert abs(st["final_err"] - hist[-1]) / hist[-1] < 1e-4
+    assert np.linalg.norm(X - Xo) / np.linalg.norm(Xo) < 1e-6
+
+
+def test_result_dat_reproduced_on_gpu():
+    t = golden("target_N512.json")
+    g = golden("result_dat_N512.json")
+    scale = g["scale_factor"]
+    n = tuple(t["n"])
+    lf = t["lf"] * scale
+    addr = np.array(t["address"], dtype=np.int32)
+    vol = np.array(t["vol"]) * scale ** 3
+    k = 2 * math.pi / 0.3
+    r_p = np.cbrt(3 * vol / (4 * math.pi))
+    alpha = np.array([bdda.polarizability(0.3, r, complex(*g["eper"]), k) for r in r_p])
+    diag = np.repeat(1.0 / alpha, 3)
+    u, e, _ = physics.reference_incident_waves(4)
+    B = bdda.incident_fields(n, lf, addr, k, u, e)
+    op = bdda.Operator(n, lf, k)
+    op.set_dipoles(addr)
+    X, st = bdda.solve(op, diag, B, bdda.solve_opts("cocg_rq", jacobi=True, tol=1e-2, itermax=300))
+    assert st["iterations"] == len(g["oracle_history"])
+    cext, cabs, csca = bdda.cross_sections(k, alpha[0], B, X)
+    rec = g["recorded"]
+    mass = vol.sum() * 1e-12 * g["density"]
+    assert abs(csca.mean() - rec["mean_Csca"]) / rec["mean_Csca"] < 2e-6
+    assert abs(csca.std(ddof=1) - rec["std_Csca"]) / rec["std_Csca"] < 2e-5
+    assert abs((cabs * 1e-12 / mass).mean() - rec["mean_MAC"]) / rec["mean_MAC"] < 2e-6
+    assert abs((csca / cext).mean() - rec["mean_SSA"]) / rec["mean_SSA"] < 2e-6
+    assert np.allclose(csca, g["oracle_Csca"], rtol=1e-7)
+
+
+@pytest.mark.parametrize("precision", [bdda.SOLVE_FP64, bdda.SOLVE_MIXED])
+@pytest.mark.parametrize("solver", ["cocg_rq", "bicgstab"])
+def test_refinement_reaches_true_residual(precision, solver):
+    prob = bdda.make_problem(1024, 1.95 + 0.79j, seed=1, n_dirs=1)
+    op = bdda.Operator(prob.n, prob.lf, prob.k)
+    op.set_dipoles(prob.address)
+    opts = bdda.solve_opts(solver, jacobi=True, precision=precision, true_tol=1e-8, itermax=1000)
+    X, st = bdda.solve(op, prob.diag, prob.B, opts, allow_not_converged=False)
+    assert st["true_res_max"] <= 1e-8
+    res = krylov.true_residual(_oracle_amul(prob), prob.B, X)
+    assert np.all(res < 2e-8), res
+
+
+def test_mixed_matches_fp64_cross_sections():
+    prob = bdda.make_problem(2000, 2.3 + 0.6j, seed=4, n_dirs=4)
+    op = bdda.Operator(prob.n, prob.lf, prob.k)
+    op.set_dipoles(prob.address)
+    X64, s64 = bdda.solve(op, prob.diag, prob.B, bdda.solve_opts("cocg_rq", precision=bdda.SOLVE_FP64,
+                                                                  true_tol=1e-8, itermax=2000))
+    X32, s32 = bdda.solve(op, prob.diag, prob.B, bdda.solve_opts("cocg_rq", precision=bdda.SOLVE_MIXED,
+                                                                  true_tol=1e-8, itermax=2000))
+    assert s64["true_res_max"] <= 1e-8 and s32["true_res_max"] <= 1e-8
+    c64 = bdda.cross_sections(prob.k, prob.alpha[0], prob.B, X64)
+    c32 = bdda.cross_sections(prob.k, prob.alpha[0], prob.B, X32)
+    for a, b in zip(c32, c64):
+        assert np.max(np.abs(a - b) / np.abs(b)) < 1e-6
+    assert np.linalg.norm(X32 - X64) / np.linalg.norm(X64) < 1e-6
+
+
+def test_solve_status_codes():
+    prob, B = _small_problem(nocc=60, L=2)
+    op = bdda.Operator(prob.n, prob.lf, prob.k)
+    op.set_dipoles(prob.address)
+    _X, st = bdda.solve(op, prob.diag, B, bdda.solve_opts("cocg_rq", tol=1e-14, itermax=3))
+    assert st["status"] == bdda.ERR_NOT_CONVERGED and st["iterations"] == 3
+    Bz = B.copy()
+    Bz[:, 1] = 0.0
+    with pytest.raises(bdda.BddaError) as ei:
+        bdda.solve(op, prob.diag, Bz, bdda.solve_opts("cocg_rq", true_tol=1e-8))
+    assert ei.value.code == bdda.ERR_INVALID
+    with pytest.raises(bdda.BddaError):
+        bdda.solve(op, prob.diag, np.zeros((3 * prob.nocc, 33)), bdda.solve_opts())

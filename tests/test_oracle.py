@@ -1,0 +1,130 @@
+"""The CPU oracle, pinned against the reference's own golden data (no GPU).
+
+* ``mvp_fft_example.cpp:37-103`` f=1 known-answer table pins the BT_fft ordering;
+* the literal 1-D MBT restatement, dense assembly and the 3-D padded FFT agree;
+* ``result.dat:14-42`` (f=3 block COCG-RQ-Jacobi on DDA_target_0_agg_N512,
+  tol 1e-2, 4 incident waves) is reproduced to its printed digits;
+* libstdc++'s ``default_random_engine`` draws (compiled and recorded) match the
+  restated generator bit for bit.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import krylov, mbt, physics
+
+
+def test_bt_fft_f1_known_answer():
+    table = golden("mbt_f1_index_table.json")
+    lut = {(tuple(r["row0"]), tuple(r["row1"])): r["value"] for r in table}
+
+    def leaf(n_ind):
+        return [[lut[(tuple(int(v) for v in n_ind[0]), tuple(int(v) for v in n_ind[1]))]]]
+
+    au = mbt.bt_fft([2, 2, 2], 1, np.ones((2, 3), dtype=np.int64), 1, 1.0, 1.0, leaf=leaf)
+    assert np.array_equal(au.real, np.arange(1, 28))
+
+
+@pytest.mark.parametrize("n,f", [((3, 2, 4), 3), ((2, 3, 2), 6), ((1, 1, 5), 3), ((4, 3, 3), 3), ((2, 1, 3), 6)])
+def test_literal_dense_3d_agree(n, f):
+    rng = np.random.default_rng(1)
+    lf, k = 0.7, 1.3 + 0.2j
+    N = int(np.prod(n))
+    x = rng.standard_normal(f * N) + 1j * rng.standard_normal(f * N)
+    y_lit = mbt.mbt_fft_mvp(n, f, mbt.mbt_fft_init(n, f, lf, k), x)
+    y_dense = mbt.dense_matrix(n, f, lf, k) @ x
+    gh, P = mbt.green_hat(n, f, lf, k)
+    y_3d = mbt.mvp3d(n, f, gh, P, x)
+    scale = np.linalg.norm(y_dense)
+    assert np.linalg.norm(y_lit - y_dense) / scale < 1e-13
+    assert np.linalg.norm(y_3d - y_dense) / scale < 1e-13
+
+
+def test_application_function_symmetry():
+    # f=3 block is complex symmetric and even in the offset; r = 0 gives zero
+    a = mbt.application_function((1, -2, 3), 3, 0.5, 2.0 + 0.1j)
+    assert np.allclose(a, a.T)
+    assert np.allclose(a, mbt.application_function((-1, 2, -3), 3, 0.5, 2.0 + 0.1j))
+    assert not np.any(mbt.application_function((0, 0, 0), 3, 0.5, 2.0))
+
+
+def test_rng_restatement_bit_exact():
+    g = golden("incident_dirs_ref.json")
+    u = physics.MinstdUniform(1)
+    for row in g["uniform_draws"]:
+        for v in row:
+            assert u() == v
+    us, es, _hs = physics.reference_incident_waves(g["n_inc"])
+    assert np.array_equal(us, np.array(g["uinc"]))
+    assert np.array_equal(es.real, np.array(g["einc_re"]))
+
+
+def test_qr_reduced_oracle():
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((60, 5)) + 1j * rng.standard_normal((60, 5))
+    q, r = krylov.qr_reduced(a)
+    assert np.allclose(q @ r, a)
+    assert np.allclose(q.conj().T @ q, np.eye(5))
+    assert np.allclose(np.tril(r, -1), 0)
+    assert np.all(np.abs(np.diag(r).imag) == 0) and np.all(np.diag(r).real > 0)
+
+
+def test_full_pivot_solve():
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal((7, 7)) + 1j * rng.standard_normal((7, 7))
+    b = rng.standard_normal((7, 3)) + 1j * rng.standard_normal((7, 3))
+    assert np.allclose(krylov.full_piv_solve(a, b), np.linalg.solve(a, b))
+    assert np.allclose(krylov.partial_piv_solve(a, b), np.linalg.solve(a, b))
+
+
+def _result_dat_problem():
+    t = golden("target_N512.json")
+    g = golden("result_dat_N512.json")
+    scale = g["scale_factor"]
+    n = tuple(t["n"])
+    lf = t["lf"] * scale
+    addr = np.array(t["address"])
+    vol = np.array(t["vol"]) * scale ** 3
+    k = 2 * math.pi / 0.3
+    alpha0 = complex(*g["alpha0"])
+    alpha = np.full(addr.size, alpha0)
+    diag = physics.diag_a(alpha)
+    u, e, _ = physics.reference_incident_waves(4)
+    B = physics.incident_fields(physics.positions(n, lf, addr), k, e, u)
+    return n, lf, addr, vol, k, alpha0, diag, B, g
+
+
+def test_result_dat_reproduced_by_oracle():
+    n, lf, addr, vol, k, alpha0, diag, B, g = _result_dat_problem()
+    gh, P = mbt.green_hat(n, 3, lf, k)
+    X, hist = krylov.bl_cocg_rq(lambda S: mbt.block_mvp(n, 3, gh, P, addr, diag, S), B, 1e-2, 300,
+                                diag=diag, jacobi=True)
+    cext, cabs, csca = physics.cross_sections(k, B, X, alpha0)
+    rec = g["recorded"]
+    mass = vol.sum() * 1e-12 * g["density"]
+    mac = cabs * 1e-12 / mass
+    ssa = csca / cext
+    assert len(hist) == len(g["oracle_history"])
+    assert abs(csca.mean() - rec["mean_Csca"]) / rec["mean_Csca"] < 2e-6
+    assert abs(csca.std(ddof=1) - rec["std_Csca"]) / rec["std_Csca"] < 2e-5
+    assert abs(mac.mean() - rec["mean_MAC"]) / rec["mean_MAC"] < 2e-6
+    assert abs(ssa.mean() - rec["mean_SSA"]) / rec["mean_SSA"] < 2e-6
+    assert abs(vol.sum() - rec["volume_particle"]) / rec["volume_particle"] < 1e-5
+
+
+@pytest.mark.parametrize("name", ["cocg_rq", "bicgstab", "bicggr"])
+@pytest.mark.parametrize("jacobi", [False, True])
+def test_oracle_solvers_converge(name, jacobi):
+    rng = np.random.default_rng(5)
+    n = (4, 3, 5)
+    addr = np.sort(rng.choice(int(np.prod(n)), 30, replace=False))
+    k, lf = 2 * np.pi / 0.55, 0.02
+    alpha = physics.diag_a(np.full(30, 3e-6 + 1e-6j))
+    gh, P = mbt.green_hat(n, 3, lf, k)
+    amul = lambda S: mbt.block_mvp(n, 3, gh, P, addr, alpha, S)  # noqa: E731
+    B = rng.standard_normal((90, 3)) + 1j * rng.standard_normal((90, 3))
+    X, hist = krylov.SOLVERS[name](amul, B, 1e-10, 200, diag=alpha, jacobi=jacobi)
+    assert hist[-1] < 1e-10
+    assert np.all(krylov.true_residual(amul, B, X) < 1e-8)
