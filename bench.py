@@ -1,0 +1,388 @@
+"""Benchmark: RHS-solves/s at a 1e-8 true residual on one GB300 (per GPU replica).
+
+Workload (default): seeded lattice aggregate of N=16384 dipoles (kf=1.0,
+Df=2.8), m = 2.3+0.6i, lambda = 0.55 um, |m| k d = 0.5, nrhs = 16 (8 seeded
+directions x 2 polarisations), block COCG-RQ with Jacobi scaling, complex FP32
+FFT-MVP + Krylov inside FP64 iterative refinement until every column's true
+residual ||b - A x|| / ||b|| <= 1e-8.  One step = one full solve from X = 0.
+
+* ``value``      RHS-solves/s with inputs resident in HBM (bdda_solve_device);
+* ``e2e``        the same through the host-buffer C ABI (bdda_solve: pinned host
+                 B and DIAG copied in, X copied out, inside the timed region);
+* ``fp64_path``  the plain complex-FP64 solve of the same problem;
+* ``roofline``   the dominant kernel's algorithmic bytes per launch over its
+                 CUDA-event launch time, against MEASURED_PEAKS.json hbm_gbs;
+* ``cpu_baseline`` the reference's 1-D MBT FFT matvec restated on the host
+                 cores (oracle.mbt_fast, scipy FFT standing in for FFTW),
+                 one block MVP timed and extrapolated by the solver's
+                 iteration count.
+
+``--impl reference`` times that CPU restatement as the reference arm.
+Multi-GPU: one independent replica per rank (different seeds), weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "block-dda_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "RHS-solves/s at 1e-8 residual"
+UNIT = "RHS-solves/s"
+# Iterations of block COCG-RQ-Jacobi (reference stopping rule, FP64) to a
+# recurrence error of 1e-8 on the default workload; used to extrapolate the
+# timed CPU sample.  The GPU arm re-measures it and reports both.
+REF_ITERS_DEFAULT = 33
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nocc", type=int, default=16384)
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--m", default="2.3+0.6j")
+    ap.add_argument("--wl0", type=float, default=0.55)
+    ap.add_argument("--solver", default="cocg_rq")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison solve")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload_config(a, n=None, P=None):
+    cfg = {"workload": f"block COCG-RQ-Jacobi solve, N={a.nocc} dipole lattice aggregate (kf=1.0, Df=2.8, seed=1+rank), "
+                       f"m={a.m}, lambda={a.wl0} um, |m|kd=0.5, nrhs={a.nrhs}, true residual <= 1e-8",
+           "nocc": a.nocc, "nrhs": a.nrhs, "m": a.m, "wl0_um": a.wl0, "tol": 1e-8,
+           "precision": "complex FP32 Krylov + FFT-MVP inside FP64 refinement",
+           "solver": a.solver, "jacobi": True, "l2": "working set > L2 (FFT workspace ~0.7 GB)",
+           "parallelism": "replicas (one independent target per GPU)"}
+    if n is not None:
+        cfg["box"] = list(n)
+        cfg["padded_grid"] = list(P)
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([t.strip() for t in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) < 7:
+                continue
+            for i, nm in enumerate(names):
+                if r[3 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def padded_grid(n):
+    def smooth(v):
+        while True:
+            t = v
+            for p in (2, 3, 5):
+                while t % p == 0:
+                    t //= p
+            if t == 1:
+                return v
+            v += 1
+    return [smooth(2 * int(v)) for v in n]
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_reference_sample(prob, L, threads, reps=1):
+    """Time one block MVP of the reference's 1-D MBT FFT algorithm on the host."""
+    from oracle.mbt_fast import MbtCpu
+    t0 = time.perf_counter()
+    cpu = MbtCpu(prob.n, prob.lf, prob.k, prob.address, prob.diag, threads=threads)
+    t_init = time.perf_counter() - t0
+    S = np.asfortranarray(prob.B[:, :L])
+    times = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        cpu.block_mvp(S)
+        times.append(time.perf_counter() - t)
+    return min(times), t_init, cpu.M
+
+
+def run_reference(a):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import bdda
+    threads = os.cpu_count() or 1
+    prob = bdda.make_problem(a.nocc, complex(a.m), wl0=a.wl0, seed=1, n_dirs=a.nrhs // 2)
+    L = a.nrhs
+    from oracle.mbt_fast import MbtCpu
+    cpu = MbtCpu(prob.n, prob.lf, prob.k, prob.address, prob.diag, threads=threads)
+    S = np.asfortranarray(prob.B[:, :L])
+    for _ in range(a.warmup):
+        cpu.block_mvp(S)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        cpu.block_mvp(S)
+    dt = (time.perf_counter() - t0) / a.steps
+    per_solve = REF_ITERS_DEFAULT * dt
+    value = L / per_solve
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": dict(workload_config(a, prob.n, padded_grid(prob.n)), reference_fft_length=cpu.M),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"each step = one block MVP (L={L}) of the reference's 1-D MBT FFT algorithm "
+                                       f"(FFT length {cpu.M}, scipy pocketfft for FFTW, threads over RHS as the "
+                                       f"reference's OpenMP loop); RHS-solves/s = L / ({REF_ITERS_DEFAULT} iterations "
+                                       f"x step time); Krylov block algebra not counted"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(a):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import bdda
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    seed = 1 + rank
+    m = complex(a.m)
+    L = a.nrhs
+    prob = bdda.make_problem(a.nocc, m, wl0=a.wl0, seed=seed, n_dirs=L // 2)
+    op = bdda.Operator(prob.n, prob.lf, prob.k)
+    op.set_dipoles(prob.address)
+    P, nocc, nlines = op.info()
+    n = 3 * nocc
+    stream = torch.cuda.Stream(device=dev)
+    diag_d = torch.from_numpy(prob.diag).to(dev)
+    B_d = torch.from_numpy(np.ascontiguousarray(prob.B.T)).to(dev)       # (L, n) = column-major n x L
+    X_d = torch.zeros_like(B_d)
+    opts = bdda.solve_opts(a.solver, jacobi=True, precision=bdda.SOLVE_MIXED, true_tol=1e-8, itermax=3000)
+
+    def step():
+        return bdda.solve_device(op, diag_d.data_ptr(), B_d.data_ptr(), n, X_d.data_ptr(), n, L, opts,
+                                 stream=stream.cuda_stream, allow_not_converged=False)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    torch.cuda.synchronize()
+    for _ in range(max(3, a.warmup)):
+        st = step()
+    torch.cuda.synchronize()
+    # ---- timed region (device-resident inputs) ----
+    op.set_timing(True)
+    op.kernel_stats(reset=True)
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stats = []
+    for _ in range(a.steps):
+        stats.append(step())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    t_ms = e0.elapsed_time(e1)
+    ks = op.kernel_stats(reset=True)
+    op.set_timing(False)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+    total_rhs = a.steps * L * ws
+    value = total_rhs / (t_ms / 1e3)
+    launches = int(sum(v["launches"] for v in ks.values()))
+    # true residual + cross sections of the last step (host check)
+    X = X_d.cpu().numpy().T
+    res_max = max(s["true_res_max"] for s in stats)
+    iters = [s["iterations"] for s in stats]
+
+    # ---- roofline of the dominant kernel (live CUDA events of the timed region) ----
+    mvp32 = op.mvp_bytes(L, bdda.PREC_FP32, True, True)
+    mvp64 = op.mvp_bytes(L, bdda.PREC_FP64, True, False)
+    byte_model = {f"passA_c64": mvp32[0], "passB_c64": mvp32[1], "passC_c64": mvp32[2], "passD_c64": mvp32[3],
+                  "passE_c64": mvp32[4], "passA_c128": mvp64[0], "passB_c128": mvp64[1], "passC_c128": mvp64[2],
+                  "passD_c128": mvp64[3], "passE_c128": mvp64[4]}
+    dom = max((k for k in byte_model if ks[k]["launches"]), key=lambda k: ks[k]["ms"])
+    per_launch_ms = ks[dom]["ms"] / ks[dom]["launches"]
+    peak, peak_kind = measured_peak()
+    achieved = byte_model[dom] / (per_launch_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        tr = json.load(open(tpath))
+        key = f"{dom}:{a.nocc}:{L}"
+        if key in tr:
+            traffic = tr[key]
+    # whole FP32 MVP (5 passes)
+    mvp_ms = sum(ks[f"pass{p}_c64"]["ms"] for p in "ABCDE") / max(1, ks["passA_c64"]["launches"])
+    mvp_gbs = float(np.sum(mvp32)) / (mvp_ms / 1e3) / 1e9 if mvp_ms > 0 else None
+
+    # ---- e2e through the host-buffer C ABI (pinned host memory) ----
+    Bh = torch.from_numpy(np.ascontiguousarray(prob.B.T)).pin_memory()
+    Dh = torch.from_numpy(prob.diag.copy()).pin_memory()
+    Xh = torch.zeros_like(Bh).pin_memory()
+    import ctypes as ct
+
+    def e2e_step():
+        s = bdda.SolveStats()
+        rc = bdda.lib().bdda_solve(op.handle, ct.byref(opts), ct.cast(Dh.data_ptr(), ct.POINTER(ct.c_double)),
+                                   ct.cast(Bh.data_ptr(), ct.POINTER(ct.c_double)), n,
+                                   ct.cast(Xh.data_ptr(), ct.POINTER(ct.c_double)), n, L, ct.byref(s))
+        if rc != 0:
+            raise RuntimeError(bdda.lib().bdda_last_error().decode())
+
+    e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = total_rhs / e2e_s
+
+    # ---- plain FP64 path and reference-semantics iteration count ----
+    fp64 = None
+    ref_iters = None
+    if not a.no_fp64:
+        o64 = bdda.solve_opts(a.solver, jacobi=True, precision=bdda.SOLVE_FP64, true_tol=1e-8, itermax=3000)
+        s64 = bdda.solve_device(op, diag_d.data_ptr(), B_d.data_ptr(), n, X_d.data_ptr(), n, L, o64,
+                                stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        s64 = bdda.solve_device(op, diag_d.data_ptr(), B_d.data_ptr(), n, X_d.data_ptr(), n, L, o64,
+                                stream=stream.cuda_stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = ev0.elapsed_time(ev1)
+        fp64 = {"value": L / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64, "iterations": s64["iterations"],
+                "true_res_max": s64["true_res_max"]}
+        oref = bdda.solve_opts(a.solver, jacobi=True, precision=bdda.SOLVE_FP64, tol=1e-8, itermax=3000)
+        sref = bdda.solve_device(op, diag_d.data_ptr(), B_d.data_ptr(), n, X_d.data_ptr(), n, L, oref,
+                                 stream=stream.cuda_stream)
+        ref_iters = sref["iterations"]
+
+    # ---- CPU baseline (rank 0, N=1) ----
+    cpu = None
+    if rank == 0 and ws == 1 and not a.no_cpu:
+        threads = os.cpu_count() or 1
+        t_mvp, t_init, M = cpu_reference_sample(prob, L, threads)
+        it = ref_iters or REF_ITERS_DEFAULT
+        cpu = {"value": L / (it * t_mvp), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"one block MVP (L={L}) of the reference's 1-D MBT FFT algorithm (FFT length {M}, scipy "
+                         f"pocketfft standing in for FFTW, threads over RHS) took {t_mvp:.2f} s; extrapolated by "
+                         f"{it} COCG-RQ-Jacobi iterations; Krylov block algebra not counted"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+                "warmup": max(3, a.warmup), "ms_per_step": t_ms / a.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FFT-MVP, Krylov) + c128 (refinement)",
+                "data": "synthetic (seeded lattice aggregates)", "config": workload_config(a, prob.n, P),
+                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                             "bytes_per_launch": byte_model[dom], "ms_per_launch": per_launch_ms,
+                             "mvp_c64_ms": mvp_ms, "mvp_c64_GBs": mvp_gbs, "mvp_c64_bytes": float(np.sum(mvp32))},
+                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(Bh.numel() * 16 + Dh.numel() * 16),
+                        "d2h_bytes_per_step": int(Xh.numel() * 16)},
+                "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu,
+                "fp64_path": fp64, "mixed_vs_fp64": (value / ws) / fp64["value"] if fp64 else None,
+                "solve": {"iterations_per_step": iters, "true_res_max": res_max,
+                          "ref_semantics_iterations": ref_iters, "nlines": nlines},
+                "kernels_ms": {k: round(v["ms"], 3) for k, v in ks.items() if v["launches"]},
+                "kernels_launches": {k: v["launches"] for k, v in ks.items() if v["launches"]}}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_ours(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -23,14 +23,16 @@ PREC_FP64, PREC_FP32 = 1, 2
 SOLVER_COCG_RQ, SOLVER_BICGSTAB, SOLVER_BICGGR = 0, 1, 2
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 SOLVERS = {"cocg_rq": SOLVER_COCG_RQ, "bicgstab": SOLVER_BICGSTAB, "bicggr": SOLVER_BICGGR}
-KERNEL_NAMES = ["passA", "passB", "passC", "passD", "passE", "gram", "update", "small", "other"]
+KERNEL_NAMES = ["passA_c64", "passB_c64", "passC_c64", "passD_c64", "passE_c64",
+                "passA_c128", "passB_c128", "passC_c128", "passD_c128", "passE_c128",
+                "gram", "update", "small", "other"]
 
 # every symbol include/bdda.h declares
 EXPORTS = [
     "bdda_op_create", "bdda_op_destroy", "bdda_op_set_dipoles", "bdda_op_info", "bdda_mbt_fft_mvp",
     "bdda_op_mvp_device", "bdda_solve_opts_default", "bdda_solve_device", "bdda_solve", "bdda_qr_reduced",
     "bdda_mie_a1b1", "bdda_aggregate", "bdda_incident_fields", "bdda_cross_sections", "bdda_op_set_timing",
-    "bdda_op_kernel_stats", "bdda_last_error",
+    "bdda_op_kernel_stats", "bdda_last_error", "bdda_op_mvp_bytes", "bdda_host_fft_line",
 ]
 
 
@@ -87,10 +89,11 @@ def lib(build_if_missing: bool = False):
     L.bdda_aggregate.argtypes = [ct.c_int, ct.c_double, ct.c_double, ct.c_ulonglong, ip, ip]
     L.bdda_incident_fields.argtypes = [ip, ct.c_double, ip, ct.c_int, ct.c_double, ct.c_int, dp, dp, dp, ct.c_int]
     L.bdda_cross_sections.argtypes = [ct.c_double, dp, dp, ct.c_int, dp, ct.c_int, ct.c_int, ct.c_int, dp]
+    L.bdda_op_mvp_bytes.argtypes = [vp, ct.c_int, ct.c_int, ct.c_int, ct.c_int, dp]
     L.bdda_op_set_timing.argtypes = [vp, ct.c_int]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
     L.bdda_last_error.restype = ct.c_char_p
-    L.bdda_host_fft_line.argtypes = [ct.c_int, ct.c_int, ct.c_int, dp, ip]
+    L.bdda_host_fft_line.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int, dp, ip]
     _LIB = L
     return L
 
@@ -156,7 +159,7 @@ class Operator:
 
     def info(self):
         P = np.zeros(3, np.int32)
-        nocc, nl = ct.c_int(), ct.c_int()
+        nocc, nl = ct.c_int(), ct.c_int()  # nl: occupied (y, z-tile) tiles
         _check(lib().bdda_op_info(self._h, _iptr(P), ct.byref(nocc), ct.byref(nl)))
         return tuple(int(v) for v in P), nocc.value, nl.value
 
@@ -172,6 +175,12 @@ class Operator:
         _check(lib().bdda_op_mvp_device(self._h, prec, ct.c_void_p(x), ldx, ct.c_void_p(y), ldy, L,
                                         ct.c_void_p(diag) if diag else None, ct.c_void_p(jpre) if jpre else None,
                                         ct.c_void_p(stream) if stream else None))
+
+    def mvp_bytes(self, L, prec=PREC_FP32, with_diag=True, with_jpre=True):
+        """Algorithmic HBM bytes of one block MVP, per pass (A..E)."""
+        b = np.zeros(5)
+        _check(lib().bdda_op_mvp_bytes(self._h, prec, int(L), int(with_diag), int(with_jpre), _dptr(b)))
+        return b
 
     def set_timing(self, on=True):
         _check(lib().bdda_op_set_timing(self._h, 1 if on else 0))
@@ -282,11 +291,11 @@ def cross_sections(k, alpha0, E, P):
     return out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy()
 
 
-def host_fft_line(x, inverse=False, prec=1):
+def host_fft_line(x, inverse=False, prec=1, nvalid=0):
     """Run the device FFT core on the CPU (unit tests).  Returns (y, radices)."""
     a = np.ascontiguousarray(x, dtype=np.complex128).copy()
     rad = np.zeros(16, np.int32)
-    nst = lib().bdda_host_fft_line(int(a.size), 1 if inverse else 0, int(prec), _dptr(a), _iptr(rad))
+    nst = lib().bdda_host_fft_line(int(a.size), 1 if inverse else 0, int(prec), int(nvalid), _dptr(a), _iptr(rad))
     if nst < 0:
         raise BddaError(ERR_INVALID, "unsupported FFT length")
     return a, [int(v) for v in rad[:nst]]

@@ -39,11 +39,19 @@ template <typename C> BDDA_HD C czero() { return cmake(decltype(C::x)(0), declty
 constexpr int kMaxLine = 512;   // longest line one warp transforms
 constexpr int kMaxStages = 16;
 
-// Radix schedule of one axis: N = prod(radix[0..nst)).
+// Radix schedule of one axis: N = prod(radix[0..nst)), with the per-stage
+// constants of the in-place DIF/DIT transform precomputed on the host:
+// stage s works on blocks of Ls[s] = N / (radix[0] ... radix[s-1]) points,
+// M[s] = Ls[s] / radix[s], twiddle stride N / Ls[s]; invM[s] = 1/M[s] lets a
+// lane split its butterfly index t into (t / M, t % M) without an integer
+// division (exact for t < 2^12).
 struct AxisPlan {
   int N;
   int nst;
   int radix[kMaxStages];
+  int M[kMaxStages];
+  int tstride[kMaxStages];
+  float invM[kMaxStages];
 };
 
 }  // namespace bdda

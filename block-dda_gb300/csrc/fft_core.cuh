@@ -15,8 +15,9 @@
 // produced by the same forward transform, so the pointwise product pairs
 // matching (permuted) frequencies and the inverse restores natural order.
 // Each butterfly reads and writes the same positions, so a stage needs no
-// register staging and only one buffer; lanes take consecutive n1
-// (stride-1, bank-conflict free while Ms >= 32).
+// register staging and only one buffer; lanes take consecutive n1.  Lines
+// are stored with a 128-byte skew (skw) so that the strided accesses of the
+// last stages do not collide in shared-memory banks.
 //
 // Twiddle table (per axis, global memory, read through L1):
 //   tw[t] = exp(-2 pi i t / N), t in [0, N), computed in FP64 on the host.
@@ -130,18 +131,32 @@ template <int R, bool INV, typename C> BDDA_FFT_FN void dft(C* v) {
   else dft8<INV>(v);
 }
 
+// ---- shared-memory line layout ---------------------------------------------
+// Element i of a line lives at skw(i) = i + i / (128 bytes / sizeof(C)): one
+// pad element per 128 bytes, so the stride-R accesses of the last stages (and
+// the transposed tile loads) spread over all banks.
+template <typename C> BDDA_FFT_FN int skw(int i) { return i + (i >> (sizeof(C) == 8 ? 4 : 3)); }
+// Shared-memory elements one line of n points occupies (rounded to 16 bytes).
+template <typename C> BDDA_HD int line_words(int n) { return ((n + (n >> (sizeof(C) == 8 ? 4 : 3)) + 1) + 1) & ~1; }
+
 // ---- one in-place stage, one warp -----------------------------------------
+// nvalid < N (forward first stage only): inputs at positions >= nvalid are
+// known zeros and are not read (zero padding needs no shared-memory fill).
 template <int R, bool INV, typename C>
-BDDA_FFT_FN void warp_stage(C* __restrict__ s, const C* __restrict__ tw, int N, int Ls, int lane, int lanes) {
-  const int M = Ls / R;
+BDDA_FFT_FN void warp_stage(C* __restrict__ s, const C* __restrict__ tw, int M, int tstride, float invM, int N,
+                            int lane, int lanes, int nvalid) {
   const int nb = N / R;
-  const int tstride = N / Ls;
+  const int Ls = M * R;
   for (int t = lane; t < nb; t += lanes) {
-    const int b = t / M, n1 = t - b * M;
-    C* base = s + b * Ls + n1;
+    const int b = (int)(((float)t + 0.5f) * invM);
+    const int n1 = t - b * M;
+    const int base = b * Ls + n1;
     C v[R];
 #pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = base[i * M];
+    for (int i = 0; i < R; ++i) {
+      if (nvalid < N) v[i] = (n1 + i * M < nvalid) ? s[skw<C>(base + i * M)] : czero<C>();
+      else v[i] = s[skw<C>(base + i * M)];
+    }
     if (!INV) {
       dft<R, false>(v);
       if (n1 != 0) {
@@ -158,40 +173,35 @@ BDDA_FFT_FN void warp_stage(C* __restrict__ s, const C* __restrict__ tw, int N, 
       dft<R, true>(v);
     }
 #pragma unroll
-    for (int i = 0; i < R; ++i) base[i * M] = v[i];
+    for (int i = 0; i < R; ++i) s[skw<C>(base + i * M)] = v[i];
   }
   BDDA_SYNCWARP();
 }
 
 template <bool INV, typename C>
-BDDA_FFT_FN void warp_stage_dispatch(int R, C* s, const C* tw, int N, int Ls, int lane, int lanes) {
-  switch (R) {
-    case 2: warp_stage<2, INV>(s, tw, N, Ls, lane, lanes); break;
-    case 3: warp_stage<3, INV>(s, tw, N, Ls, lane, lanes); break;
-    case 4: warp_stage<4, INV>(s, tw, N, Ls, lane, lanes); break;
-    case 5: warp_stage<5, INV>(s, tw, N, Ls, lane, lanes); break;
-    default: warp_stage<8, INV>(s, tw, N, Ls, lane, lanes); break;
+BDDA_FFT_FN void warp_stage_dispatch(const AxisPlan& p, int st, C* s, const C* tw, int lane, int lanes, int nvalid) {
+  const int M = p.M[st], ts = p.tstride[st];
+  const float iM = p.invM[st];
+  switch (p.radix[st]) {
+    case 2: warp_stage<2, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 3: warp_stage<3, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 4: warp_stage<4, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 5: warp_stage<5, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    default: warp_stage<8, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
   }
 }
 
 // Full in-place transform of one line by one warp.
-// INV = false: natural -> digit-reversed (DIF).  INV = true: digit-reversed -> natural (DIT).
+// INV = false: natural -> digit-reversed (DIF); only the first nvalid inputs
+// are read (the rest are taken as zero).  INV = true: digit-reversed ->
+// natural (DIT), unnormalised.
 template <bool INV, typename C>
-BDDA_FFT_FN void warp_fft(C* __restrict__ s, const C* __restrict__ tw, const AxisPlan& p, int lane, int lanes = 32) {
+BDDA_FFT_FN void warp_fft(C* __restrict__ s, const C* __restrict__ tw, const AxisPlan& p, int lane, int lanes = 32,
+                          int nvalid = 1 << 30) {
   if (!INV) {
-    int Ls = p.N;
-    for (int st = 0; st < p.nst; ++st) {
-      const int R = p.radix[st];
-      warp_stage_dispatch<false>(R, s, tw, p.N, Ls, lane, lanes);
-      Ls /= R;
-    }
+    for (int st = 0; st < p.nst; ++st) warp_stage_dispatch<false>(p, st, s, tw, lane, lanes, st == 0 ? nvalid : p.N);
   } else {
-    int Ls = p.radix[p.nst - 1];
-    for (int st = p.nst - 1; st >= 0; --st) {
-      const int R = p.radix[st];
-      warp_stage_dispatch<true>(R, s, tw, p.N, Ls, lane, lanes);
-      if (st > 0) Ls *= p.radix[st - 1];
-    }
+    for (int st = p.nst - 1; st >= 0; --st) warp_stage_dispatch<true>(p, st, s, tw, lane, lanes, p.N);
   }
 }
 

@@ -69,69 +69,59 @@ __global__ void k_green_eval(double2* __restrict__ g, int nx, int ny, int nz, in
 }
 
 // In-place FFT of contiguous lines (length p.N), one warp per line.
-template <bool INV>
-__global__ void __launch_bounds__(kLineWarps * 32)
+constexpr int kInitWarps = 8;
+__global__ void __launch_bounds__(kInitWarps * 32)
 k_fft_contig(double2* __restrict__ data, size_t nlines, AxisPlan p, const double2* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lw = line_words<double2>(p.N);
   double2* smem = reinterpret_cast<double2*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const size_t line = (size_t)blockIdx.x * kLineWarps + warp;
+  const size_t line = (size_t)blockIdx.x * kInitWarps + warp;
   if (line >= nlines) return;
-  double2* s = smem + warp * p.N;
+  double2* s = smem + warp * lw;
   double2* d = data + line * p.N;
-  for (int i = lane; i < p.N; i += 32) s[i] = d[i];
+  for (int i = lane; i < p.N; i += 32) s[skw<double2>(i)] = d[i];
   __syncwarp();
-  warp_fft<INV>(s, tw, p, lane);
-  for (int i = lane; i < p.N; i += 32) d[i] = s[i];
+  warp_fft<false>(s, tw, p, lane);
+  for (int i = lane; i < p.N; i += 32) d[i] = s[skw<double2>(i)];
 }
 
-// In-place FFT along the middle index of data[A][N][Cc], tiles of TS columns.
-constexpr int kStridedTile = 8;
-template <bool INV>
-__global__ void __launch_bounds__(kStridedTile * 32)
+// In-place forward FFT along the middle index of data[A][N][Cc], 8 columns per CTA.
+__global__ void __launch_bounds__(kInitWarps * 32)
 k_fft_strided(double2* __restrict__ data, int N, size_t Cc, AxisPlan p, const double2* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lw = line_words<double2>(N);
   double2* smem = reinterpret_cast<double2*>(smem_raw);
-  const int lds = N | 1;
-  const size_t c0 = (size_t)blockIdx.x * kStridedTile;
+  const size_t c0 = (size_t)blockIdx.x * kInitWarps;
   double2* base = data + (size_t)blockIdx.y * N * Cc;
   const int tid = threadIdx.x;
-  for (int idx = tid; idx < N * kStridedTile; idx += kStridedTile * 32) {
-    const int w = idx % kStridedTile, i = idx / kStridedTile;
+  for (int idx = tid; idx < N * kInitWarps; idx += kInitWarps * 32) {
+    const int w = idx % kInitWarps, i = idx / kInitWarps;
     const size_t c = c0 + w;
-    smem[w * lds + i] = (c < Cc) ? base[(size_t)i * Cc + c] : make_double2(0.0, 0.0);
+    smem[w * lw + skw<double2>(i)] = (c < Cc) ? base[(size_t)i * Cc + c] : make_double2(0.0, 0.0);
   }
   __syncthreads();
-  warp_fft<INV>(smem + (tid >> 5) * lds, tw, p, tid & 31);
+  warp_fft<false>(smem + (tid >> 5) * lw, tw, p, tid & 31);
   __syncthreads();
-  for (int idx = tid; idx < N * kStridedTile; idx += kStridedTile * 32) {
-    const int w = idx % kStridedTile, i = idx / kStridedTile;
+  for (int idx = tid; idx < N * kInitWarps; idx += kInitWarps * 32) {
+    const int w = idx % kInitWarps, i = idx / kInitWarps;
     const size_t c = c0 + w;
-    if (c < Cc) base[(size_t)i * Cc + c] = smem[w * lds + i];
+    if (c < Cc) base[(size_t)i * Cc + c] = smem[w * lw + skw<double2>(i)];
   }
 }
 
-// g[comp][qx][y][z] / Ng  ->  ghat[y][zt][comp][qx][w]   (TZ-wide z tiles)
-template <typename C, int TZ>
-__global__ void k_green_tile(const double2* __restrict__ g, C* __restrict__ out, int Px, int Py, int Pz, double scale) {
-  const int nzt = (Pz + TZ - 1) / TZ;
-  const size_t total = (size_t)Py * nzt * 6 * Px * TZ;
+// g[comp][qx][qy][qz] / Ng  ->  ghat[qx][qy][comp][qz]
+template <typename C>
+__global__ void k_green_pack(const double2* __restrict__ g, C* __restrict__ out, int Px, int Py, int Pz, double scale) {
   const size_t ng = (size_t)Px * Py * Pz;
+  const size_t total = 6 * ng;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
-    const int w = (int)(idx % TZ);
-    size_t t = idx / TZ;
-    const int qx = (int)(t % Px); t /= Px;
-    const int comp = (int)(t % 6); t /= 6;
-    const int zt = (int)(t % nzt);
-    const int y = (int)(t / nzt);
-    const int z = zt * TZ + w;
-    double2 v = make_double2(0.0, 0.0);
-    if (z < Pz) {
-      v = g[(size_t)comp * ng + ((size_t)qx * Py + y) * Pz + z];
-      v.x *= scale;
-      v.y *= scale;
-    }
-    out[idx] = cmake((decltype(C::x))v.x, (decltype(C::x))v.y);
+    const int qz = (int)(idx % Pz);
+    const size_t t = idx / Pz;
+    const int comp = (int)(t % 6);
+    const size_t line = t / 6;  // qx * Py + qy
+    double2 v = g[(size_t)comp * ng + line * Pz + qz];
+    out[idx] = cmake((decltype(C::x))(v.x * scale), (decltype(C::x))(v.y * scale));
   }
 }
 
@@ -143,35 +133,32 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
   const int Px = g.Px, Py = g.Py, Pz = g.Pz;
   const size_t ng = (size_t)Px * Py * Pz;
   cudaError_t e;
+  const int maxsm = kInitWarps * line_words<double2>(kMaxLine) * (int)sizeof(double2);
+  if ((e = cudaFuncSetAttribute(k_fft_contig, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_fft_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm)) != cudaSuccess) return e;
   k_green_eval<<<1216, 256, 0, st>>>(work, g.nx, g.ny, g.nz, Px, Py, Pz, lf, k_re, k_im);
   // z lines (contiguous)
   {
-    size_t nlines = 6 * (size_t)Px * Py;
-    int sm = kLineWarps * Pz * (int)sizeof(double2);
-    e = cudaFuncSetAttribute(k_fft_contig<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kLineWarps * kMaxLine * (int)sizeof(double2));
-    if (e != cudaSuccess) return e;
-    k_fft_contig<false><<<(unsigned)((nlines + kLineWarps - 1) / kLineWarps), kLineWarps * 32, sm, st>>>(work, nlines, g.pz, twz);
+    const size_t nlines = 6 * (size_t)Px * Py;
+    const int sm = kInitWarps * line_words<double2>(Pz) * (int)sizeof(double2);
+    k_fft_contig<<<(unsigned)((nlines + kInitWarps - 1) / kInitWarps), kInitWarps * 32, sm, st>>>(work, nlines, g.pz, twz);
   }
-  e = cudaFuncSetAttribute(k_fft_strided<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kStridedTile * (kMaxLine | 1) * (int)sizeof(double2));
-  if (e != cudaSuccess) return e;
   // y lines: data[6*Px][Py][Pz]
   {
-    dim3 grid((unsigned)((Pz + kStridedTile - 1) / kStridedTile), 6 * Px);
-    int sm = kStridedTile * (Py | 1) * (int)sizeof(double2);
-    k_fft_strided<false><<<grid, kStridedTile * 32, sm, st>>>(work, Py, (size_t)Pz, g.py, twy);
+    dim3 grid((unsigned)((Pz + kInitWarps - 1) / kInitWarps), 6 * Px);
+    const int sm = kInitWarps * line_words<double2>(Py) * (int)sizeof(double2);
+    k_fft_strided<<<grid, kInitWarps * 32, sm, st>>>(work, Py, (size_t)Pz, g.py, twy);
   }
   // x lines: data[6][Px][Py*Pz]
   {
-    size_t cc = (size_t)Py * Pz;
-    dim3 grid((unsigned)((cc + kStridedTile - 1) / kStridedTile), 6);
-    int sm = kStridedTile * (Px | 1) * (int)sizeof(double2);
-    k_fft_strided<false><<<grid, kStridedTile * 32, sm, st>>>(work, Px, cc, g.px, twx);
+    const size_t cc = (size_t)Py * Pz;
+    dim3 grid((unsigned)((cc + kInitWarps - 1) / kInitWarps), 6);
+    const int sm = kInitWarps * line_words<double2>(Px) * (int)sizeof(double2);
+    k_fft_strided<<<grid, kInitWarps * 32, sm, st>>>(work, Px, cc, g.px, twx);
   }
   const double scale = 1.0 / (double)ng;
-  if (ghat_d) k_green_tile<double2, TileCfg<double>::TZ><<<2432, 256, 0, st>>>(work, ghat_d, Px, Py, Pz, scale);
-  if (ghat_f) k_green_tile<float2, TileCfg<float>::TZ><<<2432, 256, 0, st>>>(work, ghat_f, Px, Py, Pz, scale);
+  if (ghat_d) k_green_pack<double2><<<2432, 256, 0, st>>>(work, ghat_d, Px, Py, Pz, scale);
+  if (ghat_f) k_green_pack<float2><<<2432, 256, 0, st>>>(work, ghat_f, Px, Py, Pz, scale);
   return cudaGetLastError();
 }
 

@@ -8,23 +8,24 @@
 
 namespace bdda {
 
-// Warps (one line each) per CTA in the contiguous-axis passes A and E.
-constexpr int kLineWarps = 8;
-
-// z-tile width of the strided passes: 8 x c64 = 64 B, 4 x c128 = 64 B rows.
-template <typename T> struct TileCfg;
-template <> struct TileCfg<float> { static constexpr int TZ = 8; };
-template <> struct TileCfg<double> { static constexpr int TZ = 4; };
+// z-tile width of the strided passes (8 lines per CTA, one warp each):
+// rows of 8 x c64 = 64 B or 8 x c128 = 128 B.
+constexpr int kTZ = 8;
+constexpr int kTileThreads = kTZ * 32;
+// Warps per CTA of the fused z pass (one (x, y, rhs) task each).
+constexpr int kZWarps = 8;
 
 // Geometry shared by both precisions (device pointers).
 struct MvpGeom {
   int nx, ny, nz;
   int Px, Py, Pz;
   AxisPlan px, py, pz;
-  int nlines;                 // lattice lines (x, y) that hold >= 1 dipole
-  const int* occ;             // [nx*ny*nz] dipole index or -1
-  const int* lines;           // [nlines]  x*ny + y
-  const unsigned char* lmask; // [nx*ny]
+  int nzt;                     // ceil(nz / kTZ)
+  int ntiles;                  // (y, z-tile) pairs holding >= 1 dipole
+  long long tile_rows;         // sum over those tiles of their valid z count
+  const int* occ;              // [nx*ny*nz] dipole index or -1
+  const int* tiles;            // [ntiles]  y*nzt + zt
+  const unsigned char* tmask;  // [ny*nzt]  1 for those tiles
 };
 
 // Precision-specific tables (device pointers).
@@ -33,11 +34,14 @@ template <typename T> struct MvpPrec {
   const C* twx;
   const C* twy;
   const C* twz;
-  const C* ghat;  // [Py][ceil(Pz/TZ)][6][Px][TZ], already divided by Px*Py*Pz
+  const C* ghat;  // [Px][Py][6][Pz] (digit-reversed frequencies), divided by Px*Py*Pz
 };
 
+// Timed kernel classes: the five MVP passes per precision (FP32 first), then
+// the Krylov block kernels.
 enum KernelId {
-  kPassA = 0, kPassB, kPassC, kPassD, kPassE,
+  kPassA = 0, kPassB, kPassC, kPassD, kPassE,            // complex FP32 MVP
+  kPassA64, kPassB64, kPassC64, kPassD64, kPassE64,       // complex FP64 MVP
   kGram, kUpdate, kSmall, kOther,
   kNumKernelIds
 };
@@ -56,6 +60,7 @@ struct KernelTimer {
     if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
     cudaEvent_t e; cudaEventCreate(&e); return e;
   }
+  void count(int id, int k = 1) { launches[id] += k; }
   void begin(int id, cudaStream_t st) {
     launches[id]++;
     if (!enabled) return;
@@ -87,6 +92,10 @@ struct KernelTimer {
   }
 };
 
+// Workspace elements (complex T) the MVP needs for L right-hand sides.
+inline size_t mvp_t1_elems(const MvpGeom& g, int L) { return 3ull * L * g.Px * g.ny * g.nz; }
+inline size_t mvp_t2_elems(const MvpGeom& g, int L) { return 3ull * L * g.Px * g.Py * g.nz; }
+
 template <typename T>
 cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typename cplx<T>::type* x, int ldx,
                              typename cplx<T>::type* y, int ldy, int L,
@@ -94,11 +103,11 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
                              typename cplx<T>::type* t1, typename cplx<T>::type* t2,
                              cudaStream_t st, KernelTimer* timer, const int* done = nullptr);
 
-template <typename T> cudaError_t configure_mvp_kernels(int max_px);
+template <typename T> cudaError_t configure_mvp_kernels();
 
-// Green tensor: build Ghat (FP64 evaluation + FP64 3-D FFT) for both layouts.
-// ghat_d: c128 tiles for TZ=TileCfg<double>::TZ; ghat_f: c64 tiles for
-// TZ=TileCfg<float>::TZ (either may be null).  work: c128 [6*Px*Py*Pz].
+// Green tensor: build Ghat (FP64 evaluation + FP64 3-D FFT), layout
+// [Px][Py][6][Pz], for either precision (null pointers skipped).
+// work: c128 [6*Px*Py*Pz].
 cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_im,
                             const double2* twx, const double2* twy, const double2* twz,
                             double2* work, double2* ghat_d, float2* ghat_f, cudaStream_t st);

@@ -10,20 +10,28 @@
 // HBM layouts (element = complex T):
 //   x, y   : column-major (rows 3*m + c, column l, leading dimension ld) --
 //            the reference's Eigen layout of S / AS.
-//   occ    : int32 [nx*ny*nz], dipole index of a lattice site or -1.
-//   lines  : int32 list of (x*ny + y) lattice lines holding >= 1 dipole.
-//   lmask  : uint8 [nx*ny], 1 for such lines.
-//   T1     : [3L][nx*ny][Pz]   after the z pass (only lines in `lines` valid)
-//   T2     : [3L][nx][Py][Pz]  after the y pass; the x pass works in place
-//   Ghat   : [Py][ceil(Pz/TZ)][6][Px][TZ] -- Ghat/Ng, tile-contiguous for the
-//            x pass, components (xx, xy, xz, yy, yz, zz).
+//   occ    : int32 [nx][ny][nz], dipole index of a lattice site or -1.
+//   tiles  : int32 list of (y, z-tile) pairs (y*nzt + zt, 8-wide z tiles)
+//            holding >= 1 dipole; tmask [ny][nzt] marks them.
+//   T1     : [3L][Px][ny][nz]  after the x pass (only rows of listed tiles valid)
+//   T2     : [3L][Px][Py][nz]  after the y pass; the z pass works in place
+//   Ghat   : [Px][Py][6][Pz]  Ghat / (Px Py Pz), digit-reversed frequencies,
+//            components (xx, xy, xz, yy, yz, zz).
 //
-// Pass order (forward z, y, x; inverse x, y, z), each a separate kernel:
-//   A  z-forward, input pruned to occupied sites           x  -> T1
-//   B  y-forward, input pruned to ny rows and to non-empty lines   T1 -> T2
-//   C  x-forward, Ghat product, x-inverse, pruned to nx    T2 -> T2 (in place)
-//   D  y-inverse, output pruned to ny rows of non-empty lines      T2 -> T1
-//   E  z-inverse, gather at occupied sites, + diag o x, o jpre     T1 -> y
+// Passes (forward x, y; fused z; inverse y, x), each one kernel:
+//   A  x-forward, gathers the occupied sites of a (y, z-tile), loops over
+//      the fields; input pruned to nx                       x  -> T1
+//   B  y-forward, rows of empty tiles never read, pruned to ny     T1 -> T2
+//   C  z-forward (pruned to nz), 3x3 symmetric Ghat product, z-inverse,
+//      output truncated to nz; one warp per (x, y, rhs) holds the three
+//      components, no block barrier                          T2 -> T2
+//   D  y-inverse, rows y < ny of listed tiles written        T2 -> T1
+//   E  x-inverse, scatter to occupied sites, + diag o x, o jpre    T1 -> y
+// The strided passes stage 8 z-columns per CTA; B, D and E prefetch the next
+// tile with cp.async (zero-filled outside the box) while the current one is
+// transformed.
+#include <algorithm>
+
 #include "fft_core.cuh"
 #include "mvp.hpp"
 
@@ -31,192 +39,263 @@ namespace bdda {
 
 namespace {
 
-__host__ __device__ __forceinline__ int odd_stride(int n) { return n | 1; }
+// ---- cp.async helpers (LDGSTS: global -> shared without registers) --------
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  const int sz = valid ? BYTES : 0;  // src-size 0: nothing read, destination zero-filled
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ bool skip(const int* done) { return done && *(volatile const int*)done; }
 
 // ---------------------------------------------------------------- pass A
+// One CTA per listed (y, z-tile): warp w owns z = z0 + w; loops over fields.
 template <typename T>
-__global__ void __launch_bounds__(kLineWarps * 32)
-k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield,
-         const int* __restrict__ occ, const int* __restrict__ lines, int nz, int nxy,
-         AxisPlan pz, const typename cplx<T>::type* __restrict__ twz,
-         typename cplx<T>::type* __restrict__ t1, const int* done) {
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, const int* __restrict__ occ,
+         const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, AxisPlan px,
+         const typename cplx<T>::type* __restrict__ twx, typename cplx<T>::type* __restrict__ t1, const int* done) {
   using C = typename cplx<T>::type;
-  if (done && *(volatile const int*)done) return;
+  if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* smem = reinterpret_cast<C*>(smem_raw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int field = blockIdx.y * kLineWarps + warp;
-  if (field >= nfield) return;
-  const int line = lines[blockIdx.x];
-  const int l = field / 3, c = field - 3 * (field / 3);
-  C* s = smem + warp * pz.N;
-  const C* xc = x + (size_t)l * ldx + c;
-  for (int z = lane; z < pz.N; z += 32) {
-    C v = czero<C>();
-    if (z < nz) {
-      const int m = occ[(size_t)line * nz + z];
-      if (m >= 0) v = xc[3 * (size_t)m];
-    }
-    s[z] = v;
+  const int Px = px.N;
+  const int lw = line_words<C>(Px);
+  C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
+  int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
+  const int tile = tiles[blockIdx.x];
+  const int y = tile / nzt, z0 = (tile - y * nzt) * kTZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
+    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
+    socc[idx] = z < nz ? occ[((size_t)xi * ny + y) * nz + z] : -1;
   }
-  __syncwarp();
-  warp_fft<false>(s, twz, pz, lane);
-  C* out = t1 + ((size_t)field * nxy + line) * pz.N;
-  for (int z = lane; z < pz.N; z += 32) out[z] = s[z];
+  __syncthreads();
+  const size_t rowstride = (size_t)ny * nz;  // T1 stride between x rows
+  int l = 0, c = 0;
+  for (int f = 0; f < nfield; ++f) {
+    C* line = lines + ((f & 1) * kTZ + warp) * lw;
+    const C* xc = x + (size_t)l * ldx + c;
+    for (int xi = lane; xi < nx; xi += 32) {
+      const int m = socc[xi * kTZ + warp];
+      line[skw<C>(xi)] = m >= 0 ? xc[3 * (size_t)m] : czero<C>();
+    }
+    __syncwarp();
+    warp_fft<false>(line, twx, px, lane, 32, nx);
+    __syncthreads();
+    C* out = t1 + (size_t)f * Px * rowstride + (size_t)y * nz + z0;
+    const C* lb = lines + (f & 1) * kTZ * lw;
+    for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
+      const int w = idx & 7, q = idx >> 3;
+      if (z0 + w < nz) out[(size_t)q * rowstride + w] = lb[w * lw + skw<C>(q)];
+    }
+    if (++c == 3) { c = 0; ++l; }
+  }
 }
 
 // ---------------------------------------------------------------- pass B / D
-// B: T1 -> T2 forward along y.  D: T2 -> T1 inverse along y.
+// Persistent CTAs over tasks (field, x, z-tile); lines along y.
+// B: T1[f][q][y<ny][z] -> T2[f][q][Py][z]   (rows of empty tiles zero-filled)
+// D: T2[f][q][Py][z]   -> T1[f][q][y<ny][z] (rows of listed tiles only)
 template <typename T, bool INV>
-__global__ void __launch_bounds__(TileCfg<T>::TZ * 32)
+__global__ void __launch_bounds__(kTileThreads)
 k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type* __restrict__ dst,
-         const unsigned char* __restrict__ lmask, int nx, int ny, int Pz,
-         AxisPlan py, const typename cplx<T>::type* __restrict__ twy, const int* done) {
+         const unsigned char* __restrict__ tmask, int ny, int nz, int nzt, int ntask, AxisPlan py,
+         const typename cplx<T>::type* __restrict__ twy, const int* done) {
   using C = typename cplx<T>::type;
-  if (done && *(volatile const int*)done) return;
-  constexpr int TZ = TileCfg<T>::TZ;
+  if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* smem = reinterpret_cast<C*>(smem_raw);
   const int Py = py.N;
-  const int lds = odd_stride(Py);
-  const int z0 = blockIdx.x * TZ;
-  const int xi = blockIdx.y;
-  const size_t field = blockIdx.z;
-  const int tid = threadIdx.x;
-  const unsigned char* lm = lmask + (size_t)xi * ny;
-  if (!INV) {
-    // rows y < ny from T1[field][xi*ny + y][z], zero elsewhere
-    const C* base = src + ((size_t)field * nx * ny + (size_t)xi * ny) * Pz;
-    for (int idx = tid; idx < Py * TZ; idx += TZ * 32) {
-      const int w = idx % TZ, y = idx / TZ, z = z0 + w;
-      C v = czero<C>();
-      if (y < ny && z < Pz && lm[y]) v = base[(size_t)y * Pz + z];
-      smem[w * lds + y] = v;
+  const int lw = line_words<C>(Py);
+  C* lines = reinterpret_cast<C*>(smem_raw);  // [2][kTZ][lw]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nin = INV ? Py : ny;    // rows read
+  const int nout = INV ? ny : Py;   // rows written
+  const size_t in_rows = (size_t)nin, out_rows = (size_t)nout;
+
+  auto issue = [&](int task, int buf) {
+    const int zt = task % nzt;
+    const int r = task / nzt;  // f * Px + q
+    const int z0 = zt * kTZ;
+    const C* base = src + (size_t)r * in_rows * nz + z0;
+    C* lb = lines + buf * kTZ * lw;
+    for (int idx = tid; idx < nin * kTZ; idx += kTileThreads) {
+      const int w = idx & 7, yy = idx >> 3;
+      bool valid = z0 + w < nz;
+      if (!INV) valid = valid && tmask[yy * nzt + zt];
+      const C* g = valid ? base + (size_t)yy * nz + w : src;
+      cp_async<sizeof(C)>(lb + w * lw + skw<C>(yy), g, valid);
     }
-  } else {
-    const C* base = src + ((size_t)field * nx + xi) * (size_t)Py * Pz;
-    for (int idx = tid; idx < Py * TZ; idx += TZ * 32) {
-      const int w = idx % TZ, y = idx / TZ, z = z0 + w;
-      C v = czero<C>();
-      if (z < Pz) v = base[(size_t)y * Pz + z];
-      smem[w * lds + y] = v;
+    cp_commit();
+  };
+
+  int task = blockIdx.x;
+  if (task < ntask) issue(task, 0);
+  for (int it = 0; task < ntask; ++it, task += gridDim.x) {
+    const int buf = it & 1;
+    const int next = task + gridDim.x;
+    if (next < ntask) {
+      issue(next, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
     }
-  }
-  __syncthreads();
-  const int warp = tid >> 5, lane = tid & 31;
-  warp_fft<INV>(smem + warp * lds, twy, py, lane);
-  __syncthreads();
-  if (!INV) {
-    C* base = dst + ((size_t)field * nx + xi) * (size_t)Py * Pz;
-    for (int idx = tid; idx < Py * TZ; idx += TZ * 32) {
-      const int w = idx % TZ, y = idx / TZ, z = z0 + w;
-      if (z < Pz) base[(size_t)y * Pz + z] = smem[w * lds + y];
+    __syncthreads();
+    C* line = lines + (buf * kTZ + warp) * lw;
+    warp_fft<INV>(line, twy, py, lane, 32, INV ? Py : ny);
+    __syncthreads();
+    const int zt = task % nzt;
+    const int r = task / nzt;
+    const int z0 = zt * kTZ;
+    C* ob = dst + (size_t)r * out_rows * nz + z0;
+    const C* lb = lines + buf * kTZ * lw;
+    for (int idx = tid; idx < nout * kTZ; idx += kTileThreads) {
+      const int w = idx & 7, yy = idx >> 3;
+      if (z0 + w >= nz) continue;
+      if (INV && !tmask[yy * nzt + zt]) continue;
+      ob[(size_t)yy * nz + w] = lb[w * lw + skw<C>(yy)];
     }
-  } else {
-    C* base = dst + ((size_t)field * nx * ny + (size_t)xi * ny) * Pz;
-    for (int idx = tid; idx < ny * TZ; idx += TZ * 32) {
-      const int w = idx % TZ, y = idx / TZ, z = z0 + w;
-      if (z < Pz && lm[y]) base[(size_t)y * Pz + z] = smem[w * lds + y];
-    }
+    __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
   }
 }
 
 // ---------------------------------------------------------------- pass C
+// One warp per task (x = q, y = qy, rhs l): the three component lines along z.
 template <typename T>
-__global__ void __launch_bounds__(3 * TileCfg<T>::TZ * 32)
-k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int nx, int Py, int Pz,
-         AxisPlan px, const typename cplx<T>::type* __restrict__ twx,
-         const typename cplx<T>::type* __restrict__ ghat, const int* done) {
+__global__ void __launch_bounds__(kZWarps * 32)
+k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz, AxisPlan pz,
+         const typename cplx<T>::type* __restrict__ twz, const typename cplx<T>::type* __restrict__ ghat,
+         const int* done) {
   using C = typename cplx<T>::type;
-  if (done && *(volatile const int*)done) return;
-  constexpr int TZ = TileCfg<T>::TZ;
-  constexpr int NT = 3 * TZ * 32;
+  if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* smem = reinterpret_cast<C*>(smem_raw);
-  const int Px = px.N;
-  const int lds = odd_stride(Px);
-  const int zt = blockIdx.x, z0 = zt * TZ;
-  const int y = blockIdx.y;
-  const int nzt = gridDim.x;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const size_t pstride = (size_t)Py * Pz;  // x stride in T2
-  const C* gb = ghat + ((size_t)y * nzt + zt) * 6 * (size_t)Px * TZ;
-  for (int l = 0; l < L; ++l) {
-    // load 3 components x TZ columns, rows x < nx; zero-fill to Px
-    for (int idx = tid; idx < 3 * Px * TZ; idx += NT) {
-      const int w = idx % TZ, t = idx / TZ;
-      const int xi = t % Px, c = t / Px, z = z0 + w;
-      C v = czero<C>();
-      if (xi < nx && z < Pz) v = t2[((size_t)(3 * l + c) * nx + xi) * pstride + (size_t)y * Pz + z];
-      smem[(c * TZ + w) * lds + xi] = v;
-    }
-    __syncthreads();
-    warp_fft<false>(smem + warp * lds, twx, px, lane);
-    __syncthreads();
-    for (int p = tid; p < Px * TZ; p += NT) {
-      const int w = p % TZ, q = p / TZ;
-      C a0 = smem[(0 * TZ + w) * lds + q];
-      C a1 = smem[(1 * TZ + w) * lds + q];
-      C a2 = smem[(2 * TZ + w) * lds + q];
-      const size_t PT = (size_t)Px * TZ;
-      C gxx = gb[0 * PT + p], gxy = gb[1 * PT + p], gxz = gb[2 * PT + p];
-      C gyy = gb[3 * PT + p], gyz = gb[4 * PT + p], gzz = gb[5 * PT + p];
-      C b0 = cadd(cadd(cmul(gxx, a0), cmul(gxy, a1)), cmul(gxz, a2));
-      C b1 = cadd(cadd(cmul(gxy, a0), cmul(gyy, a1)), cmul(gyz, a2));
-      C b2 = cadd(cadd(cmul(gxz, a0), cmul(gyz, a1)), cmul(gzz, a2));
-      smem[(0 * TZ + w) * lds + q] = b0;
-      smem[(1 * TZ + w) * lds + q] = b1;
-      smem[(2 * TZ + w) * lds + q] = b2;
-    }
-    __syncthreads();
-    warp_fft<true>(smem + warp * lds, twx, px, lane);
-    __syncthreads();
-    for (int idx = tid; idx < 3 * nx * TZ; idx += NT) {
-      const int w = idx % TZ, t = idx / TZ;
-      const int xi = t % nx, c = t / nx, z = z0 + w;
-      if (z < Pz) t2[((size_t)(3 * l + c) * nx + xi) * pstride + (size_t)y * Pz + z] = smem[(c * TZ + w) * lds + xi];
-    }
-    __syncthreads();
+  const int Pz = pz.N;
+  const int lw = line_words<C>(Pz);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long task = (long long)blockIdx.x * kZWarps + warp;
+  const long long ntask = (long long)Px * Py * L;
+  if (task >= ntask) return;
+  const int l = (int)(task % L);
+  const long long line = task / L;  // q * Py + qy
+  C* s0 = reinterpret_cast<C*>(smem_raw) + (size_t)warp * 3 * lw;
+  C* s1 = s0 + lw;
+  C* s2 = s1 + lw;
+  const size_t fstride = (size_t)Px * Py * nz;  // between fields
+  C* g0 = t2 + (size_t)(3 * l) * fstride + (size_t)line * nz;
+  for (int z = lane; z < nz; z += 32) {
+    s0[skw<C>(z)] = g0[z];
+    s1[skw<C>(z)] = g0[fstride + z];
+    s2[skw<C>(z)] = g0[2 * fstride + z];
+  }
+  __syncwarp();
+  warp_fft<false>(s0, twz, pz, lane, 32, nz);
+  warp_fft<false>(s1, twz, pz, lane, 32, nz);
+  warp_fft<false>(s2, twz, pz, lane, 32, nz);
+  const C* gl = ghat + (size_t)line * 6 * Pz;
+  for (int p = lane; p < Pz; p += 32) {
+    const int sp = skw<C>(p);
+    const C a0 = s0[sp], a1 = s1[sp], a2 = s2[sp];
+    const C gxx = __ldg(gl + p), gxy = __ldg(gl + Pz + p), gxz = __ldg(gl + 2 * Pz + p);
+    const C gyy = __ldg(gl + 3 * Pz + p), gyz = __ldg(gl + 4 * Pz + p), gzz = __ldg(gl + 5 * Pz + p);
+    s0[sp] = cadd(cadd(cmul(gxx, a0), cmul(gxy, a1)), cmul(gxz, a2));
+    s1[sp] = cadd(cadd(cmul(gxy, a0), cmul(gyy, a1)), cmul(gyz, a2));
+    s2[sp] = cadd(cadd(cmul(gxz, a0), cmul(gyz, a1)), cmul(gzz, a2));
+  }
+  __syncwarp();
+  warp_fft<true>(s0, twz, pz, lane);
+  warp_fft<true>(s1, twz, pz, lane);
+  warp_fft<true>(s2, twz, pz, lane);
+  for (int z = lane; z < nz; z += 32) {
+    g0[z] = s0[skw<C>(z)];
+    g0[fstride + z] = s1[skw<C>(z)];
+    g0[2 * fstride + z] = s2[skw<C>(z)];
   }
 }
 
 // ---------------------------------------------------------------- pass E
+// One CTA per listed (y, z-tile); loops over fields with the next field's
+// tile prefetched by cp.async; scatters the occupied sites.
 template <typename T>
-__global__ void __launch_bounds__(kLineWarps * 32)
-k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int nz, int nxy,
-         const int* __restrict__ occ, const int* __restrict__ lines,
-         AxisPlan pz, const typename cplx<T>::type* __restrict__ twz,
-         const typename cplx<T>::type* __restrict__ x, int ldx,
-         const typename cplx<T>::type* __restrict__ diag,
-         const typename cplx<T>::type* __restrict__ jpre,
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, const int* __restrict__ occ,
+         const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, AxisPlan px,
+         const typename cplx<T>::type* __restrict__ twx, const typename cplx<T>::type* __restrict__ x, int ldx,
+         const typename cplx<T>::type* __restrict__ diag, const typename cplx<T>::type* __restrict__ jpre,
          typename cplx<T>::type* __restrict__ y, int ldy, const int* done) {
   using C = typename cplx<T>::type;
-  if (done && *(volatile const int*)done) return;
+  if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* smem = reinterpret_cast<C*>(smem_raw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int field = blockIdx.y * kLineWarps + warp;
-  if (field >= nfield) return;
-  const int line = lines[blockIdx.x];
-  const int l = field / 3, c = field - 3 * (field / 3);
-  C* s = smem + warp * pz.N;
-  const C* in = t1 + ((size_t)field * nxy + line) * pz.N;
-  for (int z = lane; z < pz.N; z += 32) s[z] = in[z];
-  __syncwarp();
-  warp_fft<true>(s, twz, pz, lane);
-  for (int z = lane; z < nz; z += 32) {
-    const int m = occ[(size_t)line * nz + z];
-    if (m < 0) continue;
-    const size_t r = 3 * (size_t)m + c;
-    C v = s[z];
-    if (diag != nullptr) v = cadd(v, cmul(diag[r], x[(size_t)l * ldx + r]));
-    if (jpre != nullptr) v = cmul(v, jpre[r]);
-    y[(size_t)l * ldy + r] = v;
+  const int Px = px.N;
+  const int lw = line_words<C>(Px);
+  C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
+  int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
+  const int tile = tiles[blockIdx.x];
+  const int yy = tile / nzt, z0 = (tile - yy * nzt) * kTZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const size_t rowstride = (size_t)ny * nz;
+  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
+    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
+    socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
+  }
+  auto issue = [&](int f, int buf) {
+    const C* base = t1 + (size_t)f * Px * rowstride + (size_t)yy * nz + z0;
+    C* lb = lines + buf * kTZ * lw;
+    for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
+      const int w = idx & 7, q = idx >> 3;
+      const bool valid = z0 + w < nz;
+      cp_async<sizeof(C)>(lb + w * lw + skw<C>(q), valid ? base + (size_t)q * rowstride + w : t1, valid);
+    }
+    cp_commit();
+  };
+  issue(0, 0);
+  int l = 0, c = 0;
+  for (int f = 0; f < nfield; ++f) {
+    const int buf = f & 1;
+    if (f + 1 < nfield) {
+      issue(f + 1, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    C* line = lines + (buf * kTZ + warp) * lw;
+    warp_fft<true>(line, twx, px, lane);
+    for (int xi = lane; xi < nx; xi += 32) {
+      const int m = socc[xi * kTZ + warp];
+      if (m < 0) continue;
+      const size_t r = 3 * (size_t)m + c;
+      C v = line[skw<C>(xi)];
+      if (diag != nullptr) v = cadd(v, cmul(diag[r], x[(size_t)l * ldx + r]));
+      if (jpre != nullptr) v = cmul(v, jpre[r]);
+      y[(size_t)l * ldy + r] = v;
+    }
+    __syncthreads();  // buffer 'buf' is the cp.async target of field f + 2
+    if (++c == 3) { c = 0; ++l; }
   }
 }
 
-template <typename T>
-int smem_line_pass(int Pz) { return kLineWarps * Pz * (int)sizeof(typename cplx<T>::type); }
+template <typename T> int smem_tile(int N, int nx) {
+  return 2 * kTZ * line_words<typename cplx<T>::type>(N) * (int)sizeof(typename cplx<T>::type) + nx * kTZ * 4;
+}
+template <typename T> int smem_z(int Pz) {
+  return kZWarps * 3 * line_words<typename cplx<T>::type>(Pz) * (int)sizeof(typename cplx<T>::type);
+}
+
+int num_sms() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
 
 }  // namespace
 
@@ -227,77 +306,53 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
                              const typename cplx<T>::type* diag, const typename cplx<T>::type* jpre,
                              typename cplx<T>::type* t1, typename cplx<T>::type* t2,
                              cudaStream_t st, KernelTimer* timer, const int* done) {
-  using C = typename cplx<T>::type;
-  constexpr int TZ = TileCfg<T>::TZ;
   const int nfield = 3 * L;
-  const int nxy = g.nx * g.ny;
-  const int nzt = (g.Pz + TZ - 1) / TZ;
-  if (g.nlines == 0) {
-    // no dipoles at all: y = diag o x (o jpre) is empty as well
-    return cudaSuccess;
-  }
+  const int pbase = sizeof(T) == sizeof(double) ? (kPassA64 - kPassA) : 0;
+  if (g.ntiles == 0) return cudaSuccess;  // no dipoles
+  const int ntask_y = nfield * g.Px * g.nzt;
+  const int grid_y = std::min(ntask_y, num_sms() * 8);
   // A
-  {
-    dim3 grid(g.nlines, (nfield + kLineWarps - 1) / kLineWarps);
-    int sm = smem_line_pass<T>(g.Pz);
-    if (timer) timer->begin(kPassA, st);
-    k_pass_a<T><<<grid, kLineWarps * 32, sm, st>>>(x, ldx, nfield, g.occ, g.lines, g.nz, nxy, g.pz, p.twz, t1, done);
-    if (timer) timer->end(kPassA, st);
-  }
+  if (timer) timer->begin(kPassA + pbase, st);
+  k_pass_a<T><<<g.ntiles, kTileThreads, smem_tile<T>(g.Px, g.nx), st>>>(x, ldx, nfield, g.occ, g.tiles, g.nx, g.ny,
+                                                                       g.nz, g.nzt, g.px, p.twx, t1, done);
+  if (timer) timer->end(kPassA + pbase, st);
   // B
-  {
-    dim3 grid(nzt, g.nx, nfield);
-    int sm = TZ * (g.Py | 1) * (int)sizeof(C);
-    if (timer) timer->begin(kPassB, st);
-    k_pass_y<T, false><<<grid, TZ * 32, sm, st>>>(t1, t2, g.lmask, g.nx, g.ny, g.Pz, g.py, p.twy, done);
-    if (timer) timer->end(kPassB, st);
-  }
+  if (timer) timer->begin(kPassB + pbase, st);
+  k_pass_y<T, false><<<grid_y, kTileThreads, smem_tile<T>(g.Py, 0), st>>>(t1, t2, g.tmask, g.ny, g.nz, g.nzt,
+                                                                         ntask_y, g.py, p.twy, done);
+  if (timer) timer->end(kPassB + pbase, st);
   // C
   {
-    dim3 grid(nzt, g.Py);
-    int sm = 3 * TZ * (g.Px | 1) * (int)sizeof(C);
-    if (timer) timer->begin(kPassC, st);
-    k_pass_c<T><<<grid, 3 * TZ * 32, sm, st>>>(t2, L, g.nx, g.Py, g.Pz, g.px, p.twx, p.ghat, done);
-    if (timer) timer->end(kPassC, st);
+    const long long ntask = (long long)g.Px * g.Py * L;
+    const unsigned grid = (unsigned)((ntask + kZWarps - 1) / kZWarps);
+    if (timer) timer->begin(kPassC + pbase, st);
+    k_pass_c<T><<<grid, kZWarps * 32, smem_z<T>(g.Pz), st>>>(t2, L, g.Px, g.Py, g.nz, g.pz, p.twz, p.ghat, done);
+    if (timer) timer->end(kPassC + pbase, st);
   }
   // D
-  {
-    dim3 grid(nzt, g.nx, nfield);
-    int sm = TZ * (g.Py | 1) * (int)sizeof(C);
-    if (timer) timer->begin(kPassD, st);
-    k_pass_y<T, true><<<grid, TZ * 32, sm, st>>>(t2, t1, g.lmask, g.nx, g.ny, g.Pz, g.py, p.twy, done);
-    if (timer) timer->end(kPassD, st);
-  }
+  if (timer) timer->begin(kPassD + pbase, st);
+  k_pass_y<T, true><<<grid_y, kTileThreads, smem_tile<T>(g.Py, 0), st>>>(t2, t1, g.tmask, g.ny, g.nz, g.nzt,
+                                                                        ntask_y, g.py, p.twy, done);
+  if (timer) timer->end(kPassD + pbase, st);
   // E
-  {
-    dim3 grid(g.nlines, (nfield + kLineWarps - 1) / kLineWarps);
-    int sm = smem_line_pass<T>(g.Pz);
-    if (timer) timer->begin(kPassE, st);
-    k_pass_e<T><<<grid, kLineWarps * 32, sm, st>>>(t1, nfield, g.nz, nxy, g.occ, g.lines, g.pz, p.twz, x, ldx,
-                                                   diag, jpre, y, ldy, done);
-    if (timer) timer->end(kPassE, st);
-  }
+  if (timer) timer->begin(kPassE + pbase, st);
+  k_pass_e<T><<<g.ntiles, kTileThreads, smem_tile<T>(g.Px, g.nx), st>>>(t1, nfield, g.occ, g.tiles, g.nx, g.ny, g.nz,
+                                                                       g.nzt, g.px, p.twx, x, ldx, diag, jpre, y, ldy,
+                                                                       done);
+  if (timer) timer->end(kPassE + pbase, st);
   return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t configure_mvp_kernels(int max_px) {
-  using C = typename cplx<T>::type;
-  constexpr int TZ = TileCfg<T>::TZ;
+cudaError_t configure_mvp_kernels() {
+  const int tile = smem_tile<T>(kMaxLine, kMaxLine / 2);
+  const int zs = smem_z<T>(kMaxLine);
   cudaError_t e;
-  int sm_c = 3 * TZ * (max_px | 1) * (int)sizeof(C);
-  e = cudaFuncSetAttribute(k_pass_c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_c > 48 * 1024 ? sm_c : 48 * 1024);
-  if (e != cudaSuccess) return e;
-  int sm_y = TZ * (kMaxLine | 1) * (int)sizeof(C);
-  e = cudaFuncSetAttribute(k_pass_y<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_y > 48 * 1024 ? sm_y : 48 * 1024);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_pass_y<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_y > 48 * 1024 ? sm_y : 48 * 1024);
-  if (e != cudaSuccess) return e;
-  int sm_l = kLineWarps * kMaxLine * (int)sizeof(C);
-  e = cudaFuncSetAttribute(k_pass_a<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_l > 48 * 1024 ? sm_l : 48 * 1024);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_pass_e<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_l > 48 * 1024 ? sm_l : 48 * 1024);
-  return e;
+  if ((e = cudaFuncSetAttribute(k_pass_a<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_pass_e<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_pass_y<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_pass_y<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_pass_c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, zs);
 }
 
 template cudaError_t launch_block_mvp<float>(const MvpGeom&, const MvpPrec<float>&, const float2*, int, float2*, int, int,
@@ -306,7 +361,7 @@ template cudaError_t launch_block_mvp<float>(const MvpGeom&, const MvpPrec<float
 template cudaError_t launch_block_mvp<double>(const MvpGeom&, const MvpPrec<double>&, const double2*, int, double2*, int,
                                               int, const double2*, const double2*, double2*, double2*, cudaStream_t,
                                               KernelTimer*, const int*);
-template cudaError_t configure_mvp_kernels<float>(int);
-template cudaError_t configure_mvp_kernels<double>(int);
+template cudaError_t configure_mvp_kernels<float>();
+template cudaError_t configure_mvp_kernels<double>();
 
 }  // namespace bdda

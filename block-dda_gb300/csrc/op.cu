@@ -41,9 +41,10 @@ Op::~Op() {
 
 int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o) {
   const int nx = op->n[0], ny = op->n[1], nz = op->n[2];
+  const int nzt = (nz + kTZ - 1) / kTZ;
   const size_t nc = (size_t)nx * ny * nz;
   std::vector<int> occ(nc, -1);
-  std::vector<unsigned char> lmask((size_t)nx * ny, 0);
+  std::vector<unsigned char> tmask((size_t)ny * nzt, 0);
   if (address == nullptr) nocc = (int)nc;
   for (int m = 0; m < nocc; ++m) {
     const long long a = address ? address[m] : m;
@@ -56,19 +57,26 @@ int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o) {
       return BDDA_ERR_INVALID;
     }
     occ[a] = m;
-    lmask[a / nz] = 1;
+    const long long iy = (a / nz) % ny, iz = a % nz;
+    tmask[iy * nzt + iz / kTZ] = 1;
   }
-  std::vector<int> lines;
-  for (size_t i = 0; i < lmask.size(); ++i)
-    if (lmask[i]) lines.push_back((int)i);
+  std::vector<int> tiles;
+  long long rows = 0;
+  for (int t = 0; t < ny * nzt; ++t)
+    if (tmask[t]) {
+      tiles.push_back(t);
+      const int z0 = (t % nzt) * kTZ;
+      rows += std::min(kTZ, nz - z0);
+    }
   o->nocc = nocc;
-  o->nlines = (int)lines.size();
+  o->ntiles = (int)tiles.size();
+  o->tile_rows = rows;
   BDDA_CUDA(o->occ.ensure(nc * sizeof(int)));
-  BDDA_CUDA(o->lmask.ensure(lmask.size()));
-  BDDA_CUDA(o->lines.ensure(std::max<size_t>(1, lines.size()) * sizeof(int)));
+  BDDA_CUDA(o->tmask.ensure(tmask.size()));
+  BDDA_CUDA(o->tiles.ensure(std::max<size_t>(1, tiles.size()) * sizeof(int)));
   BDDA_CUDA(cudaMemcpy(o->occ.p, occ.data(), nc * sizeof(int), cudaMemcpyHostToDevice));
-  BDDA_CUDA(cudaMemcpy(o->lmask.p, lmask.data(), lmask.size(), cudaMemcpyHostToDevice));
-  if (!lines.empty()) BDDA_CUDA(cudaMemcpy(o->lines.p, lines.data(), lines.size() * sizeof(int), cudaMemcpyHostToDevice));
+  BDDA_CUDA(cudaMemcpy(o->tmask.p, tmask.data(), tmask.size(), cudaMemcpyHostToDevice));
+  if (!tiles.empty()) BDDA_CUDA(cudaMemcpy(o->tiles.p, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice));
   return BDDA_OK;
 }
 
@@ -87,15 +95,11 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
     set_error("bad L or leading dimension");
     return BDDA_ERR_INVALID;
   }
-  const size_t nf = 3 * (size_t)L;
-  const size_t t1 = nf * op->n[0] * op->n[1] * op->P[2] * sizeof(C);
-  const size_t t2 = nf * op->n[0] * (size_t)op->P[1] * op->P[2] * sizeof(C);
-  BDDA_CUDA(op->t1[pi].ensure(t1));
-  BDDA_CUDA(op->t2[pi].ensure(t2));
   MvpGeom g = op->geom(o);
+  BDDA_CUDA(op->t1[pi].ensure(mvp_t1_elems(g, L) * sizeof(C)));
+  BDDA_CUDA(op->t2[pi].ensure(mvp_t2_elems(g, L) * sizeof(C)));
   cudaError_t e = launch_block_mvp<T>(g, op->tables<T>(), x, ldx, y, ldy, L, diag, jpre, op->t1[pi].as<C>(),
                                       op->t2[pi].as<C>(), st, &op->timer, done);
-  op->kernel_launches += 5;
   if (e != cudaSuccess) return cuda_fail(e, "block MVP launch");
   return BDDA_OK;
 }
@@ -147,17 +151,15 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     BDDA_CUDA(op->tw32[i].ensure(tf.size() * sizeof(float2)));
     BDDA_CUDA(cudaMemcpy(op->tw32[i].p, tf.data(), tf.size() * sizeof(float2), cudaMemcpyHostToDevice));
   }
-  BDDA_CUDA(configure_mvp_kernels<double>(kMaxLine));  // largest line, so every live operator fits
-  BDDA_CUDA(configure_mvp_kernels<float>(kMaxLine));
+  BDDA_CUDA(configure_mvp_kernels<double>());  // sized for the largest line, so every live operator fits
+  BDDA_CUDA(configure_mvp_kernels<float>());
   // Green spectrum
   const int Px = op->P[0], Py = op->P[1], Pz = op->P[2];
   const size_t ng = (size_t)Px * Py * Pz;
   DevBuf work;
   BDDA_CUDA(work.ensure(6 * ng * sizeof(double2)));
-  const int nzt_d = (Pz + TileCfg<double>::TZ - 1) / TileCfg<double>::TZ;
-  const int nzt_f = (Pz + TileCfg<float>::TZ - 1) / TileCfg<float>::TZ;
-  if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure((size_t)Py * nzt_d * 6 * Px * TileCfg<double>::TZ * sizeof(double2)));
-  if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure((size_t)Py * nzt_f * 6 * Px * TileCfg<float>::TZ * sizeof(float2)));
+  if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure(6 * ng * sizeof(double2)));
+  if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure(6 * ng * sizeof(float2)));
   MvpGeom g = op->geom(op->dip);
   BDDA_CUDA(build_green_hat(g, lf, k_re, k_im, op->tw64[0].as<double2>(), op->tw64[1].as<double2>(),
                             op->tw64[2].as<double2>(), work.as<double2>(), op->ghat64.as<double2>(),
@@ -181,11 +183,11 @@ int bdda_op_set_dipoles(bdda_op* op, const int* address, int nocc) {
   return build_occupancy(op, address, nocc, &op->dip);
 }
 
-int bdda_op_info(const bdda_op* op, int P[3], int* nocc, int* nlines) {
+int bdda_op_info(const bdda_op* op, int P[3], int* nocc, int* ntiles) {
   if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
   if (P) for (int i = 0; i < 3; ++i) P[i] = op->P[i];
   if (nocc) *nocc = op->dip.nocc;
-  if (nlines) *nlines = op->dip.nlines;
+  if (ntiles) *ntiles = op->dip.ntiles;
   return BDDA_OK;
 }
 
@@ -224,6 +226,29 @@ int bdda_op_mvp_device(bdda_op* op, int prec, const void* x, int ldx, void* y, i
                                (const float2*)jpre, st);
   set_error("prec must be BDDA_PREC_FP64 or BDDA_PREC_FP32");
   return BDDA_ERR_INVALID;
+}
+
+int bdda_op_mvp_bytes(const bdda_op* op, int prec, int L, int with_diag, int with_jpre, double bytes[5]) {
+  if (!op || !bytes || L < 1 || (prec != BDDA_PREC_FP64 && prec != BDDA_PREC_FP32)) {
+    set_error("bad mvp_bytes arguments");
+    return BDDA_ERR_INVALID;
+  }
+  const double s = prec == BDDA_PREC_FP64 ? 16.0 : 8.0;
+  const double F = 3.0 * L;
+  const double nocc = op->dip.nocc;
+  const double nx = op->n[0], nz = op->n[2], Px = op->P[0], Py = op->P[1], Pz = op->P[2];
+  const double rows = (double)op->dip.tile_rows;          // (y, z) columns of occupied tiles
+  const double t1 = F * Px * rows * s;                    // x-transformed rows of those tiles
+  const double t2 = F * Px * Py * nz * s;                 // y-transformed planes
+  const double vec = F * nocc * s;                        // one compact block
+  const double occ = nx * rows * 4.0;                     // occupancy of the tiles
+  const double ghat = 6.0 * Px * Py * Pz * s;
+  bytes[0] = vec + occ + t1;
+  bytes[1] = t1 + t2;
+  bytes[2] = 2.0 * t2 + ghat;
+  bytes[3] = t2 + t1;
+  bytes[4] = t1 + occ + vec + (with_diag ? vec + 3.0 * nocc * s : 0.0) + (with_jpre ? 3.0 * nocc * s : 0.0);
+  return BDDA_OK;
 }
 
 int bdda_op_set_timing(bdda_op* op, int enable) {

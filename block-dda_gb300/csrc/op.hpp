@@ -38,8 +38,9 @@ struct DevBuf {
 // Occupancy of the lattice by dipoles, on the device.
 struct Occupancy {
   int nocc = 0;
-  int nlines = 0;
-  DevBuf occ, lines, lmask, address;
+  int ntiles = 0;             // (y, z-tile) pairs holding >= 1 dipole
+  long long tile_rows = 0;    // their valid (y, z) columns
+  DevBuf occ, tiles, tmask;
 };
 
 struct SolverWork;  // solver.cu
@@ -60,17 +61,18 @@ struct Op {
   KernelTimer timer;
   std::mutex mu;
   std::shared_ptr<SolverWork> solver;   // cached Krylov workspace (solver.cu)
-  long long kernel_launches = 0;
 
   MvpGeom geom(const Occupancy& o) const {
     MvpGeom g;
     g.nx = n[0]; g.ny = n[1]; g.nz = n[2];
     g.Px = P[0]; g.Py = P[1]; g.Pz = P[2];
     g.px = plan[0]; g.py = plan[1]; g.pz = plan[2];
-    g.nlines = o.nlines;
+    g.nzt = (n[2] + kTZ - 1) / kTZ;
+    g.ntiles = o.ntiles;
+    g.tile_rows = o.tile_rows;
     g.occ = o.occ.as<int>();
-    g.lines = o.lines.as<int>();
-    g.lmask = o.lmask.as<unsigned char>();
+    g.tiles = o.tiles.as<int>();
+    g.tmask = o.tmask.as<unsigned char>();
     return g;
   }
   template <typename T> MvpPrec<T> tables() const;

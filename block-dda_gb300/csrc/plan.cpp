@@ -25,6 +25,13 @@ bool make_axis_plan(int N, AxisPlan* p) {
   for (int i = 0; i < c; ++i) push(5);
   for (int i = 0; i < b; ++i) push(3);
   if (p->nst == 0) push(2);  // N == 1 is rejected by callers; keep the plan well formed
+  int Ls = N;
+  for (int s = 0; s < p->nst; ++s) {
+    p->M[s] = Ls / p->radix[s];
+    p->tstride[s] = N / Ls;
+    p->invM[s] = 1.0f / (float)p->M[s];
+    Ls = p->M[s];
+  }
   return p->nst <= kMaxStages;
 }
 
@@ -55,28 +62,38 @@ extern "C" {
 // Runs the device FFT core (one "lane") on a host line: forward (natural ->
 // digit-reversed) or inverse (digit-reversed -> natural, unnormalised).
 // data: N interleaved complex values; prec 1 = FP64, 2 = FP32 arithmetic
-// (values are rounded to float and back).  Returns the number of stages, or
+// (values are rounded to float and back).  nvalid in (0, N): the forward
+// transform reads only the first nvalid inputs and takes the rest as zero
+// (the pad slots hold poison values to prove it).  Returns the number of stages, or
 // a negative value for an unsupported N.  Radices are written to radix (<= 16).
-int bdda_host_fft_line(int N, int inverse, int prec, double* data, int* radix) {
+int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, int* radix) {
   bdda::AxisPlan p;
   if (!bdda::make_axis_plan(N, &p)) return -1;
   std::vector<double2> tw;
   bdda::make_twiddles(N, &tw);
+  // nvalid: forward transforms read only the first nvalid inputs (zero padding)
+  const int nv = (nvalid > 0 && nvalid < N) ? nvalid : (1 << 30);
   if (prec == 1) {
-    std::vector<double2> s(N);
-    for (int i = 0; i < N; ++i) s[i] = make_double2(data[2 * i], data[2 * i + 1]);
+    std::vector<double2> s(bdda::line_words<double2>(N), make_double2(1e300, 1e300));
+    for (int i = 0; i < N; ++i) s[bdda::skw<double2>(i)] = make_double2(data[2 * i], data[2 * i + 1]);
     if (inverse) bdda::warp_fft<true>(s.data(), tw.data(), p, 0, 1);
-    else bdda::warp_fft<false>(s.data(), tw.data(), p, 0, 1);
-    for (int i = 0; i < N; ++i) { data[2 * i] = s[i].x; data[2 * i + 1] = s[i].y; }
-  } else {
-    std::vector<float2> s(N), t(N);
+    else bdda::warp_fft<false>(s.data(), tw.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
-      s[i] = make_float2((float)data[2 * i], (float)data[2 * i + 1]);
+      const double2 v = s[bdda::skw<double2>(i)];
+      data[2 * i] = v.x; data[2 * i + 1] = v.y;
+    }
+  } else {
+    std::vector<float2> s(bdda::line_words<float2>(N), make_float2(1e30f, 1e30f)), t(N);
+    for (int i = 0; i < N; ++i) {
+      s[bdda::skw<float2>(i)] = make_float2((float)data[2 * i], (float)data[2 * i + 1]);
       t[i] = make_float2((float)tw[i].x, (float)tw[i].y);
     }
     if (inverse) bdda::warp_fft<true>(s.data(), t.data(), p, 0, 1);
-    else bdda::warp_fft<false>(s.data(), t.data(), p, 0, 1);
-    for (int i = 0; i < N; ++i) { data[2 * i] = s[i].x; data[2 * i + 1] = s[i].y; }
+    else bdda::warp_fft<false>(s.data(), t.data(), p, 0, 1, nv);
+    for (int i = 0; i < N; ++i) {
+      const float2 v = s[bdda::skw<float2>(i)];
+      data[2 * i] = v.x; data[2 * i + 1] = v.y;
+    }
   }
   if (radix)
     for (int i = 0; i < p.nst; ++i) radix[i] = p.radix[i];

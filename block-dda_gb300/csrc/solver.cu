@@ -288,38 +288,32 @@ struct Krylov {
     op->timer.begin(kGram, st);
     k_gram<T, CONJ><<<G(), kGramThreads, 0, st>>>(A, n, B, n, n, L, part, ctl());
     op->timer.end(kGram, st);
-    ++op->kernel_launches;
   }
   void rowmm(const C* A, const double2* Ma, const C* B, const double2* Mb, const C* Cadd, C* Out) {
     op->timer.begin(kUpdate, st);
     k_rowmm<T><<<(n + kRowThreads - 1) / kRowThreads, kRowThreads, rowmm_smem<T>(L, B != nullptr), st>>>(
         n, L, A, n, Ma, B, n, Mb, Cadd, n, Out, n, ctl());
     op->timer.end(kUpdate, st);
-    ++op->kernel_launches;
   }
   void axpby(const double2* a, const C* A, const double2* b, const C* B, C* Out) {
     op->timer.begin(kUpdate, st);
     k_axpby<T><<<vec_grid((size_t)n * L), 256, 0, st>>>(n, L, a, A, n, b, B, n, Out, n, ctl());
     op->timer.end(kUpdate, st);
-    ++op->kernel_launches;
   }
   void dotc(const C* A, const C* B, double2* part) {
     op->timer.begin(kGram, st);
     k_dotc<T><<<vec_grid((size_t)n * L), 256, 0, st>>>(n, L, A, n, B, n, part, ctl());
     op->timer.end(kGram, st);
-    ++op->kernel_launches;
   }
   void colnorm(const C* A, double* part) {
     op->timer.begin(kGram, st);
     k_colnorm2<T><<<vec_grid((size_t)n * L), 256, 0, st>>>(A, n, n, L, part);
     op->timer.end(kGram, st);
-    ++op->kernel_launches;
   }
   template <typename K, typename... Args> void small_launch(K kern, Args... args) {
     op->timer.begin(kSmall, st);
     kern<<<1, kSmallThreads, SmallSmem::bytes(L), st>>>(args...);
     op->timer.end(kSmall, st);
-    ++op->kernel_launches;
   }
 
   // poll the control block; returns 1 when the device signalled done
@@ -336,7 +330,7 @@ struct Krylov {
     const int g = vec_grid((size_t)n * L);
     k_colnorm2<T><<<g, 256, 0, st>>>(Bp, n, n, L, vp);
     k_small_init<<<1, 256, 0, st>>>(vp, g, L, small(), ctl());
-    op->kernel_launches += 2;
+    op->timer.count(kOther, 2);
     return cudaGetLastError() == cudaSuccess ? BDDA_OK : cuda_fail(cudaGetLastError(), "init");
   }
 
@@ -420,14 +414,12 @@ struct Krylov {
       op->timer.begin(kSmall, st);
       k_small_zeta<<<1, 256, 0, st>>>(vp, vp + gv, gv, L, small(), scal, ctl());
       op->timer.end(kSmall, st);
-      ++op->kernel_launches;
       rowmm(P, sl(kAlpha), Tm, sl(kZetaI), X, X);            // X = X + P alpha + zeta T
       axpby(nullptr, Tm, scal + 1, Z, R);                    // R = T - zeta Z
       colnorm(R, w->vpart.as<double>());
       op->timer.begin(kSmall, st);
       k_small_err<<<1, 32, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
       op->timer.end(kSmall, st);
-      ++op->kernel_launches;
       gram<true>(R0, Z, p);
       small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, G(), L, small(), ctl(), (int)kM, -1, -1.0,
                    (const double2*)nullptr, (int)kBeta, -1);  // beta = M^-1 (-R0^H Z)
@@ -474,7 +466,6 @@ struct Krylov {
       op->timer.begin(kSmall, st);
       k_small_zeta<<<1, 256, 0, st>>>(vp, vp + gv, gv, L, small(), scal, ctl());
       op->timer.end(kSmall, st);
-      ++op->kernel_launches;
       axpby(nullptr, P, scal + 1, V, Rn);                    // S = P - zeta V   (Rn as scratch)
       rowmm(Rn, sl(kAlpha), nullptr, nullptr, nullptr, U);   // U = S alpha
       BDDA_TRY(mvp(U, Y));                                   // Y = A U
@@ -484,7 +475,6 @@ struct Krylov {
       op->timer.begin(kSmall, st);
       k_small_err<<<1, 32, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
       op->timer.end(kSmall, st);
-      ++op->kernel_launches;
       BDDA_TRY(mvp(Rn, Wm));                                 // W = A Rnew
       gram<true>(R0, Rn, p);
       small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, G(), L, small(), ctl(), (int)kM2, -1, 1.0,
@@ -568,7 +558,7 @@ static int host_colnorm2(Op* op, cudaStream_t st, const double2* A, int n, int L
   const int g = vec_grid((size_t)n * L);
   double* vp = w->vpart.as<double>();
   k_colnorm2<double><<<g, 256, 0, st>>>(A, n, n, L, vp);
-  ++op->kernel_launches;
+  op->timer.count(kOther);
   std::vector<double> h((size_t)g * L);
   BDDA_CUDA(cudaMemcpyAsync(h.data(), vp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
   BDDA_CUDA(cudaStreamSynchronize(st));
@@ -585,7 +575,7 @@ static int true_residual(Op* op, cudaStream_t st, const double2* diag, const dou
   BDDA_TRY(op_block_mvp<double>(op, op->dip, X, n, w->Y64.as<double2>(), n, L, diag, nullptr, st));
   ++*mvps;
   k_residual<<<vec_grid((size_t)n * L), 256, 0, st>>>(n, L, B, ldb, w->Y64.as<double2>(), n, w->R64.as<double2>(), n);
-  ++op->kernel_launches;
+  op->timer.count(kOther);
   std::vector<double> rn2;
   BDDA_TRY(host_colnorm2(op, st, w->R64.as<double2>(), n, L, &rn2));
   double mx = 0.0;
@@ -619,7 +609,7 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
   cudaEventCreate(&e1);
   cudaEventRecord(e0, st);
   k_diag_prep<<<vec_grid(n), 256, 0, st>>>(n, diag, w->jpre64.as<double2>(), w->diag32.as<float2>(), w->jpre32.as<float2>());
-  ++op->kernel_launches;
+  op->timer.count(kOther);
   const double2* jpre64 = o->jacobi ? w->jpre64.as<double2>() : nullptr;
   const float2* jpre32 = o->jacobi ? w->jpre32.as<float2>() : nullptr;
   const bool full = !o->jacobi && o->solver == BDDA_SOLVER_COCG_RQ;  // fullPivLu only in bl_cocg_rq_mvp_fft
@@ -641,21 +631,21 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
       double2* D = w->blk64[9].as<double2>();
       if (o->jacobi) k_rowscale<double, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n);
       else k_convert<double, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n);
-      ++op->kernel_launches;
+      op->timer.count(kOther);
       BDDA_TRY(k64.run(o->solver, Bp, D, full, tol, itermax, &it, &er, &stt));
       if (accumulate) k_accumulate<double><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
       else k_convert<double, double><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
-      ++op->kernel_launches;
+      op->timer.count(kOther);
     } else {
       float2* Bp = w->blk32[8].as<float2>();
       float2* D = w->blk32[9].as<float2>();
       if (o->jacobi) k_rowscale<float, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n);
       else k_convert<float, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n);
-      ++op->kernel_launches;
+      op->timer.count(kOther);
       BDDA_TRY(k32.run(o->solver, Bp, D, full, tol, itermax, &it, &er, &stt));
       if (accumulate) k_accumulate<float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
       else k_convert<double, float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
-      ++op->kernel_launches;
+      op->timer.count(kOther);
     }
     total_iters += it;
     last_err = er;

@@ -70,8 +70,8 @@ int bdda_op_destroy(bdda_op* op);
  */
 int bdda_op_set_dipoles(bdda_op* op, const int* address, int nocc);
 
-/* Padded grid, dipole count and number of occupied (x, y) lattice lines. */
-int bdda_op_info(const bdda_op* op, int P[3], int* nocc, int* nlines);
+/* Padded grid, dipole count and number of occupied (y, 8-wide z) lattice tiles. */
+int bdda_op_info(const bdda_op* op, int P[3], int* nocc, int* ntiles);
 
 /*
  * Reference MBT_fft_mvp (mvp_fft/MBT_fft_mvp.cpp:8-43, MBT_utils.hpp:6):
@@ -179,13 +179,22 @@ int bdda_cross_sections(double k, const double alpha0[2], const double* E, int l
 
 /* ---- instrumentation ------------------------------------------------------ */
 
+/*
+ * Algorithmic HBM bytes of one block MVP over the operator's dipoles with L
+ * right-hand sides (prec BDDA_PREC_FP64 / BDDA_PREC_FP32), per kernel pass:
+ * bytes[0..4] = passes A..E (the minimum reads + writes each pass must do).
+ * with_diag / with_jpre add the diagonal and Jacobi reads.  Returns BDDA_OK.
+ */
+int bdda_op_mvp_bytes(const bdda_op* op, int prec, int L, int with_diag, int with_jpre, double bytes[5]);
+
 /* Enable (1) / disable (0) per-kernel CUDA-event timing on the operator. */
 int bdda_op_set_timing(bdda_op* op, int enable);
 
 /*
  * Per-kernel totals since the last reset: ms[i], launches[i] for
- * i = 0..n-1 in the order passA, passB, passC, passD, passE, gram, update,
- * small, other.  Returns the number of entries written (<= n).  reset=1 zeroes
+ * i = 0..n-1 in the order passA..passE of the complex FP32 MVP, passA..passE
+ * of the complex FP64 MVP, gram (Gram / dot / norm reductions), update (row
+ * transforms), small (one-CTA L x L steps), other (conversions, residuals).  Returns the number of entries written (<= n).  reset=1 zeroes
  * the counters after reading.
  */
 int bdda_op_kernel_stats(bdda_op* op, double* ms, long long* launches, int n, int reset);
@@ -197,11 +206,13 @@ const char* bdda_last_error(void);
  * Test hook: run the device FFT core (the same source the kernels inline) on
  * the CPU for one line of length N (5-smooth, <= 512).  inverse = 0: natural
  * order in, digit-reversed spectrum out; inverse = 1: digit-reversed in,
- * natural out, unnormalised.  prec 1 = FP64, 2 = FP32 arithmetic.  data holds
- * N interleaved complex doubles, overwritten.  Returns the number of radix
- * stages (radices written to radix[0..16)) or -1 for an unsupported N.
+ * natural out, unnormalised.  prec 1 = FP64, 2 = FP32 arithmetic.  nvalid in
+ * (0, N) makes the forward transform read only the first nvalid inputs (the
+ * rest count as zero); 0 reads all.  data holds N interleaved complex doubles,
+ * overwritten.  Returns the number of radix stages (radices written to
+ * radix[0..16)) or -1 for an unsupported N.
  */
-int bdda_host_fft_line(int N, int inverse, int prec, double* data, int* radix);
+int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, int* radix);
 
 #ifdef __cplusplus
 }

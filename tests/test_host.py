@@ -71,6 +71,13 @@ def test_device_fft_core_on_cpu(N):
     fb32, _ = bdda.host_fft_line(b, prec=2)
     conv32, _ = bdda.host_fft_line(fa32 * fb32, inverse=True, prec=2)
     assert np.max(np.abs(conv32 / N - cref)) / np.max(np.abs(cref)) < 1e-6
+    # pruned input: only the first nv values are read (the rest are poisoned in the hook)
+    nv = max(1, N // 2)
+    ap = a.copy()
+    ap[nv:] = 0.0
+    fp, _ = bdda.host_fft_line(a, nvalid=nv)
+    fz, _ = bdda.host_fft_line(ap)
+    assert np.max(np.abs(fp - fz)) <= 1e-12 * np.max(np.abs(fz))
 
 
 def test_mie_a1b1_matches_reference_gmie():

@@ -128,3 +128,21 @@ def test_oracle_solvers_converge(name, jacobi):
     X, hist = krylov.SOLVERS[name](amul, B, 1e-10, 200, diag=alpha, jacobi=jacobi)
     assert hist[-1] < 1e-10
     assert np.all(krylov.true_residual(amul, B, X) < 1e-8)
+
+
+@pytest.mark.parametrize("n", [(3, 2, 4), (2, 5, 3), (1, 1, 4)])
+def test_vectorised_reference_algorithm_matches_literal(n):
+    from oracle import mbt_fast
+    rng = np.random.default_rng(7)
+    lf, k = 0.4, 1.7 + 0.1j
+    assert np.array_equal(mbt_fast.pad_map(n, 3), np.flatnonzero(mbt.bt_pad(n, 3, np.ones(3 * int(np.prod(n))))))
+    au_lit = mbt.bt_fft(list(n), 3, np.ones((2, 3), dtype=np.int64), 1, lf, k)
+    assert np.allclose(mbt_fast.au_vector(n, lf, k), au_lit, rtol=1e-14, atol=0)
+    N = int(np.prod(n))
+    addr = np.arange(N)
+    diag = rng.standard_normal(3 * N) + 1j
+    cpu = mbt_fast.MbtCpu(n, lf, k, addr, diag, threads=2)
+    S = rng.standard_normal((3 * N, 2)) + 1j * rng.standard_normal((3 * N, 2))
+    gh, P = mbt.green_hat(n, 3, lf, k)
+    ref = mbt.block_mvp(n, 3, gh, P, addr, diag, S)
+    assert np.linalg.norm(cpu.block_mvp(S) - ref) / np.linalg.norm(ref) < 1e-13
