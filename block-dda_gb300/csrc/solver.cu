@@ -88,18 +88,32 @@ __device__ void fail(SolverCtl* ctl) {
   if (threadIdx.x == 0) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; }
 }
 
-// Identity helpers and ||B|| from column-norm partials.
-__global__ void k_small_init(const double* __restrict__ vpart, int nparts, int L, double2* st, SolverCtl* ctl) {
+// Deterministic sum of vpart[0..count) by one CTA of 256 threads (fixed tree).
+__device__ double block_sum_256(const double* __restrict__ vpart, int count) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < count; i += 256) s += vpart[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// Identity helpers and ||B|| from column-norm partials.  256 threads.
+__global__ void __launch_bounds__(256) k_small_init(const double* __restrict__ vpart, int nparts, int L, double2* st, SolverCtl* ctl) {
   const int LL = L * L;
   for (int e = threadIdx.x; e < LL; e += blockDim.x) {
     const int i = e % L, j = e / L;
     slot(st, kIdent, L)[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
     slot(st, kNIdent, L)[e] = make_double2(i == j ? -1.0 : 0.0, 0.0);
   }
+  const double s = block_sum_256(vpart, nparts * L);
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int p = 0; p < nparts; ++p)
-      for (int l = 0; l < L; ++l) s += vpart[(size_t)p * L + l];
     ctl->bnorm = sqrt(s);
     ctl->done = 0;
     ctl->status = 0;
@@ -236,13 +250,12 @@ __global__ void k_small_zeta(const double2* __restrict__ p1, const double2* __re
   }
 }
 
-// err = sqrt(sum of column-norm partials) / bnorm ; stopping test
-__global__ void k_small_err(const double* __restrict__ vpart, int nparts, int L, SolverCtl* ctl, double tol, double* hist, int k) {
+// err = sqrt(sum of column-norm partials) / bnorm ; stopping test.  256 threads.
+__global__ void __launch_bounds__(256) k_small_err(const double* __restrict__ vpart, int nparts, int L, SolverCtl* ctl, double tol,
+                                                   double* hist, int k) {
   if (ctl_skip(ctl)) return;
+  const double s = block_sum_256(vpart, nparts * L);
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int p = 0; p < nparts; ++p)
-      for (int l = 0; l < L; ++l) s += vpart[(size_t)p * L + l];
     const double err = sqrt(s) / ctl->bnorm;
     ctl->err = err;
     if (hist) hist[k] = err;
@@ -418,7 +431,7 @@ struct Krylov {
       axpby(nullptr, Tm, scal + 1, Z, R);                    // R = T - zeta Z
       colnorm(R, w->vpart.as<double>());
       op->timer.begin(kSmall, st);
-      k_small_err<<<1, 32, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
+      k_small_err<<<1, 256, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
       op->timer.end(kSmall, st);
       gram<true>(R0, Z, p);
       small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, G(), L, small(), ctl(), (int)kM, -1, -1.0,
@@ -473,7 +486,7 @@ struct Krylov {
       rowmm(Wm, sl(kNZetaI), Y, sl(kNIdent), R, Rn);         // Rn = R - zeta W - Y
       colnorm(Rn, w->vpart.as<double>());
       op->timer.begin(kSmall, st);
-      k_small_err<<<1, 32, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
+      k_small_err<<<1, 256, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
       op->timer.end(kSmall, st);
       BDDA_TRY(mvp(Rn, Wm));                                 // W = A Rnew
       gram<true>(R0, Rn, p);
