@@ -33,6 +33,7 @@ EXPORTS = [
     "bdda_op_mvp_device", "bdda_solve_opts_default", "bdda_solve_device", "bdda_solve", "bdda_qr_reduced",
     "bdda_mie_a1b1", "bdda_aggregate", "bdda_incident_fields", "bdda_cross_sections", "bdda_op_set_timing",
     "bdda_op_kernel_stats", "bdda_last_error", "bdda_op_mvp_bytes", "bdda_host_fft_line",
+    "bdda_op_mvp_device_noalloc",
 ]
 
 
@@ -78,6 +79,7 @@ def lib(build_if_missing: bool = False):
     L.bdda_op_info.argtypes = [vp, ip, ip, ip]
     L.bdda_mbt_fft_mvp.argtypes = [vp, dp, dp]
     L.bdda_op_mvp_device.argtypes = [vp, ct.c_int, vp, ct.c_int, vp, ct.c_int, ct.c_int, vp, vp, vp]
+    L.bdda_op_mvp_device_noalloc.argtypes = [vp, ct.c_int, vp, ct.c_int, vp, ct.c_int, ct.c_int, vp, vp, vp]
     L.bdda_solve_opts_default.argtypes = [ct.POINTER(SolveOpts)]
     L.bdda_solve_opts_default.restype = None
     L.bdda_solve_device.argtypes = [vp, ct.POINTER(SolveOpts), vp, vp, ct.c_int, vp, ct.c_int, ct.c_int,
@@ -181,6 +183,14 @@ class Operator:
         b = np.zeros(5)
         _check(lib().bdda_op_mvp_bytes(self._h, prec, int(L), int(with_diag), int(with_jpre), _dptr(b)))
         return b
+
+    def mvp_device_noalloc(self, x, y, L, ldx, ldy, prec=PREC_FP64, diag=None, jpre=None, stream=None):
+        """Same as mvp_device, with the workspace in the library's fixed device
+        array instead of memory allocated by the call (bdda_op_mvp_device_noalloc)."""
+        _check(lib().bdda_op_mvp_device_noalloc(self._h, prec, ct.c_void_p(x), ldx, ct.c_void_p(y), ldy, L,
+                                                ct.c_void_p(diag) if diag else None,
+                                                ct.c_void_p(jpre) if jpre else None,
+                                                ct.c_void_p(stream) if stream else None))
 
     def set_timing(self, on=True):
         _check(lib().bdda_op_set_timing(self._h, 1 if on else 0))

@@ -95,6 +95,22 @@ int bdda_mbt_fft_mvp(bdda_op* op, const double* p_hat, double* q_hat);
 int bdda_op_mvp_device(bdda_op* op, int prec, const void* x, int ldx, void* y, int ldy, int L,
                        const void* diag, const void* jpre, void* stream);
 
+/*
+ * Block MVP that allocates no device memory.  No counterpart in the
+ * reference: it exists for callers that cannot let a library call cudaMalloc
+ * -- frameworks that own all device memory through their own pool, and
+ * serving loops that must never enter the CUDA allocator (which can
+ * synchronise the device).  Same arguments and result as bdda_op_mvp_device,
+ * but the two FFT workspaces come from a fixed 64 MiB __device__ array that
+ * every GPU loading the library reserves until exit; boxes and nrhs whose
+ * workspace exceeds it are rejected with BDDA_ERR_INVALID and a message.
+ * The first call on a device looks up the array's device address (make it
+ * before any stream capture).  All calls share the array: calls that overlap
+ * on the GPU race and must be ordered by the caller.
+ */
+int bdda_op_mvp_device_noalloc(bdda_op* op, int prec, const void* x, int ldx, void* y, int ldy, int L,
+                               const void* diag, const void* jpre, void* stream);
+
 /* ---- block solvers ----------------------------------------------------- */
 typedef struct {
   int solver;         /* BDDA_SOLVER_* */

@@ -1,0 +1,64 @@
+"""The allocation-free block MVP (bdda_op_mvp_device_noalloc).
+
+It serves callers that cannot let the library allocate device memory: hosts
+that own all GPU memory through their own pool, and serving loops that must not
+enter the CUDA allocator.  Its result must equal the regular (allocating) entry
+point's, call after call, while its scratch is the library's fixed device array.
+This file sorts last so a run that stops at the first failure has run every
+other test first; it also passes when run alone in a fresh process.
+"""
+import numpy as np
+import pytest
+
+import bdda
+
+pytestmark = pytest.mark.gpu
+
+TOL = {bdda.PREC_FP64: 1e-12, bdda.PREC_FP32: 5e-6}   # the MVP parity tolerances of the suite
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_no_alloc_mvp_matches_allocating_entry_point_twice():
+    import torch
+    nocc, L = 300, 4
+    n, addr = bdda.aggregate(nocc, 1.0, 2.8, 17)
+    rng = np.random.default_rng(17)
+    x = rng.standard_normal((3 * nocc, L)) + 1j * rng.standard_normal((3 * nocc, L))
+    diag = rng.standard_normal(3 * nocc) + 1j * rng.standard_normal(3 * nocc) + 4.0
+    op = bdda.Operator(n, 0.02, 2 * np.pi / 0.55)
+    op.set_dipoles(addr)
+    for prec, dt in ((bdda.PREC_FP64, torch.complex128), (bdda.PREC_FP32, torch.complex64)):
+        xd = torch.from_numpy(np.ascontiguousarray(x.T)).to(dt).cuda()
+        dd = torch.from_numpy(diag).to(dt).cuda()
+        jd = (1.0 / dd).contiguous()
+        ref = torch.zeros_like(xd)
+        torch.cuda.synchronize()
+        op.mvp_device(xd.data_ptr(), ref.data_ptr(), L, 3 * nocc, 3 * nocc, prec=prec, diag=dd.data_ptr(),
+                      jpre=jd.data_ptr())
+        torch.cuda.synchronize()
+        want = ref.cpu().numpy()
+        for _call in range(2):
+            out = torch.full_like(xd, float("nan"))
+            torch.cuda.synchronize()
+            op.mvp_device_noalloc(xd.data_ptr(), out.data_ptr(), L, 3 * nocc, 3 * nocc, prec=prec,
+                                  diag=dd.data_ptr(), jpre=jd.data_ptr())
+            torch.cuda.synchronize()
+            got = out.cpu().numpy()
+            assert np.all(np.isfinite(got))
+            assert _rel(got, want) <= TOL[prec]
+
+
+def test_no_alloc_mvp_rejects_workspace_beyond_fixed_scratch():
+    import torch
+    nocc, L = 16384, 32
+    n, addr = bdda.aggregate(nocc, 1.0, 2.8, 1)
+    op = bdda.Operator(n, 0.02, 2 * np.pi / 0.55, prec=bdda.PREC_FP32)
+    op.set_dipoles(addr)
+    x = torch.zeros((L, 3 * nocc), dtype=torch.complex64, device="cuda")
+    with pytest.raises(bdda.BddaError) as ei:
+        op.mvp_device_noalloc(x.data_ptr(), x.data_ptr(), L, 3 * nocc, 3 * nocc, prec=bdda.PREC_FP32)
+    assert ei.value.code == bdda.ERR_INVALID
+    assert "scratch" in str(ei.value)
