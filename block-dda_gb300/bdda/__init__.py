@@ -33,7 +33,8 @@ EXPORTS = [
     "bdda_op_mvp_device", "bdda_solve_opts_default", "bdda_solve_device", "bdda_solve", "bdda_qr_reduced",
     "bdda_mie_a1b1", "bdda_aggregate", "bdda_incident_fields", "bdda_cross_sections", "bdda_op_set_timing",
     "bdda_op_kernel_stats", "bdda_last_error", "bdda_op_mvp_bytes", "bdda_host_fft_line",
-    "bdda_op_mvp_device_noalloc",
+    "bdda_op_mvp_device_noalloc", "bdda_request_footprint", "bdda_server_create", "bdda_server_submit",
+    "bdda_server_wait", "bdda_server_stats", "bdda_server_destroy", "bdda_batch_solve",
 ]
 
 
@@ -47,6 +48,21 @@ class SolveOpts(ct.Structure):
     _fields_ = [("solver", ct.c_int), ("jacobi", ct.c_int), ("precision", ct.c_int), ("tol", ct.c_double),
                 ("itermax", ct.c_int), ("true_tol", ct.c_double), ("inner_tol", ct.c_double),
                 ("max_refine", ct.c_int), ("check_every", ct.c_int)]
+
+
+class Request(ct.Structure):
+    _fields_ = [("n", ct.c_int * 3), ("lf", ct.c_double), ("k_re", ct.c_double), ("k_im", ct.c_double),
+                ("address", ct.POINTER(ct.c_int)), ("nocc", ct.c_int), ("diag", ct.POINTER(ct.c_double)),
+                ("B", ct.POINTER(ct.c_double)), ("L", ct.c_int), ("X", ct.POINTER(ct.c_double))]
+
+
+class RequestResult(ct.Structure):
+    _fields_ = [("status", ct.c_int), ("iterations", ct.c_int), ("refinements", ct.c_int),
+                ("true_res_max", ct.c_double), ("t_submit", ct.c_double), ("t_start", ct.c_double),
+                ("t_done", ct.c_double), ("footprint_bytes", ct.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class SolveStats(ct.Structure):
@@ -95,6 +111,15 @@ def lib(build_if_missing: bool = False):
     L.bdda_op_set_timing.argtypes = [vp, ct.c_int]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
     L.bdda_last_error.restype = ct.c_char_p
+    L.bdda_request_footprint.argtypes = [ip, ct.c_int, ct.c_int, ct.c_int]
+    L.bdda_request_footprint.restype = ct.c_double
+    L.bdda_server_create.argtypes = [ct.POINTER(vp), ct.c_int, ct.c_double, ct.POINTER(SolveOpts), ct.c_int]
+    L.bdda_server_submit.argtypes = [vp, ct.POINTER(Request), ct.POINTER(ct.c_longlong)]
+    L.bdda_server_wait.argtypes = [vp, ct.c_longlong, ct.POINTER(RequestResult)]
+    L.bdda_server_stats.argtypes = [vp, dp, ip, ct.POINTER(ct.c_longlong)]
+    L.bdda_server_destroy.argtypes = [vp]
+    L.bdda_batch_solve.argtypes = [ct.POINTER(Request), ct.c_int, ct.c_int, ct.c_double, ct.POINTER(SolveOpts),
+                                   ct.POINTER(RequestResult)]
     L.bdda_host_fft_line.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int, dp, ip]
     _LIB = L
     return L
@@ -361,3 +386,110 @@ def make_problem(nocc, m, wl0=0.55, kf=1.0, Df=2.8, seed=1, n_dirs=1, mkd=0.5):
     u, e = directions(n_dirs, seed + 1000)
     B = incident_fields(n, d, addr, k, u, e)
     return Problem(n=n, lf=d, address=addr, k=k, alpha=alpha, diag=diag, B=B)
+
+
+# ---------------------------------------------------------------------------
+# batched solves and the request server
+# ---------------------------------------------------------------------------
+
+def footprint(n, nocc, L, precision=SOLVE_MIXED):
+    n3 = (ct.c_int * 3)(*[int(v) for v in n])
+    return float(lib().bdda_request_footprint(n3, int(nocc), int(L), int(precision)))
+
+
+class _Held:
+    """Keeps the numpy buffers of a request alive while the server uses them."""
+
+    def __init__(self, prob: Problem):
+        self.address = np.ascontiguousarray(prob.address, dtype=np.int32)
+        self.diag = np.ascontiguousarray(prob.diag, dtype=np.complex128)
+        self.B = np.asfortranarray(prob.B, dtype=np.complex128)
+        self.X = np.zeros_like(self.B, order="F")
+        self.req = Request()
+        for i in range(3):
+            self.req.n[i] = int(prob.n[i])
+        self.req.lf = float(prob.lf)
+        self.req.k_re = float(np.real(prob.k))
+        self.req.k_im = float(np.imag(prob.k))
+        self.req.address = _iptr(self.address)
+        self.req.nocc = int(self.address.size)
+        self.req.diag = _dptr(self.diag)
+        self.req.B = _dptr(self.B)
+        self.req.L = int(self.B.shape[1])
+        self.req.X = _dptr(self.X)
+
+
+class Server:
+    """Request server (``bdda_server_*``): concurrent solves admitted by memory footprint."""
+
+    def __init__(self, slots, mem_budget_bytes, opts: SolveOpts, dry_run=False):
+        self._h = ct.c_void_p()
+        self._opts = opts
+        _check(lib().bdda_server_create(ct.byref(self._h), int(slots), float(mem_budget_bytes), ct.byref(opts),
+                                        1 if dry_run else 0))
+        self._held = {}
+
+    def submit(self, prob: Problem):
+        h = _Held(prob)
+        t = ct.c_longlong()
+        _check(lib().bdda_server_submit(self._h, ct.byref(h.req), ct.byref(t)))
+        self._held[t.value] = h
+        return t.value
+
+    def wait(self, ticket, allow_fail=False):
+        r = RequestResult()
+        rc = lib().bdda_server_wait(self._h, ticket, ct.byref(r))
+        h = self._held.pop(ticket)
+        if not allow_fail:
+            _check(rc)
+        return h.X, r.as_dict()
+
+    def stats(self):
+        pb, pr, done = ct.c_double(), ct.c_int(), ct.c_longlong()
+        _check(lib().bdda_server_stats(self._h, ct.byref(pb), ct.byref(pr), ct.byref(done)))
+        return {"peak_inflight_bytes": pb.value, "peak_running": pr.value, "completed": done.value}
+
+    def close(self):
+        if self._h:
+            lib().bdda_server_destroy(self._h)
+            self._h = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_solve(problems, slots, mem_budget_bytes, opts: SolveOpts):
+    """Solve many problems concurrently (``bdda_batch_solve``).  Returns [(X, result dict)]."""
+    held = [_Held(p) for p in problems]
+    reqs = (Request * len(held))(*[h.req for h in held])
+    res = (RequestResult * len(held))()
+    rc = lib().bdda_batch_solve(reqs, len(held), int(slots), float(mem_budget_bytes), ct.byref(opts), res)
+    out = [(h.X, res[i].as_dict()) for i, h in enumerate(held)]
+    if rc != OK and rc != ERR_NOT_CONVERGED:
+        _check(rc)
+    return out
+
+
+def random_problem(rng, n_range=(64, 8192), wl_range=(0.55, 0.55), L_choices=(2, 4, 8, 16), L_range=None,
+                   seed=None):
+    """One seeded aggregate problem with the batched/serving parameter ranges:
+    N log-uniform, Df ~ U[1.8, 2.8], kf ~ U[1.0, 1.3], Re m ~ U[1.3, 2.4],
+    Im m ~ U[0, 0.9], L from L_choices (or uniform in L_range)."""
+    lo, hi = np.log(n_range[0]), np.log(n_range[1])
+    nocc = int(round(np.exp(rng.uniform(lo, hi))))
+    df = rng.uniform(1.8, 2.8)
+    kf = rng.uniform(1.0, 1.3)
+    m = complex(rng.uniform(1.3, 2.4), rng.uniform(0.0, 0.9))
+    wl0 = rng.uniform(*wl_range)
+    if L_range is not None:
+        L = int(rng.integers(L_range[0], L_range[1] + 1))
+    else:
+        L = int(rng.choice(L_choices))
+    s = int(rng.integers(1, 2 ** 31 - 1)) if seed is None else seed
+    prob = make_problem(nocc, m, wl0=wl0, kf=kf, Df=df, seed=s, n_dirs=(L + 1) // 2)
+    if prob.B.shape[1] != L:
+        prob.B = np.asfortranarray(prob.B[:, :L])
+    return prob

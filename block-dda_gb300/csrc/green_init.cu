@@ -7,6 +7,7 @@
 // circulant grid (index j -> offset j for j < n, j - P for j > P - n, zero in
 // the gap and at d = 0), its 6 distinct components are transformed with a full
 // 3-D FFT in FP64, divided by Px*Py*Pz and re-tiled for the fused x pass.
+#include <mutex>
 #include <vector>
 
 #include "fft_core.cuh"
@@ -133,9 +134,14 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
   const int Px = g.Px, Py = g.Py, Pz = g.Pz;
   const size_t ng = (size_t)Px * Py * Pz;
   cudaError_t e;
-  const int maxsm = kInitWarps * line_words<double2>(kMaxLine) * (int)sizeof(double2);
-  if ((e = cudaFuncSetAttribute(k_fft_contig, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_fft_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm)) != cudaSuccess) return e;
+  static std::once_flag once;
+  static cudaError_t cfg = cudaSuccess;
+  std::call_once(once, [] {
+    const int maxsm = kInitWarps * line_words<double2>(kMaxLine) * (int)sizeof(double2);
+    cfg = cudaFuncSetAttribute(k_fft_contig, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    if (cfg == cudaSuccess) cfg = cudaFuncSetAttribute(k_fft_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+  });
+  if ((e = cfg) != cudaSuccess) return e;
   k_green_eval<<<1216, 256, 0, st>>>(work, g.nx, g.ny, g.nz, Px, Py, Pz, lf, k_re, k_im);
   // z lines (contiguous)
   {

@@ -7,6 +7,8 @@
 #include "../../include/bdda.h"
 #include "op.hpp"
 
+#include <mutex>
+
 namespace bdda {
 
 namespace {
@@ -26,6 +28,19 @@ static int cuda_fail(cudaError_t e, const char* where) {
     if (_e != cudaSuccess) return cuda_fail(_e, #call);   \
   } while (0)
 
+#define BDDA_TRY_CUDA(call) BDDA_CUDA(call)
+
+// Make stream 'later' wait for everything enqueued so far on 'earlier'.
+cudaError_t order_after(cudaStream_t later, cudaStream_t earlier) {
+  cudaEvent_t ev;
+  cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) return e;
+  e = cudaEventRecord(ev, earlier);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(later, ev, 0);
+  cudaEventDestroy(ev);
+  return e;
+}
+
 static int smooth235(int v) {
   for (;; ++v) {
     int t = v;
@@ -35,8 +50,32 @@ static int smooth235(int v) {
   }
 }
 
+void keep_pool_memory() {
+  static bool done[64] = {};
+  static std::mutex mu;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    unsigned long long thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev] = true;
+}
+
 Op::~Op() {
-  if (stream) cudaStreamDestroy(stream);
+  // release every stream-ordered buffer on the operator's stream before it goes away
+  solver.reset();
+  for (auto* o : {&dip, &cub}) { o->occ.release(); o->tiles.release(); o->tmask.release(); }
+  for (int i = 0; i < 3; ++i) { tw64[i].release(); tw32[i].release(); }
+  ghat64.release(); ghat32.release();
+  for (int i = 0; i < 2; ++i) { t1[i].release(); t2[i].release(); }
+  if (stream) {
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
 }
 
 int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o) {
@@ -71,9 +110,9 @@ int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o) {
   o->nocc = nocc;
   o->ntiles = (int)tiles.size();
   o->tile_rows = rows;
-  BDDA_CUDA(o->occ.ensure(nc * sizeof(int)));
-  BDDA_CUDA(o->tmask.ensure(tmask.size()));
-  BDDA_CUDA(o->tiles.ensure(std::max<size_t>(1, tiles.size()) * sizeof(int)));
+  BDDA_CUDA(o->occ.ensure(nc * sizeof(int), op->stream));
+  BDDA_CUDA(o->tmask.ensure(tmask.size(), op->stream));
+  BDDA_CUDA(o->tiles.ensure(std::max<size_t>(1, tiles.size()) * sizeof(int), op->stream));
   BDDA_CUDA(cudaMemcpy(o->occ.p, occ.data(), nc * sizeof(int), cudaMemcpyHostToDevice));
   BDDA_CUDA(cudaMemcpy(o->tmask.p, tmask.data(), tmask.size(), cudaMemcpyHostToDevice));
   if (!tiles.empty()) BDDA_CUDA(cudaMemcpy(o->tiles.p, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -96,8 +135,11 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
     return BDDA_ERR_INVALID;
   }
   MvpGeom g = op->geom(o);
-  BDDA_CUDA(op->t1[pi].ensure(mvp_t1_elems(g, L) * sizeof(C)));
-  BDDA_CUDA(op->t2[pi].ensure(mvp_t2_elems(g, L) * sizeof(C)));
+  const bool grow = op->t1[pi].bytes < mvp_t1_elems(g, L) * sizeof(C) || op->t2[pi].bytes < mvp_t2_elems(g, L) * sizeof(C);
+  if (grow && st != op->stream) BDDA_TRY_CUDA(order_after(op->stream, st));  // old buffers may be in use on st
+  BDDA_CUDA(op->t1[pi].ensure(mvp_t1_elems(g, L) * sizeof(C), op->stream));
+  BDDA_CUDA(op->t2[pi].ensure(mvp_t2_elems(g, L) * sizeof(C), op->stream));
+  if (grow && st != op->stream) BDDA_TRY_CUDA(order_after(st, op->stream));  // new buffers exist before st uses them
   cudaError_t e = launch_block_mvp<T>(g, op->tables<T>(), x, ldx, y, ldy, L, diag, jpre, op->t1[pi].as<C>(),
                                       op->t2[pi].as<C>(), st, &op->timer, done);
   if (e != cudaSuccess) return cuda_fail(e, "block MVP launch");
@@ -140,26 +182,35 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     if (!make_axis_plan(op->P[i], &op->plan[i])) { set_error("no FFT plan for the padded grid"); return BDDA_ERR_INVALID; }
   }
   BDDA_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  keep_pool_memory();
   // twiddles
   for (int i = 0; i < 3; ++i) {
     std::vector<double2> tw;
     make_twiddles(op->P[i], &tw);
-    BDDA_CUDA(op->tw64[i].ensure(tw.size() * sizeof(double2)));
+    BDDA_CUDA(op->tw64[i].ensure(tw.size() * sizeof(double2), op->stream));
     BDDA_CUDA(cudaMemcpy(op->tw64[i].p, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
     std::vector<float2> tf(tw.size());
     for (size_t t = 0; t < tw.size(); ++t) tf[t] = make_float2((float)tw[t].x, (float)tw[t].y);
-    BDDA_CUDA(op->tw32[i].ensure(tf.size() * sizeof(float2)));
+    BDDA_CUDA(op->tw32[i].ensure(tf.size() * sizeof(float2), op->stream));
     BDDA_CUDA(cudaMemcpy(op->tw32[i].p, tf.data(), tf.size() * sizeof(float2), cudaMemcpyHostToDevice));
   }
-  BDDA_CUDA(configure_mvp_kernels<double>());  // sized for the largest line, so every live operator fits
-  BDDA_CUDA(configure_mvp_kernels<float>());
+  {
+    // kernel attributes sized for the largest line, so every live operator fits; once per process
+    static std::once_flag once;
+    static cudaError_t cfg = cudaSuccess;
+    std::call_once(once, [] {
+      cfg = configure_mvp_kernels<double>();
+      if (cfg == cudaSuccess) cfg = configure_mvp_kernels<float>();
+    });
+    BDDA_CUDA(cfg);
+  }
   // Green spectrum
   const int Px = op->P[0], Py = op->P[1], Pz = op->P[2];
   const size_t ng = (size_t)Px * Py * Pz;
   DevBuf work;
-  BDDA_CUDA(work.ensure(6 * ng * sizeof(double2)));
-  if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure(6 * ng * sizeof(double2)));
-  if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure(6 * ng * sizeof(float2)));
+  BDDA_CUDA(work.ensure(6 * ng * sizeof(double2), op->stream));
+  if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure(6 * ng * sizeof(double2), op->stream));
+  if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure(6 * ng * sizeof(float2), op->stream));
   MvpGeom g = op->geom(op->dip);
   BDDA_CUDA(build_green_hat(g, lf, k_re, k_im, op->tw64[0].as<double2>(), op->tw64[1].as<double2>(),
                             op->tw64[2].as<double2>(), work.as<double2>(), op->ghat64.as<double2>(),
@@ -201,8 +252,8 @@ int bdda_mbt_fft_mvp(bdda_op* op, const double* p_hat, double* q_hat) {
   }
   const size_t nrow = 3 * (size_t)op->cub.nocc;
   DevBuf x, y;
-  BDDA_CUDA(x.ensure(nrow * sizeof(double2)));
-  BDDA_CUDA(y.ensure(nrow * sizeof(double2)));
+  BDDA_CUDA(x.ensure(nrow * sizeof(double2), op->stream));
+  BDDA_CUDA(y.ensure(nrow * sizeof(double2), op->stream));
   BDDA_CUDA(cudaMemcpyAsync(x.p, p_hat, nrow * sizeof(double2), cudaMemcpyHostToDevice, op->stream));
   int rc = op_block_mvp<double>(op, op->cub, x.as<double2>(), (int)nrow, y.as<double2>(), (int)nrow, 1, nullptr, nullptr,
                                 op->stream);

@@ -16,24 +16,37 @@ namespace bdda {
 void set_error(const std::string& msg);
 const char* last_error();
 
-// RAII device buffer.
+// RAII device buffer on the stream-ordered allocator: allocation and release
+// are ordered on the owning stream (cudaMallocAsync / cudaFreeAsync), so
+// freeing an operator never synchronises the device and concurrent solves on
+// other streams keep running.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
-  void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
-  cudaError_t ensure(size_t b) {
+  void release() {
+    if (p) cudaFreeAsync(p, stream);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t b, cudaStream_t st) {
     if (b <= bytes) return cudaSuccess;
     release();
-    cudaError_t e = cudaMalloc(&p, b);
+    stream = st;
+    cudaError_t e = cudaMallocAsync(&p, b, st);
     if (e == cudaSuccess) bytes = b; else p = nullptr;
     return e;
   }
   template <typename X> X* as() const { return static_cast<X*>(p); }
 };
+
+// Keep freed stream-ordered memory in the device pool (no release to the OS
+// at every synchronisation); called once per device.
+void keep_pool_memory();
 
 // Occupancy of the lattice by dipoles, on the device.
 struct Occupancy {
@@ -85,6 +98,9 @@ template <> inline MvpPrec<double> Op::tables<double>() const {
 template <> inline MvpPrec<float> Op::tables<float>() const {
   return {tw32[0].as<float2>(), tw32[1].as<float2>(), tw32[2].as<float2>(), ghat32.as<float2>()};
 }
+
+// Make stream 'later' wait for the work enqueued so far on 'earlier'.
+cudaError_t order_after(cudaStream_t later, cudaStream_t earlier);
 
 // Build the occupancy tables from a host list of lattice addresses (null -> all sites).
 int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o);

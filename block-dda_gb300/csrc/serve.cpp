@@ -1,0 +1,281 @@
+// Request server and batched solves: many targets of uneven size and nrhs on
+// one GPU, admitted by device-memory footprint and run concurrently.
+//
+// Replaces the reference's sequential wavelength x target loop
+// (block_DDA_main.cpp:138-163: one target at a time, full re-initialisation
+// per target, no overlap).  Each admitted request gets its own operator
+// (Green spectrum of its box and wavenumber), its own stream and its own
+// Krylov workspace, all resident in HBM until the request completes; worker
+// slots run requests concurrently so that small targets fill the GPU together.
+//
+// Admission: requests are considered in arrival order; the head of the queue
+// is admitted as soon as its footprint fits in the memory budget.  A later
+// request that fits may start before a head that does not, but at most
+// kMaxBypass times per head request, so large requests cannot starve.  A
+// request whose footprint exceeds the whole budget is rejected at submission.
+//
+// Results do not depend on the mix: every solve uses only its own buffers and
+// fixed-order reductions, so a request computes bitwise the same X alone or
+// among others.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/bdda.h"
+
+namespace bdda {
+void set_error(const std::string& msg);
+}
+
+namespace {
+
+constexpr int kMaxBypass = 8;
+
+int smooth235(int v) {
+  for (;; ++v) {
+    int t = v;
+    for (int p : {2, 3, 5})
+      while (t % p == 0) t /= p;
+    if (t == 1) return v;
+  }
+}
+
+double footprint_bytes(const int n[3], int nocc, int L, int precision) {
+  const double Px = smooth235(2 * n[0]), Py = smooth235(2 * n[1]), Pz = smooth235(2 * n[2]);
+  const double Ng = Px * Py * Pz;
+  const double nc = (double)n[0] * n[1] * n[2];
+  const bool mixed = precision == BDDA_SOLVE_MIXED;
+  const double tables = 6.0 * Ng * (16.0 + (mixed ? 8.0 : 0.0));
+  const double init_work = 6.0 * Ng * 16.0;
+  const double occ = nc * 4.0 + (double)n[1] * ((n[2] + 7) / 8) * 5.0;
+  const double t1 = 3.0 * L * Px * n[1] * n[2], t2 = 3.0 * L * Px * Py * n[2];
+  const double mvp = (t1 + t2) * (16.0 + (mixed ? 8.0 : 0.0));
+  const double nu = 3.0 * nocc, LL = (double)L * L;
+  const double blocks = 10.0 * nu * L * (mixed ? 8.0 : 16.0) + 3.0 * nu * L * 16.0 + nu * 32.0;
+  const double small = 2.0 * LL * 152.0 * 16.0 + 2.0 * std::max(608.0 * L, 1216.0) * 16.0 + LL * 16.0 * 20.0 + 8.0 * 4096;
+  const double io = nu * 16.0 + 2.0 * nu * L * 16.0;
+  const double peak = std::max(tables + init_work + occ, tables + occ + mvp + blocks + small + io);
+  return peak * 1.05 + 8.0 * (1 << 20);
+}
+
+double now_s(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+struct bdda_server {
+  struct Item {
+    bdda_request req;
+    long long ticket;
+    double footprint;
+    double t_submit;
+    int bypassed = 0;
+  };
+
+  int slots;
+  double budget;
+  bdda_solve_opts opts;
+  bool dry;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Item> pending;
+  std::unordered_map<long long, bdda_request_result> done;
+  double in_use = 0, peak_in_use = 0;
+  int running = 0, peak_running = 0;
+  long long completed = 0, next_ticket = 1;
+  bool stopping = false;
+  std::vector<std::thread> threads;
+
+  // index of the request to admit now, or -1 (caller holds mu)
+  int pick() const {
+    if (pending.empty()) return -1;
+    if (in_use + pending.front().footprint <= budget) return 0;
+    if (pending.front().bypassed >= kMaxBypass) return -1;
+    for (size_t i = 1; i < pending.size(); ++i)
+      if (in_use + pending[i].footprint <= budget) return (int)i;
+    return -1;
+  }
+
+  void execute(const Item& it, bdda_request_result* res) {
+    const bdda_request& r = it.req;
+    if (dry) {
+      // no device work: hold the slot for a time proportional to the footprint
+      std::this_thread::sleep_for(std::chrono::microseconds((long long)(it.footprint / 1e6 * 200.0) + 200));
+      res->status = BDDA_OK;
+      return;
+    }
+    bdda_op* op = nullptr;
+    const int prec = BDDA_PREC_FP64 | (opts.precision == BDDA_SOLVE_MIXED ? BDDA_PREC_FP32 : 0);
+    int rc = bdda_op_create(&op, r.n, 3, r.lf, r.k_re, r.k_im, prec);
+    if (rc == BDDA_OK) rc = bdda_op_set_dipoles(op, r.address, r.nocc);
+    bdda_solve_stats st{};
+    if (rc == BDDA_OK) rc = bdda_solve(op, &opts, r.diag, r.B, 3 * r.nocc, r.X, 3 * r.nocc, r.L, &st);
+    if (op) bdda_op_destroy(op);
+    res->status = rc;
+    res->iterations = st.iterations;
+    res->refinements = st.refinements;
+    res->true_res_max = st.true_res_max;
+  }
+
+  void worker() {
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+      cv_work.wait(lk, [&] { return (stopping && pending.empty()) || pick() >= 0; });
+      if (stopping && pending.empty()) return;
+      const int i = pick();
+      if (i < 0) continue;
+      if (i > 0) pending.front().bypassed++;
+      Item it = pending[i];
+      pending.erase(pending.begin() + i);
+      in_use += it.footprint;
+      peak_in_use = std::max(peak_in_use, in_use);
+      peak_running = std::max(peak_running, ++running);
+      bdda_request_result res{};
+      res.t_submit = it.t_submit;
+      res.t_start = now_s(t0);
+      res.footprint_bytes = it.footprint;
+      lk.unlock();
+      execute(it, &res);
+      res.t_done = now_s(t0);
+      lk.lock();
+      in_use -= it.footprint;
+      --running;
+      ++completed;
+      done[it.ticket] = res;
+      cv_done.notify_all();
+      cv_work.notify_all();
+    }
+  }
+};
+
+extern "C" {
+
+double bdda_request_footprint(const int n[3], int nocc, int L, int precision) {
+  if (!n || nocc < 1 || L < 1) return -1.0;
+  return footprint_bytes(n, nocc, L, precision);
+}
+
+int bdda_server_create(bdda_server** out, int slots, double mem_budget_bytes, const bdda_solve_opts* opts, int dry_run) {
+  if (!out || slots < 1 || slots > 256 || !(mem_budget_bytes > 0) || !opts) {
+    bdda::set_error("bad server arguments");
+    return BDDA_ERR_INVALID;
+  }
+  if (opts->true_tol <= 0) {
+    bdda::set_error("the server solves to a true residual: set opts.true_tol > 0");
+    return BDDA_ERR_INVALID;
+  }
+  bdda_server* s = new bdda_server();
+  s->slots = slots;
+  s->budget = mem_budget_bytes;
+  s->opts = *opts;
+  s->dry = dry_run != 0;
+  for (int i = 0; i < slots; ++i) s->threads.emplace_back([s] { s->worker(); });
+  *out = s;
+  return BDDA_OK;
+}
+
+int bdda_server_submit(bdda_server* s, const bdda_request* r, long long* ticket) {
+  if (!s || !r || !ticket || r->nocc < 1 || r->L < 1 || r->L > 32 || !r->address || !r->diag || !r->B || !r->X) {
+    bdda::set_error("bad request");
+    return BDDA_ERR_INVALID;
+  }
+  const double fp = footprint_bytes(r->n, r->nocc, r->L, s->opts.precision);
+  if (fp > s->budget) {
+    bdda::set_error("request footprint " + std::to_string((long long)fp) + " bytes exceeds the server memory budget");
+    return BDDA_ERR_NOMEM;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stopping) {
+    bdda::set_error("server is shutting down");
+    return BDDA_ERR_INVALID;
+  }
+  bdda_server::Item it;
+  it.req = *r;
+  it.ticket = s->next_ticket++;
+  it.footprint = fp;
+  it.t_submit = now_s(s->t0);
+  s->pending.push_back(it);
+  *ticket = it.ticket;
+  s->cv_work.notify_all();
+  return BDDA_OK;
+}
+
+int bdda_server_wait(bdda_server* s, long long ticket, bdda_request_result* res) {
+  if (!s || !res) {
+    bdda::set_error("bad wait arguments");
+    return BDDA_ERR_INVALID;
+  }
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (ticket < 1 || ticket >= s->next_ticket) {
+    bdda::set_error("unknown ticket");
+    return BDDA_ERR_INVALID;
+  }
+  s->cv_done.wait(lk, [&] { return s->done.count(ticket) != 0; });
+  *res = s->done[ticket];
+  s->done.erase(ticket);
+  if (res->status != BDDA_OK) bdda::set_error("request failed with status " + std::to_string(res->status));
+  return res->status;
+}
+
+int bdda_server_stats(bdda_server* s, double* peak_inflight_bytes, int* peak_running, long long* completed) {
+  if (!s) {
+    bdda::set_error("null server");
+    return BDDA_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (peak_inflight_bytes) *peak_inflight_bytes = s->peak_in_use;
+  if (peak_running) *peak_running = s->peak_running;
+  if (completed) *completed = s->completed;
+  return BDDA_OK;
+}
+
+int bdda_server_destroy(bdda_server* s) {
+  if (!s) return BDDA_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stopping = true;
+    s->cv_work.notify_all();
+  }
+  for (auto& t : s->threads) t.join();
+  delete s;
+  return BDDA_OK;
+}
+
+int bdda_batch_solve(const bdda_request* reqs, int count, int slots, double mem_budget_bytes, const bdda_solve_opts* opts,
+                     bdda_request_result* results) {
+  if (!reqs || count < 1 || !results) {
+    bdda::set_error("bad batch arguments");
+    return BDDA_ERR_INVALID;
+  }
+  bdda_server* s = nullptr;
+  int rc = bdda_server_create(&s, slots, mem_budget_bytes, opts, 0);
+  if (rc) return rc;
+  std::vector<long long> tickets(count, 0);
+  int first_err = BDDA_OK;
+  for (int i = 0; i < count; ++i) {
+    rc = bdda_server_submit(s, &reqs[i], &tickets[i]);
+    if (rc != BDDA_OK) {
+      std::memset(&results[i], 0, sizeof(results[i]));
+      results[i].status = rc;
+      if (!first_err) first_err = rc;
+    }
+  }
+  for (int i = 0; i < count; ++i) {
+    if (!tickets[i]) continue;
+    rc = bdda_server_wait(s, tickets[i], &results[i]);
+    if (rc != BDDA_OK && !first_err) first_err = rc;
+  }
+  bdda_server_destroy(s);
+  return first_err;
+}
+
+}  // extern "C"

@@ -26,15 +26,34 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
 __device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 
-// dst[e] = sum_p partials[p*LL + e] in order p = 0..nparts-1
+// dst[e] = sum over p of partials[p*LL + e].  16 independent accumulators
+// (partial p goes to accumulator p mod 16), combined in a fixed order: the
+// loads of one round are in flight together and the result is bitwise
+// reproducible for a given nparts.
 __device__ void sm_reduce(double2* dst, const double2* __restrict__ partials, int nparts, int LL) {
+  constexpr int U = 16;
   for (int e = threadIdx.x; e < LL; e += blockDim.x) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int p = 0; p < nparts; ++p) {
-      const double2 v = partials[(size_t)p * LL + e];
-      s.x += v.x;
-      s.y += v.y;
+    double2 acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc[u] = make_double2(0.0, 0.0);
+    int p = 0;
+    for (; p + U <= nparts; p += U) {
+      double2 v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) v[u] = __ldg(partials + (size_t)(p + u) * LL + e);
+#pragma unroll
+      for (int u = 0; u < U; ++u) { acc[u].x += v[u].x; acc[u].y += v[u].y; }
     }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (p + u < nparts) {
+        const double2 v = __ldg(partials + (size_t)(p + u) * LL + e);
+        acc[u].x += v.x;
+        acc[u].y += v.y;
+      }
+    double2 s = acc[0];
+#pragma unroll
+    for (int u = 1; u < U; ++u) { s.x += acc[u].x; s.y += acc[u].y; }
     dst[e] = s;
   }
   __syncthreads();
@@ -123,13 +142,16 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
     }
     __syncthreads();
     if (bad) continue;
-    // ---- eliminate below the pivot
+    // ---- multipliers (one complex division per row), then the trailing update
     const double2 p = A[k + k * L];
+    const double2 pinv = cdiv(make_double2(1.0, 0.0), p);
+    for (int i = k + 1 + tid; i < L; i += blockDim.x) A[i + k * L] = cmul(A[i + k * L], pinv);
+    __syncthreads();
     const int rows = L - k - 1;
     for (int t = tid; t < rows * (L - k - 1 + nrhs); t += blockDim.x) {
       const int i = k + 1 + t % rows;
       const int jj = t / rows;  // 0..(L-k-2) -> A columns k+1.., then B columns
-      const double2 f = cdiv(A[i + k * L], p);
+      const double2 f = A[i + k * L];
       if (jj < L - k - 1) {
         const int j = k + 1 + jj;
         A[i + j * L] = csub(A[i + j * L], cmul(f, A[k + j * L]));
@@ -139,15 +161,18 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
       }
     }
     __syncthreads();
-    for (int i = k + 1 + tid; i < L; i += blockDim.x) A[i + k * L] = cdiv(A[i + k * L], p);  // store multipliers
-    __syncthreads();
   }
-  // ---- back substitution, one thread per right-hand side
+  // ---- back substitution, one thread per right-hand side (reciprocal pivots first)
+  for (int k = tid; k < L; k += blockDim.x) {
+    const double2 inv = cdiv(make_double2(1.0, 0.0), A[k + k * L]);
+    A[k + k * L] = inv;  // the diagonal now holds 1 / pivot
+  }
+  __syncthreads();
   for (int j = tid; j < nrhs; j += blockDim.x) {
     for (int k = L - 1; k >= 0; --k) {
       double2 s = B[k + j * L];
       for (int c = k + 1; c < L; ++c) s = csub(s, cmul(A[k + c * L], B[c + j * L]));
-      B[k + j * L] = cdiv(s, A[k + k * L]);
+      B[k + j * L] = cmul(s, A[k + k * L]);
     }
   }
   __syncthreads();
@@ -186,11 +211,11 @@ __device__ bool sm_cholesky(double2* R, const double2* H, int L) {
       R[k + k * L] = make_double2(sqrt(d), 0.0);
     }
     __syncthreads();
-    const double rkk = R[k + k * L].x;
+    const double rinv = 1.0 / R[k + k * L].x;
     for (int j = k + 1 + tid; j < L; j += blockDim.x) {
       double2 s = R[k + j * L];
       for (int i = 0; i < k; ++i) s = csub(s, cconjmul(R[i + k * L], R[i + j * L]));
-      R[k + j * L] = make_double2(s.x / rkk, s.y / rkk);
+      R[k + j * L] = make_double2(s.x * rinv, s.y * rinv);
     }
     __syncthreads();
   }
@@ -205,14 +230,18 @@ __device__ bool sm_cholesky(double2* R, const double2* H, int L) {
   return ok;
 }
 
-// Inverse of an upper triangular matrix (one thread per column).
+// Inverse of an upper triangular matrix with a real positive diagonal (the
+// Cholesky factors): one thread per column, diagonal reciprocals precomputed.
 __device__ void sm_tri_inv(double2* Ri, const double2* R, int L) {
+  __shared__ double dinv[kMaxL];
+  for (int i = threadIdx.x; i < L; i += blockDim.x) dinv[i] = 1.0 / R[i + i * L].x;
+  __syncthreads();
   for (int j = threadIdx.x; j < L; j += blockDim.x) {
     for (int i = L - 1; i >= 0; --i) {
       if (i > j) { Ri[i + j * L] = make_double2(0.0, 0.0); continue; }
       double2 s = make_double2(i == j ? 1.0 : 0.0, 0.0);
       for (int k = i + 1; k <= j; ++k) s = csub(s, cmul(R[i + k * L], Ri[k + j * L]));
-      Ri[i + j * L] = cdiv(s, R[i + i * L]);
+      Ri[i + j * L] = make_double2(s.x * dinv[i], s.y * dinv[i]);
     }
   }
   __syncthreads();

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/bdda.h"
@@ -36,8 +37,8 @@ struct SolverWork {
   DevBuf small;                 // c128 [kNumSlots][L*L] + scalars
   DevBuf ctl;                   // SolverCtl
   DevBuf hist;                  // double[itermax]
-  SolverCtl* ctl_host = nullptr;
-  ~SolverWork() { if (ctl_host) cudaFreeHost(ctl_host); }
+  SolverCtl ctl_host_buf{};           // pageable: the poll copy completes before returning
+  SolverCtl* ctl_host = &ctl_host_buf;
 };
 
 namespace {
@@ -57,7 +58,7 @@ int cuda_fail(cudaError_t e, const char* where) {
     if (_rc != BDDA_OK) return _rc; \
   } while (0)
 
-inline int gram_grid(int n) { return std::max(1, std::min(296, (n + 127) / 128)); }
+inline int gram_grid(int n) { return std::max(1, std::min(152, (n + 127) / 128)); }
 inline int vec_grid(size_t total) { return (int)std::max<size_t>(1, std::min<size_t>(608, (total + 255) / 256)); }
 
 __device__ __forceinline__ double2* slot(double2* st, int s, int L) { return st + (size_t)s * L * L; }
@@ -529,39 +530,42 @@ static int ensure_work(Op* op, int n, int L, int itermax, bool need64, bool need
   SolverWork* w = op->solver.get();
   const size_t b64 = sizeof(double2) * (size_t)n * L, b32 = sizeof(float2) * (size_t)n * L;
   for (int i = 0; i < 10; ++i) {
-    if (need64) BDDA_CUDA(w->blk64[i].ensure(b64));
-    if (need32) BDDA_CUDA(w->blk32[i].ensure(b32));
+    if (need64) BDDA_CUDA(w->blk64[i].ensure(b64, op->stream));
+    if (need32) BDDA_CUDA(w->blk32[i].ensure(b32, op->stream));
   }
-  BDDA_CUDA(w->X64.ensure(b64));
-  BDDA_CUDA(w->R64.ensure(b64));
-  BDDA_CUDA(w->Y64.ensure(b64));
-  BDDA_CUDA(w->jpre64.ensure(sizeof(double2) * (size_t)n));
-  BDDA_CUDA(w->diag32.ensure(sizeof(float2) * (size_t)n));
-  BDDA_CUDA(w->jpre32.ensure(sizeof(float2) * (size_t)n));
+  BDDA_CUDA(w->X64.ensure(b64, op->stream));
+  BDDA_CUDA(w->R64.ensure(b64, op->stream));
+  BDDA_CUDA(w->Y64.ensure(b64, op->stream));
+  BDDA_CUDA(w->jpre64.ensure(sizeof(double2) * (size_t)n, op->stream));
+  BDDA_CUDA(w->diag32.ensure(sizeof(float2) * (size_t)n, op->stream));
+  BDDA_CUDA(w->jpre32.ensure(sizeof(float2) * (size_t)n, op->stream));
   const size_t LL = (size_t)L * L;
-  BDDA_CUDA(w->partials.ensure(sizeof(double2) * LL * gram_grid(n)));
-  BDDA_CUDA(w->partials2.ensure(sizeof(double2) * LL * gram_grid(n)));
-  BDDA_CUDA(w->vpart.ensure(sizeof(double2) * 2 * (size_t)std::max(vec_grid((size_t)n * L) * L, 2 * 608)));
-  BDDA_CUDA(w->small.ensure(sizeof(double2) * (LL * kNumSlots + 8)));
-  BDDA_CUDA(w->ctl.ensure(sizeof(SolverCtl)));
-  BDDA_CUDA(w->hist.ensure(sizeof(double) * (size_t)std::max(1, itermax)));
-  if (!w->ctl_host) BDDA_CUDA(cudaMallocHost(&w->ctl_host, sizeof(SolverCtl)));
+  BDDA_CUDA(w->partials.ensure(sizeof(double2) * LL * gram_grid(n), op->stream));
+  BDDA_CUDA(w->partials2.ensure(sizeof(double2) * LL * gram_grid(n), op->stream));
+  BDDA_CUDA(w->vpart.ensure(sizeof(double2) * 2 * (size_t)std::max(vec_grid((size_t)n * L) * L, 2 * 608), op->stream));
+  BDDA_CUDA(w->small.ensure(sizeof(double2) * (LL * kNumSlots + 8), op->stream));
+  BDDA_CUDA(w->ctl.ensure(sizeof(SolverCtl), op->stream));
+  BDDA_CUDA(w->hist.ensure(sizeof(double) * (size_t)std::max(1, itermax), op->stream));
   w->n = n;
   w->L = L;
-  static bool attr_done = false;
-  if (!attr_done) {
+  static std::once_flag attr_once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr_once, [] {
+    auto set = [](const void* f, int b) {
+      const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+      if (e != cudaSuccess) attr_err = e;
+    };
     const int mx = (int)SmallSmem::bytes(kMaxL);
-    BDDA_CUDA(cudaFuncSetAttribute(k_small_chol1, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    BDDA_CUDA(cudaFuncSetAttribute(k_small_chol2, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    BDDA_CUDA(cudaFuncSetAttribute(k_small_cocg_alpha, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    BDDA_CUDA(cudaFuncSetAttribute(k_small_cocg_beta, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    BDDA_CUDA(cudaFuncSetAttribute(k_small_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    BDDA_CUDA(cudaFuncSetAttribute(k_small_store_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    const int r64 = rowmm_smem<double>(kMaxL, true), r32 = rowmm_smem<float>(kMaxL, true);
-    BDDA_CUDA(cudaFuncSetAttribute(k_rowmm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, r64));
-    BDDA_CUDA(cudaFuncSetAttribute(k_rowmm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, r32));
-    attr_done = true;
-  }
+    set((const void*)k_small_chol1, mx);
+    set((const void*)k_small_chol2, mx);
+    set((const void*)k_small_cocg_alpha, mx);
+    set((const void*)k_small_cocg_beta, mx);
+    set((const void*)k_small_solve, mx);
+    set((const void*)k_small_store_reduce, mx);
+    set((const void*)k_rowmm<double>, rowmm_smem<double>(kMaxL, true));
+    set((const void*)k_rowmm<float>, rowmm_smem<float>(kMaxL, true));
+  });
+  BDDA_CUDA(attr_err);
   return BDDA_OK;
 }
 
@@ -614,7 +618,10 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
   }
   const bool refine = o->true_tol > 0;
   const int itermax = o->itermax > 0 ? o->itermax : 300;
+  // workspace lives on the operator's stream; order it against a caller's stream
+  if (st != op->stream) BDDA_CUDA(order_after(op->stream, st));
   BDDA_TRY(ensure_work(op, n, L, itermax, !mixed, mixed));
+  if (st != op->stream) BDDA_CUDA(order_after(st, op->stream));
   SolverWork* w = op->solver.get();
   const int check_every = o->check_every > 0 ? o->check_every : 4;
   cudaEvent_t e0, e1;
@@ -749,9 +756,9 @@ int bdda_solve(bdda_op* op, const bdda_solve_opts* opts, const double* diag, con
   if (ldb < n || ldx < n || L < 1) { set_error("bad leading dimension or nrhs"); return BDDA_ERR_INVALID; }
   cudaStream_t st = op->stream;
   DevBuf d, b, x;
-  BDDA_CUDA(d.ensure(sizeof(double2) * (size_t)n));
-  BDDA_CUDA(b.ensure(sizeof(double2) * (size_t)n * L));
-  BDDA_CUDA(x.ensure(sizeof(double2) * (size_t)n * L));
+  BDDA_CUDA(d.ensure(sizeof(double2) * (size_t)n, op->stream));
+  BDDA_CUDA(b.ensure(sizeof(double2) * (size_t)n * L, op->stream));
+  BDDA_CUDA(x.ensure(sizeof(double2) * (size_t)n * L, op->stream));
   BDDA_CUDA(cudaMemcpyAsync(d.p, diag, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
   BDDA_CUDA(cudaMemcpy2DAsync(b.p, sizeof(double2) * n, B, sizeof(double2) * (size_t)ldb, sizeof(double2) * n, L,
                               cudaMemcpyHostToDevice, st));
@@ -769,33 +776,36 @@ int bdda_qr_reduced(const double* A, int m, int nc, int lda, double* Q, int ldq,
     set_error("bad qr_reduced arguments");
     return BDDA_ERR_INVALID;
   }
-  cudaStream_t st;
-  BDDA_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  Op tmp;  // bookkeeping only (timer, workspace); no tables
+  Op tmp;  // bookkeeping only (stream, timer, workspace); no tables
+  BDDA_CUDA(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking));
+  keep_pool_memory();
+  const cudaStream_t st = tmp.stream;
   int rc = ensure_work(&tmp, m, nc, 1, true, false);
-  if (rc) { cudaStreamDestroy(st); return rc; }
+  if (rc) return rc;
   SolverWork* w = tmp.solver.get();
   Krylov<double> kr{&tmp, w, st, m, nc, nullptr, nullptr, 4};
   double2* a = w->blk64[0].as<double2>();
   double2* q = w->blk64[1].as<double2>();
   double2* s = w->blk64[2].as<double2>();
-  cudaMemcpy2DAsync(a, sizeof(double2) * m, A, sizeof(double2) * (size_t)lda, sizeof(double2) * m, nc, cudaMemcpyHostToDevice, st);
-  // ctl reset with a unit norm so the init kernel does not flag a zero block
+  BDDA_CUDA(cudaMemcpy2DAsync(a, sizeof(double2) * m, A, sizeof(double2) * (size_t)lda, sizeof(double2) * m, nc,
+                              cudaMemcpyHostToDevice, st));
   rc = kr.init(a);
-  if (rc == BDDA_OK) {
-    kr.cholqr2(a, s, q, 2);
-    std::vector<double2> hr((size_t)nc * nc);
-    cudaMemcpy2DAsync(Q, sizeof(double2) * (size_t)ldq, q, sizeof(double2) * m, sizeof(double2) * m, nc, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(hr.data(), kr.sl(kXi), sizeof(double2) * hr.size(), cudaMemcpyDeviceToHost, st);
-    bool done = false;
-    kr.poll(&done);
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) rc = cuda_fail(e, "qr_reduced");
-    else if (w->ctl_host->status != 0) { set_error("qr_reduced: rank-deficient block (Cholesky failed)"); rc = BDDA_ERR_BREAKDOWN; }
-    std::memcpy(R, hr.data(), sizeof(double2) * hr.size());
+  if (rc != BDDA_OK) return rc;
+  kr.cholqr2(a, s, q, 2);
+  std::vector<double2> hr((size_t)nc * nc);
+  BDDA_CUDA(cudaMemcpy2DAsync(Q, sizeof(double2) * (size_t)ldq, q, sizeof(double2) * m, sizeof(double2) * m, nc,
+                              cudaMemcpyDeviceToHost, st));
+  BDDA_CUDA(cudaMemcpyAsync(hr.data(), kr.sl(kXi), sizeof(double2) * hr.size(), cudaMemcpyDeviceToHost, st));
+  bool done = false;
+  rc = kr.poll(&done);
+  if (rc != BDDA_OK) return rc;
+  BDDA_CUDA(cudaStreamSynchronize(st));
+  if (w->ctl_host->status != 0) {
+    set_error("qr_reduced: rank-deficient block (Cholesky failed)");
+    return BDDA_ERR_BREAKDOWN;
   }
-  cudaStreamDestroy(st);
-  return rc;
+  std::memcpy(R, hr.data(), sizeof(double2) * hr.size());
+  return BDDA_OK;
 }
 
 }  // extern "C"

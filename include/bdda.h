@@ -160,6 +160,61 @@ int bdda_solve(bdda_op* op, const bdda_solve_opts* opts, const double* diag, con
  */
 int bdda_qr_reduced(const double* A, int m, int n, int lda, double* Q, int ldq, double* R);
 
+/* ---- batched solves and the request server ------------------------------- */
+/*
+ * Replace the reference's sequential wavelength x target loop
+ * (block_DDA_main.cpp:138-163) with concurrent solves on one GPU.  A request
+ * is one target: its box, spacing, wavenumber, dipole addresses, DIAG_A and
+ * right-hand sides (host buffers that must stay valid until the request is
+ * done; X receives the solution).
+ */
+typedef struct {
+  int n[3];
+  double lf;
+  double k_re, k_im;
+  const int* address;
+  int nocc;
+  const double* diag;   /* 3*nocc complex */
+  const double* B;      /* 3*nocc x L complex, column-major, ld 3*nocc */
+  int L;                /* 1..32 */
+  double* X;            /* 3*nocc x L complex output */
+} bdda_request;
+
+typedef struct {
+  int status;             /* BDDA_OK or the solve's error code */
+  int iterations;
+  int refinements;
+  double true_res_max;
+  double t_submit, t_start, t_done;   /* seconds since the server started (steady clock) */
+  double footprint_bytes;             /* device memory reserved for the request */
+} bdda_request_result;
+
+/* Device-memory footprint the server reserves for one request (bytes). */
+double bdda_request_footprint(const int n[3], int nocc, int L, int precision);
+
+typedef struct bdda_server bdda_server;
+
+/*
+ * Start a server with `slots` concurrent solves and a device-memory budget.
+ * Requests are admitted in arrival order when their footprint fits the
+ * budget; a later request that fits may overtake a waiting head at most 8
+ * times.  opts must ask for a true residual (true_tol > 0).  dry_run != 0
+ * runs no device work (each request just holds its slot and memory for a
+ * time proportional to its footprint) -- for testing admission and queueing.
+ */
+int bdda_server_create(bdda_server** s, int slots, double mem_budget_bytes, const bdda_solve_opts* opts, int dry_run);
+/* Queue a request; BDDA_ERR_NOMEM if its footprint exceeds the whole budget. */
+int bdda_server_submit(bdda_server* s, const bdda_request* r, long long* ticket);
+/* Block until the request is done; returns its status and fills res. */
+int bdda_server_wait(bdda_server* s, long long ticket, bdda_request_result* res);
+/* Peak reserved memory, peak concurrent requests, completed requests. */
+int bdda_server_stats(bdda_server* s, double* peak_inflight_bytes, int* peak_running, long long* completed);
+/* Drain the queue, join the workers, free the server. */
+int bdda_server_destroy(bdda_server* s);
+/* Solve `count` requests concurrently (a server submitted all at once). */
+int bdda_batch_solve(const bdda_request* reqs, int count, int slots, double mem_budget_bytes,
+                     const bdda_solve_opts* opts, bdda_request_result* results);
+
 /* ---- target, fields and cross sections (host) --------------------------- */
 
 /*
