@@ -19,7 +19,7 @@ from . import build as _build
 _LIB = None
 
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_BREAKDOWN, ERR_NOT_CONVERGED = 0, 1, 2, 3, 4, 5
-PREC_FP64, PREC_FP32 = 1, 2
+PREC_FP64, PREC_FP32, PREC_DF64 = 1, 2, 4
 SOLVER_COCG_RQ, SOLVER_BICGSTAB, SOLVER_BICGGR = 0, 1, 2
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 SOLVERS = {"cocg_rq": SOLVER_COCG_RQ, "bicgstab": SOLVER_BICGSTAB, "bicggr": SOLVER_BICGGR}
@@ -154,7 +154,7 @@ def _cmat(a, rows=None):
 class Operator:
     """Green-tensor operator of one lattice box (``bdda_op``)."""
 
-    def __init__(self, n, lf, k, prec=PREC_FP64 | PREC_FP32, f=3):
+    def __init__(self, n, lf, k, prec=PREC_FP64 | PREC_FP32 | PREC_DF64, f=3):
         self._h = ct.c_void_p()
         n3 = np.ascontiguousarray(n, dtype=np.int32)
         k = complex(k)

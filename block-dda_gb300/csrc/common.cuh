@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <cmath>
 #include <cstdint>
 
 #if defined(__CUDACC__)
@@ -12,13 +13,59 @@
 
 namespace bdda {
 
-// Complex value types: c64 = float2 (complex FP32), c128 = double2 (complex FP64).
+// ---------------------------------------------------------------------------
+// Double-float scalar: value = hi + lo with |lo| <= ulp(hi)/2 (about 48
+// significant bits), computed with FP32 instructions only.  GB300's FP32 pipes
+// run ~64x the FP64 rate, so an FFT in double-float arithmetic is several
+// times faster than in FP64 while keeping the refinement residual accurate to
+// ~1e-14.  Sums use the two-sum of Knuth, products the FMA-based two-product;
+// the addition is the short ("sloppy") variant whose error is bounded
+// relative to |a| + |b|, which is what FFT error analysis needs.
+// ---------------------------------------------------------------------------
+struct __align__(8) dfl {
+  float hi, lo;
+  dfl() = default;
+  BDDA_HD constexpr dfl(float h, float l) : hi(h), lo(l) {}
+  BDDA_HD constexpr dfl(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+  BDDA_HD constexpr dfl(int v) : hi((float)v), lo(0.0f) {}
+};
+BDDA_HD dfl df_quick_two_sum(float a, float b) {
+  const float s = a + b;
+  return dfl(s, b - (s - a));
+}
+BDDA_HD dfl operator+(dfl a, dfl b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  return df_quick_two_sum(s, e);
+}
+BDDA_HD dfl operator-(dfl a) { return dfl(-a.hi, -a.lo); }
+BDDA_HD dfl operator-(dfl a, dfl b) { return a + (-b); }
+BDDA_HD dfl operator*(dfl a, dfl b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);  // exact low part of a.hi * b.hi
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_quick_two_sum(p, e);
+}
+BDDA_HD double df_to_double(dfl a) { return (double)a.hi + (double)a.lo; }
+
+// Complex double-float (16 bytes, the size of a complex FP64 value).
+struct __align__(16) dfc {
+  dfl x, y;
+};
+
+// Complex value types: c64 = float2 (complex FP32), c128 = double2 (complex
+// FP64), dfc (complex double-float).
 template <typename T> struct cplx;
 template <> struct cplx<float> { using type = float2; };
 template <> struct cplx<double> { using type = double2; };
+template <> struct cplx<dfl> { using type = dfc; };
 
 BDDA_HD float2 cmake(float a, float b) { return make_float2(a, b); }
 BDDA_HD double2 cmake(double a, double b) { return make_double2(a, b); }
+BDDA_HD dfc cmake(dfl a, dfl b) { dfc c; c.x = a; c.y = b; return c; }
 
 template <typename C> BDDA_HD C cadd(C a, C b) { return cmake(a.x + b.x, a.y + b.y); }
 template <typename C> BDDA_HD C csub(C a, C b) { return cmake(a.x - b.x, a.y - b.y); }
@@ -34,6 +81,21 @@ template <typename C> BDDA_HD C cconjmul(C a, C b) {
   return cmake(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
 }
 template <typename C> BDDA_HD C czero() { return cmake(decltype(C::x)(0), decltype(C::x)(0)); }
+
+// Read-only load of a complex value through the non-coherent cache.
+#if defined(__CUDACC__)
+__device__ __forceinline__ float2 ldg_c(const float2* p) { return __ldg(p); }
+__device__ __forceinline__ double2 ldg_c(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ dfc ldg_c(const dfc* p) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  dfc c;
+  c.x = dfl(v.x, v.y);
+  c.y = dfl(v.z, v.w);
+  return c;
+}
+#else
+template <typename C> inline C ldg_c(const C* p) { return *p; }
+#endif
 
 // Transform length limits of the warp-per-line FFT.
 constexpr int kMaxLine = 512;   // longest line one warp transforms

@@ -29,7 +29,7 @@
 // walks every butterfly; butterflies of a stage are independent).
 #if defined(__CUDACC__)
 #define BDDA_FFT_FN __device__ __forceinline__
-#define BDDA_LDG(p) __ldg(p)
+#define BDDA_LDG(p) ldg_c(p)
 #define BDDA_SYNCWARP() __syncwarp()
 #else
 #define BDDA_FFT_FN inline

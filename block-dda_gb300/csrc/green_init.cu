@@ -130,7 +130,7 @@ __global__ void k_green_pack(const double2* __restrict__ g, C* __restrict__ out,
 
 cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_im,
                             const double2* twx, const double2* twy, const double2* twz,
-                            double2* work, double2* ghat_d, float2* ghat_f, cudaStream_t st) {
+                            double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, cudaStream_t st) {
   const int Px = g.Px, Py = g.Py, Pz = g.Pz;
   const size_t ng = (size_t)Px * Py * Pz;
   cudaError_t e;
@@ -165,6 +165,7 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
   const double scale = 1.0 / (double)ng;
   if (ghat_d) k_green_pack<double2><<<2432, 256, 0, st>>>(work, ghat_d, Px, Py, Pz, scale);
   if (ghat_f) k_green_pack<float2><<<2432, 256, 0, st>>>(work, ghat_f, Px, Py, Pz, scale);
+  if (ghat_df) k_green_pack<dfc><<<2432, 256, 0, st>>>(work, ghat_df, Px, Py, Pz, scale);
   return cudaGetLastError();
 }
 

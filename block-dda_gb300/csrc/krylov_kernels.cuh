@@ -88,6 +88,44 @@ k_gram(const typename cplx<T>::type* __restrict__ A, int lda,
   }
 }
 
+// out[e] = sum over p of part[p*LL + e], spread over ceil(LL/64) CTAs: thread
+// group g (of 4) sums p = g, g+4, ... with four independent accumulators;
+// the groups are combined in a fixed order (deterministic).
+__global__ void __launch_bounds__(256)
+k_gram_reduce(const double2* __restrict__ part, int nparts, int LL, double2* __restrict__ out, const SolverCtl* ctl) {
+  if (ctl_skip(ctl)) return;
+  __shared__ double2 red[4][64];
+  const int el = threadIdx.x & 63, g = threadIdx.x >> 6;
+  const int e = blockIdx.x * 64 + el;
+  double2 acc[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) acc[u] = make_double2(0.0, 0.0);
+  if (e < LL) {
+    int p = g, u = 0;
+    for (; p + 12 < nparts; p += 16) {
+      const double2 v0 = __ldg(part + (size_t)p * LL + e), v1 = __ldg(part + (size_t)(p + 4) * LL + e);
+      const double2 v2 = __ldg(part + (size_t)(p + 8) * LL + e), v3 = __ldg(part + (size_t)(p + 12) * LL + e);
+      acc[0].x += v0.x; acc[0].y += v0.y;
+      acc[1].x += v1.x; acc[1].y += v1.y;
+      acc[2].x += v2.x; acc[2].y += v2.y;
+      acc[3].x += v3.x; acc[3].y += v3.y;
+    }
+    for (; p < nparts; p += 4, ++u) {
+      const double2 v = __ldg(part + (size_t)p * LL + e);
+      acc[u & 3].x += v.x;
+      acc[u & 3].y += v.y;
+    }
+  }
+  red[g][el] = make_double2(acc[0].x + acc[1].x + acc[2].x + acc[3].x, acc[0].y + acc[1].y + acc[2].y + acc[3].y);
+  __syncthreads();
+  if (g == 0 && e < LL) {
+    double2 s = red[0][el];
+#pragma unroll
+    for (int k = 1; k < 4; ++k) { s.x += red[k][el].x; s.y += red[k][el].y; }
+    out[e] = s;
+  }
+}
+
 // Column sums of |A[r,l]|^2 (squared column norms) -> partials[blk][l] (double)
 template <typename T>
 __global__ void __launch_bounds__(256)
@@ -214,6 +252,24 @@ __global__ void k_convert(int n, int L, const typename cplx<TI>::type* __restric
     const size_t l = idx / n, r = idx - l * n;
     const auto v = in[l * ldi + r];
     out[l * ldo + r] = cmake((TO)v.x, (TO)v.y);
+  }
+}
+
+// complex FP64 <-> complex double-float blocks
+__global__ void k_to_df(int n, int L, const double2* __restrict__ in, int ldi, dfc* __restrict__ out, int ldo) {
+  const size_t total = (size_t)n * L;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = idx / n, r = idx - l * n;
+    const double2 v = in[l * ldi + r];
+    out[l * ldo + r] = cmake(dfl(v.x), dfl(v.y));
+  }
+}
+__global__ void k_from_df(int n, int L, const dfc* __restrict__ in, int ldi, double2* __restrict__ out, int ldo) {
+  const size_t total = (size_t)n * L;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t l = idx / n, r = idx - l * n;
+    const dfc v = in[l * ldi + r];
+    out[l * ldo + r] = make_double2(df_to_double(v.x), df_to_double(v.y));
   }
 }
 

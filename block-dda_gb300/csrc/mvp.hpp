@@ -110,7 +110,7 @@ template <typename T> cudaError_t configure_mvp_kernels();
 // work: c128 [6*Px*Py*Pz].
 cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_im,
                             const double2* twx, const double2* twy, const double2* twz,
-                            double2* work, double2* ghat_d, float2* ghat_f, cudaStream_t st);
+                            double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, cudaStream_t st);
 
 // Radix schedule + FP64 twiddles for a 5-smooth N <= kMaxLine.
 bool make_axis_plan(int N, AxisPlan* p);

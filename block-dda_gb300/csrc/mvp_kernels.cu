@@ -200,8 +200,8 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz,
   for (int p = lane; p < Pz; p += 32) {
     const int sp = skw<C>(p);
     const C a0 = s0[sp], a1 = s1[sp], a2 = s2[sp];
-    const C gxx = __ldg(gl + p), gxy = __ldg(gl + Pz + p), gxz = __ldg(gl + 2 * Pz + p);
-    const C gyy = __ldg(gl + 3 * Pz + p), gyz = __ldg(gl + 4 * Pz + p), gzz = __ldg(gl + 5 * Pz + p);
+    const C gxx = ldg_c(gl + p), gxy = ldg_c(gl + Pz + p), gxz = ldg_c(gl + 2 * Pz + p);
+    const C gyy = ldg_c(gl + 3 * Pz + p), gyz = ldg_c(gl + 4 * Pz + p), gzz = ldg_c(gl + 5 * Pz + p);
     s0[sp] = cadd(cadd(cmul(gxx, a0), cmul(gxy, a1)), cmul(gxz, a2));
     s1[sp] = cadd(cadd(cmul(gxy, a0), cmul(gyy, a1)), cmul(gyz, a2));
     s2[sp] = cadd(cadd(cmul(gxz, a0), cmul(gyz, a1)), cmul(gzz, a2));
@@ -360,7 +360,10 @@ template cudaError_t launch_block_mvp<float>(const MvpGeom&, const MvpPrec<float
 template cudaError_t launch_block_mvp<double>(const MvpGeom&, const MvpPrec<double>&, const double2*, int, double2*, int,
                                               int, const double2*, const double2*, double2*, double2*, cudaStream_t,
                                               KernelTimer*, const int*);
+template cudaError_t launch_block_mvp<dfl>(const MvpGeom&, const MvpPrec<dfl>&, const dfc*, int, dfc*, int, int,
+                                           const dfc*, const dfc*, dfc*, dfc*, cudaStream_t, KernelTimer*, const int*);
 template cudaError_t configure_mvp_kernels<float>();
 template cudaError_t configure_mvp_kernels<double>();
+template cudaError_t configure_mvp_kernels<dfl>();
 
 }  // namespace bdda

@@ -66,7 +66,7 @@ template <typename T>
 int mvp_noalloc(Op* op, const void* x, int ldx, void* y, int ldy, int L, const void* diag, const void* jpre,
                 cudaStream_t st) {
   using C = typename cplx<T>::type;
-  const int need = std::is_same<T, double>::value ? BDDA_PREC_FP64 : BDDA_PREC_FP32;
+  const int need = PrecInfo<T>::bit;
   if (!(op->prec & need)) {
     set_error("operator was created without the tables of this precision");
     return BDDA_ERR_INVALID;

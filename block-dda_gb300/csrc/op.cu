@@ -41,6 +41,17 @@ cudaError_t order_after(cudaStream_t later, cudaStream_t earlier) {
   return e;
 }
 
+cudaError_t wait_stream(cudaStream_t st) {
+  thread_local cudaEvent_t ev = nullptr;
+  if (ev == nullptr) {
+    const cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventBlockingSync | cudaEventDisableTiming);
+    if (e != cudaSuccess) { ev = nullptr; return e; }
+  }
+  cudaError_t e = cudaEventRecord(ev, st);
+  if (e != cudaSuccess) return e;
+  return cudaEventSynchronize(ev);
+}
+
 static int smooth235(int v) {
   for (;; ++v) {
     int t = v;
@@ -69,11 +80,11 @@ Op::~Op() {
   // release every stream-ordered buffer on the operator's stream before it goes away
   solver.reset();
   for (auto* o : {&dip, &cub}) { o->occ.release(); o->tiles.release(); o->tmask.release(); }
-  for (int i = 0; i < 3; ++i) { tw64[i].release(); tw32[i].release(); }
-  ghat64.release(); ghat32.release();
-  for (int i = 0; i < 2; ++i) { t1[i].release(); t2[i].release(); }
+  for (int i = 0; i < 3; ++i) { tw64[i].release(); tw32[i].release(); twdf[i].release(); }
+  ghat64.release(); ghat32.release(); ghatdf.release();
+  for (int i = 0; i < 3; ++i) { t1[i].release(); t2[i].release(); }
   if (stream) {
-    cudaStreamSynchronize(stream);
+    wait_stream(stream);
     cudaStreamDestroy(stream);
   }
 }
@@ -113,9 +124,11 @@ int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o) {
   BDDA_CUDA(o->occ.ensure(nc * sizeof(int), op->stream));
   BDDA_CUDA(o->tmask.ensure(tmask.size(), op->stream));
   BDDA_CUDA(o->tiles.ensure(std::max<size_t>(1, tiles.size()) * sizeof(int), op->stream));
-  BDDA_CUDA(cudaMemcpy(o->occ.p, occ.data(), nc * sizeof(int), cudaMemcpyHostToDevice));
-  BDDA_CUDA(cudaMemcpy(o->tmask.p, tmask.data(), tmask.size(), cudaMemcpyHostToDevice));
-  if (!tiles.empty()) BDDA_CUDA(cudaMemcpy(o->tiles.p, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice));
+  BDDA_CUDA(cudaMemcpyAsync(o->occ.p, occ.data(), nc * sizeof(int), cudaMemcpyHostToDevice, op->stream));
+  BDDA_CUDA(cudaMemcpyAsync(o->tmask.p, tmask.data(), tmask.size(), cudaMemcpyHostToDevice, op->stream));
+  if (!tiles.empty())
+    BDDA_CUDA(cudaMemcpyAsync(o->tiles.p, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice, op->stream));
+  BDDA_CUDA(wait_stream(op->stream));  // host vectors die on return
   return BDDA_OK;
 }
 
@@ -124,8 +137,8 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
                  int L, const typename cplx<T>::type* diag, const typename cplx<T>::type* jpre, cudaStream_t st,
                  const int* done) {
   using C = typename cplx<T>::type;
-  const int pi = std::is_same<T, double>::value ? 0 : 1;
-  const int need = std::is_same<T, double>::value ? BDDA_PREC_FP64 : BDDA_PREC_FP32;
+  const int pi = PrecInfo<T>::slot;
+  const int need = PrecInfo<T>::bit;
   if (!(op->prec & need)) {
     set_error("operator was created without the tables of this precision");
     return BDDA_ERR_INVALID;
@@ -150,6 +163,8 @@ template int op_block_mvp<double>(Op*, const Occupancy&, const double2*, int, do
                                   const double2*, cudaStream_t, const int*);
 template int op_block_mvp<float>(Op*, const Occupancy&, const float2*, int, float2*, int, int, const float2*,
                                  const float2*, cudaStream_t, const int*);
+template int op_block_mvp<dfl>(Op*, const Occupancy&, const dfc*, int, dfc*, int, int, const dfc*, const dfc*,
+                               cudaStream_t, const int*);
 
 }  // namespace bdda
 
@@ -163,7 +178,10 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
   if (!out || !n) { set_error("null argument"); return BDDA_ERR_INVALID; }
   *out = nullptr;
   if (f != 3) { set_error("unknown f value (only f=3 is supported)"); return BDDA_ERR_INVALID; }
-  if ((prec & (BDDA_PREC_FP64 | BDDA_PREC_FP32)) == 0) { set_error("no precision requested"); return BDDA_ERR_INVALID; }
+  if ((prec & (BDDA_PREC_FP64 | BDDA_PREC_FP32 | BDDA_PREC_DF64)) == 0) {
+    set_error("no precision requested");
+    return BDDA_ERR_INVALID;
+  }
   for (int i = 0; i < 3; ++i)
     if (n[i] < 1 || n[i] > kMaxLine / 2) {
       set_error("lattice box dimension outside 1..256");
@@ -188,11 +206,16 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     std::vector<double2> tw;
     make_twiddles(op->P[i], &tw);
     BDDA_CUDA(op->tw64[i].ensure(tw.size() * sizeof(double2), op->stream));
-    BDDA_CUDA(cudaMemcpy(op->tw64[i].p, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    BDDA_CUDA(cudaMemcpyAsync(op->tw64[i].p, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, op->stream));
     std::vector<float2> tf(tw.size());
     for (size_t t = 0; t < tw.size(); ++t) tf[t] = make_float2((float)tw[t].x, (float)tw[t].y);
     BDDA_CUDA(op->tw32[i].ensure(tf.size() * sizeof(float2), op->stream));
-    BDDA_CUDA(cudaMemcpy(op->tw32[i].p, tf.data(), tf.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    BDDA_CUDA(cudaMemcpyAsync(op->tw32[i].p, tf.data(), tf.size() * sizeof(float2), cudaMemcpyHostToDevice, op->stream));
+    std::vector<dfc> td(tw.size());
+    for (size_t t = 0; t < tw.size(); ++t) td[t] = cmake(dfl(tw[t].x), dfl(tw[t].y));
+    BDDA_CUDA(op->twdf[i].ensure(td.size() * sizeof(dfc), op->stream));
+    BDDA_CUDA(cudaMemcpyAsync(op->twdf[i].p, td.data(), td.size() * sizeof(dfc), cudaMemcpyHostToDevice, op->stream));
+    BDDA_CUDA(wait_stream(op->stream));  // tw / tf die at the end of this iteration
   }
   {
     // kernel attributes sized for the largest line, so every live operator fits; once per process
@@ -201,6 +224,7 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     std::call_once(once, [] {
       cfg = configure_mvp_kernels<double>();
       if (cfg == cudaSuccess) cfg = configure_mvp_kernels<float>();
+      if (cfg == cudaSuccess) cfg = configure_mvp_kernels<dfl>();
     });
     BDDA_CUDA(cfg);
   }
@@ -211,11 +235,12 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
   BDDA_CUDA(work.ensure(6 * ng * sizeof(double2), op->stream));
   if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure(6 * ng * sizeof(double2), op->stream));
   if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure(6 * ng * sizeof(float2), op->stream));
+  if (prec & BDDA_PREC_DF64) BDDA_CUDA(op->ghatdf.ensure(6 * ng * sizeof(dfc), op->stream));
   MvpGeom g = op->geom(op->dip);
   BDDA_CUDA(build_green_hat(g, lf, k_re, k_im, op->tw64[0].as<double2>(), op->tw64[1].as<double2>(),
                             op->tw64[2].as<double2>(), work.as<double2>(), op->ghat64.as<double2>(),
-                            op->ghat32.as<float2>(), op->stream));
-  BDDA_CUDA(cudaStreamSynchronize(op->stream));
+                            op->ghat32.as<float2>(), op->ghatdf.as<dfc>(), op->stream));
+  BDDA_CUDA(wait_stream(op->stream));
   *out = op.release();
   return BDDA_OK;
 }
@@ -259,7 +284,7 @@ int bdda_mbt_fft_mvp(bdda_op* op, const double* p_hat, double* q_hat) {
                                 op->stream);
   if (rc) return rc;
   BDDA_CUDA(cudaMemcpyAsync(q_hat, y.p, nrow * sizeof(double2), cudaMemcpyDeviceToHost, op->stream));
-  BDDA_CUDA(cudaStreamSynchronize(op->stream));
+  BDDA_CUDA(wait_stream(op->stream));
   return BDDA_OK;
 }
 
@@ -275,7 +300,9 @@ int bdda_op_mvp_device(bdda_op* op, int prec, const void* x, int ldx, void* y, i
   if (prec == BDDA_PREC_FP32)
     return op_block_mvp<float>(op, op->dip, (const float2*)x, ldx, (float2*)y, ldy, L, (const float2*)diag,
                                (const float2*)jpre, st);
-  set_error("prec must be BDDA_PREC_FP64 or BDDA_PREC_FP32");
+  if (prec == BDDA_PREC_DF64)
+    return op_block_mvp<dfl>(op, op->dip, (const dfc*)x, ldx, (dfc*)y, ldy, L, (const dfc*)diag, (const dfc*)jpre, st);
+  set_error("prec must be BDDA_PREC_FP64, BDDA_PREC_FP32 or BDDA_PREC_DF64");
   return BDDA_ERR_INVALID;
 }
 
@@ -312,7 +339,7 @@ int bdda_op_set_timing(bdda_op* op, int enable) {
 int bdda_op_kernel_stats(bdda_op* op, double* ms, long long* launches, int n, int reset) {
   if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
   std::lock_guard<std::mutex> lk(op->mu);
-  cudaStreamSynchronize(op->stream);
+  wait_stream(op->stream);
   cudaDeviceSynchronize();
   op->timer.resolve();
   const int m = std::min(n, (int)kNumKernelIds);

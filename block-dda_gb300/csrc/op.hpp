@@ -65,11 +65,11 @@ struct Op {
   double lf = 0, kr = 0, ki = 0;
   int prec = 0;  // bit mask BDDA_PREC_FP64 | BDDA_PREC_FP32
   AxisPlan plan[3];
-  DevBuf tw64[3], tw32[3];
-  DevBuf ghat64, ghat32;
+  DevBuf tw64[3], tw32[3], twdf[3];
+  DevBuf ghat64, ghat32, ghatdf;
   Occupancy dip;    // dipole occupancy (set_dipoles)
   Occupancy cub;    // every cuboid site (the reference's MBT_fft_mvp vector)
-  DevBuf t1[2], t2[2];   // MVP workspace per precision (0 = FP64, 1 = FP32)
+  DevBuf t1[3], t2[3];   // MVP workspace per precision (0 = FP64, 1 = FP32, 2 = double-float)
   cudaStream_t stream = nullptr;
   KernelTimer timer;
   std::mutex mu;
@@ -98,9 +98,22 @@ template <> inline MvpPrec<double> Op::tables<double>() const {
 template <> inline MvpPrec<float> Op::tables<float>() const {
   return {tw32[0].as<float2>(), tw32[1].as<float2>(), tw32[2].as<float2>(), ghat32.as<float2>()};
 }
+template <> inline MvpPrec<dfl> Op::tables<dfl>() const {
+  return {twdf[0].as<dfc>(), twdf[1].as<dfc>(), twdf[2].as<dfc>(), ghatdf.as<dfc>()};
+}
+
+// Workspace slot and precision bit of each arithmetic type.
+template <typename T> struct PrecInfo;
+template <> struct PrecInfo<double> { static constexpr int slot = 0, bit = 1; };
+template <> struct PrecInfo<float> { static constexpr int slot = 1, bit = 2; };
+template <> struct PrecInfo<dfl> { static constexpr int slot = 2, bit = 4; };
 
 // Make stream 'later' wait for the work enqueued so far on 'earlier'.
 cudaError_t order_after(cudaStream_t later, cudaStream_t earlier);
+
+// Wait for a stream without spinning a CPU core: records a blocking-sync event
+// and sleeps on it, so many host threads can wait on concurrent solves.
+cudaError_t wait_stream(cudaStream_t st);
 
 // Build the occupancy tables from a host list of lattice addresses (null -> all sites).
 int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o);

@@ -61,7 +61,7 @@ extern "C" {
 
 // Runs the device FFT core (one "lane") on a host line: forward (natural ->
 // digit-reversed) or inverse (digit-reversed -> natural, unnormalised).
-// data: N interleaved complex values; prec 1 = FP64, 2 = FP32 arithmetic
+// data: N interleaved complex values; prec 1 = FP64, 2 = FP32, 3 = double-float arithmetic
 // (values are rounded to float and back).  nvalid in (0, N): the forward
 // transform reads only the first nvalid inputs and takes the rest as zero
 // (the pad slots hold poison values to prove it).  Returns the number of stages, or
@@ -81,6 +81,18 @@ int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, i
     for (int i = 0; i < N; ++i) {
       const double2 v = s[bdda::skw<double2>(i)];
       data[2 * i] = v.x; data[2 * i + 1] = v.y;
+    }
+  } else if (prec == 3) {
+    std::vector<bdda::dfc> s(bdda::line_words<bdda::dfc>(N), bdda::cmake(bdda::dfl(1e30), bdda::dfl(1e30))), t(N);
+    for (int i = 0; i < N; ++i) {
+      s[bdda::skw<bdda::dfc>(i)] = bdda::cmake(bdda::dfl(data[2 * i]), bdda::dfl(data[2 * i + 1]));
+      t[i] = bdda::cmake(bdda::dfl(tw[i].x), bdda::dfl(tw[i].y));
+    }
+    if (inverse) bdda::warp_fft<true>(s.data(), t.data(), p, 0, 1);
+    else bdda::warp_fft<false>(s.data(), t.data(), p, 0, 1, nv);
+    for (int i = 0; i < N; ++i) {
+      const bdda::dfc v = s[bdda::skw<bdda::dfc>(i)];
+      data[2 * i] = bdda::df_to_double(v.x); data[2 * i + 1] = bdda::df_to_double(v.y);
     }
   } else {
     std::vector<float2> s(bdda::line_words<float2>(N), make_float2(1e30f, 1e30f)), t(N);

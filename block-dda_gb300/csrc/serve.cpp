@@ -114,7 +114,8 @@ struct bdda_server {
       return;
     }
     bdda_op* op = nullptr;
-    const int prec = BDDA_PREC_FP64 | (opts.precision == BDDA_SOLVE_MIXED ? BDDA_PREC_FP32 : 0);
+    // mixed: FP32 inner solves + double-float residuals; otherwise plain FP64
+    const int prec = opts.precision == BDDA_SOLVE_MIXED ? (BDDA_PREC_FP32 | BDDA_PREC_DF64) : BDDA_PREC_FP64;
     int rc = bdda_op_create(&op, r.n, 3, r.lf, r.k_re, r.k_im, prec);
     if (rc == BDDA_OK) rc = bdda_op_set_dipoles(op, r.address, r.nocc);
     bdda_solve_stats st{};
@@ -188,6 +189,11 @@ int bdda_server_submit(bdda_server* s, const bdda_request* r, long long* ticket)
     bdda::set_error("bad request");
     return BDDA_ERR_INVALID;
   }
+  for (int i = 0; i < 3; ++i)
+    if (r->n[i] < 1 || r->n[i] > 256) {
+      bdda::set_error("lattice box dimension outside 1..256 (padded FFT lines are limited to 512 points)");
+      return BDDA_ERR_INVALID;
+    }
   const double fp = footprint_bytes(r->n, r->nocc, r->L, s->opts.precision);
   if (fp > s->budget) {
     bdda::set_error("request footprint " + std::to_string((long long)fp) + " bytes exceeds the server memory budget");

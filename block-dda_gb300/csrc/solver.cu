@@ -31,8 +31,10 @@ struct SolverWork {
   int n = 0, L = 0;
   DevBuf blk64[10], blk32[10];   // 0-7 Krylov blocks, 8 right-hand side, 9 solution
   DevBuf X64, R64, Y64;
+  DevBuf xdf, ydf, diagdf;      // double-float residual MVP (mixed solves)
   DevBuf jpre64, diag32, jpre32;
-  DevBuf partials, partials2;   // Gram partials (c128) [G][L*L]
+  DevBuf gpart;                 // per-CTA Gram partials (c128) [G][L*L]
+  DevBuf partials, partials2;   // reduced Gram matrices (c128) [L*L]
   DevBuf vpart;                 // dot / norm partials
   DevBuf small;                 // c128 [kNumSlots][L*L] + scalars
   DevBuf ctl;                   // SolverCtl
@@ -298,10 +300,13 @@ struct Krylov {
     ++mvps;
     return op_block_mvp<T>(op, op->dip, x, n, y, n, L, diag, jpre, st, &ctl()->done);
   }
-  template <bool CONJ> void gram(const C* A, const C* B, double2* part) {
+  // out = op(A)^T B (L x L, FP64): per-CTA partials, then a multi-CTA ordered reduction
+  template <bool CONJ> void gram(const C* A, const C* B, double2* out) {
     op->timer.begin(kGram, st);
-    k_gram<T, CONJ><<<G(), kGramThreads, 0, st>>>(A, n, B, n, n, L, part, ctl());
+    k_gram<T, CONJ><<<G(), kGramThreads, 0, st>>>(A, n, B, n, n, L, w->gpart.template as<double2>(), ctl());
+    k_gram_reduce<<<(L * L + 63) / 64, 256, 0, st>>>(w->gpart.template as<double2>(), G(), L * L, out, ctl());
     op->timer.end(kGram, st);
+    op->timer.count(kGram);
   }
   void rowmm(const C* A, const double2* Ma, const C* B, const double2* Mb, const C* Cadd, C* Out) {
     op->timer.begin(kUpdate, st);
@@ -333,7 +338,7 @@ struct Krylov {
   // poll the control block; returns 1 when the device signalled done
   int poll(bool* done, bool wait = true) {
     BDDA_CUDA(cudaMemcpyAsync(w->ctl_host, ctl(), sizeof(SolverCtl), cudaMemcpyDeviceToHost, st));
-    if (wait) BDDA_CUDA(cudaStreamSynchronize(st));
+    if (wait) BDDA_CUDA(wait_stream(st));
     *done = w->ctl_host->done != 0;
     return BDDA_OK;
   }
@@ -352,10 +357,10 @@ struct Krylov {
   void cholqr2(const C* A, C* W, C* Q, int mode) {
     double2* p = w->partials.template as<double2>();
     gram<true>(A, A, p);
-    small_launch(k_small_chol1, (const double2*)p, G(), L, small(), ctl());
+    small_launch(k_small_chol1, (const double2*)p, 1, L, small(), ctl());
     rowmm(A, sl(kR1Inv), nullptr, nullptr, nullptr, W);
     gram<true>(W, W, p);
-    small_launch(k_small_chol2, (const double2*)p, G(), L, small(), ctl(), 0.0, (double*)nullptr, 0, mode);
+    small_launch(k_small_chol2, (const double2*)p, 1, L, small(), ctl(), 0.0, (double*)nullptr, 0, mode);
     rowmm(W, sl(kR2Inv), nullptr, nullptr, nullptr, Q);
   }
 
@@ -374,18 +379,18 @@ struct Krylov {
       BDDA_TRY(mvp(S, AS));
       gram<false>(S, AS, p);
       if (k == 0) gram<false>(Q, Q, p2);
-      small_launch(k_small_cocg_alpha, (const double2*)p, (const double2*)(k == 0 ? p2 : nullptr), G(), L, small(), ctl(),
+      small_launch(k_small_cocg_alpha, (const double2*)p, (const double2*)(k == 0 ? p2 : nullptr), 1, L, small(), ctl(),
                    (int)full);
       rowmm(S, sl(kAXi), nullptr, nullptr, X, X);           // X += S alpha xi
       rowmm(AS, sl(kNAlpha), nullptr, nullptr, Q, W);       // W = Q - AS alpha
       gram<true>(W, W, p);
-      small_launch(k_small_chol1, (const double2*)p, G(), L, small(), ctl());
+      small_launch(k_small_chol1, (const double2*)p, 1, L, small(), ctl());
       rowmm(W, sl(kR1Inv), nullptr, nullptr, nullptr, W);
       gram<true>(W, W, p);
-      small_launch(k_small_chol2, (const double2*)p, G(), L, small(), ctl(), tol, w->hist.as<double>(), k, 1);
+      small_launch(k_small_chol2, (const double2*)p, 1, L, small(), ctl(), tol, w->hist.as<double>(), k, 1);
       rowmm(W, sl(kR2Inv), nullptr, nullptr, nullptr, Qn);  // Q'
       gram<false>(Qn, Qn, p);
-      small_launch(k_small_cocg_beta, (const double2*)p, G(), L, small(), ctl(), (int)full);
+      small_launch(k_small_cocg_beta, (const double2*)p, 1, L, small(), ctl(), (int)full);
       rowmm(S, sl(kBeta), nullptr, nullptr, Qn, S);         // S = Q' + S beta
       std::swap(Q, Qn);
       if ((k + 1) % check_every == 0 || k + 1 == itermax) {
@@ -419,7 +424,7 @@ struct Krylov {
       BDDA_TRY(mvp(P, V));                                   // V = A P
       gram<true>(R0, V, p);
       gram<true>(R0, R, p2);
-      small_launch(k_small_solve, (const double2*)p, (const double2*)p2, G(), L, small(), ctl(), 0, (int)kM, 1.0,
+      small_launch(k_small_solve, (const double2*)p, (const double2*)p2, 1, L, small(), ctl(), 0, (int)kM, 1.0,
                    (const double2*)nullptr, (int)kAlpha, (int)kNAlpha);
       rowmm(V, sl(kNAlpha), nullptr, nullptr, R, Tm);        // T = R - V alpha
       BDDA_TRY(mvp(Tm, Z));                                  // Z = A T
@@ -435,7 +440,7 @@ struct Krylov {
       k_small_err<<<1, 256, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
       op->timer.end(kSmall, st);
       gram<true>(R0, Z, p);
-      small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, G(), L, small(), ctl(), (int)kM, -1, -1.0,
+      small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, 1, L, small(), ctl(), (int)kM, -1, -1.0,
                    (const double2*)nullptr, (int)kBeta, -1);  // beta = M^-1 (-R0^H Z)
       axpby(nullptr, P, scal + 1, V, Pt);                    // Pt = P - zeta V
       rowmm(Pt, sl(kBeta), nullptr, nullptr, R, P);          // P = R + Pt beta
@@ -471,10 +476,10 @@ struct Krylov {
     for (; k < itermax; ++k) {
       gram<true>(R0, V, p);
       gram<true>(R0, R, p2);
-      small_launch(k_small_solve, (const double2*)p, (const double2*)p2, G(), L, small(), ctl(), 0, -1, 1.0,
+      small_launch(k_small_solve, (const double2*)p, (const double2*)p2, 1, L, small(), ctl(), 0, -1, 1.0,
                    (const double2*)nullptr, (int)kAlpha, -1);
       // keep R0^H R (old R) for gamma
-      small_launch(k_small_store_reduce, (const double2*)p2, G(), L, small(), ctl(), (int)kM2);
+      small_launch(k_small_store_reduce, (const double2*)p2, 1, L, small(), ctl(), (int)kM2);
       dotc(Wm, R, vp);
       dotc(Wm, Wm, vp + gv);
       op->timer.begin(kSmall, st);
@@ -491,7 +496,7 @@ struct Krylov {
       op->timer.end(kSmall, st);
       BDDA_TRY(mvp(Rn, Wm));                                 // W = A Rnew
       gram<true>(R0, Rn, p);
-      small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, G(), L, small(), ctl(), (int)kM2, -1, 1.0,
+      small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, 1, L, small(), ctl(), (int)kM2, -1, 1.0,
                    (const double2*)scal, (int)kBeta, -1);    // gamma = (R0^H R)^-1 (R0^H Rnew / zeta)
       std::swap(R, Rn);
       rowmm(U, sl(kBeta), nullptr, nullptr, R, P);           // P = R + U gamma
@@ -537,9 +542,15 @@ static int ensure_work(Op* op, int n, int L, int itermax, bool need64, bool need
   BDDA_CUDA(w->R64.ensure(b64, op->stream));
   BDDA_CUDA(w->Y64.ensure(b64, op->stream));
   BDDA_CUDA(w->jpre64.ensure(sizeof(double2) * (size_t)n, op->stream));
+  if (op->prec & BDDA_PREC_DF64) {
+    BDDA_CUDA(w->xdf.ensure(sizeof(dfc) * (size_t)n * L, op->stream));
+    BDDA_CUDA(w->ydf.ensure(sizeof(dfc) * (size_t)n * L, op->stream));
+    BDDA_CUDA(w->diagdf.ensure(sizeof(dfc) * (size_t)n, op->stream));
+  }
   BDDA_CUDA(w->diag32.ensure(sizeof(float2) * (size_t)n, op->stream));
   BDDA_CUDA(w->jpre32.ensure(sizeof(float2) * (size_t)n, op->stream));
   const size_t LL = (size_t)L * L;
+  BDDA_CUDA(w->gpart.ensure(sizeof(double2) * LL * gram_grid(n), op->stream));
   BDDA_CUDA(w->partials.ensure(sizeof(double2) * LL * gram_grid(n), op->stream));
   BDDA_CUDA(w->partials2.ensure(sizeof(double2) * LL * gram_grid(n), op->stream));
   BDDA_CUDA(w->vpart.ensure(sizeof(double2) * 2 * (size_t)std::max(vec_grid((size_t)n * L) * L, 2 * 608), op->stream));
@@ -578,20 +589,31 @@ static int host_colnorm2(Op* op, cudaStream_t st, const double2* A, int n, int L
   op->timer.count(kOther);
   std::vector<double> h((size_t)g * L);
   BDDA_CUDA(cudaMemcpyAsync(h.data(), vp, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
-  BDDA_CUDA(cudaStreamSynchronize(st));
+  BDDA_CUDA(wait_stream(st));
   out->assign(L, 0.0);
   for (int p = 0; p < g; ++p)
     for (int l = 0; l < L; ++l) (*out)[l] += h[(size_t)p * L + l];
   return BDDA_OK;
 }
 
-// R = B - (diag o X + A_off X) in FP64; returns max_l ||r_l|| / ||b_l||
+// R = B - (diag o X + A_off X); returns max_l ||r_l|| / ||b_l||.  The product
+// runs in FP64, or in double-float arithmetic when use_df is set (FP64-level
+// accuracy on the FP32 pipes); the subtraction and norms are FP64.
 static int true_residual(Op* op, cudaStream_t st, const double2* diag, const double2* B, int ldb, const double2* X, int n,
-                         int L, const std::vector<double>& bn2, double* resmax, int* mvps) {
+                         int L, const std::vector<double>& bn2, double* resmax, int* mvps, bool use_df) {
   SolverWork* w = op->solver.get();
-  BDDA_TRY(op_block_mvp<double>(op, op->dip, X, n, w->Y64.as<double2>(), n, L, diag, nullptr, st));
+  const int gv = vec_grid((size_t)n * L);
+  if (use_df) {
+    k_to_df<<<gv, 256, 0, st>>>(n, L, X, n, w->xdf.as<dfc>(), n);
+    op->timer.count(kOther);
+    BDDA_TRY(op_block_mvp<dfl>(op, op->dip, w->xdf.as<dfc>(), n, w->ydf.as<dfc>(), n, L, w->diagdf.as<dfc>(), nullptr, st));
+    k_from_df<<<gv, 256, 0, st>>>(n, L, w->ydf.as<dfc>(), n, w->Y64.as<double2>(), n);
+    op->timer.count(kOther);
+  } else {
+    BDDA_TRY(op_block_mvp<double>(op, op->dip, X, n, w->Y64.as<double2>(), n, L, diag, nullptr, st));
+  }
   ++*mvps;
-  k_residual<<<vec_grid((size_t)n * L), 256, 0, st>>>(n, L, B, ldb, w->Y64.as<double2>(), n, w->R64.as<double2>(), n);
+  k_residual<<<gv, 256, 0, st>>>(n, L, B, ldb, w->Y64.as<double2>(), n, w->R64.as<double2>(), n);
   op->timer.count(kOther);
   std::vector<double> rn2;
   BDDA_TRY(host_colnorm2(op, st, w->R64.as<double2>(), n, L, &rn2));
@@ -612,8 +634,10 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
   if (ldb < n || ldx < n) { set_error("leading dimension smaller than 3*nocc"); return BDDA_ERR_INVALID; }
   const bool mixed = o->precision == BDDA_SOLVE_MIXED;
   if (mixed && !(op->prec & BDDA_PREC_FP32)) { set_error("mixed precision needs BDDA_PREC_FP32 tables"); return BDDA_ERR_INVALID; }
-  if (!(op->prec & BDDA_PREC_FP64) && (!mixed || o->true_tol > 0)) {
-    set_error("this solve needs BDDA_PREC_FP64 tables");
+  // residuals of a mixed refinement run on double-float tables when present
+  const bool use_df = mixed && (op->prec & BDDA_PREC_DF64);
+  if (!(op->prec & BDDA_PREC_FP64) && (!mixed || (o->true_tol > 0 && !use_df))) {
+    set_error("this solve needs BDDA_PREC_FP64 tables (or BDDA_PREC_DF64 for mixed-precision residuals)");
     return BDDA_ERR_INVALID;
   }
   const bool refine = o->true_tol > 0;
@@ -629,6 +653,10 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
   cudaEventCreate(&e1);
   cudaEventRecord(e0, st);
   k_diag_prep<<<vec_grid(n), 256, 0, st>>>(n, diag, w->jpre64.as<double2>(), w->diag32.as<float2>(), w->jpre32.as<float2>());
+  if (use_df) {
+    k_to_df<<<vec_grid(n), 256, 0, st>>>(n, 1, diag, n, w->diagdf.as<dfc>(), n);
+    op->timer.count(kOther);
+  }
   op->timer.count(kOther);
   const double2* jpre64 = o->jacobi ? w->jpre64.as<double2>() : nullptr;
   const float2* jpre32 = o->jacobi ? w->jpre32.as<float2>() : nullptr;
@@ -691,7 +719,7 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
     for (int r = 0; r < max_refine; ++r) {
       BDDA_TRY(inner(R, ldr, itol, X, ldx, true));
       if (status == BDDA_ERR_BREAKDOWN) break;
-      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, n, L, bn2, &resmax, &mvps));
+      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, n, L, bn2, &resmax, &mvps, use_df));
       R = w->R64.as<double2>();
       ldr = n;
       if (resmax <= o->true_tol) { converged = true; break; }
@@ -699,7 +727,7 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
     if (status == BDDA_OK && !converged) status = BDDA_ERR_NOT_CONVERGED;
   }
   cudaEventRecord(e1, st);
-  BDDA_CUDA(cudaStreamSynchronize(st));
+  BDDA_CUDA(wait_stream(st));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
@@ -766,7 +794,7 @@ int bdda_solve(bdda_op* op, const bdda_solve_opts* opts, const double* diag, con
   if (rc == BDDA_OK || rc == BDDA_ERR_NOT_CONVERGED) {
     BDDA_CUDA(cudaMemcpy2DAsync(X, sizeof(double2) * (size_t)ldx, x.p, sizeof(double2) * n, sizeof(double2) * n, L,
                                 cudaMemcpyDeviceToHost, st));
-    BDDA_CUDA(cudaStreamSynchronize(st));
+    BDDA_CUDA(wait_stream(st));
   }
   return rc;
 }
@@ -799,7 +827,7 @@ int bdda_qr_reduced(const double* A, int m, int nc, int lda, double* Q, int ldq,
   bool done = false;
   rc = kr.poll(&done);
   if (rc != BDDA_OK) return rc;
-  BDDA_CUDA(cudaStreamSynchronize(st));
+  BDDA_CUDA(wait_stream(st));
   if (w->ctl_host->status != 0) {
     set_error("qr_reduced: rank-deficient block (Cholesky failed)");
     return BDDA_ERR_BREAKDOWN;

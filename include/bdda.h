@@ -35,6 +35,8 @@ extern "C" {
 /* ---- precision bits of an operator ----------------------------------- */
 #define BDDA_PREC_FP64 1        /* complex FP64 tables (plain FP64 path, true residuals) */
 #define BDDA_PREC_FP32 2        /* complex FP32 tables (mixed-precision inner solves)   */
+#define BDDA_PREC_DF64 4        /* complex double-float tables: FP32 pairs hi+lo, ~48-bit significand;
+                                   the mixed solve's true residuals run on them when present */
 
 /* ---- solvers (bl_*_mvp_fft in bl_krylov_mvp_fft/DDA_linear_solvers.hpp:1-6) */
 #define BDDA_SOLVER_COCG_RQ 0   /* block COCG-RQ, complex-symmetric systems  */
@@ -56,7 +58,7 @@ typedef struct bdda_op bdda_op;
  *   f           3 (electric dipoles, the reference's CED)
  *   lf          lattice spacing (physical length)
  *   k_re, k_im  wavenumber in the medium
- *   prec        BDDA_PREC_FP64 and/or BDDA_PREC_FP32
+ *   prec        any of BDDA_PREC_FP64, BDDA_PREC_FP32, BDDA_PREC_DF64
  */
 int bdda_op_create(bdda_op** op, const int n[3], int f, double lf, double k_re, double k_im, int prec);
 
@@ -86,7 +88,8 @@ int bdda_mbt_fft_mvp(bdda_op* op, const double* p_hat, double* q_hat);
  *   y = [diag o x +] A_off x [o jpre]
  * This is the inline block-MVP wrapper of every reference solver
  * (e.g. bl_krylov_mvp_fft/bl_cocg_rq_jacobi_mvp_fft.cpp:43-60).
- *   prec      BDDA_PREC_FP64 (double2 buffers) or BDDA_PREC_FP32 (float2 buffers)
+ *   prec      BDDA_PREC_FP64 (double2 buffers), BDDA_PREC_FP32 (float2 buffers) or
+ *             BDDA_PREC_DF64 (buffers of {re_hi, re_lo, im_hi, im_lo} floats)
  *   x, y      3*nocc x L column-major, leading dimensions ldx, ldy (>= 3*nocc)
  *   diag      3*nocc complex or null (off-diagonal part only)
  *   jpre      3*nocc complex or null (no Jacobi scaling)
@@ -277,7 +280,8 @@ const char* bdda_last_error(void);
  * Test hook: run the device FFT core (the same source the kernels inline) on
  * the CPU for one line of length N (5-smooth, <= 512).  inverse = 0: natural
  * order in, digit-reversed spectrum out; inverse = 1: digit-reversed in,
- * natural out, unnormalised.  prec 1 = FP64, 2 = FP32 arithmetic.  nvalid in
+ * natural out, unnormalised.  prec 1 = FP64, 2 = FP32, 3 = double-float
+ * arithmetic.  nvalid in
  * (0, N) makes the forward transform read only the first nvalid inputs (the
  * rest count as zero); 0 reads all.  data holds N interleaved complex doubles,
  * overwritten.  Returns the number of radix stages (radices written to

@@ -146,3 +146,32 @@ def test_block_mvp_rejects_bad_arguments():
     x = torch.zeros((1, 9), dtype=torch.complex128, device="cuda")
     with pytest.raises(bdda.BddaError):                  # FP64 tables absent
         op.mvp_device(x.data_ptr(), x.data_ptr(), 1, 9, 9, prec=bdda.PREC_FP64)
+
+
+def test_block_mvp_double_float_vs_oracle():
+    """Double-float (FP32 hi/lo pairs) MVP used for mixed-precision residuals: FP64-level accuracy."""
+    torch = _torch()
+    nocc, L = 900, 6
+    n, addr, x, diag = _aggregate_case(nocc, 31, L)
+    lf, k = 0.021, 2 * np.pi / 0.55
+    gh, P = mbt.green_hat(n, 3, lf, k)
+    ref = mbt.block_mvp(n, 3, gh, P, addr, diag, x)
+    op = bdda.Operator(n, lf, k)
+    op.set_dipoles(addr)
+
+    def to_df(a):   # complex128 (rows, cols) -> float32 [..., 4] = (re_hi, re_lo, im_hi, im_lo)
+        hi_r = a.real.astype(np.float32)
+        hi_i = a.imag.astype(np.float32)
+        lo_r = (a.real - hi_r.astype(np.float64)).astype(np.float32)
+        lo_i = (a.imag - hi_i.astype(np.float64)).astype(np.float32)
+        return np.stack([hi_r, lo_r, hi_i, lo_i], axis=-1)
+
+    xd = torch.from_numpy(np.ascontiguousarray(to_df(x.T))).cuda()
+    dd = torch.from_numpy(np.ascontiguousarray(to_df(diag))).cuda()
+    yd = torch.zeros_like(xd)
+    torch.cuda.synchronize()
+    op.mvp_device(xd.data_ptr(), yd.data_ptr(), L, 3 * nocc, 3 * nocc, prec=bdda.PREC_DF64, diag=dd.data_ptr())
+    torch.cuda.synchronize()
+    y = yd.cpu().numpy().astype(np.float64)
+    got = ((y[..., 0] + y[..., 1]) + 1j * (y[..., 2] + y[..., 3])).T
+    assert _rel(got, ref) < TOL64

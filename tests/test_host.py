@@ -71,6 +71,11 @@ def test_device_fft_core_on_cpu(N):
     fb32, _ = bdda.host_fft_line(b, prec=2)
     conv32, _ = bdda.host_fft_line(fa32 * fb32, inverse=True, prec=2)
     assert np.max(np.abs(conv32 / N - cref)) / np.max(np.abs(cref)) < 1e-6
+    # double-float arithmetic (FP32 pairs): FP64-level accuracy
+    fad, _ = bdda.host_fft_line(a, prec=3)
+    fbd, _ = bdda.host_fft_line(b, prec=3)
+    convd, _ = bdda.host_fft_line(fad * fbd, inverse=True, prec=3)
+    assert np.max(np.abs(convd / N - cref)) / np.max(np.abs(cref)) < 1e-13
     # pruned input: only the first nv values are read (the rest are poisoned in the hook)
     nv = max(1, N // 2)
     ap = a.copy()
