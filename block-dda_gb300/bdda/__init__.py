@@ -326,10 +326,11 @@ def cross_sections(k, alpha0, E, P):
     return out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy()
 
 
-def host_fft_line(x, inverse=False, prec=1, nvalid=0):
+def host_fft_line(x, inverse=False, prec=1, nvalid=0, max_radix=8):
     """Run the device FFT core on the CPU (unit tests).  Returns (y, radices)."""
     a = np.ascontiguousarray(x, dtype=np.complex128).copy()
     rad = np.zeros(16, np.int32)
+    rad[0] = int(max_radix)
     nst = lib().bdda_host_fft_line(int(a.size), 1 if inverse else 0, int(prec), int(nvalid), _dptr(a), _iptr(rad))
     if nst < 0:
         raise BddaError(ERR_INVALID, "unsupported FFT length")

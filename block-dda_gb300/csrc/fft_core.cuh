@@ -123,12 +123,111 @@ template <bool INV, typename C> BDDA_FFT_FN void dft8(C* v) {
   }
 }
 
+// ---- compile-time twiddles for composite register radices -----------------
+// cos / sin of 2 pi p / q evaluated at compile time: exact integer reduction
+// of p/q to an octant, then Taylor series (|x| <= pi/4, 18 terms) in double.
+namespace ct {
+constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr double taylor_sin(double x) {
+  double term = x, sum = x;
+  for (int k = 1; k < 18; ++k) {
+    term *= -x * x / ((2 * k) * (2 * k + 1));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double taylor_cos(double x) {
+  double term = 1, sum = 1;
+  for (int k = 1; k < 18; ++k) {
+    term *= -x * x / ((2 * k - 1) * (2 * k));
+    sum += term;
+  }
+  return sum;
+}
+// angle 2 pi p / q; returns {cos, sin} (double, constexpr)
+struct CS { double c, s; };
+constexpr CS cossin(long long p, long long q) {
+  p %= q;
+  if (p < 0) p += q;
+  // theta = 2 pi p / q = (pi/4) * (8p/q); octant o = floor(8p/q), remainder r in [0, 1)
+  const long long o = (8 * p) / q;
+  const double r = (double)(8 * p - o * q) / (double)q;  // in [0,1)
+  // phi in [0, pi/4]: reflect odd octants
+  const bool odd = (o & 1) != 0;
+  const double phi = (odd ? (1.0 - r) : r) * (kPi / 4.0);
+  double c = taylor_cos(phi), s = taylor_sin(phi);
+  if (odd) { const double t = c; c = s; s = t; }   // angle = (o+1) pi/4 - phi -> swap
+  // rotate by (o/2) quarter turns
+  switch ((o / 2) & 3) {
+    case 0: return {c, s};
+    case 1: return {-s, c};
+    case 2: return {-c, -s};
+    default: return {s, -c};
+  }
+}
+template <int R> struct TwTab {
+  double c[R * R > 0 ? R : 1];
+  double s[R * R > 0 ? R : 1];
+  constexpr TwTab() : c(), s() {
+    for (int i = 0; i < R; ++i) {
+      const CS v = cossin(i, R);
+      c[i] = v.c;
+      s[i] = v.s;
+    }
+  }
+};
+}  // namespace ct
+
+template <int R, bool INV, typename C> BDDA_FFT_FN void dft(C* v);
+
+// Composite radix R = A * B in registers (natural-order output):
+// X[B k1 + k2] = sum_n1 w_A^{n1 k1} w_R^{n1 k2} sum_n2 x[n1 + A n2] w_B^{n2 k2}.
+template <int A, int B, bool INV, typename C> BDDA_FFT_FN void dft_ct(C* v) {
+  using T = decltype(C::x);
+  constexpr int R = A * B;
+  constexpr ct::TwTab<R> tw{};
+  C y[R];
+#pragma unroll
+  for (int n1 = 0; n1 < A; ++n1) {
+    C u[B];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) u[n2] = v[n1 + A * n2];
+    dft<B, INV>(u);
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) {
+      const int e = (n1 * k2) % R;
+      if (e == 0) {
+        y[n1 * B + k2] = u[k2];
+      } else {
+        const T c = T(tw.c[e]);
+        const T sn = INV ? T(tw.s[e]) : T(-tw.s[e]);   // forward: exp(-2 pi i e / R)
+        y[n1 * B + k2] = cmake(u[k2].x * c - u[k2].y * sn, u[k2].x * sn + u[k2].y * c);
+      }
+    }
+  }
+#pragma unroll
+  for (int k2 = 0; k2 < B; ++k2) {
+    C u[A];
+#pragma unroll
+    for (int n1 = 0; n1 < A; ++n1) u[n1] = y[n1 * B + k2];
+    dft<A, INV>(u);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) v[B * k1 + k2] = u[k1];
+  }
+}
+
 template <int R, bool INV, typename C> BDDA_FFT_FN void dft(C* v) {
   if constexpr (R == 2) dft2<INV>(v);
   else if constexpr (R == 3) dft3<INV>(v);
   else if constexpr (R == 4) dft4<INV>(v);
   else if constexpr (R == 5) dft5<INV>(v);
-  else dft8<INV>(v);
+  else if constexpr (R == 6) dft_ct<2, 3, INV>(v);
+  else if constexpr (R == 8) dft8<INV>(v);
+  else if constexpr (R == 9) dft_ct<3, 3, INV>(v);
+  else if constexpr (R == 10) dft_ct<2, 5, INV>(v);
+  else if constexpr (R == 12) dft_ct<4, 3, INV>(v);
+  else if constexpr (R == 15) dft_ct<3, 5, INV>(v);
+  else dft_ct<4, 4, INV>(v);  // 16
 }
 
 // ---- shared-memory line layout ---------------------------------------------
@@ -139,23 +238,29 @@ template <typename C> BDDA_FFT_FN int skw(int i) { return i + (i >> (sizeof(C) =
 // Shared-memory elements one line of n points occupies (rounded to 16 bytes).
 template <typename C> BDDA_HD int line_words(int n) { return ((n + (n >> (sizeof(C) == 8 ? 4 : 3)) + 1) + 1) & ~1; }
 
-// ---- one in-place stage, one warp -----------------------------------------
-// nvalid < N (forward first stage only): inputs at positions >= nvalid are
-// known zeros and are not read (zero padding needs no shared-memory fill).
-template <int R, bool INV, typename C>
-BDDA_FFT_FN void warp_stage(C* __restrict__ s, const C* __restrict__ tw, int M, int tstride, float invM, int N,
-                            int lane, int lanes, int nvalid) {
+// ---- in-place stages ---------------------------------------------------------
+// One stage applied to NL lines of one warp (line j at s + j * lw); the
+// butterflies of all lines share one loop so that large radices still fill
+// the warp.  nvalid < N (forward first stage only): inputs at positions
+// >= nvalid are known zeros and are not read (zero padding needs no fill).
+template <int R, bool INV, int NL, typename C>
+BDDA_FFT_FN void warp_stage_lines(C* __restrict__ s, int lw, const C* __restrict__ tw, int M, int tstride, float invM,
+                                  int N, int lane, int lanes, int nvalid) {
   const int nb = N / R;
   const int Ls = M * R;
-  for (int t = lane; t < nb; t += lanes) {
-    const int b = (int)(((float)t + 0.5f) * invM);
-    const int n1 = t - b * M;
+  const float inv_nb = 1.0f / (float)nb;
+  for (int t = lane; t < NL * nb; t += lanes) {
+    const int j = NL == 1 ? 0 : (int)(((float)t + 0.5f) * inv_nb);
+    const int tt = t - j * nb;
+    const int b = (int)(((float)tt + 0.5f) * invM);
+    const int n1 = tt - b * M;
     const int base = b * Ls + n1;
+    C* sl = s + j * lw;
     C v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      if (nvalid < N) v[i] = (n1 + i * M < nvalid) ? s[skw<C>(base + i * M)] : czero<C>();
-      else v[i] = s[skw<C>(base + i * M)];
+      if (nvalid < N) v[i] = (n1 + i * M < nvalid) ? sl[skw<C>(base + i * M)] : czero<C>();
+      else v[i] = sl[skw<C>(base + i * M)];
     }
     if (!INV) {
       dft<R, false>(v);
@@ -173,36 +278,66 @@ BDDA_FFT_FN void warp_stage(C* __restrict__ s, const C* __restrict__ tw, int M, 
       dft<R, true>(v);
     }
 #pragma unroll
-    for (int i = 0; i < R; ++i) s[skw<C>(base + i * M)] = v[i];
+    for (int i = 0; i < R; ++i) sl[skw<C>(base + i * M)] = v[i];
   }
   BDDA_SYNCWARP();
 }
 
-template <bool INV, typename C>
-BDDA_FFT_FN void warp_stage_dispatch(const AxisPlan& p, int st, C* s, const C* tw, int lane, int lanes, int nvalid) {
+// Stage dispatch.  FULL: every radix of make_axis_plan(N, 16) (composite
+// register radices); otherwise the radices of make_axis_plan(N, 8) only.
+template <bool INV, int NL, bool FULL, typename C>
+BDDA_FFT_FN void warp_stage_lines_dispatch(const AxisPlan& p, int st, C* s, int lw, const C* tw, int lane, int lanes,
+                                           int nvalid) {
   const int M = p.M[st], ts = p.tstride[st];
   const float iM = p.invM[st];
+  if (!FULL) {
+    switch (p.radix[st]) {
+      case 2: warp_stage_lines<2, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+      case 3: warp_stage_lines<3, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+      case 4: warp_stage_lines<4, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+      case 5: warp_stage_lines<5, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+      default: warp_stage_lines<8, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    }
+    return;
+  }
   switch (p.radix[st]) {
-    case 2: warp_stage<2, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 3: warp_stage<3, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 4: warp_stage<4, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 5: warp_stage<5, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    default: warp_stage<8, INV>(s, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 2: warp_stage_lines<2, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 3: warp_stage_lines<3, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 4: warp_stage_lines<4, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 5: warp_stage_lines<5, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 6: warp_stage_lines<6, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 8: warp_stage_lines<8, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 9: warp_stage_lines<9, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 10: warp_stage_lines<10, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 12: warp_stage_lines<12, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 15: warp_stage_lines<15, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    default: warp_stage_lines<16, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
   }
 }
 
-// Full in-place transform of one line by one warp.
-// INV = false: natural -> digit-reversed (DIF); only the first nvalid inputs
-// are read (the rest are taken as zero).  INV = true: digit-reversed ->
-// natural (DIT), unnormalised.
+// NL lines of one warp transformed together (forward pruned to nvalid inputs),
+// any radix schedule (FULL) or the small-radix one.
+template <bool INV, int NL, bool FULL = true, typename C>
+BDDA_FFT_FN void warp_fft_lines(C* __restrict__ s, int lw, const C* __restrict__ tw, const AxisPlan& p, int lane,
+                                int lanes = 32, int nvalid = 1 << 30) {
+  if (!INV) {
+    for (int st = 0; st < p.nst; ++st)
+      warp_stage_lines_dispatch<false, NL, FULL>(p, st, s, lw, tw, lane, lanes, st == 0 ? nvalid : p.N);
+  } else {
+    for (int st = p.nst - 1; st >= 0; --st)
+      warp_stage_lines_dispatch<true, NL, FULL>(p, st, s, lw, tw, lane, lanes, p.N);
+  }
+}
+
+// Full in-place transform of one line by one warp with a small-radix plan
+// (make_axis_plan(N, 8)).  INV = false: natural -> digit-reversed (DIF); only
+// the first nvalid inputs are read (the rest are taken as zero).  INV = true:
+// digit-reversed -> natural (DIT), unnormalised.
 template <bool INV, typename C>
 BDDA_FFT_FN void warp_fft(C* __restrict__ s, const C* __restrict__ tw, const AxisPlan& p, int lane, int lanes = 32,
                           int nvalid = 1 << 30) {
-  if (!INV) {
-    for (int st = 0; st < p.nst; ++st) warp_stage_dispatch<false>(p, st, s, tw, lane, lanes, st == 0 ? nvalid : p.N);
-  } else {
-    for (int st = p.nst - 1; st >= 0; --st) warp_stage_dispatch<true>(p, st, s, tw, lane, lanes, p.N);
-  }
+  warp_fft_lines<INV, 1, false>(s, 0, tw, p, lane, lanes, nvalid);
 }
 
 }  // namespace bdda
+

@@ -83,7 +83,7 @@ k_fft_contig(double2* __restrict__ data, size_t nlines, AxisPlan p, const double
   double2* d = data + line * p.N;
   for (int i = lane; i < p.N; i += 32) s[skw<double2>(i)] = d[i];
   __syncwarp();
-  warp_fft<false>(s, tw, p, lane);
+  warp_fft_lines<false, 1>(s, 0, tw, p, lane);  // any schedule (the z axis uses composite radices)
   for (int i = lane; i < p.N; i += 32) d[i] = s[skw<double2>(i)];
 }
 

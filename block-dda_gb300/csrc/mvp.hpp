@@ -112,8 +112,10 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
                             const double2* twx, const double2* twy, const double2* twz,
                             double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, cudaStream_t st);
 
-// Radix schedule + FP64 twiddles for a 5-smooth N <= kMaxLine.
-bool make_axis_plan(int N, AxisPlan* p);
+// Radix schedule + FP64 twiddles for a 5-smooth N <= kMaxLine.  max_radix 8:
+// radices 8, 4, 2, 5, 3 (one line per warp); max_radix 16: fewest stages with
+// composite register radices up to 16 (multi-line warps).
+bool make_axis_plan(int N, AxisPlan* p, int max_radix = 8);
 void make_twiddles(int N, std::vector<double2>* out);
 
 }  // namespace bdda

@@ -193,9 +193,7 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz,
     s2[skw<C>(z)] = g0[2 * fstride + z];
   }
   __syncwarp();
-  warp_fft<false>(s0, twz, pz, lane, 32, nz);
-  warp_fft<false>(s1, twz, pz, lane, 32, nz);
-  warp_fft<false>(s2, twz, pz, lane, 32, nz);
+  warp_fft_lines<false, 3>(s0, lw, twz, pz, lane, 32, nz);
   const C* gl = ghat + (size_t)line * 6 * Pz;
   for (int p = lane; p < Pz; p += 32) {
     const int sp = skw<C>(p);
@@ -207,9 +205,7 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz,
     s2[sp] = cadd(cadd(cmul(gxz, a0), cmul(gyz, a1)), cmul(gzz, a2));
   }
   __syncwarp();
-  warp_fft<true>(s0, twz, pz, lane);
-  warp_fft<true>(s1, twz, pz, lane);
-  warp_fft<true>(s2, twz, pz, lane);
+  warp_fft_lines<true, 3>(s0, lw, twz, pz, lane);
   for (int z = lane; z < nz; z += 32) {
     g0[z] = s0[skw<C>(z)];
     g0[fstride + z] = s1[skw<C>(z)];

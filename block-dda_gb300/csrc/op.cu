@@ -197,7 +197,11 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
   for (int i = 0; i < 3; ++i) {
     op->n[i] = n[i];
     op->P[i] = smooth235(2 * n[i]);
-    if (!make_axis_plan(op->P[i], &op->plan[i])) { set_error("no FFT plan for the padded grid"); return BDDA_ERR_INVALID; }
+    // z lines (the fused pass, three lines per warp) take composite register radices
+    if (!make_axis_plan(op->P[i], &op->plan[i], i == 2 ? 16 : 8)) {
+      set_error("no FFT plan for the padded grid");
+      return BDDA_ERR_INVALID;
+    }
   }
   BDDA_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
   keep_pool_memory();

@@ -1,5 +1,6 @@
 // FFT radix schedules and FP64 twiddle tables (host), plus a host entry point
 // that runs the exact device FFT core on the CPU for unit tests.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -9,22 +10,54 @@
 
 namespace bdda {
 
-bool make_axis_plan(int N, AxisPlan* p) {
+namespace {
+// Fewest stages using register radices from `allowed` (largest first on ties
+// of stage count, then the smallest largest radix for lane occupancy).
+void best_factorization(int N, const std::vector<int>& allowed, std::vector<int>& cur, std::vector<int>& best) {
+  if (N == 1) {
+    if (best.empty() || cur.size() < best.size() ||
+        (cur.size() == best.size() && *std::max_element(cur.begin(), cur.end()) < *std::max_element(best.begin(), best.end())))
+      best = cur;
+    return;
+  }
+  if (!best.empty() && cur.size() + 1 > best.size()) return;
+  for (int r : allowed) {
+    if (N % r) continue;
+    if (!cur.empty() && r > cur.back()) continue;  // non-increasing order: each multiset once
+    cur.push_back(r);
+    best_factorization(N / r, allowed, cur, best);
+    cur.pop_back();
+  }
+}
+}  // namespace
+
+bool make_axis_plan(int N, AxisPlan* p, int max_radix) {
   if (N < 1 || N > kMaxLine) return false;
-  int a = 0, b = 0, c = 0, t = N;
-  while (t % 2 == 0) { t /= 2; ++a; }
-  while (t % 3 == 0) { t /= 3; ++b; }
-  while (t % 5 == 0) { t /= 5; ++c; }
+  int t = N;
+  for (int q : {2, 3, 5})
+    while (t % q == 0) t /= q;
   if (t != 1) return false;
   p->N = N;
   p->nst = 0;
-  auto push = [&](int r) { p->radix[p->nst++] = r; };
-  while (a >= 3) { push(8); a -= 3; }
-  if (a == 2) push(4);
-  if (a == 1) push(2);
-  for (int i = 0; i < c; ++i) push(5);
-  for (int i = 0; i < b; ++i) push(3);
-  if (p->nst == 0) push(2);  // N == 1 is rejected by callers; keep the plan well formed
+  if (max_radix <= 8) {
+    int a = 0, b = 0, c = 0;
+    t = N;
+    while (t % 2 == 0) { t /= 2; ++a; }
+    while (t % 3 == 0) { t /= 3; ++b; }
+    while (t % 5 == 0) { t /= 5; ++c; }
+    auto push = [&](int r) { p->radix[p->nst++] = r; };
+    while (a >= 3) { push(8); a -= 3; }
+    if (a == 2) push(4);
+    if (a == 1) push(2);
+    for (int i = 0; i < c; ++i) push(5);
+    for (int i = 0; i < b; ++i) push(3);
+  } else {
+    const std::vector<int> allowed = {16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2};
+    std::vector<int> cur, best;
+    best_factorization(N, allowed, cur, best);
+    for (int r : best) p->radix[p->nst++] = r;
+  }
+  if (p->nst == 0) p->radix[p->nst++] = N == 1 ? 1 : N;  // N == 1 is rejected by callers
   int Ls = N;
   for (int s = 0; s < p->nst; ++s) {
     p->M[s] = Ls / p->radix[s];
@@ -68,7 +101,8 @@ extern "C" {
 // a negative value for an unsupported N.  Radices are written to radix (<= 16).
 int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, int* radix) {
   bdda::AxisPlan p;
-  if (!bdda::make_axis_plan(N, &p)) return -1;
+  const int max_radix = (radix && radix[0] > 8) ? radix[0] : 8;
+  if (!bdda::make_axis_plan(N, &p, max_radix)) return -1;
   std::vector<double2> tw;
   bdda::make_twiddles(N, &tw);
   // nvalid: forward transforms read only the first nvalid inputs (zero padding)
@@ -76,8 +110,8 @@ int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, i
   if (prec == 1) {
     std::vector<double2> s(bdda::line_words<double2>(N), make_double2(1e300, 1e300));
     for (int i = 0; i < N; ++i) s[bdda::skw<double2>(i)] = make_double2(data[2 * i], data[2 * i + 1]);
-    if (inverse) bdda::warp_fft<true>(s.data(), tw.data(), p, 0, 1);
-    else bdda::warp_fft<false>(s.data(), tw.data(), p, 0, 1, nv);
+    if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, tw.data(), p, 0, 1);
+    else bdda::warp_fft_lines<false, 1>(s.data(), 0, tw.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
       const double2 v = s[bdda::skw<double2>(i)];
       data[2 * i] = v.x; data[2 * i + 1] = v.y;
@@ -88,8 +122,8 @@ int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, i
       s[bdda::skw<bdda::dfc>(i)] = bdda::cmake(bdda::dfl(data[2 * i]), bdda::dfl(data[2 * i + 1]));
       t[i] = bdda::cmake(bdda::dfl(tw[i].x), bdda::dfl(tw[i].y));
     }
-    if (inverse) bdda::warp_fft<true>(s.data(), t.data(), p, 0, 1);
-    else bdda::warp_fft<false>(s.data(), t.data(), p, 0, 1, nv);
+    if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, t.data(), p, 0, 1);
+    else bdda::warp_fft_lines<false, 1>(s.data(), 0, t.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
       const bdda::dfc v = s[bdda::skw<bdda::dfc>(i)];
       data[2 * i] = bdda::df_to_double(v.x); data[2 * i + 1] = bdda::df_to_double(v.y);
@@ -100,8 +134,8 @@ int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, i
       s[bdda::skw<float2>(i)] = make_float2((float)data[2 * i], (float)data[2 * i + 1]);
       t[i] = make_float2((float)tw[i].x, (float)tw[i].y);
     }
-    if (inverse) bdda::warp_fft<true>(s.data(), t.data(), p, 0, 1);
-    else bdda::warp_fft<false>(s.data(), t.data(), p, 0, 1, nv);
+    if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, t.data(), p, 0, 1);
+    else bdda::warp_fft_lines<false, 1>(s.data(), 0, t.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
       const float2 v = s[bdda::skw<float2>(i)];
       data[2 * i] = v.x; data[2 * i + 1] = v.y;

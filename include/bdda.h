@@ -284,8 +284,10 @@ const char* bdda_last_error(void);
  * arithmetic.  nvalid in
  * (0, N) makes the forward transform read only the first nvalid inputs (the
  * rest count as zero); 0 reads all.  data holds N interleaved complex doubles,
- * overwritten.  Returns the number of radix stages (radices written to
- * radix[0..16)) or -1 for an unsupported N.
+ * overwritten.  radix[0] on input > 8 selects the composite-radix schedule
+ * (register radices up to that value, as used along z); radices are written
+ * to radix[0..16) on return.  Returns the number of radix stages or -1 for an
+ * unsupported N.
  */
 int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, int* radix);
 
