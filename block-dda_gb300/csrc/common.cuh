@@ -114,6 +114,10 @@ struct AxisPlan {
   int M[kMaxStages];
   int tstride[kMaxStages];
   float invM[kMaxStages];
+  int sk[2];  // shared-memory skew shift for 8-byte / 16-byte elements (31: no skew)
+  int lw[2];  // shared-memory line pitch (elements) for 8-byte / 16-byte elements
 };
+// Upper bound of AxisPlan::lw (skew shift >= 3, pitch padding < 16).
+constexpr int kMaxLineWords = kMaxLine + kMaxLine / 8 + 16;
 
 }  // namespace bdda

@@ -1,6 +1,7 @@
-// Warp-per-line in-place mixed-radix (2,3,4,5,8) FFT in shared memory.
+// Warp-per-line in-place mixed-radix FFT in shared memory: register radices
+// 2, 3, 4, 5, 8 and the composite 6, 9, 10, 12, 15, 16.
 //
-// One warp owns one line of length N <= kMaxLine held in shared memory.
+// One warp owns one (or NL) line(s) of length N <= kMaxLine held in shared memory.
 //
 // Forward = decimation in frequency (Gentleman-Sande), natural-order input,
 // digit-reversed output.  With N = R_1 R_2 ... R_m, stage s works on blocks
@@ -16,8 +17,8 @@
 // matching (permuted) frequencies and the inverse restores natural order.
 // Each butterfly reads and writes the same positions, so a stage needs no
 // register staging and only one buffer; lanes take consecutive n1.  Lines
-// are stored with a 128-byte skew (skw) so that the strided accesses of the
-// last stages do not collide in shared-memory banks.
+// are stored skewed (skw) with a per-plan shift and pitch, so that the strided
+// accesses of the last stages do not collide in shared-memory banks.
 //
 // Twiddle table (per axis, global memory, read through L1):
 //   tw[t] = exp(-2 pi i t / N), t in [0, N), computed in FP64 on the host.
@@ -231,12 +232,14 @@ template <int R, bool INV, typename C> BDDA_FFT_FN void dft(C* v) {
 }
 
 // ---- shared-memory line layout ---------------------------------------------
-// Element i of a line lives at skw(i) = i + i / (128 bytes / sizeof(C)): one
-// pad element per 128 bytes, so the stride-R accesses of the last stages (and
-// the transposed tile loads) spread over all banks.
-template <typename C> BDDA_FFT_FN int skw(int i) { return i + (i >> (sizeof(C) == 8 ? 4 : 3)); }
-// Shared-memory elements one line of n points occupies (rounded to 16 bytes).
-template <typename C> BDDA_HD int line_words(int n) { return ((n + (n >> (sizeof(C) == 8 ? 4 : 3)) + 1) + 1) & ~1; }
+// Element i of a line lives at skw(i, sh) = i + (i >> sh) and consecutive
+// lines are lw elements apart.  The axis plan picks sh and lw per element
+// size (and the radix order) with a bank model, so that the strided butterfly
+// accesses, the multi-line stages and the transposed tile loads spread over
+// the 32 banks (make_axis_plan).
+BDDA_FFT_FN int skw(int i, int sh) { return i + (i >> sh); }
+template <typename C> BDDA_HD int plan_sk(const AxisPlan& p) { return p.sk[sizeof(C) == 8 ? 0 : 1]; }
+template <typename C> BDDA_HD int plan_lw(const AxisPlan& p) { return p.lw[sizeof(C) == 8 ? 0 : 1]; }
 
 // ---- in-place stages ---------------------------------------------------------
 // One stage applied to NL lines of one warp (line j at s + j * lw); the
@@ -244,8 +247,8 @@ template <typename C> BDDA_HD int line_words(int n) { return ((n + (n >> (sizeof
 // the warp.  nvalid < N (forward first stage only): inputs at positions
 // >= nvalid are known zeros and are not read (zero padding needs no fill).
 template <int R, bool INV, int NL, typename C>
-BDDA_FFT_FN void warp_stage_lines(C* __restrict__ s, int lw, const C* __restrict__ tw, int M, int tstride, float invM,
-                                  int N, int lane, int lanes, int nvalid) {
+BDDA_FFT_FN void warp_stage_lines(C* __restrict__ s, int lw, int sh, const C* __restrict__ tw, int M, int tstride,
+                                  float invM, int N, int lane, int lanes, int nvalid) {
   const int nb = N / R;
   const int Ls = M * R;
   const float inv_nb = 1.0f / (float)nb;
@@ -259,8 +262,8 @@ BDDA_FFT_FN void warp_stage_lines(C* __restrict__ s, int lw, const C* __restrict
     C v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      if (nvalid < N) v[i] = (n1 + i * M < nvalid) ? sl[skw<C>(base + i * M)] : czero<C>();
-      else v[i] = sl[skw<C>(base + i * M)];
+      if (nvalid < N) v[i] = (n1 + i * M < nvalid) ? sl[skw(base + i * M, sh)] : czero<C>();
+      else v[i] = sl[skw(base + i * M, sh)];
     }
     if (!INV) {
       dft<R, false>(v);
@@ -278,7 +281,7 @@ BDDA_FFT_FN void warp_stage_lines(C* __restrict__ s, int lw, const C* __restrict
       dft<R, true>(v);
     }
 #pragma unroll
-    for (int i = 0; i < R; ++i) sl[skw<C>(base + i * M)] = v[i];
+    for (int i = 0; i < R; ++i) sl[skw(base + i * M, sh)] = v[i];
   }
   BDDA_SYNCWARP();
 }
@@ -288,30 +291,30 @@ BDDA_FFT_FN void warp_stage_lines(C* __restrict__ s, int lw, const C* __restrict
 template <bool INV, int NL, bool FULL, typename C>
 BDDA_FFT_FN void warp_stage_lines_dispatch(const AxisPlan& p, int st, C* s, int lw, const C* tw, int lane, int lanes,
                                            int nvalid) {
-  const int M = p.M[st], ts = p.tstride[st];
+  const int M = p.M[st], ts = p.tstride[st], sh = plan_sk<C>(p);
   const float iM = p.invM[st];
   if (!FULL) {
     switch (p.radix[st]) {
-      case 2: warp_stage_lines<2, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-      case 3: warp_stage_lines<3, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-      case 4: warp_stage_lines<4, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-      case 5: warp_stage_lines<5, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-      default: warp_stage_lines<8, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+      case 2: warp_stage_lines<2, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+      case 3: warp_stage_lines<3, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+      case 4: warp_stage_lines<4, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+      case 5: warp_stage_lines<5, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+      default: warp_stage_lines<8, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
     }
     return;
   }
   switch (p.radix[st]) {
-    case 2: warp_stage_lines<2, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 3: warp_stage_lines<3, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 4: warp_stage_lines<4, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 5: warp_stage_lines<5, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 6: warp_stage_lines<6, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 8: warp_stage_lines<8, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 9: warp_stage_lines<9, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 10: warp_stage_lines<10, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 12: warp_stage_lines<12, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    case 15: warp_stage_lines<15, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    default: warp_stage_lines<16, INV, NL>(s, lw, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 2: warp_stage_lines<2, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 3: warp_stage_lines<3, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 4: warp_stage_lines<4, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 5: warp_stage_lines<5, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 6: warp_stage_lines<6, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 8: warp_stage_lines<8, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 9: warp_stage_lines<9, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 10: warp_stage_lines<10, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 12: warp_stage_lines<12, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 15: warp_stage_lines<15, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    default: warp_stage_lines<16, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
   }
 }
 

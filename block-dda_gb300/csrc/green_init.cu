@@ -74,24 +74,25 @@ constexpr int kInitWarps = 8;
 __global__ void __launch_bounds__(kInitWarps * 32)
 k_fft_contig(double2* __restrict__ data, size_t nlines, AxisPlan p, const double2* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lw = line_words<double2>(p.N);
+  const int lw = plan_lw<double2>(p), sh = plan_sk<double2>(p);
   double2* smem = reinterpret_cast<double2*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t line = (size_t)blockIdx.x * kInitWarps + warp;
   if (line >= nlines) return;
   double2* s = smem + warp * lw;
   double2* d = data + line * p.N;
-  for (int i = lane; i < p.N; i += 32) s[skw<double2>(i)] = d[i];
+  for (int i = lane; i < p.N; i += 32) s[skw(i, sh)] = d[i];
   __syncwarp();
   warp_fft_lines<false, 1>(s, 0, tw, p, lane);  // any schedule (the z axis uses composite radices)
-  for (int i = lane; i < p.N; i += 32) d[i] = s[skw<double2>(i)];
+  for (int i = lane; i < p.N; i += 32) d[i] = s[skw(i, sh)];
 }
 
 // In-place forward FFT along the middle index of data[A][N][Cc], 8 columns per CTA.
 __global__ void __launch_bounds__(kInitWarps * 32)
-k_fft_strided(double2* __restrict__ data, int N, size_t Cc, AxisPlan p, const double2* __restrict__ tw) {
+k_fft_strided(double2* __restrict__ data, size_t Cc, AxisPlan p, const double2* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lw = line_words<double2>(N);
+  const int N = p.N;
+  const int lw = plan_lw<double2>(p), sh = plan_sk<double2>(p);
   double2* smem = reinterpret_cast<double2*>(smem_raw);
   const size_t c0 = (size_t)blockIdx.x * kInitWarps;
   double2* base = data + (size_t)blockIdx.y * N * Cc;
@@ -99,7 +100,7 @@ k_fft_strided(double2* __restrict__ data, int N, size_t Cc, AxisPlan p, const do
   for (int idx = tid; idx < N * kInitWarps; idx += kInitWarps * 32) {
     const int w = idx % kInitWarps, i = idx / kInitWarps;
     const size_t c = c0 + w;
-    smem[w * lw + skw<double2>(i)] = (c < Cc) ? base[(size_t)i * Cc + c] : make_double2(0.0, 0.0);
+    smem[w * lw + skw(i, sh)] = (c < Cc) ? base[(size_t)i * Cc + c] : make_double2(0.0, 0.0);
   }
   __syncthreads();
   warp_fft<false>(smem + (tid >> 5) * lw, tw, p, tid & 31);
@@ -107,7 +108,7 @@ k_fft_strided(double2* __restrict__ data, int N, size_t Cc, AxisPlan p, const do
   for (int idx = tid; idx < N * kInitWarps; idx += kInitWarps * 32) {
     const int w = idx % kInitWarps, i = idx / kInitWarps;
     const size_t c = c0 + w;
-    if (c < Cc) base[(size_t)i * Cc + c] = smem[w * lw + skw<double2>(i)];
+    if (c < Cc) base[(size_t)i * Cc + c] = smem[w * lw + skw(i, sh)];
   }
 }
 
@@ -137,7 +138,7 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
   static std::once_flag once;
   static cudaError_t cfg = cudaSuccess;
   std::call_once(once, [] {
-    const int maxsm = kInitWarps * line_words<double2>(kMaxLine) * (int)sizeof(double2);
+    const int maxsm = kInitWarps * kMaxLineWords * (int)sizeof(double2);
     cfg = cudaFuncSetAttribute(k_fft_contig, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     if (cfg == cudaSuccess) cfg = cudaFuncSetAttribute(k_fft_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
   });
@@ -146,21 +147,21 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
   // z lines (contiguous)
   {
     const size_t nlines = 6 * (size_t)Px * Py;
-    const int sm = kInitWarps * line_words<double2>(Pz) * (int)sizeof(double2);
+    const int sm = kInitWarps * plan_lw<double2>(g.pz) * (int)sizeof(double2);
     k_fft_contig<<<(unsigned)((nlines + kInitWarps - 1) / kInitWarps), kInitWarps * 32, sm, st>>>(work, nlines, g.pz, twz);
   }
   // y lines: data[6*Px][Py][Pz]
   {
     dim3 grid((unsigned)((Pz + kInitWarps - 1) / kInitWarps), 6 * Px);
-    const int sm = kInitWarps * line_words<double2>(Py) * (int)sizeof(double2);
-    k_fft_strided<<<grid, kInitWarps * 32, sm, st>>>(work, Py, (size_t)Pz, g.py, twy);
+    const int sm = kInitWarps * plan_lw<double2>(g.py) * (int)sizeof(double2);
+    k_fft_strided<<<grid, kInitWarps * 32, sm, st>>>(work, (size_t)Pz, g.py, twy);
   }
   // x lines: data[6][Px][Py*Pz]
   {
     const size_t cc = (size_t)Py * Pz;
     dim3 grid((unsigned)((cc + kInitWarps - 1) / kInitWarps), 6);
-    const int sm = kInitWarps * line_words<double2>(Px) * (int)sizeof(double2);
-    k_fft_strided<<<grid, kInitWarps * 32, sm, st>>>(work, Px, cc, g.px, twx);
+    const int sm = kInitWarps * plan_lw<double2>(g.px) * (int)sizeof(double2);
+    k_fft_strided<<<grid, kInitWarps * 32, sm, st>>>(work, cc, g.px, twx);
   }
   const double scale = 1.0 / (double)ng;
   if (ghat_d) k_green_pack<double2><<<2432, 256, 0, st>>>(work, ghat_d, Px, Py, Pz, scale);

@@ -105,6 +105,11 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
 
 template <typename T> cudaError_t configure_mvp_kernels();
 
+// Pass C for complex FP32 with the compile-time z plan of g.Pz (zplans.inc);
+// returns false (nothing launched) when g.Pz has none.  *err: launch status.
+bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2* ghat, cudaStream_t st,
+                          const int* done, cudaError_t* err);
+
 // Green tensor: build Ghat (FP64 evaluation + FP64 3-D FFT), layout
 // [Px][Py][6][Pz], for either precision (null pointers skipped).
 // work: c128 [6*Px*Py*Pz].
@@ -112,9 +117,11 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
                             const double2* twx, const double2* twy, const double2* twz,
                             double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, cudaStream_t st);
 
-// Radix schedule + FP64 twiddles for a 5-smooth N <= kMaxLine.  max_radix 8:
-// radices 8, 4, 2, 5, 3 (one line per warp); max_radix 16: fewest stages with
-// composite register radices up to 16 (multi-line warps).
+// Radix schedule, shared-memory layout and FP64 twiddles for a 5-smooth
+// 2 <= N <= kMaxLine.  max_radix 8: radices 2, 3, 4, 5, 8 for the single-line
+// tile passes; max_radix 16: composite register radices up to 16 for the
+// three-line z pass.  Fewest stages; the radix order, skew shift and line
+// pitch minimise a shared-memory bank model of the pass (cached per N).
 bool make_axis_plan(int N, AxisPlan* p, int max_radix = 8);
 void make_twiddles(int N, std::vector<double2>* out);
 

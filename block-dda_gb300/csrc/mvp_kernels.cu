@@ -31,8 +31,10 @@
 // tile with cp.async (zero-filled outside the box) while the current one is
 // transformed.
 #include <algorithm>
+#include <type_traits>
 
 #include "fft_core.cuh"
+
 #include "mvp.hpp"
 
 namespace bdda {
@@ -65,7 +67,7 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, cons
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Px = px.N;
-  const int lw = line_words<C>(Px);
+  const int lw = plan_lw<C>(px), sh = plan_sk<C>(px);
   C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
   int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
   const int tile = tiles[blockIdx.x];
@@ -83,7 +85,7 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, cons
     const C* xc = x + (size_t)l * ldx + c;
     for (int xi = lane; xi < nx; xi += 32) {
       const int m = socc[xi * kTZ + warp];
-      line[skw<C>(xi)] = m >= 0 ? xc[3 * (size_t)m] : czero<C>();
+      line[skw(xi, sh)] = m >= 0 ? xc[3 * (size_t)m] : czero<C>();
     }
     __syncwarp();
     warp_fft<false>(line, twx, px, lane, 32, nx);
@@ -92,7 +94,7 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, cons
     const C* lb = lines + (f & 1) * kTZ * lw;
     for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
       const int w = idx & 7, q = idx >> 3;
-      if (z0 + w < nz) out[(size_t)q * rowstride + w] = lb[w * lw + skw<C>(q)];
+      if (z0 + w < nz) out[(size_t)q * rowstride + w] = lb[w * lw + skw(q, sh)];
     }
     if (++c == 3) { c = 0; ++l; }
   }
@@ -111,7 +113,7 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Py = py.N;
-  const int lw = line_words<C>(Py);
+  const int lw = plan_lw<C>(py), sh = plan_sk<C>(py);
   C* lines = reinterpret_cast<C*>(smem_raw);  // [2][kTZ][lw]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nin = INV ? Py : ny;    // rows read
@@ -129,7 +131,7 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
       bool valid = z0 + w < nz;
       if (!INV) valid = valid && tmask[yy * nzt + zt];
       const C* g = valid ? base + (size_t)yy * nz + w : src;
-      cp_async<sizeof(C)>(lb + w * lw + skw<C>(yy), g, valid);
+      cp_async<sizeof(C)>(lb + w * lw + skw(yy, sh), g, valid);
     }
     cp_commit();
   };
@@ -158,7 +160,7 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
       const int w = idx & 7, yy = idx >> 3;
       if (z0 + w >= nz) continue;
       if (INV && !tmask[yy * nzt + zt]) continue;
-      ob[(size_t)yy * nz + w] = lb[w * lw + skw<C>(yy)];
+      ob[(size_t)yy * nz + w] = lb[w * lw + skw(yy, sh)];
     }
     __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
   }
@@ -175,7 +177,7 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz,
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Pz = pz.N;
-  const int lw = line_words<C>(Pz);
+  const int lw = plan_lw<C>(pz), sh = plan_sk<C>(pz);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long task = (long long)blockIdx.x * kZWarps + warp;
   const long long ntask = (long long)Px * Py * L;
@@ -188,15 +190,15 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz,
   const size_t fstride = (size_t)Px * Py * nz;  // between fields
   C* g0 = t2 + (size_t)(3 * l) * fstride + (size_t)line * nz;
   for (int z = lane; z < nz; z += 32) {
-    s0[skw<C>(z)] = g0[z];
-    s1[skw<C>(z)] = g0[fstride + z];
-    s2[skw<C>(z)] = g0[2 * fstride + z];
+    s0[skw(z, sh)] = g0[z];
+    s1[skw(z, sh)] = g0[fstride + z];
+    s2[skw(z, sh)] = g0[2 * fstride + z];
   }
   __syncwarp();
   warp_fft_lines<false, 3>(s0, lw, twz, pz, lane, 32, nz);
   const C* gl = ghat + (size_t)line * 6 * Pz;
   for (int p = lane; p < Pz; p += 32) {
-    const int sp = skw<C>(p);
+    const int sp = skw(p, sh);
     const C a0 = s0[sp], a1 = s1[sp], a2 = s2[sp];
     const C gxx = ldg_c(gl + p), gxy = ldg_c(gl + Pz + p), gxz = ldg_c(gl + 2 * Pz + p);
     const C gyy = ldg_c(gl + 3 * Pz + p), gyz = ldg_c(gl + 4 * Pz + p), gzz = ldg_c(gl + 5 * Pz + p);
@@ -207,9 +209,9 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz,
   __syncwarp();
   warp_fft_lines<true, 3>(s0, lw, twz, pz, lane);
   for (int z = lane; z < nz; z += 32) {
-    g0[z] = s0[skw<C>(z)];
-    g0[fstride + z] = s1[skw<C>(z)];
-    g0[2 * fstride + z] = s2[skw<C>(z)];
+    g0[z] = s0[skw(z, sh)];
+    g0[fstride + z] = s1[skw(z, sh)];
+    g0[2 * fstride + z] = s2[skw(z, sh)];
   }
 }
 
@@ -227,7 +229,7 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, const int* _
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Px = px.N;
-  const int lw = line_words<C>(Px);
+  const int lw = plan_lw<C>(px), sh = plan_sk<C>(px);
   C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
   int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
   const int tile = tiles[blockIdx.x];
@@ -244,7 +246,7 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, const int* _
     for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
       const int w = idx & 7, q = idx >> 3;
       const bool valid = z0 + w < nz;
-      cp_async<sizeof(C)>(lb + w * lw + skw<C>(q), valid ? base + (size_t)q * rowstride + w : t1, valid);
+      cp_async<sizeof(C)>(lb + w * lw + skw(q, sh), valid ? base + (size_t)q * rowstride + w : t1, valid);
     }
     cp_commit();
   };
@@ -265,7 +267,7 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, const int* _
       const int m = socc[xi * kTZ + warp];
       if (m < 0) continue;
       const size_t r = 3 * (size_t)m + c;
-      C v = line[skw<C>(xi)];
+      C v = line[skw(xi, sh)];
       if (diag != nullptr) v = cadd(v, cmul(diag[r], x[(size_t)l * ldx + r]));
       if (jpre != nullptr) v = cmul(v, jpre[r]);
       y[(size_t)l * ldy + r] = v;
@@ -275,12 +277,10 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, const int* _
   }
 }
 
-template <typename T> int smem_tile(int N, int nx) {
-  return 2 * kTZ * line_words<typename cplx<T>::type>(N) * (int)sizeof(typename cplx<T>::type) + nx * kTZ * 4;
+template <typename T> int smem_tile(int lw, int nx) {
+  return 2 * kTZ * lw * (int)sizeof(typename cplx<T>::type) + nx * kTZ * 4;
 }
-template <typename T> int smem_z(int Pz) {
-  return kZWarps * 3 * line_words<typename cplx<T>::type>(Pz) * (int)sizeof(typename cplx<T>::type);
-}
+template <typename T> int smem_z(int lw) { return kZWarps * 3 * lw * (int)sizeof(typename cplx<T>::type); }
 
 int num_sms() {
   static const int n = [] {
@@ -301,6 +301,7 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
                              const typename cplx<T>::type* diag, const typename cplx<T>::type* jpre,
                              typename cplx<T>::type* t1, typename cplx<T>::type* t2,
                              cudaStream_t st, KernelTimer* timer, const int* done) {
+  using C = typename cplx<T>::type;
   const int nfield = 3 * L;
   const int pbase = sizeof(T) == sizeof(double) ? (kPassA64 - kPassA) : 0;
   if (g.ntiles == 0) return cudaSuccess;  // no dipoles
@@ -308,12 +309,12 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   const int grid_y = std::min(ntask_y, num_sms() * 8);
   // A
   if (timer) timer->begin(kPassA + pbase, st);
-  k_pass_a<T><<<g.ntiles, kTileThreads, smem_tile<T>(g.Px, g.nx), st>>>(x, ldx, nfield, g.occ, g.tiles, g.nx, g.ny,
+  k_pass_a<T><<<g.ntiles, kTileThreads, smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(x, ldx, nfield, g.occ, g.tiles, g.nx, g.ny,
                                                                        g.nz, g.nzt, g.px, p.twx, t1, done);
   if (timer) timer->end(kPassA + pbase, st);
   // B
   if (timer) timer->begin(kPassB + pbase, st);
-  k_pass_y<T, false><<<grid_y, kTileThreads, smem_tile<T>(g.Py, 0), st>>>(t1, t2, g.tmask, g.ny, g.nz, g.nzt,
+  k_pass_y<T, false><<<grid_y, kTileThreads, smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(t1, t2, g.tmask, g.ny, g.nz, g.nzt,
                                                                          ntask_y, g.py, p.twy, done);
   if (timer) timer->end(kPassB + pbase, st);
   // C
@@ -321,17 +322,25 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
     const long long ntask = (long long)g.Px * g.Py * L;
     const unsigned grid = (unsigned)((ntask + kZWarps - 1) / kZWarps);
     if (timer) timer->begin(kPassC + pbase, st);
-    k_pass_c<T><<<grid, kZWarps * 32, smem_z<T>(g.Pz), st>>>(t2, L, g.Px, g.Py, g.nz, g.pz, p.twz, p.ghat, done);
+    bool launched = false;
+    if constexpr (std::is_same<T, float>::value) {
+      cudaError_t e = cudaSuccess;
+      launched = launch_pass_c_static(g, t2, L, p.twz, p.ghat, st, done, &e);
+      if (launched && e != cudaSuccess) return e;
+    }
+    if (!launched)
+      k_pass_c<T><<<grid, kZWarps * 32, smem_z<T>(plan_lw<C>(g.pz)), st>>>(t2, L, g.Px, g.Py, g.nz, g.pz, p.twz, p.ghat,
+                                                                          done);
     if (timer) timer->end(kPassC + pbase, st);
   }
   // D
   if (timer) timer->begin(kPassD + pbase, st);
-  k_pass_y<T, true><<<grid_y, kTileThreads, smem_tile<T>(g.Py, 0), st>>>(t2, t1, g.tmask, g.ny, g.nz, g.nzt,
+  k_pass_y<T, true><<<grid_y, kTileThreads, smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(t2, t1, g.tmask, g.ny, g.nz, g.nzt,
                                                                         ntask_y, g.py, p.twy, done);
   if (timer) timer->end(kPassD + pbase, st);
   // E
   if (timer) timer->begin(kPassE + pbase, st);
-  k_pass_e<T><<<g.ntiles, kTileThreads, smem_tile<T>(g.Px, g.nx), st>>>(t1, nfield, g.occ, g.tiles, g.nx, g.ny, g.nz,
+  k_pass_e<T><<<g.ntiles, kTileThreads, smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(t1, nfield, g.occ, g.tiles, g.nx, g.ny, g.nz,
                                                                        g.nzt, g.px, p.twx, x, ldx, diag, jpre, y, ldy,
                                                                        done);
   if (timer) timer->end(kPassE + pbase, st);
@@ -340,8 +349,8 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
 
 template <typename T>
 cudaError_t configure_mvp_kernels() {
-  const int tile = smem_tile<T>(kMaxLine, kMaxLine / 2);
-  const int zs = smem_z<T>(kMaxLine);
+  const int tile = smem_tile<T>(kMaxLineWords, kMaxLine / 2);
+  const int zs = smem_z<T>(kMaxLineWords);
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(k_pass_a<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_pass_e<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;

@@ -2,6 +2,9 @@
 // that runs the exact device FFT core on the CPU for unit tests.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "../../include/bdda.h"
@@ -11,61 +14,229 @@
 namespace bdda {
 
 namespace {
-// Fewest stages using register radices from `allowed` (largest first on ties
-// of stage count, then the smallest largest radix for lane occupancy).
-void best_factorization(int N, const std::vector<int>& allowed, std::vector<int>& cur, std::vector<int>& best) {
-  if (N == 1) {
-    if (best.empty() || cur.size() < best.size() ||
-        (cur.size() == best.size() && *std::max_element(cur.begin(), cur.end()) < *std::max_element(best.begin(), best.end())))
-      best = cur;
+// Fewest stages using register radices from `allowed`.
+int min_stages(int N, const std::vector<int>& allowed, int depth, int best) {
+  if (N == 1) return depth;
+  if (depth + 1 >= best) return best;
+  for (int r : allowed)
+    if (N % r == 0) best = std::min(best, min_stages(N / r, allowed, depth + 1, best));
+  return best;
+}
+
+// Every ordered radix sequence of exactly `len` stages with product N.
+void sequences(int N, const std::vector<int>& allowed, int len, std::vector<int>& cur,
+               std::vector<std::vector<int>>& out) {
+  if ((int)cur.size() == len) {
+    if (N == 1) out.push_back(cur);
     return;
   }
-  if (!best.empty() && cur.size() + 1 > best.size()) return;
   for (int r : allowed) {
     if (N % r) continue;
-    if (!cur.empty() && r > cur.back()) continue;  // non-increasing order: each multiset once
     cur.push_back(r);
-    best_factorization(N / r, allowed, cur, best);
+    sequences(N / r, allowed, len, cur, out);
     cur.pop_back();
   }
+}
+
+// ---- shared-memory bank model ----------------------------------------------
+// 32 banks of 4 bytes.  8-byte accesses of a warp are served per half-warp and
+// 16-byte accesses per quarter-warp; a group takes as many wavefronts as the
+// largest number of distinct 4-byte words that fall into one bank.  (This
+// reproduces the shared-memory wavefront counts ncu reports for the passes.)
+int wavefronts(const int* addr, int n, int esize) {
+  const int g = 128 / esize, wpe = esize / 4;
+  int total = 0;
+  for (int g0 = 0; g0 < n; g0 += g) {
+    int cnt[32] = {0};
+    int words[32][16];
+    int worst = 0;
+    const int g1 = std::min(n, g0 + g);
+    for (int l = g0; l < g1; ++l)
+      for (int k = 0; k < wpe; ++k) {
+        const int w = addr[l] * wpe + k, b = w & 31;
+        bool seen = false;
+        for (int q = 0; q < cnt[b] && !seen; ++q) seen = words[b][q] == w;
+        if (!seen) {
+          words[b][cnt[b]++] = w;
+          worst = std::max(worst, cnt[b]);
+        }
+      }
+    total += worst;
+  }
+  return total;
+}
+
+int skew(int i, int sh) { return i + (i >> sh); }
+
+// Butterfly loads of one transform over NL lines of pitch lw, lanes mapped as
+// warp_stage_lines maps them (the stores repeat the same addresses).
+long stage_cost(int N, const std::vector<int>& rad, int NL, int lw, int sh, int esize) {
+  long c = 0;
+  int addr[32];
+  int Ls = N;
+  for (int R : rad) {
+    const int M = Ls / R, nb = N / R;
+    for (int t0 = 0; t0 < NL * nb; t0 += 32) {
+      const int n = std::min(32, NL * nb - t0);
+      for (int i = 0; i < R; ++i) {
+        for (int l = 0; l < n; ++l) {
+          const int t = t0 + l, j = t / nb, tt = t - j * nb, b = tt / M, n1 = tt - b * M;
+          addr[l] = j * lw + skew(b * Ls + n1 + i * M, sh);
+        }
+        c += wavefronts(addr, n, esize);
+      }
+    }
+    Ls = M;
+  }
+  return c;
+}
+
+// Tile transposes of the strided passes: idx -> line idx & 7, position idx >> 3.
+long tile_cost(int N, int lw, int sh, int esize) {
+  long c = 0;
+  int addr[32];
+  for (int i0 = 0; i0 < 8 * N; i0 += 32) {
+    const int n = std::min(32, 8 * N - i0);
+    for (int l = 0; l < n; ++l) addr[l] = ((i0 + l) & 7) * lw + skew((i0 + l) >> 3, sh);
+    c += wavefronts(addr, n, esize);
+  }
+  return c;
+}
+
+// Contiguous per-line accesses (loads, stores and the spectral product of the z pass).
+long contig_cost(int N, int NL, int lw, int sh, int esize) {
+  long c = 0;
+  int addr[32];
+  for (int j = 0; j < NL; ++j)
+    for (int z0 = 0; z0 < N; z0 += 32) {
+      const int n = std::min(32, N - z0);
+      for (int l = 0; l < n; ++l) addr[l] = j * lw + skew(z0 + l, sh);
+      c += wavefronts(addr, n, esize);
+    }
+  return c;
+}
+
+constexpr int kNoSkew = 31;
+const int kShifts[] = {kNoSkew, 3, 4, 5, 6, 7, 8};
+
+// Modelled wavefronts per line of the pass that uses the plan: single-line
+// plans serve the tile passes (one forward or inverse transform + a tile fill
+// and drain), three-line plans the fused z pass (forward + inverse + the
+// contiguous load, product and store).
+long plan_cost(int N, const std::vector<int>& rad, bool three, int lw, int sh, int esize) {
+  if (three) return 2 * stage_cost(N, rad, 3, lw, sh, esize) + 2 * contig_cost(N, 3, lw, sh, esize);
+  return stage_cost(N, rad, 1, lw, sh, esize) + tile_cost(N, lw, sh, esize);
+}
+
+struct Layout { long cost; int sh, lw; };
+
+Layout best_layout(int N, const std::vector<int>& rad, bool three, int esize) {
+  Layout best{-1, kNoSkew, N};
+  const int dmax = esize == 8 ? 16 : 8;
+  for (int sh : kShifts)
+    for (int d = 0; d < dmax; ++d) {
+      const int lw = skew(N - 1, sh) + 1 + d;
+      const long c = plan_cost(N, rad, three, lw, sh, esize);
+      if (best.cost < 0 || c < best.cost) best = {c, sh, lw};
+    }
+  return best;
+}
+
+struct PlanChoice { std::vector<int> rad; Layout l8, l16; };
+
+// Radix sequences of the compile-time z plans (the fused z pass for complex
+// FP32 runs them; the z axis of every operator uses the same sequence so that
+// all transforms share the Green spectrum's digit order).
+struct ZPlanRow { int N, S, LW; int rad[kMaxStages]; };
+constexpr ZPlanRow kZPlans[] = {
+#define BDDA_ZPLAN(I, N, S, LW, ...) {N, S, LW, {__VA_ARGS__}},
+#include "zplans.inc"
+#undef BDDA_ZPLAN
+};
+
+bool zplan_radices(int N, std::vector<int>* rad) {
+  for (const ZPlanRow& z : kZPlans)
+    if (z.N == N) {
+      rad->clear();
+      for (int s = 0; s < kMaxStages && z.rad[s] > 0; ++s) rad->push_back(z.rad[s]);
+      return true;
+    }
+  return false;
+}
+
+// Radix order, skew and pitch by the bank model: among the fewest-stage radix
+// sequences, the one whose best 8-byte layout takes the fewest wavefronts
+// (complex FP32 is the hot precision); the 16-byte layout is then fitted to it.
+PlanChoice choose_plan(int N, bool three) {
+  PlanChoice best;
+  if (three && zplan_radices(N, &best.rad)) {
+    best.l8 = best_layout(N, best.rad, true, 8);
+    best.l16 = best_layout(N, best.rad, true, 16);
+    return best;
+  }
+  const std::vector<int> allowed = three ? std::vector<int>{16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2}
+                                         : std::vector<int>{8, 5, 4, 3, 2};
+  const int len = min_stages(N, allowed, 0, 64);
+  std::vector<std::vector<int>> seqs;
+  std::vector<int> cur;
+  sequences(N, allowed, len, cur, seqs);
+  // coarse pass: every sequence and shift at the minimal pitch; the best few then get every pitch
+  struct Cand { long cost; size_t s; };
+  std::vector<Cand> cand;
+  for (size_t i = 0; i < seqs.size(); ++i) {
+    long c = -1;
+    for (int sh : kShifts) {
+      const long v = plan_cost(N, seqs[i], three, skew(N - 1, sh) + 1, sh, 8);
+      if (c < 0 || v < c) c = v;
+    }
+    cand.push_back({c, i});
+  }
+  std::stable_sort(cand.begin(), cand.end(), [](const Cand& a, const Cand& b) { return a.cost < b.cost; });
+  best.l8.cost = -1;
+  for (size_t k = 0; k < cand.size() && k < 4; ++k) {
+    const Layout l = best_layout(N, seqs[cand[k].s], three, 8);
+    if (best.l8.cost < 0 || l.cost < best.l8.cost) {
+      best.rad = seqs[cand[k].s];
+      best.l8 = l;
+    }
+  }
+  best.l16 = best_layout(N, best.rad, three, 16);
+  return best;
 }
 }  // namespace
 
 bool make_axis_plan(int N, AxisPlan* p, int max_radix) {
-  if (N < 1 || N > kMaxLine) return false;
+  if (N < 2 || N > kMaxLine) return false;
   int t = N;
   for (int q : {2, 3, 5})
     while (t % q == 0) t /= q;
   if (t != 1) return false;
-  p->N = N;
-  p->nst = 0;
-  if (max_radix <= 8) {
-    int a = 0, b = 0, c = 0;
-    t = N;
-    while (t % 2 == 0) { t /= 2; ++a; }
-    while (t % 3 == 0) { t /= 3; ++b; }
-    while (t % 5 == 0) { t /= 5; ++c; }
-    auto push = [&](int r) { p->radix[p->nst++] = r; };
-    while (a >= 3) { push(8); a -= 3; }
-    if (a == 2) push(4);
-    if (a == 1) push(2);
-    for (int i = 0; i < c; ++i) push(5);
-    for (int i = 0; i < b; ++i) push(3);
-  } else {
-    const std::vector<int> allowed = {16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2};
-    std::vector<int> cur, best;
-    best_factorization(N, allowed, cur, best);
-    for (int r : best) p->radix[p->nst++] = r;
+  const bool three = max_radix > 8;
+  static std::mutex mu;
+  static std::map<std::pair<int, bool>, PlanChoice> cache;
+  PlanChoice ch;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({N, three});
+    if (it == cache.end()) it = cache.emplace(std::make_pair(N, three), choose_plan(N, three)).first;
+    ch = it->second;
   }
-  if (p->nst == 0) p->radix[p->nst++] = N == 1 ? 1 : N;  // N == 1 is rejected by callers
+  if ((int)ch.rad.size() > kMaxStages) return false;
+  p->N = N;
+  p->nst = (int)ch.rad.size();
   int Ls = N;
   for (int s = 0; s < p->nst; ++s) {
+    p->radix[s] = ch.rad[s];
     p->M[s] = Ls / p->radix[s];
     p->tstride[s] = N / Ls;
     p->invM[s] = 1.0f / (float)p->M[s];
     Ls = p->M[s];
   }
-  return p->nst <= kMaxStages;
+  p->sk[0] = ch.l8.sh;
+  p->lw[0] = ch.l8.lw;
+  p->sk[1] = ch.l16.sh;
+  p->lw[1] = ch.l16.lw;
+  return p->lw[0] <= kMaxLineWords && p->lw[1] <= kMaxLineWords;
 }
 
 void make_twiddles(int N, std::vector<double2>* out) {
@@ -108,36 +279,39 @@ int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, i
   // nvalid: forward transforms read only the first nvalid inputs (zero padding)
   const int nv = (nvalid > 0 && nvalid < N) ? nvalid : (1 << 30);
   if (prec == 1) {
-    std::vector<double2> s(bdda::line_words<double2>(N), make_double2(1e300, 1e300));
-    for (int i = 0; i < N; ++i) s[bdda::skw<double2>(i)] = make_double2(data[2 * i], data[2 * i + 1]);
+    const int sh = bdda::plan_sk<double2>(p);
+    std::vector<double2> s(bdda::plan_lw<double2>(p), make_double2(1e300, 1e300));
+    for (int i = 0; i < N; ++i) s[bdda::skw(i, sh)] = make_double2(data[2 * i], data[2 * i + 1]);
     if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, tw.data(), p, 0, 1);
     else bdda::warp_fft_lines<false, 1>(s.data(), 0, tw.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
-      const double2 v = s[bdda::skw<double2>(i)];
+      const double2 v = s[bdda::skw(i, sh)];
       data[2 * i] = v.x; data[2 * i + 1] = v.y;
     }
   } else if (prec == 3) {
-    std::vector<bdda::dfc> s(bdda::line_words<bdda::dfc>(N), bdda::cmake(bdda::dfl(1e30), bdda::dfl(1e30))), t(N);
+    const int sh = bdda::plan_sk<bdda::dfc>(p);
+    std::vector<bdda::dfc> s(bdda::plan_lw<bdda::dfc>(p), bdda::cmake(bdda::dfl(1e30), bdda::dfl(1e30))), t(N);
     for (int i = 0; i < N; ++i) {
-      s[bdda::skw<bdda::dfc>(i)] = bdda::cmake(bdda::dfl(data[2 * i]), bdda::dfl(data[2 * i + 1]));
+      s[bdda::skw(i, sh)] = bdda::cmake(bdda::dfl(data[2 * i]), bdda::dfl(data[2 * i + 1]));
       t[i] = bdda::cmake(bdda::dfl(tw[i].x), bdda::dfl(tw[i].y));
     }
     if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, t.data(), p, 0, 1);
     else bdda::warp_fft_lines<false, 1>(s.data(), 0, t.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
-      const bdda::dfc v = s[bdda::skw<bdda::dfc>(i)];
+      const bdda::dfc v = s[bdda::skw(i, sh)];
       data[2 * i] = bdda::df_to_double(v.x); data[2 * i + 1] = bdda::df_to_double(v.y);
     }
   } else {
-    std::vector<float2> s(bdda::line_words<float2>(N), make_float2(1e30f, 1e30f)), t(N);
+    const int sh = bdda::plan_sk<float2>(p);
+    std::vector<float2> s(bdda::plan_lw<float2>(p), make_float2(1e30f, 1e30f)), t(N);
     for (int i = 0; i < N; ++i) {
-      s[bdda::skw<float2>(i)] = make_float2((float)data[2 * i], (float)data[2 * i + 1]);
+      s[bdda::skw(i, sh)] = make_float2((float)data[2 * i], (float)data[2 * i + 1]);
       t[i] = make_float2((float)tw[i].x, (float)tw[i].y);
     }
     if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, t.data(), p, 0, 1);
     else bdda::warp_fft_lines<false, 1>(s.data(), 0, t.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
-      const float2 v = s[bdda::skw<float2>(i)];
+      const float2 v = s[bdda::skw(i, sh)];
       data[2 * i] = v.x; data[2 * i + 1] = v.y;
     }
   }
