@@ -327,7 +327,11 @@ def cross_sections(k, alpha0, E, P):
 
 
 def host_fft_line(x, inverse=False, prec=1, nvalid=0, max_radix=8):
-    """Run the device FFT core on the CPU (unit tests).  Returns (y, radices)."""
+    """Run the device FFT core on the CPU (unit tests).  Returns (y, radices).
+
+    The schedule is the operator's for an axis of this length and the element
+    width of prec: max_radix > 8 selects the z axis (three-line fused pass),
+    otherwise the x / y axes."""
     a = np.ascontiguousarray(x, dtype=np.complex128).copy()
     rad = np.zeros(16, np.int32)
     rad[0] = int(max_radix)

@@ -286,23 +286,13 @@ BDDA_FFT_FN void warp_stage_lines(C* __restrict__ s, int lw, int sh, const C* __
   BDDA_SYNCWARP();
 }
 
-// Stage dispatch.  FULL: every radix of make_axis_plan(N, 16) (composite
-// register radices); otherwise the radices of make_axis_plan(N, 8) only.
-template <bool INV, int NL, bool FULL, typename C>
+// Stage dispatch over every register radix of the plans (2, 3, 4, 5, 8 and
+// the composite 6, 9, 10, 12, 15, 16).
+template <bool INV, int NL, typename C>
 BDDA_FFT_FN void warp_stage_lines_dispatch(const AxisPlan& p, int st, C* s, int lw, const C* tw, int lane, int lanes,
                                            int nvalid) {
   const int M = p.M[st], ts = p.tstride[st], sh = plan_sk<C>(p);
   const float iM = p.invM[st];
-  if (!FULL) {
-    switch (p.radix[st]) {
-      case 2: warp_stage_lines<2, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-      case 3: warp_stage_lines<3, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-      case 4: warp_stage_lines<4, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-      case 5: warp_stage_lines<5, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-      default: warp_stage_lines<8, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    }
-    return;
-  }
   switch (p.radix[st]) {
     case 2: warp_stage_lines<2, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
     case 3: warp_stage_lines<3, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
@@ -318,29 +308,21 @@ BDDA_FFT_FN void warp_stage_lines_dispatch(const AxisPlan& p, int st, C* s, int 
   }
 }
 
-// NL lines of one warp transformed together (forward pruned to nvalid inputs),
-// any radix schedule (FULL) or the small-radix one.
-template <bool INV, int NL, bool FULL = true, typename C>
+// NL lines of one warp transformed together (forward pruned to nvalid inputs):
+// forward natural -> digit-reversed (DIF), inverse digit-reversed -> natural
+// (DIT, unnormalised).
+template <bool INV, int NL, typename C>
 BDDA_FFT_FN void warp_fft_lines(C* __restrict__ s, int lw, const C* __restrict__ tw, const AxisPlan& p, int lane,
                                 int lanes = 32, int nvalid = 1 << 30) {
   if (!INV) {
     for (int st = 0; st < p.nst; ++st)
-      warp_stage_lines_dispatch<false, NL, FULL>(p, st, s, lw, tw, lane, lanes, st == 0 ? nvalid : p.N);
+      warp_stage_lines_dispatch<false, NL>(p, st, s, lw, tw, lane, lanes, st == 0 ? nvalid : p.N);
   } else {
     for (int st = p.nst - 1; st >= 0; --st)
-      warp_stage_lines_dispatch<true, NL, FULL>(p, st, s, lw, tw, lane, lanes, p.N);
+      warp_stage_lines_dispatch<true, NL>(p, st, s, lw, tw, lane, lanes, p.N);
   }
 }
 
-// Full in-place transform of one line by one warp with a small-radix plan
-// (make_axis_plan(N, 8)).  INV = false: natural -> digit-reversed (DIF); only
-// the first nvalid inputs are read (the rest are taken as zero).  INV = true:
-// digit-reversed -> natural (DIT), unnormalised.
-template <bool INV, typename C>
-BDDA_FFT_FN void warp_fft(C* __restrict__ s, const C* __restrict__ tw, const AxisPlan& p, int lane, int lanes = 32,
-                          int nvalid = 1 << 30) {
-  warp_fft_lines<INV, 1, false>(s, 0, tw, p, lane, lanes, nvalid);
-}
 
 }  // namespace bdda
 

@@ -1,10 +1,14 @@
-"""Generates zplans.inc: the compile-time z-axis FFT plans of the fused z pass.
+"""Generates the compile-time FFT plans of the complex FP32 block-MVP passes.
+
+  zplans.inc  three-line plans of the fused z pass (one warp transforms the
+              three component lines of an (x, y, rhs) task)
+  tplans.inc  single-line plans of the strided x / y passes (one warp per
+              line, eight lines per CTA filled and drained as a tile)
 
 For every 5-smooth line length 2 <= N <= 512 it picks, among the radix
-sequences with the fewest stages (register radices 2..16), the sequence and the
-padded layout that minimise a cost of shared-memory wavefronts plus issued
-instructions of one three-line warp task (forward transform, spectral product,
-inverse transform).
+sequences with the fewest or one more than the fewest stages (register
+radices 2..16), the sequence and the padded layout that minimise a cost of
+shared-memory wavefronts plus issued instructions per line.
 
 Layout: element idx = q * R_last + r of a line lives at q * S + r (S >= R_last),
 so every butterfly of every stage reads its R elements at one base address plus
@@ -14,12 +18,12 @@ Bank model: 32 banks of 4 bytes; 8-byte accesses are served per half-warp and
 a group takes as many wavefronts as the largest number of distinct words in one
 bank (this reproduces the shared-memory wavefront counts ncu reports).
 
-Usage: python gen_zplans.py > zplans.inc
+Usage: python gen_zplans.py [z] [t]   (writes zplans.inc / tplans.inc beside it)
 """
+import os
 import sys
 
 RADICES = (16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2)
-NL = 3          # component lines per warp task
 ESIZE = 8       # complex FP32
 
 
@@ -31,22 +35,26 @@ def smooth(n):
 
 
 def sequences(n):
-    out = []
+    """Radix sequences with the fewest stages and with one more."""
+    out = {}
 
     def rec(rem, cur, depth):
         if rem == 1:
-            out.append(tuple(cur))
+            out.setdefault(len(cur), []).append(tuple(cur))
             return
         if depth == 0:
             return
         for r in RADICES:
             if rem % r == 0:
                 rec(rem // r, cur + [r], depth - 1)
-    for depth in range(1, 10):
+    for depth in range(1, 12):
         rec(n, [], depth)
         if out:
-            return [s for s in out if len(s) == depth]
-    return []
+            break
+    m = min(out)
+    out = {}
+    rec(n, [], m + 1)
+    return out.get(m, []) + out.get(m + 1, [])
 
 
 def wavefronts(addrs):
@@ -71,7 +79,8 @@ def dft_cost(r):
     return a * dft_cost(b) + b * dft_cost(a) + 4 * (a - 1) * (b - 1)
 
 
-def cost(n, rad, S, LW):
+def stage_cost(n, rad, S, LW, NL):
+    """Wavefronts and warp instructions of one transform of NL lines."""
     rl = rad[-1]
 
     def addr(idx):
@@ -79,7 +88,7 @@ def cost(n, rad, S, LW):
     wf = 0
     instr = 0
     Ls = n
-    for s, R in enumerate(rad):
+    for R in rad:
         M = Ls // R
         B = n // R
         T = NL * B
@@ -94,15 +103,32 @@ def cost(n, rad, S, LW):
                 wf += 2 * wavefronts(a)                       # load + store
             instr += 2 * R + dft_cost(R) + (5 * (R - 1) if M > 1 else 0) + 16
         Ls = M
-    wf *= 2                                                       # forward + inverse
-    instr *= 2
-    for j in range(NL):                                           # load, product (2), store
+    return wf, instr
+
+
+def cost_z(n, rad, S, LW):
+    """One three-line task: forward, product, inverse."""
+    rl = rad[-1]
+    wf, instr = stage_cost(n, rad, S, LW, 3)
+    wf, instr = 2 * wf, 2 * instr
+    for j in range(3):                                            # load, product (2), store
         for z0 in range(0, n, 32):
-            wf += 4 * wavefronts([j * LW + addr(z) for z in range(z0, min(n, z0 + 32))])
+            wf += 4 * wavefronts([j * LW + (z // rl) * S + z % rl for z in range(z0, min(n, z0 + 32))])
     return wf + instr / 4.0
 
 
-def choose(n):
+def cost_tile(n, rad, S, LW):
+    """One line of a tile pass: one transform plus its share of the tile fill and drain."""
+    rl = rad[-1]
+    wf, instr = stage_cost(n, rad, S, LW, 1)
+    tw = 0
+    for i0 in range(0, 8 * n, 32):
+        tw += wavefronts([((i0 + l) & 7) * LW + ((((i0 + l) >> 3) // rl) * S + ((i0 + l) >> 3) % rl)
+                          for l in range(min(32, 8 * n - i0))])
+    return wf + instr / 4.0 + 2 * tw / 8.0
+
+
+def choose(n, cost):
     best = None
     for rad in sequences(n):
         rl = rad[-1]
@@ -110,25 +136,35 @@ def choose(n):
             top = (n // rl - 1) * S + rl
             for d in range(16):
                 LW = top + d
-                c = cost(n, rad, S, LW)
-                key = (c, LW, S)
+                key = (cost(n, rad, S, LW), LW, S)
                 if best is None or key < best[0]:
                     best = (key, rad, S, LW)
     return best[1], best[2], best[3]
 
 
-def main():
-    lines = ["// Generated by gen_zplans.py: compile-time z-axis plans of the fused z pass.",
-             "// BDDA_ZPLAN(index, N, S, LW, radices...): element q*R_last + r at q*S + r, lines LW apart."]
+def write(path, macro, what, cost):
+    lines = ["// Generated by gen_zplans.py: compile-time plans of the %s." % what,
+             "// %s(index, N, S, LW, radices...): element q*R_last + r at q*S + r, lines LW apart." % macro]
     idx = 0
     for n in range(2, 513):
         if not smooth(n):
             continue
-        rad, S, LW = choose(n)
-        lines.append("BDDA_ZPLAN(%d, %d, %d, %d, %s)" % (idx, n, S, LW, ", ".join(str(r) for r in rad)))
+        rad, S, LW = choose(n, cost)
+        lines.append("%s(%d, %d, %d, %d, %s)" % (macro, idx, n, S, LW, ", ".join(str(r) for r in rad)))
         idx += 1
-        print(n, rad, S, LW, file=sys.stderr, flush=True)
-    print("\n".join(lines))
+        print(macro, n, rad, S, LW, file=sys.stderr, flush=True)
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def main():
+    here = os.path.dirname(os.path.abspath(__file__))
+    which = sys.argv[1:] or ["z", "t"]
+    if "z" in which:
+        write(os.path.join(here, "zplans.inc"), "BDDA_ZPLAN", "fused z pass (three lines per warp)", cost_z)
+    if "t" in which:
+        write(os.path.join(here, "tplans.inc"), "BDDA_TPLAN", "strided x / y passes (one line per warp)",
+              cost_tile)
 
 
 if __name__ == "__main__":

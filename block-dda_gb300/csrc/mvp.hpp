@@ -105,6 +105,31 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
 
 template <typename T> cudaError_t configure_mvp_kernels();
 
+// Arguments of the strided passes of one complex FP32 block MVP.
+struct TileArgs {
+  const MvpGeom* g;
+  const float2* x;
+  int ldx;
+  float2* y;
+  int ldy;
+  int nfield;
+  const float2* diag;
+  const float2* jpre;
+  float2* t1;
+  float2* t2;
+  const float2* twx;
+  const float2* twy;
+  int grid_y, ntask_y;  // persistent grid and tasks of passes B / D
+  cudaStream_t st;
+  const int* done;
+};
+enum TilePass { kTileA = 0, kTileB, kTileD, kTileE };
+
+// Strided pass `pass` for complex FP32 with the compile-time plan of its axis
+// (tplans.inc: Px for A / E, Py for B / D); false (nothing launched) when the
+// length has none.  *err: launch status.
+bool launch_tile_static(int pass, const TileArgs& a, cudaError_t* err);
+
 // Pass C for complex FP32 with the compile-time z plan of g.Pz (zplans.inc);
 // returns false (nothing launched) when g.Pz has none.  *err: launch status.
 bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2* ghat, cudaStream_t st,
@@ -117,12 +142,16 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
                             const double2* twx, const double2* twy, const double2* twz,
                             double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, cudaStream_t st);
 
-// Radix schedule, shared-memory layout and FP64 twiddles for a 5-smooth
-// 2 <= N <= kMaxLine.  max_radix 8: radices 2, 3, 4, 5, 8 for the single-line
-// tile passes; max_radix 16: composite register radices up to 16 for the
-// three-line z pass.  Fewest stages; the radix order, skew shift and line
-// pitch minimise a shared-memory bank model of the pass (cached per N).
-bool make_axis_plan(int N, AxisPlan* p, int max_radix = 8);
+// Radix schedule and shared-memory layout for a 5-smooth 2 <= N <= kMaxLine.
+// three: the fused z pass (three lines per warp), else the single-line tile
+// passes.  wide = false (complex FP32): the radix sequence of the compile-time
+// plan tables (zplans.inc / tplans.inc); wide = true (16-byte FP64 and
+// double-float): the z table's sequence, and for the tile passes the radices
+// 2, 3, 4, 5, 8 with the fewest stages in the order a shared-memory bank model
+// prefers.  The skew shift and line pitch of both element widths come from the
+// same bank model (cached per plan).
+bool make_axis_plan(int N, AxisPlan* p, bool three, bool wide);
+// FP64 twiddle table exp(-2 pi i t / N), t < N.
 void make_twiddles(int N, std::vector<double2>* out);
 
 }  // namespace bdda

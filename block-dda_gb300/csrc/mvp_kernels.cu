@@ -36,135 +36,13 @@
 #include "fft_core.cuh"
 
 #include "mvp.hpp"
+#include "tile_passes.cuh"
 
 namespace bdda {
 
 namespace {
 
-// ---- cp.async helpers (LDGSTS: global -> shared without registers) --------
-template <int BYTES>
-__device__ __forceinline__ void cp_async(void* smem, const void* gmem, bool valid) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  const int sz = valid ? BYTES : 0;  // src-size 0: nothing read, destination zero-filled
-  if constexpr (BYTES == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(sz) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
 __device__ __forceinline__ bool skip(const int* done) { return done && *(volatile const int*)done; }
-
-// ---------------------------------------------------------------- pass A
-// One CTA per listed (y, z-tile): warp w owns z = z0 + w; loops over fields.
-template <typename T>
-__global__ void __launch_bounds__(kTileThreads)
-k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, const int* __restrict__ occ,
-         const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, AxisPlan px,
-         const typename cplx<T>::type* __restrict__ twx, typename cplx<T>::type* __restrict__ t1, const int* done) {
-  using C = typename cplx<T>::type;
-  if (skip(done)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int Px = px.N;
-  const int lw = plan_lw<C>(px), sh = plan_sk<C>(px);
-  C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
-  int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
-  const int tile = tiles[blockIdx.x];
-  const int y = tile / nzt, z0 = (tile - y * nzt) * kTZ;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
-    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
-    socc[idx] = z < nz ? occ[((size_t)xi * ny + y) * nz + z] : -1;
-  }
-  __syncthreads();
-  const size_t rowstride = (size_t)ny * nz;  // T1 stride between x rows
-  int l = 0, c = 0;
-  for (int f = 0; f < nfield; ++f) {
-    C* line = lines + ((f & 1) * kTZ + warp) * lw;
-    const C* xc = x + (size_t)l * ldx + c;
-    for (int xi = lane; xi < nx; xi += 32) {
-      const int m = socc[xi * kTZ + warp];
-      line[skw(xi, sh)] = m >= 0 ? xc[3 * (size_t)m] : czero<C>();
-    }
-    __syncwarp();
-    warp_fft<false>(line, twx, px, lane, 32, nx);
-    __syncthreads();
-    C* out = t1 + (size_t)f * Px * rowstride + (size_t)y * nz + z0;
-    const C* lb = lines + (f & 1) * kTZ * lw;
-    for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
-      const int w = idx & 7, q = idx >> 3;
-      if (z0 + w < nz) out[(size_t)q * rowstride + w] = lb[w * lw + skw(q, sh)];
-    }
-    if (++c == 3) { c = 0; ++l; }
-  }
-}
-
-// ---------------------------------------------------------------- pass B / D
-// Persistent CTAs over tasks (field, x, z-tile); lines along y.
-// B: T1[f][q][y<ny][z] -> T2[f][q][Py][z]   (rows of empty tiles zero-filled)
-// D: T2[f][q][Py][z]   -> T1[f][q][y<ny][z] (rows of listed tiles only)
-template <typename T, bool INV>
-__global__ void __launch_bounds__(kTileThreads)
-k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type* __restrict__ dst,
-         const unsigned char* __restrict__ tmask, int ny, int nz, int nzt, int ntask, AxisPlan py,
-         const typename cplx<T>::type* __restrict__ twy, const int* done) {
-  using C = typename cplx<T>::type;
-  if (skip(done)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int Py = py.N;
-  const int lw = plan_lw<C>(py), sh = plan_sk<C>(py);
-  C* lines = reinterpret_cast<C*>(smem_raw);  // [2][kTZ][lw]
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nin = INV ? Py : ny;    // rows read
-  const int nout = INV ? ny : Py;   // rows written
-  const size_t in_rows = (size_t)nin, out_rows = (size_t)nout;
-
-  auto issue = [&](int task, int buf) {
-    const int zt = task % nzt;
-    const int r = task / nzt;  // f * Px + q
-    const int z0 = zt * kTZ;
-    const C* base = src + (size_t)r * in_rows * nz + z0;
-    C* lb = lines + buf * kTZ * lw;
-    for (int idx = tid; idx < nin * kTZ; idx += kTileThreads) {
-      const int w = idx & 7, yy = idx >> 3;
-      bool valid = z0 + w < nz;
-      if (!INV) valid = valid && tmask[yy * nzt + zt];
-      const C* g = valid ? base + (size_t)yy * nz + w : src;
-      cp_async<sizeof(C)>(lb + w * lw + skw(yy, sh), g, valid);
-    }
-    cp_commit();
-  };
-
-  int task = blockIdx.x;
-  if (task < ntask) issue(task, 0);
-  for (int it = 0; task < ntask; ++it, task += gridDim.x) {
-    const int buf = it & 1;
-    const int next = task + gridDim.x;
-    if (next < ntask) {
-      issue(next, buf ^ 1);
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
-    }
-    __syncthreads();
-    C* line = lines + (buf * kTZ + warp) * lw;
-    warp_fft<INV>(line, twy, py, lane, 32, INV ? Py : ny);
-    __syncthreads();
-    const int zt = task % nzt;
-    const int r = task / nzt;
-    const int z0 = zt * kTZ;
-    C* ob = dst + (size_t)r * out_rows * nz + z0;
-    const C* lb = lines + buf * kTZ * lw;
-    for (int idx = tid; idx < nout * kTZ; idx += kTileThreads) {
-      const int w = idx & 7, yy = idx >> 3;
-      if (z0 + w >= nz) continue;
-      if (INV && !tmask[yy * nzt + zt]) continue;
-      ob[(size_t)yy * nz + w] = lb[w * lw + skw(yy, sh)];
-    }
-    __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
-  }
-}
 
 // ---------------------------------------------------------------- pass C
 // One warp per task (x = q, y = qy, rhs l): the three component lines along z.
@@ -215,71 +93,6 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz,
   }
 }
 
-// ---------------------------------------------------------------- pass E
-// One CTA per listed (y, z-tile); loops over fields with the next field's
-// tile prefetched by cp.async; scatters the occupied sites.
-template <typename T>
-__global__ void __launch_bounds__(kTileThreads)
-k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, const int* __restrict__ occ,
-         const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, AxisPlan px,
-         const typename cplx<T>::type* __restrict__ twx, const typename cplx<T>::type* __restrict__ x, int ldx,
-         const typename cplx<T>::type* __restrict__ diag, const typename cplx<T>::type* __restrict__ jpre,
-         typename cplx<T>::type* __restrict__ y, int ldy, const int* done) {
-  using C = typename cplx<T>::type;
-  if (skip(done)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int Px = px.N;
-  const int lw = plan_lw<C>(px), sh = plan_sk<C>(px);
-  C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
-  int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
-  const int tile = tiles[blockIdx.x];
-  const int yy = tile / nzt, z0 = (tile - yy * nzt) * kTZ;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const size_t rowstride = (size_t)ny * nz;
-  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
-    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
-    socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
-  }
-  auto issue = [&](int f, int buf) {
-    const C* base = t1 + (size_t)f * Px * rowstride + (size_t)yy * nz + z0;
-    C* lb = lines + buf * kTZ * lw;
-    for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
-      const int w = idx & 7, q = idx >> 3;
-      const bool valid = z0 + w < nz;
-      cp_async<sizeof(C)>(lb + w * lw + skw(q, sh), valid ? base + (size_t)q * rowstride + w : t1, valid);
-    }
-    cp_commit();
-  };
-  issue(0, 0);
-  int l = 0, c = 0;
-  for (int f = 0; f < nfield; ++f) {
-    const int buf = f & 1;
-    if (f + 1 < nfield) {
-      issue(f + 1, buf ^ 1);
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
-    }
-    __syncthreads();
-    C* line = lines + (buf * kTZ + warp) * lw;
-    warp_fft<true>(line, twx, px, lane);
-    for (int xi = lane; xi < nx; xi += 32) {
-      const int m = socc[xi * kTZ + warp];
-      if (m < 0) continue;
-      const size_t r = 3 * (size_t)m + c;
-      C v = line[skw(xi, sh)];
-      if (diag != nullptr) v = cadd(v, cmul(diag[r], x[(size_t)l * ldx + r]));
-      if (jpre != nullptr) v = cmul(v, jpre[r]);
-      y[(size_t)l * ldy + r] = v;
-    }
-    __syncthreads();  // buffer 'buf' is the cp.async target of field f + 2
-    if (++c == 3) { c = 0; ++l; }
-  }
-}
-
-template <typename T> int smem_tile(int lw, int nx) {
-  return 2 * kTZ * lw * (int)sizeof(typename cplx<T>::type) + nx * kTZ * 4;
-}
 template <typename T> int smem_z(int lw) { return kZWarps * 3 * lw * (int)sizeof(typename cplx<T>::type); }
 
 int num_sms() {
@@ -307,16 +120,36 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   if (g.ntiles == 0) return cudaSuccess;  // no dipoles
   const int ntask_y = nfield * g.Px * g.nzt;
   const int grid_y = std::min(ntask_y, num_sms() * 8);
+  const tile::RtLine<C> lx{g.px}, ly{g.py};
+  // Strided pass `pass` with the compile-time plan of its axis (complex FP32);
+  // false when it was not launched that way.
+  cudaError_t serr = cudaSuccess;
+  auto static_tile = [&](int pass) -> bool {
+    if constexpr (std::is_same<T, float>::value) {
+      const TileArgs a{&g, x, ldx, y, ldy, nfield, diag, jpre, t1, t2, p.twx, p.twy, grid_y, ntask_y, st, done};
+      cudaError_t e = cudaSuccess;
+      const bool ok = launch_tile_static(pass, a, &e);
+      if (ok && e != cudaSuccess) serr = e;
+      return ok;
+    } else {
+      (void)pass;
+      return false;
+    }
+  };
   // A
   if (timer) timer->begin(kPassA + pbase, st);
-  k_pass_a<T><<<g.ntiles, kTileThreads, smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(x, ldx, nfield, g.occ, g.tiles, g.nx, g.ny,
-                                                                       g.nz, g.nzt, g.px, p.twx, t1, done);
+  if (!static_tile(kTileA))
+    tile::k_pass_a<T><<<g.ntiles, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
+        x, ldx, nfield, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, lx, p.twx, t1, done);
   if (timer) timer->end(kPassA + pbase, st);
+  if (serr != cudaSuccess) return serr;
   // B
   if (timer) timer->begin(kPassB + pbase, st);
-  k_pass_y<T, false><<<grid_y, kTileThreads, smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(t1, t2, g.tmask, g.ny, g.nz, g.nzt,
-                                                                         ntask_y, g.py, p.twy, done);
+  if (!static_tile(kTileB))
+    tile::k_pass_y<T, false><<<grid_y, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
+        t1, t2, g.tmask, g.ny, g.nz, g.nzt, ntask_y, ly, p.twy, done);
   if (timer) timer->end(kPassB + pbase, st);
+  if (serr != cudaSuccess) return serr;
   // C
   {
     const long long ntask = (long long)g.Px * g.Py * L;
@@ -335,28 +168,34 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   }
   // D
   if (timer) timer->begin(kPassD + pbase, st);
-  k_pass_y<T, true><<<grid_y, kTileThreads, smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(t2, t1, g.tmask, g.ny, g.nz, g.nzt,
-                                                                        ntask_y, g.py, p.twy, done);
+  if (!static_tile(kTileD))
+    tile::k_pass_y<T, true><<<grid_y, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
+        t2, t1, g.tmask, g.ny, g.nz, g.nzt, ntask_y, ly, p.twy, done);
   if (timer) timer->end(kPassD + pbase, st);
+  if (serr != cudaSuccess) return serr;
   // E
   if (timer) timer->begin(kPassE + pbase, st);
-  k_pass_e<T><<<g.ntiles, kTileThreads, smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(t1, nfield, g.occ, g.tiles, g.nx, g.ny, g.nz,
-                                                                       g.nzt, g.px, p.twx, x, ldx, diag, jpre, y, ldy,
-                                                                       done);
+  if (!static_tile(kTileE))
+    tile::k_pass_e<T><<<g.ntiles, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
+        t1, nfield, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, done);
   if (timer) timer->end(kPassE + pbase, st);
+  if (serr != cudaSuccess) return serr;
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t configure_mvp_kernels() {
-  const int tile = smem_tile<T>(kMaxLineWords, kMaxLine / 2);
+  using C = typename cplx<T>::type;
+  using Rt = tile::RtLine<C>;
+  const int ts = tile::smem_tile<T>(kMaxLineWords, kMaxLine / 2);
   const int zs = smem_z<T>(kMaxLineWords);
+  const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_pass_a<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_pass_e<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_pass_y<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_pass_y<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile)) != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_pass_c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, zs);
+  if ((e = cudaFuncSetAttribute(tile::k_pass_a<T, Rt>, attr, ts)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(tile::k_pass_e<T, Rt>, attr, ts)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(tile::k_pass_y<T, false, Rt>, attr, ts)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(tile::k_pass_y<T, true, Rt>, attr, ts)) != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_pass_c<T>, attr, zs);
 }
 
 template cudaError_t launch_block_mvp<float>(const MvpGeom&, const MvpPrec<float>&, const float2*, int, float2*, int, int,

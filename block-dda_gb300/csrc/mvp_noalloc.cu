@@ -76,7 +76,7 @@ int mvp_noalloc(Op* op, const void* x, int ldx, void* y, int ldy, int L, const v
     set_error("bad L or leading dimension");
     return BDDA_ERR_INVALID;
   }
-  const MvpGeom g = op->geom(o);
+  const MvpGeom g = op->geom<T>(o);
   const size_t b1 = align256(mvp_t1_elems(g, L) * sizeof(C));
   const size_t b2 = align256(mvp_t2_elems(g, L) * sizeof(C));
   if (b1 + b2 > kNoAllocScratchBytes) {

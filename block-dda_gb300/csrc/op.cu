@@ -147,7 +147,7 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
     set_error("bad L or leading dimension");
     return BDDA_ERR_INVALID;
   }
-  MvpGeom g = op->geom(o);
+  MvpGeom g = op->geom<T>(o);
   const bool grow = op->t1[pi].bytes < mvp_t1_elems(g, L) * sizeof(C) || op->t2[pi].bytes < mvp_t2_elems(g, L) * sizeof(C);
   if (grow && st != op->stream) BDDA_TRY_CUDA(order_after(op->stream, st));  // old buffers may be in use on st
   BDDA_CUDA(op->t1[pi].ensure(mvp_t1_elems(g, L) * sizeof(C), op->stream));
@@ -197,8 +197,9 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
   for (int i = 0; i < 3; ++i) {
     op->n[i] = n[i];
     op->P[i] = smooth235(2 * n[i]);
-    // z lines (the fused pass, three lines per warp) take composite register radices
-    if (!make_axis_plan(op->P[i], &op->plan[i], i == 2 ? 16 : 8)) {
+    // z lines: the fused pass (three lines per warp); x / y: the tile passes
+    if (!make_axis_plan(op->P[i], &op->plan[0][i], i == 2, false) ||
+        !make_axis_plan(op->P[i], &op->plan[1][i], i == 2, true)) {
       set_error("no FFT plan for the padded grid");
       return BDDA_ERR_INVALID;
     }
@@ -240,10 +241,19 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
   if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure(6 * ng * sizeof(double2), op->stream));
   if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure(6 * ng * sizeof(float2), op->stream));
   if (prec & BDDA_PREC_DF64) BDDA_CUDA(op->ghatdf.ensure(6 * ng * sizeof(dfc), op->stream));
-  MvpGeom g = op->geom(op->dip);
-  BDDA_CUDA(build_green_hat(g, lf, k_re, k_im, op->tw64[0].as<double2>(), op->tw64[1].as<double2>(),
-                            op->tw64[2].as<double2>(), work.as<double2>(), op->ghat64.as<double2>(),
-                            op->ghat32.as<float2>(), op->ghatdf.as<dfc>(), op->stream));
+  // one spectrum per distinct digit order (radix sequences) of the plan sets
+  bool same = true;
+  for (int i = 0; i < 3; ++i) {
+    const AxisPlan &a = op->plan[0][i], &b = op->plan[1][i];
+    same = same && a.nst == b.nst && std::equal(a.radix, a.radix + a.nst, b.radix);
+  }
+  const double2 *tx = op->tw64[0].as<double2>(), *ty = op->tw64[1].as<double2>(), *tz = op->tw64[2].as<double2>();
+  BDDA_CUDA(build_green_hat(op->geom(op->dip, 1), lf, k_re, k_im, tx, ty, tz, work.as<double2>(),
+                            op->ghat64.as<double2>(), same ? op->ghat32.as<float2>() : nullptr,
+                            op->ghatdf.as<dfc>(), op->stream));
+  if (!same && op->ghat32.p)
+    BDDA_CUDA(build_green_hat(op->geom(op->dip, 0), lf, k_re, k_im, tx, ty, tz, work.as<double2>(), nullptr,
+                              op->ghat32.as<float2>(), nullptr, op->stream));
   BDDA_CUDA(wait_stream(op->stream));
   *out = op.release();
   return BDDA_OK;

@@ -64,7 +64,10 @@ struct Op {
   int f = 3;
   double lf = 0, kr = 0, ki = 0;
   int prec = 0;  // bit mask BDDA_PREC_FP64 | BDDA_PREC_FP32
-  AxisPlan plan[3];
+  // Axis plans per element width: [0] complex FP32 (the compile-time plan
+  // tables' radix sequences), [1] 16-byte FP64 / double-float (radices <= 8 on
+  // the single-line x / y axes).  Each set has its own Green spectrum order.
+  AxisPlan plan[2][3];
   DevBuf tw64[3], tw32[3], twdf[3];
   DevBuf ghat64, ghat32, ghatdf;
   Occupancy dip;    // dipole occupancy (set_dipoles)
@@ -75,11 +78,11 @@ struct Op {
   std::mutex mu;
   std::shared_ptr<SolverWork> solver;   // cached Krylov workspace (solver.cu)
 
-  MvpGeom geom(const Occupancy& o) const {
+  MvpGeom geom(const Occupancy& o, int set) const {
     MvpGeom g;
     g.nx = n[0]; g.ny = n[1]; g.nz = n[2];
     g.Px = P[0]; g.Py = P[1]; g.Pz = P[2];
-    g.px = plan[0]; g.py = plan[1]; g.pz = plan[2];
+    g.px = plan[set][0]; g.py = plan[set][1]; g.pz = plan[set][2];
     g.nzt = (n[2] + kTZ - 1) / kTZ;
     g.ntiles = o.ntiles;
     g.tile_rows = o.tile_rows;
@@ -88,6 +91,7 @@ struct Op {
     g.tmask = o.tmask.as<unsigned char>();
     return g;
   }
+  template <typename T> MvpGeom geom(const Occupancy& o) const { return geom(o, sizeof(T) == sizeof(float) ? 0 : 1); }
   template <typename T> MvpPrec<T> tables() const;
   ~Op();
 };

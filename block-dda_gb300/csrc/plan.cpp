@@ -4,6 +4,7 @@
 #include <cmath>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -144,18 +145,26 @@ Layout best_layout(int N, const std::vector<int>& rad, bool three, int esize) {
 
 struct PlanChoice { std::vector<int> rad; Layout l8, l16; };
 
-// Radix sequences of the compile-time z plans (the fused z pass for complex
-// FP32 runs them; the z axis of every operator uses the same sequence so that
-// all transforms share the Green spectrum's digit order).
-struct ZPlanRow { int N, S, LW; int rad[kMaxStages]; };
-constexpr ZPlanRow kZPlans[] = {
+// Radix sequences of the compile-time plans of complex FP32: the fused z pass
+// (three-line plans) ...  Every operator's axes use the same sequences, so
+// the runtime-plan kernels of the other precisions and the Green spectrum
+// share the digit order of the compile-time ones.
+struct PlanRow { int N, S, LW; int rad[kMaxStages]; };
+constexpr PlanRow kZPlans[] = {
 #define BDDA_ZPLAN(I, N, S, LW, ...) {N, S, LW, {__VA_ARGS__}},
 #include "zplans.inc"
 #undef BDDA_ZPLAN
 };
+// ... and of the strided x / y passes (single-line plans).
+constexpr PlanRow kTPlans[] = {
+#define BDDA_TPLAN(I, N, S, LW, ...) {N, S, LW, {__VA_ARGS__}},
+#include "tplans.inc"
+#undef BDDA_TPLAN
+};
 
-bool zplan_radices(int N, std::vector<int>* rad) {
-  for (const ZPlanRow& z : kZPlans)
+template <size_t K>
+bool table_radices(const PlanRow (&tab)[K], int N, std::vector<int>* rad) {
+  for (const PlanRow& z : tab)
     if (z.N == N) {
       rad->clear();
       for (int s = 0; s < kMaxStages && z.rad[s] > 0; ++s) rad->push_back(z.rad[s]);
@@ -167,58 +176,62 @@ bool zplan_radices(int N, std::vector<int>* rad) {
 // Radix order, skew and pitch by the bank model: among the fewest-stage radix
 // sequences, the one whose best 8-byte layout takes the fewest wavefronts
 // (complex FP32 is the hot precision); the 16-byte layout is then fitted to it.
-PlanChoice choose_plan(int N, bool three) {
+// Radix sequence: the compile-time tables' for complex FP32 and for every
+// z axis; otherwise (16-byte tile passes) the fewest-stage sequence of radices
+// <= 8 whose best 16-byte layout takes the fewest wavefronts.  Then the best
+// layout of each element width for that sequence.
+PlanChoice choose_plan(int N, bool three, bool wide) {
   PlanChoice best;
-  if (three && zplan_radices(N, &best.rad)) {
-    best.l8 = best_layout(N, best.rad, true, 8);
-    best.l16 = best_layout(N, best.rad, true, 16);
-    return best;
-  }
-  const std::vector<int> allowed = three ? std::vector<int>{16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2}
-                                         : std::vector<int>{8, 5, 4, 3, 2};
-  const int len = min_stages(N, allowed, 0, 64);
-  std::vector<std::vector<int>> seqs;
-  std::vector<int> cur;
-  sequences(N, allowed, len, cur, seqs);
-  // coarse pass: every sequence and shift at the minimal pitch; the best few then get every pitch
-  struct Cand { long cost; size_t s; };
-  std::vector<Cand> cand;
-  for (size_t i = 0; i < seqs.size(); ++i) {
-    long c = -1;
-    for (int sh : kShifts) {
-      const long v = plan_cost(N, seqs[i], three, skew(N - 1, sh) + 1, sh, 8);
-      if (c < 0 || v < c) c = v;
+  const bool tabled = three ? table_radices(kZPlans, N, &best.rad) : (!wide && table_radices(kTPlans, N, &best.rad));
+  if (!tabled) {
+    const std::vector<int> allowed = three ? std::vector<int>{16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2}
+                                           : std::vector<int>{8, 5, 4, 3, 2};
+    const int es = wide ? 16 : 8;
+    const int len = min_stages(N, allowed, 0, 64);
+    std::vector<std::vector<int>> seqs;
+    std::vector<int> cur;
+    sequences(N, allowed, len, cur, seqs);
+    // coarse pass: every sequence and shift at the minimal pitch; the best few then get every pitch
+    struct Cand { long cost; size_t s; };
+    std::vector<Cand> cand;
+    for (size_t i = 0; i < seqs.size(); ++i) {
+      long c = -1;
+      for (int sh : kShifts) {
+        const long v = plan_cost(N, seqs[i], three, skew(N - 1, sh) + 1, sh, es);
+        if (c < 0 || v < c) c = v;
+      }
+      cand.push_back({c, i});
     }
-    cand.push_back({c, i});
-  }
-  std::stable_sort(cand.begin(), cand.end(), [](const Cand& a, const Cand& b) { return a.cost < b.cost; });
-  best.l8.cost = -1;
-  for (size_t k = 0; k < cand.size() && k < 4; ++k) {
-    const Layout l = best_layout(N, seqs[cand[k].s], three, 8);
-    if (best.l8.cost < 0 || l.cost < best.l8.cost) {
-      best.rad = seqs[cand[k].s];
-      best.l8 = l;
+    std::stable_sort(cand.begin(), cand.end(), [](const Cand& a, const Cand& b) { return a.cost < b.cost; });
+    long bc = -1;
+    for (size_t k = 0; k < cand.size() && k < 4; ++k) {
+      const Layout l = best_layout(N, seqs[cand[k].s], three, es);
+      if (bc < 0 || l.cost < bc) {
+        best.rad = seqs[cand[k].s];
+        bc = l.cost;
+      }
     }
   }
+  best.l8 = best_layout(N, best.rad, three, 8);
   best.l16 = best_layout(N, best.rad, three, 16);
   return best;
 }
 }  // namespace
 
-bool make_axis_plan(int N, AxisPlan* p, int max_radix) {
+bool make_axis_plan(int N, AxisPlan* p, bool three, bool wide) {
   if (N < 2 || N > kMaxLine) return false;
   int t = N;
   for (int q : {2, 3, 5})
     while (t % q == 0) t /= q;
   if (t != 1) return false;
-  const bool three = max_radix > 8;
   static std::mutex mu;
-  static std::map<std::pair<int, bool>, PlanChoice> cache;
+  static std::map<std::tuple<int, bool, bool>, PlanChoice> cache;
   PlanChoice ch;
   {
     std::lock_guard<std::mutex> lk(mu);
-    auto it = cache.find({N, three});
-    if (it == cache.end()) it = cache.emplace(std::make_pair(N, three), choose_plan(N, three)).first;
+    const auto key = std::make_tuple(N, three, wide);
+    auto it = cache.find(key);
+    if (it == cache.end()) it = cache.emplace(key, choose_plan(N, three, wide)).first;
     ch = it->second;
   }
   if ((int)ch.rad.size() > kMaxStages) return false;
@@ -268,12 +281,14 @@ extern "C" {
 // data: N interleaved complex values; prec 1 = FP64, 2 = FP32, 3 = double-float arithmetic
 // (values are rounded to float and back).  nvalid in (0, N): the forward
 // transform reads only the first nvalid inputs and takes the rest as zero
-// (the pad slots hold poison values to prove it).  Returns the number of stages, or
-// a negative value for an unsupported N.  Radices are written to radix (<= 16).
+// (the pad slots hold poison values to prove it).  radix[0] > 8 on input: the
+// z-axis schedule, else the x / y one, each for the element width of prec.
+// Returns the number of stages, or a negative value for an unsupported N.
+// Radices are written to radix (<= 16).
 int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, int* radix) {
   bdda::AxisPlan p;
-  const int max_radix = (radix && radix[0] > 8) ? radix[0] : 8;
-  if (!bdda::make_axis_plan(N, &p, max_radix)) return -1;
+  const bool three = radix && radix[0] > 8;
+  if (!bdda::make_axis_plan(N, &p, three, prec != 2)) return -1;
   std::vector<double2> tw;
   bdda::make_twiddles(N, &tw);
   // nvalid: forward transforms read only the first nvalid inputs (zero padding)

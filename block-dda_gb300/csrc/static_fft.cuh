@@ -1,0 +1,111 @@
+// Warp FFT with a compile-time plan (complex FP32 block-MVP passes).
+//
+// The same in-place DIF forward / DIT inverse transform pair as the runtime
+// core (fft_core.cuh: same butterflies, twiddles and digit order for the same
+// radix sequence), with the plan as a type: the radix sequence, the padded
+// shared-memory layout and the line pitch are template constants, so each
+// butterfly element is a per-butterfly base address plus an immediate offset
+// and the index arithmetic divides by constants.
+//
+// Layout: element idx = q * R_last + r of a line lives at q * S + r.  Every
+// stage s before the last steps through its butterfly in multiples of R_last
+// (M_s is a multiple of it), so its elements are (M_s / R_last) * S apart; the
+// last stage's are adjacent.  Lines are LW elements apart.  The plans come
+// from zplans.inc / tplans.inc (gen_zplans.py).
+#pragma once
+
+#include "fft_core.cuh"
+
+namespace bdda {
+namespace sfft {
+
+template <int N_, int S_, int LW_, int... R>
+struct Plan {
+  static constexpr int N = N_, S = S_, LW = LW_, nst = sizeof...(R);
+  static constexpr int rad[nst] = {R...};
+  static constexpr int Rl = rad[nst - 1];
+  // product of the radices after stage s (the butterfly span M_s)
+  static constexpr int M(int s) {
+    int m = 1;
+    for (int t = s + 1; t < nst; ++t) m *= rad[t];
+    return m;
+  }
+  __device__ static __forceinline__ int addr(int idx) { return (idx / Rl) * S + idx % Rl; }
+};
+
+// One stage over NL lines of a warp.  Forward (DIF): DFT then twiddle;
+// inverse (DIT, the adjoint): conjugate twiddle then inverse DFT.  The forward
+// first stage reads only inputs idx < nv (the rest are zero padding); the
+// inverse last stage writes only outputs idx < nv (the rest are discarded).
+template <class P, int s, bool INV, int NL>
+__device__ __forceinline__ void stage(float2* __restrict__ sm, const float2* __restrict__ tw, int lane, int nv) {
+  constexpr int R = P::rad[s];
+  constexpr int M = P::M(s);
+  constexpr int Ls = M * R;
+  constexpr int B = P::N / R;    // butterflies per line
+  constexpr int T = NL * B;      // butterflies of the warp
+  constexpr int ts = P::N / Ls;  // twiddle table stride
+  constexpr int off = (s == P::nst - 1) ? 1 : (M / P::Rl) * P::S;
+  constexpr bool prune_in = !INV && s == 0;
+  constexpr bool prune_out = INV && s == 0;
+  for (int t = lane; t < T; t += 32) {
+    const int j = NL == 1 ? 0 : t / B;
+    const int u = t - j * B;
+    const int b = u / M, n1 = u - b * M;
+    const int idx0 = b * Ls + n1;
+    float2* p = sm + j * P::LW + P::addr(idx0);
+    float2 v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      if (prune_in) v[i] = (idx0 + i * M < nv) ? p[i * off] : make_float2(0.f, 0.f);
+      else v[i] = p[i * off];
+    }
+    if (!INV) {
+      dft<R, false>(v);
+      if (M > 1 && n1 != 0) {
+        const int step = n1 * ts;
+#pragma unroll
+        for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tw + k * step));
+      }
+    } else {
+      if (M > 1 && n1 != 0) {
+        const int step = n1 * ts;
+#pragma unroll
+        for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tw + k * step));
+      }
+      dft<R, true>(v);
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      if (prune_out) {
+        if (idx0 + i * M < nv) p[i * off] = v[i];
+      } else {
+        p[i * off] = v[i];
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// Forward transform of NL lines: natural order in, digit-reversed out, only
+// the first nv inputs read.
+template <class P, int NL, int s = 0>
+__device__ __forceinline__ void forward(float2* sm, const float2* tw, int lane, int nv) {
+  if constexpr (s < P::nst) {
+    stage<P, s, false, NL>(sm, tw, lane, nv);
+    forward<P, NL, s + 1>(sm, tw, lane, nv);
+  }
+}
+
+// Inverse transform (unnormalised): digit-reversed in, natural order out,
+// only the first nv outputs written.
+template <class P, int NL, int s = P::nst - 1>
+__device__ __forceinline__ void inverse(float2* sm, const float2* tw, int lane, int nv) {
+  if constexpr (s >= 0) {
+    stage<P, s, true, NL>(sm, tw, lane, nv);
+    inverse<P, NL, s - 1>(sm, tw, lane, nv);
+  }
+}
+
+}  // namespace sfft
+}  // namespace bdda

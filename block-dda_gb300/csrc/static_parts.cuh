@@ -1,0 +1,53 @@
+// Dispatch of the compile-time-plan kernels of complex FP32 by line length.
+// The plans are spread over kParts translation units (by their position in
+// the plan tables) so that the build compiles them in parallel.
+#pragma once
+
+#include "tile_static.cuh"
+#include "zpass_static.cuh"
+
+namespace bdda {
+namespace sparts {
+
+constexpr int kParts = 4;
+
+template <int PART>
+bool dispatch_z(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2* ghat, cudaStream_t st,
+                const int* done, cudaError_t* err) {
+  switch (g.Pz) {
+#define BDDA_ZPLAN(I, N, S, LW, ...)                                                     \
+  case N:                                                                                \
+    if constexpr ((I) % kParts == PART) {                                                \
+      *err = zstatic::launch<sfft::Plan<N, S, LW, __VA_ARGS__>>(g, t2, L, twz, ghat, st, done); \
+      return true;                                                                       \
+    }                                                                                    \
+    return false;
+#include "zplans.inc"
+#undef BDDA_ZPLAN
+    default:
+      break;
+  }
+  return false;
+}
+
+template <int PART>
+bool dispatch_tile(int pass, const TileArgs& a, cudaError_t* err) {
+  const int n = (pass == kTileA || pass == kTileE) ? a.g->Px : a.g->Py;
+  switch (n) {
+#define BDDA_TPLAN(I, N, S, LW, ...)                                                     \
+  case N:                                                                                \
+    if constexpr ((I) % kParts == PART) {                                                \
+      *err = tstatic::launch<sfft::Plan<N, S, LW, __VA_ARGS__>>(pass, a);                \
+      return true;                                                                       \
+    }                                                                                    \
+    return false;
+#include "tplans.inc"
+#undef BDDA_TPLAN
+    default:
+      break;
+  }
+  return false;
+}
+
+}  // namespace sparts
+}  // namespace bdda

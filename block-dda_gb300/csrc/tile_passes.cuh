@@ -1,0 +1,240 @@
+// Strided passes of the block MVP (A: x-forward gather, B: y-forward,
+// D: y-inverse, E: x-inverse scatter), shared by the runtime-plan kernels of
+// every precision and the compile-time-plan kernels of complex FP32.
+//
+// A CTA stages 8 z-columns (one line per warp) of one (field, x) or
+// (y, field) tile in shared memory; the line layout and the warp transform
+// come from a layout policy:
+//   RtLine<C>  runtime axis plan (fft_core.cuh; skewed layout of the plan)
+//   StLine<P>  compile-time plan P (static_fft.cuh; padded layout of P)
+// Forward transforms read only the first nv inputs; inverse transforms need
+// only the first nv outputs (StLine writes only those).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fft_core.cuh"
+#include "mvp.hpp"
+#include "static_fft.cuh"
+
+namespace bdda {
+namespace tile {
+
+template <typename C>
+struct RtLine {
+  AxisPlan p;
+  __device__ __forceinline__ int n() const { return p.N; }
+  __device__ __forceinline__ int lw() const { return plan_lw<C>(p); }
+  __device__ __forceinline__ int addr(int i) const { return skw(i, plan_sk<C>(p)); }
+  template <bool INV>
+  __device__ __forceinline__ void fft(C* line, const C* tw, int lane, int nv) const {
+    if (!INV) warp_fft_lines<false, 1>(line, 0, tw, p, lane, 32, nv);
+    else warp_fft_lines<true, 1>(line, 0, tw, p, lane);
+  }
+};
+
+template <class P>
+struct StLine {
+  __device__ __forceinline__ static constexpr int n() { return P::N; }
+  __device__ __forceinline__ static constexpr int lw() { return P::LW; }
+  __device__ __forceinline__ static int addr(int i) { return P::addr(i); }
+  template <bool INV>
+  __device__ __forceinline__ static void fft(float2* line, const float2* tw, int lane, int nv) {
+    if (!INV) sfft::forward<P, 1>(line, tw, lane, nv);
+    else sfft::inverse<P, 1>(line, tw, lane, nv);
+  }
+};
+
+// ---- cp.async helpers (LDGSTS: global -> shared without registers) --------
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  const int sz = valid ? BYTES : 0;  // src-size 0: nothing read, destination zero-filled
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ bool skip(const int* done) { return done && *(volatile const int*)done; }
+
+// ---------------------------------------------------------------- pass A
+// One CTA per listed (y, z-tile): warp w owns z = z0 + w; loops over fields.
+template <typename T, class Line>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, const int* __restrict__ occ,
+         const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, Line lay,
+         const typename cplx<T>::type* __restrict__ twx, typename cplx<T>::type* __restrict__ t1, const int* done) {
+  using C = typename cplx<T>::type;
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Px = lay.n();
+  const int lw = lay.lw();
+  C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
+  int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
+  const int tile = tiles[blockIdx.x];
+  const int y = tile / nzt, z0 = (tile - y * nzt) * kTZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
+    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
+    socc[idx] = z < nz ? occ[((size_t)xi * ny + y) * nz + z] : -1;
+  }
+  __syncthreads();
+  const size_t rowstride = (size_t)ny * nz;  // T1 stride between x rows
+  int l = 0, c = 0;
+  for (int f = 0; f < nfield; ++f) {
+    C* line = lines + ((f & 1) * kTZ + warp) * lw;
+    const C* xc = x + (size_t)l * ldx + c;
+    for (int xi = lane; xi < nx; xi += 32) {
+      const int m = socc[xi * kTZ + warp];
+      line[lay.addr(xi)] = m >= 0 ? xc[3 * (size_t)m] : czero<C>();
+    }
+    __syncwarp();
+    lay.template fft<false>(line, twx, lane, nx);
+    __syncthreads();
+    C* out = t1 + (size_t)f * Px * rowstride + (size_t)y * nz + z0;
+    const C* lb = lines + (f & 1) * kTZ * lw;
+    for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
+      const int w = idx & 7, q = idx >> 3;
+      if (z0 + w < nz) out[(size_t)q * rowstride + w] = lb[w * lw + lay.addr(q)];
+    }
+    if (++c == 3) { c = 0; ++l; }
+  }
+}
+
+// ---------------------------------------------------------------- pass B / D
+// Persistent CTAs over tasks (field, x, z-tile); lines along y.
+// B: T1[f][q][y<ny][z] -> T2[f][q][Py][z]   (rows of empty tiles zero-filled)
+// D: T2[f][q][Py][z]   -> T1[f][q][y<ny][z] (rows of listed tiles only)
+template <typename T, bool INV, class Line>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type* __restrict__ dst,
+         const unsigned char* __restrict__ tmask, int ny, int nz, int nzt, int ntask, Line lay,
+         const typename cplx<T>::type* __restrict__ twy, const int* done) {
+  using C = typename cplx<T>::type;
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Py = lay.n();
+  const int lw = lay.lw();
+  C* lines = reinterpret_cast<C*>(smem_raw);  // [2][kTZ][lw]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nin = INV ? Py : ny;    // rows read
+  const int nout = INV ? ny : Py;   // rows written
+  const size_t in_rows = (size_t)nin, out_rows = (size_t)nout;
+
+  auto issue = [&](int task, int buf) {
+    const int zt = task % nzt;
+    const int r = task / nzt;  // f * Px + q
+    const int z0 = zt * kTZ;
+    const C* base = src + (size_t)r * in_rows * nz + z0;
+    C* lb = lines + buf * kTZ * lw;
+    for (int idx = tid; idx < nin * kTZ; idx += kTileThreads) {
+      const int w = idx & 7, yy = idx >> 3;
+      bool valid = z0 + w < nz;
+      if (!INV) valid = valid && tmask[yy * nzt + zt];
+      const C* g = valid ? base + (size_t)yy * nz + w : src;
+      cp_async<sizeof(C)>(lb + w * lw + lay.addr(yy), g, valid);
+    }
+    cp_commit();
+  };
+
+  int task = blockIdx.x;
+  if (task < ntask) issue(task, 0);
+  for (int it = 0; task < ntask; ++it, task += gridDim.x) {
+    const int buf = it & 1;
+    const int next = task + gridDim.x;
+    if (next < ntask) {
+      issue(next, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    C* line = lines + (buf * kTZ + warp) * lw;
+    lay.template fft<INV>(line, twy, lane, ny);
+    __syncthreads();
+    const int zt = task % nzt;
+    const int r = task / nzt;
+    const int z0 = zt * kTZ;
+    C* ob = dst + (size_t)r * out_rows * nz + z0;
+    const C* lb = lines + buf * kTZ * lw;
+    for (int idx = tid; idx < nout * kTZ; idx += kTileThreads) {
+      const int w = idx & 7, yy = idx >> 3;
+      if (z0 + w >= nz) continue;
+      if (INV && !tmask[yy * nzt + zt]) continue;
+      ob[(size_t)yy * nz + w] = lb[w * lw + lay.addr(yy)];
+    }
+    __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
+  }
+}
+
+// ---------------------------------------------------------------- pass E
+// One CTA per listed (y, z-tile); loops over fields with the next field's
+// tile prefetched by cp.async; scatters the occupied sites.
+template <typename T, class Line>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, const int* __restrict__ occ,
+         const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, Line lay,
+         const typename cplx<T>::type* __restrict__ twx, const typename cplx<T>::type* __restrict__ x, int ldx,
+         const typename cplx<T>::type* __restrict__ diag, const typename cplx<T>::type* __restrict__ jpre,
+         typename cplx<T>::type* __restrict__ y, int ldy, const int* done) {
+  using C = typename cplx<T>::type;
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Px = lay.n();
+  const int lw = lay.lw();
+  C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
+  int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
+  const int tile = tiles[blockIdx.x];
+  const int yy = tile / nzt, z0 = (tile - yy * nzt) * kTZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const size_t rowstride = (size_t)ny * nz;
+  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
+    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
+    socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
+  }
+  auto issue = [&](int f, int buf) {
+    const C* base = t1 + (size_t)f * Px * rowstride + (size_t)yy * nz + z0;
+    C* lb = lines + buf * kTZ * lw;
+    for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
+      const int w = idx & 7, q = idx >> 3;
+      const bool valid = z0 + w < nz;
+      cp_async<sizeof(C)>(lb + w * lw + lay.addr(q), valid ? base + (size_t)q * rowstride + w : t1, valid);
+    }
+    cp_commit();
+  };
+  issue(0, 0);
+  int l = 0, c = 0;
+  for (int f = 0; f < nfield; ++f) {
+    const int buf = f & 1;
+    if (f + 1 < nfield) {
+      issue(f + 1, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    C* line = lines + (buf * kTZ + warp) * lw;
+    lay.template fft<true>(line, twx, lane, nx);
+    for (int xi = lane; xi < nx; xi += 32) {
+      const int m = socc[xi * kTZ + warp];
+      if (m < 0) continue;
+      const size_t r = 3 * (size_t)m + c;
+      C v = line[lay.addr(xi)];
+      if (diag != nullptr) v = cadd(v, cmul(diag[r], x[(size_t)l * ldx + r]));
+      if (jpre != nullptr) v = cmul(v, jpre[r]);
+      y[(size_t)l * ldy + r] = v;
+    }
+    __syncthreads();  // buffer 'buf' is the cp.async target of field f + 2
+    if (++c == 3) { c = 0; ++l; }
+  }
+}
+
+template <typename T> int smem_tile(int lw, int nx) {
+  return 2 * kTZ * lw * (int)sizeof(typename cplx<T>::type) + nx * kTZ * 4;
+}
+
+}  // namespace tile
+}  // namespace bdda

@@ -1,0 +1,59 @@
+// Strided passes (A, B, D, E) for complex FP32 with compile-time axis plans
+// (tplans.inc): the runtime kernels of tile_passes.cuh instantiated with the
+// StLine layout of the plan of their axis length.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "mvp.hpp"
+#include "tile_passes.cuh"
+
+namespace bdda {
+namespace tstatic {
+
+template <class K>
+cudaError_t set_smem(K kernel, int bytes, std::once_flag& once, cudaError_t& cfg) {
+  std::call_once(once, [&] { cfg = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes); });
+  return cfg;
+}
+
+template <class P>
+cudaError_t launch(int pass, const TileArgs& a) {
+  using L = tile::StLine<P>;
+  const MvpGeom& g = *a.g;
+  const int max_nx = kMaxLine / 2;
+  const int smem_ae = tile::smem_tile<float>(P::LW, max_nx);
+  const int smem_bd = tile::smem_tile<float>(P::LW, 0);
+  static std::once_flag oa, ob, od, oe;
+  static cudaError_t ca = cudaSuccess, cb = cudaSuccess, cd = cudaSuccess, ce = cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  switch (pass) {
+    case kTileA:
+      if ((e = set_smem(tile::k_pass_a<float, L>, smem_ae, oa, ca)) != cudaSuccess) return e;
+      tile::k_pass_a<float, L><<<g.ntiles, kTileThreads, tile::smem_tile<float>(P::LW, g.nx), a.st>>>(
+          a.x, a.ldx, a.nfield, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, L{}, a.twx, a.t1, a.done);
+      break;
+    case kTileB:
+      if ((e = set_smem(tile::k_pass_y<float, false, L>, smem_bd, ob, cb)) != cudaSuccess) return e;
+      tile::k_pass_y<float, false, L><<<a.grid_y, kTileThreads, smem_bd, a.st>>>(
+          a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzt, a.ntask_y, L{}, a.twy, a.done);
+      break;
+    case kTileD:
+      if ((e = set_smem(tile::k_pass_y<float, true, L>, smem_bd, od, cd)) != cudaSuccess) return e;
+      tile::k_pass_y<float, true, L><<<a.grid_y, kTileThreads, smem_bd, a.st>>>(
+          a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzt, a.ntask_y, L{}, a.twy, a.done);
+      break;
+    default:
+      if ((e = set_smem(tile::k_pass_e<float, L>, smem_ae, oe, ce)) != cudaSuccess) return e;
+      tile::k_pass_e<float, L><<<g.ntiles, kTileThreads, tile::smem_tile<float>(P::LW, g.nx), a.st>>>(
+          a.t1, a.nfield, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, L{}, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
+          a.done);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tstatic
+}  // namespace bdda

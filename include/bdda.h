@@ -284,10 +284,11 @@ const char* bdda_last_error(void);
  * arithmetic.  nvalid in
  * (0, N) makes the forward transform read only the first nvalid inputs (the
  * rest count as zero); 0 reads all.  data holds N interleaved complex doubles,
- * overwritten.  radix[0] on input > 8 selects the composite-radix schedule
- * (register radices up to that value, as used along z); radices are written
- * to radix[0..16) on return.  Returns the number of radix stages or -1 for an
- * unsupported N.
+ * overwritten.  The schedule is the one the operator gives an axis of that
+ * length for the element width of prec: radix[0] on input > 8 selects the z
+ * axis (fused three-line pass), otherwise the x / y axes (single-line tile
+ * passes).  Radices are written to radix[0..16) on return.  Returns the
+ * number of radix stages or -1 for an unsupported N.
  */
 int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, int* radix);
 
