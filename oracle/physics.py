@@ -106,28 +106,45 @@ def positions(n, lf, address):
     return np.stack([ix, iy, iz], axis=1).astype(np.float64) * lf
 
 
-def incident_fields(pos, k, einc, uinc):
-    """EHinc for f=3: ``einc_l exp(i k u_l . r_m)`` (``Target_manager.cpp:267-277``)."""
+def incident_fields(pos, k, einc, uinc, hinc=None):
+    """EHinc: f=3 rows ``einc_l exp(i k u_l . r_m)`` (``Target_manager.cpp:267-277``);
+    with ``hinc`` (f=6) rows 6m..6m+5 hold ``[einc_l, hinc_l] exp(i k u_l . r_m)``
+    (``Target_manager.cpp:280-291``)."""
     nocc = pos.shape[0]
     L = len(einc)
-    out = np.zeros((3 * nocc, L), dtype=np.complex128)
+    f = 3 if hinc is None else 6
+    out = np.zeros((f * nocc, L), dtype=np.complex128)
     for l in range(L):
         ph = np.exp(1j * k * (pos @ np.asarray(uinc[l])))
-        out[:, l] = (ph[:, None] * np.asarray(einc[l])[None, :]).reshape(-1)
+        amp = np.asarray(einc[l]) if hinc is None else np.concatenate([np.asarray(einc[l]), np.asarray(hinc[l])])
+        out[:, l] = (ph[:, None] * amp[None, :]).reshape(-1)
     return out
 
 
-def diag_a(alpha_e):
-    """DIAG_A = 1/alpha_E repeated over the 3 components (``Solver.cpp:33-36``)."""
-    return np.repeat(1.0 / np.asarray(alpha_e, dtype=np.complex128), 3)
+def diag_a(alpha_e, alpha_h=None):
+    """DIAG_A: 1/alpha_E over the 3 components (``Solver.cpp:33-36``); with
+    ``alpha_h`` (f=6) 1/alpha_E then 1/alpha_H per dipole (``Solver.cpp:40-45``)."""
+    ae = 1.0 / np.asarray(alpha_e, dtype=np.complex128)
+    if alpha_h is None:
+        return np.repeat(ae, 3)
+    ah = 1.0 / np.asarray(alpha_h, dtype=np.complex128)
+    return np.concatenate([np.repeat(ae[:, None], 3, 1), np.repeat(ah[:, None], 3, 1)], axis=1).reshape(-1)
 
 
-def cross_sections(k: float, ehinc, pm, alpha0):
-    """Cext, Cabs, Csca per incident wave, f=3 (``Result_manager.cpp:132-143``).
+def cross_sections(k: float, ehinc, pm, alpha0, alpha_h0=None):
+    """Cext, Cabs, Csca per incident wave (``Result_manager.cpp:66-115``).
 
-    Cext = 4 pi k Im(E^H P); Cabs = 4 pi k (Im(conj(1/alpha_0)) - 2k^3/3) ||P||^2
-    with the polarizability of dipole 0 used for every dipole (``:135``).
+    Cext = 4 pi k Im(EH^H PM) over all rows.  f=3: Cabs = 4 pi k (Im(conj(1/alpha_0))
+    - 2k^3/3) ||P||^2 with the polarizability of dipole 0 used for every dipole
+    (``:73``).  f=6 (``alpha_h0`` given): the electric rows weigh with alpha_E(0),
+    the magnetic rows with alpha_H(0) (``:94-99``).
     """
     cext = 4 * math.pi * k * np.imag(np.sum(np.conj(ehinc) * pm, axis=0))
-    cabs = 4 * math.pi * k * (np.imag(np.conj(1.0 / alpha0)) - 2.0 * k ** 3 / 3.0) * np.sum(np.abs(pm) ** 2, axis=0)
+    we = np.imag(np.conj(1.0 / alpha0)) - 2.0 * k ** 3 / 3.0
+    if alpha_h0 is None:
+        cabs = 4 * math.pi * k * we * np.sum(np.abs(pm) ** 2, axis=0)
+    else:
+        wh = np.imag(np.conj(1.0 / alpha_h0)) - 2.0 * k ** 3 / 3.0
+        p6 = np.abs(pm.reshape(-1, 6, pm.shape[1])) ** 2
+        cabs = 4 * math.pi * k * (we * p6[:, :3].sum(axis=(0, 1)) + wh * p6[:, 3:].sum(axis=(0, 1)))
     return cext, cabs, cext - cabs

@@ -20,6 +20,10 @@ Fixtures:
 * ``result_dat_N512.json`` -- the recorded cross sections of ``result.dat:14-42``
   (f=3 block COCG-RQ-Jacobi, tol 1e-2, N_inc 4) plus the oracle's per-iteration
   error history and solution-level cross sections for the same run.
+* ``result_f6_BC_rpp20nm.json`` -- recorded f=6 (electric + magnetic dipoles)
+  BiCGSTAB-Jacobi runs of ``DDA_result_BC_rpp20nm.dat`` for the N8..N64
+  targets at eleven wavelengths, their target files, and the oracle's
+  reproduction of each.
 """
 from __future__ import annotations
 
@@ -157,20 +161,72 @@ def result_dat(ref, lib):
             "oracle_Cext": cext.tolist(), "oracle_Cabs": cabs.tolist(), "oracle_Csca": csca.tolist()}
 
 
+def _dat_sections(path):
+    txt = open(path).read()
+    secs = txt.split("####################### Start of result section #######################")[1:]
+    return [dict(re.findall(r"^(\w+)\t(.*)$", sec, re.M)) for sec in secs]
+
+
+def result_f6(ref, lib):
+    """Recorded f=6 runs of ``DDA_result_BC_rpp20nm.dat`` (BiCGSTAB-Jacobi, tol 1e-2,
+    ``Solver.cpp:64-66``; BC particles of r_pp = 20 nm) for the targets
+    ``DDA_target_0_agg_N{8,16,32,64}`` at all eleven wavelengths, with the
+    oracle's reproduction of each (iteration count and mean cross sections)."""
+    rows = _dat_sections(os.path.join(ref, "DDA_result_BC_rpp20nm.dat"))
+    scale = 0.02
+    names = [f"DDA_target_0_agg_N{N}_kf1.0_Df2.8.out" for N in (8, 16, 32, 64)]
+    targets = {nm: target_fixture(ref, nm, scale) for nm in names}
+    u, e, h = physics.reference_incident_waves(4)
+    cases = []
+    for r in rows:
+        if r["target_fname"] not in targets:
+            continue
+        t = targets[r["target_fname"]]
+        n, lf = tuple(t["n"]), t["lf"] * scale           # fixtures store the file's unscaled values
+        addr = np.array(t["address"])
+        vol = np.array(t["vol"]) * scale ** 3
+        wl0 = float(r["wl0"])
+        k = 2 * math.pi / wl0
+        ep = complex(*[float(v) for v in r["eper_particle"].strip("()").split(",")])
+        rp = np.cbrt(vol * 3 / (4 * math.pi))
+        ab = [gmie_a1b1(lib, wl0, x, ep) for x in rp]
+        ae = np.array([3j * a / (2 * k ** 3) for a, _b in ab])
+        ah = np.array([3j * b / (2 * k ** 3) for _a, b in ab])
+        diag = physics.diag_a(ae, ah)
+        B = physics.incident_fields(physics.positions(n, lf, addr), k, e, u, h)
+        gh, P = mbt.green_hat(n, 6, lf, k)
+        X, hist = krylov.bl_bicgstab(lambda S: mbt.block_mvp(n, 6, gh, P, addr, diag, S), B, 1e-2, 300,
+                                     diag=diag, jacobi=True)
+        cext, cabs, csca = physics.cross_sections(k, B, X, ae[0], ah[0])
+        mass = float(r["mass_particle"])
+        rec = {key: float(r[key]) for key in ("mean_Csca", "std_Csca", "mean_MAC", "std_MAC", "mean_SSA", "std_SSA",
+                                              "mass_particle", "volume_particle", "num_element_occupy", "wl0")}
+        cases.append({"target": r["target_fname"], "wl0": wl0, "eper": [ep.real, ep.imag], "recorded": rec,
+                      "alpha_e0": [ae[0].real, ae[0].imag], "alpha_h0": [ah[0].real, ah[0].imag],
+                      "oracle_iterations": len(hist), "oracle_mean_Csca": float(csca.mean()),
+                      "oracle_mean_MAC": float((cabs * 1e-12 / mass).mean()),
+                      "oracle_mean_SSA": float((csca / cext).mean())})
+    return {"scale_factor": scale, "tol": 1e-2, "itermax": 300, "solver": "bicgstab", "jacobi": True,
+            "targets": targets, "cases": cases}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", nargs="*", help="write only these fixture files")
     args = ap.parse_args()
     ref = args.ref
     lib = load_gmie(ref)
-    out = {
-        "mbt_f1_index_table.json": f1_table(ref),
-        "mie_ref.json": mie_sweep(lib),
-        "incident_dirs_ref.json": incident_dirs(),
-        "target_N512.json": target_fixture(ref, "DDA_target_0_agg_N512_kf1.0_Df2.8.out", 0.03),
-        "target_N16_coated.json": target_fixture(ref, "DDA_target_2_agg_N16_kf1.0_Df2.8.out", 0.02),
-        "result_dat_N512.json": result_dat(ref, lib),
+    makers = {
+        "mbt_f1_index_table.json": lambda: f1_table(ref),
+        "mie_ref.json": lambda: mie_sweep(lib),
+        "incident_dirs_ref.json": incident_dirs,
+        "target_N512.json": lambda: target_fixture(ref, "DDA_target_0_agg_N512_kf1.0_Df2.8.out", 0.03),
+        "target_N16_coated.json": lambda: target_fixture(ref, "DDA_target_2_agg_N16_kf1.0_Df2.8.out", 0.02),
+        "result_dat_N512.json": lambda: result_dat(ref, lib),
+        "result_f6_BC_rpp20nm.json": lambda: result_f6(ref, lib),
     }
+    out = {name: make() for name, make in makers.items() if not args.only or name in args.only}
     for name, obj in out.items():
         with open(os.path.join(HERE, name), "w") as fh:
             json.dump(obj, fh, indent=None, separators=(",", ":"))
