@@ -4,7 +4,8 @@ Thin ctypes layer over ``block-dda_gb300/_lib/libbdda.so`` used by the tests,
 the benchmark and ``__graft_entry__``.  There is no CPU fallback: if the
 library is missing, :func:`lib` raises.  Host matrices are numpy complex128
 arrays in column-major (Fortran) order, exactly the reference's Eigen layout
-(column l = right-hand side, row 3*m + c = component c of dipole m).
+(column l = right-hand side, row f*m + c = component c of dipole m; f = 3
+electric dipoles, f = 6 electric then magnetic).
 """
 from __future__ import annotations
 
@@ -35,6 +36,7 @@ EXPORTS = [
     "bdda_op_kernel_stats", "bdda_last_error", "bdda_op_mvp_bytes", "bdda_host_fft_line",
     "bdda_op_mvp_device_noalloc", "bdda_request_footprint", "bdda_server_create", "bdda_server_submit",
     "bdda_server_wait", "bdda_server_stats", "bdda_server_destroy", "bdda_batch_solve",
+    "bdda_incident_fields_eh", "bdda_cross_sections_eh",
 ]
 
 
@@ -107,6 +109,9 @@ def lib(build_if_missing: bool = False):
     L.bdda_aggregate.argtypes = [ct.c_int, ct.c_double, ct.c_double, ct.c_ulonglong, ip, ip]
     L.bdda_incident_fields.argtypes = [ip, ct.c_double, ip, ct.c_int, ct.c_double, ct.c_int, dp, dp, dp, ct.c_int]
     L.bdda_cross_sections.argtypes = [ct.c_double, dp, dp, ct.c_int, dp, ct.c_int, ct.c_int, ct.c_int, dp]
+    L.bdda_incident_fields_eh.argtypes = [ip, ct.c_double, ip, ct.c_int, ct.c_double, ct.c_int, dp, dp, dp, dp,
+                                          ct.c_int]
+    L.bdda_cross_sections_eh.argtypes = [ct.c_double, dp, dp, dp, ct.c_int, dp, ct.c_int, ct.c_int, ct.c_int, dp]
     L.bdda_op_mvp_bytes.argtypes = [vp, ct.c_int, ct.c_int, ct.c_int, ct.c_int, dp]
     L.bdda_op_set_timing.argtypes = [vp, ct.c_int]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
@@ -162,6 +167,7 @@ class Operator:
         self.n = tuple(int(v) for v in n3)
         self.lf = float(lf)
         self.k = k
+        self.f = int(f)    # 3: electric dipoles; 6: electric + magnetic (rows f*m + c)
         self.nocc = 0
 
     @property
@@ -295,6 +301,22 @@ def polarizability(wl0, r_p, eps_p, k, mu_p=1 + 0j):
     return 3j * a1 / (2.0 * k ** 3)
 
 
+def polarizabilities(wl0, r_p, eps_p, k, mu_p=1 + 0j):
+    """(alpha_E, alpha_H) = 3 i (a1, b1) / (2 k^3) (Target_manager.cpp:246-247)."""
+    a1, b1 = mie_a1b1(wl0, r_p, eps_p, mu_p)
+    return 3j * a1 / (2.0 * k ** 3), 3j * b1 / (2.0 * k ** 3)
+
+
+def diag_a(alpha_e, alpha_h=None):
+    """DIAG_A per row: 1/alpha_E over rows 3m..3m+2 (f=3, Solver.cpp:33-36), or
+    1/alpha_E then 1/alpha_H over rows 6m..6m+5 (f=6, Solver.cpp:40-45)."""
+    ae = 1.0 / np.asarray(alpha_e, dtype=np.complex128).reshape(-1)
+    if alpha_h is None:
+        return np.repeat(ae, 3)
+    ah = 1.0 / np.asarray(alpha_h, dtype=np.complex128).reshape(-1)
+    return np.concatenate([np.repeat(ae[:, None], 3, 1), np.repeat(ah[:, None], 3, 1)], axis=1).reshape(-1)
+
+
 def aggregate(nocc, kf=1.0, Df=2.8, seed=1):
     n = np.zeros(3, np.int32)
     addr = np.zeros(nocc, np.int32)
@@ -302,26 +324,39 @@ def aggregate(nocc, kf=1.0, Df=2.8, seed=1):
     return tuple(int(v) for v in n), addr
 
 
-def incident_fields(n, lf, address, k, uinc, einc):
+def incident_fields(n, lf, address, k, uinc, einc, hinc=None):
+    """EHinc: f=3 rows e exp(i k u.r); with ``hinc`` the f=6 rows [e, h] exp(i k u.r)."""
     n3 = np.ascontiguousarray(n, dtype=np.int32)
     a = np.ascontiguousarray(address, dtype=np.int32)
     u = np.ascontiguousarray(uinc, dtype=np.float64).reshape(-1, 3)
     e = np.ascontiguousarray(einc, dtype=np.complex128).reshape(-1, 3)
     L = u.shape[0]
-    B = np.zeros((3 * a.size, L), dtype=np.complex128, order="F")
-    _check(lib().bdda_incident_fields(_iptr(n3), float(lf), _iptr(a), int(a.size), float(k), L, _dptr(u),
-                                      _dptr(e), _dptr(B), 3 * a.size))
+    if hinc is None:
+        B = np.zeros((3 * a.size, L), dtype=np.complex128, order="F")
+        _check(lib().bdda_incident_fields(_iptr(n3), float(lf), _iptr(a), int(a.size), float(k), L, _dptr(u),
+                                          _dptr(e), _dptr(B), 3 * a.size))
+        return B
+    h = np.ascontiguousarray(hinc, dtype=np.complex128).reshape(-1, 3)
+    B = np.zeros((6 * a.size, L), dtype=np.complex128, order="F")
+    _check(lib().bdda_incident_fields_eh(_iptr(n3), float(lf), _iptr(a), int(a.size), float(k), L, _dptr(u),
+                                         _dptr(e), _dptr(h), _dptr(B), 6 * a.size))
     return B
 
 
-def cross_sections(k, alpha0, E, P):
+def cross_sections(k, alpha0, E, P, alpha_h0=None):
+    """(Cext, Cabs, Csca) per column; with ``alpha_h0`` the f=6 form (rows 6m + c)."""
     Em = _cmat(E)
     Pm = _cmat(P)
     n, L = Em.shape
     out = np.zeros(3 * L)
     a0 = np.array([complex(alpha0).real, complex(alpha0).imag])
-    _check(lib().bdda_cross_sections(float(k), _dptr(a0), _dptr(Em), n, _dptr(Pm),
-                                     n, n, L, _dptr(out)))
+    if alpha_h0 is None:
+        _check(lib().bdda_cross_sections(float(k), _dptr(a0), _dptr(Em), n, _dptr(Pm),
+                                         n, n, L, _dptr(out)))
+    else:
+        h0 = np.array([complex(alpha_h0).real, complex(alpha_h0).imag])
+        _check(lib().bdda_cross_sections_eh(float(k), _dptr(a0), _dptr(h0), _dptr(Em), n, _dptr(Pm), n, n // 6, L,
+                                            _dptr(out)))
     out = out.reshape(L, 3)
     return out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy()
 

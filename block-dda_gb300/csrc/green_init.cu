@@ -5,8 +5,9 @@
 // mvp_fft/MBT_fft_init.cpp:22-35): instead of the length f^2 prod(2n_i-1) 1-D
 // MBT projection, the 3x3 block A(d) = -G(d lf) is evaluated on the 2x-padded
 // circulant grid (index j -> offset j for j < n, j - P for j > P - n, zero in
-// the gap and at d = 0), its 6 distinct components are transformed with a full
-// 3-D FFT in FP64, divided by Px*Py*Pz and re-tiled for the fused x pass.
+// the gap and at d = 0), its 6 distinct components (9 with the magnetic
+// coupling of f = 6) are transformed with a full 3-D FFT in FP64, divided by
+// Px*Py*Pz and re-tiled for the fused z pass.
 #include <mutex>
 #include <vector>
 
@@ -23,8 +24,10 @@ __device__ __forceinline__ bool circ_offset(int j, int n, int P, int* d) {
   return false;
 }
 
-// g[comp][jx][jy][jz], comp = xx, xy, xz, yy, yz, zz of A = -G.
-__global__ void k_green_eval(double2* __restrict__ g, int nx, int ny, int nz, int Px, int Py, int Pz,
+// g[comp][jx][jy][jz], comp = xx, xy, xz, yy, yz, zz of A = -G; with nc = 9
+// (f = 6) also comp 6..8 = xy, xz, yz of B = -F, F = -k^2 e^{ikr}/r
+// (1 - 1/(ikr)) [r^ x] (mvp_fft/application_function.cpp:52-64).
+__global__ void k_green_eval(double2* __restrict__ g, int nc, int nx, int ny, int nz, int Px, int Py, int Pz,
                              double lf, double kr, double ki) {
   const size_t ng = (size_t)Px * Py * Pz;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < ng; idx += (size_t)gridDim.x * blockDim.x) {
@@ -32,9 +35,9 @@ __global__ void k_green_eval(double2* __restrict__ g, int nx, int ny, int nz, in
     const int jy = (int)((idx / Pz) % Py);
     const int jx = (int)(idx / ((size_t)Pz * Py));
     int dx, dy, dz;
-    double2 out[6];
+    double2 out[9];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) out[c] = make_double2(0.0, 0.0);
+    for (int c = 0; c < 9; ++c) out[c] = make_double2(0.0, 0.0);
     if (circ_offset(jx, nx, Px, &dx) && circ_offset(jy, ny, Py, &dy) && circ_offset(jz, nz, Pz, &dz) &&
         (dx | dy | dz) != 0) {
       const double rx = dx * lf, ry = dy * lf, rz = dz * lf;
@@ -63,9 +66,20 @@ __global__ void k_green_eval(double2* __restrict__ g, int nx, int ny, int nz, in
           out[c++] = make_double2(-gab.x, -gab.y);
         }
       }
+      if (nc == 9) {
+        // fac = -k^2 e (1 - 1/w), w = i k r; B = -F: B_xy = fac u_z, B_xz = -fac u_y, B_yz = fac u_x
+        const double2 w = make_double2(-ki * r, kr * r);
+        const double w2 = w.x * w.x + w.y * w.y;
+        const double2 one_m = make_double2(1.0 - w.x / w2, w.y / w2);  // 1 - conj(w) / |w|^2
+        const double2 ce = cmul(c1, e);
+        const double2 fac = cmul(make_double2(-ce.x, -ce.y), one_m);
+        const double ux = rx / r, uy = ry / r, uz = rz / r;
+        out[6] = make_double2(fac.x * uz, fac.y * uz);
+        out[7] = make_double2(-fac.x * uy, -fac.y * uy);
+        out[8] = make_double2(fac.x * ux, fac.y * ux);
+      }
     }
-#pragma unroll
-    for (int c = 0; c < 6; ++c) g[(size_t)c * ng + idx] = out[c];
+    for (int c = 0; c < nc; ++c) g[(size_t)c * ng + idx] = out[c];
   }
 }
 
@@ -112,16 +126,17 @@ k_fft_strided(double2* __restrict__ data, size_t Cc, AxisPlan p, const double2* 
   }
 }
 
-// g[comp][qx][qy][qz] / Ng  ->  ghat[qx][qy][comp][qz]
+// g[comp][qx][qy][qz] / Ng  ->  ghat[qx][qy][comp][qz], nc components
 template <typename C>
-__global__ void k_green_pack(const double2* __restrict__ g, C* __restrict__ out, int Px, int Py, int Pz, double scale) {
+__global__ void k_green_pack(const double2* __restrict__ g, C* __restrict__ out, int nc, int Px, int Py, int Pz,
+                             double scale) {
   const size_t ng = (size_t)Px * Py * Pz;
-  const size_t total = 6 * ng;
+  const size_t total = (size_t)nc * ng;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
     const int qz = (int)(idx % Pz);
     const size_t t = idx / Pz;
-    const int comp = (int)(t % 6);
-    const size_t line = t / 6;  // qx * Py + qy
+    const int comp = (int)(t % nc);
+    const size_t line = t / nc;  // qx * Py + qy
     double2 v = g[(size_t)comp * ng + line * Pz + qz];
     out[idx] = cmake((decltype(C::x))(v.x * scale), (decltype(C::x))(v.y * scale));
   }
@@ -143,30 +158,31 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
     if (cfg == cudaSuccess) cfg = cudaFuncSetAttribute(k_fft_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
   });
   if ((e = cfg) != cudaSuccess) return e;
-  k_green_eval<<<1216, 256, 0, st>>>(work, g.nx, g.ny, g.nz, Px, Py, Pz, lf, k_re, k_im);
+  const int nc = g.f == 6 ? 9 : 6;
+  k_green_eval<<<1216, 256, 0, st>>>(work, nc, g.nx, g.ny, g.nz, Px, Py, Pz, lf, k_re, k_im);
   // z lines (contiguous)
   {
-    const size_t nlines = 6 * (size_t)Px * Py;
+    const size_t nlines = (size_t)nc * Px * Py;
     const int sm = kInitWarps * plan_lw<double2>(g.pz) * (int)sizeof(double2);
     k_fft_contig<<<(unsigned)((nlines + kInitWarps - 1) / kInitWarps), kInitWarps * 32, sm, st>>>(work, nlines, g.pz, twz);
   }
   // y lines: data[6*Px][Py][Pz]
   {
-    dim3 grid((unsigned)((Pz + kInitWarps - 1) / kInitWarps), 6 * Px);
+    dim3 grid((unsigned)((Pz + kInitWarps - 1) / kInitWarps), nc * Px);
     const int sm = kInitWarps * plan_lw<double2>(g.py) * (int)sizeof(double2);
     k_fft_strided<<<grid, kInitWarps * 32, sm, st>>>(work, (size_t)Pz, g.py, twy);
   }
   // x lines: data[6][Px][Py*Pz]
   {
     const size_t cc = (size_t)Py * Pz;
-    dim3 grid((unsigned)((cc + kInitWarps - 1) / kInitWarps), 6);
+    dim3 grid((unsigned)((cc + kInitWarps - 1) / kInitWarps), nc);
     const int sm = kInitWarps * plan_lw<double2>(g.px) * (int)sizeof(double2);
     k_fft_strided<<<grid, kInitWarps * 32, sm, st>>>(work, cc, g.px, twx);
   }
   const double scale = 1.0 / (double)ng;
-  if (ghat_d) k_green_pack<double2><<<2432, 256, 0, st>>>(work, ghat_d, Px, Py, Pz, scale);
-  if (ghat_f) k_green_pack<float2><<<2432, 256, 0, st>>>(work, ghat_f, Px, Py, Pz, scale);
-  if (ghat_df) k_green_pack<dfc><<<2432, 256, 0, st>>>(work, ghat_df, Px, Py, Pz, scale);
+  if (ghat_d) k_green_pack<double2><<<2432, 256, 0, st>>>(work, ghat_d, nc, Px, Py, Pz, scale);
+  if (ghat_f) k_green_pack<float2><<<2432, 256, 0, st>>>(work, ghat_f, nc, Px, Py, Pz, scale);
+  if (ghat_df) k_green_pack<dfc><<<2432, 256, 0, st>>>(work, ghat_df, nc, Px, Py, Pz, scale);
   return cudaGetLastError();
 }
 

@@ -12,11 +12,19 @@ namespace bdda {
 // rows of 8 x c64 = 64 B or 8 x c128 = 128 B.
 constexpr int kTZ = 8;
 constexpr int kTileThreads = kTZ * 32;
-// Warps per CTA of the fused z pass (one (x, y, rhs) task each).
+// Warps per CTA of the fused z pass (one (x, y, rhs) task each), at most.
 constexpr int kZWarps = 8;
+// Dynamic shared memory one CTA may take (227 KB).
+constexpr int kZSmemMax = 227 * 1024;
+// Warps per CTA of the z pass when each warp needs per_warp bytes of lines.
+inline int z_warps_per_cta(int per_warp) {
+  const int w = kZSmemMax / (per_warp > 0 ? per_warp : 1);
+  return w < 1 ? 1 : (w > kZWarps ? kZWarps : w);
+}
 
 // Geometry shared by both precisions (device pointers).
 struct MvpGeom {
+  int f;                       // components per dipole: 3 (E) or 6 (E, M)
   int nx, ny, nz;
   int Px, Py, Pz;
   AxisPlan px, py, pz;
@@ -34,7 +42,7 @@ template <typename T> struct MvpPrec {
   const C* twx;
   const C* twy;
   const C* twz;
-  const C* ghat;  // [Px][Py][6][Pz] (digit-reversed frequencies), divided by Px*Py*Pz
+  const C* ghat;  // [Px][Py][6 or 9][Pz] (digit-reversed frequencies), divided by Px*Py*Pz
 };
 
 // Timed kernel classes: the five MVP passes per precision (FP32 first), then
@@ -93,8 +101,8 @@ struct KernelTimer {
 };
 
 // Workspace elements (complex T) the MVP needs for L right-hand sides.
-inline size_t mvp_t1_elems(const MvpGeom& g, int L) { return 3ull * L * g.Px * g.ny * g.nz; }
-inline size_t mvp_t2_elems(const MvpGeom& g, int L) { return 3ull * L * g.Px * g.Py * g.nz; }
+inline size_t mvp_t1_elems(const MvpGeom& g, int L) { return (size_t)g.f * L * g.Px * g.ny * g.nz; }
+inline size_t mvp_t2_elems(const MvpGeom& g, int L) { return (size_t)g.f * L * g.Px * g.Py * g.nz; }
 
 template <typename T>
 cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typename cplx<T>::type* x, int ldx,
@@ -136,8 +144,8 @@ bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz
                           const int* done, cudaError_t* err);
 
 // Green tensor: build Ghat (FP64 evaluation + FP64 3-D FFT), layout
-// [Px][Py][6][Pz], for either precision (null pointers skipped).
-// work: c128 [6*Px*Py*Pz].
+// [Px][Py][nc][Pz] with nc = 6 (g.f = 3) or 9 (g.f = 6), for any of the
+// precisions (null pointers skipped).  work: c128 [nc*Px*Py*Pz].
 cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_im,
                             const double2* twx, const double2* twy, const double2* twz,
                             double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, cudaStream_t st);

@@ -4,11 +4,12 @@
 // Au_til product -> FFTW inv -> BT_reconstruct -> gather -> DIAG add -> jpre
 // (mvp_fft/MBT_fft_mvp.cpp:19-32, bl_krylov_mvp_fft/bl_cocg_rq_jacobi_mvp_fft.cpp:43-60)
 // by the mathematically identical 2x-padded 3-D FFT convolution with the
-// 6-component symmetric Green tensor.  Fields are the 3*L (component, RHS)
-// pairs; field f = 3*l + c.
+// 6-component symmetric Green tensor (f = 3; f = 6 adds the magnetic dipoles
+// and the 3-component antisymmetric coupling).  Fields are the f*L
+// (component, RHS) pairs; field = f*l + c.
 //
 // HBM layouts (element = complex T):
-//   x, y   : column-major (rows 3*m + c, column l, leading dimension ld) --
+//   x, y   : column-major (rows f*m + c, column l, leading dimension ld) --
 //            the reference's Eigen layout of S / AS.
 //   occ    : int32 [nx][ny][nz], dipole index of a lattice site or -1.
 //   tiles  : int32 list of (y, z-tile) pairs (y*nzt + zt, 8-wide z tiles)
@@ -30,6 +31,8 @@
 // The strided passes stage 8 z-columns per CTA; B, D and E prefetch the next
 // tile with cp.async (zero-filled outside the box) while the current one is
 // transformed.
+#pragma once
+
 #include <algorithm>
 #include <type_traits>
 
@@ -37,6 +40,7 @@
 
 #include "mvp.hpp"
 #include "tile_passes.cuh"
+#include "zproduct.cuh"
 
 namespace bdda {
 
@@ -45,10 +49,12 @@ namespace {
 __device__ __forceinline__ bool skip(const int* done) { return done && *(volatile const int*)done; }
 
 // ---------------------------------------------------------------- pass C
-// One warp per task (x = q, y = qy, rhs l): the three component lines along z.
+// One warp per task (x = q, y = qy, rhs l): the fc = 3 (E) or 6 (E, M)
+// component lines along z, transformed three at a time; blockDim.x / 32
+// warps per CTA.
 template <typename T>
 __global__ void __launch_bounds__(kZWarps * 32)
-k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz, AxisPlan pz,
+k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int fc, int Px, int Py, int nz, AxisPlan pz,
          const typename cplx<T>::type* __restrict__ twz, const typename cplx<T>::type* __restrict__ ghat,
          const int* done) {
   using C = typename cplx<T>::type;
@@ -57,43 +63,32 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int Px, int Py, int nz,
   const int Pz = pz.N;
   const int lw = plan_lw<C>(pz), sh = plan_sk<C>(pz);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long task = (long long)blockIdx.x * kZWarps + warp;
+  const long long task = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
   const long long ntask = (long long)Px * Py * L;
   if (task >= ntask) return;
   const int l = (int)(task % L);
   const long long line = task / L;  // q * Py + qy
-  C* s0 = reinterpret_cast<C*>(smem_raw) + (size_t)warp * 3 * lw;
-  C* s1 = s0 + lw;
-  C* s2 = s1 + lw;
+  C* s0 = reinterpret_cast<C*>(smem_raw) + (size_t)warp * fc * lw;
   const size_t fstride = (size_t)Px * Py * nz;  // between fields
-  C* g0 = t2 + (size_t)(3 * l) * fstride + (size_t)line * nz;
+  C* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nz;
+  const bool six = fc == 6;
   for (int z = lane; z < nz; z += 32) {
-    s0[skw(z, sh)] = g0[z];
-    s1[skw(z, sh)] = g0[fstride + z];
-    s2[skw(z, sh)] = g0[2 * fstride + z];
+    const int a = skw(z, sh);
+    for (int c = 0; c < fc; ++c) s0[c * lw + a] = g0[c * fstride + z];
   }
   __syncwarp();
-  warp_fft_lines<false, 3>(s0, lw, twz, pz, lane, 32, nz);
-  const C* gl = ghat + (size_t)line * 6 * Pz;
-  for (int p = lane; p < Pz; p += 32) {
-    const int sp = skw(p, sh);
-    const C a0 = s0[sp], a1 = s1[sp], a2 = s2[sp];
-    const C gxx = ldg_c(gl + p), gxy = ldg_c(gl + Pz + p), gxz = ldg_c(gl + 2 * Pz + p);
-    const C gyy = ldg_c(gl + 3 * Pz + p), gyz = ldg_c(gl + 4 * Pz + p), gzz = ldg_c(gl + 5 * Pz + p);
-    s0[sp] = cadd(cadd(cmul(gxx, a0), cmul(gxy, a1)), cmul(gxz, a2));
-    s1[sp] = cadd(cadd(cmul(gxy, a0), cmul(gyy, a1)), cmul(gyz, a2));
-    s2[sp] = cadd(cadd(cmul(gxz, a0), cmul(gyz, a1)), cmul(gzz, a2));
-  }
+  const int halves = six ? 2 : 1;  // line triples: E, then M
+  for (int h = 0; h < halves; ++h) warp_fft_lines<false, 3>(s0 + 3 * h * lw, lw, twz, pz, lane, 32, nz);
+  const C* gl = ghat + (size_t)line * (six ? 9 : 6) * Pz;
+  for (int p = lane; p < Pz; p += 32) z_product(s0, lw, skw(p, sh), gl, Pz, p, six);
   __syncwarp();
-  warp_fft_lines<true, 3>(s0, lw, twz, pz, lane);
+  for (int h = 0; h < halves; ++h) warp_fft_lines<true, 3>(s0 + 3 * h * lw, lw, twz, pz, lane);
   for (int z = lane; z < nz; z += 32) {
-    g0[z] = s0[skw(z, sh)];
-    g0[fstride + z] = s1[skw(z, sh)];
-    g0[2 * fstride + z] = s2[skw(z, sh)];
+    const int a = skw(z, sh);
+    for (int c = 0; c < fc; ++c) g0[c * fstride + z] = s0[c * lw + a];
   }
 }
 
-template <typename T> int smem_z(int lw) { return kZWarps * 3 * lw * (int)sizeof(typename cplx<T>::type); }
 
 int num_sms() {
   static const int n = [] {
@@ -115,7 +110,7 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
                              typename cplx<T>::type* t1, typename cplx<T>::type* t2,
                              cudaStream_t st, KernelTimer* timer, const int* done) {
   using C = typename cplx<T>::type;
-  const int nfield = 3 * L;
+  const int nfield = g.f * L;
   const int pbase = sizeof(T) == sizeof(double) ? (kPassA64 - kPassA) : 0;
   if (g.ntiles == 0) return cudaSuccess;  // no dipoles
   const int ntask_y = nfield * g.Px * g.nzt;
@@ -140,7 +135,7 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   if (timer) timer->begin(kPassA + pbase, st);
   if (!static_tile(kTileA))
     tile::k_pass_a<T><<<g.ntiles, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
-        x, ldx, nfield, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, lx, p.twx, t1, done);
+        x, ldx, nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, lx, p.twx, t1, done);
   if (timer) timer->end(kPassA + pbase, st);
   if (serr != cudaSuccess) return serr;
   // B
@@ -153,7 +148,6 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   // C
   {
     const long long ntask = (long long)g.Px * g.Py * L;
-    const unsigned grid = (unsigned)((ntask + kZWarps - 1) / kZWarps);
     if (timer) timer->begin(kPassC + pbase, st);
     bool launched = false;
     if constexpr (std::is_same<T, float>::value) {
@@ -161,9 +155,12 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
       launched = launch_pass_c_static(g, t2, L, p.twz, p.ghat, st, done, &e);
       if (launched && e != cudaSuccess) return e;
     }
-    if (!launched)
-      k_pass_c<T><<<grid, kZWarps * 32, smem_z<T>(plan_lw<C>(g.pz)), st>>>(t2, L, g.Px, g.Py, g.nz, g.pz, p.twz, p.ghat,
-                                                                          done);
+    if (!launched) {
+      const int per_warp = g.f * plan_lw<C>(g.pz) * (int)sizeof(C);
+      const int wpc = z_warps_per_cta(per_warp);
+      const unsigned grid = (unsigned)((ntask + wpc - 1) / wpc);
+      k_pass_c<T><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.f, g.Px, g.Py, g.nz, g.pz, p.twz, p.ghat, done);
+    }
     if (timer) timer->end(kPassC + pbase, st);
   }
   // D
@@ -177,7 +174,7 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   if (timer) timer->begin(kPassE + pbase, st);
   if (!static_tile(kTileE))
     tile::k_pass_e<T><<<g.ntiles, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
-        t1, nfield, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, done);
+        t1, nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, done);
   if (timer) timer->end(kPassE + pbase, st);
   if (serr != cudaSuccess) return serr;
   return cudaGetLastError();
@@ -188,7 +185,7 @@ cudaError_t configure_mvp_kernels() {
   using C = typename cplx<T>::type;
   using Rt = tile::RtLine<C>;
   const int ts = tile::smem_tile<T>(kMaxLineWords, kMaxLine / 2);
-  const int zs = smem_z<T>(kMaxLineWords);
+  const int zs = kZSmemMax;
   const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(tile::k_pass_a<T, Rt>, attr, ts)) != cudaSuccess) return e;
@@ -197,17 +194,5 @@ cudaError_t configure_mvp_kernels() {
   if ((e = cudaFuncSetAttribute(tile::k_pass_y<T, true, Rt>, attr, ts)) != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_pass_c<T>, attr, zs);
 }
-
-template cudaError_t launch_block_mvp<float>(const MvpGeom&, const MvpPrec<float>&, const float2*, int, float2*, int, int,
-                                             const float2*, const float2*, float2*, float2*, cudaStream_t, KernelTimer*,
-                                             const int*);
-template cudaError_t launch_block_mvp<double>(const MvpGeom&, const MvpPrec<double>&, const double2*, int, double2*, int,
-                                              int, const double2*, const double2*, double2*, double2*, cudaStream_t,
-                                              KernelTimer*, const int*);
-template cudaError_t launch_block_mvp<dfl>(const MvpGeom&, const MvpPrec<dfl>&, const dfc*, int, dfc*, int, int,
-                                           const dfc*, const dfc*, dfc*, dfc*, cudaStream_t, KernelTimer*, const int*);
-template cudaError_t configure_mvp_kernels<float>();
-template cudaError_t configure_mvp_kernels<double>();
-template cudaError_t configure_mvp_kernels<dfl>();
 
 }  // namespace bdda

@@ -72,7 +72,7 @@ int mvp_noalloc(Op* op, const void* x, int ldx, void* y, int ldy, int L, const v
     return BDDA_ERR_INVALID;
   }
   const Occupancy& o = op->dip;
-  if (L < 1 || ldx < 3 * o.nocc || ldy < 3 * o.nocc) {
+  if (L < 1 || ldx < op->f * o.nocc || ldy < op->f * o.nocc) {
     set_error("bad L or leading dimension");
     return BDDA_ERR_INVALID;
   }

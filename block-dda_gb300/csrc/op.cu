@@ -143,7 +143,7 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
     set_error("operator was created without the tables of this precision");
     return BDDA_ERR_INVALID;
   }
-  if (L < 1 || ldx < 3 * o.nocc || ldy < 3 * o.nocc) {
+  if (L < 1 || ldx < op->f * o.nocc || ldy < op->f * o.nocc) {
     set_error("bad L or leading dimension");
     return BDDA_ERR_INVALID;
   }
@@ -177,7 +177,7 @@ const char* bdda_last_error(void) { return bdda::last_error(); }
 int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re, double k_im, int prec) {
   if (!out || !n) { set_error("null argument"); return BDDA_ERR_INVALID; }
   *out = nullptr;
-  if (f != 3) { set_error("unknown f value (only f=3 is supported)"); return BDDA_ERR_INVALID; }
+  if (f != 3 && f != 6) { set_error("unknown f value (3 or 6)"); return BDDA_ERR_INVALID; }
   if ((prec & (BDDA_PREC_FP64 | BDDA_PREC_FP32 | BDDA_PREC_DF64)) == 0) {
     set_error("no precision requested");
     return BDDA_ERR_INVALID;
@@ -237,10 +237,11 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
   const int Px = op->P[0], Py = op->P[1], Pz = op->P[2];
   const size_t ng = (size_t)Px * Py * Pz;
   DevBuf work;
-  BDDA_CUDA(work.ensure(6 * ng * sizeof(double2), op->stream));
-  if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure(6 * ng * sizeof(double2), op->stream));
-  if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure(6 * ng * sizeof(float2), op->stream));
-  if (prec & BDDA_PREC_DF64) BDDA_CUDA(op->ghatdf.ensure(6 * ng * sizeof(dfc), op->stream));
+  const size_t nc = f == 6 ? 9 : 6;  // Green components (symmetric A; f = 6 adds antisymmetric B)
+  BDDA_CUDA(work.ensure(nc * ng * sizeof(double2), op->stream));
+  if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure(nc * ng * sizeof(double2), op->stream));
+  if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure(nc * ng * sizeof(float2), op->stream));
+  if (prec & BDDA_PREC_DF64) BDDA_CUDA(op->ghatdf.ensure(nc * ng * sizeof(dfc), op->stream));
   // one spectrum per distinct digit order (radix sequences) of the plan sets
   bool same = true;
   for (int i = 0; i < 3; ++i) {
@@ -289,7 +290,7 @@ int bdda_mbt_fft_mvp(bdda_op* op, const double* p_hat, double* q_hat) {
     int rc = build_occupancy(op, nullptr, 0, &op->cub);
     if (rc) return rc;
   }
-  const size_t nrow = 3 * (size_t)op->cub.nocc;
+  const size_t nrow = (size_t)op->f * op->cub.nocc;
   DevBuf x, y;
   BDDA_CUDA(x.ensure(nrow * sizeof(double2), op->stream));
   BDDA_CUDA(y.ensure(nrow * sizeof(double2), op->stream));
@@ -326,7 +327,8 @@ int bdda_op_mvp_bytes(const bdda_op* op, int prec, int L, int with_diag, int wit
     return BDDA_ERR_INVALID;
   }
   const double s = prec == BDDA_PREC_FP64 ? 16.0 : 8.0;
-  const double F = 3.0 * L;
+  const double F = (double)op->f * L;                     // fields
+  const double nc = op->f == 6 ? 9.0 : 6.0;               // Green components
   const double nocc = op->dip.nocc;
   const double nx = op->n[0], nz = op->n[2], Px = op->P[0], Py = op->P[1], Pz = op->P[2];
   const double rows = (double)op->dip.tile_rows;          // (y, z) columns of occupied tiles
@@ -334,12 +336,12 @@ int bdda_op_mvp_bytes(const bdda_op* op, int prec, int L, int with_diag, int wit
   const double t2 = F * Px * Py * nz * s;                 // y-transformed planes
   const double vec = F * nocc * s;                        // one compact block
   const double occ = nx * rows * 4.0;                     // occupancy of the tiles
-  const double ghat = 6.0 * Px * Py * Pz * s;
+  const double ghat = nc * Px * Py * Pz * s;
   bytes[0] = vec + occ + t1;
   bytes[1] = t1 + t2;
   bytes[2] = 2.0 * t2 + ghat;
   bytes[3] = t2 + t1;
-  bytes[4] = t1 + occ + vec + (with_diag ? vec + 3.0 * nocc * s : 0.0) + (with_jpre ? 3.0 * nocc * s : 0.0);
+  bytes[4] = t1 + occ + vec + (with_diag ? vec + op->f * nocc * s : 0.0) + (with_jpre ? op->f * nocc * s : 0.0);
   return BDDA_OK;
 }
 

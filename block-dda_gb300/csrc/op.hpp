@@ -80,6 +80,7 @@ struct Op {
 
   MvpGeom geom(const Occupancy& o, int set) const {
     MvpGeom g;
+    g.f = f;
     g.nx = n[0]; g.ny = n[1]; g.nz = n[2];
     g.Px = P[0]; g.Py = P[1]; g.Pz = P[2];
     g.px = plan[set][0]; g.py = plan[set][1]; g.pz = plan[set][2];

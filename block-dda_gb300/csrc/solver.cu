@@ -628,10 +628,10 @@ static int true_residual(Op* op, cudaStream_t st, const double2* diag, const dou
 
 static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, const double2* B, int ldb, double2* X,
                       int ldx, int L, bdda_solve_stats* stats, cudaStream_t st) {
-  const int n = 3 * op->dip.nocc;
+  const int n = op->f * op->dip.nocc;
   if (n == 0) { set_error("no dipoles set on the operator"); return BDDA_ERR_INVALID; }
   if (L < 1 || L > kMaxL) { set_error("nrhs must be 1..32"); return BDDA_ERR_INVALID; }
-  if (ldb < n || ldx < n) { set_error("leading dimension smaller than 3*nocc"); return BDDA_ERR_INVALID; }
+  if (ldb < n || ldx < n) { set_error("leading dimension smaller than f*nocc"); return BDDA_ERR_INVALID; }
   const bool mixed = o->precision == BDDA_SOLVE_MIXED;
   if (mixed && !(op->prec & BDDA_PREC_FP32)) { set_error("mixed precision needs BDDA_PREC_FP32 tables"); return BDDA_ERR_INVALID; }
   // residuals of a mixed refinement run on double-float tables when present
@@ -779,7 +779,7 @@ int bdda_solve(bdda_op* op, const bdda_solve_opts* opts, const double* diag, con
                int L, bdda_solve_stats* stats) {
   if (!op || !opts || !diag || !B || !X) { set_error("null argument"); return BDDA_ERR_INVALID; }
   std::lock_guard<std::mutex> lk(op->mu);
-  const int n = 3 * op->dip.nocc;
+  const int n = op->f * op->dip.nocc;
   if (n == 0) { set_error("no dipoles set on the operator"); return BDDA_ERR_INVALID; }
   if (ldb < n || ldx < n || L < 1) { set_error("bad leading dimension or nrhs"); return BDDA_ERR_INVALID; }
   cudaStream_t st = op->stream;

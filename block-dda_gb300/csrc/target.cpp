@@ -226,4 +226,61 @@ int bdda_cross_sections(double k, const double alpha0[2], const double* E, int l
   return BDDA_OK;
 }
 
+int bdda_incident_fields_eh(const int n[3], double lf, const int* address, int nocc, double k, int L,
+                            const double* uinc, const double* einc, const double* hinc, double* B, int ldb) {
+  if (!n || !address || !uinc || !einc || !hinc || !B || nocc < 1 || L < 1 || ldb < 6 * nocc) {
+    bdda::set_error("bad incident-field arguments");
+    return BDDA_ERR_INVALID;
+  }
+  const long long nyz = (long long)n[1] * n[2];
+  for (int l = 0; l < L; ++l) {
+    const double* u = uinc + 3 * l;
+    cd eh[6];
+    for (int c = 0; c < 3; ++c) {
+      eh[c] = cd(einc[6 * l + 2 * c], einc[6 * l + 2 * c + 1]);
+      eh[3 + c] = cd(hinc[6 * l + 2 * c], hinc[6 * l + 2 * c + 1]);
+    }
+    for (int m = 0; m < nocc; ++m) {
+      const long long a = address[m];
+      const long long ix = a / nyz, iy = (a - nyz * ix) / n[2], iz = a - nyz * ix - (long long)n[2] * iy;
+      const double ph = k * lf * (u[0] * ix + u[1] * iy + u[2] * iz);
+      const cd p(std::cos(ph), std::sin(ph));
+      for (int c = 0; c < 6; ++c) {
+        const cd v = eh[c] * p;
+        const size_t r = (size_t)l * ldb + 6 * (size_t)m + c;
+        B[2 * r] = v.real();
+        B[2 * r + 1] = v.imag();
+      }
+    }
+  }
+  return BDDA_OK;
+}
+
+int bdda_cross_sections_eh(double k, const double alpha_e0[2], const double alpha_h0[2], const double* EH, int lde,
+                           const double* PM, int ldp, int nocc, int L, double* out) {
+  if (!alpha_e0 || !alpha_h0 || !EH || !PM || !out || nocc < 1 || L < 1 || lde < 6 * nocc || ldp < 6 * nocc) {
+    bdda::set_error("bad cross-section arguments");
+    return BDDA_ERR_INVALID;
+  }
+  const double we = std::imag(std::conj(1.0 / cd(alpha_e0[0], alpha_e0[1]))) - 2.0 * k * k * k / 3.0;
+  const double wh = std::imag(std::conj(1.0 / cd(alpha_h0[0], alpha_h0[1]))) - 2.0 * k * k * k / 3.0;
+  for (int l = 0; l < L; ++l) {
+    cd dot(0, 0);
+    double pe = 0.0, pm = 0.0;
+    for (int r = 0; r < 6 * nocc; ++r) {
+      const cd e(EH[2 * ((size_t)l * lde + r)], EH[2 * ((size_t)l * lde + r) + 1]);
+      const cd p(PM[2 * ((size_t)l * ldp + r)], PM[2 * ((size_t)l * ldp + r) + 1]);
+      dot += std::conj(e) * p;
+      if (r % 6 < 3) pe += std::norm(p);
+      else pm += std::norm(p);
+    }
+    const double cext = 4.0 * M_PI * k * dot.imag();
+    const double cabs = 4.0 * M_PI * k * (we * pe + wh * pm);
+    out[3 * l + 0] = cext;
+    out[3 * l + 1] = cabs;
+    out[3 * l + 2] = cext - cabs;
+  }
+  return BDDA_OK;
+}
+
 }  // extern "C"

@@ -64,7 +64,7 @@ __device__ __forceinline__ bool skip(const int* done) { return done && *(volatil
 // One CTA per listed (y, z-tile): warp w owns z = z0 + w; loops over fields.
 template <typename T, class Line>
 __global__ void __launch_bounds__(kTileThreads)
-k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, const int* __restrict__ occ,
+k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int fc, const int* __restrict__ occ,
          const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, Line lay,
          const typename cplx<T>::type* __restrict__ twx, typename cplx<T>::type* __restrict__ t1, const int* done) {
   using C = typename cplx<T>::type;
@@ -89,7 +89,7 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, cons
     const C* xc = x + (size_t)l * ldx + c;
     for (int xi = lane; xi < nx; xi += 32) {
       const int m = socc[xi * kTZ + warp];
-      line[lay.addr(xi)] = m >= 0 ? xc[3 * (size_t)m] : czero<C>();
+      line[lay.addr(xi)] = m >= 0 ? xc[fc * (size_t)m] : czero<C>();
     }
     __syncwarp();
     lay.template fft<false>(line, twx, lane, nx);
@@ -100,7 +100,7 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, cons
       const int w = idx & 7, q = idx >> 3;
       if (z0 + w < nz) out[(size_t)q * rowstride + w] = lb[w * lw + lay.addr(q)];
     }
-    if (++c == 3) { c = 0; ++l; }
+    if (++c == fc) { c = 0; ++l; }
   }
 }
 
@@ -175,7 +175,7 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
 // tile prefetched by cp.async; scatters the occupied sites.
 template <typename T, class Line>
 __global__ void __launch_bounds__(kTileThreads)
-k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, const int* __restrict__ occ,
+k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, const int* __restrict__ occ,
          const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, Line lay,
          const typename cplx<T>::type* __restrict__ twx, const typename cplx<T>::type* __restrict__ x, int ldx,
          const typename cplx<T>::type* __restrict__ diag, const typename cplx<T>::type* __restrict__ jpre,
@@ -221,14 +221,14 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, const int* _
     for (int xi = lane; xi < nx; xi += 32) {
       const int m = socc[xi * kTZ + warp];
       if (m < 0) continue;
-      const size_t r = 3 * (size_t)m + c;
+      const size_t r = fc * (size_t)m + c;
       C v = line[lay.addr(xi)];
       if (diag != nullptr) v = cadd(v, cmul(diag[r], x[(size_t)l * ldx + r]));
       if (jpre != nullptr) v = cmul(v, jpre[r]);
       y[(size_t)l * ldy + r] = v;
     }
     __syncthreads();  // buffer 'buf' is the cp.async target of field f + 2
-    if (++c == 3) { c = 0; ++l; }
+    if (++c == fc) { c = 0; ++l; }
   }
 }
 

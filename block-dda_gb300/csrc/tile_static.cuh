@@ -33,7 +33,7 @@ cudaError_t launch(int pass, const TileArgs& a) {
     case kTileA:
       if ((e = set_smem(tile::k_pass_a<float, L>, smem_ae, oa, ca)) != cudaSuccess) return e;
       tile::k_pass_a<float, L><<<g.ntiles, kTileThreads, tile::smem_tile<float>(P::LW, g.nx), a.st>>>(
-          a.x, a.ldx, a.nfield, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, L{}, a.twx, a.t1, a.done);
+          a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, L{}, a.twx, a.t1, a.done);
       break;
     case kTileB:
       if ((e = set_smem(tile::k_pass_y<float, false, L>, smem_bd, ob, cb)) != cudaSuccess) return e;
@@ -48,7 +48,7 @@ cudaError_t launch(int pass, const TileArgs& a) {
     default:
       if ((e = set_smem(tile::k_pass_e<float, L>, smem_ae, oe, ce)) != cudaSuccess) return e;
       tile::k_pass_e<float, L><<<g.ntiles, kTileThreads, tile::smem_tile<float>(P::LW, g.nx), a.st>>>(
-          a.t1, a.nfield, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, L{}, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
+          a.t1, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, L{}, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
           a.done);
       break;
   }

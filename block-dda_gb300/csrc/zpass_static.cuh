@@ -1,8 +1,9 @@
 // Fused z pass (pass C) for complex FP32 with a compile-time z plan.
 //
 // Same work as the runtime-plan k_pass_c: one warp per (x, y, rhs) task runs
-// the pruned forward z transform of the three component lines, the symmetric
-// 3x3 Green product and the inverse transform (output truncated to nz).  The
+// the pruned forward z transform of the 3 (f = 3) or 6 (f = 6) component
+// lines, the Green product (zproduct.cuh) and the inverse transform (output
+// truncated to nz).  The
 // plan (zplans.inc) is a type, so every butterfly element and every line
 // element is addressed as a base plus compile-time offsets (static_fft.cuh).
 // Its radix sequence is the one the host planner gives the z axis, so the
@@ -15,67 +16,80 @@
 
 #include "mvp.hpp"
 #include "static_fft.cuh"
+#include "zproduct.cuh"
 
 namespace bdda {
 namespace zstatic {
 
-template <class P>
+template <class P, bool SIX>
 __global__ void __launch_bounds__(kZWarps * 32)
 k_pass_c_static(float2* __restrict__ t2, int L, int Px, int Py, int nz, const float2* __restrict__ twz,
                 const float2* __restrict__ ghat, const int* done) {
+  constexpr int fc = SIX ? 6 : 3;
   if (done && *(volatile const int*)done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int Pz = P::N;
+  constexpr int Pz = P::N, LW = P::LW;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long task = (long long)blockIdx.x * kZWarps + warp;
+  const long long task = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
   if (task >= (long long)Px * Py * L) return;
   const int l = (int)(task % L);
   const long long line = task / L;  // q * Py + qy
-  float2* s0 = reinterpret_cast<float2*>(smem_raw) + (size_t)warp * 3 * P::LW;
+  float2* s0 = reinterpret_cast<float2*>(smem_raw) + (size_t)warp * fc * LW;
   const size_t fstride = (size_t)Px * Py * nz;  // between fields
-  float2* g0 = t2 + (size_t)(3 * l) * fstride + (size_t)line * nz;
+  float2* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nz;
+  constexpr bool six = SIX;
   for (int z = lane; z < nz; z += 32) {
     const int a = P::addr(z);
     s0[a] = g0[z];
-    s0[P::LW + a] = g0[fstride + z];
-    s0[2 * P::LW + a] = g0[2 * fstride + z];
+    s0[LW + a] = g0[fstride + z];
+    s0[2 * LW + a] = g0[2 * fstride + z];
+    if (six) {
+      s0[3 * LW + a] = g0[3 * fstride + z];
+      s0[4 * LW + a] = g0[4 * fstride + z];
+      s0[5 * LW + a] = g0[5 * fstride + z];
+    }
   }
   __syncwarp();
-  sfft::forward<P, 3>(s0, twz, lane, nz);
-  const float2* gl = ghat + (size_t)line * 6 * Pz;
-  for (int p = lane; p < Pz; p += 32) {
-    const int a = P::addr(p);
-    const float2 a0 = s0[a], a1 = s0[P::LW + a], a2 = s0[2 * P::LW + a];
-    const float2 gxx = ldg_c(gl + p), gxy = ldg_c(gl + Pz + p), gxz = ldg_c(gl + 2 * Pz + p);
-    const float2 gyy = ldg_c(gl + 3 * Pz + p), gyz = ldg_c(gl + 4 * Pz + p), gzz = ldg_c(gl + 5 * Pz + p);
-    s0[a] = cadd(cadd(cmul(gxx, a0), cmul(gxy, a1)), cmul(gxz, a2));
-    s0[P::LW + a] = cadd(cadd(cmul(gxy, a0), cmul(gyy, a1)), cmul(gyz, a2));
-    s0[2 * P::LW + a] = cadd(cadd(cmul(gxz, a0), cmul(gyz, a1)), cmul(gzz, a2));
-  }
+  constexpr int halves = six ? 2 : 1;  // line triples: E, then M
+  for (int h = 0; h < halves; ++h) sfft::forward<P, 3>(s0 + 3 * h * LW, twz, lane, nz);
+  const float2* gl = ghat + (size_t)line * (six ? 9 : 6) * Pz;
+  for (int p = lane; p < Pz; p += 32) z_product(s0, LW, P::addr(p), gl, Pz, p, six);
   __syncwarp();
-  sfft::inverse<P, 3>(s0, twz, lane, nz);
+  for (int h = 0; h < halves; ++h) sfft::inverse<P, 3>(s0 + 3 * h * LW, twz, lane, nz);
   for (int z = lane; z < nz; z += 32) {
     const int a = P::addr(z);
     g0[z] = s0[a];
-    g0[fstride + z] = s0[P::LW + a];
-    g0[2 * fstride + z] = s0[2 * P::LW + a];
+    g0[fstride + z] = s0[LW + a];
+    g0[2 * fstride + z] = s0[2 * LW + a];
+    if (six) {
+      g0[3 * fstride + z] = s0[3 * LW + a];
+      g0[4 * fstride + z] = s0[4 * LW + a];
+      g0[5 * fstride + z] = s0[5 * LW + a];
+    }
   }
+}
+
+template <class P, bool SIX>
+cudaError_t launch_f(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2* ghat, cudaStream_t st,
+                     const int* done) {
+  static std::once_flag once;
+  static cudaError_t cfg = cudaSuccess;
+  std::call_once(once, [] {
+    cfg = cudaFuncSetAttribute(k_pass_c_static<P, SIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, kZSmemMax);
+  });
+  if (cfg != cudaSuccess) return cfg;
+  const int per_warp = (SIX ? 6 : 3) * P::LW * (int)sizeof(float2);
+  const int wpc = z_warps_per_cta(per_warp);
+  const long long ntask = (long long)g.Px * g.Py * L;
+  const unsigned grid = (unsigned)((ntask + wpc - 1) / wpc);
+  k_pass_c_static<P, SIX><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.Px, g.Py, g.nz, twz, ghat, done);
+  return cudaGetLastError();
 }
 
 template <class P>
 cudaError_t launch(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2* ghat, cudaStream_t st,
                    const int* done) {
-  constexpr int smem = kZWarps * 3 * P::LW * (int)sizeof(float2);
-  static std::once_flag once;
-  static cudaError_t cfg = cudaSuccess;
-  std::call_once(once, [] {
-    cfg = cudaFuncSetAttribute(k_pass_c_static<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  });
-  if (cfg != cudaSuccess) return cfg;
-  const long long ntask = (long long)g.Px * g.Py * L;
-  const unsigned grid = (unsigned)((ntask + kZWarps - 1) / kZWarps);
-  k_pass_c_static<P><<<grid, kZWarps * 32, smem, st>>>(t2, L, g.Px, g.Py, g.nz, twz, ghat, done);
-  return cudaGetLastError();
+  return g.f == 6 ? launch_f<P, true>(g, t2, L, twz, ghat, st, done) : launch_f<P, false>(g, t2, L, twz, ghat, st, done);
 }
 
 }  // namespace zstatic

@@ -55,7 +55,9 @@ typedef struct bdda_op bdda_op;
  * projection Au_til, the Green-tensor spectrum on the 2x-padded 5-smooth grid
  * is built on the device and kept in the handle.
  *   n[3]        lattice box (nx, ny, nz), each 1..256
- *   f           3 (electric dipoles, the reference's CED)
+ *   f           3 (electric dipoles, the reference's CED) or 6 (electric and
+ *               magnetic dipoles, its default CEMD mode): rows f*m + c of every
+ *               vector, c < 3 electric, c >= 3 magnetic
  *   lf          lattice spacing (physical length)
  *   k_re, k_im  wavenumber in the medium
  *   prec        any of BDDA_PREC_FP64, BDDA_PREC_FP32, BDDA_PREC_DF64
@@ -90,9 +92,9 @@ int bdda_mbt_fft_mvp(bdda_op* op, const double* p_hat, double* q_hat);
  * (e.g. bl_krylov_mvp_fft/bl_cocg_rq_jacobi_mvp_fft.cpp:43-60).
  *   prec      BDDA_PREC_FP64 (double2 buffers), BDDA_PREC_FP32 (float2 buffers) or
  *             BDDA_PREC_DF64 (buffers of {re_hi, re_lo, im_hi, im_lo} floats)
- *   x, y      3*nocc x L column-major, leading dimensions ldx, ldy (>= 3*nocc)
- *   diag      3*nocc complex or null (off-diagonal part only)
- *   jpre      3*nocc complex or null (no Jacobi scaling)
+ *   x, y      f*nocc x L column-major, leading dimensions ldx, ldy (>= f*nocc)
+ *   diag      f*nocc complex or null (off-diagonal part only)
+ *   jpre      f*nocc complex or null (no Jacobi scaling)
  *   stream    cudaStream_t or null (the operator's stream)
  */
 int bdda_op_mvp_device(bdda_op* op, int prec, const void* x, int ldx, void* y, int ldy, int L,
@@ -146,7 +148,8 @@ void bdda_solve_opts_default(bdda_solve_opts* opts);
  * bl_cocg_rq_mvp_fft, bl_cocg_rq_jacobi_mvp_fft, bl_bicgstab_mvp_fft,
  * bl_bicgstab_jacobi_mvp_fft, bl_bicggr_mvp_fft, bl_bicggr_jacobi_mvp_fft
  * (bl_krylov_mvp_fft/DDA_linear_solvers.hpp:1-6).
- * Device buffers, complex FP64: diag[3*nocc], B (ldb), X (ldx), X is overwritten.
+ * Device buffers, complex FP64: diag[f*nocc], B (ldb), X (ldx), X is overwritten
+ * (f = the operator's 3 or 6 components per dipole).
  */
 int bdda_solve_device(bdda_op* op, const bdda_solve_opts* opts, const double* diag, const double* B, int ldb,
                       double* X, int ldx, int L, bdda_solve_stats* stats, void* stream);
@@ -181,7 +184,7 @@ typedef struct {
   const double* B;      /* 3*nocc x L complex, column-major, ld 3*nocc */
   int L;                /* 1..32 */
   double* X;            /* 3*nocc x L complex output */
-} bdda_request;
+} bdda_request;         /* requests are f = 3 (electric dipoles) */
 
 typedef struct {
   int status;             /* BDDA_OK or the solve's error code */
@@ -250,6 +253,23 @@ int bdda_incident_fields(const int n[3], double lf, const int* address, int nocc
  */
 int bdda_cross_sections(double k, const double alpha0[2], const double* E, int lde, const double* P, int ldp,
                         int nrows, int L, double* out);
+
+/*
+ * Incident fields for f=6 (Target_manager.cpp:280-291): rows 6m..6m+2 =
+ * e_l exp(i k u_l . r_m), rows 6m+3..6m+5 = h_l exp(i k u_l . r_m).  hinc:
+ * L x 3 complex interleaved (the H amplitude of each wave).  ldb >= 6*nocc.
+ */
+int bdda_incident_fields_eh(const int n[3], double lf, const int* address, int nocc, double k, int L,
+                            const double* uinc, const double* einc, const double* hinc, double* B, int ldb);
+
+/*
+ * Cext, Cabs, Csca per column for f=6 (Result_manager.cpp:90-115):
+ * out[3*l + {0,1,2}].  Cext over all 6*nocc rows; Cabs weighs the electric
+ * rows (6m..6m+2) with alpha_E of dipole 0 and the magnetic rows with
+ * alpha_H of dipole 0, as the reference does for every dipole.
+ */
+int bdda_cross_sections_eh(double k, const double alpha_e0[2], const double alpha_h0[2], const double* EH, int lde,
+                           const double* PM, int ldp, int nocc, int L, double* out);
 
 /* ---- instrumentation ------------------------------------------------------ */
 

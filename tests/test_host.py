@@ -175,3 +175,37 @@ def test_cross_sections_match_oracle():
     ref = physics.cross_sections(10.0, E, P, a0)
     for g_, r_ in zip(got, ref):
         assert np.allclose(g_, r_, rtol=1e-13, atol=0)
+
+
+def test_f6_incident_fields_and_cross_sections_match_oracle():
+    t = golden("target_N16_coated.json")
+    n, lf = tuple(t["n"]), t["lf"] * 0.02
+    addr = np.array(t["address"])
+    k = 2 * math.pi / 0.45
+    u, e, h = physics.reference_incident_waves(5)
+    B = bdda.incident_fields(n, lf, addr, k, u, e, h)
+    Bo = physics.incident_fields(physics.positions(n, lf, addr), k, e, u, h)
+    assert B.shape == (6 * addr.size, 5)
+    assert np.max(np.abs(B - Bo)) < 1e-12
+    rng = np.random.default_rng(4)
+    P = rng.standard_normal(B.shape) + 1j * rng.standard_normal(B.shape)
+    ae, ah = 1e-4 + 3e-5j, 2e-6 + 1e-6j
+    got = bdda.cross_sections(k, ae, B, P, ah)
+    ref = physics.cross_sections(k, B, P, ae, ah)
+    for g_, r_ in zip(got, ref):
+        assert np.allclose(g_, r_, rtol=1e-13, atol=0)
+
+
+def test_f6_polarizabilities_match_reference_gmie():
+    g = golden("result_f6_BC_rpp20nm.json")
+    worst = 0.0
+    for c in g["cases"][::5]:
+        t = g["targets"][c["target"]]
+        r_p = (3.0 * t["vol"][0] * g["scale_factor"] ** 3 / (4.0 * math.pi)) ** (1.0 / 3.0)
+        k = 2 * math.pi / c["wl0"]
+        ae, ah = bdda.polarizabilities(c["wl0"], r_p, complex(*c["eper"]), k)
+        for got, ref in ((ae, complex(*c["alpha_e0"])), (ah, complex(*c["alpha_h0"]))):
+            worst = max(worst, abs(got - ref) / abs(ref))
+    assert worst < 1e-9, worst
+    d = bdda.diag_a([2.0, 4.0j], [0.5, 1.0])
+    assert np.allclose(d, [0.5] * 3 + [2.0] * 3 + [-0.25j] * 3 + [1.0] * 3)
