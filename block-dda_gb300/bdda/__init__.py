@@ -36,8 +36,12 @@ EXPORTS = [
     "bdda_op_kernel_stats", "bdda_last_error", "bdda_op_mvp_bytes", "bdda_host_fft_line",
     "bdda_op_mvp_device_noalloc", "bdda_request_footprint", "bdda_server_create", "bdda_server_submit",
     "bdda_server_wait", "bdda_server_stats", "bdda_server_destroy", "bdda_batch_solve",
-    "bdda_incident_fields_eh", "bdda_cross_sections_eh",
+    "bdda_incident_fields_eh", "bdda_cross_sections_eh", "bdda_read_target_file", "bdda_shape_target",
+    "bdda_material_load", "bdda_material_constant", "bdda_material_eval", "bdda_material_destroy",
+    "bdda_polarizabilities", "bdda_diag_a",
 ]
+
+SHAPES = {"sphere": 0, "cube": 1, "ellipsoid": 2, "cuboid": 3, "cylinder": 4, "rounded_cylinder": 5}
 
 
 class BddaError(RuntimeError):
@@ -112,6 +116,14 @@ def lib(build_if_missing: bool = False):
     L.bdda_incident_fields_eh.argtypes = [ip, ct.c_double, ip, ct.c_int, ct.c_double, ct.c_int, dp, dp, dp, dp,
                                           ct.c_int]
     L.bdda_cross_sections_eh.argtypes = [ct.c_double, dp, dp, dp, ct.c_int, dp, ct.c_int, ct.c_int, ct.c_int, dp]
+    L.bdda_read_target_file.argtypes = [ct.c_char_p, ct.c_double, ip, dp, ip, ct.c_int, ip, dp, ip]
+    L.bdda_shape_target.argtypes = [ct.c_int, ct.c_int, dp, ip, dp, ip, ct.c_int, ip]
+    L.bdda_material_load.argtypes = [ct.c_char_p, ct.c_double, ct.POINTER(vp)]
+    L.bdda_material_constant.argtypes = [dp, dp, ct.c_double, ct.POINTER(vp)]
+    L.bdda_material_eval.argtypes = [vp, ct.c_double, dp, dp, dp]
+    L.bdda_material_destroy.argtypes = [vp]
+    L.bdda_polarizabilities.argtypes = [ct.c_double, ct.c_int, dp, ip, ct.POINTER(vp), ct.c_int, dp, dp, ip]
+    L.bdda_diag_a.argtypes = [ct.c_int, ct.c_int, dp, dp, dp]
     L.bdda_op_mvp_bytes.argtypes = [vp, ct.c_int, ct.c_int, ct.c_int, ct.c_int, dp]
     L.bdda_op_set_timing.argtypes = [vp, ct.c_int]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
@@ -308,13 +320,104 @@ def polarizabilities(wl0, r_p, eps_p, k, mu_p=1 + 0j):
 
 
 def diag_a(alpha_e, alpha_h=None):
-    """DIAG_A per row: 1/alpha_E over rows 3m..3m+2 (f=3, Solver.cpp:33-36), or
-    1/alpha_E then 1/alpha_H over rows 6m..6m+5 (f=6, Solver.cpp:40-45)."""
-    ae = 1.0 / np.asarray(alpha_e, dtype=np.complex128).reshape(-1)
-    if alpha_h is None:
-        return np.repeat(ae, 3)
-    ah = 1.0 / np.asarray(alpha_h, dtype=np.complex128).reshape(-1)
-    return np.concatenate([np.repeat(ae[:, None], 3, 1), np.repeat(ah[:, None], 3, 1)], axis=1).reshape(-1)
+    """DIAG_A per row (``bdda_diag_a``): 1/alpha_E over rows 3m..3m+2 (f=3,
+    Solver.cpp:33-36), or 1/alpha_E then 1/alpha_H over rows 6m..6m+5 (f=6,
+    Solver.cpp:40-45)."""
+    ae = np.ascontiguousarray(np.asarray(alpha_e, dtype=np.complex128).reshape(-1))
+    f = 3 if alpha_h is None else 6
+    ah = None if alpha_h is None else np.ascontiguousarray(np.asarray(alpha_h, dtype=np.complex128).reshape(-1))
+    d = np.zeros(f * ae.size, dtype=np.complex128)
+    _check(lib().bdda_diag_a(f, int(ae.size), _dptr(ae), _dptr(ah) if ah is not None else None, _dptr(d)))
+    return d
+
+
+def read_target_file(path, scale_factor=1.0):
+    """Target file ``DDA_target_*.out`` -> (n, lf, address, vol, material) (``bdda_read_target_file``)."""
+    n = np.zeros(3, np.int32)
+    lf, nocc = ct.c_double(), ct.c_int()
+    bp = os.fsencode(path)
+    _check(lib().bdda_read_target_file(bp, float(scale_factor), _iptr(n), ct.byref(lf), ct.byref(nocc), 0,
+                                       None, None, None))
+    m = nocc.value
+    addr, vol, mat = np.zeros(m, np.int32), np.zeros(m), np.zeros(m, np.int32)
+    _check(lib().bdda_read_target_file(bp, float(scale_factor), _iptr(n), ct.byref(lf), ct.byref(nocc), m,
+                                       _iptr(addr), _dptr(vol), _iptr(mat)))
+    return tuple(int(v) for v in n), lf.value, addr, vol, mat
+
+
+def shape_target(shape, nmax, side_lengths):
+    """Lattice sites of a shape (``bdda_shape_target``) -> (n, lf, address); element volume lf^3."""
+    code = SHAPES[shape] if isinstance(shape, str) else int(shape)
+    s3 = np.ascontiguousarray(side_lengths, dtype=np.float64)
+    n = np.zeros(3, np.int32)
+    lf, nocc = ct.c_double(), ct.c_int()
+    _check(lib().bdda_shape_target(code, int(nmax), _dptr(s3), _iptr(n), ct.byref(lf), ct.byref(nocc), 0, None))
+    addr = np.zeros(nocc.value, np.int32)
+    _check(lib().bdda_shape_target(code, int(nmax), _dptr(s3), _iptr(n), ct.byref(lf), ct.byref(nocc), nocc.value,
+                                   _iptr(addr)))
+    return tuple(int(v) for v in n), lf.value, addr
+
+
+class Material:
+    """Material table or constant (``bdda_material``)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def load(cls, path, density):
+        h = ct.c_void_p()
+        _check(lib().bdda_material_load(os.fsencode(path), float(density), ct.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def constant(cls, eper, mper=1 + 0j, density=0.0):
+        h = ct.c_void_p()
+        e = np.array([complex(eper).real, complex(eper).imag])
+        m = np.array([complex(mper).real, complex(mper).imag])
+        _check(lib().bdda_material_constant(_dptr(e), _dptr(m), float(density), ct.byref(h)))
+        return cls(h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __call__(self, wl0):
+        """(eper, mper) at the free-space wavelength wl0."""
+        e, m, d = np.zeros(2), np.zeros(2), ct.c_double()
+        _check(lib().bdda_material_eval(self._h, float(wl0), _dptr(e), _dptr(m), ct.byref(d)))
+        return complex(e[0], e[1]), complex(m[0], m[1])
+
+    @property
+    def density(self):
+        d = ct.c_double()
+        _check(lib().bdda_material_eval(self._h, 0.0, None, None, ct.byref(d)))
+        return d.value
+
+    def close(self):
+        if self._h:
+            lib().bdda_material_destroy(self._h)
+            self._h = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def dipole_polarizabilities(wl0, vol, materials, material_index=None):
+    """(alpha_E, alpha_H, Mie evaluations) of every dipole in vacuum (``bdda_polarizabilities``)."""
+    v = np.ascontiguousarray(vol, dtype=np.float64)
+    mi = None if material_index is None else np.ascontiguousarray(material_index, dtype=np.int32)
+    hs = (ct.c_void_p * len(materials))(*[m.handle.value for m in materials])
+    ae = np.zeros(v.size, np.complex128)
+    ah = np.zeros(v.size, np.complex128)
+    nev = ct.c_int()
+    _check(lib().bdda_polarizabilities(float(wl0), int(v.size), _dptr(v), _iptr(mi) if mi is not None else None,
+                                       ct.cast(hs, ct.POINTER(ct.c_void_p)), len(materials), _dptr(ae), _dptr(ah),
+                                       ct.byref(nev)))
+    return ae, ah, nev.value
 
 
 def aggregate(nocc, kf=1.0, Df=2.8, seed=1):

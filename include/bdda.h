@@ -271,6 +271,64 @@ int bdda_incident_fields_eh(const int n[3], double lf, const int* address, int n
 int bdda_cross_sections_eh(double k, const double alpha_e0[2], const double alpha_h0[2], const double* EH, int lde,
                            const double* PM, int ldp, int nocc, int L, double* out);
 
+/* ---- target ingestion ------------------------------------------------------ */
+
+/*
+ * Read a target file DDA_target_*.out (Target_manager.cpp:114-202): header
+ * lines pp radius, aggregate volume, coating volume, "nx ny nz", lf; then rows
+ * "address vol material_index" (index 0 or 1).  lf and vol are multiplied by
+ * scale_factor and scale_factor^3 (:157,172).  *nocc receives the row count;
+ * address, vol, material (each may be null) receive up to capacity rows.
+ * Call with capacity 0 to size the arrays; capacity > 0 and smaller than the
+ * row count is an error.  Blank and '#' lines are skipped.
+ */
+int bdda_read_target_file(const char* path, double scale_factor, int n[3], double* lf, int* nocc, int capacity,
+                          int* address, double* vol, int* material);
+
+/* Shapes of Target_manager::is_in_target_volume (Shape_Name.hpp). */
+#define BDDA_SHAPE_SPHERE 0
+#define BDDA_SHAPE_CUBE 1
+#define BDDA_SHAPE_ELLIPSOID 2
+#define BDDA_SHAPE_CUBOID 3
+#define BDDA_SHAPE_CYLINDER 4
+#define BDDA_SHAPE_ROUNDED_CYLINDER 5  /* as the reference: only the lower cap is rounded */
+
+/*
+ * Shape target (Target_manager.cpp:84-112): lf = max side / nmax, n_i =
+ * ceil(nmax side_i / max side), every site (ix, iy, iz) lf inside the shape is
+ * occupied (element volume lf^3).  Sizing as bdda_read_target_file.
+ */
+int bdda_shape_target(int shape, int nmax, const double side_lengths[3], int n[3], double* lf, int* nocc,
+                      int capacity, int* address);
+
+/*
+ * Materials (Material.cpp:10-124): a table file (rows "wl0 (re,im) (re,im)"
+ * of eper and mper against ascending free-space wavelength, '##' comments)
+ * interpolated linearly in wl0, or a constant.  Evaluating outside the table
+ * is an error (the reference exits).  bdda_material_eval with eper and mper
+ * both null returns only the density (g/cm^3, may be null).
+ */
+typedef struct bdda_material bdda_material;
+int bdda_material_load(const char* path, double density, bdda_material** out);
+int bdda_material_constant(const double eper[2], const double mper[2], double density, bdda_material** out);
+int bdda_material_eval(const bdda_material* m, double wl0, double eper[2], double mper[2], double* density);
+int bdda_material_destroy(bdda_material* m);
+
+/*
+ * alpha_E (and alpha_H if not null) of every dipole in vacuum
+ * (Target_manager.cpp:215-260): 3 i a1 / (2 k^3), 3 i b1 / (2 k^3), k = 2 pi /
+ * wl0, Mie a1, b1 of the volume-equivalent sphere (Target.cpp:13-19) of the
+ * dipole's element volume and material mats[material[i]] (material may be
+ * null: all 0).  The Mie coefficients are computed once per distinct
+ * (volume, material); *mie_evaluations (may be null) receives that count.
+ */
+int bdda_polarizabilities(double wl0, int nocc, const double* vol, const int* material,
+                          const bdda_material* const* mats, int nmat, double* alpha_e, double* alpha_h,
+                          int* mie_evaluations);
+
+/* DIAG_A (Solver.cpp:28-56): 1/alpha_E on rows f*m + 0..2, 1/alpha_H on rows 6m + 3..5 (f = 6). */
+int bdda_diag_a(int f, int nocc, const double* alpha_e, const double* alpha_h, double* diag);
+
 /* ---- instrumentation ------------------------------------------------------ */
 
 /*

@@ -148,3 +148,62 @@ def cross_sections(k: float, ehinc, pm, alpha0, alpha_h0=None):
         p6 = np.abs(pm.reshape(-1, 6, pm.shape[1])) ** 2
         cabs = 4 * math.pi * k * (we * p6[:, :3].sum(axis=(0, 1)) + wh * p6[:, 3:].sum(axis=(0, 1)))
     return cext, cabs, cext - cabs
+
+
+# --------------------------------------------------------------------------
+# materials and shape targets
+# --------------------------------------------------------------------------
+
+def material_eval(rows, wl0):
+    """Linear interpolation of a material table in free-space wavelength,
+    ``Material.cpp:88-124`` (same operation order): rows = [(wl0, eper, mper)]
+    ascending; outside the table raises."""
+    w = [r[0] for r in rows]
+    if not (w[0] <= wl0 <= w[-1]):
+        raise ValueError("wavelength outside the material table")
+    for i in range(len(rows) - 1):
+        if w[i] <= wl0 <= w[i + 1]:
+            e0, e1 = complex(*rows[i][1]), complex(*rows[i + 1][1])
+            m0, m1 = complex(*rows[i][2]), complex(*rows[i + 1][2])
+            d = w[i + 1] - w[i]
+            return e0 + (e1 - e0) / d * (wl0 - w[i]), m0 + (m1 - m0) / d * (wl0 - w[i])
+    return complex(*rows[0][1]), complex(*rows[0][2])
+
+
+def in_shape(shape, x, y, z, s):
+    """``Target_manager::is_in_target_volume`` (``Target_manager.cpp:8-82``);
+    shape 0 sphere, 1 cube, 2 ellipsoid, 3 cuboid, 4 cylinder, 5 rounded
+    cylinder (whose second test ``r < z || z < l - r`` is always true above
+    the lower cap, so the upper cap stays flat)."""
+    if shape == 0:
+        r = s[0] / 2.0
+        return math.sqrt((x - r) ** 2 + (y - r) ** 2 + (z - r) ** 2) <= r
+    if shape in (1, 3):
+        return x <= s[0] and y <= s[1] and z <= s[2]
+    if shape == 2:
+        a, b, c = s[0] / 2.0, s[1] / 2.0, s[2] / 2.0
+        return (x - a) * (x - a) / (a * a) + (y - b) * (y - b) / (b * b) + (z - c) * (z - c) / (c * c) <= 1.0
+    r = s[0] / 2.0
+    if shape == 4:
+        return math.sqrt((x - r) ** 2 + (y - r) ** 2) <= r and z <= s[2]
+    l = s[2]
+    if z <= r:
+        return math.sqrt((x - r) ** 2 + (y - r) ** 2 + (z - r) ** 2) <= r
+    if r < z or z < l - r:
+        return math.sqrt((x - r) ** 2 + (y - r) ** 2) <= r
+    return math.sqrt((x - r) ** 2 + (y - r) ** 2 + (z - (l - r)) ** 2) <= r
+
+
+def shape_target(shape, nmax, side_lengths):
+    """``Target_manager::add_to_target_queue`` for a shape (``:84-112``):
+    returns n, lf, occupied addresses."""
+    mx = max(side_lengths)
+    lf = mx / nmax
+    n = [int(math.ceil(nmax * (s / mx))) for s in side_lengths]
+    addr = []
+    for ix in range(n[0]):
+        for iy in range(n[1]):
+            for iz in range(n[2]):
+                if in_shape(shape, lf * ix, lf * iy, lf * iz, side_lengths):
+                    addr.append(n[1] * n[2] * ix + n[2] * iy + iz)
+    return tuple(n), lf, np.array(addr, dtype=np.int64)

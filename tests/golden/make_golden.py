@@ -24,6 +24,8 @@ Fixtures:
   BiCGSTAB-Jacobi runs of ``DDA_result_BC_rpp20nm.dat`` for the N8..N64
   targets at eleven wavelengths, their target files, and the oracle's
   reproduction of each.
+* ``materials_ref.json`` -- the four material tables and the eper the recorded
+  runs used at each wavelength (interpolation pins).
 """
 from __future__ import annotations
 
@@ -210,6 +212,34 @@ def result_f6(ref, lib):
             "targets": targets, "cases": cases}
 
 
+def materials_ref(ref):
+    """The reference's material tables (``material_*.dat``, data files read as
+    text) with the densities ``Material.cpp:31-57`` gives them, and the eper the
+    recorded runs used at each wavelength (``DDA_result_BC_rpp20nm.dat``,
+    ``DDA_result_MAGNETITE_rpp40nm.dat``): interpolation pins, e.g. magnetite
+    at 0.3 um lies between the table rows 0.294118 and 0.303030."""
+    dens = {"water": 1.0, "ice": 0.917, "bc": 1.8, "magnetite": 5.17}
+    tables = {}
+    for name in dens:
+        rows = []
+        for line in open(os.path.join(ref, f"material_{name}.dat")).read().splitlines():
+            tok = line.split()
+            if not tok or tok[0] == "##":
+                continue
+            e = [float(v) for v in tok[1].strip("()").split(",")]
+            m = [float(v) for v in tok[2].strip("()").split(",")]
+            rows.append([float(tok[0]), e, m])
+        tables[name] = {"density": dens[name], "rows": rows}
+    pins = {}
+    for name, fn in (("bc", "DDA_result_BC_rpp20nm.dat"), ("magnetite", "DDA_result_MAGNETITE_rpp40nm.dat")):
+        seen = {}
+        for r in _dat_sections(os.path.join(ref, fn)):
+            if "eper_particle" in r:  # homogeneous targets
+                seen[float(r["wl0"])] = [float(v) for v in r["eper_particle"].strip("()").split(",")]
+        pins[name] = sorted([w, e] for w, e in seen.items())
+    return {"tables": tables, "recorded_eper": pins}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -225,6 +255,7 @@ def main():
         "target_N16_coated.json": lambda: target_fixture(ref, "DDA_target_2_agg_N16_kf1.0_Df2.8.out", 0.02),
         "result_dat_N512.json": lambda: result_dat(ref, lib),
         "result_f6_BC_rpp20nm.json": lambda: result_f6(ref, lib),
+        "materials_ref.json": lambda: materials_ref(ref),
     }
     out = {name: make() for name, make in makers.items() if not args.only or name in args.only}
     for name, obj in out.items():
