@@ -38,7 +38,8 @@ EXPORTS = [
     "bdda_server_wait", "bdda_server_stats", "bdda_server_destroy", "bdda_batch_solve",
     "bdda_incident_fields_eh", "bdda_cross_sections_eh", "bdda_read_target_file", "bdda_shape_target",
     "bdda_material_load", "bdda_material_constant", "bdda_material_eval", "bdda_material_destroy",
-    "bdda_polarizabilities", "bdda_diag_a",
+    "bdda_polarizabilities", "bdda_diag_a", "bdda_op_set_wavenumber", "bdda_sweep", "bdda_mie_q",
+    "bdda_format_result",
 ]
 
 SHAPES = {"sphere": 0, "cube": 1, "ellipsoid": 2, "cuboid": 3, "cylinder": 4, "rounded_cylinder": 5}
@@ -53,7 +54,43 @@ class BddaError(RuntimeError):
 class SolveOpts(ct.Structure):
     _fields_ = [("solver", ct.c_int), ("jacobi", ct.c_int), ("precision", ct.c_int), ("tol", ct.c_double),
                 ("itermax", ct.c_int), ("true_tol", ct.c_double), ("inner_tol", ct.c_double),
-                ("max_refine", ct.c_int), ("check_every", ct.c_int)]
+                ("max_refine", ct.c_int), ("check_every", ct.c_int), ("warm_start", ct.c_int)]
+
+
+class SweepTarget(ct.Structure):
+    _fields_ = [("n", ct.c_int * 3), ("lf", ct.c_double), ("nocc", ct.c_int), ("address", ct.POINTER(ct.c_int)),
+                ("vol", ct.POINTER(ct.c_double)), ("material", ct.POINTER(ct.c_int))]
+
+
+class SweepSpec(ct.Structure):
+    _fields_ = [("f", ct.c_int), ("n_wl", ct.c_int), ("wl0", ct.POINTER(ct.c_double)), ("n_targets", ct.c_int),
+                ("targets", ct.POINTER(SweepTarget)), ("nmat", ct.c_int), ("materials", ct.POINTER(ct.c_void_p)),
+                ("L", ct.c_int), ("uinc", ct.POINTER(ct.c_double)), ("einc", ct.POINTER(ct.c_double)),
+                ("hinc", ct.POINTER(ct.c_double)), ("opts", SolveOpts), ("warm_start", ct.c_int), ("prec", ct.c_int)]
+
+
+class SweepResult(ct.Structure):
+    _fields_ = [("status", ct.c_int), ("iterations", ct.c_int), ("refinements", ct.c_int),
+                ("mie_evaluations", ct.c_int), ("true_res_max", ct.c_double), ("final_err", ct.c_double),
+                ("ms_solve", ct.c_double), ("alpha_e0", ct.c_double * 2), ("alpha_h0", ct.c_double * 2)]
+
+    def as_dict(self):
+        return {"status": self.status, "iterations": self.iterations, "refinements": self.refinements,
+                "mie_evaluations": self.mie_evaluations, "true_res_max": self.true_res_max,
+                "final_err": self.final_err, "ms_solve": self.ms_solve,
+                "alpha_e0": complex(self.alpha_e0[0], self.alpha_e0[1]),
+                "alpha_h0": complex(self.alpha_h0[0], self.alpha_h0[1])}
+
+
+class ResultRecord(ct.Structure):
+    _fields_ = [("wl0_index", ct.c_int), ("target_index", ct.c_int), ("wl0", ct.c_double), ("N_inc", ct.c_int),
+                ("eper_medium", ct.c_double * 2), ("mper_medium", ct.c_double * 2), ("target_fname", ct.c_char_p),
+                ("is_homogeneous", ct.c_int), ("eper_core", ct.c_double * 2), ("mper_core", ct.c_double * 2),
+                ("volume_core", ct.c_double), ("density_core", ct.c_double), ("eper_coat", ct.c_double * 2),
+                ("mper_coat", ct.c_double * 2), ("volume_coat", ct.c_double), ("L", ct.c_int),
+                ("cext", ct.POINTER(ct.c_double)), ("cabs", ct.POINTER(ct.c_double)), ("f", ct.c_int),
+                ("nx", ct.c_int), ("ny", ct.c_int), ("nz", ct.c_int), ("num_element_occupy", ct.c_int),
+                ("solver_time", ct.c_double), ("append_mac_mie", ct.c_int)]
 
 
 class Request(ct.Structure):
@@ -97,6 +134,7 @@ def lib(build_if_missing: bool = False):
     vp, ip, dp = ct.c_void_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_double)
     L.bdda_op_create.argtypes = [ct.POINTER(vp), ip, ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_int]
     L.bdda_op_destroy.argtypes = [vp]
+    L.bdda_op_set_wavenumber.argtypes = [vp, ct.c_double, ct.c_double]
     L.bdda_op_set_dipoles.argtypes = [vp, ip, ct.c_int]
     L.bdda_op_info.argtypes = [vp, ip, ip, ip]
     L.bdda_mbt_fft_mvp.argtypes = [vp, dp, dp]
@@ -124,6 +162,9 @@ def lib(build_if_missing: bool = False):
     L.bdda_material_destroy.argtypes = [vp]
     L.bdda_polarizabilities.argtypes = [ct.c_double, ct.c_int, dp, ip, ct.POINTER(vp), ct.c_int, dp, dp, ip]
     L.bdda_diag_a.argtypes = [ct.c_int, ct.c_int, dp, dp, dp]
+    L.bdda_sweep.argtypes = [ct.POINTER(SweepSpec), dp, ct.POINTER(SweepResult)]
+    L.bdda_mie_q.argtypes = [ct.c_double, ct.c_double, dp, dp, dp, dp, dp]
+    L.bdda_format_result.argtypes = [ct.POINTER(ResultRecord), ct.c_char_p, ct.c_int, ip]
     L.bdda_op_mvp_bytes.argtypes = [vp, ct.c_int, ct.c_int, ct.c_int, ct.c_int, dp]
     L.bdda_op_set_timing.argtypes = [vp, ct.c_int]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
@@ -197,6 +238,12 @@ class Operator:
         except Exception:
             pass
 
+    def set_wavenumber(self, k):
+        """New wavenumber (next wavelength): rebuilds the Green spectra only."""
+        k = complex(k)
+        _check(lib().bdda_op_set_wavenumber(self._h, k.real, k.imag))
+        self.k = k
+
     def set_dipoles(self, address):
         a = np.ascontiguousarray(address, dtype=np.int32)
         _check(lib().bdda_op_set_dipoles(self._h, _iptr(a), int(a.size)))
@@ -247,7 +294,7 @@ class Operator:
 
 
 def solve_opts(solver="cocg_rq", jacobi=True, precision=SOLVE_FP64, tol=1e-2, itermax=300, true_tol=0.0,
-               inner_tol=0.0, max_refine=8, check_every=4) -> SolveOpts:
+               inner_tol=0.0, max_refine=8, check_every=4, warm_start=False) -> SolveOpts:
     o = SolveOpts()
     lib().bdda_solve_opts_default(ct.byref(o))
     o.solver = SOLVERS[solver] if isinstance(solver, str) else int(solver)
@@ -259,15 +306,18 @@ def solve_opts(solver="cocg_rq", jacobi=True, precision=SOLVE_FP64, tol=1e-2, it
     o.inner_tol = float(inner_tol)
     o.max_refine = int(max_refine)
     o.check_every = int(check_every)
+    o.warm_start = 1 if warm_start else 0
     return o
 
 
-def solve(op: Operator, diag, B, opts: SolveOpts, allow_not_converged=True):
-    """Host-buffer solve (``bdda_solve``).  Returns (X, stats dict)."""
+def solve(op: Operator, diag, B, opts: SolveOpts, allow_not_converged=True, X0=None):
+    """Host-buffer solve (``bdda_solve``).  Returns (X, stats dict).  X0: initial
+    guess for a warm-started refinement (``opts.warm_start``)."""
     d = np.ascontiguousarray(diag, dtype=np.complex128)
     Bm = _cmat(B)
     n, L = Bm.shape
-    X = np.zeros((n, L), dtype=np.complex128, order="F")
+    X = np.zeros((n, L), dtype=np.complex128, order="F") if X0 is None else np.array(X0, dtype=np.complex128,
+                                                                                      order="F")
     st = SolveStats()
     allow = (ERR_NOT_CONVERGED,) if allow_not_converged else ()
     _check(lib().bdda_solve(op.handle, ct.byref(opts), _dptr(d), _dptr(Bm), n,
@@ -636,3 +686,88 @@ def random_problem(rng, n_range=(64, 8192), wl_range=(0.55, 0.55), L_choices=(2,
     if prob.B.shape[1] != L:
         prob.B = np.asfortranarray(prob.B[:, :L])
     return prob
+
+
+def sweep(wl0_list, targets, materials, uinc, einc, hinc=None, opts=None, warm_start=False, f=None, prec=0):
+    """Wavelength x target sweep (``bdda_sweep``).
+
+    targets: list of (n, lf, address, vol, material_index or None); materials:
+    list of :class:`Material`.  f = 6 when ``hinc`` is given, else 3.  Returns
+    (cross, results): cross[w, t, l] = (Cext, Cabs, Csca), results[w][t] dicts.
+    """
+    f = f or (6 if hinc is not None else 3)
+    keep = []
+
+    def arr(a, dt):
+        v = np.ascontiguousarray(a, dtype=dt)
+        keep.append(v)
+        return v
+    wl = arr(wl0_list, np.float64)
+    tg = (SweepTarget * len(targets))()
+    for i, (n, lf, address, vol, mat) in enumerate(targets):
+        a = arr(address, np.int32)
+        tg[i].n[:] = [int(v) for v in n]
+        tg[i].lf = float(lf)
+        tg[i].nocc = int(a.size)
+        tg[i].address = _iptr(a)
+        tg[i].vol = _dptr(arr(vol, np.float64))
+        tg[i].material = _iptr(arr(mat, np.int32)) if mat is not None else None
+    mh = (ct.c_void_p * len(materials))(*[m.handle.value for m in materials])
+    u = arr(np.reshape(uinc, (-1, 3)), np.float64)
+    e = arr(np.reshape(einc, (-1, 3)), np.complex128)
+    spec = SweepSpec()
+    spec.f, spec.n_wl, spec.wl0 = f, int(wl.size), _dptr(wl)
+    spec.n_targets, spec.targets = len(targets), ct.cast(tg, ct.POINTER(SweepTarget))
+    spec.nmat, spec.materials = len(materials), ct.cast(mh, ct.POINTER(ct.c_void_p))
+    spec.L, spec.uinc, spec.einc = int(u.shape[0]), _dptr(u), _dptr(e)
+    spec.hinc = _dptr(arr(np.reshape(hinc, (-1, 3)), np.complex128)) if hinc is not None else None
+    spec.opts = opts if opts is not None else solve_opts()
+    spec.warm_start = 1 if warm_start else 0
+    spec.prec = int(prec)
+    cross = np.zeros((wl.size, len(targets), spec.L, 3))
+    res = (SweepResult * (wl.size * len(targets)))()
+    rc = lib().bdda_sweep(ct.byref(spec), _dptr(cross), ct.cast(res, ct.POINTER(SweepResult)))
+    _check(rc, (ERR_NOT_CONVERGED,))
+    out = [[res[w * len(targets) + t].as_dict() for t in range(len(targets))] for w in range(wl.size)]
+    return cross, out
+
+
+def mie_q(wl0, r_p, eps_p, mu_p=1 + 0j, eps_m=1 + 0j, mu_m=1 + 0j):
+    """(Qsca, Qabs, Qext) of a sphere (``bdda_mie_q``)."""
+    vals = [np.array([complex(v).real, complex(v).imag]) for v in (eps_p, mu_p, eps_m, mu_m)]
+    q = np.zeros(3)
+    _check(lib().bdda_mie_q(float(wl0), float(r_p), *[_dptr(v) for v in vals], _dptr(q)))
+    return tuple(float(v) for v in q)
+
+
+def format_result(wl0, cext, cabs, eper, volume, density, n, nocc, f, target_fname="", N_inc=None, wl0_index=0,
+                  target_index=0, mper=1 + 0j, eper_medium=1 + 0j, mper_medium=1 + 0j, coat=None, solver_time=0.0,
+                  mac_mie=True):
+    """One result section of the reference's DDA_result.dat (``bdda_format_result``).
+
+    eper / mper / volume / density are the particle's (or the core's when
+    ``coat`` = (eper, mper, volume) is given)."""
+    ce = np.ascontiguousarray(cext, dtype=np.float64)
+    ca = np.ascontiguousarray(cabs, dtype=np.float64)
+    r = ResultRecord()
+    r.wl0_index, r.target_index, r.wl0 = int(wl0_index), int(target_index), float(wl0)
+    r.N_inc = int(N_inc if N_inc is not None else ce.size)
+    r.eper_medium[:] = [complex(eper_medium).real, complex(eper_medium).imag]
+    r.mper_medium[:] = [complex(mper_medium).real, complex(mper_medium).imag]
+    r.target_fname = target_fname.encode()
+    r.is_homogeneous = 1 if coat is None else 0
+    r.eper_core[:] = [complex(eper).real, complex(eper).imag]
+    r.mper_core[:] = [complex(mper).real, complex(mper).imag]
+    r.volume_core, r.density_core = float(volume), float(density)
+    if coat is not None:
+        r.eper_coat[:] = [complex(coat[0]).real, complex(coat[0]).imag]
+        r.mper_coat[:] = [complex(coat[1]).real, complex(coat[1]).imag]
+        r.volume_coat = float(coat[2])
+    r.L, r.cext, r.cabs = int(ce.size), _dptr(ce), _dptr(ca)
+    r.f, (r.nx, r.ny, r.nz), r.num_element_occupy = int(f), [int(v) for v in n], int(nocc)
+    r.solver_time, r.append_mac_mie = float(solver_time), 1 if mac_mie else 0
+    ln = ct.c_int()
+    _check(lib().bdda_format_result(ct.byref(r), None, 0, ct.byref(ln)))
+    buf = ct.create_string_buffer(ln.value + 1)
+    _check(lib().bdda_format_result(ct.byref(r), buf, ln.value + 1, ct.byref(ln)))
+    return buf.value.decode()

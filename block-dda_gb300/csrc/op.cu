@@ -170,6 +170,38 @@ template int op_block_mvp<dfl>(Op*, const Occupancy&, const dfc*, int, dfc*, int
 
 using namespace bdda;
 
+// Green spectra of the operator's box, spacing and f at wavenumber k (FP64
+// evaluation and transform; packed for every precision the operator holds).
+static int build_spectrum(Op* op, double k_re, double k_im) {
+  const int f = op->f, prec = op->prec;
+  const double lf = op->lf;
+  const int Px = op->P[0], Py = op->P[1], Pz = op->P[2];
+  const size_t ng = (size_t)Px * Py * Pz;
+  DevBuf work;
+  const size_t nc = f == 6 ? 9 : 6;  // Green components (symmetric A; f = 6 adds antisymmetric B)
+  BDDA_CUDA(work.ensure(nc * ng * sizeof(double2), op->stream));
+  if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure(nc * ng * sizeof(double2), op->stream));
+  if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure(nc * ng * sizeof(float2), op->stream));
+  if (prec & BDDA_PREC_DF64) BDDA_CUDA(op->ghatdf.ensure(nc * ng * sizeof(dfc), op->stream));
+  // one spectrum per distinct digit order (radix sequences) of the plan sets
+  bool same = true;
+  for (int i = 0; i < 3; ++i) {
+    const AxisPlan &a = op->plan[0][i], &b = op->plan[1][i];
+    same = same && a.nst == b.nst && std::equal(a.radix, a.radix + a.nst, b.radix);
+  }
+  const double2 *tx = op->tw64[0].as<double2>(), *ty = op->tw64[1].as<double2>(), *tz = op->tw64[2].as<double2>();
+  BDDA_CUDA(build_green_hat(op->geom(op->dip, 1), lf, k_re, k_im, tx, ty, tz, work.as<double2>(),
+                            op->ghat64.as<double2>(), same ? op->ghat32.as<float2>() : nullptr,
+                            op->ghatdf.as<dfc>(), op->stream));
+  if (!same && op->ghat32.p)
+    BDDA_CUDA(build_green_hat(op->geom(op->dip, 0), lf, k_re, k_im, tx, ty, tz, work.as<double2>(), nullptr,
+                              op->ghat32.as<float2>(), nullptr, op->stream));
+  BDDA_CUDA(wait_stream(op->stream));
+  op->kr = k_re;
+  op->ki = k_im;
+  return BDDA_OK;
+}
+
 extern "C" {
 
 const char* bdda_last_error(void) { return bdda::last_error(); }
@@ -233,31 +265,20 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     });
     BDDA_CUDA(cfg);
   }
-  // Green spectrum
-  const int Px = op->P[0], Py = op->P[1], Pz = op->P[2];
-  const size_t ng = (size_t)Px * Py * Pz;
-  DevBuf work;
-  const size_t nc = f == 6 ? 9 : 6;  // Green components (symmetric A; f = 6 adds antisymmetric B)
-  BDDA_CUDA(work.ensure(nc * ng * sizeof(double2), op->stream));
-  if (prec & BDDA_PREC_FP64) BDDA_CUDA(op->ghat64.ensure(nc * ng * sizeof(double2), op->stream));
-  if (prec & BDDA_PREC_FP32) BDDA_CUDA(op->ghat32.ensure(nc * ng * sizeof(float2), op->stream));
-  if (prec & BDDA_PREC_DF64) BDDA_CUDA(op->ghatdf.ensure(nc * ng * sizeof(dfc), op->stream));
-  // one spectrum per distinct digit order (radix sequences) of the plan sets
-  bool same = true;
-  for (int i = 0; i < 3; ++i) {
-    const AxisPlan &a = op->plan[0][i], &b = op->plan[1][i];
-    same = same && a.nst == b.nst && std::equal(a.radix, a.radix + a.nst, b.radix);
+  {
+    const int rc = build_spectrum(op.get(), k_re, k_im);
+    if (rc != BDDA_OK) return rc;
   }
-  const double2 *tx = op->tw64[0].as<double2>(), *ty = op->tw64[1].as<double2>(), *tz = op->tw64[2].as<double2>();
-  BDDA_CUDA(build_green_hat(op->geom(op->dip, 1), lf, k_re, k_im, tx, ty, tz, work.as<double2>(),
-                            op->ghat64.as<double2>(), same ? op->ghat32.as<float2>() : nullptr,
-                            op->ghatdf.as<dfc>(), op->stream));
-  if (!same && op->ghat32.p)
-    BDDA_CUDA(build_green_hat(op->geom(op->dip, 0), lf, k_re, k_im, tx, ty, tz, work.as<double2>(), nullptr,
-                              op->ghat32.as<float2>(), nullptr, op->stream));
   BDDA_CUDA(wait_stream(op->stream));
   *out = op.release();
   return BDDA_OK;
+}
+
+int bdda_op_set_wavenumber(bdda_op* op, double k_re, double k_im) {
+  if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(op->mu);
+  BDDA_CUDA(cudaStreamSynchronize(op->stream));  // no MVP of the old spectrum may still be running
+  return build_spectrum(op, k_re, k_im);
 }
 
 int bdda_op_destroy(bdda_op* op) {

@@ -599,18 +599,18 @@ static int host_colnorm2(Op* op, cudaStream_t st, const double2* A, int n, int L
 // R = B - (diag o X + A_off X); returns max_l ||r_l|| / ||b_l||.  The product
 // runs in FP64, or in double-float arithmetic when use_df is set (FP64-level
 // accuracy on the FP32 pipes); the subtraction and norms are FP64.
-static int true_residual(Op* op, cudaStream_t st, const double2* diag, const double2* B, int ldb, const double2* X, int n,
-                         int L, const std::vector<double>& bn2, double* resmax, int* mvps, bool use_df) {
+static int true_residual(Op* op, cudaStream_t st, const double2* diag, const double2* B, int ldb, const double2* X,
+                         int ldx, int n, int L, const std::vector<double>& bn2, double* resmax, int* mvps, bool use_df) {
   SolverWork* w = op->solver.get();
   const int gv = vec_grid((size_t)n * L);
   if (use_df) {
-    k_to_df<<<gv, 256, 0, st>>>(n, L, X, n, w->xdf.as<dfc>(), n);
+    k_to_df<<<gv, 256, 0, st>>>(n, L, X, ldx, w->xdf.as<dfc>(), n);
     op->timer.count(kOther);
     BDDA_TRY(op_block_mvp<dfl>(op, op->dip, w->xdf.as<dfc>(), n, w->ydf.as<dfc>(), n, L, w->diagdf.as<dfc>(), nullptr, st));
     k_from_df<<<gv, 256, 0, st>>>(n, L, w->ydf.as<dfc>(), n, w->Y64.as<double2>(), n);
     op->timer.count(kOther);
   } else {
-    BDDA_TRY(op_block_mvp<double>(op, op->dip, X, n, w->Y64.as<double2>(), n, L, diag, nullptr, st));
+    BDDA_TRY(op_block_mvp<double>(op, op->dip, X, ldx, w->Y64.as<double2>(), n, L, diag, nullptr, st));
   }
   ++*mvps;
   k_residual<<<gv, 256, 0, st>>>(n, L, B, ldb, w->Y64.as<double2>(), n, w->R64.as<double2>(), n);
@@ -641,6 +641,10 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
     return BDDA_ERR_INVALID;
   }
   const bool refine = o->true_tol > 0;
+  if (o->warm_start && !refine) {
+    set_error("warm_start needs true_tol > 0 (refinement from the initial residual)");
+    return BDDA_ERR_INVALID;
+  }
   const int itermax = o->itermax > 0 ? o->itermax : 300;
   // workspace lives on the operator's stream; order it against a caller's stream
   if (st != op->stream) BDDA_CUDA(order_after(op->stream, st));
@@ -710,16 +714,39 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
     BDDA_TRY(host_colnorm2(op, st, B, n, L, &bn2));
     for (int l = 0; l < L; ++l)
       if (!(bn2[l] > 0.0)) { set_error("zero right-hand side column"); return BDDA_ERR_INVALID; }
-    BDDA_CUDA(cudaMemset2DAsync(X, sizeof(double2) * (size_t)ldx, 0, sizeof(double2) * (size_t)n, L, st));
     const int max_refine = o->max_refine > 0 ? o->max_refine : 8;
     const double itol = o->inner_tol > 0 ? o->inner_tol : (mixed ? 2e-5 : 0.3 * o->true_tol);
     const double2* R = B;
     int ldr = ldb;
     bool converged = false;
-    for (int r = 0; r < max_refine; ++r) {
-      BDDA_TRY(inner(R, ldr, itol, X, ldx, true));
+    if (o->warm_start) {
+      // X holds the initial guess (e.g. the previous wavelength's solution): refine from r = B - A X
+      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, ldx, n, L, bn2, &resmax, &mvps, use_df));
+      R = w->R64.as<double2>();
+      ldr = n;
+      converged = resmax <= o->true_tol;
+      if (!(resmax < 1.0)) {  // the guess is no better than zero: start from zero
+        BDDA_CUDA(cudaMemset2DAsync(X, sizeof(double2) * (size_t)ldx, 0, sizeof(double2) * (size_t)n, L, st));
+        R = B;
+        ldr = ldb;
+      }
+    } else {
+      BDDA_CUDA(cudaMemset2DAsync(X, sizeof(double2) * (size_t)ldx, 0, sizeof(double2) * (size_t)n, L, st));
+    }
+    const bool warm = o->warm_start && R != B;  // refining from a kept initial guess
+    for (int r = 0; r < max_refine && !converged; ++r) {
+      // Inner tolerance: the default for a cold first step; afterwards (and
+      // from a warm guess) the reduction this step needs, 0.3 true_tol /
+      // residual, but not tighter than the default (or 1e-6 from a warm guess,
+      // which lets a close guess converge in one step) and not looser than 0.1.
+      double tol_r = itol;
+      if (r > 0 || warm) {
+        const double need = std::min(0.1, 0.3 * o->true_tol / std::max(resmax, 1e-300));
+        tol_r = std::max(need, (r == 0 && o->inner_tol <= 0) ? std::min(itol, 1e-6) : itol);
+      }
+      BDDA_TRY(inner(R, ldr, tol_r, X, ldx, true));
       if (status == BDDA_ERR_BREAKDOWN) break;
-      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, n, L, bn2, &resmax, &mvps, use_df));
+      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, ldx, n, L, bn2, &resmax, &mvps, use_df));
       R = w->R64.as<double2>();
       ldr = n;
       if (resmax <= o->true_tol) { converged = true; break; }
@@ -790,6 +817,9 @@ int bdda_solve(bdda_op* op, const bdda_solve_opts* opts, const double* diag, con
   BDDA_CUDA(cudaMemcpyAsync(d.p, diag, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
   BDDA_CUDA(cudaMemcpy2DAsync(b.p, sizeof(double2) * n, B, sizeof(double2) * (size_t)ldb, sizeof(double2) * n, L,
                               cudaMemcpyHostToDevice, st));
+  if (opts->warm_start)
+    BDDA_CUDA(cudaMemcpy2DAsync(x.p, sizeof(double2) * n, X, sizeof(double2) * (size_t)ldx, sizeof(double2) * n, L,
+                                cudaMemcpyHostToDevice, st));
   const int rc = solve_impl(op, opts, d.as<double2>(), b.as<double2>(), n, x.as<double2>(), n, L, stats, st);
   if (rc == BDDA_OK || rc == BDDA_ERR_NOT_CONVERGED) {
     BDDA_CUDA(cudaMemcpy2DAsync(X, sizeof(double2) * (size_t)ldx, x.p, sizeof(double2) * n, sizeof(double2) * n, L,

@@ -50,6 +50,48 @@ void mie_a1b1(double wl0, double rp, cd eps_p, cd mu_p, cd eps_m, cd mu_m, cd* a
   *b1 = (fb * psi1 - psi0) / (fb * xi1 - xi0);
 }
 
+// Efficiencies of a sphere in a non-absorbing medium (Bohren & Huffman 1983,
+// eqs. 4.61-4.62): Qsca = 2/x^2 sum (2n+1)(|a_n|^2 + |b_n|^2), Qext = 2/x^2
+// sum (2n+1) Re(a_n + b_n), n <= x + 4 x^(1/3) + 2 (Wiscombe 1980).  a_n, b_n
+// as for n = 1 above; psi_n from the ratios psi_n / psi_{n-1} (downward
+// continued fraction, stable for every n), chi_n upward (its stable direction).
+bool mie_q(double wl0, double rp, cd eps_p, cd mu_p, cd eps_m, cd mu_m, double* qsca, double* qabs, double* qext) {
+  const double k0 = 2.0 * M_PI / wl0;
+  const cd m_m = std::sqrt(eps_m * mu_m);
+  if (std::abs(m_m.imag()) > 0.0) return false;
+  const cd m_p = std::sqrt(eps_p * mu_p);
+  const double x = m_m.real() * k0 * rp;
+  const cd mr = m_p / m_m;
+  const cd y = mr * x;
+  const int nstop = (int)(x + 4.0 * std::cbrt(x) + 2.0);
+  const int nmx = std::max(nstop, (int)std::ceil(std::abs(y))) + 16;
+  std::vector<cd> D(nmx + 1), r(nmx + 2);
+  D[nmx] = cd(0.0, 0.0);
+  for (int n = nmx; n > 0; --n) D[n - 1] = (double)n / y - 1.0 / (D[n] + (double)n / y);
+  r[nmx + 1] = cd(0.0, 0.0);
+  for (int n = nmx; n >= 1; --n) r[n] = 1.0 / ((2.0 * n + 1.0) / x - r[n + 1]);
+  double psi_m1 = std::sin(x), chi_m1 = -std::cos(x);  // n = 0
+  double psi = (r[1] * psi_m1).real(), chi = -std::cos(x) / x - std::sin(x);  // n = 1
+  double ssca = 0.0, sext = 0.0;
+  for (int n = 1; n <= nstop; ++n) {
+    const cd xi(psi, chi), xi_m1(psi_m1, chi_m1);
+    const cd fa = (mu_p / (mu_m * mr)) * D[n] + (double)n / x;
+    const cd fb = (mu_m * mr / mu_p) * D[n] + (double)n / x;
+    const cd an = (fa * psi - psi_m1) / (fa * xi - xi_m1);
+    const cd bn = (fb * psi - psi_m1) / (fb * xi - xi_m1);
+    ssca += (2.0 * n + 1.0) * (std::norm(an) + std::norm(bn));
+    sext += (2.0 * n + 1.0) * (an + bn).real();
+    const double psi_n1 = (r[n + 1] * psi).real();
+    const double chi_n1 = (2.0 * n + 1.0) / x * chi - chi_m1;
+    psi_m1 = psi; psi = psi_n1;
+    chi_m1 = chi; chi = chi_n1;
+  }
+  *qsca = 2.0 / (x * x) * ssca;
+  *qext = 2.0 / (x * x) * sext;
+  *qabs = *qext - *qsca;
+  return true;
+}
+
 // splitmix64 + uniform double in [0,1)
 struct Rng {
   uint64_t s;
@@ -84,6 +126,20 @@ int bdda_mie_a1b1(double wl0, double r_p, const double eps_p[2], const double mu
   mie_a1b1(wl0, r_p, cd(eps_p[0], eps_p[1]), cd(mu_p[0], mu_p[1]), cd(eps_m[0], eps_m[1]), cd(mu_m[0], mu_m[1]), &a, &b);
   a1[0] = a.real(); a1[1] = a.imag();
   b1[0] = b.real(); b1[1] = b.imag();
+  return BDDA_OK;
+}
+
+int bdda_mie_q(double wl0, double r_p, const double eps_p[2], const double mu_p[2], const double eps_m[2],
+               const double mu_m[2], double q[3]) {
+  if (!(wl0 > 0) || !(r_p > 0) || !eps_p || !mu_p || !eps_m || !mu_m || !q) {
+    bdda::set_error("bad Mie arguments");
+    return BDDA_ERR_INVALID;
+  }
+  if (!mie_q(wl0, r_p, cd(eps_p[0], eps_p[1]), cd(mu_p[0], mu_p[1]), cd(eps_m[0], eps_m[1]), cd(mu_m[0], mu_m[1]),
+             &q[0], &q[1], &q[2])) {
+    bdda::set_error("Mie efficiencies need a non-absorbing medium");
+    return BDDA_ERR_INVALID;
+  }
   return BDDA_OK;
 }
 

@@ -68,6 +68,15 @@ int bdda_op_create(bdda_op** op, const int n[3], int f, double lf, double k_re, 
 int bdda_op_destroy(bdda_op* op);
 
 /*
+ * Rebuild the Green spectra for a new wavenumber (the next wavelength of a
+ * sweep) and keep everything else: plans, twiddles, dipoles, workspaces.  No
+ * counterpart in the reference, which re-creates its Solver per wavelength and
+ * target (block_DDA_main.cpp:138-163).  Waits for the operator's stream; MVPs
+ * or solves the caller runs on other streams must be finished.
+ */
+int bdda_op_set_wavenumber(bdda_op* op, double k_re, double k_im);
+
+/*
  * Occupied lattice sites (host array of 0-based addresses
  * ny*nz*ix + nz*iy + iz, Target_manager.cpp:98,167-169, in the caller's dipole
  * order).  Required before bdda_op_mvp_device / bdda_solve*.
@@ -128,6 +137,8 @@ typedef struct {
   double inner_tol;   /* tolerance of each inner Krylov solve in refinement mode (0 -> automatic) */
   int max_refine;     /* refinement steps limit (0 -> 8) */
   int check_every;    /* host convergence poll period in iterations (0 -> 4) */
+  int warm_start;     /* 1: X holds an initial guess on entry (e.g. the solution at a neighbouring
+                         wavelength) and refinement starts from B - A X; needs true_tol > 0 */
 } bdda_solve_opts;
 
 typedef struct {
@@ -328,6 +339,93 @@ int bdda_polarizabilities(double wl0, int nocc, const double* vol, const int* ma
 
 /* DIAG_A (Solver.cpp:28-56): 1/alpha_E on rows f*m + 0..2, 1/alpha_H on rows 6m + 3..5 (f = 6). */
 int bdda_diag_a(int f, int nocc, const double* alpha_e, const double* alpha_h, double* diag);
+
+/*
+ * Mie efficiencies {Qsca, Qabs, Qext} of a sphere of radius r_p in a
+ * non-absorbing medium (what the reference's gmie returns first,
+ * gmie/gmie.cpp:9-152, for its volume-equivalent Mie comparison).
+ */
+int bdda_mie_q(double wl0, double r_p, const double eps_p[2], const double mu_p[2], const double eps_m[2],
+               const double mu_m[2], double q[3]);
+
+/* ---- result files ---------------------------------------------------------- */
+
+typedef struct {
+  int wl0_index, target_index;
+  double wl0;
+  int N_inc;
+  double eper_medium[2], mper_medium[2];
+  const char* target_fname;
+  int is_homogeneous;                  /* 1: one material ("particle"); 0: core + coat */
+  double eper_core[2], mper_core[2];   /* the particle's material when homogeneous */
+  double volume_core;                  /* um^3 (the particle's when homogeneous) */
+  double density_core;                 /* g/cm^3 */
+  double eper_coat[2], mper_coat[2];
+  double volume_coat;
+  int L;
+  const double* cext;                  /* L values, um^2 */
+  const double* cabs;
+  int f, nx, ny, nz, num_element_occupy;
+  double solver_time;                  /* seconds */
+  int append_mac_mie;                  /* add the volume-equivalent Mie MAC line the driver writes */
+} bdda_result_record;
+
+/*
+ * One result section in the reference's DDA_result.dat format
+ * (Result_manager.cpp:10-133 and :178-245, Basic_Stats.hpp; MAC_mie line of
+ * block_DDA_main.cpp:169-183).  *len receives the text length; buf (cap bytes,
+ * may be null) receives the text, NUL-terminated.
+ */
+int bdda_format_result(const bdda_result_record* r, char* buf, int cap, int* len);
+
+/* ---- wavelength x target sweep ------------------------------------------- */
+
+typedef struct {
+  int n[3];               /* lattice box */
+  double lf;              /* physical lattice spacing (um) */
+  int nocc;
+  const int* address;     /* occupied sites */
+  const double* vol;      /* element volumes (um^3) */
+  const int* material;    /* index into bdda_sweep_spec.materials, or null: all 0 */
+} bdda_sweep_target;
+
+typedef struct {
+  int f;                                   /* 3 or 6 */
+  int n_wl;
+  const double* wl0;                       /* free-space wavelengths (um), vacuum medium */
+  int n_targets;
+  const bdda_sweep_target* targets;
+  int nmat;
+  const bdda_material* const* materials;
+  int L;                                   /* incident waves, 1..32 */
+  const double* uinc;                      /* L x 3 propagation directions */
+  const double* einc;                      /* L x 3 complex E amplitudes */
+  const double* hinc;                      /* L x 3 complex H amplitudes (f = 6) */
+  bdda_solve_opts opts;                    /* per solve (opts.warm_start is set by the sweep) */
+  int warm_start;                          /* refine each wavelength from the previous one's solution */
+  int prec;                                /* operator tables (0: FP64 | FP32 | DF64) */
+} bdda_sweep_spec;
+
+typedef struct {
+  int status;                  /* BDDA_OK or the first error of this (wavelength, target) */
+  int iterations;
+  int refinements;
+  int mie_evaluations;         /* distinct (volume, material) Mie evaluations */
+  double true_res_max;
+  double final_err;
+  double ms_solve;
+  double alpha_e0[2], alpha_h0[2];   /* polarizabilities of dipole 0 (the cross sections use them) */
+} bdda_sweep_result;
+
+/*
+ * The reference's experiment loop (block_DDA_main.cpp:138-163) as one call:
+ * for every wavelength and target, material constants, polarizabilities,
+ * DIAG_A, incident fields, solve and cross sections.  One operator per target
+ * is reused across wavelengths (only its spectrum is rebuilt).
+ * cross[((w * n_targets + t) * L + l) * 3 + {0,1,2}] = Cext, Cabs, Csca;
+ * res[w * n_targets + t].  Returns BDDA_OK or the first error.
+ */
+int bdda_sweep(const bdda_sweep_spec* spec, double* cross, bdda_sweep_result* res);
 
 /* ---- instrumentation ------------------------------------------------------ */
 

@@ -138,6 +138,8 @@ def target_fixture(ref, name, scale):
 
 def result_dat(ref, lib):
     txt = open(os.path.join(ref, "result.dat")).read()
+    sec = txt[txt.index(SECTION):]
+    recorded_text = sec[:sec.index("MAC_mie")] + sec[sec.index("MAC_mie"):].split("\n")[0] + "\n"
     rec = {}
     for key in ("mean_Csca", "std_Csca", "mean_MAC", "std_MAC", "mean_SSA", "std_SSA", "MAC_mie",
                 "volume_particle", "num_element_occupy", "wl0", "N_inc"):
@@ -158,15 +160,23 @@ def result_dat(ref, lib):
     X, hist = krylov.bl_cocg_rq(lambda S: mbt.block_mvp(n, 3, gh, P, addr, diag, S), B, 1e-2, 300,
                                 diag=diag, jacobi=True)
     cext, cabs, csca = physics.cross_sections(k, B, X, alpha[0])
-    return {"recorded": rec, "scale_factor": scale, "eper": [eper.real, eper.imag], "density": 1.8,
+    return {"recorded": rec, "recorded_text": recorded_text, "scale_factor": scale, "eper": [eper.real, eper.imag],
+            "density": 1.8,
             "alpha0": [alpha[0].real, alpha[0].imag], "oracle_history": hist,
             "oracle_Cext": cext.tolist(), "oracle_Cabs": cabs.tolist(), "oracle_Csca": csca.tolist()}
 
 
-def _dat_sections(path):
+SECTION = "####################### Start of result section #######################"
+
+
+def _dat_sections(path, text=False):
     txt = open(path).read()
-    secs = txt.split("####################### Start of result section #######################")[1:]
-    return [dict(re.findall(r"^(\w+)\t(.*)$", sec, re.M)) for sec in secs]
+    secs = txt.split(SECTION)[1:]
+    parsed = [dict(re.findall(r"^(\w+)\t(.*)$", sec, re.M)) for sec in secs]
+    if text:
+        for d, sec in zip(parsed, secs):
+            d["_text"] = SECTION + sec.rstrip("\n") + "\n"
+    return parsed
 
 
 def result_f6(ref, lib):
@@ -174,7 +184,7 @@ def result_f6(ref, lib):
     ``Solver.cpp:64-66``; BC particles of r_pp = 20 nm) for the targets
     ``DDA_target_0_agg_N{8,16,32,64}`` at all eleven wavelengths, with the
     oracle's reproduction of each (iteration count and mean cross sections)."""
-    rows = _dat_sections(os.path.join(ref, "DDA_result_BC_rpp20nm.dat"))
+    rows = _dat_sections(os.path.join(ref, "DDA_result_BC_rpp20nm.dat"), text=True)
     scale = 0.02
     names = [f"DDA_target_0_agg_N{N}_kf1.0_Df2.8.out" for N in (8, 16, 32, 64)]
     targets = {nm: target_fixture(ref, nm, scale) for nm in names}
@@ -205,7 +215,8 @@ def result_f6(ref, lib):
                                               "mass_particle", "volume_particle", "num_element_occupy", "wl0")}
         cases.append({"target": r["target_fname"], "wl0": wl0, "eper": [ep.real, ep.imag], "recorded": rec,
                       "alpha_e0": [ae[0].real, ae[0].imag], "alpha_h0": [ah[0].real, ah[0].imag],
-                      "oracle_iterations": len(hist), "oracle_mean_Csca": float(csca.mean()),
+                      "oracle_iterations": len(hist), "oracle_Cext": cext.tolist(), "oracle_Cabs": cabs.tolist(),
+                      "recorded_text": r["_text"], "oracle_mean_Csca": float(csca.mean()),
                       "oracle_mean_MAC": float((cabs * 1e-12 / mass).mean()),
                       "oracle_mean_SSA": float((csca / cext).mean())})
     return {"scale_factor": scale, "tol": 1e-2, "itermax": 300, "solver": "bicgstab", "jacobi": True,
