@@ -60,6 +60,9 @@ template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.as
 
 __device__ __forceinline__ bool skip(const int* done) { return done && *(volatile const int*)done; }
 
+// Rows of a tile one thread visits: rows r, r + kRowStep, ... in column tid % kTZ.
+constexpr int kRowStep = kTileThreads / kTZ;
+
 // ---------------------------------------------------------------- pass A
 // One CTA per listed (y, z-tile): warp w owns z = z0 + w; loops over fields.
 template <typename T, class Line>
@@ -77,6 +80,8 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int 
   const int tile = tiles[blockIdx.x];
   const int y = tile / nzt, z0 = (tile - y * nzt) * kTZ;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tw8 = tid & (kTZ - 1), tq = tid / kTZ;  // tile column and first row of this thread
+  const bool zval = z0 + tw8 < nz;
   for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
     const int xi = idx >> 3, w = idx & 7, z = z0 + w;
     socc[idx] = z < nz ? occ[((size_t)xi * ny + y) * nz + z] : -1;
@@ -94,11 +99,11 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int 
     __syncwarp();
     lay.template fft<false>(line, twx, lane, nx);
     __syncthreads();
-    C* out = t1 + (size_t)f * Px * rowstride + (size_t)y * nz + z0;
-    const C* lb = lines + (f & 1) * kTZ * lw;
-    for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
-      const int w = idx & 7, q = idx >> 3;
-      if (z0 + w < nz) out[(size_t)q * rowstride + w] = lb[w * lw + lay.addr(q)];
+    // drain: thread tid writes column w = tid % 8 of rows q = tid / 8 + 32 k
+    if (zval) {
+      const C* lb = lines + ((f & 1) * kTZ + tw8) * lw;
+      C* out = t1 + (size_t)f * Px * rowstride + (size_t)y * nz + z0 + tw8 + (size_t)tq * rowstride;
+      for (int q = tq; q < Px; q += kRowStep, out += kRowStep * rowstride) *out = lb[lay.addr(q)];
     }
     if (++c == fc) { c = 0; ++l; }
   }
@@ -124,18 +129,19 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
   const int nout = INV ? ny : Py;   // rows written
   const size_t in_rows = (size_t)nin, out_rows = (size_t)nout;
 
+  const int tw8 = tid & (kTZ - 1), ty = tid / kTZ;  // tile column and first row of this thread
+  // fill: thread tid loads column w = tid % 8 of rows yy = tid / 8 + 32 k (zero-filled outside the data)
   auto issue = [&](int task, int buf) {
     const int zt = task % nzt;
     const int r = task / nzt;  // f * Px + q
     const int z0 = zt * kTZ;
-    const C* base = src + (size_t)r * in_rows * nz + z0;
-    C* lb = lines + buf * kTZ * lw;
-    for (int idx = tid; idx < nin * kTZ; idx += kTileThreads) {
-      const int w = idx & 7, yy = idx >> 3;
-      bool valid = z0 + w < nz;
-      if (!INV) valid = valid && tmask[yy * nzt + zt];
-      const C* g = valid ? base + (size_t)yy * nz + w : src;
-      cp_async<sizeof(C)>(lb + w * lw + lay.addr(yy), g, valid);
+    const bool zval = z0 + tw8 < nz;
+    const C* g = src + (size_t)r * in_rows * nz + z0 + tw8 + (size_t)ty * nz;
+    const unsigned char* tm = tmask + zt + (size_t)ty * nzt;
+    C* lb = lines + (buf * kTZ + tw8) * lw;
+    for (int yy = ty; yy < nin; yy += kRowStep, g += (size_t)kRowStep * nz, tm += (size_t)kRowStep * nzt) {
+      const bool valid = zval && (INV || *tm);
+      cp_async<sizeof(C)>(lb + lay.addr(yy), valid ? g : src, valid);
     }
     cp_commit();
   };
@@ -158,13 +164,12 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
     const int zt = task % nzt;
     const int r = task / nzt;
     const int z0 = zt * kTZ;
-    C* ob = dst + (size_t)r * out_rows * nz + z0;
-    const C* lb = lines + buf * kTZ * lw;
-    for (int idx = tid; idx < nout * kTZ; idx += kTileThreads) {
-      const int w = idx & 7, yy = idx >> 3;
-      if (z0 + w >= nz) continue;
-      if (INV && !tmask[yy * nzt + zt]) continue;
-      ob[(size_t)yy * nz + w] = lb[w * lw + lay.addr(yy)];
+    if (z0 + tw8 < nz) {
+      C* ob = dst + (size_t)r * out_rows * nz + z0 + tw8 + (size_t)ty * nz;
+      const unsigned char* tm = tmask + zt + (size_t)ty * nzt;
+      const C* lb = lines + (buf * kTZ + tw8) * lw;
+      for (int yy = ty; yy < nout; yy += kRowStep, ob += (size_t)kRowStep * nz, tm += (size_t)kRowStep * nzt)
+        if (!INV || *tm) *ob = lb[lay.addr(yy)];
     }
     __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
   }
@@ -195,14 +200,14 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, cons
     const int xi = idx >> 3, w = idx & 7, z = z0 + w;
     socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
   }
+  const int tw8 = tid & (kTZ - 1), tq = tid / kTZ;  // tile column and first row of this thread
+  const bool zval = z0 + tw8 < nz;
+  // fill: thread tid loads column w = tid % 8 of rows q = tid / 8 + 32 k (zero-filled past nz)
   auto issue = [&](int f, int buf) {
-    const C* base = t1 + (size_t)f * Px * rowstride + (size_t)yy * nz + z0;
-    C* lb = lines + buf * kTZ * lw;
-    for (int idx = tid; idx < Px * kTZ; idx += kTileThreads) {
-      const int w = idx & 7, q = idx >> 3;
-      const bool valid = z0 + w < nz;
-      cp_async<sizeof(C)>(lb + w * lw + lay.addr(q), valid ? base + (size_t)q * rowstride + w : t1, valid);
-    }
+    const C* g = t1 + (size_t)f * Px * rowstride + (size_t)yy * nz + z0 + tw8 + (size_t)tq * rowstride;
+    C* lb = lines + (buf * kTZ + tw8) * lw;
+    for (int q = tq; q < Px; q += kRowStep, g += (size_t)kRowStep * rowstride)
+      cp_async<sizeof(C)>(lb + lay.addr(q), zval ? g : t1, zval);
     cp_commit();
   };
   issue(0, 0);
