@@ -90,33 +90,31 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
   if (tid == 0) bad = 0;
   __syncthreads();
   for (int k = 0; k < L; ++k) {
-    // ---- pivot search
-    const int m = L - k;
-    const int cnt = full ? m * m : m;
-    double best = -1.0;
-    int bidx = 0x7fffffff;
-    for (int t = tid; t < cnt; t += blockDim.x) {
-      const int ii = k + (t % m);
-      const int jj = full ? k + t / m : k;
-      const double v = sqrt(cabs2(A[ii + jj * L]));
-      const int lin = ii + jj * L;  // column-major order
-      if (v > best || (v == best && lin < bidx)) { best = v; bidx = lin; }
-    }
-    red_v[tid] = best;
-    red_i[tid] = bidx;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (tid < s) {
-        const double v2 = red_v[tid + s];
-        const int i2 = red_i[tid + s];
-        if (v2 > red_v[tid] || (v2 == red_v[tid] && i2 < red_i[tid])) { red_v[tid] = v2; red_i[tid] = i2; }
+    // ---- pivot search by warp 0: lanes scan candidates, shuffle argmax (the
+    // largest |a|, first in column-major order on ties)
+    if (tid < 32) {
+      const int m = L - k;
+      const int cnt = full ? m * m : m;
+      double best = -1.0;
+      int bidx = 0x7fffffff;
+      for (int t = tid; t < cnt; t += 32) {
+        const int ii = k + (t % m);
+        const int jj = full ? k + t / m : k;
+        const double v = sqrt(cabs2(A[ii + jj * L]));
+        const int lin = ii + jj * L;  // column-major order
+        if (v > best || (v == best && lin < bidx)) { best = v; bidx = lin; }
       }
-      __syncthreads();
-    }
-    if (tid == 0) {
-      piv[0] = red_i[0] % L;
-      piv[1] = red_i[0] / L;
-      if (!(red_v[0] > 0.0) || !isfinite(red_v[0])) bad = 1;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double v2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, bidx, o);
+        if (v2 > best || (v2 == best && i2 < bidx)) { best = v2; bidx = i2; }
+      }
+      if (tid == 0) {
+        piv[0] = bidx % L;
+        piv[1] = bidx / L;
+        if (!(best > 0.0) || !isfinite(best)) bad = 1;
+      }
     }
     __syncthreads();
     const int pr = piv[0], pc = piv[1];
@@ -162,20 +160,23 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
     }
     __syncthreads();
   }
-  // ---- back substitution, one thread per right-hand side (reciprocal pivots first)
+  // ---- back substitution, right-looking: row k of X is final once the rows
+  // below were eliminated; then every remaining row sheds its row-k term in
+  // parallel (the serial chain per row is one product per step, not L)
   for (int k = tid; k < L; k += blockDim.x) {
     const double2 inv = cdiv(make_double2(1.0, 0.0), A[k + k * L]);
     A[k + k * L] = inv;  // the diagonal now holds 1 / pivot
   }
   __syncthreads();
-  for (int j = tid; j < nrhs; j += blockDim.x) {
-    for (int k = L - 1; k >= 0; --k) {
-      double2 s = B[k + j * L];
-      for (int c = k + 1; c < L; ++c) s = csub(s, cmul(A[k + c * L], B[c + j * L]));
-      B[k + j * L] = cmul(s, A[k + k * L]);
+  for (int k = L - 1; k >= 0; --k) {
+    for (int j = tid; j < nrhs; j += blockDim.x) B[k + j * L] = cmul(B[k + j * L], A[k + k * L]);
+    __syncthreads();
+    for (int t = tid; t < k * nrhs; t += blockDim.x) {
+      const int r = t % k, j = t / k;
+      B[r + j * L] = csub(B[r + j * L], cmul(A[r + k * L], B[k + j * L]));
     }
+    __syncthreads();
   }
-  __syncthreads();
   if (full) {
     // x[colperm[k]] = y[k]; use A's first column block as scratch (A no longer needed)
     for (int e = tid; e < L * nrhs; e += blockDim.x) A[e] = B[e];
@@ -196,26 +197,36 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
 }
 
 // H = R^H R with R upper triangular, real positive diagonal.  R may alias H.
+// Right-looking: step k takes the square root of the (already updated)
+// diagonal, scales row k and subtracts its outer product from the trailing
+// block, every element in parallel.
 __device__ bool sm_cholesky(double2* R, const double2* H, int L) {
   __shared__ int bad;
+  __shared__ double dinv;
   const int tid = threadIdx.x;
   if (tid == 0) bad = 0;
   if (R != H) for (int e = tid; e < L * L; e += blockDim.x) R[e] = H[e];
   __syncthreads();
   for (int k = 0; k < L; ++k) {
-    // diagonal
     if (tid == 0) {
       double d = R[k + k * L].x;
-      for (int i = 0; i < k; ++i) d -= cabs2(R[i + k * L]);
       if (!(d > 0.0) || !isfinite(d)) { bad = 1; d = 1.0; }
-      R[k + k * L] = make_double2(sqrt(d), 0.0);
+      d = sqrt(d);
+      R[k + k * L] = make_double2(d, 0.0);
+      dinv = 1.0 / d;
     }
     __syncthreads();
-    const double rinv = 1.0 / R[k + k * L].x;
+    const double di = dinv;
     for (int j = k + 1 + tid; j < L; j += blockDim.x) {
-      double2 s = R[k + j * L];
-      for (int i = 0; i < k; ++i) s = csub(s, cconjmul(R[i + k * L], R[i + j * L]));
-      R[k + j * L] = make_double2(s.x * rinv, s.y * rinv);
+      const double2 v = R[k + j * L];
+      R[k + j * L] = make_double2(v.x * di, v.y * di);
+    }
+    __syncthreads();
+    // trailing block (upper part, i <= j): H_ij -= conj(R_ki) R_kj
+    const int m = L - k - 1;
+    for (int t = tid; t < m * m; t += blockDim.x) {
+      const int i = k + 1 + t % m, j = k + 1 + t / m;
+      if (i <= j) R[i + j * L] = csub(R[i + j * L], cconjmul(R[k + i * L], R[k + j * L]));
     }
     __syncthreads();
   }
@@ -231,20 +242,29 @@ __device__ bool sm_cholesky(double2* R, const double2* H, int L) {
 }
 
 // Inverse of an upper triangular matrix with a real positive diagonal (the
-// Cholesky factors): one thread per column, diagonal reciprocals precomputed.
+// Cholesky factors): R X = I solved bottom-up, right-looking -- row i of X is
+// final after scaling by 1 / R_ii, then the rows above shed their row-i term,
+// all elements in parallel.
 __device__ void sm_tri_inv(double2* Ri, const double2* R, int L) {
   __shared__ double dinv[kMaxL];
   for (int i = threadIdx.x; i < L; i += blockDim.x) dinv[i] = 1.0 / R[i + i * L].x;
+  for (int e = threadIdx.x; e < L * L; e += blockDim.x)
+    Ri[e] = make_double2((e % L) == (e / L) ? 1.0 : 0.0, 0.0);
   __syncthreads();
-  for (int j = threadIdx.x; j < L; j += blockDim.x) {
-    for (int i = L - 1; i >= 0; --i) {
-      if (i > j) { Ri[i + j * L] = make_double2(0.0, 0.0); continue; }
-      double2 s = make_double2(i == j ? 1.0 : 0.0, 0.0);
-      for (int k = i + 1; k <= j; ++k) s = csub(s, cmul(R[i + k * L], Ri[k + j * L]));
-      Ri[i + j * L] = make_double2(s.x * dinv[i], s.y * dinv[i]);
+  for (int i = L - 1; i >= 0; --i) {
+    for (int j = i + threadIdx.x; j < L; j += blockDim.x) {
+      const double2 v = Ri[i + j * L];
+      Ri[i + j * L] = make_double2(v.x * dinv[i], v.y * dinv[i]);
     }
+    __syncthreads();
+    // rows r < i, columns j >= i: X_rj -= R_ri X_ij
+    const int nc = L - i;
+    for (int t = threadIdx.x; t < i * nc; t += blockDim.x) {
+      const int r = t % i, j = i + t / i;
+      Ri[r + j * L] = csub(Ri[r + j * L], cmul(R[r + i * L], Ri[i + j * L]));
+    }
+    __syncthreads();
   }
-  __syncthreads();
 }
 
 // Frobenius norm (thread 0 result broadcast through smem)

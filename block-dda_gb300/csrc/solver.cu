@@ -73,18 +73,18 @@ struct SmallSmem {
   static size_t bytes(int L) { return 6 * (size_t)L * L * sizeof(double2) + kSmallThreads * (sizeof(double) + sizeof(int)) + (2 + kMaxL) * sizeof(int); }
 };
 
-#define SMALL_PROLOGUE                                                               \
-  extern __shared__ __align__(16) unsigned char smem_raw[];                          \
-  double2* m0 = reinterpret_cast<double2*>(smem_raw);                                \
-  double2* m1 = m0 + L * L;                                                          \
-  double2* m2 = m1 + L * L;                                                          \
-  double2* m3 = m2 + L * L;                                                          \
-  double2* m4 = m3 + L * L;                                                          \
-  double2* m5 = m4 + L * L;                                                          \
-  double* red_v = reinterpret_cast<double*>(m5 + L * L);                             \
-  int* red_i = reinterpret_cast<int*>(red_v + kSmallThreads);                        \
-  int* piv = red_i + kSmallThreads;                                                  \
-  int* colperm = piv + 2;                                                            \
+#define SMALL_PROLOGUE                                                                              \
+  extern __shared__ __align__(16) unsigned char smem_raw[];                                         \
+  double2* m0 = reinterpret_cast<double2*>(smem_raw);                                               \
+  double2* m1 = m0 + L * L;                                                                         \
+  [[maybe_unused]] double2* m2 = m1 + L * L;                                                        \
+  [[maybe_unused]] double2* m3 = m2 + L * L;                                                        \
+  [[maybe_unused]] double2* m4 = m3 + L * L;                                                        \
+  [[maybe_unused]] double2* m5 = m4 + L * L;                                                        \
+  [[maybe_unused]] double* red_v = reinterpret_cast<double*>(m5 + L * L);                           \
+  [[maybe_unused]] int* red_i = reinterpret_cast<int*>(red_v + kSmallThreads);                      \
+  [[maybe_unused]] int* piv = red_i + kSmallThreads;                                                \
+  [[maybe_unused]] int* colperm = piv + 2;                                                          \
   const int LL = L * L;
 
 __device__ void fail(SolverCtl* ctl) {
