@@ -87,6 +87,65 @@ __device__ __forceinline__ void stage(float2* __restrict__ sm, const float2* __r
   __syncwarp();
 }
 
+// First forward stage with its inputs read from global memory instead of
+// shared memory: line j's element idx < nv at gsrc[j * gstride + idx] (the
+// zero padding past nv is never read), results stored to the padded shared
+// line as stage<P, 0, false, NL> stores them.
+template <class P, int NL>
+__device__ __forceinline__ void stage0_from_global(float2* __restrict__ sm, const float2* __restrict__ tw, int lane,
+                                                   int nv, const float2* __restrict__ gsrc, size_t gstride) {
+  constexpr int R = P::rad[0];
+  constexpr int M = P::M(0);       // butterflies per line (Ls = N)
+  constexpr int T = NL * M;
+  constexpr int off = (P::nst == 1) ? 1 : (M / P::Rl) * P::S;
+  for (int t = lane; t < T; t += 32) {
+    const int j = NL == 1 ? 0 : t / M;
+    const int n1 = t - j * M;
+    const float2* g = gsrc + (size_t)j * gstride + n1;
+    float2 v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = (n1 + i * M < nv) ? g[i * M] : make_float2(0.f, 0.f);
+    dft<R, false>(v);
+    if (M > 1 && n1 != 0) {
+#pragma unroll
+      for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tw + k * n1));
+    }
+    float2* p = sm + j * P::LW + P::addr(n1);
+#pragma unroll
+    for (int i = 0; i < R; ++i) p[i * off] = v[i];
+  }
+  __syncwarp();
+}
+
+// Last inverse stage with its outputs written to global memory: line j's
+// element idx < nv to gdst[j * gstride + idx] (the rest are discarded).
+template <class P, int NL>
+__device__ __forceinline__ void stage0_to_global(const float2* __restrict__ sm, const float2* __restrict__ tw,
+                                                 int lane, int nv, float2* __restrict__ gdst, size_t gstride) {
+  constexpr int R = P::rad[0];
+  constexpr int M = P::M(0);
+  constexpr int T = NL * M;
+  constexpr int off = (P::nst == 1) ? 1 : (M / P::Rl) * P::S;
+  for (int t = lane; t < T; t += 32) {
+    const int j = NL == 1 ? 0 : t / M;
+    const int n1 = t - j * M;
+    const float2* p = sm + j * P::LW + P::addr(n1);
+    float2 v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = p[i * off];
+    if (M > 1 && n1 != 0) {
+#pragma unroll
+      for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tw + k * n1));
+    }
+    dft<R, true>(v);
+    float2* g = gdst + (size_t)j * gstride + n1;
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+      if (n1 + i * M < nv) g[i * M] = v[i];
+  }
+  __syncwarp();
+}
+
 // Forward transform of NL lines: natural order in, digit-reversed out, only
 // the first nv inputs read.
 template <class P, int NL, int s = 0>
@@ -97,14 +156,30 @@ __device__ __forceinline__ void forward(float2* sm, const float2* tw, int lane, 
   }
 }
 
+// Forward transform whose input lines are in global memory (see stage0_from_global).
+template <class P, int NL>
+__device__ __forceinline__ void forward_from_global(float2* sm, const float2* tw, int lane, int nv,
+                                                    const float2* gsrc, size_t gstride) {
+  stage0_from_global<P, NL>(sm, tw, lane, nv, gsrc, gstride);
+  forward<P, NL, 1>(sm, tw, lane, nv);
+}
+
 // Inverse transform (unnormalised): digit-reversed in, natural order out,
 // only the first nv outputs written.
-template <class P, int NL, int s = P::nst - 1>
+template <class P, int NL, int s = P::nst - 1, int last = 0>
 __device__ __forceinline__ void inverse(float2* sm, const float2* tw, int lane, int nv) {
-  if constexpr (s >= 0) {
+  if constexpr (s >= last) {
     stage<P, s, true, NL>(sm, tw, lane, nv);
-    inverse<P, NL, s - 1>(sm, tw, lane, nv);
+    inverse<P, NL, s - 1, last>(sm, tw, lane, nv);
   }
+}
+
+// Inverse transform whose output lines go to global memory (see stage0_to_global).
+template <class P, int NL>
+__device__ __forceinline__ void inverse_to_global(float2* sm, const float2* tw, int lane, int nv, float2* gdst,
+                                                  size_t gstride) {
+  inverse<P, NL, P::nst - 1, 1>(sm, tw, lane, nv);
+  stage0_to_global<P, NL>(sm, tw, lane, nv, gdst, gstride);
 }
 
 }  // namespace sfft

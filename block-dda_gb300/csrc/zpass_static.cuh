@@ -38,35 +38,16 @@ k_pass_c_static(float2* __restrict__ t2, int L, int Px, int Py, int nz, const fl
   const size_t fstride = (size_t)Px * Py * nz;  // between fields
   float2* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nz;
   constexpr bool six = SIX;
-  for (int z = lane; z < nz; z += 32) {
-    const int a = P::addr(z);
-    s0[a] = g0[z];
-    s0[LW + a] = g0[fstride + z];
-    s0[2 * LW + a] = g0[2 * fstride + z];
-    if (six) {
-      s0[3 * LW + a] = g0[3 * fstride + z];
-      s0[4 * LW + a] = g0[4 * fstride + z];
-      s0[5 * LW + a] = g0[5 * fstride + z];
-    }
-  }
-  __syncwarp();
   constexpr int halves = six ? 2 : 1;  // line triples: E, then M
-  for (int h = 0; h < halves; ++h) sfft::forward<P, 3>(s0 + 3 * h * LW, twz, lane, nz);
+  // the first forward stage reads the lines straight from T2 (no staging loop)
+  for (int h = 0; h < halves; ++h)
+    sfft::forward_from_global<P, 3>(s0 + 3 * h * LW, twz, lane, nz, g0 + 3 * h * fstride, fstride);
   const float2* gl = ghat + (size_t)line * (six ? 9 : 6) * Pz;
   for (int p = lane; p < Pz; p += 32) z_product(s0, LW, P::addr(p), gl, Pz, p, six);
   __syncwarp();
-  for (int h = 0; h < halves; ++h) sfft::inverse<P, 3>(s0 + 3 * h * LW, twz, lane, nz);
-  for (int z = lane; z < nz; z += 32) {
-    const int a = P::addr(z);
-    g0[z] = s0[a];
-    g0[fstride + z] = s0[LW + a];
-    g0[2 * fstride + z] = s0[2 * LW + a];
-    if (six) {
-      g0[3 * fstride + z] = s0[3 * LW + a];
-      g0[4 * fstride + z] = s0[4 * LW + a];
-      g0[5 * fstride + z] = s0[5 * LW + a];
-    }
-  }
+  // the last inverse stage writes the lines straight back to T2 (rows past nz dropped)
+  for (int h = 0; h < halves; ++h)
+    sfft::inverse_to_global<P, 3>(s0 + 3 * h * LW, twz, lane, nz, g0 + 3 * h * fstride, fstride);
 }
 
 template <class P, bool SIX>
