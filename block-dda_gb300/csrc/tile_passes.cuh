@@ -175,6 +175,70 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
   }
 }
 
+// ---------------------------------------------------------------- pass B / D, two lines per warp
+// Same as k_pass_y with 16 z-columns per task: warp w transforms columns 2w
+// and 2w + 1 together (the butterflies of both lines share the lanes), and
+// every row segment is 16 elements wide.  Compile-time plans only.
+constexpr int kTZ2 = 2 * kTZ;
+constexpr int kRowStep2 = kTileThreads / kTZ2;
+
+template <bool INV, class P>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_y2(const float2* __restrict__ src, float2* __restrict__ dst, const unsigned char* __restrict__ tmask, int ny,
+          int nz, int nzt, int ntask, const float2* __restrict__ twy, const int* done) {
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int Py = P::N, lw = P::LW;
+  float2* lines = reinterpret_cast<float2*>(smem_raw);  // [2][kTZ2][lw]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nin = INV ? Py : ny;
+  const int nout = INV ? ny : Py;
+  const int nzt2 = (nz + kTZ2 - 1) / kTZ2;
+  const int tw = tid & (kTZ2 - 1), ty = tid / kTZ2;  // tile column and first row of this thread
+  auto issue = [&](int task, int buf) {
+    const int zt2 = task % nzt2;
+    const int r = task / nzt2;  // f * Px + q
+    const int z = zt2 * kTZ2 + tw;
+    const bool zval = z < nz;
+    const float2* g = src + (size_t)r * nin * nz + z + (size_t)ty * nz;
+    const unsigned char* tm = tmask + (zval ? z / kTZ : 0) + (size_t)ty * nzt;
+    float2* lb = lines + (buf * kTZ2 + tw) * lw;
+    for (int yy = ty; yy < nin; yy += kRowStep2, g += (size_t)kRowStep2 * nz, tm += (size_t)kRowStep2 * nzt) {
+      const bool valid = zval && (INV || *tm);
+      cp_async<sizeof(float2)>(lb + P::addr(yy), valid ? g : src, valid);
+    }
+    cp_commit();
+  };
+  int task = blockIdx.x;
+  if (task < ntask) issue(task, 0);
+  for (int it = 0; task < ntask; ++it, task += gridDim.x) {
+    const int buf = it & 1;
+    const int next = task + gridDim.x;
+    if (next < ntask) {
+      issue(next, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    float2* wl = lines + (buf * kTZ2 + 2 * warp) * lw;
+    if (!INV) sfft::forward<P, 2>(wl, twy, lane, ny);
+    else sfft::inverse<P, 2>(wl, twy, lane, ny);
+    __syncthreads();
+    const int zt2 = task % nzt2;
+    const int r = task / nzt2;
+    const int z = zt2 * kTZ2 + tw;
+    if (z < nz) {
+      float2* ob = dst + (size_t)r * nout * nz + z + (size_t)ty * nz;
+      const unsigned char* tm = tmask + z / kTZ + (size_t)ty * nzt;
+      const float2* lb = lines + (buf * kTZ2 + tw) * lw;
+      for (int yy = ty; yy < nout; yy += kRowStep2, ob += (size_t)kRowStep2 * nz, tm += (size_t)kRowStep2 * nzt)
+        if (!INV || *tm) *ob = lb[P::addr(yy)];
+    }
+    __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
+  }
+}
+
 // ---------------------------------------------------------------- pass E
 // One CTA per listed (y, z-tile); loops over fields with the next field's
 // tile prefetched by cp.async; scatters the occupied sites.

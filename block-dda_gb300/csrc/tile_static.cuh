@@ -5,6 +5,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <mutex>
 
 #include "mvp.hpp"
@@ -25,7 +27,9 @@ cudaError_t launch(int pass, const TileArgs& a) {
   const MvpGeom& g = *a.g;
   const int max_nx = kMaxLine / 2;
   const int smem_ae = tile::smem_tile<float>(P::LW, max_nx);
-  const int smem_bd = tile::smem_tile<float>(P::LW, 0);
+  const int smem_bd = 2 * tile::kTZ2 * P::LW * (int)sizeof(float2);  // y passes: 16 columns per task
+  const int ntask2 = a.nfield * g.Px * ((g.nz + tile::kTZ2 - 1) / tile::kTZ2);
+  const int grid2 = std::min(ntask2, a.grid_y);
   static std::once_flag oa, ob, od, oe;
   static cudaError_t ca = cudaSuccess, cb = cudaSuccess, cd = cudaSuccess, ce = cudaSuccess;
   cudaError_t e = cudaSuccess;
@@ -36,14 +40,14 @@ cudaError_t launch(int pass, const TileArgs& a) {
           a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, L{}, a.twx, a.t1, a.done);
       break;
     case kTileB:
-      if ((e = set_smem(tile::k_pass_y<float, false, L>, smem_bd, ob, cb)) != cudaSuccess) return e;
-      tile::k_pass_y<float, false, L><<<a.grid_y, kTileThreads, smem_bd, a.st>>>(
-          a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzt, a.ntask_y, L{}, a.twy, a.done);
+      if ((e = set_smem(tile::k_pass_y2<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
+      tile::k_pass_y2<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzt,
+                                                                        ntask2, a.twy, a.done);
       break;
     case kTileD:
-      if ((e = set_smem(tile::k_pass_y<float, true, L>, smem_bd, od, cd)) != cudaSuccess) return e;
-      tile::k_pass_y<float, true, L><<<a.grid_y, kTileThreads, smem_bd, a.st>>>(
-          a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzt, a.ntask_y, L{}, a.twy, a.done);
+      if ((e = set_smem(tile::k_pass_y2<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
+      tile::k_pass_y2<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzt,
+                                                                       ntask2, a.twy, a.done);
       break;
     default:
       if ((e = set_smem(tile::k_pass_e<float, L>, smem_ae, oe, ce)) != cudaSuccess) return e;
