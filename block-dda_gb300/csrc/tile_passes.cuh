@@ -1,14 +1,14 @@
 // Strided passes of the block MVP (A: x-forward gather, B: y-forward,
-// D: y-inverse, E: x-inverse scatter), shared by the runtime-plan kernels of
-// every precision and the compile-time-plan kernels of complex FP32.
+// D: y-inverse, E: x-inverse scatter).
 //
-// A CTA stages 8 z-columns (one line per warp) of one (field, x) or
-// (y, field) tile in shared memory; the line layout and the warp transform
-// come from a layout policy:
-//   RtLine<C>  runtime axis plan (fft_core.cuh; skewed layout of the plan)
-//   StLine<P>  compile-time plan P (static_fft.cuh; padded layout of P)
-// Forward transforms read only the first nv inputs; inverse transforms need
-// only the first nv outputs (StLine writes only those).
+// k_pass_a / k_pass_y / k_pass_e: runtime axis plans (fft_core.cuh, skewed
+// layout of the plan; every precision).  A CTA stages 8 z-columns (one line
+// per warp) of one tile in shared memory; forward transforms read only the
+// first nv inputs.
+// k_pass_a2 / k_pass_y2 / k_pass_e2: compile-time plans (static_fft.cuh,
+// padded layout; complex FP32).  Each warp transforms two lines at once -- two
+// fields of its z-column in the x passes, two z-columns of a 16-column tile in
+// the y passes -- and inverse transforms write only the first nv outputs.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -33,17 +33,6 @@ struct RtLine {
   }
 };
 
-template <class P>
-struct StLine {
-  __device__ __forceinline__ static constexpr int n() { return P::N; }
-  __device__ __forceinline__ static constexpr int lw() { return P::LW; }
-  __device__ __forceinline__ static int addr(int i) { return P::addr(i); }
-  template <bool INV>
-  __device__ __forceinline__ static void fft(float2* line, const float2* tw, int lane, int nv) {
-    if (!INV) sfft::forward<P, 1>(line, tw, lane, nv);
-    else sfft::inverse<P, 1>(line, tw, lane, nv);
-  }
-};
 
 // ---- cp.async helpers (LDGSTS: global -> shared without registers) --------
 template <int BYTES>
@@ -298,6 +287,124 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, cons
     }
     __syncthreads();  // buffer 'buf' is the cp.async target of field f + 2
     if (++c == fc) { c = 0; ++l; }
+  }
+}
+
+// ---------------------------------------------------------------- pass A / E, two fields per warp
+// Same as k_pass_a / k_pass_e (one CTA per listed (y, z-tile)) with the
+// fields taken two at a time: warp w transforms column w of fields f and f + 1
+// together (lines [buf][w][2]).  Compile-time plans only.
+template <class P>
+__device__ __forceinline__ float2* x2_line(float2* lines, int buf, int w, int h) {
+  return lines + ((buf * kTZ + w) * 2 + h) * P::LW;
+}
+
+template <class P>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_a2(const float2* __restrict__ x, int ldx, int nfield, int fc, const int* __restrict__ occ,
+          const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, const float2* __restrict__ twx,
+          float2* __restrict__ t1, const int* done) {
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int Px = P::N;
+  float2* lines = reinterpret_cast<float2*>(smem_raw);                       // [2][kTZ][2][LW]
+  int* socc = reinterpret_cast<int*>(lines + 4 * kTZ * P::LW);               // [nx][kTZ]
+  const int tile = tiles[blockIdx.x];
+  const int y = tile / nzt, z0 = (tile - y * nzt) * kTZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tw8 = tid & (kTZ - 1), tq = tid / kTZ;
+  const bool zval = z0 + tw8 < nz;
+  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
+    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
+    socc[idx] = z < nz ? occ[((size_t)xi * ny + y) * nz + z] : -1;
+  }
+  __syncthreads();
+  const size_t rowstride = (size_t)ny * nz;
+  for (int f = 0, it = 0; f < nfield; f += 2, ++it) {
+    const int buf = it & 1;
+    const int nh = f + 1 < nfield ? 2 : 1;
+    for (int h = 0; h < nh; ++h) {
+      const int fh = f + h, l = fh / fc, c = fh - l * fc;
+      const float2* xc = x + (size_t)l * ldx + c;
+      float2* line = x2_line<P>(lines, buf, warp, h);
+      for (int xi = lane; xi < nx; xi += 32) {
+        const int m = socc[xi * kTZ + warp];
+        line[P::addr(xi)] = m >= 0 ? xc[fc * (size_t)m] : make_float2(0.f, 0.f);
+      }
+    }
+    __syncwarp();
+    if (nh == 2) sfft::forward<P, 2>(x2_line<P>(lines, buf, warp, 0), twx, lane, nx);
+    else sfft::forward<P, 1>(x2_line<P>(lines, buf, warp, 0), twx, lane, nx);
+    __syncthreads();
+    if (zval) {
+      for (int h = 0; h < nh; ++h) {
+        const float2* lb = x2_line<P>(lines, buf, tw8, h);
+        float2* out = t1 + (size_t)(f + h) * Px * rowstride + (size_t)y * nz + z0 + tw8 + (size_t)tq * rowstride;
+        for (int q = tq; q < Px; q += kRowStep, out += kRowStep * rowstride) *out = lb[P::addr(q)];
+      }
+    }
+  }
+}
+
+template <class P>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_e2(const float2* __restrict__ t1, int nfield, int fc, const int* __restrict__ occ,
+          const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, const float2* __restrict__ twx,
+          const float2* __restrict__ x, int ldx, const float2* __restrict__ diag, const float2* __restrict__ jpre,
+          float2* __restrict__ y, int ldy, const int* done) {
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int Px = P::N;
+  float2* lines = reinterpret_cast<float2*>(smem_raw);                       // [2][kTZ][2][LW]
+  int* socc = reinterpret_cast<int*>(lines + 4 * kTZ * P::LW);               // [nx][kTZ]
+  const int tile = tiles[blockIdx.x];
+  const int yy = tile / nzt, z0 = (tile - yy * nzt) * kTZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const size_t rowstride = (size_t)ny * nz;
+  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
+    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
+    socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
+  }
+  const int tw8 = tid & (kTZ - 1), tq = tid / kTZ;
+  const bool zval = z0 + tw8 < nz;
+  // fill fields f, f + 1 (if any) of the tile: column tw8, rows tq + 32 k
+  auto issue = [&](int f, int buf) {
+    const int nh = f + 1 < nfield ? 2 : 1;
+    for (int h = 0; h < nh; ++h) {
+      const float2* g = t1 + (size_t)(f + h) * Px * rowstride + (size_t)yy * nz + z0 + tw8 + (size_t)tq * rowstride;
+      float2* lb = x2_line<P>(lines, buf, tw8, h);
+      for (int q = tq; q < Px; q += kRowStep, g += (size_t)kRowStep * rowstride)
+        cp_async<sizeof(float2)>(lb + P::addr(q), zval ? g : t1, zval);
+    }
+    cp_commit();
+  };
+  issue(0, 0);
+  for (int f = 0, it = 0; f < nfield; f += 2, ++it) {
+    const int buf = it & 1;
+    const int nh = f + 1 < nfield ? 2 : 1;
+    if (f + 2 < nfield) {
+      issue(f + 2, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    if (nh == 2) sfft::inverse<P, 2>(x2_line<P>(lines, buf, warp, 0), twx, lane, nx);
+    else sfft::inverse<P, 1>(x2_line<P>(lines, buf, warp, 0), twx, lane, nx);
+    for (int h = 0; h < nh; ++h) {
+      const int fh = f + h, l = fh / fc, c = fh - l * fc;
+      const float2* line = x2_line<P>(lines, buf, warp, h);
+      for (int xi = lane; xi < nx; xi += 32) {
+        const int m = socc[xi * kTZ + warp];
+        if (m < 0) continue;
+        const size_t r = fc * (size_t)m + c;
+        float2 v = line[P::addr(xi)];
+        if (diag != nullptr) v = cadd(v, cmul(diag[r], x[(size_t)l * ldx + r]));
+        if (jpre != nullptr) v = cmul(v, jpre[r]);
+        y[(size_t)l * ldy + r] = v;
+      }
+    }
+    __syncthreads();  // buffer 'buf' is the cp.async target of fields f + 4, f + 5
   }
 }
 

@@ -1,6 +1,6 @@
 // Strided passes (A, B, D, E) for complex FP32 with compile-time axis plans
-// (tplans.inc): the runtime kernels of tile_passes.cuh instantiated with the
-// StLine layout of the plan of their axis length.
+// (tplans.inc): the two-line kernels of tile_passes.cuh instantiated for the
+// plan of their axis length.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -23,10 +23,11 @@ cudaError_t set_smem(K kernel, int bytes, std::once_flag& once, cudaError_t& cfg
 
 template <class P>
 cudaError_t launch(int pass, const TileArgs& a) {
-  using L = tile::StLine<P>;
   const MvpGeom& g = *a.g;
   const int max_nx = kMaxLine / 2;
-  const int smem_ae = tile::smem_tile<float>(P::LW, max_nx);
+  // x passes: [2 buffers][8 columns][2 fields] lines + the occupancy of the tile
+  auto smem_x2 = [](int nx) { return 4 * kTZ * P::LW * (int)sizeof(float2) + nx * kTZ * 4; };
+  const int smem_ae = smem_x2(max_nx);
   const int smem_bd = 2 * tile::kTZ2 * P::LW * (int)sizeof(float2);  // y passes: 16 columns per task
   const int ntask2 = a.nfield * g.Px * ((g.nz + tile::kTZ2 - 1) / tile::kTZ2);
   const int grid2 = std::min(ntask2, a.grid_y);
@@ -35,9 +36,9 @@ cudaError_t launch(int pass, const TileArgs& a) {
   cudaError_t e = cudaSuccess;
   switch (pass) {
     case kTileA:
-      if ((e = set_smem(tile::k_pass_a<float, L>, smem_ae, oa, ca)) != cudaSuccess) return e;
-      tile::k_pass_a<float, L><<<g.ntiles, kTileThreads, tile::smem_tile<float>(P::LW, g.nx), a.st>>>(
-          a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, L{}, a.twx, a.t1, a.done);
+      if ((e = set_smem(tile::k_pass_a2<P>, smem_ae, oa, ca)) != cudaSuccess) return e;
+      tile::k_pass_a2<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
+          a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, a.twx, a.t1, a.done);
       break;
     case kTileB:
       if ((e = set_smem(tile::k_pass_y2<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
@@ -50,9 +51,9 @@ cudaError_t launch(int pass, const TileArgs& a) {
                                                                        ntask2, a.twy, a.done);
       break;
     default:
-      if ((e = set_smem(tile::k_pass_e<float, L>, smem_ae, oe, ce)) != cudaSuccess) return e;
-      tile::k_pass_e<float, L><<<g.ntiles, kTileThreads, tile::smem_tile<float>(P::LW, g.nx), a.st>>>(
-          a.t1, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, L{}, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
+      if ((e = set_smem(tile::k_pass_e2<P>, smem_ae, oe, ce)) != cudaSuccess) return e;
+      tile::k_pass_e2<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
+          a.t1, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
           a.done);
       break;
   }
