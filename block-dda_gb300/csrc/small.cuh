@@ -1,13 +1,19 @@
-// Single-CTA complex-FP64 L x L algebra for the block Krylov solvers
-// (included by solver.cu only).  Matrices are column-major in shared memory,
-// M[i + j*L].  Every routine is called by all kSmallThreads threads of the CTA
-// and ends with a barrier.
+// Single-CTA complex L x L algebra for the block Krylov solvers (included by
+// solver.cu only).  Matrices are column-major in shared memory, M[i + j*L].
+// Every routine is called by all kSmallThreads threads of the CTA and ends
+// with a barrier.
 //
 // Replaces Eigen's partialPivLu / fullPivLu solves
 // (bl_krylov_mvp_fft/bl_cocg_rq_mvp_fft.cpp:56,66, bl_cocg_rq_jacobi_mvp_fft.cpp:63,73,
 // bl_bicgstab_mvp_fft.cpp:58-59,93, bl_bicggr_mvp_fft.cpp:51,110) and the L x L
 // part of qr_reduced (qr_reduced.cpp:9-31, here as the Cholesky factors of
 // CholQR2), so a whole Krylov iteration runs without a host round trip.
+//
+// Two arithmetics, R: double (complex FP64, double2 matrices) for FP64
+// solves, and dfl (double-float, dfc matrices, ~48-bit significand) for the
+// mixed-precision inner solves, whose block vectors are FP32 -- GB300 issues
+// FP32 at 64 times its FP64 rate.  Inputs (Gram partials) and the state slots
+// in global memory stay complex FP64 either way.
 #pragma once
 
 #include "common.cuh"
@@ -17,20 +23,82 @@ namespace bdda {
 
 constexpr int kSmallThreads = 256;
 
-__device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
-__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
-  // Smith-free plain division; operands are O(1) pivots.
+template <typename R> struct SmallMat;
+template <> struct SmallMat<double> { using M = double2; };
+template <> struct SmallMat<dfl> { using M = dfc; };
+
+// ---- double-float reciprocal and square root --------------------------------
+// The FP32 result refined by Newton steps whose residual is evaluated in
+// double-float (Dekker 1971; Hida, Li and Bailey 2001, "Algorithms for
+// quad-double precision floating point arithmetic").
+__device__ __forceinline__ dfl df_recip(dfl b) {
+  const float q1 = 1.0f / b.hi;
+  const dfl one(1.0f, 0.0f);
+  const dfl q = df_quick_two_sum(q1, (one - b * dfl(q1, 0.0f)).hi * q1);
+  return q + dfl((one - b * q).hi * q1, 0.0f);
+}
+__device__ __forceinline__ dfl df_sqrt(dfl a) {
+  if (!(a.hi > 0.0f)) return dfl(sqrtf(a.hi), 0.0f);  // zero, negative or NaN: the FP32 answer
+  const float x = sqrtf(a.hi);
+  const dfl xx(x, 0.0f);
+  return xx + dfl((a - xx * xx).hi * (0.5f / x), 0.0f);
+}
+
+// ---- scalar and complex helpers of the two arithmetics ---------------------
+__device__ __forceinline__ double r_recip(double a) { return 1.0 / a; }
+__device__ __forceinline__ dfl r_recip(dfl a) { return df_recip(a); }
+__device__ __forceinline__ double r_sqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ dfl r_sqrt(dfl a) { return df_sqrt(a); }
+__device__ __forceinline__ bool r_gt(double a, double b) { return a > b; }
+__device__ __forceinline__ bool r_gt(dfl a, dfl b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
+__device__ __forceinline__ bool r_eq(double a, double b) { return a == b; }
+__device__ __forceinline__ bool r_eq(dfl a, dfl b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool r_pos_finite(double a) { return a > 0.0 && isfinite(a); }
+__device__ __forceinline__ bool r_pos_finite(dfl a) { return a.hi > 0.0f && isfinite(a.hi) && isfinite(a.lo); }
+__device__ __forceinline__ double r_to_double(double a) { return a; }
+__device__ __forceinline__ double r_to_double(dfl a) { return df_to_double(a); }
+__device__ __forceinline__ double r_shfl_xor(double a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+__device__ __forceinline__ dfl r_shfl_xor(dfl a, int o) {
+  return dfl(__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o));
+}
+template <typename R> __device__ __forceinline__ R r_const(float v) { return R(v); }
+template <> __device__ __forceinline__ dfl r_const<dfl>(float v) { return dfl(v, 0.0f); }
+
+__device__ __forceinline__ double2 m_to_double2(double2 a) { return a; }
+__device__ __forceinline__ double2 m_to_double2(dfc a) { return make_double2(df_to_double(a.x), df_to_double(a.y)); }
+template <typename M> __device__ M m_from_double2(double2 a);
+template <> __device__ __forceinline__ double2 m_from_double2<double2>(double2 a) { return a; }
+template <> __device__ __forceinline__ dfc m_from_double2<dfc>(double2 a) { return cmake(dfl(a.x), dfl(a.y)); }
+
+template <typename M> __device__ __forceinline__ auto m_abs2(M a) { return a.x * a.x + a.y * a.y; }
+template <typename M> __device__ __forceinline__ M m_neg(M a) { return cmake(-a.x, -a.y); }
+template <typename M> __device__ __forceinline__ bool m_finite(M a) {
+  return isfinite(r_to_double(a.x)) && isfinite(r_to_double(a.y));
+}
+// a / b; operands are O(1) pivots (no scaling against overflow)
+__device__ __forceinline__ double2 m_div(double2 a, double2 b) {
   const double d = b.x * b.x + b.y * b.y;
   return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
 }
-__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ dfc m_div(dfc a, dfc b) {
+  const dfl di = df_recip(b.x * b.x + b.y * b.y);
+  return cmake((a.x * b.x + a.y * b.y) * di, (a.y * b.x - a.x * b.y) * di);
+}
+template <typename R> __device__ __forceinline__ typename SmallMat<R>::M m_one() {
+  return cmake(r_const<R>(1.0f), r_const<R>(0.0f));
+}
+
+// complex FP64 helpers used outside the templated routines
+__device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) { return m_div(a, b); }
 __device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 
-// dst[e] = sum over p of partials[p*LL + e].  16 independent accumulators
-// (partial p goes to accumulator p mod 16), combined in a fixed order: the
-// loads of one round are in flight together and the result is bitwise
-// reproducible for a given nparts.
-__device__ void sm_reduce(double2* dst, const double2* __restrict__ partials, int nparts, int LL) {
+// dst[e] = sum over p of partials[p*LL + e] (complex FP64 partials).  16
+// independent accumulators (partial p goes to accumulator p mod 16), combined
+// in a fixed order: the loads of one round are in flight together and the
+// result is bitwise reproducible for a given nparts.
+template <typename R>
+__device__ void sm_reduce(typename SmallMat<R>::M* dst, const double2* __restrict__ partials, int nparts, int LL) {
   constexpr int U = 16;
   for (int e = threadIdx.x; e < LL; e += blockDim.x) {
     double2 acc[U];
@@ -54,26 +122,35 @@ __device__ void sm_reduce(double2* dst, const double2* __restrict__ partials, in
     double2 s = acc[0];
 #pragma unroll
     for (int u = 1; u < U; ++u) { s.x += acc[u].x; s.y += acc[u].y; }
-    dst[e] = s;
+    dst[e] = m_from_double2<typename SmallMat<R>::M>(s);
   }
   __syncthreads();
 }
 
-__device__ void sm_copy(double2* dst, const double2* src, int LL) {
+template <typename M> __device__ void sm_copy(M* dst, const M* src, int LL) {
   for (int e = threadIdx.x; e < LL; e += blockDim.x) dst[e] = src[e];
+  __syncthreads();
+}
+// state slot (complex FP64, global) <-> shared matrix
+template <typename M> __device__ void sm_load(M* dst, const double2* src, int LL) {
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) dst[e] = m_from_double2<M>(src[e]);
+  __syncthreads();
+}
+template <typename M> __device__ void sm_store(double2* dst, const M* src, int LL, bool negate = false) {
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) dst[e] = m_to_double2(negate ? m_neg(src[e]) : src[e]);
   __syncthreads();
 }
 
 // C = op(A) * B with op = transpose (TA=1) or identity (TA=0); C must not alias.
-__device__ void sm_matmul(double2* Cm, const double2* A, const double2* B, int L, bool TA, double2 scale = make_double2(1.0, 0.0)) {
+template <typename M> __device__ void sm_matmul(M* Cm, const M* A, const M* B, int L, bool TA) {
   for (int e = threadIdx.x; e < L * L; e += blockDim.x) {
     const int i = e % L, j = e / L;
-    double2 s = make_double2(0.0, 0.0);
+    M s = czero<M>();
     for (int k = 0; k < L; ++k) {
-      const double2 a = TA ? A[k + i * L] : A[i + k * L];
+      const M a = TA ? A[k + i * L] : A[i + k * L];
       s = cadd(s, cmul(a, B[k + j * L]));
     }
-    Cm[e] = cmul(s, scale);
+    Cm[e] = s;
   }
   __syncthreads();
 }
@@ -82,8 +159,10 @@ __device__ void sm_matmul(double2* Cm, const double2* A, const double2* B, int L
 // full=false: partial (row) pivoting on the largest |a| in the column (first
 // max); full=true: complete pivoting on the largest |a| of the trailing block,
 // first max in column-major order.  Returns false on a zero / non-finite pivot.
-__device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, int* colperm /*smem[L]*/,
-                            int* piv /*smem[2]*/, double* red_v /*smem[kSmallThreads]*/, int* red_i /*smem[kSmallThreads]*/) {
+template <typename R>
+__device__ bool sm_lu_solve(typename SmallMat<R>::M* A, typename SmallMat<R>::M* B, int L, int nrhs, bool full,
+                            int* colperm /*smem[L]*/, int* piv /*smem[2]*/) {
+  using M = typename SmallMat<R>::M;
   const int tid = threadIdx.x;
   for (int i = tid; i < L; i += blockDim.x) colperm[i] = i;
   __shared__ int bad;
@@ -91,29 +170,30 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
   __syncthreads();
   for (int k = 0; k < L; ++k) {
     // ---- pivot search by warp 0: lanes scan candidates, shuffle argmax (the
-    // largest |a|, first in column-major order on ties)
+    // largest |a|, first in column-major order on ties); |a|^2 orders the
+    // candidates as |a| does, without a square root
     if (tid < 32) {
       const int m = L - k;
       const int cnt = full ? m * m : m;
-      double best = -1.0;
+      R best = r_const<R>(-1.0f);
       int bidx = 0x7fffffff;
       for (int t = tid; t < cnt; t += 32) {
         const int ii = k + (t % m);
         const int jj = full ? k + t / m : k;
-        const double v = sqrt(cabs2(A[ii + jj * L]));
+        const R v = m_abs2(A[ii + jj * L]);
         const int lin = ii + jj * L;  // column-major order
-        if (v > best || (v == best && lin < bidx)) { best = v; bidx = lin; }
+        if (r_gt(v, best) || (r_eq(v, best) && lin < bidx)) { best = v; bidx = lin; }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const double v2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const R v2 = r_shfl_xor(best, o);
         const int i2 = __shfl_xor_sync(0xffffffffu, bidx, o);
-        if (v2 > best || (v2 == best && i2 < bidx)) { best = v2; bidx = i2; }
+        if (r_gt(v2, best) || (r_eq(v2, best) && i2 < bidx)) { best = v2; bidx = i2; }
       }
       if (tid == 0) {
         piv[0] = bidx % L;
         piv[1] = bidx / L;
-        if (!(best > 0.0) || !isfinite(best)) bad = 1;
+        if (!r_pos_finite(best)) bad = 1;
       }
     }
     __syncthreads();
@@ -121,18 +201,18 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
     // ---- row swap k <-> pr (A and B)
     if (pr != k) {
       for (int j = tid; j < L + nrhs; j += blockDim.x) {
-        double2* M = j < L ? A : B;
+        M* Mt = j < L ? A : B;
         const int jc = j < L ? j : j - L;
-        const double2 t = M[k + jc * L];
-        M[k + jc * L] = M[pr + jc * L];
-        M[pr + jc * L] = t;
+        const M t = Mt[k + jc * L];
+        Mt[k + jc * L] = Mt[pr + jc * L];
+        Mt[pr + jc * L] = t;
       }
     }
     __syncthreads();
     // ---- column swap k <-> pc (A only, record permutation)
     if (full && pc != k) {
       for (int i = tid; i < L; i += blockDim.x) {
-        const double2 t = A[i + k * L];
+        const M t = A[i + k * L];
         A[i + k * L] = A[i + pc * L];
         A[i + pc * L] = t;
       }
@@ -141,15 +221,14 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
     __syncthreads();
     if (bad) continue;
     // ---- multipliers (one complex division per row), then the trailing update
-    const double2 p = A[k + k * L];
-    const double2 pinv = cdiv(make_double2(1.0, 0.0), p);
+    const M pinv = m_div(m_one<R>(), A[k + k * L]);
     for (int i = k + 1 + tid; i < L; i += blockDim.x) A[i + k * L] = cmul(A[i + k * L], pinv);
     __syncthreads();
     const int rows = L - k - 1;
     for (int t = tid; t < rows * (L - k - 1 + nrhs); t += blockDim.x) {
       const int i = k + 1 + t % rows;
       const int jj = t / rows;  // 0..(L-k-2) -> A columns k+1.., then B columns
-      const double2 f = A[i + k * L];
+      const M f = A[i + k * L];
       if (jj < L - k - 1) {
         const int j = k + 1 + jj;
         A[i + j * L] = csub(A[i + j * L], cmul(f, A[k + j * L]));
@@ -163,11 +242,8 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
   // ---- back substitution, right-looking: row k of X is final once the rows
   // below were eliminated; then every remaining row sheds its row-k term in
   // parallel (the serial chain per row is one product per step, not L)
-  for (int k = tid; k < L; k += blockDim.x) {
-    const double2 inv = cdiv(make_double2(1.0, 0.0), A[k + k * L]);
-    A[k + k * L] = inv;  // the diagonal now holds 1 / pivot
-  }
-  __syncthreads();
+  for (int k = tid; k < L; k += blockDim.x) A[k + k * L] = m_div(m_one<R>(), A[k + k * L]);
+  __syncthreads();  // the diagonal now holds 1 / pivot
   for (int k = L - 1; k >= 0; --k) {
     for (int j = tid; j < nrhs; j += blockDim.x) B[k + j * L] = cmul(B[k + j * L], A[k + k * L]);
     __syncthreads();
@@ -178,7 +254,7 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
     __syncthreads();
   }
   if (full) {
-    // x[colperm[k]] = y[k]; use A's first column block as scratch (A no longer needed)
+    // x[colperm[k]] = y[k]; use A as scratch (A no longer needed)
     for (int e = tid; e < L * nrhs; e += blockDim.x) A[e] = B[e];
     __syncthreads();
     for (int e = tid; e < L * nrhs; e += blockDim.x) {
@@ -187,11 +263,10 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
     }
     __syncthreads();
   }
-  bool ok = !bad;
   for (int e = tid; e < L * nrhs; e += blockDim.x)
-    if (!cfinite(B[e])) bad = 1;
+    if (!m_finite(B[e])) bad = 1;
   __syncthreads();
-  ok = !bad;
+  const bool ok = !bad;
   __syncthreads();
   return ok;
 }
@@ -200,40 +275,42 @@ __device__ bool sm_lu_solve(double2* A, double2* B, int L, int nrhs, bool full, 
 // Right-looking: step k takes the square root of the (already updated)
 // diagonal, scales row k and subtracts its outer product from the trailing
 // block, every element in parallel.
-__device__ bool sm_cholesky(double2* R, const double2* H, int L) {
+template <typename R>
+__device__ bool sm_cholesky(typename SmallMat<R>::M* Rm, const typename SmallMat<R>::M* H, int L) {
+  using M = typename SmallMat<R>::M;
   __shared__ int bad;
-  __shared__ double dinv;
+  __shared__ R dinv;
   const int tid = threadIdx.x;
   if (tid == 0) bad = 0;
-  if (R != H) for (int e = tid; e < L * L; e += blockDim.x) R[e] = H[e];
+  if (Rm != H) for (int e = tid; e < L * L; e += blockDim.x) Rm[e] = H[e];
   __syncthreads();
   for (int k = 0; k < L; ++k) {
     if (tid == 0) {
-      double d = R[k + k * L].x;
-      if (!(d > 0.0) || !isfinite(d)) { bad = 1; d = 1.0; }
-      d = sqrt(d);
-      R[k + k * L] = make_double2(d, 0.0);
-      dinv = 1.0 / d;
+      R d = Rm[k + k * L].x;
+      if (!r_pos_finite(d)) { bad = 1; d = r_const<R>(1.0f); }
+      d = r_sqrt(d);
+      Rm[k + k * L] = cmake(d, r_const<R>(0.0f));
+      dinv = r_recip(d);
     }
     __syncthreads();
-    const double di = dinv;
+    const R di = dinv;
     for (int j = k + 1 + tid; j < L; j += blockDim.x) {
-      const double2 v = R[k + j * L];
-      R[k + j * L] = make_double2(v.x * di, v.y * di);
+      const M v = Rm[k + j * L];
+      Rm[k + j * L] = cmake(v.x * di, v.y * di);
     }
     __syncthreads();
     // trailing block (upper part, i <= j): H_ij -= conj(R_ki) R_kj
     const int m = L - k - 1;
     for (int t = tid; t < m * m; t += blockDim.x) {
       const int i = k + 1 + t % m, j = k + 1 + t / m;
-      if (i <= j) R[i + j * L] = csub(R[i + j * L], cconjmul(R[k + i * L], R[k + j * L]));
+      if (i <= j) Rm[i + j * L] = csub(Rm[i + j * L], cconjmul(Rm[k + i * L], Rm[k + j * L]));
     }
     __syncthreads();
   }
   // zero the strictly lower part
   for (int e = tid; e < L * L; e += blockDim.x) {
     const int i = e % L, j = e / L;
-    if (i > j) R[e] = make_double2(0.0, 0.0);
+    if (i > j) Rm[e] = czero<M>();
   }
   __syncthreads();
   const bool ok = !bad;
@@ -245,34 +322,35 @@ __device__ bool sm_cholesky(double2* R, const double2* H, int L) {
 // Cholesky factors): R X = I solved bottom-up, right-looking -- row i of X is
 // final after scaling by 1 / R_ii, then the rows above shed their row-i term,
 // all elements in parallel.
-__device__ void sm_tri_inv(double2* Ri, const double2* R, int L) {
-  __shared__ double dinv[kMaxL];
-  for (int i = threadIdx.x; i < L; i += blockDim.x) dinv[i] = 1.0 / R[i + i * L].x;
-  for (int e = threadIdx.x; e < L * L; e += blockDim.x)
-    Ri[e] = make_double2((e % L) == (e / L) ? 1.0 : 0.0, 0.0);
+template <typename R>
+__device__ void sm_tri_inv(typename SmallMat<R>::M* Ri, const typename SmallMat<R>::M* Rm, int L) {
+  using M = typename SmallMat<R>::M;
+  __shared__ R dinv[kMaxL];
+  for (int i = threadIdx.x; i < L; i += blockDim.x) dinv[i] = r_recip(Rm[i + i * L].x);
+  for (int e = threadIdx.x; e < L * L; e += blockDim.x) Ri[e] = (e % L) == (e / L) ? m_one<R>() : czero<M>();
   __syncthreads();
   for (int i = L - 1; i >= 0; --i) {
     for (int j = i + threadIdx.x; j < L; j += blockDim.x) {
-      const double2 v = Ri[i + j * L];
-      Ri[i + j * L] = make_double2(v.x * dinv[i], v.y * dinv[i]);
+      const M v = Ri[i + j * L];
+      Ri[i + j * L] = cmake(v.x * dinv[i], v.y * dinv[i]);
     }
     __syncthreads();
     // rows r < i, columns j >= i: X_rj -= R_ri X_ij
     const int nc = L - i;
     for (int t = threadIdx.x; t < i * nc; t += blockDim.x) {
       const int r = t % i, j = i + t / i;
-      Ri[r + j * L] = csub(Ri[r + j * L], cmul(R[r + i * L], Ri[i + j * L]));
+      Ri[r + j * L] = csub(Ri[r + j * L], cmul(Rm[r + i * L], Ri[i + j * L]));
     }
     __syncthreads();
   }
 }
 
-// Frobenius norm (thread 0 result broadcast through smem)
-__device__ double sm_fro(const double2* M, int LL) {
+// Frobenius norm, summed in FP64 (thread 0 result broadcast through smem)
+template <typename R> __device__ double sm_fro(const typename SmallMat<R>::M* Mm, int LL) {
   __shared__ double r;
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int e = 0; e < LL; ++e) s += cabs2(M[e]);
+    for (int e = 0; e < LL; ++e) s += cabs2(m_to_double2(Mm[e]));
     r = sqrt(s);
   }
   __syncthreads();

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/bdda.h"
@@ -70,20 +71,19 @@ __device__ __forceinline__ double2* slot(double2* st, int s, int L) { return st 
 // ---------------------------------------------------------------------------
 struct SmallSmem {
   // dynamic smem carve-up: 6 matrices + reduction scratch
-  static size_t bytes(int L) { return 6 * (size_t)L * L * sizeof(double2) + kSmallThreads * (sizeof(double) + sizeof(int)) + (2 + kMaxL) * sizeof(int); }
+  static size_t bytes(int L) { return 6 * (size_t)L * L * sizeof(double2) + (2 + kMaxL) * sizeof(int); }
 };
 
 #define SMALL_PROLOGUE                                                                              \
+  using M = typename SmallMat<R>::M;                                                                \
   extern __shared__ __align__(16) unsigned char smem_raw[];                                         \
-  double2* m0 = reinterpret_cast<double2*>(smem_raw);                                               \
-  double2* m1 = m0 + L * L;                                                                         \
-  [[maybe_unused]] double2* m2 = m1 + L * L;                                                        \
-  [[maybe_unused]] double2* m3 = m2 + L * L;                                                        \
-  [[maybe_unused]] double2* m4 = m3 + L * L;                                                        \
-  [[maybe_unused]] double2* m5 = m4 + L * L;                                                        \
-  [[maybe_unused]] double* red_v = reinterpret_cast<double*>(m5 + L * L);                           \
-  [[maybe_unused]] int* red_i = reinterpret_cast<int*>(red_v + kSmallThreads);                      \
-  [[maybe_unused]] int* piv = red_i + kSmallThreads;                                                \
+  M* m0 = reinterpret_cast<M*>(smem_raw);                                                           \
+  M* m1 = m0 + L * L;                                                                               \
+  [[maybe_unused]] M* m2 = m1 + L * L;                                                              \
+  [[maybe_unused]] M* m3 = m2 + L * L;                                                              \
+  [[maybe_unused]] M* m4 = m3 + L * L;                                                              \
+  [[maybe_unused]] M* m5 = m4 + L * L;                                                              \
+  [[maybe_unused]] int* piv = reinterpret_cast<int*>(m5 + L * L);                                   \
   [[maybe_unused]] int* colperm = piv + 2;                                                          \
   const int LL = L * L;
 
@@ -126,42 +126,81 @@ __global__ void __launch_bounds__(256) k_small_init(const double* __restrict__ v
   }
 }
 
+// Cholesky factor and its inverse of the Gram matrix in m0 (into m1, m2).
+// In double-float the matrix is first scaled by an exact power of two so that
+// its largest diagonal is O(1) (the double-float exponent range is FP32's),
+// and the factors are scaled back; FP64 factors it as it is.
+template <typename R>
+__device__ bool chol_and_inverse(typename SmallMat<R>::M* m0, typename SmallMat<R>::M* m1, typename SmallMat<R>::M* m2,
+                                 int L) {
+  if constexpr (std::is_same<R, dfl>::value) {
+    __shared__ int e2;
+    if (threadIdx.x == 0) {
+      double mx = 0.0;
+      for (int i = 0; i < L; ++i) mx = fmax(mx, fabs(r_to_double(m0[i + i * L].x)));
+      e2 = mx > 0.0 && isfinite(mx) ? ilogb(mx) / 2 : 0;  // H / 4^e2 has diagonals O(1)
+    }
+    __syncthreads();
+    const float sh = ldexpf(1.0f, -2 * e2);
+    for (int e = threadIdx.x; e < L * L; e += blockDim.x) {
+      m0[e].x = dfl(m0[e].x.hi * sh, m0[e].x.lo * sh);
+      m0[e].y = dfl(m0[e].y.hi * sh, m0[e].y.lo * sh);
+    }
+    __syncthreads();
+    if (!sm_cholesky<R>(m1, m0, L)) return false;
+    sm_tri_inv<R>(m2, m1, L);
+    const float sr = ldexpf(1.0f, e2), si = ldexpf(1.0f, -e2);  // R = R' 2^e2, R^-1 = R'^-1 2^-e2
+    for (int e = threadIdx.x; e < L * L; e += blockDim.x) {
+      m1[e].x = dfl(m1[e].x.hi * sr, m1[e].x.lo * sr);
+      m1[e].y = dfl(m1[e].y.hi * sr, m1[e].y.lo * sr);
+      m2[e].x = dfl(m2[e].x.hi * si, m2[e].x.lo * si);
+      m2[e].y = dfl(m2[e].y.hi * si, m2[e].y.lo * si);
+    }
+    __syncthreads();
+    return true;
+  } else {
+    if (!sm_cholesky<R>(m1, m0, L)) return false;
+    sm_tri_inv<R>(m2, m1, L);
+    return true;
+  }
+}
+
 // QR step 1: H = W^H W ; R1 = chol(H) ; R1inv
+template <typename R>
 __global__ void __launch_bounds__(kSmallThreads)
 k_small_chol1(const double2* __restrict__ part, int nparts, int L, double2* st, SolverCtl* ctl) {
   if (ctl_skip(ctl)) return;
   SMALL_PROLOGUE
-  sm_reduce(m0, part, nparts, LL);
-  if (!sm_cholesky(m1, m0, L)) { fail(ctl); return; }
-  sm_tri_inv(m2, m1, L);
-  sm_copy(slot(st, kR1, L), m1, LL);
-  sm_copy(slot(st, kR1Inv, L), m2, LL);
+  sm_reduce<R>(m0, part, nparts, LL);
+  if (!chol_and_inverse<R>(m0, m1, m2, L)) { fail(ctl); return; }
+  sm_store(slot(st, kR1, L), m1, LL);
+  sm_store(slot(st, kR1Inv, L), m2, LL);
 }
 
 // QR step 2: H2 = W1^H W1 ; R2 = chol ; R2inv ; tau = R2 R1.
 // mode 0: xi = tau (initial QR of the right-hand side)
 // mode 1: xi = tau xi ; err = ||xi|| / bnorm ; stopping test
 // mode 2: like mode 0 but R = tau returned in kXi only (qr_reduced)
+template <typename R>
 __global__ void __launch_bounds__(kSmallThreads)
 k_small_chol2(const double2* __restrict__ part, int nparts, int L, double2* st, SolverCtl* ctl, double tol,
               double* hist, int k, int mode) {
   if (ctl_skip(ctl)) return;
   SMALL_PROLOGUE
-  sm_reduce(m0, part, nparts, LL);
-  if (!sm_cholesky(m1, m0, L)) { fail(ctl); return; }
-  sm_tri_inv(m2, m1, L);
-  sm_copy(slot(st, kR2Inv, L), m2, LL);
-  sm_copy(m3, slot(st, kR1, L), LL);
+  sm_reduce<R>(m0, part, nparts, LL);
+  if (!chol_and_inverse<R>(m0, m1, m2, L)) { fail(ctl); return; }
+  sm_store(slot(st, kR2Inv, L), m2, LL);
+  sm_load(m3, slot(st, kR1, L), LL);
   sm_matmul(m4, m1, m3, L, false);  // tau = R2 R1
-  sm_copy(slot(st, kTau, L), m4, LL);
+  sm_store(slot(st, kTau, L), m4, LL);
   if (mode != 1) {
-    sm_copy(slot(st, kXi, L), m4, LL);
+    sm_store(slot(st, kXi, L), m4, LL);
     return;
   }
-  sm_copy(m5, slot(st, kXi, L), LL);
+  sm_load(m5, slot(st, kXi, L), LL);
   sm_matmul(m0, m4, m5, L, false);  // xi = tau xi
-  sm_copy(slot(st, kXi, L), m0, LL);
-  const double nrm = sm_fro(m0, LL);
+  sm_store(slot(st, kXi, L), m0, LL);
+  const double nrm = sm_fro<R>(m0, LL);
   if (threadIdx.x == 0) {
     const double err = nrm / ctl->bnorm;
     ctl->err = err;
@@ -173,59 +212,62 @@ k_small_chol2(const double2* __restrict__ part, int nparts, int L, double2* st, 
 }
 
 // COCG-RQ alpha: alpha = (S^T AS)^-1 (Q^T Q) ; A_xi = alpha xi ; -alpha
+template <typename R>
 __global__ void __launch_bounds__(kSmallThreads)
 k_small_cocg_alpha(const double2* __restrict__ pSAS, const double2* __restrict__ pQQ, int nparts, int L, double2* st,
                    SolverCtl* ctl, int full) {
   if (ctl_skip(ctl)) return;
   SMALL_PROLOGUE
-  sm_reduce(m0, pSAS, nparts, LL);
+  sm_reduce<R>(m0, pSAS, nparts, LL);
   if (pQQ) {
-    sm_reduce(m1, pQQ, nparts, LL);
-    sm_copy(slot(st, kQtQ, L), m1, LL);
+    sm_reduce<R>(m1, pQQ, nparts, LL);
+    sm_store(slot(st, kQtQ, L), m1, LL);
   } else {
-    sm_copy(m1, slot(st, kQtQ, L), LL);
+    sm_load(m1, slot(st, kQtQ, L), LL);
   }
-  if (!sm_lu_solve(m0, m1, L, L, full != 0, colperm, piv, red_v, red_i)) { fail(ctl); return; }
-  sm_copy(slot(st, kAlpha, L), m1, LL);
-  for (int e = threadIdx.x; e < LL; e += blockDim.x) slot(st, kNAlpha, L)[e] = make_double2(-m1[e].x, -m1[e].y);
-  sm_copy(m2, slot(st, kXi, L), LL);
+  if (!sm_lu_solve<R>(m0, m1, L, L, full != 0, colperm, piv)) { fail(ctl); return; }
+  sm_store(slot(st, kAlpha, L), m1, LL);
+  sm_store(slot(st, kNAlpha, L), m1, LL, true);
+  sm_load(m2, slot(st, kXi, L), LL);
   sm_matmul(m3, m1, m2, L, false);
-  sm_copy(slot(st, kAXi, L), m3, LL);
+  sm_store(slot(st, kAXi, L), m3, LL);
 }
 
 // COCG-RQ beta: beta = (Q^T Q)^-1 (tau^T Q'^T Q') ; Q^T Q <- Q'^T Q'
+template <typename R>
 __global__ void __launch_bounds__(kSmallThreads)
 k_small_cocg_beta(const double2* __restrict__ pQQn, int nparts, int L, double2* st, SolverCtl* ctl, int full) {
   if (ctl_skip(ctl)) return;
   SMALL_PROLOGUE
-  sm_reduce(m0, pQQn, nparts, LL);           // Q'^T Q'
-  sm_copy(m1, slot(st, kTau, L), LL);
+  sm_reduce<R>(m0, pQQn, nparts, LL);        // Q'^T Q'
+  sm_load(m1, slot(st, kTau, L), LL);
   sm_matmul(m2, m1, m0, L, true);            // tau^T Q'^T Q'
-  sm_copy(m3, slot(st, kQtQ, L), LL);
-  if (!sm_lu_solve(m3, m2, L, L, full != 0, colperm, piv, red_v, red_i)) { fail(ctl); return; }
-  sm_copy(slot(st, kBeta, L), m2, LL);
-  sm_copy(slot(st, kQtQ, L), m0, LL);
+  sm_load(m3, slot(st, kQtQ, L), LL);
+  if (!sm_lu_solve<R>(m3, m2, L, L, full != 0, colperm, piv)) { fail(ctl); return; }
+  sm_store(slot(st, kBeta, L), m2, LL);
+  sm_store(slot(st, kQtQ, L), m0, LL);
 }
 
 // BiCG*: X = M^-1 RHS with M = reduce(pM) (stored in kM), RHS = scale * reduce(pR).
 // out slots: x -> so, -x -> sno (optional)
+template <typename R>
 __global__ void __launch_bounds__(kSmallThreads)
 k_small_solve(const double2* __restrict__ pM, const double2* __restrict__ pR, int nparts, int L, double2* st,
               SolverCtl* ctl, int mslot_in, int mslot_store, double rhs_scale, const double2* scal_div, int so, int sno) {
   if (ctl_skip(ctl)) return;
   SMALL_PROLOGUE
-  if (pM) sm_reduce(m0, pM, nparts, LL);
-  else sm_copy(m0, slot(st, mslot_in, L), LL);
-  if (mslot_store >= 0) sm_copy(slot(st, mslot_store, L), m0, LL);
-  sm_reduce(m1, pR, nparts, LL);
+  if (pM) sm_reduce<R>(m0, pM, nparts, LL);
+  else sm_load(m0, slot(st, mslot_in, L), LL);
+  if (mslot_store >= 0) sm_store(slot(st, mslot_store, L), m0, LL);
+  sm_reduce<R>(m1, pR, nparts, LL);
   double2 sc = make_double2(rhs_scale, 0.0);
   if (scal_div) sc = cdiv(sc, *scal_div);
-  for (int e = threadIdx.x; e < LL; e += blockDim.x) m1[e] = cmul(m1[e], sc);
+  const M scm = m_from_double2<M>(sc);
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) m1[e] = cmul(m1[e], scm);
   __syncthreads();
-  if (!sm_lu_solve(m0, m1, L, L, false, colperm, piv, red_v, red_i)) { fail(ctl); return; }
-  sm_copy(slot(st, so, L), m1, LL);
-  if (sno >= 0)
-    for (int e = threadIdx.x; e < LL; e += blockDim.x) slot(st, sno, L)[e] = make_double2(-m1[e].x, -m1[e].y);
+  if (!sm_lu_solve<R>(m0, m1, L, L, false, colperm, piv)) { fail(ctl); return; }
+  sm_store(slot(st, so, L), m1, LL);
+  if (sno >= 0) sm_store(slot(st, sno, L), m1, LL, true);
 }
 
 // zeta = sum(p1) / sum(p2) ; kZetaI = zeta I ; kNZetaI = -zeta I ; scal[0] = zeta, scal[1] = -zeta
@@ -272,7 +314,7 @@ __global__ void __launch_bounds__(256) k_small_err(const double* __restrict__ vp
 __global__ void __launch_bounds__(kSmallThreads)
 k_small_store_reduce(const double2* __restrict__ part, int nparts, int L, double2* st, SolverCtl* ctl, int s) {
   if (ctl_skip(ctl)) return;
-  sm_reduce(slot(st, s, L), part, nparts, L * L);
+  sm_reduce<double>(slot(st, s, L), part, nparts, L * L);
 }
 
 // ---------------------------------------------------------------------------
@@ -281,6 +323,12 @@ k_small_store_reduce(const double2* __restrict__ part, int nparts, int L, double
 template <typename T>
 struct Krylov {
   using C = typename cplx<T>::type;
+  // Arithmetic of the L x L steps of COCG-RQ and CholQR2, whose Gram matrices
+  // are of orthonormalised blocks (O(1) entries): FP64 for FP64 solves,
+  // double-float for the FP32 inner solves.  The BiCG* steps solve with
+  // unnormalised Grams whose entries shrink with the residual (their squares
+  // can leave the FP32 exponent range) and stay FP64.
+  using SR = typename std::conditional<std::is_same<T, float>::value, dfl, double>::type;
   Op* op;
   SolverWork* w;
   cudaStream_t st;
@@ -357,10 +405,10 @@ struct Krylov {
   void cholqr2(const C* A, C* W, C* Q, int mode) {
     double2* p = w->partials.template as<double2>();
     gram<true>(A, A, p);
-    small_launch(k_small_chol1, (const double2*)p, 1, L, small(), ctl());
+    small_launch(k_small_chol1<SR>, (const double2*)p, 1, L, small(), ctl());
     rowmm(A, sl(kR1Inv), nullptr, nullptr, nullptr, W);
     gram<true>(W, W, p);
-    small_launch(k_small_chol2, (const double2*)p, 1, L, small(), ctl(), 0.0, (double*)nullptr, 0, mode);
+    small_launch(k_small_chol2<SR>, (const double2*)p, 1, L, small(), ctl(), 0.0, (double*)nullptr, 0, mode);
     rowmm(W, sl(kR2Inv), nullptr, nullptr, nullptr, Q);
   }
 
@@ -379,18 +427,18 @@ struct Krylov {
       BDDA_TRY(mvp(S, AS));
       gram<false>(S, AS, p);
       if (k == 0) gram<false>(Q, Q, p2);
-      small_launch(k_small_cocg_alpha, (const double2*)p, (const double2*)(k == 0 ? p2 : nullptr), 1, L, small(), ctl(),
+      small_launch(k_small_cocg_alpha<SR>, (const double2*)p, (const double2*)(k == 0 ? p2 : nullptr), 1, L, small(), ctl(),
                    (int)full);
       rowmm(S, sl(kAXi), nullptr, nullptr, X, X);           // X += S alpha xi
       rowmm(AS, sl(kNAlpha), nullptr, nullptr, Q, W);       // W = Q - AS alpha
       gram<true>(W, W, p);
-      small_launch(k_small_chol1, (const double2*)p, 1, L, small(), ctl());
+      small_launch(k_small_chol1<SR>, (const double2*)p, 1, L, small(), ctl());
       rowmm(W, sl(kR1Inv), nullptr, nullptr, nullptr, W);
       gram<true>(W, W, p);
-      small_launch(k_small_chol2, (const double2*)p, 1, L, small(), ctl(), tol, w->hist.as<double>(), k, 1);
+      small_launch(k_small_chol2<SR>, (const double2*)p, 1, L, small(), ctl(), tol, w->hist.as<double>(), k, 1);
       rowmm(W, sl(kR2Inv), nullptr, nullptr, nullptr, Qn);  // Q'
       gram<false>(Qn, Qn, p);
-      small_launch(k_small_cocg_beta, (const double2*)p, 1, L, small(), ctl(), (int)full);
+      small_launch(k_small_cocg_beta<SR>, (const double2*)p, 1, L, small(), ctl(), (int)full);
       rowmm(S, sl(kBeta), nullptr, nullptr, Qn, S);         // S = Q' + S beta
       std::swap(Q, Qn);
       if ((k + 1) % check_every == 0 || k + 1 == itermax) {
@@ -424,7 +472,7 @@ struct Krylov {
       BDDA_TRY(mvp(P, V));                                   // V = A P
       gram<true>(R0, V, p);
       gram<true>(R0, R, p2);
-      small_launch(k_small_solve, (const double2*)p, (const double2*)p2, 1, L, small(), ctl(), 0, (int)kM, 1.0,
+      small_launch(k_small_solve<double>, (const double2*)p, (const double2*)p2, 1, L, small(), ctl(), 0, (int)kM, 1.0,
                    (const double2*)nullptr, (int)kAlpha, (int)kNAlpha);
       rowmm(V, sl(kNAlpha), nullptr, nullptr, R, Tm);        // T = R - V alpha
       BDDA_TRY(mvp(Tm, Z));                                  // Z = A T
@@ -440,7 +488,7 @@ struct Krylov {
       k_small_err<<<1, 256, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
       op->timer.end(kSmall, st);
       gram<true>(R0, Z, p);
-      small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, 1, L, small(), ctl(), (int)kM, -1, -1.0,
+      small_launch(k_small_solve<double>, (const double2*)nullptr, (const double2*)p, 1, L, small(), ctl(), (int)kM, -1, -1.0,
                    (const double2*)nullptr, (int)kBeta, -1);  // beta = M^-1 (-R0^H Z)
       axpby(nullptr, P, scal + 1, V, Pt);                    // Pt = P - zeta V
       rowmm(Pt, sl(kBeta), nullptr, nullptr, R, P);          // P = R + Pt beta
@@ -476,7 +524,7 @@ struct Krylov {
     for (; k < itermax; ++k) {
       gram<true>(R0, V, p);
       gram<true>(R0, R, p2);
-      small_launch(k_small_solve, (const double2*)p, (const double2*)p2, 1, L, small(), ctl(), 0, -1, 1.0,
+      small_launch(k_small_solve<double>, (const double2*)p, (const double2*)p2, 1, L, small(), ctl(), 0, -1, 1.0,
                    (const double2*)nullptr, (int)kAlpha, -1);
       // keep R0^H R (old R) for gamma
       small_launch(k_small_store_reduce, (const double2*)p2, 1, L, small(), ctl(), (int)kM2);
@@ -496,7 +544,7 @@ struct Krylov {
       op->timer.end(kSmall, st);
       BDDA_TRY(mvp(Rn, Wm));                                 // W = A Rnew
       gram<true>(R0, Rn, p);
-      small_launch(k_small_solve, (const double2*)nullptr, (const double2*)p, 1, L, small(), ctl(), (int)kM2, -1, 1.0,
+      small_launch(k_small_solve<double>, (const double2*)nullptr, (const double2*)p, 1, L, small(), ctl(), (int)kM2, -1, 1.0,
                    (const double2*)scal, (int)kBeta, -1);    // gamma = (R0^H R)^-1 (R0^H Rnew / zeta)
       std::swap(R, Rn);
       rowmm(U, sl(kBeta), nullptr, nullptr, R, P);           // P = R + U gamma
@@ -567,11 +615,15 @@ static int ensure_work(Op* op, int n, int L, int itermax, bool need64, bool need
       if (e != cudaSuccess) attr_err = e;
     };
     const int mx = (int)SmallSmem::bytes(kMaxL);
-    set((const void*)k_small_chol1, mx);
-    set((const void*)k_small_chol2, mx);
-    set((const void*)k_small_cocg_alpha, mx);
-    set((const void*)k_small_cocg_beta, mx);
-    set((const void*)k_small_solve, mx);
+    set((const void*)k_small_chol1<double>, mx);
+    set((const void*)k_small_chol2<double>, mx);
+    set((const void*)k_small_cocg_alpha<double>, mx);
+    set((const void*)k_small_cocg_beta<double>, mx);
+    set((const void*)k_small_solve<double>, mx);
+    set((const void*)k_small_chol1<dfl>, mx);
+    set((const void*)k_small_chol2<dfl>, mx);
+    set((const void*)k_small_cocg_alpha<dfl>, mx);
+    set((const void*)k_small_cocg_beta<dfl>, mx);
     set((const void*)k_small_store_reduce, mx);
     set((const void*)k_rowmm<double>, rowmm_smem<double>(kMaxL, true));
     set((const void*)k_rowmm<float>, rowmm_smem<float>(kMaxL, true));
