@@ -29,26 +29,42 @@ __device__ __forceinline__ bool ctl_skip(const SolverCtl* ctl) {
   return ctl != nullptr && *(volatile const int*)&ctl->done != 0;
 }
 
+// Gram partial sums: complex FP64 for FP64 blocks; double-float (FP32
+// instructions only -- GB300 runs FP64 at a small fraction of its FP32 rate)
+// for FP32 blocks.
+template <typename T> struct GramPart { using type = double2; };
+template <> struct GramPart<float> { using type = dfc; };
+__device__ __forceinline__ void gp_zero(double2& a) { a = make_double2(0.0, 0.0); }
+__device__ __forceinline__ void gp_zero(dfc& a) { a.x = dfl(0.0f, 0.0f); a.y = dfl(0.0f, 0.0f); }
+__device__ __forceinline__ void gp_add(double2& a, double2 b) { a.x += b.x; a.y += b.y; }
+__device__ __forceinline__ void gp_add(double2& a, float2 b) { a.x += (double)b.x; a.y += (double)b.y; }
+__device__ __forceinline__ void gp_add(dfc& a, dfc b) { a.x = a.x + b.x; a.y = a.y + b.y; }
+__device__ __forceinline__ void gp_add(dfc& a, float2 b) { a.x = a.x + dfl(b.x, 0.0f); a.y = a.y + dfl(b.y, 0.0f); }
+__device__ __forceinline__ double2 gp_d2(double2 a) { return a; }
+__device__ __forceinline__ double2 gp_d2(dfc a) { return make_double2(df_to_double(a.x), df_to_double(a.y)); }
+
 // ---------------------------------------------------------------------------
 // Gram partials: partials[blk][i + j*L] = sum_{r in chunk} op(A[r,i]) B[r,j]
 // Each CTA owns a contiguous row chunk; FP32 data is multiplied in FP32 and
-// summed in FP32 over one 32-row sub-tile, then added to FP64 accumulators.
+// summed in FP32 over one 32-row sub-tile, then added to double-float
+// accumulators (FP64 data: FP64 throughout).
 // ---------------------------------------------------------------------------
 template <typename T, bool CONJ>
 __global__ void __launch_bounds__(kGramThreads)
 k_gram(const typename cplx<T>::type* __restrict__ A, int lda,
        const typename cplx<T>::type* __restrict__ B, int ldb,
-       int n, int L, double2* __restrict__ partials, const SolverCtl* ctl) {
+       int n, int L, typename GramPart<T>::type* __restrict__ partials, const SolverCtl* ctl) {
   using C = typename cplx<T>::type;
+  using P = typename GramPart<T>::type;
   if (ctl_skip(ctl)) return;
   __shared__ C sa[kMaxL][kGramRows + 1];
   __shared__ C sb[kMaxL][kGramRows + 1];
   const int tid = threadIdx.x;
   const int LL = L * L;
   // entries owned by this thread: e = tid + k*256, k < 4  (L <= 32 -> LL <= 1024)
-  double2 acc[4];
+  P acc[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) acc[k] = make_double2(0.0, 0.0);
+  for (int k = 0; k < 4; ++k) gp_zero(acc[k]);
   const long long rows_per = ((long long)n + gridDim.x - 1) / gridDim.x;
   const long long r0 = (long long)blockIdx.x * rows_per;
   const long long r1 = min((long long)n, r0 + rows_per);
@@ -76,8 +92,7 @@ k_gram(const typename cplx<T>::type* __restrict__ A, int lda,
           const C a = sa[i][rr], b = sb[j][rr];
           s = CONJ ? cadd(s, cconjmul(a, b)) : cadd(s, cmul(a, b));
         }
-        acc[k].x += (double)s.x;
-        acc[k].y += (double)s.y;
+        gp_add(acc[k], s);
       }
     }
   }
@@ -88,41 +103,42 @@ k_gram(const typename cplx<T>::type* __restrict__ A, int lda,
   }
 }
 
-// out[e] = sum over p of part[p*LL + e], spread over ceil(LL/64) CTAs: thread
-// group g (of 4) sums p = g, g+4, ... with four independent accumulators;
-// the groups are combined in a fixed order (deterministic).
+// out[e] = sum over p of part[p*LL + e] (complex FP64 out), spread over
+// ceil(LL/64) CTAs: thread group g (of 4) sums p = g, g+4, ... with four
+// independent accumulators; the groups are combined in a fixed order
+// (deterministic).  Sums in the partials' arithmetic (FP64 or double-float).
+template <typename P>
 __global__ void __launch_bounds__(256)
-k_gram_reduce(const double2* __restrict__ part, int nparts, int LL, double2* __restrict__ out, const SolverCtl* ctl) {
+k_gram_reduce(const P* __restrict__ part, int nparts, int LL, double2* __restrict__ out, const SolverCtl* ctl) {
   if (ctl_skip(ctl)) return;
-  __shared__ double2 red[4][64];
+  __shared__ P red[4][64];
   const int el = threadIdx.x & 63, g = threadIdx.x >> 6;
   const int e = blockIdx.x * 64 + el;
-  double2 acc[4];
+  P acc[4];
 #pragma unroll
-  for (int u = 0; u < 4; ++u) acc[u] = make_double2(0.0, 0.0);
+  for (int u = 0; u < 4; ++u) gp_zero(acc[u]);
   if (e < LL) {
     int p = g, u = 0;
     for (; p + 12 < nparts; p += 16) {
-      const double2 v0 = __ldg(part + (size_t)p * LL + e), v1 = __ldg(part + (size_t)(p + 4) * LL + e);
-      const double2 v2 = __ldg(part + (size_t)(p + 8) * LL + e), v3 = __ldg(part + (size_t)(p + 12) * LL + e);
-      acc[0].x += v0.x; acc[0].y += v0.y;
-      acc[1].x += v1.x; acc[1].y += v1.y;
-      acc[2].x += v2.x; acc[2].y += v2.y;
-      acc[3].x += v3.x; acc[3].y += v3.y;
+      const P v0 = part[(size_t)p * LL + e], v1 = part[(size_t)(p + 4) * LL + e];
+      const P v2 = part[(size_t)(p + 8) * LL + e], v3 = part[(size_t)(p + 12) * LL + e];
+      gp_add(acc[0], v0);
+      gp_add(acc[1], v1);
+      gp_add(acc[2], v2);
+      gp_add(acc[3], v3);
     }
-    for (; p < nparts; p += 4, ++u) {
-      const double2 v = __ldg(part + (size_t)p * LL + e);
-      acc[u & 3].x += v.x;
-      acc[u & 3].y += v.y;
-    }
+    for (; p < nparts; p += 4, ++u) gp_add(acc[u & 3], part[(size_t)p * LL + e]);
   }
-  red[g][el] = make_double2(acc[0].x + acc[1].x + acc[2].x + acc[3].x, acc[0].y + acc[1].y + acc[2].y + acc[3].y);
+  gp_add(acc[0], acc[1]);
+  gp_add(acc[2], acc[3]);
+  gp_add(acc[0], acc[2]);
+  red[g][el] = acc[0];
   __syncthreads();
   if (g == 0 && e < LL) {
-    double2 s = red[0][el];
+    P s = red[0][el];
 #pragma unroll
-    for (int k = 1; k < 4; ++k) { s.x += red[k][el].x; s.y += red[k][el].y; }
-    out[e] = s;
+    for (int k = 1; k < 4; ++k) gp_add(s, red[k][el]);
+    out[e] = gp_d2(s);
   }
 }
 

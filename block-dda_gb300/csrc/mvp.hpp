@@ -43,6 +43,7 @@ template <typename T> struct MvpPrec {
   const C* twy;
   const C* twz;
   const C* ghat;  // [Px][Py][6 or 9][Pz] (digit-reversed frequencies), divided by Px*Py*Pz
+  const float4* twzp = nullptr;  // complex FP32: z twiddle pairs {wx, wx, wy, wy} (packed kernels)
 };
 
 // Timed kernel classes: the five MVP passes per precision (FP32 first), then
@@ -139,9 +140,11 @@ enum TilePass { kTileA = 0, kTileB, kTileD, kTileE };
 bool launch_tile_static(int pass, const TileArgs& a, cudaError_t* err);
 
 // Pass C for complex FP32 with the compile-time z plan of g.Pz (zplans.inc);
-// returns false (nothing launched) when g.Pz has none.  *err: launch status.
-bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2* ghat, cudaStream_t st,
-                          const int* done, cudaError_t* err);
+// returns false (nothing launched) when g.Pz has none.  With twzp (the z
+// twiddle pair table {wx, wx, wy, wy}) and f = 3 the packed-pair kernel runs.
+// *err: launch status.
+bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz, const float4* twzp, const float2* ghat,
+                          cudaStream_t st, const int* done, cudaError_t* err);
 
 // Green tensor: build Ghat (FP64 evaluation + FP64 3-D FFT), layout
 // [Px][Py][nc][Pz] with nc = 6 (g.f = 3) or 9 (g.f = 6), for any of the

@@ -152,7 +152,7 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
     bool launched = false;
     if constexpr (std::is_same<T, float>::value) {
       cudaError_t e = cudaSuccess;
-      launched = launch_pass_c_static(g, t2, L, p.twz, p.ghat, st, done, &e);
+      launched = launch_pass_c_static(g, t2, L, p.twz, p.twzp, p.ghat, st, done, &e);
       if (launched && e != cudaSuccess) return e;
     }
     if (!launched) {

@@ -1,5 +1,6 @@
 // Operator lifecycle and MVP entry points of the C ABI.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -80,7 +81,7 @@ Op::~Op() {
   // release every stream-ordered buffer on the operator's stream before it goes away
   solver.reset();
   for (auto* o : {&dip, &cub}) { o->occ.release(); o->tiles.release(); o->tmask.release(); }
-  for (int i = 0; i < 3; ++i) { tw64[i].release(); tw32[i].release(); twdf[i].release(); }
+  for (int i = 0; i < 3; ++i) { tw64[i].release(); tw32[i].release(); twdf[i].release(); tw32p[i].release(); }
   ghat64.release(); ghat32.release(); ghatdf.release();
   for (int i = 0; i < 3; ++i) { t1[i].release(); t2[i].release(); }
   if (stream) {
@@ -248,6 +249,12 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     for (size_t t = 0; t < tw.size(); ++t) tf[t] = make_float2((float)tw[t].x, (float)tw[t].y);
     BDDA_CUDA(op->tw32[i].ensure(tf.size() * sizeof(float2), op->stream));
     BDDA_CUDA(cudaMemcpyAsync(op->tw32[i].p, tf.data(), tf.size() * sizeof(float2), cudaMemcpyHostToDevice, op->stream));
+    std::vector<float4> tp(tw.size());
+    for (size_t t = 0; t < tw.size(); ++t) tp[t] = make_float4(tf[t].x, tf[t].x, tf[t].y, tf[t].y);
+    if (!std::getenv("BDDA_NO_PACK")) {
+      BDDA_CUDA(op->tw32p[i].ensure(tp.size() * sizeof(float4), op->stream));
+      BDDA_CUDA(cudaMemcpyAsync(op->tw32p[i].p, tp.data(), tp.size() * sizeof(float4), cudaMemcpyHostToDevice, op->stream));
+    }
     std::vector<dfc> td(tw.size());
     for (size_t t = 0; t < tw.size(); ++t) td[t] = cmake(dfl(tw[t].x), dfl(tw[t].y));
     BDDA_CUDA(op->twdf[i].ensure(td.size() * sizeof(dfc), op->stream));

@@ -100,6 +100,11 @@ __device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isf
 template <typename R>
 __device__ void sm_reduce(typename SmallMat<R>::M* dst, const double2* __restrict__ partials, int nparts, int LL) {
   constexpr int U = 16;
+  if (nparts == 1) {  // an already reduced matrix: convert only (FP64 adds are scarce on GB300)
+    for (int e = threadIdx.x; e < LL; e += blockDim.x) dst[e] = m_from_double2<typename SmallMat<R>::M>(__ldg(partials + e));
+    __syncthreads();
+    return;
+  }
   for (int e = threadIdx.x; e < LL; e += blockDim.x) {
     double2 acc[U];
 #pragma unroll
@@ -345,13 +350,21 @@ __device__ void sm_tri_inv(typename SmallMat<R>::M* Ri, const typename SmallMat<
   }
 }
 
-// Frobenius norm, summed in FP64 (thread 0 result broadcast through smem)
+// Frobenius norm in FP64 (any scale): per-thread sums of |m|^2, a warp
+// shuffle tree, then the warps' sums in order (deterministic).
 template <typename R> __device__ double sm_fro(const typename SmallMat<R>::M* Mm, int LL) {
+  __shared__ double wsum[kSmallThreads / 32];
   __shared__ double r;
+  double s = 0.0;
+  for (int e = threadIdx.x; e < LL; e += blockDim.x) s += cabs2(m_to_double2(Mm[e]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = s;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int e = 0; e < LL; ++e) s += cabs2(m_to_double2(Mm[e]));
-    r = sqrt(s);
+    double t = wsum[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+    r = sqrt(t);
   }
   __syncthreads();
   const double v = r;

@@ -135,10 +135,11 @@ __device__ bool chol_and_inverse(typename SmallMat<R>::M* m0, typename SmallMat<
                                  int L) {
   if constexpr (std::is_same<R, dfl>::value) {
     __shared__ int e2;
-    if (threadIdx.x == 0) {
-      double mx = 0.0;
-      for (int i = 0; i < L; ++i) mx = fmax(mx, fabs(r_to_double(m0[i + i * L].x)));
-      e2 = mx > 0.0 && isfinite(mx) ? ilogb(mx) / 2 : 0;  // H / 4^e2 has diagonals O(1)
+    if (threadIdx.x < 32) {  // largest diagonal (leading parts), one warp, FP32
+      float mx = threadIdx.x < L ? fabsf(m0[threadIdx.x * (L + 1)].x.hi) : 0.0f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (threadIdx.x == 0) e2 = mx > 0.0f && isfinite(mx) ? ilogbf(mx) / 2 : 0;  // H / 4^e2 has diagonals O(1)
     }
     __syncthreads();
     const float sh = ldexpf(1.0f, -2 * e2);
@@ -351,8 +352,9 @@ struct Krylov {
   // out = op(A)^T B (L x L, FP64): per-CTA partials, then a multi-CTA ordered reduction
   template <bool CONJ> void gram(const C* A, const C* B, double2* out) {
     op->timer.begin(kGram, st);
-    k_gram<T, CONJ><<<G(), kGramThreads, 0, st>>>(A, n, B, n, n, L, w->gpart.template as<double2>(), ctl());
-    k_gram_reduce<<<(L * L + 63) / 64, 256, 0, st>>>(w->gpart.template as<double2>(), G(), L * L, out, ctl());
+    using P = typename GramPart<T>::type;
+    k_gram<T, CONJ><<<G(), kGramThreads, 0, st>>>(A, n, B, n, n, L, w->gpart.template as<P>(), ctl());
+    k_gram_reduce<P><<<(L * L + 63) / 64, 256, 0, st>>>(w->gpart.template as<P>(), G(), L * L, out, ctl());
     op->timer.end(kGram, st);
     op->timer.count(kGram);
   }

@@ -4,6 +4,7 @@
 #pragma once
 
 #include "tile_static.cuh"
+#include "zpass_packed.cuh"
 #include "zpass_static.cuh"
 
 namespace bdda {
@@ -12,13 +13,15 @@ namespace sparts {
 constexpr int kParts = 4;
 
 template <int PART>
-bool dispatch_z(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2* ghat, cudaStream_t st,
-                const int* done, cudaError_t* err) {
+bool dispatch_z(const MvpGeom& g, float2* t2, int L, const float2* twz, const float4* twzp, const float2* ghat,
+                cudaStream_t st, const int* done, cudaError_t* err) {
   switch (g.Pz) {
 #define BDDA_ZPLAN(I, N, S, LW, ...)                                                     \
   case N:                                                                                \
     if constexpr ((I) % kParts == PART) {                                                \
-      *err = zstatic::launch<sfft::Plan<N, S, LW, __VA_ARGS__>>(g, t2, L, twz, ghat, st, done); \
+      using Pl = sfft::Plan<N, S, LW, __VA_ARGS__>;                                      \
+      *err = (twzp && g.f == 3) ? zpacked::launch<Pl>(g, t2, L, twzp, ghat, st, done)    \
+                                : zstatic::launch<Pl>(g, t2, L, twz, ghat, st, done);    \
       return true;                                                                       \
     }                                                                                    \
     return false;
