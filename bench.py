@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--m", default="2.3+0.6j")
     ap.add_argument("--wl0", type=float, default=0.55)
     ap.add_argument("--solver", default="cocg_rq")
+    ap.add_argument("--no-jacobi", action="store_true", help="unpreconditioned solver (default: Jacobi-preconditioned)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
     ap.add_argument("--workload", default="single", choices=["single", "batched", "serving"],
@@ -79,11 +80,14 @@ def dist_env():
 
 
 def workload_config(a, n=None, P=None):
-    cfg = {"workload": f"block COCG-RQ-Jacobi solve, N={a.nocc} dipole lattice aggregate (kf=1.0, Df=2.8, seed=1+rank), "
+    pre = "" if getattr(a, "no_jacobi", False) else "-Jacobi"
+    name = {"cocg_rq": "COCG-RQ", "bicgstab": "BiCGSTAB", "bicggr": "BiCGGR"}.get(a.solver, a.solver)
+    cfg = {"workload": f"block {name}{pre} solve, N={a.nocc} dipole lattice aggregate (kf=1.0, Df=2.8, seed=1+rank), "
                        f"m={a.m}, lambda={a.wl0} um, |m|kd=0.5, nrhs={a.nrhs}, true residual <= 1e-8",
            "nocc": a.nocc, "nrhs": a.nrhs, "m": a.m, "wl0_um": a.wl0, "tol": 1e-8,
            "precision": "complex FP32 Krylov + FFT-MVP inside FP64 refinement",
-           "solver": a.solver, "jacobi": True, "l2": "working set > L2 (FFT workspace ~0.7 GB)",
+           "solver": a.solver, "jacobi": not getattr(a, "no_jacobi", False),
+           "l2": "working set > L2 (FFT workspace ~0.7 GB)",
            "parallelism": "replicas (one independent target per GPU)"}
     if n is not None:
         cfg["box"] = list(n)
@@ -231,7 +235,7 @@ def run_ours(a):
     diag_d = torch.from_numpy(prob.diag).to(dev)
     B_d = torch.from_numpy(np.ascontiguousarray(prob.B.T)).to(dev)       # (L, n) = column-major n x L
     X_d = torch.zeros_like(B_d)
-    opts = bdda.solve_opts(a.solver, jacobi=True, precision=bdda.SOLVE_MIXED, true_tol=1e-8, itermax=3000)
+    opts = bdda.solve_opts(a.solver, jacobi=not a.no_jacobi, precision=bdda.SOLVE_MIXED, true_tol=1e-8, itermax=3000)
 
     def step():
         return bdda.solve_device(op, diag_d.data_ptr(), B_d.data_ptr(), n, X_d.data_ptr(), n, L, opts,
@@ -324,7 +328,7 @@ def run_ours(a):
     fp64 = None
     ref_iters = None
     if not a.no_fp64:
-        o64 = bdda.solve_opts(a.solver, jacobi=True, precision=bdda.SOLVE_FP64, true_tol=1e-8, itermax=3000)
+        o64 = bdda.solve_opts(a.solver, jacobi=not a.no_jacobi, precision=bdda.SOLVE_FP64, true_tol=1e-8, itermax=3000)
         s64 = bdda.solve_device(op, diag_d.data_ptr(), B_d.data_ptr(), n, X_d.data_ptr(), n, L, o64,
                                 stream=stream.cuda_stream)
         torch.cuda.synchronize()
@@ -338,7 +342,7 @@ def run_ours(a):
         ms64 = ev0.elapsed_time(ev1)
         fp64 = {"value": L / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64, "iterations": s64["iterations"],
                 "true_res_max": s64["true_res_max"]}
-        oref = bdda.solve_opts(a.solver, jacobi=True, precision=bdda.SOLVE_FP64, tol=1e-8, itermax=3000)
+        oref = bdda.solve_opts(a.solver, jacobi=not a.no_jacobi, precision=bdda.SOLVE_FP64, tol=1e-8, itermax=3000)
         sref = bdda.solve_device(op, diag_d.data_ptr(), B_d.data_ptr(), n, X_d.data_ptr(), n, L, oref,
                                  stream=stream.cuda_stream)
         ref_iters = sref["iterations"]

@@ -13,7 +13,8 @@ namespace bdda {
 constexpr int kMaxL = 32;          // largest block width (nrhs) supported
 constexpr int kGramThreads = 256;
 constexpr int kGramRows = 32;      // rows per shared-memory sub-tile
-constexpr int kRowThreads = 64;    // rows per CTA of the row-transform kernels
+constexpr int kRowRows = 64;       // rows per CTA of the row-transform kernel
+constexpr int kRowThreads = 256;   // its threads: kRowRows rows x 4 column groups
 
 // Device-side solver control block (lives in device memory).
 struct SolverCtl {
@@ -104,40 +105,36 @@ k_gram(const typename cplx<T>::type* __restrict__ A, int lda,
 }
 
 // out[e] = sum over p of part[p*LL + e] (complex FP64 out), spread over
-// ceil(LL/64) CTAs: thread group g (of 4) sums p = g, g+4, ... with four
+// ceil(LL/16) CTAs: thread group g (of 16) sums p = g, g+16, ... with two
 // independent accumulators; the groups are combined in a fixed order
 // (deterministic).  Sums in the partials' arithmetic (FP64 or double-float).
+constexpr int kRedEntries = 16, kRedGroups = 16;
 template <typename P>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kRedEntries * kRedGroups)
 k_gram_reduce(const P* __restrict__ part, int nparts, int LL, double2* __restrict__ out, const SolverCtl* ctl) {
   if (ctl_skip(ctl)) return;
-  __shared__ P red[4][64];
-  const int el = threadIdx.x & 63, g = threadIdx.x >> 6;
-  const int e = blockIdx.x * 64 + el;
-  P acc[4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u) gp_zero(acc[u]);
+  __shared__ P red[kRedGroups][kRedEntries];
+  const int el = threadIdx.x % kRedEntries, g = threadIdx.x / kRedEntries;
+  const int e = blockIdx.x * kRedEntries + el;
+  P acc[2];
+  gp_zero(acc[0]);
+  gp_zero(acc[1]);
   if (e < LL) {
-    int p = g, u = 0;
-    for (; p + 12 < nparts; p += 16) {
-      const P v0 = part[(size_t)p * LL + e], v1 = part[(size_t)(p + 4) * LL + e];
-      const P v2 = part[(size_t)(p + 8) * LL + e], v3 = part[(size_t)(p + 12) * LL + e];
+    int p = g;
+    for (; p + kRedGroups < nparts; p += 2 * kRedGroups) {
+      const P v0 = part[(size_t)p * LL + e], v1 = part[(size_t)(p + kRedGroups) * LL + e];
       gp_add(acc[0], v0);
       gp_add(acc[1], v1);
-      gp_add(acc[2], v2);
-      gp_add(acc[3], v3);
     }
-    for (; p < nparts; p += 4, ++u) gp_add(acc[u & 3], part[(size_t)p * LL + e]);
+    if (p < nparts) gp_add(acc[0], part[(size_t)p * LL + e]);
   }
   gp_add(acc[0], acc[1]);
-  gp_add(acc[2], acc[3]);
-  gp_add(acc[0], acc[2]);
   red[g][el] = acc[0];
   __syncthreads();
   if (g == 0 && e < LL) {
     P s = red[0][el];
 #pragma unroll
-    for (int k = 1; k < 4; ++k) gp_add(s, red[k][el]);
+    for (int k = 1; k < kRedGroups; ++k) gp_add(s, red[k][el]);
     out[e] = gp_d2(s);
   }
 }
@@ -165,6 +162,8 @@ k_colnorm2(const typename cplx<T>::type* __restrict__ A, int lda, int n, int L, 
 
 // ---------------------------------------------------------------------------
 // Row transform: Out = A*Ma [+ B*Mb] [+ Cadd]
+// A CTA stages kRowRows rows of A (and B) in shared memory; thread (row,
+// group) then forms the columns j = group, group + 4, ... of its row.
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(kRowThreads)
@@ -172,14 +171,16 @@ k_rowmm(int n, int L, const typename cplx<T>::type* A, int lda, const double2* _
         const typename cplx<T>::type* B, int ldb, const double2* __restrict__ Mb,
         const typename cplx<T>::type* Cadd, int ldc,
         typename cplx<T>::type* Out, int ldo, const SolverCtl* ctl) {
-  // Out may alias A, B or Cadd: every row is read completely before it is written.
+  // Out may alias A, B or Cadd: a CTA reads its rows of A and B completely
+  // before it writes, each Cadd element is read by the thread that then
+  // writes it, and CTAs own disjoint rows.
   using C = typename cplx<T>::type;
   if (ctl_skip(ctl)) return;
-  // dynamic smem: ta[L][kRowThreads], tb[L][kRowThreads], ma[L*L], mb[L*L]
+  // dynamic smem: ta[L][kRowRows], tb[L][kRowRows], ma[L*L], mb[L*L]
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* ta = reinterpret_cast<C*>(smem_raw);
-  C* tb = ta + L * kRowThreads;
-  C* ma = tb + (B ? L * kRowThreads : 0);
+  C* tb = ta + L * kRowRows;
+  C* ma = tb + (B ? L * kRowRows : 0);
   C* mb = ma + L * L;
   const int tid = threadIdx.x;
   const int LL = L * L;
@@ -188,26 +189,29 @@ k_rowmm(int n, int L, const typename cplx<T>::type* A, int lda, const double2* _
     ma[e] = cmake((T)v.x, (T)v.y);
     if (Mb) { const double2 w = Mb[e]; mb[e] = cmake((T)w.x, (T)w.y); }
   }
-  const long long r = (long long)blockIdx.x * kRowThreads + tid;
-  const bool ok = r < n;
-  for (int l = 0; l < L; ++l) {
-    ta[l * kRowThreads + tid] = ok ? A[(size_t)l * lda + r] : czero<C>();
-    if (B) tb[l * kRowThreads + tid] = ok ? B[(size_t)l * ldb + r] : czero<C>();
+  const long long row0 = (long long)blockIdx.x * kRowRows;
+  for (int e = tid; e < L * kRowRows; e += kRowThreads) {
+    const int l = e / kRowRows;
+    const long long r = row0 + (e - l * kRowRows);
+    ta[e] = r < n ? A[(size_t)l * lda + r] : czero<C>();
+    if (B) tb[e] = r < n ? B[(size_t)l * ldb + r] : czero<C>();
   }
   __syncthreads();
-  if (!ok) return;
-  for (int j = 0; j < L; ++j) {
+  const int rr = tid % kRowRows, grp = tid / kRowRows;
+  const long long r = row0 + rr;
+  if (r >= n) return;
+  for (int j = grp; j < L; j += kRowThreads / kRowRows) {
     C acc = Cadd ? Cadd[(size_t)j * ldc + r] : czero<C>();
-    for (int l = 0; l < L; ++l) acc = cadd(acc, cmul(ta[l * kRowThreads + tid], ma[l + j * L]));
+    for (int l = 0; l < L; ++l) acc = cadd(acc, cmul(ta[l * kRowRows + rr], ma[l + j * L]));
     if (B)
-      for (int l = 0; l < L; ++l) acc = cadd(acc, cmul(tb[l * kRowThreads + tid], mb[l + j * L]));
+      for (int l = 0; l < L; ++l) acc = cadd(acc, cmul(tb[l * kRowRows + rr], mb[l + j * L]));
     Out[(size_t)j * ldo + r] = acc;
   }
 }
 
 template <typename T>
 inline int rowmm_smem(int L, bool two) {
-  return (int)sizeof(typename cplx<T>::type) * ((two ? 2 : 1) * L * kRowThreads + 2 * L * L);
+  return (int)sizeof(typename cplx<T>::type) * ((two ? 2 : 1) * L * kRowRows + 2 * L * L);
 }
 
 // Out = a*A + b*B (a, b complex FP64 scalars in device memory; null a -> 1; null B -> no term)

@@ -61,7 +61,7 @@ int cuda_fail(cudaError_t e, const char* where) {
     if (_rc != BDDA_OK) return _rc; \
   } while (0)
 
-inline int gram_grid(int n) { return std::max(1, std::min(152, (n + 127) / 128)); }
+inline int gram_grid(int n) { return std::max(1, std::min(2 * 152, (n + 63) / 64)); }
 inline int vec_grid(size_t total) { return (int)std::max<size_t>(1, std::min<size_t>(608, (total + 255) / 256)); }
 
 __device__ __forceinline__ double2* slot(double2* st, int s, int L) { return st + (size_t)s * L * L; }
@@ -354,13 +354,14 @@ struct Krylov {
     op->timer.begin(kGram, st);
     using P = typename GramPart<T>::type;
     k_gram<T, CONJ><<<G(), kGramThreads, 0, st>>>(A, n, B, n, n, L, w->gpart.template as<P>(), ctl());
-    k_gram_reduce<P><<<(L * L + 63) / 64, 256, 0, st>>>(w->gpart.template as<P>(), G(), L * L, out, ctl());
+    k_gram_reduce<P><<<(L * L + kRedEntries - 1) / kRedEntries, kRedEntries * kRedGroups, 0, st>>>(
+        w->gpart.template as<P>(), G(), L * L, out, ctl());
     op->timer.end(kGram, st);
     op->timer.count(kGram);
   }
   void rowmm(const C* A, const double2* Ma, const C* B, const double2* Mb, const C* Cadd, C* Out) {
     op->timer.begin(kUpdate, st);
-    k_rowmm<T><<<(n + kRowThreads - 1) / kRowThreads, kRowThreads, rowmm_smem<T>(L, B != nullptr), st>>>(
+    k_rowmm<T><<<(n + kRowRows - 1) / kRowRows, kRowThreads, rowmm_smem<T>(L, B != nullptr), st>>>(
         n, L, A, n, Ma, B, n, Mb, Cadd, n, Out, n, ctl());
     op->timer.end(kUpdate, st);
   }
