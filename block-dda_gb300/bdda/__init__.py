@@ -283,7 +283,8 @@ class Operator:
                                                 ct.c_void_p(stream) if stream else None))
 
     def set_timing(self, on=True):
-        _check(lib().bdda_op_set_timing(self._h, 1 if on else 0))
+        """True / 1: time every kernel class; 2: the fused z pass only; False / 0: off."""
+        _check(lib().bdda_op_set_timing(self._h, int(on) if not isinstance(on, bool) else (1 if on else 0)))
 
     def kernel_stats(self, reset=False):
         n = len(KERNEL_NAMES)

@@ -64,20 +64,22 @@ struct KernelTimer {
   long long launches[kNumKernelIds] = {0};
   cudaEvent_t cur_a[kNumKernelIds] = {};
   bool enabled = false;
+  unsigned mask = ~0u;  // kernel classes timed while enabled (bit per KernelId)
 
   cudaEvent_t get() {
     if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
     cudaEvent_t e; cudaEventCreate(&e); return e;
   }
   void count(int id, int k = 1) { launches[id] += k; }
+  bool on(int id) const { return enabled && ((mask >> id) & 1u); }
   void begin(int id, cudaStream_t st) {
     launches[id]++;
-    if (!enabled) return;
+    if (!on(id)) return;
     cur_a[id] = get();
     cudaEventRecord(cur_a[id], st);
   }
   void end(int id, cudaStream_t st) {
-    if (!enabled) return;
+    if (!on(id)) return;
     cudaEvent_t b = get();
     cudaEventRecord(b, st);
     pending.push_back({id, cur_a[id], b});

@@ -154,8 +154,14 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
   BDDA_CUDA(op->t1[pi].ensure(mvp_t1_elems(g, L) * sizeof(C), op->stream));
   BDDA_CUDA(op->t2[pi].ensure(mvp_t2_elems(g, L) * sizeof(C), op->stream));
   if (grow && st != op->stream) BDDA_TRY_CUDA(order_after(st, op->stream));  // new buffers exist before st uses them
-  cudaError_t e = launch_block_mvp<T>(g, op->tables<T>(), x, ldx, y, ldy, L, diag, jpre, op->t1[pi].as<C>(),
-                                      op->t2[pi].as<C>(), st, &op->timer, done);
+  // the kernels' arithmetic: dfz (unrenormalised) for the double-float tables
+  using A = typename MvpArith<T>::type;
+  using CA = typename cplx<A>::type;
+  static_assert(sizeof(CA) == sizeof(C), "storage layouts agree");
+  const MvpPrec<T> tb = op->tables<T>();
+  MvpPrec<A> ta{(const CA*)tb.twx, (const CA*)tb.twy, (const CA*)tb.twz, (const CA*)tb.ghat, tb.twzp};
+  cudaError_t e = launch_block_mvp<A>(g, ta, (const CA*)x, ldx, (CA*)y, ldy, L, (const CA*)diag, (const CA*)jpre,
+                                      op->t1[pi].as<CA>(), op->t2[pi].as<CA>(), st, &op->timer, done);
   if (e != cudaSuccess) return cuda_fail(e, "block MVP launch");
   return BDDA_OK;
 }
@@ -268,7 +274,7 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     std::call_once(once, [] {
       cfg = configure_mvp_kernels<double>();
       if (cfg == cudaSuccess) cfg = configure_mvp_kernels<float>();
-      if (cfg == cudaSuccess) cfg = configure_mvp_kernels<dfl>();
+      if (cfg == cudaSuccess) cfg = configure_mvp_kernels<dfz>();
     });
     BDDA_CUDA(cfg);
   }
@@ -377,6 +383,7 @@ int bdda_op_set_timing(bdda_op* op, int enable) {
   if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
   std::lock_guard<std::mutex> lk(op->mu);
   op->timer.enabled = enable != 0;
+  op->timer.mask = enable == 2 ? (1u << kPassC) | (1u << kPassC64) : ~0u;
   return BDDA_OK;
 }
 

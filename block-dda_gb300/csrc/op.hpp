@@ -108,6 +108,10 @@ template <> inline MvpPrec<dfl> Op::tables<dfl>() const {
   return {twdf[0].as<dfc>(), twdf[1].as<dfc>(), twdf[2].as<dfc>(), ghatdf.as<dfc>()};
 }
 
+// Arithmetic of the block-MVP kernels for each table precision.
+template <typename T> struct MvpArith { using type = T; };
+template <> struct MvpArith<dfl> { using type = dfz; };
+
 // Workspace slot and precision bit of each arithmetic type.
 template <typename T> struct PrecInfo;
 template <> struct PrecInfo<double> { static constexpr int slot = 0, bit = 1; };

@@ -303,18 +303,18 @@ int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, i
       const double2 v = s[bdda::skw(i, sh)];
       data[2 * i] = v.x; data[2 * i + 1] = v.y;
     }
-  } else if (prec == 3) {
-    const int sh = bdda::plan_sk<bdda::dfc>(p);
-    std::vector<bdda::dfc> s(bdda::plan_lw<bdda::dfc>(p), bdda::cmake(bdda::dfl(1e30), bdda::dfl(1e30))), t(N);
+  } else if (prec == 3) {  // the double-float MVP's arithmetic (dfz)
+    const int sh = bdda::plan_sk<bdda::dfzc>(p);
+    std::vector<bdda::dfzc> s(bdda::plan_lw<bdda::dfzc>(p), bdda::cmake(bdda::dfz(1e30), bdda::dfz(1e30))), t(N);
     for (int i = 0; i < N; ++i) {
-      s[bdda::skw(i, sh)] = bdda::cmake(bdda::dfl(data[2 * i]), bdda::dfl(data[2 * i + 1]));
-      t[i] = bdda::cmake(bdda::dfl(tw[i].x), bdda::dfl(tw[i].y));
+      s[bdda::skw(i, sh)] = bdda::cmake(bdda::dfz(data[2 * i]), bdda::dfz(data[2 * i + 1]));
+      t[i] = bdda::cmake(bdda::dfz(tw[i].x), bdda::dfz(tw[i].y));
     }
     if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, t.data(), p, 0, 1);
     else bdda::warp_fft_lines<false, 1>(s.data(), 0, t.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
-      const bdda::dfc v = s[bdda::skw(i, sh)];
-      data[2 * i] = bdda::df_to_double(v.x); data[2 * i + 1] = bdda::df_to_double(v.y);
+      const bdda::dfzc v = s[bdda::skw(i, sh)];
+      data[2 * i] = (double)v.x.hi + (double)v.x.lo; data[2 * i + 1] = (double)v.y.hi + (double)v.y.lo;
     }
   } else {
     const int sh = bdda::plan_sk<float2>(p);

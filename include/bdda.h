@@ -437,7 +437,9 @@ int bdda_sweep(const bdda_sweep_spec* spec, double* cross, bdda_sweep_result* re
  */
 int bdda_op_mvp_bytes(const bdda_op* op, int prec, int L, int with_diag, int with_jpre, double bytes[5]);
 
-/* Enable (1) / disable (0) per-kernel CUDA-event timing on the operator. */
+/* Per-kernel CUDA-event timing on the operator: 0 off, 1 every kernel class,
+ * 2 the fused z pass (pass C) of each precision only (two events per block
+ * MVP, for timing a whole solve with little overhead). */
 int bdda_op_set_timing(bdda_op* op, int enable);
 
 /*
