@@ -159,7 +159,7 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
   using CA = typename cplx<A>::type;
   static_assert(sizeof(CA) == sizeof(C), "storage layouts agree");
   const MvpPrec<T> tb = op->tables<T>();
-  MvpPrec<A> ta{(const CA*)tb.twx, (const CA*)tb.twy, (const CA*)tb.twz, (const CA*)tb.ghat, tb.twzp};
+  MvpPrec<A> ta{(const CA*)tb.twx, (const CA*)tb.twy, (const CA*)tb.twz, (const CA*)tb.ghat, tb.twzp, tb.twxp, tb.twyp};
   cudaError_t e = launch_block_mvp<A>(g, ta, (const CA*)x, ldx, (CA*)y, ldy, L, (const CA*)diag, (const CA*)jpre,
                                       op->t1[pi].as<CA>(), op->t2[pi].as<CA>(), st, &op->timer, done);
   if (e != cudaSuccess) return cuda_fail(e, "block MVP launch");

@@ -1,0 +1,96 @@
+// y passes (B, D) for complex FP32 in packed-pair arithmetic.
+//
+// Same tasks, tiles and double-buffered cp.async staging as k_pass_y2: a task
+// is one (field, x, 16-column z tile); warp w transforms the y lines of
+// columns 2w and 2w + 1 -- here as one line pair in the two lanes of the
+// f32x2 instructions (pfft.cuh).  The tile lives in shared memory in the
+// pair layout {re_a, re_b, im_a, im_b}: every element is staged as two 4-byte
+// copies (real and imaginary part into their lanes), and read back lane by
+// lane when the rows are stored.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mvp.hpp"
+#include "pfft.cuh"
+#include "tile_passes.cuh"
+
+namespace bdda {
+namespace tile {
+
+// The packed y kernel gives each warp one line pair, i.e. N / R butterflies
+// per stage: worth it only where every stage still fills most of a warp (the
+// two-line scalar kernel gives the other plans twice the butterflies).
+template <class P> constexpr bool packed_y_fills_warps() {
+  int m = P::N;
+  for (int s = 0; s < P::nst; ++s) m = P::N / P::rad[s] < m ? P::N / P::rad[s] : m;
+  return m >= 20;
+}
+
+template <bool INV, class P>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_y2p(const float2* __restrict__ src, float2* __restrict__ dst, const unsigned char* __restrict__ tmask, int ny,
+           int nz, int nzt, int ntask, const float4* __restrict__ twy, const int* done) {
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int Py = P::N, lw = P::LW;
+  constexpr int kPairs = kTZ2 / 2;
+  ulonglong2* pairs = reinterpret_cast<ulonglong2*>(smem_raw);  // [2][kPairs][lw]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nin = INV ? Py : ny;
+  const int nout = INV ? ny : Py;
+  const int nzt2 = (nz + kTZ2 - 1) / kTZ2;
+  const int tw = tid & (kTZ2 - 1), ty = tid / kTZ2;  // tile column and first row of this thread
+  const int half = tw & 1;                           // lane of the column in its pair
+  auto issue = [&](int task, int buf) {
+    const int zt2 = task % nzt2;
+    const int r = task / nzt2;  // f * Px + q
+    const int z = zt2 * kTZ2 + tw;
+    const bool zval = z < nz;
+    const float2* g = src + (size_t)r * nin * nz + z + (size_t)ty * nz;
+    const unsigned char* tm = tmask + (zval ? z / kTZ : 0) + (size_t)ty * nzt;
+    float* lb = reinterpret_cast<float*>(pairs + (buf * kPairs + (tw >> 1)) * lw) + half;
+    for (int yy = ty; yy < nin; yy += kRowStep2, g += (size_t)kRowStep2 * nz, tm += (size_t)kRowStep2 * nzt) {
+      const bool valid = zval && (INV || *tm);
+      const float* gs = reinterpret_cast<const float*>(valid ? g : src);
+      float* d = lb + 4 * P::addr(yy);
+      cp_async<4>(d, gs, valid);          // real part -> lane `half` of re
+      cp_async<4>(d + 2, gs + 1, valid);  // imaginary part -> lane `half` of im
+    }
+    cp_commit();
+  };
+  int task = blockIdx.x;
+  if (task < ntask) issue(task, 0);
+  for (int it = 0; task < ntask; ++it, task += gridDim.x) {
+    const int buf = it & 1;
+    const int next = task + gridDim.x;
+    if (next < ntask) {
+      issue(next, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    ulonglong2* wl = pairs + (buf * kPairs + warp) * lw;
+    if (!INV) pk::forward<P, 1>(wl, twy, lane, ny);
+    else pk::inverse<P, 1>(wl, twy, lane, ny);
+    __syncthreads();
+    const int zt2 = task % nzt2;
+    const int r = task / nzt2;
+    const int z = zt2 * kTZ2 + tw;
+    if (z < nz) {
+      float2* ob = dst + (size_t)r * nout * nz + z + (size_t)ty * nz;
+      const unsigned char* tm = tmask + z / kTZ + (size_t)ty * nzt;
+      const float* lb = reinterpret_cast<const float*>(pairs + (buf * kPairs + (tw >> 1)) * lw) + half;
+      for (int yy = ty; yy < nout; yy += kRowStep2, ob += (size_t)kRowStep2 * nz, tm += (size_t)kRowStep2 * nzt)
+        if (!INV || *tm) {
+          const float* s = lb + 4 * P::addr(yy);
+          *ob = make_float2(s[0], s[2]);
+        }
+    }
+    __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
+  }
+}
+
+}  // namespace tile
+}  // namespace bdda

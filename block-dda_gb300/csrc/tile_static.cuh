@@ -10,6 +10,7 @@
 #include <mutex>
 
 #include "mvp.hpp"
+#include "tile_packed.cuh"
 #include "tile_passes.cuh"
 
 namespace bdda {
@@ -31,8 +32,9 @@ cudaError_t launch(int pass, const TileArgs& a) {
   const int smem_bd = 2 * tile::kTZ2 * P::LW * (int)sizeof(float2);  // y passes: 16 columns per task
   const int ntask2 = a.nfield * g.Px * ((g.nz + tile::kTZ2 - 1) / tile::kTZ2);
   const int grid2 = std::min(ntask2, a.grid_y);
-  static std::once_flag oa, ob, od, oe;
-  static cudaError_t ca = cudaSuccess, cb = cudaSuccess, cd = cudaSuccess, ce = cudaSuccess;
+  static std::once_flag oa, ob, od, oe, obp, odp;
+  static cudaError_t ca = cudaSuccess, cb = cudaSuccess, cd = cudaSuccess, ce = cudaSuccess, cbp = cudaSuccess,
+                     cdp = cudaSuccess;
   cudaError_t e = cudaSuccess;
   switch (pass) {
     case kTileA:
@@ -41,11 +43,23 @@ cudaError_t launch(int pass, const TileArgs& a) {
           a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, a.twx, a.t1, a.done);
       break;
     case kTileB:
+      if (a.twyp && tile::packed_y_fills_warps<P>()) {
+        if ((e = set_smem(tile::k_pass_y2p<false, P>, smem_bd, obp, cbp)) != cudaSuccess) return e;
+        tile::k_pass_y2p<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzt,
+                                                                           ntask2, a.twyp, a.done);
+        break;
+      }
       if ((e = set_smem(tile::k_pass_y2<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
       tile::k_pass_y2<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzt,
                                                                         ntask2, a.twy, a.done);
       break;
     case kTileD:
+      if (a.twyp && tile::packed_y_fills_warps<P>()) {
+        if ((e = set_smem(tile::k_pass_y2p<true, P>, smem_bd, odp, cdp)) != cudaSuccess) return e;
+        tile::k_pass_y2p<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzt,
+                                                                          ntask2, a.twyp, a.done);
+        break;
+      }
       if ((e = set_smem(tile::k_pass_y2<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
       tile::k_pass_y2<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzt,
                                                                        ntask2, a.twy, a.done);
