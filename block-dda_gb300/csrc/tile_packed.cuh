@@ -1,9 +1,9 @@
 // y passes (B, D) for complex FP32 in packed-pair arithmetic.
 //
 // Same tasks, tiles and double-buffered cp.async staging as k_pass_y2: a task
-// is one (field, x, 16-column z tile); warp w transforms the y lines of
-// columns 2w and 2w + 1 -- here as one line pair in the two lanes of the
-// f32x2 instructions (pfft.cuh).  The tile lives in shared memory in the
+// is one (field, x, 16-column z tile), i.e. 8 line pairs (columns 2p and
+// 2p + 1 in the two lanes of the f32x2 instructions, pfft.cuh); a CTA of
+// 8 / NP warps gives each warp NP pairs.  The tile lives in shared memory in the
 // pair layout {re_a, re_b, im_a, im_b}: every element is staged as two 4-byte
 // copies (real and imaginary part into their lanes), and read back lane by
 // lane when the rows are stored.
@@ -18,23 +18,27 @@
 namespace bdda {
 namespace tile {
 
-// The packed y kernel gives each warp one line pair, i.e. N / R butterflies
-// per stage: worth it only where every stage still fills most of a warp (the
-// two-line scalar kernel gives the other plans twice the butterflies).
-template <class P> constexpr bool packed_y_fills_warps() {
+// Line pairs per warp for plan P (a warp's NP pairs give N / R * NP
+// butterflies per stage): 1 where every stage then still fills most of a
+// warp, else 0, the two-line scalar kernel.  Two pairs per warp (CTAs of four
+// warps) measured no faster than the scalar kernel on the two-stage radix
+// 10 / 12 / 16 plans that one pair underfills.
+template <class P> constexpr int packed_y_pairs() {
   int m = P::N;
   for (int s = 0; s < P::nst; ++s) m = P::N / P::rad[s] < m ? P::N / P::rad[s] : m;
-  return m >= 20;
+  return m >= 20 ? 1 : 0;
 }
 
-template <bool INV, class P>
-__global__ void __launch_bounds__(kTileThreads)
+template <bool INV, class P, int NP>
+__global__ void __launch_bounds__(8 / NP * 32)
 k_pass_y2p(const float2* __restrict__ src, float2* __restrict__ dst, const unsigned char* __restrict__ tmask, int ny,
            int nz, int nzt, int ntask, const float4* __restrict__ twy, const int* done) {
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int Py = P::N, lw = P::LW;
   constexpr int kPairs = kTZ2 / 2;
+  constexpr int kThreads = kPairs / NP * 32;
+  constexpr int kStep = kThreads / kTZ2;  // rows per staging step
   ulonglong2* pairs = reinterpret_cast<ulonglong2*>(smem_raw);  // [2][kPairs][lw]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nin = INV ? Py : ny;
@@ -50,7 +54,7 @@ k_pass_y2p(const float2* __restrict__ src, float2* __restrict__ dst, const unsig
     const float2* g = src + (size_t)r * nin * nz + z + (size_t)ty * nz;
     const unsigned char* tm = tmask + (zval ? z / kTZ : 0) + (size_t)ty * nzt;
     float* lb = reinterpret_cast<float*>(pairs + (buf * kPairs + (tw >> 1)) * lw) + half;
-    for (int yy = ty; yy < nin; yy += kRowStep2, g += (size_t)kRowStep2 * nz, tm += (size_t)kRowStep2 * nzt) {
+    for (int yy = ty; yy < nin; yy += kStep, g += (size_t)kStep * nz, tm += (size_t)kStep * nzt) {
       const bool valid = zval && (INV || *tm);
       const float* gs = reinterpret_cast<const float*>(valid ? g : src);
       float* d = lb + 4 * P::addr(yy);
@@ -71,9 +75,9 @@ k_pass_y2p(const float2* __restrict__ src, float2* __restrict__ dst, const unsig
       cp_wait<0>();
     }
     __syncthreads();
-    ulonglong2* wl = pairs + (buf * kPairs + warp) * lw;
-    if (!INV) pk::forward<P, 1>(wl, twy, lane, ny);
-    else pk::inverse<P, 1>(wl, twy, lane, ny);
+    ulonglong2* wl = pairs + (buf * kPairs + warp * NP) * lw;
+    if (!INV) pk::forward<P, NP>(wl, twy, lane, ny);
+    else pk::inverse<P, NP>(wl, twy, lane, ny);
     __syncthreads();
     const int zt2 = task % nzt2;
     const int r = task / nzt2;
@@ -82,7 +86,7 @@ k_pass_y2p(const float2* __restrict__ src, float2* __restrict__ dst, const unsig
       float2* ob = dst + (size_t)r * nout * nz + z + (size_t)ty * nz;
       const unsigned char* tm = tmask + z / kTZ + (size_t)ty * nzt;
       const float* lb = reinterpret_cast<const float*>(pairs + (buf * kPairs + (tw >> 1)) * lw) + half;
-      for (int yy = ty; yy < nout; yy += kRowStep2, ob += (size_t)kRowStep2 * nz, tm += (size_t)kRowStep2 * nzt)
+      for (int yy = ty; yy < nout; yy += kStep, ob += (size_t)kStep * nz, tm += (size_t)kStep * nzt)
         if (!INV || *tm) {
           const float* s = lb + 4 * P::addr(yy);
           *ob = make_float2(s[0], s[2]);
