@@ -50,7 +50,9 @@ __device__ __forceinline__ double2 gp_d2(dfc a) { return make_double2(df_to_doub
 // summed in FP32 over one 32-row sub-tile, then added to double-float
 // accumulators (FP64 data: FP64 throughout).
 // ---------------------------------------------------------------------------
-template <typename T, bool CONJ>
+// BOTH (with A == B): the Hermitian and the unconjugated Gram of A in one
+// pass, partials[blk][e] = A^H A and partials[blk][LL + e] = A^T A.
+template <typename T, bool CONJ, bool BOTH = false>
 __global__ void __launch_bounds__(kGramThreads)
 k_gram(const typename cplx<T>::type* __restrict__ A, int lda,
        const typename cplx<T>::type* __restrict__ B, int ldb,
@@ -63,9 +65,11 @@ k_gram(const typename cplx<T>::type* __restrict__ A, int lda,
   const int tid = threadIdx.x;
   const int LL = L * L;
   // entries owned by this thread: e = tid + k*256, k < 4  (L <= 32 -> LL <= 1024)
-  P acc[4];
+  P acc[4], acc2[BOTH ? 4 : 1];
 #pragma unroll
   for (int k = 0; k < 4; ++k) gp_zero(acc[k]);
+#pragma unroll
+  for (int k = 0; k < (BOTH ? 4 : 1); ++k) gp_zero(acc2[k]);
   const long long rows_per = ((long long)n + gridDim.x - 1) / gridDim.x;
   const long long r0 = (long long)blockIdx.x * rows_per;
   const long long r1 = min((long long)n, r0 + rows_per);
@@ -88,19 +92,25 @@ k_gram(const typename cplx<T>::type* __restrict__ A, int lda,
       const int e = tid + k * kGramThreads;
       if (e < LL) {
         const int i = e % L, j = e / L;
-        C s = czero<C>();
+        C s = czero<C>(), s2 = czero<C>();
         for (int rr = 0; rr < nr; ++rr) {
           const C a = sa[i][rr], b = sb[j][rr];
           s = CONJ ? cadd(s, cconjmul(a, b)) : cadd(s, cmul(a, b));
+          if (BOTH) s2 = cadd(s2, cmul(a, b));
         }
         gp_add(acc[k], s);
+        if (BOTH) gp_add(acc2[BOTH ? k : 0], s2);
       }
     }
   }
+  const int LLo = BOTH ? 2 * LL : LL;  // partial entries per CTA
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int e = tid + k * kGramThreads;
-    if (e < LL) partials[(size_t)blockIdx.x * LL + e] = acc[k];
+    if (e < LL) {
+      partials[(size_t)blockIdx.x * LLo + e] = acc[k];
+      if (BOTH) partials[(size_t)blockIdx.x * LLo + LL + e] = acc2[BOTH ? k : 0];
+    }
   }
 }
 
@@ -206,6 +216,46 @@ k_rowmm(int n, int L, const typename cplx<T>::type* A, int lda, const double2* _
     if (B)
       for (int l = 0; l < L; ++l) acc = cadd(acc, cmul(tb[l * kRowRows + rr], mb[l + j * L]));
     Out[(size_t)j * ldo + r] = acc;
+  }
+}
+
+// Out1 = A*Ma and Out2 = Out1 + B*Mb in one pass (Out2 may alias B).
+template <typename T>
+__global__ void __launch_bounds__(kRowThreads)
+k_rowmm2(int n, int L, const typename cplx<T>::type* A, const double2* __restrict__ Ma,
+         const typename cplx<T>::type* B, const double2* __restrict__ Mb,
+         typename cplx<T>::type* Out1, typename cplx<T>::type* Out2, const SolverCtl* ctl) {
+  using C = typename cplx<T>::type;
+  if (ctl_skip(ctl)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* ta = reinterpret_cast<C*>(smem_raw);
+  C* tb = ta + L * kRowRows;
+  C* ma = tb + L * kRowRows;
+  C* mb = ma + L * L;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < L * L; e += kRowThreads) {
+    const double2 v = Ma[e], w = Mb[e];
+    ma[e] = cmake((T)v.x, (T)v.y);
+    mb[e] = cmake((T)w.x, (T)w.y);
+  }
+  const long long row0 = (long long)blockIdx.x * kRowRows;
+  for (int e = tid; e < L * kRowRows; e += kRowThreads) {
+    const int l = e / kRowRows;
+    const long long r = row0 + (e - l * kRowRows);
+    ta[e] = r < n ? A[(size_t)l * n + r] : czero<C>();
+    tb[e] = r < n ? B[(size_t)l * n + r] : czero<C>();
+  }
+  __syncthreads();
+  const int rr = tid % kRowRows, grp = tid / kRowRows;
+  const long long r = row0 + rr;
+  if (r >= n) return;
+  for (int j = grp; j < L; j += kRowThreads / kRowRows) {
+    C a1 = czero<C>();
+    for (int l = 0; l < L; ++l) a1 = cadd(a1, cmul(ta[l * kRowRows + rr], ma[l + j * L]));
+    C a2 = a1;
+    for (int l = 0; l < L; ++l) a2 = cadd(a2, cmul(tb[l * kRowRows + rr], mb[l + j * L]));
+    Out1[(size_t)j * n + r] = a1;
+    Out2[(size_t)j * n + r] = a2;
   }
 }
 

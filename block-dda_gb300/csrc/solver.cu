@@ -34,7 +34,7 @@ struct SolverWork {
   DevBuf X64, R64, Y64;
   DevBuf xdf, ydf, diagdf;      // double-float residual MVP (mixed solves)
   DevBuf jpre64, diag32, jpre32;
-  DevBuf gpart;                 // per-CTA Gram partials (c128) [G][L*L]
+  DevBuf gpart;                 // per-CTA Gram partials [G][L*L], or [G][2 L*L] for gram2
   DevBuf partials, partials2;   // reduced Gram matrices (c128) [L*L]
   DevBuf vpart;                 // dot / norm partials
   DevBuf small;                 // c128 [kNumSlots][L*L] + scalars
@@ -212,6 +212,50 @@ k_small_chol2(const double2* __restrict__ part, int nparts, int L, double2* st, 
   }
 }
 
+// COCG-RQ, the second CholQR2 step fused with beta.  part holds the
+// Hermitian and the unconjugated Gram of W1 = W R1^-1 ([2][L*L]).
+//   R2 = chol(W1^H W1), R2inv, tau = R2 R1, xi = tau xi, err, stopping test;
+//   Q' = W1 R2^-1, so Q'^T Q' = R2^-T (W1^T W1) R2^-1 without a pass over Q'
+//   (R2 is near the identity: the second CholQR2 factor);
+//   beta = (Q^T Q)^-1 (tau^T Q'^T Q') ; Q^T Q <- Q'^T Q'.
+template <typename R>
+__global__ void __launch_bounds__(kSmallThreads)
+k_small_chol2_beta(const double2* __restrict__ part, int L, double2* st, SolverCtl* ctl, double tol, double* hist, int k,
+                   int full) {
+  if (ctl_skip(ctl)) return;
+  SMALL_PROLOGUE
+  sm_reduce<R>(m0, part, 1, LL);
+  if (!chol_and_inverse<R>(m0, m1, m2, L)) { fail(ctl); return; }
+  sm_store(slot(st, kR2Inv, L), m2, LL);
+  sm_load(m3, slot(st, kR1, L), LL);
+  sm_matmul(m4, m1, m3, L, false);  // tau = R2 R1
+  sm_store(slot(st, kTau, L), m4, LL);
+  sm_load(m5, slot(st, kXi, L), LL);
+  sm_matmul(m0, m4, m5, L, false);  // xi = tau xi
+  sm_store(slot(st, kXi, L), m0, LL);
+  const double nrm = sm_fro<R>(m0, LL);
+  __shared__ int stop;
+  if (threadIdx.x == 0) {
+    const double err = nrm / ctl->bnorm;
+    ctl->err = err;
+    if (hist) hist[k] = err;
+    ctl->iter = k + 1;
+    stop = 0;
+    if (!isfinite(err)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; stop = 1; }
+    else if (err < tol) { ctl->done = 1; stop = 1; }
+  }
+  __syncthreads();
+  if (stop) return;
+  sm_reduce<R>(m0, part + LL, 1, LL);  // W1^T W1
+  sm_matmul(m3, m0, m2, L, false);     // (W1^T W1) R2^-1
+  sm_matmul(m5, m2, m3, L, true);      // Q'^T Q'
+  sm_matmul(m0, m4, m5, L, true);      // tau^T Q'^T Q'
+  sm_load(m1, slot(st, kQtQ, L), LL);
+  if (!sm_lu_solve<R>(m1, m0, L, L, full != 0, colperm, piv)) { fail(ctl); return; }
+  sm_store(slot(st, kBeta, L), m0, LL);
+  sm_store(slot(st, kQtQ, L), m5, LL);
+}
+
 // COCG-RQ alpha: alpha = (S^T AS)^-1 (Q^T Q) ; A_xi = alpha xi ; -alpha
 template <typename R>
 __global__ void __launch_bounds__(kSmallThreads)
@@ -359,6 +403,23 @@ struct Krylov {
     op->timer.end(kGram, st);
     op->timer.count(kGram);
   }
+  // out[0 .. LL) = A^H A, out[LL .. 2 LL) = A^T A
+  void gram2(const C* A, double2* out) {
+    op->timer.begin(kGram, st);
+    using P = typename GramPart<T>::type;
+    k_gram<T, true, true><<<G(), kGramThreads, 0, st>>>(A, n, A, n, n, L, w->gpart.template as<P>(), ctl());
+    k_gram_reduce<P><<<(2 * L * L + kRedEntries - 1) / kRedEntries, kRedEntries * kRedGroups, 0, st>>>(
+        w->gpart.template as<P>(), G(), 2 * L * L, out, ctl());
+    op->timer.end(kGram, st);
+    op->timer.count(kGram);
+  }
+  // Out1 = A Ma ; Out2 = Out1 + B Mb
+  void rowmm2(const C* A, const double2* Ma, const C* B, const double2* Mb, C* Out1, C* Out2) {
+    op->timer.begin(kUpdate, st);
+    k_rowmm2<T><<<(n + kRowRows - 1) / kRowRows, kRowThreads, rowmm_smem<T>(L, true), st>>>(n, L, A, Ma, B, Mb, Out1,
+                                                                                         Out2, ctl());
+    op->timer.end(kUpdate, st);
+  }
   void rowmm(const C* A, const double2* Ma, const C* B, const double2* Mb, const C* Cadd, C* Out) {
     op->timer.begin(kUpdate, st);
     k_rowmm<T><<<(n + kRowRows - 1) / kRowRows, kRowThreads, rowmm_smem<T>(L, B != nullptr), st>>>(
@@ -436,13 +497,11 @@ struct Krylov {
       rowmm(AS, sl(kNAlpha), nullptr, nullptr, Q, W);       // W = Q - AS alpha
       gram<true>(W, W, p);
       small_launch(k_small_chol1<SR>, (const double2*)p, 1, L, small(), ctl());
-      rowmm(W, sl(kR1Inv), nullptr, nullptr, nullptr, W);
-      gram<true>(W, W, p);
-      small_launch(k_small_chol2<SR>, (const double2*)p, 1, L, small(), ctl(), tol, w->hist.as<double>(), k, 1);
-      rowmm(W, sl(kR2Inv), nullptr, nullptr, nullptr, Qn);  // Q'
-      gram<false>(Qn, Qn, p);
-      small_launch(k_small_cocg_beta<SR>, (const double2*)p, 1, L, small(), ctl(), (int)full);
-      rowmm(S, sl(kBeta), nullptr, nullptr, Qn, S);         // S = Q' + S beta
+      rowmm(W, sl(kR1Inv), nullptr, nullptr, nullptr, W);   // W1
+      gram2(W, p);                                          // W1^H W1, W1^T W1
+      small_launch(k_small_chol2_beta<SR>, (const double2*)p, L, small(), ctl(), tol, w->hist.as<double>(), k,
+                   (int)full);
+      rowmm2(W, sl(kR2Inv), S, sl(kBeta), Qn, S);           // Q' = W1 R2^-1 ; S = Q' + S beta
       std::swap(Q, Qn);
       if ((k + 1) % check_every == 0 || k + 1 == itermax) {
         BDDA_TRY(poll(&done));
@@ -601,9 +660,9 @@ static int ensure_work(Op* op, int n, int L, int itermax, bool need64, bool need
   BDDA_CUDA(w->diag32.ensure(sizeof(float2) * (size_t)n, op->stream));
   BDDA_CUDA(w->jpre32.ensure(sizeof(float2) * (size_t)n, op->stream));
   const size_t LL = (size_t)L * L;
-  BDDA_CUDA(w->gpart.ensure(sizeof(double2) * LL * gram_grid(n), op->stream));
-  BDDA_CUDA(w->partials.ensure(sizeof(double2) * LL * gram_grid(n), op->stream));
-  BDDA_CUDA(w->partials2.ensure(sizeof(double2) * LL * gram_grid(n), op->stream));
+  BDDA_CUDA(w->gpart.ensure(sizeof(double2) * 2 * LL * gram_grid(n), op->stream));  // two Grams per CTA (gram2)
+  BDDA_CUDA(w->partials.ensure(sizeof(double2) * 2 * LL, op->stream));
+  BDDA_CUDA(w->partials2.ensure(sizeof(double2) * 2 * LL, op->stream));
   BDDA_CUDA(w->vpart.ensure(sizeof(double2) * 2 * (size_t)std::max(vec_grid((size_t)n * L) * L, 2 * 608), op->stream));
   BDDA_CUDA(w->small.ensure(sizeof(double2) * (LL * kNumSlots + 8), op->stream));
   BDDA_CUDA(w->ctl.ensure(sizeof(SolverCtl), op->stream));
@@ -627,6 +686,10 @@ static int ensure_work(Op* op, int n, int L, int itermax, bool need64, bool need
     set((const void*)k_small_chol2<dfl>, mx);
     set((const void*)k_small_cocg_alpha<dfl>, mx);
     set((const void*)k_small_cocg_beta<dfl>, mx);
+    set((const void*)k_small_chol2_beta<double>, mx);
+    set((const void*)k_small_chol2_beta<dfl>, mx);
+    set((const void*)k_rowmm2<double>, rowmm_smem<double>(kMaxL, true));
+    set((const void*)k_rowmm2<float>, rowmm_smem<float>(kMaxL, true));
     set((const void*)k_small_store_reduce, mx);
     set((const void*)k_rowmm<double>, rowmm_smem<double>(kMaxL, true));
     set((const void*)k_rowmm<float>, rowmm_smem<float>(kMaxL, true));
@@ -770,7 +833,10 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
     for (int l = 0; l < L; ++l)
       if (!(bn2[l] > 0.0)) { set_error("zero right-hand side column"); return BDDA_ERR_INVALID; }
     const int max_refine = o->max_refine > 0 ? o->max_refine : 8;
-    const double itol = o->inner_tol > 0 ? o->inner_tol : (mixed ? 2e-5 : 0.3 * o->true_tol);
+    // first-step inner tolerance; later steps go no tighter than ifloor, the
+    // reduction one FP32 inner solve reaches before its rounding drift
+    const double itol = o->inner_tol > 0 ? o->inner_tol : (mixed ? 5e-5 : 0.3 * o->true_tol);
+    const double ifloor = mixed ? std::min(itol, 2e-5) : itol;
     const double2* R = B;
     int ldr = ldb;
     bool converged = false;
@@ -790,14 +856,14 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
     }
     const bool warm = o->warm_start && R != B;  // refining from a kept initial guess
     for (int r = 0; r < max_refine && !converged; ++r) {
-      // Inner tolerance: the default for a cold first step; afterwards (and
-      // from a warm guess) the reduction this step needs, 0.3 true_tol /
-      // residual, but not tighter than the default (or 1e-6 from a warm guess,
-      // which lets a close guess converge in one step) and not looser than 0.1.
+      // Inner tolerance: itol for a cold first step; afterwards (and from a
+      // warm guess) the reduction this step needs, 0.3 true_tol / residual,
+      // but not tighter than ifloor (or 1e-6 from a warm guess, which lets a
+      // close guess converge in one step) and not looser than 0.1.
       double tol_r = itol;
       if (r > 0 || warm) {
         const double need = std::min(0.1, 0.3 * o->true_tol / std::max(resmax, 1e-300));
-        tol_r = std::max(need, (r == 0 && o->inner_tol <= 0) ? std::min(itol, 1e-6) : itol);
+        tol_r = std::max(need, (r == 0 && o->inner_tol <= 0) ? std::min(ifloor, 1e-6) : ifloor);
       }
       BDDA_TRY(inner(R, ldr, tol_r, X, ldx, true));
       if (status == BDDA_ERR_BREAKDOWN) break;

@@ -134,7 +134,9 @@ typedef struct {
   int itermax;        /* reference iteration limit per Krylov solve (Solver.hpp:28 default 300) */
   double true_tol;    /* >0: iterate until every column's true residual ||b-Ax||/||b|| <= true_tol
                          (FP64 residuals, iterative refinement); <=0: one reference-semantics solve */
-  double inner_tol;   /* tolerance of each inner Krylov solve in refinement mode (0 -> automatic) */
+  double inner_tol;   /* refinement mode: tolerance of the first inner Krylov solve; later ones aim at the
+                         reduction still needed, no tighter than min(inner_tol, 2e-5) for mixed solves
+                         (0 -> automatic: 5e-5 mixed, 0.3 true_tol FP64) */
   int max_refine;     /* refinement steps limit (0 -> 8) */
   int check_every;    /* host convergence poll period in iterations (0 -> 4) */
   int warm_start;     /* 1: X holds an initial guess on entry (e.g. the solution at a neighbouring
