@@ -160,23 +160,37 @@ template <typename M> __device__ void sm_matmul(M* Cm, const M* A, const M* B, i
   __syncthreads();
 }
 
-// Solve A X = B (L x L, nrhs columns) by LU; A and B are overwritten (B <- X).
-// full=false: partial (row) pivoting on the largest |a| in the column (first
-// max); full=true: complete pivoting on the largest |a| of the trailing block,
-// first max in column-major order.  Returns false on a zero / non-finite pivot.
-template <typename R>
-__device__ bool sm_lu_solve(typename SmallMat<R>::M* A, typename SmallMat<R>::M* B, int L, int nrhs, bool full,
-                            int* colperm /*smem[L]*/, int* piv /*smem[2]*/) {
+// ---- teams --------------------------------------------------------------------
+// The sequential L x L factorisations run on a team: the whole CTA (step
+// phases separated by __syncthreads) or, for L <= kWarpL, warp 0 alone (phases
+// separated by __syncwarp; the other warps wait at the routine's final
+// barrier).  For small L a step's phase is a few elements per lane, so the
+// CTA-wide barriers cost more than the work they separate (L = 2: 10% more
+// solves per second at N=1024); at L = 16 one warp's share of the trailing
+// updates (about 40 double-float elements per lane) outweighs the barriers.
+constexpr int kWarpL = 8;
+struct CtaTeam {
+  int rank, size;
+  __device__ void sync() const { __syncthreads(); }
+};
+struct WarpTeam {
+  int rank, size;
+  __device__ void sync() const { __syncwarp(); }
+};
+
+// LU solve on a team (see sm_lu_solve); *bad (shared) set on a zero /
+// non-finite pivot or result.
+template <typename R, class Team>
+__device__ void lu_solve_team(const Team tm, typename SmallMat<R>::M* A, typename SmallMat<R>::M* B, int L, int nrhs,
+                              bool full, int* colperm, int* piv, int* bad) {
   using M = typename SmallMat<R>::M;
-  const int tid = threadIdx.x;
-  for (int i = tid; i < L; i += blockDim.x) colperm[i] = i;
-  __shared__ int bad;
-  if (tid == 0) bad = 0;
-  __syncthreads();
+  const int tid = tm.rank, nt = tm.size;
+  for (int i = tid; i < L; i += nt) colperm[i] = i;
+  tm.sync();
   for (int k = 0; k < L; ++k) {
-    // ---- pivot search by warp 0: lanes scan candidates, shuffle argmax (the
-    // largest |a|, first in column-major order on ties); |a|^2 orders the
-    // candidates as |a| does, without a square root
+    // ---- pivot search by the first 32 ranks: lanes scan candidates, shuffle
+    // argmax (the largest |a|, first in column-major order on ties); |a|^2
+    // orders the candidates as |a| does, without a square root
     if (tid < 32) {
       const int m = L - k;
       const int cnt = full ? m * m : m;
@@ -198,14 +212,14 @@ __device__ bool sm_lu_solve(typename SmallMat<R>::M* A, typename SmallMat<R>::M*
       if (tid == 0) {
         piv[0] = bidx % L;
         piv[1] = bidx / L;
-        if (!r_pos_finite(best)) bad = 1;
+        if (!r_pos_finite(best)) *bad = 1;
       }
     }
-    __syncthreads();
+    tm.sync();
     const int pr = piv[0], pc = piv[1];
     // ---- row swap k <-> pr (A and B)
     if (pr != k) {
-      for (int j = tid; j < L + nrhs; j += blockDim.x) {
+      for (int j = tid; j < L + nrhs; j += nt) {
         M* Mt = j < L ? A : B;
         const int jc = j < L ? j : j - L;
         const M t = Mt[k + jc * L];
@@ -213,24 +227,24 @@ __device__ bool sm_lu_solve(typename SmallMat<R>::M* A, typename SmallMat<R>::M*
         Mt[pr + jc * L] = t;
       }
     }
-    __syncthreads();
+    if (full) tm.sync();  // the row and the column swap share elements
     // ---- column swap k <-> pc (A only, record permutation)
     if (full && pc != k) {
-      for (int i = tid; i < L; i += blockDim.x) {
+      for (int i = tid; i < L; i += nt) {
         const M t = A[i + k * L];
         A[i + k * L] = A[i + pc * L];
         A[i + pc * L] = t;
       }
       if (tid == 0) { const int t = colperm[k]; colperm[k] = colperm[pc]; colperm[pc] = t; }
     }
-    __syncthreads();
-    if (bad) continue;
+    tm.sync();
+    if (*bad) continue;
     // ---- multipliers (one complex division per row), then the trailing update
     const M pinv = m_div(m_one<R>(), A[k + k * L]);
-    for (int i = k + 1 + tid; i < L; i += blockDim.x) A[i + k * L] = cmul(A[i + k * L], pinv);
-    __syncthreads();
+    for (int i = k + 1 + tid; i < L; i += nt) A[i + k * L] = cmul(A[i + k * L], pinv);
+    tm.sync();
     const int rows = L - k - 1;
-    for (int t = tid; t < rows * (L - k - 1 + nrhs); t += blockDim.x) {
+    for (int t = tid; t < rows * (L - k - 1 + nrhs); t += nt) {
       const int i = k + 1 + t % rows;
       const int jj = t / rows;  // 0..(L-k-2) -> A columns k+1.., then B columns
       const M f = A[i + k * L];
@@ -242,38 +256,84 @@ __device__ bool sm_lu_solve(typename SmallMat<R>::M* A, typename SmallMat<R>::M*
         B[i + j * L] = csub(B[i + j * L], cmul(f, B[k + j * L]));
       }
     }
-    __syncthreads();
+    tm.sync();
   }
   // ---- back substitution, right-looking: row k of X is final once the rows
   // below were eliminated; then every remaining row sheds its row-k term in
   // parallel (the serial chain per row is one product per step, not L)
-  for (int k = tid; k < L; k += blockDim.x) A[k + k * L] = m_div(m_one<R>(), A[k + k * L]);
-  __syncthreads();  // the diagonal now holds 1 / pivot
+  for (int k = tid; k < L; k += nt) A[k + k * L] = m_div(m_one<R>(), A[k + k * L]);
+  tm.sync();  // the diagonal now holds 1 / pivot
   for (int k = L - 1; k >= 0; --k) {
-    for (int j = tid; j < nrhs; j += blockDim.x) B[k + j * L] = cmul(B[k + j * L], A[k + k * L]);
-    __syncthreads();
-    for (int t = tid; t < k * nrhs; t += blockDim.x) {
+    for (int j = tid; j < nrhs; j += nt) B[k + j * L] = cmul(B[k + j * L], A[k + k * L]);
+    tm.sync();
+    for (int t = tid; t < k * nrhs; t += nt) {
       const int r = t % k, j = t / k;
       B[r + j * L] = csub(B[r + j * L], cmul(A[r + k * L], B[k + j * L]));
     }
-    __syncthreads();
+    tm.sync();
   }
   if (full) {
     // x[colperm[k]] = y[k]; use A as scratch (A no longer needed)
-    for (int e = tid; e < L * nrhs; e += blockDim.x) A[e] = B[e];
-    __syncthreads();
-    for (int e = tid; e < L * nrhs; e += blockDim.x) {
+    for (int e = tid; e < L * nrhs; e += nt) A[e] = B[e];
+    tm.sync();
+    for (int e = tid; e < L * nrhs; e += nt) {
       const int k = e % L, j = e / L;
       B[colperm[k] + j * L] = A[e];
     }
-    __syncthreads();
+    tm.sync();
   }
-  for (int e = tid; e < L * nrhs; e += blockDim.x)
-    if (!m_finite(B[e])) bad = 1;
+  for (int e = tid; e < L * nrhs; e += nt)
+    if (!m_finite(B[e])) *bad = 1;
+}
+
+// Solve A X = B (L x L, nrhs columns) by LU; A and B are overwritten (B <- X).
+// full=false: partial (row) pivoting on the largest |a| in the column (first
+// max); full=true: complete pivoting on the largest |a| of the trailing block,
+// first max in column-major order.  Returns false on a zero / non-finite pivot.
+template <typename R>
+__device__ bool sm_lu_solve(typename SmallMat<R>::M* A, typename SmallMat<R>::M* B, int L, int nrhs, bool full,
+                            int* colperm /*smem[L]*/, int* piv /*smem[2]*/) {
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  if (L <= kWarpL) {
+    if (threadIdx.x < 32) lu_solve_team<R>(WarpTeam{(int)threadIdx.x, 32}, A, B, L, nrhs, full, colperm, piv, &bad);
+  } else {
+    lu_solve_team<R>(CtaTeam{(int)threadIdx.x, (int)blockDim.x}, A, B, L, nrhs, full, colperm, piv, &bad);
+  }
   __syncthreads();
   const bool ok = !bad;
   __syncthreads();
   return ok;
+}
+
+// Right-looking Cholesky on a team (see sm_cholesky), in place on Rm.  Every
+// rank takes the square root and reciprocal of the pivot itself (no broadcast
+// phase); rank 0 writes the diagonal after all ranks have read it.
+template <typename R, class Team>
+__device__ void cholesky_team(const Team tm, typename SmallMat<R>::M* Rm, int L, int* bad) {
+  using M = typename SmallMat<R>::M;
+  const int tid = tm.rank, nt = tm.size;
+  for (int k = 0; k < L; ++k) {
+    R d = Rm[k + k * L].x;
+    if (!r_pos_finite(d)) { if (tid == 0) *bad = 1; d = r_const<R>(1.0f); }
+    d = r_sqrt(d);
+    const R di = r_recip(d);
+    tm.sync();
+    if (tid == 0) Rm[k + k * L] = cmake(d, r_const<R>(0.0f));
+    for (int j = k + 1 + tid; j < L; j += nt) {
+      const M v = Rm[k + j * L];
+      Rm[k + j * L] = cmake(v.x * di, v.y * di);
+    }
+    tm.sync();
+    // trailing block (upper part, i <= j): H_ij -= conj(R_ki) R_kj
+    const int m = L - k - 1;
+    for (int t = tid; t < m * m; t += nt) {
+      const int i = k + 1 + t % m, j = k + 1 + t / m;
+      if (i <= j) Rm[i + j * L] = csub(Rm[i + j * L], cconjmul(Rm[k + i * L], Rm[k + j * L]));
+    }
+    tm.sync();
+  }
 }
 
 // H = R^H R with R upper triangular, real positive diagonal.  R may alias H.
@@ -284,34 +344,16 @@ template <typename R>
 __device__ bool sm_cholesky(typename SmallMat<R>::M* Rm, const typename SmallMat<R>::M* H, int L) {
   using M = typename SmallMat<R>::M;
   __shared__ int bad;
-  __shared__ R dinv;
   const int tid = threadIdx.x;
   if (tid == 0) bad = 0;
   if (Rm != H) for (int e = tid; e < L * L; e += blockDim.x) Rm[e] = H[e];
   __syncthreads();
-  for (int k = 0; k < L; ++k) {
-    if (tid == 0) {
-      R d = Rm[k + k * L].x;
-      if (!r_pos_finite(d)) { bad = 1; d = r_const<R>(1.0f); }
-      d = r_sqrt(d);
-      Rm[k + k * L] = cmake(d, r_const<R>(0.0f));
-      dinv = r_recip(d);
-    }
-    __syncthreads();
-    const R di = dinv;
-    for (int j = k + 1 + tid; j < L; j += blockDim.x) {
-      const M v = Rm[k + j * L];
-      Rm[k + j * L] = cmake(v.x * di, v.y * di);
-    }
-    __syncthreads();
-    // trailing block (upper part, i <= j): H_ij -= conj(R_ki) R_kj
-    const int m = L - k - 1;
-    for (int t = tid; t < m * m; t += blockDim.x) {
-      const int i = k + 1 + t % m, j = k + 1 + t / m;
-      if (i <= j) Rm[i + j * L] = csub(Rm[i + j * L], cconjmul(Rm[k + i * L], Rm[k + j * L]));
-    }
-    __syncthreads();
+  if (L <= kWarpL) {
+    if (tid < 32) cholesky_team<R>(WarpTeam{tid, 32}, Rm, L, &bad);
+  } else {
+    cholesky_team<R>(CtaTeam{tid, (int)blockDim.x}, Rm, L, &bad);
   }
+  __syncthreads();
   // zero the strictly lower part
   for (int e = tid; e < L * L; e += blockDim.x) {
     const int i = e % L, j = e / L;
@@ -334,20 +376,28 @@ __device__ void sm_tri_inv(typename SmallMat<R>::M* Ri, const typename SmallMat<
   for (int i = threadIdx.x; i < L; i += blockDim.x) dinv[i] = r_recip(Rm[i + i * L].x);
   for (int e = threadIdx.x; e < L * L; e += blockDim.x) Ri[e] = (e % L) == (e / L) ? m_one<R>() : czero<M>();
   __syncthreads();
-  for (int i = L - 1; i >= 0; --i) {
-    for (int j = i + threadIdx.x; j < L; j += blockDim.x) {
-      const M v = Ri[i + j * L];
-      Ri[i + j * L] = cmake(v.x * dinv[i], v.y * dinv[i]);
+  auto run = [&](auto tm) {
+    for (int i = L - 1; i >= 0; --i) {
+      for (int j = i + tm.rank; j < L; j += tm.size) {
+        const M v = Ri[i + j * L];
+        Ri[i + j * L] = cmake(v.x * dinv[i], v.y * dinv[i]);
+      }
+      tm.sync();
+      // rows r < i, columns j >= i: X_rj -= R_ri X_ij
+      const int nc = L - i;
+      for (int t = tm.rank; t < i * nc; t += tm.size) {
+        const int r = t % i, j = i + t / i;
+        Ri[r + j * L] = csub(Ri[r + j * L], cmul(Rm[r + i * L], Ri[i + j * L]));
+      }
+      tm.sync();
     }
-    __syncthreads();
-    // rows r < i, columns j >= i: X_rj -= R_ri X_ij
-    const int nc = L - i;
-    for (int t = threadIdx.x; t < i * nc; t += blockDim.x) {
-      const int r = t % i, j = i + t / i;
-      Ri[r + j * L] = csub(Ri[r + j * L], cmul(Rm[r + i * L], Ri[i + j * L]));
-    }
-    __syncthreads();
+  };
+  if (L <= kWarpL) {
+    if (threadIdx.x < 32) run(WarpTeam{(int)threadIdx.x, 32});
+  } else {
+    run(CtaTeam{(int)threadIdx.x, (int)blockDim.x});
   }
+  __syncthreads();
 }
 
 // Frobenius norm in FP64 (any scale): per-thread sums of |m|^2, a warp
