@@ -8,6 +8,7 @@
 // host only polls the control block every few iterations.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <type_traits>
@@ -166,6 +167,84 @@ __device__ bool chol_and_inverse(typename SmallMat<R>::M* m0, typename SmallMat<
   }
 }
 
+// The L x L steps of a COCG-RQ iteration on shared-memory matrices (the six
+// L x L work matrices of SMALL_PROLOGUE); each one-CTA kernel fills the inputs
+// (from reduced Gram partials) and calls one of them.
+template <typename R> struct SmallWork {
+  typename SmallMat<R>::M *m0, *m1, *m2, *m3, *m4, *m5;
+  int *piv, *colperm;
+};
+#define SMALL_WORK SmallWork<R>{m0, m1, m2, m3, m4, m5, piv, colperm}
+
+// QR step 1: R1 = chol(H), R1inv, with H = W^H W in w.m0.  false: breakdown.
+template <typename R>
+__device__ bool core_chol1(const SmallWork<R>& w, int L, double2* st, SolverCtl* ctl) {
+  const int LL = L * L;
+  if (!chol_and_inverse<R>(w.m0, w.m1, w.m2, L)) { fail(ctl); return false; }
+  sm_store(slot(st, kR1, L), w.m1, LL);
+  sm_store(slot(st, kR1Inv, L), w.m2, LL);
+  return true;
+}
+
+// COCG-RQ, the second CholQR2 step fused with beta, with H2 = W1^H W1 in
+// w.m0; load_gt(dst) puts W1^T W1 into a shared matrix.
+//   R2 = chol(H2), R2inv, tau = R2 R1, xi = tau xi, err, stopping test;
+//   Q' = W1 R2^-1, so Q'^T Q' = R2^-T (W1^T W1) R2^-1 without a pass over Q'
+//   (R2 is near the identity: the second CholQR2 factor);
+//   beta = (Q^T Q)^-1 (tau^T Q'^T Q') ; Q^T Q <- Q'^T Q'.
+// Returns false on breakdown or when the stopping test passed (done).
+template <typename R, class LoadGT>
+__device__ bool core_chol2_beta(const SmallWork<R>& w, int L, double2* st, SolverCtl* ctl, double tol, double* hist,
+                                int k, int full, LoadGT load_gt) {
+  const int LL = L * L;
+  if (!chol_and_inverse<R>(w.m0, w.m1, w.m2, L)) { fail(ctl); return false; }
+  sm_store(slot(st, kR2Inv, L), w.m2, LL);
+  sm_load(w.m3, slot(st, kR1, L), LL);
+  sm_matmul(w.m4, w.m1, w.m3, L, false);  // tau = R2 R1
+  sm_store(slot(st, kTau, L), w.m4, LL);
+  sm_load(w.m5, slot(st, kXi, L), LL);
+  sm_matmul(w.m0, w.m4, w.m5, L, false);  // xi = tau xi
+  sm_store(slot(st, kXi, L), w.m0, LL);
+  const double nrm = sm_fro<R>(w.m0, LL);
+  __shared__ int stop;
+  if (threadIdx.x == 0) {
+    const double err = nrm / ctl->bnorm;
+    ctl->err = err;
+    if (hist) hist[k] = err;
+    ctl->iter = k + 1;
+    stop = 0;
+    if (!isfinite(err)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; stop = 1; }
+    else if (err < tol) { ctl->done = 1; stop = 1; }
+  }
+  __syncthreads();
+  if (stop) return false;
+  load_gt(w.m0);                               // W1^T W1
+  sm_matmul(w.m3, w.m0, w.m2, L, false);       // (W1^T W1) R2^-1
+  sm_matmul(w.m5, w.m2, w.m3, L, true);        // Q'^T Q'
+  sm_matmul(w.m0, w.m4, w.m5, L, true);        // tau^T Q'^T Q'
+  sm_load(w.m1, slot(st, kQtQ, L), LL);
+  if (!sm_lu_solve<R>(w.m1, w.m0, L, L, full != 0, w.colperm, w.piv)) { fail(ctl); return false; }
+  sm_store(slot(st, kBeta, L), w.m0, LL);
+  sm_store(slot(st, kQtQ, L), w.m5, LL);
+  return true;
+}
+
+// COCG-RQ alpha with S^T AS in w.m0 and Q^T Q in w.m1 (have_qq; else the kept
+// slot): alpha = (S^T AS)^-1 (Q^T Q) ; A_xi = alpha xi ; -alpha.
+template <typename R>
+__device__ bool core_alpha(const SmallWork<R>& w, int L, double2* st, SolverCtl* ctl, bool have_qq, int full) {
+  const int LL = L * L;
+  if (have_qq) sm_store(slot(st, kQtQ, L), w.m1, LL);
+  else sm_load(w.m1, slot(st, kQtQ, L), LL);
+  if (!sm_lu_solve<R>(w.m0, w.m1, L, L, full != 0, w.colperm, w.piv)) { fail(ctl); return false; }
+  sm_store(slot(st, kAlpha, L), w.m1, LL);
+  sm_store(slot(st, kNAlpha, L), w.m1, LL, true);
+  sm_load(w.m2, slot(st, kXi, L), LL);
+  sm_matmul(w.m3, w.m1, w.m2, L, false);
+  sm_store(slot(st, kAXi, L), w.m3, LL);
+  return true;
+}
+
 // QR step 1: H = W^H W ; R1 = chol(H) ; R1inv
 template <typename R>
 __global__ void __launch_bounds__(kSmallThreads)
@@ -173,9 +252,7 @@ k_small_chol1(const double2* __restrict__ part, int nparts, int L, double2* st, 
   if (ctl_skip(ctl)) return;
   SMALL_PROLOGUE
   sm_reduce<R>(m0, part, nparts, LL);
-  if (!chol_and_inverse<R>(m0, m1, m2, L)) { fail(ctl); return; }
-  sm_store(slot(st, kR1, L), m1, LL);
-  sm_store(slot(st, kR1Inv, L), m2, LL);
+  core_chol1<R>(SMALL_WORK, L, st, ctl);
 }
 
 // QR step 2: H2 = W1^H W1 ; R2 = chol ; R2inv ; tau = R2 R1.
@@ -225,35 +302,7 @@ k_small_chol2_beta(const double2* __restrict__ part, int L, double2* st, SolverC
   if (ctl_skip(ctl)) return;
   SMALL_PROLOGUE
   sm_reduce<R>(m0, part, 1, LL);
-  if (!chol_and_inverse<R>(m0, m1, m2, L)) { fail(ctl); return; }
-  sm_store(slot(st, kR2Inv, L), m2, LL);
-  sm_load(m3, slot(st, kR1, L), LL);
-  sm_matmul(m4, m1, m3, L, false);  // tau = R2 R1
-  sm_store(slot(st, kTau, L), m4, LL);
-  sm_load(m5, slot(st, kXi, L), LL);
-  sm_matmul(m0, m4, m5, L, false);  // xi = tau xi
-  sm_store(slot(st, kXi, L), m0, LL);
-  const double nrm = sm_fro<R>(m0, LL);
-  __shared__ int stop;
-  if (threadIdx.x == 0) {
-    const double err = nrm / ctl->bnorm;
-    ctl->err = err;
-    if (hist) hist[k] = err;
-    ctl->iter = k + 1;
-    stop = 0;
-    if (!isfinite(err)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; stop = 1; }
-    else if (err < tol) { ctl->done = 1; stop = 1; }
-  }
-  __syncthreads();
-  if (stop) return;
-  sm_reduce<R>(m0, part + LL, 1, LL);  // W1^T W1
-  sm_matmul(m3, m0, m2, L, false);     // (W1^T W1) R2^-1
-  sm_matmul(m5, m2, m3, L, true);      // Q'^T Q'
-  sm_matmul(m0, m4, m5, L, true);      // tau^T Q'^T Q'
-  sm_load(m1, slot(st, kQtQ, L), LL);
-  if (!sm_lu_solve<R>(m1, m0, L, L, full != 0, colperm, piv)) { fail(ctl); return; }
-  sm_store(slot(st, kBeta, L), m0, LL);
-  sm_store(slot(st, kQtQ, L), m5, LL);
+  core_chol2_beta<R>(SMALL_WORK, L, st, ctl, tol, hist, k, full, [&](M* d) { sm_reduce<R>(d, part + LL, 1, LL); });
 }
 
 // COCG-RQ alpha: alpha = (S^T AS)^-1 (Q^T Q) ; A_xi = alpha xi ; -alpha
@@ -264,18 +313,8 @@ k_small_cocg_alpha(const double2* __restrict__ pSAS, const double2* __restrict__
   if (ctl_skip(ctl)) return;
   SMALL_PROLOGUE
   sm_reduce<R>(m0, pSAS, nparts, LL);
-  if (pQQ) {
-    sm_reduce<R>(m1, pQQ, nparts, LL);
-    sm_store(slot(st, kQtQ, L), m1, LL);
-  } else {
-    sm_load(m1, slot(st, kQtQ, L), LL);
-  }
-  if (!sm_lu_solve<R>(m0, m1, L, L, full != 0, colperm, piv)) { fail(ctl); return; }
-  sm_store(slot(st, kAlpha, L), m1, LL);
-  sm_store(slot(st, kNAlpha, L), m1, LL, true);
-  sm_load(m2, slot(st, kXi, L), LL);
-  sm_matmul(m3, m1, m2, L, false);
-  sm_store(slot(st, kAXi, L), m3, LL);
+  if (pQQ) sm_reduce<R>(m1, pQQ, nparts, LL);
+  core_alpha<R>(SMALL_WORK, L, st, ctl, pQQ != nullptr, full);
 }
 
 // COCG-RQ beta: beta = (Q^T Q)^-1 (tau^T Q'^T Q') ; Q^T Q <- Q'^T Q'
