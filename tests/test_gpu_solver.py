@@ -117,6 +117,26 @@ def test_mixed_matches_fp64_cross_sections():
     assert np.linalg.norm(X32 - X64) / np.linalg.norm(X64) < 1e-6
 
 
+def test_mixed_solve_on_fp32_and_double_float_tables_only():
+    """An operator holding only the tables a mixed solve uses (FP32 inner
+    solves, double-float true residuals) gives the same solution as one with
+    every table; an FP64 solve on it is refused."""
+    prob = bdda.make_problem(1500, 2.3 + 0.6j, seed=6, n_dirs=2)
+    opts = bdda.solve_opts("cocg_rq", precision=bdda.SOLVE_MIXED, true_tol=1e-8, itermax=2000)
+    full = bdda.Operator(prob.n, prob.lf, prob.k)
+    full.set_dipoles(prob.address)
+    lean = bdda.Operator(prob.n, prob.lf, prob.k, prec=bdda.PREC_FP32 | bdda.PREC_DF64)
+    lean.set_dipoles(prob.address)
+    Xf, sf = bdda.solve(full, prob.diag, prob.B, opts, allow_not_converged=False)
+    Xl, sl = bdda.solve(lean, prob.diag, prob.B, opts, allow_not_converged=False)
+    assert sl["true_res_max"] <= 1e-8 and sl["iterations"] == sf["iterations"]
+    assert np.array_equal(Xl, Xf)  # same tables, same kernels, same order: bitwise
+    res = krylov.true_residual(_oracle_amul(prob), prob.B, Xl)
+    assert np.all(res < 2e-8), res
+    with pytest.raises(bdda.BddaError):
+        bdda.solve(lean, prob.diag, prob.B, bdda.solve_opts("cocg_rq", precision=bdda.SOLVE_FP64, true_tol=1e-8))
+
+
 def test_solve_status_codes():
     prob, B = _small_problem(nocc=60, L=2)
     op = bdda.Operator(prob.n, prob.lf, prob.k)
