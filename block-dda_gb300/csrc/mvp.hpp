@@ -26,6 +26,7 @@ inline int z_warps_per_cta(int per_warp) {
 struct MvpGeom {
   int f;                       // components per dipole: 3 (E) or 6 (E, M)
   int nx, ny, nz;
+  int nzp;                     // row pitch of T1 / T2 along z: nz rounded up to a multiple of 4
   int Px, Py, Pz;
   AxisPlan px, py, pz;
   int nzt;                     // ceil(nz / kTZ)
@@ -106,8 +107,8 @@ struct KernelTimer {
 };
 
 // Workspace elements (complex T) the MVP needs for L right-hand sides.
-inline size_t mvp_t1_elems(const MvpGeom& g, int L) { return (size_t)g.f * L * g.Px * g.ny * g.nz; }
-inline size_t mvp_t2_elems(const MvpGeom& g, int L) { return (size_t)g.f * L * g.Px * g.Py * g.nz; }
+inline size_t mvp_t1_elems(const MvpGeom& g, int L) { return (size_t)g.f * L * g.Px * g.ny * g.nzp; }
+inline size_t mvp_t2_elems(const MvpGeom& g, int L) { return (size_t)g.f * L * g.Px * g.Py * g.nzp; }
 
 template <typename T>
 cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typename cplx<T>::type* x, int ldx,

@@ -14,8 +14,10 @@
 //   occ    : int32 [nx][ny][nz], dipole index of a lattice site or -1.
 //   tiles  : int32 list of (y, z-tile) pairs (y*nzt + zt, 8-wide z tiles)
 //            holding >= 1 dipole; tmask [ny][nzt] marks them.
-//   T1     : [3L][Px][ny][nz]  after the x pass (only rows of listed tiles valid)
-//   T2     : [3L][Px][Py][nz]  after the y pass; the z pass works in place
+//   T1     : [3L][Px][ny][nzp] after the x pass (only rows of listed tiles valid)
+//   T2     : [3L][Px][Py][nzp] after the y pass; the z pass works in place
+//            (nzp = nz rounded up to a multiple of 4: rows of complex FP32
+//            start on 32-byte sectors; the padding is never read)
 //   Ghat   : [Px][Py][6][Pz]  Ghat / (Px Py Pz), digit-reversed frequencies,
 //            components (xx, xy, xz, yy, yz, zz).
 //
@@ -54,7 +56,7 @@ __device__ __forceinline__ bool skip(const int* done) { return done && *(volatil
 // warps per CTA.
 template <typename T>
 __global__ void __launch_bounds__(kZWarps * 32)
-k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int fc, int Px, int Py, int nz, AxisPlan pz,
+k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int fc, int Px, int Py, int nz, int nzp, AxisPlan pz,
          const typename cplx<T>::type* __restrict__ twz, const typename cplx<T>::type* __restrict__ ghat,
          const int* done) {
   using C = typename cplx<T>::type;
@@ -69,8 +71,8 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int fc, int Px, int Py,
   const int l = (int)(task % L);
   const long long line = task / L;  // q * Py + qy
   C* s0 = reinterpret_cast<C*>(smem_raw) + (size_t)warp * fc * lw;
-  const size_t fstride = (size_t)Px * Py * nz;  // between fields
-  C* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nz;
+  const size_t fstride = (size_t)Px * Py * nzp;  // between fields
+  C* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nzp;
   const bool six = fc == 6;
   for (int z = lane; z < nz; z += 32) {
     const int a = skw(z, sh);
@@ -136,14 +138,14 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   if (timer) timer->begin(kPassA + pbase, st);
   if (!static_tile(kTileA))
     tile::k_pass_a<T><<<g.ntiles, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
-        x, ldx, nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, lx, p.twx, t1, done);
+        x, ldx, nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, t1, done);
   if (timer) timer->end(kPassA + pbase, st);
   if (serr != cudaSuccess) return serr;
   // B
   if (timer) timer->begin(kPassB + pbase, st);
   if (!static_tile(kTileB))
     tile::k_pass_y<T, false><<<grid_y, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
-        t1, t2, g.tmask, g.ny, g.nz, g.nzt, ntask_y, ly, p.twy, done);
+        t1, t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, done);
   if (timer) timer->end(kPassB + pbase, st);
   if (serr != cudaSuccess) return serr;
   // C
@@ -160,7 +162,7 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
       const int per_warp = g.f * plan_lw<C>(g.pz) * (int)sizeof(C);
       const int wpc = z_warps_per_cta(per_warp);
       const unsigned grid = (unsigned)((ntask + wpc - 1) / wpc);
-      k_pass_c<T><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.f, g.Px, g.Py, g.nz, g.pz, p.twz, p.ghat, done);
+      k_pass_c<T><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.f, g.Px, g.Py, g.nz, g.nzp, g.pz, p.twz, p.ghat, done);
     }
     if (timer) timer->end(kPassC + pbase, st);
   }
@@ -168,14 +170,14 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   if (timer) timer->begin(kPassD + pbase, st);
   if (!static_tile(kTileD))
     tile::k_pass_y<T, true><<<grid_y, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
-        t2, t1, g.tmask, g.ny, g.nz, g.nzt, ntask_y, ly, p.twy, done);
+        t2, t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, done);
   if (timer) timer->end(kPassD + pbase, st);
   if (serr != cudaSuccess) return serr;
   // E
   if (timer) timer->begin(kPassE + pbase, st);
   if (!static_tile(kTileE))
     tile::k_pass_e<T><<<g.ntiles, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
-        t1, nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, done);
+        t1, nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, done);
   if (timer) timer->end(kPassE + pbase, st);
   if (serr != cudaSuccess) return serr;
   return cudaGetLastError();

@@ -83,6 +83,7 @@ struct Op {
     MvpGeom g;
     g.f = f;
     g.nx = n[0]; g.ny = n[1]; g.nz = n[2];
+    g.nzp = (n[2] + 3) & ~3;  // 32-byte rows of complex FP32: aligned tile segments and column pairs
     g.Px = P[0]; g.Py = P[1]; g.Pz = P[2];
     g.px = plan[set][0]; g.py = plan[set][1]; g.pz = plan[set][2];
     g.nzt = (n[2] + kTZ - 1) / kTZ;

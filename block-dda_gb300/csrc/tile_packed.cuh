@@ -32,7 +32,7 @@ template <class P> constexpr int packed_y_pairs() {
 template <bool INV, class P, int NP>
 __global__ void __launch_bounds__(8 / NP * 32)
 k_pass_y2p(const float2* __restrict__ src, float2* __restrict__ dst, const unsigned char* __restrict__ tmask, int ny,
-           int nz, int nzt, int ntask, const float4* __restrict__ twy, const int* done) {
+           int nz, int nzp, int nzt, int ntask, const float4* __restrict__ twy, const int* done) {
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int Py = P::N, lw = P::LW;
@@ -51,10 +51,10 @@ k_pass_y2p(const float2* __restrict__ src, float2* __restrict__ dst, const unsig
     const int r = task / nzt2;  // f * Px + q
     const int z = zt2 * kTZ2 + tw;
     const bool zval = z < nz;
-    const float2* g = src + (size_t)r * nin * nz + z + (size_t)ty * nz;
+    const float2* g = src + (size_t)r * nin * nzp + z + (size_t)ty * nzp;
     const unsigned char* tm = tmask + (zval ? z / kTZ : 0) + (size_t)ty * nzt;
     float* lb = reinterpret_cast<float*>(pairs + (buf * kPairs + (tw >> 1)) * lw) + half;
-    for (int yy = ty; yy < nin; yy += kStep, g += (size_t)kStep * nz, tm += (size_t)kStep * nzt) {
+    for (int yy = ty; yy < nin; yy += kStep, g += (size_t)kStep * nzp, tm += (size_t)kStep * nzt) {
       const bool valid = zval && (INV || *tm);
       const float* gs = reinterpret_cast<const float*>(valid ? g : src);
       float* d = lb + 4 * P::addr(yy);
@@ -83,10 +83,10 @@ k_pass_y2p(const float2* __restrict__ src, float2* __restrict__ dst, const unsig
     const int r = task / nzt2;
     const int z = zt2 * kTZ2 + tw;
     if (z < nz) {
-      float2* ob = dst + (size_t)r * nout * nz + z + (size_t)ty * nz;
+      float2* ob = dst + (size_t)r * nout * nzp + z + (size_t)ty * nzp;
       const unsigned char* tm = tmask + z / kTZ + (size_t)ty * nzt;
       const float* lb = reinterpret_cast<const float*>(pairs + (buf * kPairs + (tw >> 1)) * lw) + half;
-      for (int yy = ty; yy < nout; yy += kStep, ob += (size_t)kStep * nz, tm += (size_t)kStep * nzt)
+      for (int yy = ty; yy < nout; yy += kStep, ob += (size_t)kStep * nzp, tm += (size_t)kStep * nzt)
         if (!INV || *tm) {
           const float* s = lb + 4 * P::addr(yy);
           *ob = make_float2(s[0], s[2]);

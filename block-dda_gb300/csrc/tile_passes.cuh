@@ -58,7 +58,7 @@ constexpr int kRowStep = kTileThreads / kTZ;
 template <typename T, class Line>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int fc, const int* __restrict__ occ,
-         const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, Line lay,
+         const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, Line lay,
          const typename cplx<T>::type* __restrict__ twx, typename cplx<T>::type* __restrict__ t1, const int* done) {
   using C = typename cplx<T>::type;
   if (skip(done)) return;
@@ -77,7 +77,7 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int 
     socc[idx] = z < nz ? occ[((size_t)xi * ny + y) * nz + z] : -1;
   }
   __syncthreads();
-  const size_t rowstride = (size_t)ny * nz;  // T1 stride between x rows
+  const size_t rowstride = (size_t)ny * nzp;  // T1 stride between x rows
   int l = 0, c = 0;
   for (int f = 0; f < nfield; ++f) {
     C* line = lines + ((f & 1) * kTZ + warp) * lw;
@@ -92,7 +92,7 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int 
     // drain: thread tid writes column w = tid % 8 of rows q = tid / 8 + 32 k
     if (zval) {
       const C* lb = lines + ((f & 1) * kTZ + tw8) * lw;
-      C* out = t1 + (size_t)f * Px * rowstride + (size_t)y * nz + z0 + tw8 + (size_t)tq * rowstride;
+      C* out = t1 + (size_t)f * Px * rowstride + (size_t)y * nzp + z0 + tw8 + (size_t)tq * rowstride;
       for (int q = tq; q < Px; q += kRowStep, out += kRowStep * rowstride) *out = lb[lay.addr(q)];
     }
     if (++c == fc) { c = 0; ++l; }
@@ -106,7 +106,7 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int 
 template <typename T, bool INV, class Line>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type* __restrict__ dst,
-         const unsigned char* __restrict__ tmask, int ny, int nz, int nzt, int ntask, Line lay,
+         const unsigned char* __restrict__ tmask, int ny, int nz, int nzp, int nzt, int ntask, Line lay,
          const typename cplx<T>::type* __restrict__ twy, const int* done) {
   using C = typename cplx<T>::type;
   if (skip(done)) return;
@@ -126,10 +126,10 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
     const int r = task / nzt;  // f * Px + q
     const int z0 = zt * kTZ;
     const bool zval = z0 + tw8 < nz;
-    const C* g = src + (size_t)r * in_rows * nz + z0 + tw8 + (size_t)ty * nz;
+    const C* g = src + (size_t)r * in_rows * nzp + z0 + tw8 + (size_t)ty * nzp;
     const unsigned char* tm = tmask + zt + (size_t)ty * nzt;
     C* lb = lines + (buf * kTZ + tw8) * lw;
-    for (int yy = ty; yy < nin; yy += kRowStep, g += (size_t)kRowStep * nz, tm += (size_t)kRowStep * nzt) {
+    for (int yy = ty; yy < nin; yy += kRowStep, g += (size_t)kRowStep * nzp, tm += (size_t)kRowStep * nzt) {
       const bool valid = zval && (INV || *tm);
       cp_async<sizeof(C)>(lb + lay.addr(yy), valid ? g : src, valid);
     }
@@ -155,10 +155,10 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
     const int r = task / nzt;
     const int z0 = zt * kTZ;
     if (z0 + tw8 < nz) {
-      C* ob = dst + (size_t)r * out_rows * nz + z0 + tw8 + (size_t)ty * nz;
+      C* ob = dst + (size_t)r * out_rows * nzp + z0 + tw8 + (size_t)ty * nzp;
       const unsigned char* tm = tmask + zt + (size_t)ty * nzt;
       const C* lb = lines + (buf * kTZ + tw8) * lw;
-      for (int yy = ty; yy < nout; yy += kRowStep, ob += (size_t)kRowStep * nz, tm += (size_t)kRowStep * nzt)
+      for (int yy = ty; yy < nout; yy += kRowStep, ob += (size_t)kRowStep * nzp, tm += (size_t)kRowStep * nzt)
         if (!INV || *tm) *ob = lb[lay.addr(yy)];
     }
     __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
@@ -175,7 +175,7 @@ constexpr int kRowStep2 = kTileThreads / kTZ2;
 template <bool INV, class P>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_y2(const float2* __restrict__ src, float2* __restrict__ dst, const unsigned char* __restrict__ tmask, int ny,
-          int nz, int nzt, int ntask, const float2* __restrict__ twy, const int* done) {
+          int nz, int nzp, int nzt, int ntask, const float2* __restrict__ twy, const int* done) {
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int Py = P::N, lw = P::LW;
@@ -190,10 +190,10 @@ k_pass_y2(const float2* __restrict__ src, float2* __restrict__ dst, const unsign
     const int r = task / nzt2;  // f * Px + q
     const int z = zt2 * kTZ2 + tw;
     const bool zval = z < nz;
-    const float2* g = src + (size_t)r * nin * nz + z + (size_t)ty * nz;
+    const float2* g = src + (size_t)r * nin * nzp + z + (size_t)ty * nzp;
     const unsigned char* tm = tmask + (zval ? z / kTZ : 0) + (size_t)ty * nzt;
     float2* lb = lines + (buf * kTZ2 + tw) * lw;
-    for (int yy = ty; yy < nin; yy += kRowStep2, g += (size_t)kRowStep2 * nz, tm += (size_t)kRowStep2 * nzt) {
+    for (int yy = ty; yy < nin; yy += kRowStep2, g += (size_t)kRowStep2 * nzp, tm += (size_t)kRowStep2 * nzt) {
       const bool valid = zval && (INV || *tm);
       cp_async<sizeof(float2)>(lb + P::addr(yy), valid ? g : src, valid);
     }
@@ -219,10 +219,10 @@ k_pass_y2(const float2* __restrict__ src, float2* __restrict__ dst, const unsign
     const int r = task / nzt2;
     const int z = zt2 * kTZ2 + tw;
     if (z < nz) {
-      float2* ob = dst + (size_t)r * nout * nz + z + (size_t)ty * nz;
+      float2* ob = dst + (size_t)r * nout * nzp + z + (size_t)ty * nzp;
       const unsigned char* tm = tmask + z / kTZ + (size_t)ty * nzt;
       const float2* lb = lines + (buf * kTZ2 + tw) * lw;
-      for (int yy = ty; yy < nout; yy += kRowStep2, ob += (size_t)kRowStep2 * nz, tm += (size_t)kRowStep2 * nzt)
+      for (int yy = ty; yy < nout; yy += kRowStep2, ob += (size_t)kRowStep2 * nzp, tm += (size_t)kRowStep2 * nzt)
         if (!INV || *tm) *ob = lb[P::addr(yy)];
     }
     __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
@@ -235,7 +235,7 @@ k_pass_y2(const float2* __restrict__ src, float2* __restrict__ dst, const unsign
 template <typename T, class Line>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, const int* __restrict__ occ,
-         const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, Line lay,
+         const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, Line lay,
          const typename cplx<T>::type* __restrict__ twx, const typename cplx<T>::type* __restrict__ x, int ldx,
          const typename cplx<T>::type* __restrict__ diag, const typename cplx<T>::type* __restrict__ jpre,
          typename cplx<T>::type* __restrict__ y, int ldy, const int* done) {
@@ -249,7 +249,7 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, cons
   const int tile = tiles[blockIdx.x];
   const int yy = tile / nzt, z0 = (tile - yy * nzt) * kTZ;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const size_t rowstride = (size_t)ny * nz;
+  const size_t rowstride = (size_t)ny * nzp;
   for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
     const int xi = idx >> 3, w = idx & 7, z = z0 + w;
     socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
@@ -258,7 +258,7 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, cons
   const bool zval = z0 + tw8 < nz;
   // fill: thread tid loads column w = tid % 8 of rows q = tid / 8 + 32 k (zero-filled past nz)
   auto issue = [&](int f, int buf) {
-    const C* g = t1 + (size_t)f * Px * rowstride + (size_t)yy * nz + z0 + tw8 + (size_t)tq * rowstride;
+    const C* g = t1 + (size_t)f * Px * rowstride + (size_t)yy * nzp + z0 + tw8 + (size_t)tq * rowstride;
     C* lb = lines + (buf * kTZ + tw8) * lw;
     for (int q = tq; q < Px; q += kRowStep, g += (size_t)kRowStep * rowstride)
       cp_async<sizeof(C)>(lb + lay.addr(q), zval ? g : t1, zval);
@@ -303,7 +303,7 @@ __device__ __forceinline__ float2* x2_line(float2* lines, int buf, int w, int h)
 template <class P>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_a2(const float2* __restrict__ x, int ldx, int nfield, int fc, const int* __restrict__ occ,
-          const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, const float2* __restrict__ twx,
+          const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, const float2* __restrict__ twx,
           float2* __restrict__ t1, const int* done) {
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -320,7 +320,7 @@ k_pass_a2(const float2* __restrict__ x, int ldx, int nfield, int fc, const int* 
     socc[idx] = z < nz ? occ[((size_t)xi * ny + y) * nz + z] : -1;
   }
   __syncthreads();
-  const size_t rowstride = (size_t)ny * nz;
+  const size_t rowstride = (size_t)ny * nzp;
   for (int f = 0, it = 0; f < nfield; f += 2, ++it) {
     const int buf = it & 1;
     const int nh = f + 1 < nfield ? 2 : 1;
@@ -340,7 +340,7 @@ k_pass_a2(const float2* __restrict__ x, int ldx, int nfield, int fc, const int* 
     if (zval) {
       for (int h = 0; h < nh; ++h) {
         const float2* lb = x2_line<P>(lines, buf, tw8, h);
-        float2* out = t1 + (size_t)(f + h) * Px * rowstride + (size_t)y * nz + z0 + tw8 + (size_t)tq * rowstride;
+        float2* out = t1 + (size_t)(f + h) * Px * rowstride + (size_t)y * nzp + z0 + tw8 + (size_t)tq * rowstride;
         for (int q = tq; q < Px; q += kRowStep, out += kRowStep * rowstride) *out = lb[P::addr(q)];
       }
     }
@@ -350,7 +350,7 @@ k_pass_a2(const float2* __restrict__ x, int ldx, int nfield, int fc, const int* 
 template <class P>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_e2(const float2* __restrict__ t1, int nfield, int fc, const int* __restrict__ occ,
-          const int* __restrict__ tiles, int nx, int ny, int nz, int nzt, const float2* __restrict__ twx,
+          const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, const float2* __restrict__ twx,
           const float2* __restrict__ x, int ldx, const float2* __restrict__ diag, const float2* __restrict__ jpre,
           float2* __restrict__ y, int ldy, const int* done) {
   if (skip(done)) return;
@@ -361,7 +361,7 @@ k_pass_e2(const float2* __restrict__ t1, int nfield, int fc, const int* __restri
   const int tile = tiles[blockIdx.x];
   const int yy = tile / nzt, z0 = (tile - yy * nzt) * kTZ;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const size_t rowstride = (size_t)ny * nz;
+  const size_t rowstride = (size_t)ny * nzp;
   for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
     const int xi = idx >> 3, w = idx & 7, z = z0 + w;
     socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
@@ -372,7 +372,7 @@ k_pass_e2(const float2* __restrict__ t1, int nfield, int fc, const int* __restri
   auto issue = [&](int f, int buf) {
     const int nh = f + 1 < nfield ? 2 : 1;
     for (int h = 0; h < nh; ++h) {
-      const float2* g = t1 + (size_t)(f + h) * Px * rowstride + (size_t)yy * nz + z0 + tw8 + (size_t)tq * rowstride;
+      const float2* g = t1 + (size_t)(f + h) * Px * rowstride + (size_t)yy * nzp + z0 + tw8 + (size_t)tq * rowstride;
       float2* lb = x2_line<P>(lines, buf, tw8, h);
       for (int q = tq; q < Px; q += kRowStep, g += (size_t)kRowStep * rowstride)
         cp_async<sizeof(float2)>(lb + P::addr(q), zval ? g : t1, zval);

@@ -42,38 +42,38 @@ cudaError_t launch(int pass, const TileArgs& a) {
     case kTileA:
       if ((e = set_smem(tile::k_pass_a2<P>, smem_ae, oa, ca)) != cudaSuccess) return e;
       tile::k_pass_a2<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
-          a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, a.twx, a.t1, a.done);
+          a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.t1, a.done);
       break;
     case kTileB:
       if constexpr (NPY > 0) {
         if (a.twyp) {
           if ((e = set_smem(tile::k_pass_y2p<false, P, NPY>, smem_bd, obp, cbp)) != cudaSuccess) return e;
-          tile::k_pass_y2p<false, P, NPY><<<grid2p, 8 / NPY * 32, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzt,
+          tile::k_pass_y2p<false, P, NPY><<<grid2p, 8 / NPY * 32, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
                                                                              ntask2, a.twyp, a.done);
           break;
         }
       }
       if ((e = set_smem(tile::k_pass_y2<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
-      tile::k_pass_y2<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzt,
+      tile::k_pass_y2<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
                                                                         ntask2, a.twy, a.done);
       break;
     case kTileD:
       if constexpr (NPY > 0) {
         if (a.twyp) {
           if ((e = set_smem(tile::k_pass_y2p<true, P, NPY>, smem_bd, odp, cdp)) != cudaSuccess) return e;
-          tile::k_pass_y2p<true, P, NPY><<<grid2p, 8 / NPY * 32, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzt,
+          tile::k_pass_y2p<true, P, NPY><<<grid2p, 8 / NPY * 32, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
                                                                             ntask2, a.twyp, a.done);
           break;
         }
       }
       if ((e = set_smem(tile::k_pass_y2<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
-      tile::k_pass_y2<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzt,
+      tile::k_pass_y2<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
                                                                        ntask2, a.twy, a.done);
       break;
     default:
       if ((e = set_smem(tile::k_pass_e2<P>, smem_ae, oe, ce)) != cudaSuccess) return e;
       tile::k_pass_e2<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
-          a.t1, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzt, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
+          a.t1, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
           a.done);
       break;
   }

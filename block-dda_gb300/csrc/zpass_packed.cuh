@@ -55,7 +55,7 @@ __device__ __forceinline__ void z_product_pair(ulonglong2* __restrict__ s, int l
 
 template <class P>
 __global__ void __launch_bounds__(kZWarps * 32)
-k_pass_c_packed(float2* __restrict__ t2, int L, int Px, int Py, int nz, const float4* __restrict__ twz,
+k_pass_c_packed(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp, const float4* __restrict__ twz,
                 const float2* __restrict__ ghat, const int* done) {
   if (done && *(volatile const int*)done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -69,8 +69,8 @@ k_pass_c_packed(float2* __restrict__ t2, int L, int Px, int Py, int nz, const fl
   const int la = 2 * lp;
   const bool has_b = la + 1 < L;
   ulonglong2* s0 = reinterpret_cast<ulonglong2*>(smem_raw) + (size_t)warp * 3 * LW;
-  const size_t fstride = (size_t)Px * Py * nz;  // between fields
-  float2* g0 = t2 + (size_t)(3 * la) * fstride + (size_t)line * nz;
+  const size_t fstride = (size_t)Px * Py * nzp;  // between fields
+  float2* g0 = t2 + (size_t)(3 * la) * fstride + (size_t)line * nzp;
   const ptrdiff_t boff = has_b ? (ptrdiff_t)(3 * fstride) : 0;  // right-hand side la + 1
   pk::stage0_from_global<P, 3>(s0, twz, lane, nz, g0, fstride, boff);
   pk::forward<P, 3, 1>(s0, twz, lane, nz);
@@ -94,7 +94,7 @@ cudaError_t launch(const MvpGeom& g, float2* t2, int L, const float4* twz, const
   const int wpc = z_warps_per_cta(per_warp);
   const long long ntask = (long long)g.Px * g.Py * ((L + 1) / 2);
   const unsigned grid = (unsigned)((ntask + wpc - 1) / wpc);
-  k_pass_c_packed<P><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.Px, g.Py, g.nz, twz, ghat, done);
+  k_pass_c_packed<P><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.Px, g.Py, g.nz, g.nzp, twz, ghat, done);
   return cudaGetLastError();
 }
 

@@ -23,7 +23,7 @@ namespace zstatic {
 
 template <class P, bool SIX>
 __global__ void __launch_bounds__(kZWarps * 32)
-k_pass_c_static(float2* __restrict__ t2, int L, int Px, int Py, int nz, const float2* __restrict__ twz,
+k_pass_c_static(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp, const float2* __restrict__ twz,
                 const float2* __restrict__ ghat, const int* done) {
   constexpr int fc = SIX ? 6 : 3;
   if (done && *(volatile const int*)done) return;
@@ -35,8 +35,8 @@ k_pass_c_static(float2* __restrict__ t2, int L, int Px, int Py, int nz, const fl
   const int l = (int)(task % L);
   const long long line = task / L;  // q * Py + qy
   float2* s0 = reinterpret_cast<float2*>(smem_raw) + (size_t)warp * fc * LW;
-  const size_t fstride = (size_t)Px * Py * nz;  // between fields
-  float2* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nz;
+  const size_t fstride = (size_t)Px * Py * nzp;  // between fields
+  float2* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nzp;
   constexpr bool six = SIX;
   constexpr int halves = six ? 2 : 1;  // line triples: E, then M
   // the first forward stage reads the lines straight from T2 (no staging loop)
@@ -63,7 +63,7 @@ cudaError_t launch_f(const MvpGeom& g, float2* t2, int L, const float2* twz, con
   const int wpc = z_warps_per_cta(per_warp);
   const long long ntask = (long long)g.Px * g.Py * L;
   const unsigned grid = (unsigned)((ntask + wpc - 1) / wpc);
-  k_pass_c_static<P, SIX><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.Px, g.Py, g.nz, twz, ghat, done);
+  k_pass_c_static<P, SIX><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.Px, g.Py, g.nz, g.nzp, twz, ghat, done);
   return cudaGetLastError();
 }
 
