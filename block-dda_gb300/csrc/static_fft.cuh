@@ -182,5 +182,75 @@ __device__ __forceinline__ void inverse_to_global(float2* sm, const float2* tw, 
   stage0_to_global<P, NL>(sm, tw, lane, nv, gdst, gstride);
 }
 
+// ---- two lines interleaved element by element ---------------------------------
+// Element idx of line h (0 or 1) at sm[2 * P::addr(idx) + h]: a 16-byte pair
+// per element, so a tile can be staged two columns per 16-byte copy.  Lane
+// parity selects the line (t = 2 u + h), so the lanes of a butterfly's two
+// lines touch adjacent words.
+template <class P, int s, bool INV>
+__device__ __forceinline__ void stage_il(float2* __restrict__ sm, const float2* __restrict__ tw, int lane, int nv) {
+  constexpr int R = P::rad[s];
+  constexpr int M = P::M(s);
+  constexpr int Ls = M * R;
+  constexpr int B = P::N / R;
+  constexpr int T = 2 * B;
+  constexpr int ts = P::N / Ls;
+  constexpr int off = 2 * ((s == P::nst - 1) ? 1 : (M / P::Rl) * P::S);
+  constexpr bool prune_in = !INV && s == 0;
+  constexpr bool prune_out = INV && s == 0;
+  for (int t = lane; t < T; t += 32) {
+    const int h = t & 1;
+    const int u = t >> 1;
+    const int b = u / M, n1 = u - b * M;
+    const int idx0 = b * Ls + n1;
+    float2* p = sm + 2 * P::addr(idx0) + h;
+    float2 v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      if (prune_in) v[i] = (idx0 + i * M < nv) ? p[i * off] : make_float2(0.f, 0.f);
+      else v[i] = p[i * off];
+    }
+    if (!INV) {
+      dft<R, false>(v);
+      if (M > 1 && n1 != 0) {
+        const int step = n1 * ts;
+#pragma unroll
+        for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tw + k * step));
+      }
+    } else {
+      if (M > 1 && n1 != 0) {
+        const int step = n1 * ts;
+#pragma unroll
+        for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tw + k * step));
+      }
+      dft<R, true>(v);
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      if (prune_out) {
+        if (idx0 + i * M < nv) p[i * off] = v[i];
+      } else {
+        p[i * off] = v[i];
+      }
+    }
+  }
+  __syncwarp();
+}
+
+template <class P, int s = 0>
+__device__ __forceinline__ void forward_il(float2* sm, const float2* tw, int lane, int nv) {
+  if constexpr (s < P::nst) {
+    stage_il<P, s, false>(sm, tw, lane, nv);
+    forward_il<P, s + 1>(sm, tw, lane, nv);
+  }
+}
+template <class P, int s = P::nst - 1>
+__device__ __forceinline__ void inverse_il(float2* sm, const float2* tw, int lane, int nv) {
+  if constexpr (s >= 0) {
+    stage_il<P, s, true>(sm, tw, lane, nv);
+    inverse_il<P, s - 1>(sm, tw, lane, nv);
+  }
+}
+
 }  // namespace sfft
 }  // namespace bdda

@@ -232,6 +232,74 @@ k_pass_y2(const float2* __restrict__ src, float2* __restrict__ dst, const unsign
 // ---------------------------------------------------------------- pass E
 // One CTA per listed (y, z-tile); loops over fields with the next field's
 // tile prefetched by cp.async; scatters the occupied sites.
+// ---------------------------------------------------------------- pass B / D, column pairs
+// Same tasks as k_pass_y2 (16 z-columns, warp w transforms columns 2w and
+// 2w + 1), with the two columns of a pair interleaved in shared memory
+// (sfft::stage_il): the tile is staged and stored one column pair -- 16
+// contiguous bytes, since rows are padded to a multiple of 4 elements -- per
+// copy, half the copies of k_pass_y2 (whose warps stall on the shared-memory
+// queue).  A pair whose second column is row padding transforms it and never
+// stores it.
+constexpr int kPairsY = kTZ2 / 2;
+constexpr int kRowStepP = kTileThreads / kPairsY;
+
+template <bool INV, class P>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_y2i(const float2* __restrict__ src, float2* __restrict__ dst, const unsigned char* __restrict__ tmask, int ny,
+           int nz, int nzp, int nzt, int ntask, const float2* __restrict__ twy, const int* done) {
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int Py = P::N, lw = P::LW;
+  float2* tile = reinterpret_cast<float2*>(smem_raw);  // [2][kPairsY][lw][2]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nin = INV ? Py : ny;
+  const int nout = INV ? ny : Py;
+  const int nzt2 = (nz + kTZ2 - 1) / kTZ2;
+  const int tp = tid & (kPairsY - 1), ty = tid / kPairsY;  // column pair and first row of this thread
+  auto issue = [&](int task, int buf) {
+    const int zt2 = task % nzt2;
+    const int r = task / nzt2;  // f * Px + q
+    const int z = zt2 * kTZ2 + 2 * tp;
+    const bool zval = z < nz;
+    const float2* g = src + (size_t)r * nin * nzp + z + (size_t)ty * nzp;
+    const unsigned char* tm = tmask + (zval ? z / kTZ : 0) + (size_t)ty * nzt;
+    float2* lb = tile + (size_t)(buf * kPairsY + tp) * lw * 2;
+    for (int yy = ty; yy < nin; yy += kRowStepP, g += (size_t)kRowStepP * nzp, tm += (size_t)kRowStepP * nzt) {
+      const bool valid = zval && (INV || *tm);
+      cp_async<16>(lb + 2 * P::addr(yy), valid ? g : src, valid);
+    }
+    cp_commit();
+  };
+  int task = blockIdx.x;
+  if (task < ntask) issue(task, 0);
+  for (int it = 0; task < ntask; ++it, task += gridDim.x) {
+    const int buf = it & 1;
+    const int next = task + gridDim.x;
+    if (next < ntask) {
+      issue(next, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    float2* wl = tile + (size_t)(buf * kPairsY + warp) * lw * 2;
+    if (!INV) sfft::forward_il<P>(wl, twy, lane, ny);
+    else sfft::inverse_il<P>(wl, twy, lane, ny);
+    __syncthreads();
+    const int zt2 = task % nzt2;
+    const int r = task / nzt2;
+    const int z = zt2 * kTZ2 + 2 * tp;
+    if (z < nz) {
+      float4* ob = reinterpret_cast<float4*>(dst + (size_t)r * nout * nzp + z + (size_t)ty * nzp);
+      const unsigned char* tm = tmask + z / kTZ + (size_t)ty * nzt;
+      const float4* lb = reinterpret_cast<const float4*>(tile + (size_t)(buf * kPairsY + tp) * lw * 2);
+      for (int yy = ty; yy < nout; yy += kRowStepP, ob += (size_t)kRowStepP * nzp / 2, tm += (size_t)kRowStepP * nzt)
+        if (!INV || *tm) *ob = lb[P::addr(yy)];
+    }
+    __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
+  }
+}
+
 template <typename T, class Line>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, const int* __restrict__ occ,

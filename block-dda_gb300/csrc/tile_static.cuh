@@ -53,8 +53,8 @@ cudaError_t launch(int pass, const TileArgs& a) {
           break;
         }
       }
-      if ((e = set_smem(tile::k_pass_y2<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
-      tile::k_pass_y2<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
+      if ((e = set_smem(tile::k_pass_y2i<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
+      tile::k_pass_y2i<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
                                                                         ntask2, a.twy, a.done);
       break;
     case kTileD:
@@ -66,8 +66,8 @@ cudaError_t launch(int pass, const TileArgs& a) {
           break;
         }
       }
-      if ((e = set_smem(tile::k_pass_y2<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
-      tile::k_pass_y2<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
+      if ((e = set_smem(tile::k_pass_y2i<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
+      tile::k_pass_y2i<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
                                                                        ntask2, a.twy, a.done);
       break;
     default:
