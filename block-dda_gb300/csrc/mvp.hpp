@@ -44,9 +44,7 @@ template <typename T> struct MvpPrec {
   const C* twy;
   const C* twz;
   const C* ghat;  // [Px][Py][6 or 9][Pz] (digit-reversed frequencies), divided by Px*Py*Pz
-  const float4* twzp = nullptr;  // complex FP32: twiddle pairs {wx, wx, wy, wy} per axis (packed kernels)
-  const float4* twxp = nullptr;
-  const float4* twyp = nullptr;
+  const float4* twzp = nullptr;  // complex FP32: z twiddle pairs {wx, wx, wy, wy} (packed z pass)
 };
 
 // Timed kernel classes: the five MVP passes per precision (FP32 first), then
@@ -136,8 +134,6 @@ struct TileArgs {
   int grid_y, ntask_y;  // persistent grid and tasks of passes B / D
   cudaStream_t st;
   const int* done;
-  const float4* twxp;   // twiddle pairs of the packed kernels (null: scalar kernels)
-  const float4* twyp;
 };
 enum TilePass { kTileA = 0, kTileB, kTileD, kTileE };
 

@@ -123,8 +123,7 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   cudaError_t serr = cudaSuccess;
   auto static_tile = [&](int pass) -> bool {
     if constexpr (std::is_same<T, float>::value) {
-      const TileArgs a{&g, x, ldx, y, ldy, nfield, diag, jpre, t1, t2, p.twx, p.twy, grid_y, ntask_y, st, done,
-                       p.twxp, p.twyp};
+      const TileArgs a{&g, x, ldx, y, ldy, nfield, diag, jpre, t1, t2, p.twx, p.twy, grid_y, ntask_y, st, done};
       cudaError_t e = cudaSuccess;
       const bool ok = launch_tile_static(pass, a, &e);
       if (ok && e != cudaSuccess) serr = e;

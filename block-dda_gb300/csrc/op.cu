@@ -159,7 +159,7 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
   using CA = typename cplx<A>::type;
   static_assert(sizeof(CA) == sizeof(C), "storage layouts agree");
   const MvpPrec<T> tb = op->tables<T>();
-  MvpPrec<A> ta{(const CA*)tb.twx, (const CA*)tb.twy, (const CA*)tb.twz, (const CA*)tb.ghat, tb.twzp, tb.twxp, tb.twyp};
+  MvpPrec<A> ta{(const CA*)tb.twx, (const CA*)tb.twy, (const CA*)tb.twz, (const CA*)tb.ghat, tb.twzp};
   cudaError_t e = launch_block_mvp<A>(g, ta, (const CA*)x, ldx, (CA*)y, ldy, L, (const CA*)diag, (const CA*)jpre,
                                       op->t1[pi].as<CA>(), op->t2[pi].as<CA>(), st, &op->timer, done);
   if (e != cudaSuccess) return cuda_fail(e, "block MVP launch");
@@ -257,7 +257,7 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     BDDA_CUDA(cudaMemcpyAsync(op->tw32[i].p, tf.data(), tf.size() * sizeof(float2), cudaMemcpyHostToDevice, op->stream));
     std::vector<float4> tp(tw.size());
     for (size_t t = 0; t < tw.size(); ++t) tp[t] = make_float4(tf[t].x, tf[t].x, tf[t].y, tf[t].y);
-    if (!std::getenv("BDDA_NO_PACK")) {
+    if (i == 2 && !std::getenv("BDDA_NO_PACK")) {
       BDDA_CUDA(op->tw32p[i].ensure(tp.size() * sizeof(float4), op->stream));
       BDDA_CUDA(cudaMemcpyAsync(op->tw32p[i].p, tp.data(), tp.size() * sizeof(float4), cudaMemcpyHostToDevice, op->stream));
     }

@@ -69,7 +69,7 @@ struct Op {
   // the single-line x / y axes).  Each set has its own Green spectrum order.
   AxisPlan plan[2][3];
   DevBuf tw64[3], tw32[3], twdf[3];
-  DevBuf tw32p[3];  // complex FP32 twiddle pairs {wx, wx, wy, wy} of the packed kernels
+  DevBuf tw32p[3];  // complex FP32 twiddle pairs {wx, wx, wy, wy} of the packed z pass ([2] only)
   DevBuf ghat64, ghat32, ghatdf;
   Occupancy dip;    // dipole occupancy (set_dipoles)
   Occupancy cub;    // every cuboid site (the reference's MBT_fft_mvp vector)
@@ -103,8 +103,7 @@ template <> inline MvpPrec<double> Op::tables<double>() const {
   return {tw64[0].as<double2>(), tw64[1].as<double2>(), tw64[2].as<double2>(), ghat64.as<double2>()};
 }
 template <> inline MvpPrec<float> Op::tables<float>() const {
-  return {tw32[0].as<float2>(), tw32[1].as<float2>(), tw32[2].as<float2>(), ghat32.as<float2>(), tw32p[2].as<float4>(),
-          tw32p[0].as<float4>(), tw32p[1].as<float4>()};
+  return {tw32[0].as<float2>(), tw32[1].as<float2>(), tw32[2].as<float2>(), ghat32.as<float2>(), tw32p[2].as<float4>()};
 }
 template <> inline MvpPrec<dfl> Op::tables<dfl>() const {
   return {twdf[0].as<dfc>(), twdf[1].as<dfc>(), twdf[2].as<dfc>(), ghatdf.as<dfc>()};

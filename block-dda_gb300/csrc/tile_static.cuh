@@ -10,7 +10,6 @@
 #include <mutex>
 
 #include "mvp.hpp"
-#include "tile_packed.cuh"
 #include "tile_passes.cuh"
 
 namespace bdda {
@@ -32,11 +31,8 @@ cudaError_t launch(int pass, const TileArgs& a) {
   const int smem_bd = 2 * tile::kTZ2 * P::LW * (int)sizeof(float2);  // y passes: 16 columns per task
   const int ntask2 = a.nfield * g.Px * ((g.nz + tile::kTZ2 - 1) / tile::kTZ2);
   const int grid2 = std::min(ntask2, a.grid_y);
-  constexpr int NPY = tile::packed_y_pairs<P>();  // packed y kernel: pairs per warp (0: scalar kernel)
-  const int grid2p = std::min(ntask2, a.grid_y * NPY);  // CTAs of 8 / NPY warps
-  static std::once_flag oa, ob, od, oe, obp, odp;
-  static cudaError_t ca = cudaSuccess, cb = cudaSuccess, cd = cudaSuccess, ce = cudaSuccess, cbp = cudaSuccess,
-                     cdp = cudaSuccess;
+  static std::once_flag oa, ob, od, oe;
+  static cudaError_t ca = cudaSuccess, cb = cudaSuccess, cd = cudaSuccess, ce = cudaSuccess;
   cudaError_t e = cudaSuccess;
   switch (pass) {
     case kTileA:
@@ -45,27 +41,11 @@ cudaError_t launch(int pass, const TileArgs& a) {
           a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.t1, a.done);
       break;
     case kTileB:
-      if constexpr (NPY > 0) {
-        if (a.twyp) {
-          if ((e = set_smem(tile::k_pass_y2p<false, P, NPY>, smem_bd, obp, cbp)) != cudaSuccess) return e;
-          tile::k_pass_y2p<false, P, NPY><<<grid2p, 8 / NPY * 32, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
-                                                                             ntask2, a.twyp, a.done);
-          break;
-        }
-      }
       if ((e = set_smem(tile::k_pass_y2i<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
       tile::k_pass_y2i<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
                                                                         ntask2, a.twy, a.done);
       break;
     case kTileD:
-      if constexpr (NPY > 0) {
-        if (a.twyp) {
-          if ((e = set_smem(tile::k_pass_y2p<true, P, NPY>, smem_bd, odp, cdp)) != cudaSuccess) return e;
-          tile::k_pass_y2p<true, P, NPY><<<grid2p, 8 / NPY * 32, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
-                                                                            ntask2, a.twyp, a.done);
-          break;
-        }
-      }
       if ((e = set_smem(tile::k_pass_y2i<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
       tile::k_pass_y2i<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
                                                                        ntask2, a.twy, a.done);

@@ -81,6 +81,13 @@ k_pass_c_packed(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp,
   pk::stage0_to_global<P, 3>(s0, twz, lane, nz, g0, fstride, boff, has_b);
 }
 
+// The packed kernel keeps twice the bytes of lines per warp (16-byte pair
+// elements); it pays where three 8-warp CTAs still fit on an SM (line pitch
+// <= 197: Pz up to ~190).  Longer lines keep the scalar kernel, whose
+// occupancy is then twice as high (Pz=250: 9.9 ms scalar vs 10.3 ms packed
+// per N=65536, L=32 block MVP; Pz=120: 0.35 vs 0.31 ms at N=8192, L=16).
+template <class P> constexpr bool worth() { return 3 * kZWarps * 3 * P::LW * 16 <= kZSmemMax; }
+
 template <class P>
 cudaError_t launch(const MvpGeom& g, float2* t2, int L, const float4* twz, const float2* ghat, cudaStream_t st,
                    const int* done) {

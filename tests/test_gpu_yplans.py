@@ -2,9 +2,9 @@
 
 For each padded y length a box can produce (Py = smallest 5-smooth >= 2 ny,
 ny = 1..256) the FP32 block MVP must agree with the FP64 block MVP to the FP32
-tolerance.  Plans whose stages all hold >= 20 butterflies per line run the
-packed-pair y kernel (two z-columns in the lanes of f32x2 instructions), the
-others the two-line scalar kernel, so both are covered.
+tolerance.  The y passes stage z-column pairs with 16-byte copies into rows
+padded to a multiple of 4; the z extents 3..7 cover pairs whose second
+column is padding (odd nz) and tiles of one to a few columns.
 """
 import numpy as np
 import pytest
