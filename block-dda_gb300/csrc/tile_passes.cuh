@@ -477,6 +477,132 @@ k_pass_e2(const float2* __restrict__ t1, int nfield, int fc, const int* __restri
   }
 }
 
+// ---------------------------------------------------------------- pass A / E, column pairs
+// Same tiles and field loop as k_pass_a2 / k_pass_e2, with warp (pair p, half
+// h) transforming columns 2p and 2p + 1 of field f + h as one interleaved
+// line pair (sfft::stage_il): T1 rows are drained (A) and filled (E) one
+// column pair -- 16 aligned bytes in the padded rows -- per copy.  Lines:
+// [2 buffers][2 fields][4 pairs][LW][2].
+constexpr int kPairsX = kTZ / 2;
+constexpr int kRowStepX = kTileThreads / kPairsX;
+
+template <class P>
+__device__ __forceinline__ float2* x2i_block(float2* lines, int buf, int h, int p) {
+  return lines + (size_t)((buf * 2 + h) * kPairsX + p) * P::LW * 2;
+}
+
+template <class P>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_a2i(const float2* __restrict__ x, int ldx, int nfield, int fc, const int* __restrict__ occ,
+           const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, const float2* __restrict__ twx,
+           float2* __restrict__ t1, const int* done) {
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int Px = P::N;
+  float2* lines = reinterpret_cast<float2*>(smem_raw);
+  int* socc = reinterpret_cast<int*>(lines + 4 * kTZ * P::LW);  // [nx][kTZ]
+  const int tile = tiles[blockIdx.x];
+  const int y = tile / nzt, z0 = (tile - y * nzt) * kTZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wp = warp & (kPairsX - 1), wh = warp / kPairsX;  // this warp's column pair and field half
+  const int tp = tid & (kPairsX - 1), tq = tid / kPairsX;     // drain: column pair and first row
+  const bool pval = z0 + 2 * tp < nz;
+  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
+    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
+    socc[idx] = z < nz ? occ[((size_t)xi * ny + y) * nz + z] : -1;
+  }
+  __syncthreads();
+  const size_t rowstride = (size_t)ny * nzp;
+  for (int f = 0, it = 0; f < nfield; f += 2, ++it) {
+    const int buf = it & 1;
+    const int nh = f + 1 < nfield ? 2 : 1;
+    if (wh < nh) {
+      const int fh = f + wh, l = fh / fc, c = fh - l * fc;
+      const float2* xc = x + (size_t)l * ldx + c;
+      float2* blk = x2i_block<P>(lines, buf, wh, wp);
+      for (int t = lane; t < 2 * nx; t += 32) {
+        const int xi = t >> 1, hc = t & 1;
+        const int m = socc[xi * kTZ + 2 * wp + hc];
+        blk[2 * P::addr(xi) + hc] = m >= 0 ? xc[fc * (size_t)m] : make_float2(0.f, 0.f);
+      }
+      __syncwarp();
+      sfft::forward_il<P>(blk, twx, lane, nx);
+    }
+    __syncthreads();
+    if (pval) {
+      for (int h = 0; h < nh; ++h) {
+        const float4* lb = reinterpret_cast<const float4*>(x2i_block<P>(lines, buf, h, tp));
+        float4* out = reinterpret_cast<float4*>(t1 + (size_t)(f + h) * Px * rowstride + (size_t)y * nzp + z0 + 2 * tp +
+                                                (size_t)tq * rowstride);
+        for (int q = tq; q < Px; q += kRowStepX, out += kRowStepX * rowstride / 2) *out = lb[P::addr(q)];
+      }
+    }
+  }
+}
+
+template <class P>
+__global__ void __launch_bounds__(kTileThreads)
+k_pass_e2i(const float2* __restrict__ t1, int nfield, int fc, const int* __restrict__ occ,
+           const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, const float2* __restrict__ twx,
+           const float2* __restrict__ x, int ldx, const float2* __restrict__ diag, const float2* __restrict__ jpre,
+           float2* __restrict__ y, int ldy, const int* done) {
+  if (skip(done)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int Px = P::N;
+  float2* lines = reinterpret_cast<float2*>(smem_raw);
+  int* socc = reinterpret_cast<int*>(lines + 4 * kTZ * P::LW);  // [nx][kTZ]
+  const int tile = tiles[blockIdx.x];
+  const int yy = tile / nzt, z0 = (tile - yy * nzt) * kTZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wp = warp & (kPairsX - 1), wh = warp / kPairsX;
+  const int tp = tid & (kPairsX - 1), tq = tid / kPairsX;
+  const bool pval = z0 + 2 * tp < nz;
+  const size_t rowstride = (size_t)ny * nzp;
+  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
+    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
+    socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
+  }
+  // fill fields f, f + 1 (if any): column pair tp, rows tq + 64 k
+  auto issue = [&](int f, int buf) {
+    const int nh = f + 1 < nfield ? 2 : 1;
+    for (int h = 0; h < nh; ++h) {
+      const float2* g = t1 + (size_t)(f + h) * Px * rowstride + (size_t)yy * nzp + z0 + 2 * tp + (size_t)tq * rowstride;
+      float2* lb = x2i_block<P>(lines, buf, h, tp);
+      for (int q = tq; q < Px; q += kRowStepX, g += (size_t)kRowStepX * rowstride)
+        cp_async<16>(lb + 2 * P::addr(q), pval ? g : t1, pval);
+    }
+    cp_commit();
+  };
+  issue(0, 0);
+  for (int f = 0, it = 0; f < nfield; f += 2, ++it) {
+    const int buf = it & 1;
+    const int nh = f + 1 < nfield ? 2 : 1;
+    if (f + 2 < nfield) {
+      issue(f + 2, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    if (wh < nh) {
+      const int fh = f + wh, l = fh / fc, c = fh - l * fc;
+      float2* blk = x2i_block<P>(lines, buf, wh, wp);
+      sfft::inverse_il<P>(blk, twx, lane, nx);
+      for (int t = lane; t < 2 * nx; t += 32) {
+        const int xi = t >> 1, hc = t & 1;
+        const int m = socc[xi * kTZ + 2 * wp + hc];
+        if (m < 0) continue;
+        const size_t r = fc * (size_t)m + c;
+        float2 v = blk[2 * P::addr(xi) + hc];
+        if (diag != nullptr) v = cadd(v, cmul(diag[r], x[(size_t)l * ldx + r]));
+        if (jpre != nullptr) v = cmul(v, jpre[r]);
+        y[(size_t)l * ldy + r] = v;
+      }
+    }
+    __syncthreads();  // buffer 'buf' is the cp.async target of fields f + 4, f + 5
+  }
+}
+
 template <typename T> int smem_tile(int lw, int nx) {
   return 2 * kTZ * lw * (int)sizeof(typename cplx<T>::type) + nx * kTZ * 4;
 }

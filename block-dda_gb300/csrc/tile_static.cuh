@@ -36,8 +36,8 @@ cudaError_t launch(int pass, const TileArgs& a) {
   cudaError_t e = cudaSuccess;
   switch (pass) {
     case kTileA:
-      if ((e = set_smem(tile::k_pass_a2<P>, smem_ae, oa, ca)) != cudaSuccess) return e;
-      tile::k_pass_a2<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
+      if ((e = set_smem(tile::k_pass_a2i<P>, smem_ae, oa, ca)) != cudaSuccess) return e;
+      tile::k_pass_a2i<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
           a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.t1, a.done);
       break;
     case kTileB:
@@ -51,8 +51,8 @@ cudaError_t launch(int pass, const TileArgs& a) {
                                                                        ntask2, a.twy, a.done);
       break;
     default:
-      if ((e = set_smem(tile::k_pass_e2<P>, smem_ae, oe, ce)) != cudaSuccess) return e;
-      tile::k_pass_e2<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
+      if ((e = set_smem(tile::k_pass_e2i<P>, smem_ae, oe, ce)) != cudaSuccess) return e;
+      tile::k_pass_e2i<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
           a.t1, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
           a.done);
       break;
