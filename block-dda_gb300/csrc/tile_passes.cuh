@@ -5,10 +5,11 @@
 // layout of the plan; every precision).  A CTA stages 8 z-columns (one line
 // per warp) of one tile in shared memory; forward transforms read only the
 // first nv inputs.
-// k_pass_a2 / k_pass_y2 / k_pass_e2: compile-time plans (static_fft.cuh,
-// padded layout; complex FP32).  Each warp transforms two lines at once -- two
-// fields of its z-column in the x passes, two z-columns of a 16-column tile in
-// the y passes -- and inverse transforms write only the first nv outputs.
+// k_pass_a2i / k_pass_y2i / k_pass_e2i: compile-time plans (static_fft.cuh,
+// padded layout; complex FP32).  Each warp transforms two adjacent z-columns
+// at once, interleaved element by element in shared memory, so the padded
+// T1 / T2 rows are staged and stored one 16-byte column pair per copy;
+// inverse transforms write only the first nv outputs.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -165,81 +166,22 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
   }
 }
 
-// ---------------------------------------------------------------- pass B / D, two lines per warp
-// Same as k_pass_y with 16 z-columns per task: warp w transforms columns 2w
-// and 2w + 1 together (the butterflies of both lines share the lanes), and
-// every row segment is 16 elements wide.  Compile-time plans only.
+// ---------------------------------------------------------------- static-plan tiles
+// The complex FP32 passes with compile-time plans process 16 z-columns (y
+// passes) or 8 (x passes) per task as column pairs.
 constexpr int kTZ2 = 2 * kTZ;
-constexpr int kRowStep2 = kTileThreads / kTZ2;
-
-template <bool INV, class P>
-__global__ void __launch_bounds__(kTileThreads)
-k_pass_y2(const float2* __restrict__ src, float2* __restrict__ dst, const unsigned char* __restrict__ tmask, int ny,
-          int nz, int nzp, int nzt, int ntask, const float2* __restrict__ twy, const int* done) {
-  if (skip(done)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int Py = P::N, lw = P::LW;
-  float2* lines = reinterpret_cast<float2*>(smem_raw);  // [2][kTZ2][lw]
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nin = INV ? Py : ny;
-  const int nout = INV ? ny : Py;
-  const int nzt2 = (nz + kTZ2 - 1) / kTZ2;
-  const int tw = tid & (kTZ2 - 1), ty = tid / kTZ2;  // tile column and first row of this thread
-  auto issue = [&](int task, int buf) {
-    const int zt2 = task % nzt2;
-    const int r = task / nzt2;  // f * Px + q
-    const int z = zt2 * kTZ2 + tw;
-    const bool zval = z < nz;
-    const float2* g = src + (size_t)r * nin * nzp + z + (size_t)ty * nzp;
-    const unsigned char* tm = tmask + (zval ? z / kTZ : 0) + (size_t)ty * nzt;
-    float2* lb = lines + (buf * kTZ2 + tw) * lw;
-    for (int yy = ty; yy < nin; yy += kRowStep2, g += (size_t)kRowStep2 * nzp, tm += (size_t)kRowStep2 * nzt) {
-      const bool valid = zval && (INV || *tm);
-      cp_async<sizeof(float2)>(lb + P::addr(yy), valid ? g : src, valid);
-    }
-    cp_commit();
-  };
-  int task = blockIdx.x;
-  if (task < ntask) issue(task, 0);
-  for (int it = 0; task < ntask; ++it, task += gridDim.x) {
-    const int buf = it & 1;
-    const int next = task + gridDim.x;
-    if (next < ntask) {
-      issue(next, buf ^ 1);
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
-    }
-    __syncthreads();
-    float2* wl = lines + (buf * kTZ2 + 2 * warp) * lw;
-    if (!INV) sfft::forward<P, 2>(wl, twy, lane, ny);
-    else sfft::inverse<P, 2>(wl, twy, lane, ny);
-    __syncthreads();
-    const int zt2 = task % nzt2;
-    const int r = task / nzt2;
-    const int z = zt2 * kTZ2 + tw;
-    if (z < nz) {
-      float2* ob = dst + (size_t)r * nout * nzp + z + (size_t)ty * nzp;
-      const unsigned char* tm = tmask + z / kTZ + (size_t)ty * nzt;
-      const float2* lb = lines + (buf * kTZ2 + tw) * lw;
-      for (int yy = ty; yy < nout; yy += kRowStep2, ob += (size_t)kRowStep2 * nzp, tm += (size_t)kRowStep2 * nzt)
-        if (!INV || *tm) *ob = lb[P::addr(yy)];
-    }
-    __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
-  }
-}
 
 // ---------------------------------------------------------------- pass E
 // One CTA per listed (y, z-tile); loops over fields with the next field's
 // tile prefetched by cp.async; scatters the occupied sites.
 // ---------------------------------------------------------------- pass B / D, column pairs
-// Same tasks as k_pass_y2 (16 z-columns, warp w transforms columns 2w and
-// 2w + 1), with the two columns of a pair interleaved in shared memory
-// (sfft::stage_il): the tile is staged and stored one column pair -- 16
-// contiguous bytes, since rows are padded to a multiple of 4 elements -- per
-// copy, half the copies of k_pass_y2 (whose warps stall on the shared-memory
-// queue).  A pair whose second column is row padding transforms it and never
-// stores it.
+// Persistent CTAs over tasks (field, x, 16-column z tile); lines along y.
+// Warp w transforms columns 2w and 2w + 1 as one line pair interleaved
+// element by element in shared memory (sfft::stage_il), so the tile is
+// staged and stored one column pair -- 16 contiguous bytes, since rows are
+// padded to a multiple of 4 elements -- per copy (a copy per column left the
+// warps stalled on the shared-memory queue).  A pair whose second column is
+// row padding transforms it and never stores it.
 constexpr int kPairsY = kTZ2 / 2;
 constexpr int kRowStepP = kTileThreads / kPairsY;
 
@@ -359,130 +301,12 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, cons
   }
 }
 
-// ---------------------------------------------------------------- pass A / E, two fields per warp
-// Same as k_pass_a / k_pass_e (one CTA per listed (y, z-tile)) with the
-// fields taken two at a time: warp w transforms column w of fields f and f + 1
-// together (lines [buf][w][2]).  Compile-time plans only.
-template <class P>
-__device__ __forceinline__ float2* x2_line(float2* lines, int buf, int w, int h) {
-  return lines + ((buf * kTZ + w) * 2 + h) * P::LW;
-}
-
-template <class P>
-__global__ void __launch_bounds__(kTileThreads)
-k_pass_a2(const float2* __restrict__ x, int ldx, int nfield, int fc, const int* __restrict__ occ,
-          const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, const float2* __restrict__ twx,
-          float2* __restrict__ t1, const int* done) {
-  if (skip(done)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int Px = P::N;
-  float2* lines = reinterpret_cast<float2*>(smem_raw);                       // [2][kTZ][2][LW]
-  int* socc = reinterpret_cast<int*>(lines + 4 * kTZ * P::LW);               // [nx][kTZ]
-  const int tile = tiles[blockIdx.x];
-  const int y = tile / nzt, z0 = (tile - y * nzt) * kTZ;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int tw8 = tid & (kTZ - 1), tq = tid / kTZ;
-  const bool zval = z0 + tw8 < nz;
-  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
-    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
-    socc[idx] = z < nz ? occ[((size_t)xi * ny + y) * nz + z] : -1;
-  }
-  __syncthreads();
-  const size_t rowstride = (size_t)ny * nzp;
-  for (int f = 0, it = 0; f < nfield; f += 2, ++it) {
-    const int buf = it & 1;
-    const int nh = f + 1 < nfield ? 2 : 1;
-    for (int h = 0; h < nh; ++h) {
-      const int fh = f + h, l = fh / fc, c = fh - l * fc;
-      const float2* xc = x + (size_t)l * ldx + c;
-      float2* line = x2_line<P>(lines, buf, warp, h);
-      for (int xi = lane; xi < nx; xi += 32) {
-        const int m = socc[xi * kTZ + warp];
-        line[P::addr(xi)] = m >= 0 ? xc[fc * (size_t)m] : make_float2(0.f, 0.f);
-      }
-    }
-    __syncwarp();
-    if (nh == 2) sfft::forward<P, 2>(x2_line<P>(lines, buf, warp, 0), twx, lane, nx);
-    else sfft::forward<P, 1>(x2_line<P>(lines, buf, warp, 0), twx, lane, nx);
-    __syncthreads();
-    if (zval) {
-      for (int h = 0; h < nh; ++h) {
-        const float2* lb = x2_line<P>(lines, buf, tw8, h);
-        float2* out = t1 + (size_t)(f + h) * Px * rowstride + (size_t)y * nzp + z0 + tw8 + (size_t)tq * rowstride;
-        for (int q = tq; q < Px; q += kRowStep, out += kRowStep * rowstride) *out = lb[P::addr(q)];
-      }
-    }
-  }
-}
-
-template <class P>
-__global__ void __launch_bounds__(kTileThreads)
-k_pass_e2(const float2* __restrict__ t1, int nfield, int fc, const int* __restrict__ occ,
-          const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, const float2* __restrict__ twx,
-          const float2* __restrict__ x, int ldx, const float2* __restrict__ diag, const float2* __restrict__ jpre,
-          float2* __restrict__ y, int ldy, const int* done) {
-  if (skip(done)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int Px = P::N;
-  float2* lines = reinterpret_cast<float2*>(smem_raw);                       // [2][kTZ][2][LW]
-  int* socc = reinterpret_cast<int*>(lines + 4 * kTZ * P::LW);               // [nx][kTZ]
-  const int tile = tiles[blockIdx.x];
-  const int yy = tile / nzt, z0 = (tile - yy * nzt) * kTZ;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const size_t rowstride = (size_t)ny * nzp;
-  for (int idx = tid; idx < nx * kTZ; idx += kTileThreads) {
-    const int xi = idx >> 3, w = idx & 7, z = z0 + w;
-    socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
-  }
-  const int tw8 = tid & (kTZ - 1), tq = tid / kTZ;
-  const bool zval = z0 + tw8 < nz;
-  // fill fields f, f + 1 (if any) of the tile: column tw8, rows tq + 32 k
-  auto issue = [&](int f, int buf) {
-    const int nh = f + 1 < nfield ? 2 : 1;
-    for (int h = 0; h < nh; ++h) {
-      const float2* g = t1 + (size_t)(f + h) * Px * rowstride + (size_t)yy * nzp + z0 + tw8 + (size_t)tq * rowstride;
-      float2* lb = x2_line<P>(lines, buf, tw8, h);
-      for (int q = tq; q < Px; q += kRowStep, g += (size_t)kRowStep * rowstride)
-        cp_async<sizeof(float2)>(lb + P::addr(q), zval ? g : t1, zval);
-    }
-    cp_commit();
-  };
-  issue(0, 0);
-  for (int f = 0, it = 0; f < nfield; f += 2, ++it) {
-    const int buf = it & 1;
-    const int nh = f + 1 < nfield ? 2 : 1;
-    if (f + 2 < nfield) {
-      issue(f + 2, buf ^ 1);
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
-    }
-    __syncthreads();
-    if (nh == 2) sfft::inverse<P, 2>(x2_line<P>(lines, buf, warp, 0), twx, lane, nx);
-    else sfft::inverse<P, 1>(x2_line<P>(lines, buf, warp, 0), twx, lane, nx);
-    for (int h = 0; h < nh; ++h) {
-      const int fh = f + h, l = fh / fc, c = fh - l * fc;
-      const float2* line = x2_line<P>(lines, buf, warp, h);
-      for (int xi = lane; xi < nx; xi += 32) {
-        const int m = socc[xi * kTZ + warp];
-        if (m < 0) continue;
-        const size_t r = fc * (size_t)m + c;
-        float2 v = line[P::addr(xi)];
-        if (diag != nullptr) v = cadd(v, cmul(diag[r], x[(size_t)l * ldx + r]));
-        if (jpre != nullptr) v = cmul(v, jpre[r]);
-        y[(size_t)l * ldy + r] = v;
-      }
-    }
-    __syncthreads();  // buffer 'buf' is the cp.async target of fields f + 4, f + 5
-  }
-}
-
 // ---------------------------------------------------------------- pass A / E, column pairs
-// Same tiles and field loop as k_pass_a2 / k_pass_e2, with warp (pair p, half
-// h) transforming columns 2p and 2p + 1 of field f + h as one interleaved
-// line pair (sfft::stage_il): T1 rows are drained (A) and filled (E) one
-// column pair -- 16 aligned bytes in the padded rows -- per copy.  Lines:
-// [2 buffers][2 fields][4 pairs][LW][2].
+// One CTA per listed (y, 8-column z tile), looping over the fields two at a
+// time: warp (pair p, half h) transforms columns 2p and 2p + 1 of field f + h
+// as one interleaved line pair (sfft::stage_il), and T1 rows are drained (A)
+// and filled (E) one column pair -- 16 aligned bytes in the padded rows -- per
+// copy.  Lines: [2 buffers][2 fields][4 pairs][LW][2].
 constexpr int kPairsX = kTZ / 2;
 constexpr int kRowStepX = kTileThreads / kPairsX;
 
