@@ -313,15 +313,17 @@ k_dotc(int n, int L, const typename cplx<T>::type* __restrict__ A, int lda,
   }
 }
 
-// Precision conversion / copy of an n x L block.
+// Precision conversion / copy of an n x L block; colf (optional, FP64 [L])
+// scales column l by colf[l].
 template <typename TO, typename TI>
 __global__ void k_convert(int n, int L, const typename cplx<TI>::type* __restrict__ in, int ldi,
-                          typename cplx<TO>::type* __restrict__ out, int ldo) {
+                          typename cplx<TO>::type* __restrict__ out, int ldo, const double* __restrict__ colf = nullptr) {
   const size_t total = (size_t)n * L;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
     const size_t l = idx / n, r = idx - l * n;
     const auto v = in[l * ldi + r];
-    out[l * ldo + r] = cmake((TO)v.x, (TO)v.y);
+    const double f = colf ? colf[l] : 1.0;
+    out[l * ldo + r] = cmake((TO)(f * (double)v.x), (TO)(f * (double)v.y));
   }
 }
 
@@ -343,17 +345,18 @@ __global__ void k_from_df(int n, int L, const dfc* __restrict__ in, int ldi, dou
   }
 }
 
-// X64 += D (D in T precision)
+// X64 += D (D in T precision); colf (optional, FP64 [L]) scales column l of D
 template <typename T>
 __global__ void k_accumulate(int n, int L, const typename cplx<T>::type* __restrict__ D, int ldd,
-                             double2* __restrict__ X, int ldx) {
+                             double2* __restrict__ X, int ldx, const double* __restrict__ colf = nullptr) {
   const size_t total = (size_t)n * L;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
     const size_t l = idx / n, r = idx - l * n;
     const auto d = D[l * ldd + r];
+    const double f = colf ? colf[l] : 1.0;
     double2 x = X[l * ldx + r];
-    x.x += (double)d.x;
-    x.y += (double)d.y;
+    x.x += f * (double)d.x;
+    x.y += f * (double)d.y;
     X[l * ldx + r] = x;
   }
 }
@@ -369,14 +372,16 @@ __global__ void k_residual(int n, int L, const double2* __restrict__ B, int ldb,
 }
 
 // Out = v o In   (per-row complex scaling, e.g. B_pre = jpre o B)
+// (colf, optional, FP64 [L]: column l also scaled by colf[l])
 template <typename TO, typename TI>
 __global__ void k_rowscale(int n, int L, const double2* __restrict__ v, const typename cplx<TI>::type* __restrict__ In, int ldi,
-                           typename cplx<TO>::type* __restrict__ Out, int ldo) {
+                           typename cplx<TO>::type* __restrict__ Out, int ldo, const double* __restrict__ colf = nullptr) {
   const size_t total = (size_t)n * L;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
     const size_t l = idx / n, r = idx - l * n;
     const auto a = In[l * ldi + r];
-    const double2 s = v[r];
+    const double f = colf ? colf[l] : 1.0;
+    const double2 s = make_double2(f * v[r].x, f * v[r].y);
     const double2 p = cmul(make_double2((double)a.x, (double)a.y), s);
     Out[l * ldo + r] = cmake((TO)p.x, (TO)p.y);
   }

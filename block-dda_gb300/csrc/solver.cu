@@ -38,6 +38,7 @@ struct SolverWork {
   DevBuf gpart;                 // per-CTA Gram partials [G][L*L], or [G][2 L*L] for gram2
   DevBuf partials, partials2;   // reduced Gram matrices (c128) [L*L]
   DevBuf vpart;                 // dot / norm partials
+  DevBuf colf;                  // FP64 [2][L]: column scaling of the inner right-hand side and its inverse
   DevBuf small;                 // c128 [kNumSlots][L*L] + scalars
   DevBuf ctl;                   // SolverCtl
   DevBuf hist;                  // double[itermax]
@@ -705,6 +706,7 @@ static int ensure_work(Op* op, int n, int L, int itermax, bool need64, bool need
   BDDA_CUDA(w->vpart.ensure(sizeof(double2) * 2 * (size_t)std::max(vec_grid((size_t)n * L) * L, 2 * 608), op->stream));
   BDDA_CUDA(w->small.ensure(sizeof(double2) * (LL * kNumSlots + 8), op->stream));
   BDDA_CUDA(w->ctl.ensure(sizeof(SolverCtl), op->stream));
+  BDDA_CUDA(w->colf.ensure(sizeof(double) * 2 * kMaxL, op->stream));
   BDDA_CUDA(w->hist.ensure(sizeof(double) * (size_t)std::max(1, itermax), op->stream));
   w->n = n;
   w->L = L;
@@ -757,7 +759,8 @@ static int host_colnorm2(Op* op, cudaStream_t st, const double2* A, int n, int L
 // runs in FP64, or in double-float arithmetic when use_df is set (FP64-level
 // accuracy on the FP32 pipes); the subtraction and norms are FP64.
 static int true_residual(Op* op, cudaStream_t st, const double2* diag, const double2* B, int ldb, const double2* X,
-                         int ldx, int n, int L, const std::vector<double>& bn2, double* resmax, int* mvps, bool use_df) {
+                         int ldx, int n, int L, const std::vector<double>& bn2, double* resmax, int* mvps, bool use_df,
+                         std::vector<double>* rn2_out = nullptr) {
   SolverWork* w = op->solver.get();
   const int gv = vec_grid((size_t)n * L);
   if (use_df) {
@@ -780,6 +783,7 @@ static int true_residual(Op* op, cudaStream_t st, const double2* diag, const dou
     if (!(r <= mx)) mx = r;  // NaN propagates as the maximum
   }
   *resmax = mx;
+  if (rn2_out) *rn2_out = rn2;
   return BDDA_OK;
 }
 
@@ -830,30 +834,49 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
 
   // inner solve on RHS R (FP64, leading dim ldr): the correction D is solved in
   // the inner precision into block 9 (right-hand side in block 8), then added
-  // to (accumulate) or written into Dst.
-  auto inner = [&](const double2* R, int ldr, double tol, double2* Dst, int ldd, bool accumulate) -> int {
+  // to (accumulate) or written into Dst.  With rn2 (the squared column norms of
+  // R, refinement mode) the right-hand side's columns are scaled to unit norm
+  // and the correction's scaled back: the block Krylov space is the same, but
+  // a residual block whose columns converged to very different sizes keeps a
+  // well-conditioned Gram matrix (its CholQR would otherwise break down).
+  auto inner = [&](const double2* R, int ldr, double tol, double2* Dst, int ldd, bool accumulate,
+                   const std::vector<double>* rn2) -> int {
     int it = 0, stt = 0;
     double er = 0.0;
     const int gv = vec_grid((size_t)n * L);
+    const double* cf = nullptr;   // column scaling of the right-hand side
+    const double* cfi = nullptr;  // and of the correction
+    if (rn2) {
+      std::vector<double> h(2 * (size_t)L);
+      for (int l = 0; l < L; ++l) {
+        const double nr = std::sqrt((*rn2)[l]);
+        h[l] = nr > 0.0 ? 1.0 / nr : 1.0;
+        h[L + l] = nr > 0.0 ? nr : 1.0;
+      }
+      BDDA_CUDA(cudaMemcpyAsync(w->colf.p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, st));
+      BDDA_CUDA(wait_stream(st));  // h is a local
+      cf = w->colf.as<double>();
+      cfi = cf + L;
+    }
     if (!mixed) {
       double2* Bp = w->blk64[8].as<double2>();
       double2* D = w->blk64[9].as<double2>();
-      if (o->jacobi) k_rowscale<double, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n);
-      else k_convert<double, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n);
+      if (o->jacobi) k_rowscale<double, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n, cf);
+      else k_convert<double, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n, cf);
       op->timer.count(kOther);
       BDDA_TRY(k64.run(o->solver, Bp, D, full, tol, itermax, &it, &er, &stt));
-      if (accumulate) k_accumulate<double><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
-      else k_convert<double, double><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
+      if (accumulate) k_accumulate<double><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd, cfi);
+      else k_convert<double, double><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd, cfi);
       op->timer.count(kOther);
     } else {
       float2* Bp = w->blk32[8].as<float2>();
       float2* D = w->blk32[9].as<float2>();
-      if (o->jacobi) k_rowscale<float, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n);
-      else k_convert<float, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n);
+      if (o->jacobi) k_rowscale<float, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n, cf);
+      else k_convert<float, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n, cf);
       op->timer.count(kOther);
       BDDA_TRY(k32.run(o->solver, Bp, D, full, tol, itermax, &it, &er, &stt));
-      if (accumulate) k_accumulate<float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
-      else k_convert<double, float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd);
+      if (accumulate) k_accumulate<float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd, cfi);
+      else k_convert<double, float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd, cfi);
       op->timer.count(kOther);
     }
     total_iters += it;
@@ -864,7 +887,7 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
   };
 
   if (!refine) {
-    BDDA_TRY(inner(B, ldb, o->tol, X, ldx, false));
+    BDDA_TRY(inner(B, ldb, o->tol, X, ldx, false, nullptr));
     if (status == BDDA_OK && last_err >= o->tol) status = BDDA_ERR_NOT_CONVERGED;
   } else {
     std::vector<double> bn2;
@@ -878,10 +901,11 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
     const double ifloor = mixed ? std::min(itol, 2e-5) : itol;
     const double2* R = B;
     int ldr = ldb;
+    std::vector<double> rn2 = bn2;  // squared column norms of R
     bool converged = false;
     if (o->warm_start) {
       // X holds the initial guess (e.g. the previous wavelength's solution): refine from r = B - A X
-      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, ldx, n, L, bn2, &resmax, &mvps, use_df));
+      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, ldx, n, L, bn2, &resmax, &mvps, use_df, &rn2));
       R = w->R64.as<double2>();
       ldr = n;
       converged = resmax <= o->true_tol;
@@ -889,6 +913,7 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
         BDDA_CUDA(cudaMemset2DAsync(X, sizeof(double2) * (size_t)ldx, 0, sizeof(double2) * (size_t)n, L, st));
         R = B;
         ldr = ldb;
+        rn2 = bn2;
       }
     } else {
       BDDA_CUDA(cudaMemset2DAsync(X, sizeof(double2) * (size_t)ldx, 0, sizeof(double2) * (size_t)n, L, st));
@@ -904,14 +929,23 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
         const double need = std::min(0.1, 0.3 * o->true_tol / std::max(resmax, 1e-300));
         tol_r = std::max(need, (r == 0 && o->inner_tol <= 0) ? std::min(ifloor, 1e-6) : ifloor);
       }
-      BDDA_TRY(inner(R, ldr, tol_r, X, ldx, true));
-      if (status == BDDA_ERR_BREAKDOWN) break;
-      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, ldx, n, L, bn2, &resmax, &mvps, use_df));
+      const double before = (r == 0 && !warm) ? 1.0 : resmax;
+      BDDA_TRY(inner(R, ldr, tol_r, X, ldx, true, &rn2));
+      // A breakdown (a rank-deficient residual block: its FP32 Gram loses
+      // positive definiteness) ends the inner solve; its iterate is kept --
+      // every kernel after the failed step returned -- and the refinement
+      // restarts the Krylov solve from the true residual, as long as that
+      // residual still decreases.
+      const bool broke = status == BDDA_ERR_BREAKDOWN;
+      if (broke) status = BDDA_OK;
+      BDDA_TRY(true_residual(op, st, diag, B, ldb, X, ldx, n, L, bn2, &resmax, &mvps, use_df, &rn2));
       R = w->R64.as<double2>();
       ldr = n;
       if (resmax <= o->true_tol) { converged = true; break; }
+      if (broke && !(resmax < before)) { status = BDDA_ERR_BREAKDOWN; break; }
     }
-    if (status == BDDA_OK && !converged) status = BDDA_ERR_NOT_CONVERGED;
+    if (converged) status = BDDA_OK;  // an inner solve that hit itermax does not matter once the residual is met
+    else if (status == BDDA_OK) status = BDDA_ERR_NOT_CONVERGED;
   }
   cudaEventRecord(e1, st);
   BDDA_CUDA(wait_stream(st));
