@@ -137,6 +137,22 @@ def test_mixed_solve_on_fp32_and_double_float_tables_only():
         bdda.solve(lean, prob.diag, prob.B, bdda.solve_opts("cocg_rq", precision=bdda.SOLVE_FP64, true_tol=1e-8))
 
 
+def test_mixed_refinement_with_unequal_residual_columns():
+    """A case of the serving stream (N=17523, L=32, m=2.11+0.23i,
+    lambda=0.398 um) whose residual after the first refinement step has
+    columns of very different sizes: the FP32 Gram of that block loses positive
+    definiteness unless the inner right-hand side is scaled to unit columns
+    (CholQR broke down there).  It must converge."""
+    prob = bdda.make_problem(17523, 2.1095600183974708 + 0.22780528458440563j, wl0=0.3976663593698059,
+                             kf=1.0931588914517667, Df=2.718068505948526, seed=940342375, n_dirs=16)
+    assert prob.B.shape[1] == 32
+    op = bdda.Operator(prob.n, prob.lf, prob.k)
+    op.set_dipoles(prob.address)
+    opts = bdda.solve_opts("cocg_rq", jacobi=True, precision=bdda.SOLVE_MIXED, true_tol=1e-8, itermax=3000)
+    _X, st = bdda.solve(op, prob.diag, prob.B, opts, allow_not_converged=False)
+    assert st["status"] == 0 and st["true_res_max"] <= 1e-8
+
+
 def test_solve_status_codes():
     prob, B = _small_problem(nocc=60, L=2)
     op = bdda.Operator(prob.n, prob.lf, prob.k)
