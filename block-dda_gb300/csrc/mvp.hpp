@@ -149,6 +149,11 @@ bool launch_tile_static(int pass, const TileArgs& a, cudaError_t* err);
 bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz, const float4* twzp, const float2* ghat,
                           cudaStream_t st, const int* done, cudaError_t* err);
 
+// Pass C of a double-float block MVP (f = 3) with the compile-time z plan of
+// g.Pz; false (nothing launched) when g.Pz has none or f = 6.
+bool launch_pass_c_static_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz, const dfzc* ghat, cudaStream_t st,
+                             const int* done, cudaError_t* err);
+
 // Green tensor: build Ghat (FP64 evaluation + FP64 3-D FFT), layout
 // [Px][Py][nc][Pz] with nc = 6 (g.f = 3) or 9 (g.f = 6), for any of the
 // precisions (null pointers skipped).  work: c128 [nc*Px*Py*Pz].

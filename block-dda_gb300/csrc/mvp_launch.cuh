@@ -156,6 +156,10 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
       cudaError_t e = cudaSuccess;
       launched = launch_pass_c_static(g, t2, L, p.twz, p.twzp, p.ghat, st, done, &e);
       if (launched && e != cudaSuccess) return e;
+    } else if constexpr (std::is_same<T, dfz>::value) {
+      cudaError_t e = cudaSuccess;
+      launched = launch_pass_c_static_df(g, t2, L, p.twz, p.ghat, st, done, &e);
+      if (launched && e != cudaSuccess) return e;
     }
     if (!launched) {
       const int per_warp = g.f * plan_lw<C>(g.pz) * (int)sizeof(C);

@@ -37,8 +37,8 @@ struct Plan {
 // inverse (DIT, the adjoint): conjugate twiddle then inverse DFT.  The forward
 // first stage reads only inputs idx < nv (the rest are zero padding); the
 // inverse last stage writes only outputs idx < nv (the rest are discarded).
-template <class P, int s, bool INV, int NL>
-__device__ __forceinline__ void stage(float2* __restrict__ sm, const float2* __restrict__ tw, int lane, int nv) {
+template <class P, int s, bool INV, int NL, typename C = float2>
+__device__ __forceinline__ void stage(C* __restrict__ sm, const C* __restrict__ tw, int lane, int nv) {
   constexpr int R = P::rad[s];
   constexpr int M = P::M(s);
   constexpr int Ls = M * R;
@@ -53,11 +53,11 @@ __device__ __forceinline__ void stage(float2* __restrict__ sm, const float2* __r
     const int u = t - j * B;
     const int b = u / M, n1 = u - b * M;
     const int idx0 = b * Ls + n1;
-    float2* p = sm + j * P::LW + P::addr(idx0);
-    float2 v[R];
+    C* p = sm + j * P::LW + P::addr(idx0);
+    C v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      if (prune_in) v[i] = (idx0 + i * M < nv) ? p[i * off] : make_float2(0.f, 0.f);
+      if (prune_in) v[i] = (idx0 + i * M < nv) ? p[i * off] : czero<C>();
       else v[i] = p[i * off];
     }
     if (!INV) {
@@ -91,9 +91,9 @@ __device__ __forceinline__ void stage(float2* __restrict__ sm, const float2* __r
 // shared memory: line j's element idx < nv at gsrc[j * gstride + idx] (the
 // zero padding past nv is never read), results stored to the padded shared
 // line as stage<P, 0, false, NL> stores them.
-template <class P, int NL>
-__device__ __forceinline__ void stage0_from_global(float2* __restrict__ sm, const float2* __restrict__ tw, int lane,
-                                                   int nv, const float2* __restrict__ gsrc, size_t gstride) {
+template <class P, int NL, typename C = float2>
+__device__ __forceinline__ void stage0_from_global(C* __restrict__ sm, const C* __restrict__ tw, int lane,
+                                                   int nv, const C* __restrict__ gsrc, size_t gstride) {
   constexpr int R = P::rad[0];
   constexpr int M = P::M(0);       // butterflies per line (Ls = N)
   constexpr int T = NL * M;
@@ -101,16 +101,16 @@ __device__ __forceinline__ void stage0_from_global(float2* __restrict__ sm, cons
   for (int t = lane; t < T; t += 32) {
     const int j = NL == 1 ? 0 : t / M;
     const int n1 = t - j * M;
-    const float2* g = gsrc + (size_t)j * gstride + n1;
-    float2 v[R];
+    const C* g = gsrc + (size_t)j * gstride + n1;
+    C v[R];
 #pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = (n1 + i * M < nv) ? g[i * M] : make_float2(0.f, 0.f);
+    for (int i = 0; i < R; ++i) v[i] = (n1 + i * M < nv) ? g[i * M] : czero<C>();
     dft<R, false>(v);
     if (M > 1 && n1 != 0) {
 #pragma unroll
       for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tw + k * n1));
     }
-    float2* p = sm + j * P::LW + P::addr(n1);
+    C* p = sm + j * P::LW + P::addr(n1);
 #pragma unroll
     for (int i = 0; i < R; ++i) p[i * off] = v[i];
   }
@@ -119,9 +119,9 @@ __device__ __forceinline__ void stage0_from_global(float2* __restrict__ sm, cons
 
 // Last inverse stage with its outputs written to global memory: line j's
 // element idx < nv to gdst[j * gstride + idx] (the rest are discarded).
-template <class P, int NL>
-__device__ __forceinline__ void stage0_to_global(const float2* __restrict__ sm, const float2* __restrict__ tw,
-                                                 int lane, int nv, float2* __restrict__ gdst, size_t gstride) {
+template <class P, int NL, typename C = float2>
+__device__ __forceinline__ void stage0_to_global(const C* __restrict__ sm, const C* __restrict__ tw,
+                                                 int lane, int nv, C* __restrict__ gdst, size_t gstride) {
   constexpr int R = P::rad[0];
   constexpr int M = P::M(0);
   constexpr int T = NL * M;
@@ -129,8 +129,8 @@ __device__ __forceinline__ void stage0_to_global(const float2* __restrict__ sm, 
   for (int t = lane; t < T; t += 32) {
     const int j = NL == 1 ? 0 : t / M;
     const int n1 = t - j * M;
-    const float2* p = sm + j * P::LW + P::addr(n1);
-    float2 v[R];
+    const C* p = sm + j * P::LW + P::addr(n1);
+    C v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) v[i] = p[i * off];
     if (M > 1 && n1 != 0) {
@@ -138,7 +138,7 @@ __device__ __forceinline__ void stage0_to_global(const float2* __restrict__ sm, 
       for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tw + k * n1));
     }
     dft<R, true>(v);
-    float2* g = gdst + (size_t)j * gstride + n1;
+    C* g = gdst + (size_t)j * gstride + n1;
 #pragma unroll
     for (int i = 0; i < R; ++i)
       if (n1 + i * M < nv) g[i * M] = v[i];
@@ -148,38 +148,36 @@ __device__ __forceinline__ void stage0_to_global(const float2* __restrict__ sm, 
 
 // Forward transform of NL lines: natural order in, digit-reversed out, only
 // the first nv inputs read.
-template <class P, int NL, int s = 0>
-__device__ __forceinline__ void forward(float2* sm, const float2* tw, int lane, int nv) {
+template <class P, int NL, int s = 0, typename C = float2>
+__device__ __forceinline__ void forward(C* sm, const C* tw, int lane, int nv) {
   if constexpr (s < P::nst) {
-    stage<P, s, false, NL>(sm, tw, lane, nv);
-    forward<P, NL, s + 1>(sm, tw, lane, nv);
+    stage<P, s, false, NL, C>(sm, tw, lane, nv);
+    forward<P, NL, s + 1, C>(sm, tw, lane, nv);
   }
 }
 
 // Forward transform whose input lines are in global memory (see stage0_from_global).
-template <class P, int NL>
-__device__ __forceinline__ void forward_from_global(float2* sm, const float2* tw, int lane, int nv,
-                                                    const float2* gsrc, size_t gstride) {
-  stage0_from_global<P, NL>(sm, tw, lane, nv, gsrc, gstride);
-  forward<P, NL, 1>(sm, tw, lane, nv);
+template <class P, int NL, typename C = float2>
+__device__ __forceinline__ void forward_from_global(C* sm, const C* tw, int lane, int nv, const C* gsrc, size_t gstride) {
+  stage0_from_global<P, NL, C>(sm, tw, lane, nv, gsrc, gstride);
+  forward<P, NL, 1, C>(sm, tw, lane, nv);
 }
 
 // Inverse transform (unnormalised): digit-reversed in, natural order out,
 // only the first nv outputs written.
-template <class P, int NL, int s = P::nst - 1, int last = 0>
-__device__ __forceinline__ void inverse(float2* sm, const float2* tw, int lane, int nv) {
+template <class P, int NL, int s = P::nst - 1, int last = 0, typename C = float2>
+__device__ __forceinline__ void inverse(C* sm, const C* tw, int lane, int nv) {
   if constexpr (s >= last) {
-    stage<P, s, true, NL>(sm, tw, lane, nv);
-    inverse<P, NL, s - 1, last>(sm, tw, lane, nv);
+    stage<P, s, true, NL, C>(sm, tw, lane, nv);
+    inverse<P, NL, s - 1, last, C>(sm, tw, lane, nv);
   }
 }
 
 // Inverse transform whose output lines go to global memory (see stage0_to_global).
-template <class P, int NL>
-__device__ __forceinline__ void inverse_to_global(float2* sm, const float2* tw, int lane, int nv, float2* gdst,
-                                                  size_t gstride) {
-  inverse<P, NL, P::nst - 1, 1>(sm, tw, lane, nv);
-  stage0_to_global<P, NL>(sm, tw, lane, nv, gdst, gstride);
+template <class P, int NL, typename C = float2>
+__device__ __forceinline__ void inverse_to_global(C* sm, const C* tw, int lane, int nv, C* gdst, size_t gstride) {
+  inverse<P, NL, P::nst - 1, 1, C>(sm, tw, lane, nv);
+  stage0_to_global<P, NL, C>(sm, tw, lane, nv, gdst, gstride);
 }
 
 // ---- two lines interleaved element by element ---------------------------------

@@ -7,6 +7,10 @@ bool static_z_part0(const MvpGeom& g, float2* t2, int L, const float2* twz, cons
   return sparts::dispatch_z<0>(g, t2, L, twz, twzp, ghat, st, done, err);
 }
 bool static_tile_part0(int pass, const TileArgs& a, cudaError_t* err) { return sparts::dispatch_tile<0>(pass, a, err); }
+bool static_z_df_part0(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz, const dfzc* ghat, cudaStream_t st,
+                       const int* done, cudaError_t* err) {
+  return sparts::dispatch_z_df<0>(g, t2, L, twz, ghat, st, done, err);
+}
 
 bool static_z_part1(const MvpGeom&, float2*, int, const float2*, const float4*, const float2*, cudaStream_t, const int*,
                     cudaError_t*);
@@ -25,6 +29,16 @@ bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz
          static_z_part1(g, t2, L, twz, twzp, ghat, st, done, err) ||
          static_z_part2(g, t2, L, twz, twzp, ghat, st, done, err) ||
          static_z_part3(g, t2, L, twz, twzp, ghat, st, done, err);
+}
+
+bool static_z_df_part1(const MvpGeom&, dfzc*, int, const dfzc*, const dfzc*, cudaStream_t, const int*, cudaError_t*);
+bool static_z_df_part2(const MvpGeom&, dfzc*, int, const dfzc*, const dfzc*, cudaStream_t, const int*, cudaError_t*);
+bool static_z_df_part3(const MvpGeom&, dfzc*, int, const dfzc*, const dfzc*, cudaStream_t, const int*, cudaError_t*);
+
+bool launch_pass_c_static_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz, const dfzc* ghat, cudaStream_t st,
+                             const int* done, cudaError_t* err) {
+  return static_z_df_part0(g, t2, L, twz, ghat, st, done, err) || static_z_df_part1(g, t2, L, twz, ghat, st, done, err) ||
+         static_z_df_part2(g, t2, L, twz, ghat, st, done, err) || static_z_df_part3(g, t2, L, twz, ghat, st, done, err);
 }
 
 bool launch_tile_static(int pass, const TileArgs& a, cudaError_t* err) {

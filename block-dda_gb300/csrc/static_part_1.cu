@@ -7,4 +7,8 @@ bool static_z_part1(const MvpGeom& g, float2* t2, int L, const float2* twz, cons
   return sparts::dispatch_z<1>(g, t2, L, twz, twzp, ghat, st, done, err);
 }
 bool static_tile_part1(int pass, const TileArgs& a, cudaError_t* err) { return sparts::dispatch_tile<1>(pass, a, err); }
+bool static_z_df_part1(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz, const dfzc* ghat, cudaStream_t st,
+                       const int* done, cudaError_t* err) {
+  return sparts::dispatch_z_df<1>(g, t2, L, twz, ghat, st, done, err);
+}
 }  // namespace bdda

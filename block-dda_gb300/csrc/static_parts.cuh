@@ -33,6 +33,28 @@ bool dispatch_z(const MvpGeom& g, float2* t2, int L, const float2* twz, const fl
   return false;
 }
 
+// The double-float z pass of f = 3 operators with the same compile-time plans
+// (the double-float Green spectrum uses the z table's radix order too).
+template <int PART>
+bool dispatch_z_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz, const dfzc* ghat, cudaStream_t st,
+                   const int* done, cudaError_t* err) {
+  if (g.f != 3) return false;
+  switch (g.Pz) {
+#define BDDA_ZPLAN(I, N, S, LW, ...)                                                                  \
+  case N:                                                                                             \
+    if constexpr ((I) % kParts == PART) {                                                             \
+      *err = zstatic::launch_f<sfft::Plan<N, S, LW, __VA_ARGS__>, false, dfzc>(g, t2, L, twz, ghat, st, done); \
+      return true;                                                                                    \
+    }                                                                                                 \
+    return false;
+#include "zplans.inc"
+#undef BDDA_ZPLAN
+    default:
+      break;
+  }
+  return false;
+}
+
 template <int PART>
 bool dispatch_tile(int pass, const TileArgs& a, cudaError_t* err) {
   const int n = (pass == kTileA || pass == kTileE) ? a.g->Px : a.g->Py;

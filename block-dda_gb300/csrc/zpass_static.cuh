@@ -21,10 +21,10 @@
 namespace bdda {
 namespace zstatic {
 
-template <class P, bool SIX>
+template <class P, bool SIX, typename C = float2>
 __global__ void __launch_bounds__(kZWarps * 32)
-k_pass_c_static(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp, const float2* __restrict__ twz,
-                const float2* __restrict__ ghat, const int* done) {
+k_pass_c_static(C* __restrict__ t2, int L, int Px, int Py, int nz, int nzp, const C* __restrict__ twz,
+                const C* __restrict__ ghat, const int* done) {
   constexpr int fc = SIX ? 6 : 3;
   if (done && *(volatile const int*)done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -34,15 +34,15 @@ k_pass_c_static(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp,
   if (task >= (long long)Px * Py * L) return;
   const int l = (int)(task % L);
   const long long line = task / L;  // q * Py + qy
-  float2* s0 = reinterpret_cast<float2*>(smem_raw) + (size_t)warp * fc * LW;
+  C* s0 = reinterpret_cast<C*>(smem_raw) + (size_t)warp * fc * LW;
   const size_t fstride = (size_t)Px * Py * nzp;  // between fields
-  float2* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nzp;
+  C* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nzp;
   constexpr bool six = SIX;
   constexpr int halves = six ? 2 : 1;  // line triples: E, then M
   // the first forward stage reads the lines straight from T2 (no staging loop)
   for (int h = 0; h < halves; ++h)
     sfft::forward_from_global<P, 3>(s0 + 3 * h * LW, twz, lane, nz, g0 + 3 * h * fstride, fstride);
-  const float2* gl = ghat + (size_t)line * (six ? 9 : 6) * Pz;
+  const C* gl = ghat + (size_t)line * (six ? 9 : 6) * Pz;
   for (int p = lane; p < Pz; p += 32) z_product(s0, LW, P::addr(p), gl, Pz, p, six);
   __syncwarp();
   // the last inverse stage writes the lines straight back to T2 (rows past nz dropped)
@@ -50,20 +50,19 @@ k_pass_c_static(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp,
     sfft::inverse_to_global<P, 3>(s0 + 3 * h * LW, twz, lane, nz, g0 + 3 * h * fstride, fstride);
 }
 
-template <class P, bool SIX>
-cudaError_t launch_f(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2* ghat, cudaStream_t st,
-                     const int* done) {
+template <class P, bool SIX, typename C = float2>
+cudaError_t launch_f(const MvpGeom& g, C* t2, int L, const C* twz, const C* ghat, cudaStream_t st, const int* done) {
   static std::once_flag once;
   static cudaError_t cfg = cudaSuccess;
   std::call_once(once, [] {
-    cfg = cudaFuncSetAttribute(k_pass_c_static<P, SIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, kZSmemMax);
+    cfg = cudaFuncSetAttribute(k_pass_c_static<P, SIX, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, kZSmemMax);
   });
   if (cfg != cudaSuccess) return cfg;
-  const int per_warp = (SIX ? 6 : 3) * P::LW * (int)sizeof(float2);
+  const int per_warp = (SIX ? 6 : 3) * P::LW * (int)sizeof(C);
   const int wpc = z_warps_per_cta(per_warp);
   const long long ntask = (long long)g.Px * g.Py * L;
   const unsigned grid = (unsigned)((ntask + wpc - 1) / wpc);
-  k_pass_c_static<P, SIX><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.Px, g.Py, g.nz, g.nzp, twz, ghat, done);
+  k_pass_c_static<P, SIX, C><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.Px, g.Py, g.nz, g.nzp, twz, ghat, done);
   return cudaGetLastError();
 }
 
