@@ -45,8 +45,8 @@ REF_ITERS_DEFAULT = 30
 # DRAM traffic of the complex FP32 MVP passes over their byte model:
 # ncu dram__bytes_read.sum + dram__bytes_write.sum per launch on the N=8192,
 # L=16 aggregate (box 54x61x57), divided by bdda_op_mvp_bytes of the same pass
-TRAFFIC_OVER_MODEL = {"passA_c64": 0.68, "passB_c64": 0.922, "passC_c64": 0.909, "passD_c64": 0.993,
-                      "passE_c64": 1.225}
+TRAFFIC_OVER_MODEL = {"passA_c64": 0.54, "passB_c64": 0.995, "passC_c64": 0.958, "passD_c64": 0.987,
+                      "passE_c64": 1.224}
 
 
 def parse():
