@@ -24,6 +24,7 @@ struct SolverCtl {
   int flags;
   double err;       // last recurrence error (the value the reference prints)
   double bnorm;     // ||B||_F of the (preconditioned) right-hand side
+  double tol;       // stopping tolerance of the COCG-RQ recurrence error
 };
 
 __device__ __forceinline__ bool ctl_skip(const SolverCtl* ctl) {

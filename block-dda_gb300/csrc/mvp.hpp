@@ -57,6 +57,32 @@ enum KernelId {
 };
 
 // Optional per-kernel CUDA-event timing (accumulated when resolved).
+// Launch counts and timed event pairs of kernels launched while a stream was
+// captured into a graph: the graph's event-record nodes re-record the same
+// events at every replay, and the timer adds the record once per replay.
+struct TimerRec {
+  struct Pair { int id; cudaEvent_t a, b; };
+  long long counts[kNumKernelIds] = {0};
+  std::vector<Pair> pairs;
+  std::vector<cudaEvent_t> owned;
+  cudaEvent_t event() {
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    owned.push_back(e);
+    return e;
+  }
+  void clear() {
+    for (auto e : owned) cudaEventDestroy(e);
+    owned.clear();
+    pairs.clear();
+    for (auto& c : counts) c = 0;
+  }
+  TimerRec() = default;
+  TimerRec(const TimerRec&) = delete;
+  TimerRec& operator=(const TimerRec&) = delete;
+  ~TimerRec() { clear(); }
+};
+
 struct KernelTimer {
   struct Pending { int id; cudaEvent_t a, b; };
   std::vector<Pending> pending;
@@ -65,25 +91,33 @@ struct KernelTimer {
   long long launches[kNumKernelIds] = {0};
   cudaEvent_t cur_a[kNumKernelIds] = {};
   bool enabled = false;
-  unsigned mask = ~0u;  // kernel classes timed while enabled (bit per KernelId)
+  unsigned mask = ~0u;      // kernel classes timed while enabled (bit per KernelId)
+  TimerRec* rec = nullptr;  // set while the launching stream is captured into a graph
 
   cudaEvent_t get() {
+    if (rec) return rec->event();
     if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
     cudaEvent_t e; cudaEventCreate(&e); return e;
   }
-  void count(int id, int k = 1) { launches[id] += k; }
+  void record(cudaEvent_t e, cudaStream_t st) {
+    if (rec) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);  // an event-record node of the graph
+    else cudaEventRecord(e, st);
+  }
+  void count(int id, int k = 1) { (rec ? rec->counts[id] : launches[id]) += k; }
   bool on(int id) const { return enabled && ((mask >> id) & 1u); }
+  unsigned state() const { return enabled ? mask : 0u; }
   void begin(int id, cudaStream_t st) {
-    launches[id]++;
+    count(id);
     if (!on(id)) return;
     cur_a[id] = get();
-    cudaEventRecord(cur_a[id], st);
+    record(cur_a[id], st);
   }
   void end(int id, cudaStream_t st) {
     if (!on(id)) return;
     cudaEvent_t b = get();
-    cudaEventRecord(b, st);
-    pending.push_back({id, cur_a[id], b});
+    record(b, st);
+    if (rec) rec->pairs.push_back({id, cur_a[id], b});
+    else pending.push_back({id, cur_a[id], b});
   }
   // Call after the stream was synchronised.
   void resolve() {
@@ -93,6 +127,14 @@ struct KernelTimer {
       pool.push_back(p.a); pool.push_back(p.b);
     }
     pending.clear();
+  }
+  // One replay of a graph recorded into r has completed (stream synchronised).
+  void replayed(const TimerRec& r) {
+    for (int i = 0; i < kNumKernelIds; ++i) launches[i] += r.counts[i];
+    for (auto& p : r.pairs) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) ms[p.id] += t;
+    }
   }
   void reset() {
     resolve();

@@ -175,6 +175,10 @@ template int op_block_mvp<dfl>(Op*, const Occupancy&, const dfc*, int, dfc*, int
 
 }  // namespace bdda
 
+void bdda::op_set_graphs(bdda_op* op, bool on) {
+  if (op) op->graphs = on;
+}
+
 using namespace bdda;
 
 // Green spectra of the operator's box, spacing and f at wavenumber k (FP64
@@ -305,6 +309,7 @@ int bdda_op_set_dipoles(bdda_op* op, const int* address, int nocc) {
     return BDDA_ERR_INVALID;
   }
   std::lock_guard<std::mutex> lk(op->mu);
+  ++op->dip_epoch;
   return build_occupancy(op, address, nocc, &op->dip);
 }
 

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -44,6 +45,23 @@ struct DevBuf {
   template <typename X> X* as() const { return static_cast<X*>(p); }
 };
 
+// Signature of buffers' addresses and sizes, folded with the MurmurHash3
+// 64-bit finaliser.  A graph captured with their pointers stays valid while
+// it is unchanged: ensure() only reallocates to a larger size, so an equal
+// (address, size) pair is the same live allocation.
+inline unsigned long long sig_mix(unsigned long long h, unsigned long long v) {
+  h ^= v;
+  h ^= h >> 33;
+  h *= 0xff51afd7ed558ccdULL;
+  h ^= h >> 33;
+  h *= 0xc4ceb9fe1a85ec53ULL;
+  h ^= h >> 33;
+  return h;
+}
+inline unsigned long long sig_add(unsigned long long h, const DevBuf& b) {
+  return sig_mix(sig_mix(h, (unsigned long long)(uintptr_t)b.p), (unsigned long long)b.bytes);
+}
+
 // Keep freed stream-ordered memory in the device pool (no release to the OS
 // at every synchronisation); called once per device.
 void keep_pool_memory();
@@ -72,12 +90,24 @@ struct Op {
   DevBuf tw32p[3];  // complex FP32 twiddle pairs {wx, wx, wy, wy} of the packed z pass ([2] only)
   DevBuf ghat64, ghat32, ghatdf;
   Occupancy dip;    // dipole occupancy (set_dipoles)
+  unsigned long long dip_epoch = 0;  // bumped whenever dip is rebuilt (captured MVPs hold its sizes)
   Occupancy cub;    // every cuboid site (the reference's MBT_fft_mvp vector)
   DevBuf t1[3], t2[3];   // MVP workspace per precision (0 = FP64, 1 = FP32, 2 = double-float)
   cudaStream_t stream = nullptr;
   KernelTimer timer;
   std::mutex mu;
   std::shared_ptr<SolverWork> solver;   // cached Krylov workspace (solver.cu)
+  bool graphs = true;  // COCG-RQ poll cycles as captured graphs (off under the request scheduler)
+
+  // signature of every buffer a block MVP's kernels are launched with
+  unsigned long long buffer_sig() const {
+    unsigned long long h = 0;
+    for (int i = 0; i < 3; ++i) {
+      for (const DevBuf* b : {&tw64[i], &tw32[i], &twdf[i], &tw32p[i], &t1[i], &t2[i]}) h = sig_add(h, *b);
+    }
+    for (const DevBuf* b : {&ghat64, &ghat32, &ghatdf, &dip.occ, &dip.tiles, &dip.tmask}) h = sig_add(h, *b);
+    return h;
+  }
 
   MvpGeom geom(const Occupancy& o, int set) const {
     MvpGeom g;
@@ -139,3 +169,8 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
 
 // The opaque handle of the C ABI.
 struct bdda_op : public bdda::Op {};
+
+namespace bdda {
+// COCG-RQ poll cycles as captured graphs for solves on op (default on).
+void op_set_graphs(bdda_op* op, bool on);
+}  // namespace bdda

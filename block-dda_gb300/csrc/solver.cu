@@ -29,6 +29,35 @@ enum Slot {
   kNumSlots
 };
 
+// One poll cycle of block COCG-RQ (the iterations between two reads of the
+// control block) captured as a CUDA graph: ~18 launches per iteration become
+// one graph launch, which is what bounds small systems.  It is replayed while
+// every argument its kernels were captured with is unchanged (the key); the
+// iteration index and the tolerance are read from the control block.
+struct CycleGraph {
+  struct Key {
+    const void *op, *X, *Bp, *Q, *diag, *jpre;
+    cudaStream_t st;
+    unsigned long long dip_epoch, op_bufs, work_bufs;
+    int n, L, full, cycle;
+    unsigned timing;
+  };
+  Key key;
+  cudaGraphExec_t exec = nullptr;
+  TimerRec rec;  // launch counts and timed pairs of one replay
+  CycleGraph() { std::memset(&key, 0, sizeof key); }
+  CycleGraph(const CycleGraph&) = delete;
+  CycleGraph& operator=(const CycleGraph&) = delete;
+  bool matches(const Key& k) const { return exec != nullptr && std::memcmp(&key, &k, sizeof k) == 0; }
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    rec.clear();
+    std::memset(&key, 0, sizeof key);
+  }
+  ~CycleGraph() { reset(); }
+};
+
 struct SolverWork {
   int n = 0, L = 0;
   DevBuf blk64[10], blk32[10];   // 0-7 Krylov blocks, 8 right-hand side, 9 solution
@@ -42,8 +71,18 @@ struct SolverWork {
   DevBuf small;                 // c128 [kNumSlots][L*L] + scalars
   DevBuf ctl;                   // SolverCtl
   DevBuf hist;                  // double[itermax]
+  CycleGraph cycle[2];          // COCG-RQ poll cycle per precision (0 FP64, 1 FP32)
   SolverCtl ctl_host_buf{};           // pageable: the poll copy completes before returning
   SolverCtl* ctl_host = &ctl_host_buf;
+
+  unsigned long long buffer_sig() const {
+    unsigned long long h = 0;
+    for (int i = 0; i < 10; ++i) h = sig_add(sig_add(h, blk64[i]), blk32[i]);
+    for (const DevBuf* b : {&X64, &R64, &Y64, &xdf, &ydf, &diagdf, &jpre64, &diag32, &jpre32, &gpart, &partials,
+                            &partials2, &vpart, &colf, &small, &ctl, &hist})
+      h = sig_add(h, *b);
+    return h;
+  }
 };
 
 namespace {
@@ -110,7 +149,8 @@ __device__ double block_sum_256(const double* __restrict__ vpart, int count) {
 }
 
 // Identity helpers and ||B|| from column-norm partials.  256 threads.
-__global__ void __launch_bounds__(256) k_small_init(const double* __restrict__ vpart, int nparts, int L, double2* st, SolverCtl* ctl) {
+__global__ void __launch_bounds__(256) k_small_init(const double* __restrict__ vpart, int nparts, int L, double2* st, SolverCtl* ctl,
+                                                    double tol) {
   const int LL = L * L;
   for (int e = threadIdx.x; e < LL; e += blockDim.x) {
     const int i = e % L, j = e / L;
@@ -124,6 +164,7 @@ __global__ void __launch_bounds__(256) k_small_init(const double* __restrict__ v
     ctl->status = 0;
     ctl->iter = 0;
     ctl->err = 1.0;
+    ctl->tol = tol;
     if (!(s > 0.0) || !isfinite(s)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; }
   }
 }
@@ -195,8 +236,8 @@ __device__ bool core_chol1(const SmallWork<R>& w, int L, double2* st, SolverCtl*
 //   beta = (Q^T Q)^-1 (tau^T Q'^T Q') ; Q^T Q <- Q'^T Q'.
 // Returns false on breakdown or when the stopping test passed (done).
 template <typename R, class LoadGT>
-__device__ bool core_chol2_beta(const SmallWork<R>& w, int L, double2* st, SolverCtl* ctl, double tol, double* hist,
-                                int k, int full, LoadGT load_gt) {
+__device__ bool core_chol2_beta(const SmallWork<R>& w, int L, double2* st, SolverCtl* ctl, double* hist, int full,
+                                LoadGT load_gt) {
   const int LL = L * L;
   if (!chol_and_inverse<R>(w.m0, w.m1, w.m2, L)) { fail(ctl); return false; }
   sm_store(slot(st, kR2Inv, L), w.m2, LL);
@@ -209,13 +250,16 @@ __device__ bool core_chol2_beta(const SmallWork<R>& w, int L, double2* st, Solve
   const double nrm = sm_fro<R>(w.m0, LL);
   __shared__ int stop;
   if (threadIdx.x == 0) {
+    // the iteration index and the tolerance come from the control block, so
+    // the launch is the same at every iteration (captured poll cycles)
+    const int k = ctl->iter;
     const double err = nrm / ctl->bnorm;
     ctl->err = err;
     if (hist) hist[k] = err;
     ctl->iter = k + 1;
     stop = 0;
     if (!isfinite(err)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; stop = 1; }
-    else if (err < tol) { ctl->done = 1; stop = 1; }
+    else if (err < ctl->tol) { ctl->done = 1; stop = 1; }
   }
   __syncthreads();
   if (stop) return false;
@@ -298,12 +342,11 @@ k_small_chol2(const double2* __restrict__ part, int nparts, int L, double2* st, 
 //   beta = (Q^T Q)^-1 (tau^T Q'^T Q') ; Q^T Q <- Q'^T Q'.
 template <typename R>
 __global__ void __launch_bounds__(kSmallThreads)
-k_small_chol2_beta(const double2* __restrict__ part, int L, double2* st, SolverCtl* ctl, double tol, double* hist, int k,
-                   int full) {
+k_small_chol2_beta(const double2* __restrict__ part, int L, double2* st, SolverCtl* ctl, double* hist, int full) {
   if (ctl_skip(ctl)) return;
   SMALL_PROLOGUE
   sm_reduce<R>(m0, part, 1, LL);
-  core_chol2_beta<R>(SMALL_WORK, L, st, ctl, tol, hist, k, full, [&](M* d) { sm_reduce<R>(d, part + LL, 1, LL); });
+  core_chol2_beta<R>(SMALL_WORK, L, st, ctl, hist, full, [&](M* d) { sm_reduce<R>(d, part + LL, 1, LL); });
 }
 
 // COCG-RQ alpha: alpha = (S^T AS)^-1 (Q^T Q) ; A_xi = alpha xi ; -alpha
@@ -496,11 +539,11 @@ struct Krylov {
   }
 
   // ||Bp||_F -> ctl->bnorm, identity slots, control reset
-  int init(const C* Bp) {
+  int init(const C* Bp, double tol) {
     double* vp = w->vpart.as<double>();
     const int g = vec_grid((size_t)n * L);
     k_colnorm2<T><<<g, 256, 0, st>>>(Bp, n, n, L, vp);
-    k_small_init<<<1, 256, 0, st>>>(vp, g, L, small(), ctl());
+    k_small_init<<<1, 256, 0, st>>>(vp, g, L, small(), ctl(), tol);
     op->timer.count(kOther, 2);
     return cudaGetLastError() == cudaSuccess ? BDDA_OK : cuda_fail(cudaGetLastError(), "init");
   }
@@ -516,34 +559,123 @@ struct Krylov {
     rowmm(W, sl(kR2Inv), nullptr, nullptr, nullptr, Q);
   }
 
-  // Block COCG-RQ (bl_cocg_rq_mvp_fft.cpp:22-71 / bl_cocg_rq_jacobi_mvp_fft.cpp:22-78)
-  int cocg_rq(const C* Bp, C* X, bool full, double tol, int itermax, int* iters, double* err, int* status) {
-    C* Q = blk(0); C* Qn = blk(1); C* S = blk(2); C* AS = blk(3); C* W = blk(4);
+  // One block COCG-RQ iteration; first adds the Gram Q^T Q of the starting block.
+  int cocg_iteration(bool first, C* Q, C* Qn, C* S, C* AS, C* W, C* X, bool full) {
     double2* p = w->partials.template as<double2>();
     double2* p2 = w->partials2.template as<double2>();
+    BDDA_TRY(mvp(S, AS));
+    gram<false>(S, AS, p);
+    if (first) gram<false>(Q, Q, p2);
+    small_launch(k_small_cocg_alpha<SR>, (const double2*)p, (const double2*)(first ? p2 : nullptr), 1, L, small(), ctl(),
+                 (int)full);
+    rowmm(S, sl(kAXi), nullptr, nullptr, X, X);           // X += S alpha xi
+    rowmm(AS, sl(kNAlpha), nullptr, nullptr, Q, W);       // W = Q - AS alpha
+    gram<true>(W, W, p);
+    small_launch(k_small_chol1<SR>, (const double2*)p, 1, L, small(), ctl());
+    rowmm(W, sl(kR1Inv), nullptr, nullptr, nullptr, W);   // W1
+    gram2(W, p);                                          // W1^H W1, W1^T W1
+    small_launch(k_small_chol2_beta<SR>, (const double2*)p, L, small(), ctl(), w->hist.as<double>(), (int)full);
+    rowmm2(W, sl(kR2Inv), S, sl(kBeta), Qn, S);           // Q' = W1 R2^-1 ; S = Q' + S beta
+    return BDDA_OK;
+  }
+
+  // Poll cycles run as graphs on a stream that can be captured, with an even
+  // cycle length (Q and Qn are back in place after it); BDDA_NO_GRAPH turns
+  // them off (diagnostics).
+  bool graphs_allowed() const {
+    return op->graphs && check_every >= 2 && check_every % 2 == 0 && st != nullptr && st != cudaStreamLegacy &&
+           std::getenv("BDDA_NO_GRAPH") == nullptr;
+  }
+
+  // Launches one poll cycle (check_every iterations, none of them the first)
+  // as a graph, captured now if the cached one was captured with other
+  // arguments.  *ran = false when the stream could not be captured: nothing
+  // was launched then, and the caller runs the cycle launch by launch.
+  int cycle_graph(C* Q, C* Qn, C* S, C* AS, C* W, C* X, const C* Bp, bool full, bool* ran) {
+    *ran = false;
+    CycleGraph& cg = w->cycle[std::is_same<T, double>::value ? 0 : 1];
+    CycleGraph::Key key;
+    std::memset(&key, 0, sizeof key);
+    key.op = op;
+    key.X = X;
+    key.Bp = Bp;
+    key.Q = Q;
+    key.diag = diag;
+    key.jpre = jpre;
+    key.st = st;
+    key.dip_epoch = op->dip_epoch;
+    key.op_bufs = op->buffer_sig();
+    key.work_bufs = w->buffer_sig();
+    key.n = n;
+    key.L = L;
+    key.full = full ? 1 : 0;
+    key.cycle = check_every;
+    key.timing = op->timer.state();
+    if (!cg.matches(key)) {
+      cg.reset();
+      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return BDDA_OK;
+      }
+      op->timer.rec = &cg.rec;
+      const int mvps_before = mvps;
+      int rc = BDDA_OK;
+      C* q = Q;
+      C* qn = Qn;
+      for (int i = 0; i < check_every && rc == BDDA_OK; ++i) {
+        rc = cocg_iteration(false, q, qn, S, AS, W, X, full);
+        std::swap(q, qn);
+      }
+      mvps = mvps_before;
+      op->timer.rec = nullptr;
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+      cudaError_t ei = cudaErrorStreamCaptureInvalidated;
+      if (rc == BDDA_OK && ec == cudaSuccess && graph) ei = cudaGraphInstantiate(&cg.exec, graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      if (ei != cudaSuccess) {
+        cg.exec = nullptr;
+        cg.reset();
+        (void)cudaGetLastError();
+        return rc;  // an argument error of the iteration itself, else OK with *ran false
+      }
+      cg.key = key;
+    }
+    BDDA_CUDA(cudaGraphLaunch(cg.exec, st));
+    mvps += check_every;
+    *ran = true;
+    return BDDA_OK;
+  }
+
+  // Block COCG-RQ (bl_cocg_rq_mvp_fft.cpp:22-71 / bl_cocg_rq_jacobi_mvp_fft.cpp:22-78).
+  // The host reads the control block every check_every iterations; the
+  // cycles after the first run as one captured graph each.
+  int cocg_rq(const C* Bp, C* X, bool full, double tol, int itermax, int* iters, double* err, int* status) {
+    C* Q = blk(0); C* Qn = blk(1); C* S = blk(2); C* AS = blk(3); C* W = blk(4);
     BDDA_CUDA(cudaMemsetAsync(X, 0, sizeof(C) * (size_t)n * L, st));
-    BDDA_TRY(init(Bp));
+    BDDA_TRY(init(Bp, tol));
     cholqr2(Bp, W, Q, 0);
     BDDA_CUDA(cudaMemcpyAsync(S, Q, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
     bool done = false;
+    bool graphs = graphs_allowed();
     int k = 0;
-    for (; k < itermax; ++k) {
-      BDDA_TRY(mvp(S, AS));
-      gram<false>(S, AS, p);
-      if (k == 0) gram<false>(Q, Q, p2);
-      small_launch(k_small_cocg_alpha<SR>, (const double2*)p, (const double2*)(k == 0 ? p2 : nullptr), 1, L, small(), ctl(),
-                   (int)full);
-      rowmm(S, sl(kAXi), nullptr, nullptr, X, X);           // X += S alpha xi
-      rowmm(AS, sl(kNAlpha), nullptr, nullptr, Q, W);       // W = Q - AS alpha
-      gram<true>(W, W, p);
-      small_launch(k_small_chol1<SR>, (const double2*)p, 1, L, small(), ctl());
-      rowmm(W, sl(kR1Inv), nullptr, nullptr, nullptr, W);   // W1
-      gram2(W, p);                                          // W1^H W1, W1^T W1
-      small_launch(k_small_chol2_beta<SR>, (const double2*)p, L, small(), ctl(), tol, w->hist.as<double>(), k,
-                   (int)full);
-      rowmm2(W, sl(kR2Inv), S, sl(kBeta), Qn, S);           // Q' = W1 R2^-1 ; S = Q' + S beta
+    while (k < itermax) {
+      if (graphs && k >= check_every && k % check_every == 0 && k + check_every <= itermax) {
+        bool ran = false;
+        BDDA_TRY(cycle_graph(Q, Qn, S, AS, W, X, Bp, full, &ran));
+        if (ran) {
+          k += check_every;  // an even number of swaps: Q and Qn are where they were
+          BDDA_TRY(poll(&done));
+          op->timer.replayed(w->cycle[std::is_same<T, double>::value ? 0 : 1].rec);
+          if (done) break;
+          continue;
+        }
+        graphs = false;
+      }
+      BDDA_TRY(cocg_iteration(k == 0, Q, Qn, S, AS, W, X, full));
       std::swap(Q, Qn);
-      if ((k + 1) % check_every == 0 || k + 1 == itermax) {
+      ++k;
+      if (k % check_every == 0 || k == itermax) {
         BDDA_TRY(poll(&done));
         if (done) break;
       }
@@ -563,7 +695,7 @@ struct Krylov {
     double2* vp = w->vpart.as<double2>();
     double2* scal = sl(kNumSlots);  // 2 scalars after the matrix slots
     BDDA_CUDA(cudaMemsetAsync(X, 0, sizeof(C) * (size_t)n * L, st));
-    BDDA_TRY(init(Bp));
+    BDDA_TRY(init(Bp, tol));
     BDDA_CUDA(cudaMemcpyAsync(R, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
     BDDA_CUDA(cudaMemcpyAsync(P, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
     BDDA_CUDA(cudaMemcpyAsync(R0, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
@@ -614,7 +746,7 @@ struct Krylov {
     double2* vp = w->vpart.as<double2>();
     double2* scal = sl(kNumSlots);
     BDDA_CUDA(cudaMemsetAsync(X, 0, sizeof(C) * (size_t)n * L, st));
-    BDDA_TRY(init(Bp));
+    BDDA_TRY(init(Bp, tol));
     BDDA_CUDA(cudaMemcpyAsync(R, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
     BDDA_CUDA(cudaMemcpyAsync(P, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
     BDDA_CUDA(cudaMemcpyAsync(R0, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
@@ -1041,7 +1173,7 @@ int bdda_qr_reduced(const double* A, int m, int nc, int lda, double* Q, int ldq,
   double2* s = w->blk64[2].as<double2>();
   BDDA_CUDA(cudaMemcpy2DAsync(a, sizeof(double2) * m, A, sizeof(double2) * (size_t)lda, sizeof(double2) * m, nc,
                               cudaMemcpyHostToDevice, st));
-  rc = kr.init(a);
+  rc = kr.init(a, 0.0);
   if (rc != BDDA_OK) return rc;
   kr.cholqr2(a, s, q, 2);
   std::vector<double2> hr((size_t)nc * nc);
