@@ -18,7 +18,13 @@ Bank model: 32 banks of 4 bytes; 8-byte accesses are served per half-warp and
 a group takes as many wavefronts as the largest number of distinct words in one
 bank (this reproduces the shared-memory wavefront counts ncu reports).
 
-Usage: python gen_zplans.py [z] [t]   (writes zplans.inc / tplans.inc beside it)
+  yplans.inc  the column-pair y passes (two lines interleaved element by
+              element per warp): the radix sequences of tplans.inc, the
+              padded layout chosen for the interleaved pairs and the 16-byte
+              tile fill / drain of eight column pairs
+
+Usage: python gen_zplans.py [z] [t] [il]   (writes the tables beside it;
+       il reads the radix sequences from tplans.inc)
 """
 import os
 import sys
@@ -128,6 +134,70 @@ def cost_tile(n, rad, S, LW):
     return wf + instr / 4.0 + 2 * tw / 8.0
 
 
+def wavefronts16(chunks):
+    """16-byte accesses, served per quarter-warp: a group of eight takes as many
+    wavefronts as the most distinct 16-byte chunks on one set of four banks."""
+    total = 0
+    for g0 in range(0, len(chunks), 8):
+        groups = {}
+        for c in chunks[g0:g0 + 8]:
+            groups.setdefault(c & 7, set()).add(c)
+        total += max(len(v) for v in groups.values())
+    return total
+
+
+def stage_cost_il(n, rad, S, LW):
+    """Shared-memory wavefronts of one transform of a line pair interleaved
+    element by element (element idx of line h at 8-byte word 2 addr(idx) + h;
+    lane t handles butterfly t >> 1 of line t & 1)."""
+    rl = rad[-1]
+
+    def addr(idx):
+        return (idx // rl) * S + idx % rl
+    wf = 0
+    Ls = n
+    for R in rad:
+        M = Ls // R
+        B = n // R
+        for t0 in range(0, 2 * B, 32):
+            chunk = range(t0, min(2 * B, t0 + 32))
+            for i in range(R):
+                a = []
+                for t in chunk:
+                    b, n1 = divmod(t >> 1, M)
+                    a.append(2 * addr(b * Ls + n1 + i * M) + (t & 1))
+                wf += 2 * wavefronts(a)                       # load + store
+        Ls = M
+    return wf
+
+
+def cost_y_il(n, rad, S, LW):
+    """One line pair of a column-pair y pass (k_pass_y2i): its transform plus
+    its share of the tile fill and drain, where the eight lanes of a
+    quarter-warp move one row of the task's eight column pairs (pair p of row
+    r at 16-byte chunk p LW + addr(r)), over the n rows of the padded line."""
+    rl = rad[-1]
+    tw = 0
+    for r in range(n):
+        a = (r // rl) * S + r % rl
+        tw += wavefronts16([p * LW + a for p in range(8)])
+    return stage_cost_il(n, rad, S, LW) + 2 * tw / 8.0
+
+
+def choose_layout(n, rad, cost):
+    """The padded layout (S, LW) for a fixed radix sequence."""
+    rl = rad[-1]
+    best = None
+    for S in range(rl, rl + 4):
+        top = (n // rl - 1) * S + rl
+        for d in range(16):
+            LW = top + d
+            key = (cost(n, rad, S, LW), LW, S)
+            if best is None or key < best[0]:
+                best = (key, S, LW)
+    return best[1], best[2]
+
+
 def choose(n, cost):
     best = None
     for rad in sequences(n):
@@ -157,9 +227,44 @@ def write(path, macro, what, cost):
         f.write("\n".join(lines) + "\n")
 
 
+def read_radices(path, macro):
+    """{N: radices} of a generated table."""
+    out = {}
+    with open(path) as f:
+        for line in f:
+            if line.startswith(macro + "("):
+                v = [int(x) for x in line[len(macro) + 1:line.index(")")].split(",")]
+                out[v[1]] = tuple(v[4:])
+    return out
+
+
+def write_il(path, macro, what, cost, radices):
+    """A table with the given radix sequences and the layout of `cost`."""
+    lines = ["// Generated by gen_zplans.py: compile-time plans of the %s." % what,
+             "// %s(index, N, S, LW, radices...): element q*R_last + r at q*S + r, lines LW apart." % macro]
+    for idx, n in enumerate(sorted(radices)):
+        rad = radices[n]
+        S, LW = choose_layout(n, rad, cost)
+        lines.append("%s(%d, %d, %d, %d, %s)" % (macro, idx, n, S, LW, ", ".join(str(r) for r in rad)))
+        print(macro, n, rad, S, LW, file=sys.stderr, flush=True)
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
 def main():
     here = os.path.dirname(os.path.abspath(__file__))
     which = sys.argv[1:] or ["z", "t"]
+    if "il" in which:
+        # the column-pair y passes: the radix sequences of the single-line
+        # table (they fix the digit order the Green spectrum is packed in),
+        # the layout for interleaved line pairs and 16-byte rows of eight
+        # pairs.  (The x passes drain two rows of four pairs per quarter-warp;
+        # modelled the same way, tplans.inc's layouts are already as good
+        # there, so they keep that table.)
+        rad = read_radices(os.path.join(here, "tplans.inc"), "BDDA_TPLAN")
+        write_il(os.path.join(here, "yplans.inc"), "BDDA_YPLAN",
+                 "column-pair y passes (line pairs interleaved, eight pairs per task)", cost_y_il, rad)
+        return
     if "z" in which:
         write(os.path.join(here, "zplans.inc"), "BDDA_ZPLAN", "fused z pass (three lines per warp)", cost_z)
     if "t" in which:

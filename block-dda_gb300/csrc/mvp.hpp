@@ -180,7 +180,7 @@ struct TileArgs {
 enum TilePass { kTileA = 0, kTileB, kTileD, kTileE };
 
 // Strided pass `pass` for complex FP32 with the compile-time plan of its axis
-// (tplans.inc: Px for A / E, Py for B / D); false (nothing launched) when the
+// (tplans.inc: Px for A / E; yplans.inc: Py for B / D); false (nothing launched) when the
 // length has none.  *err: launch status.
 bool launch_tile_static(int pass, const TileArgs& a, cudaError_t* err);
 

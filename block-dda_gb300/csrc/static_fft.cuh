@@ -11,7 +11,7 @@
 // stage s before the last steps through its butterfly in multiples of R_last
 // (M_s is a multiple of it), so its elements are (M_s / R_last) * S apart; the
 // last stage's are adjacent.  Lines are LW elements apart.  The plans come
-// from zplans.inc / tplans.inc (gen_zplans.py).
+// from zplans.inc / tplans.inc / yplans.inc (gen_zplans.py).
 #pragma once
 
 #include "fft_core.cuh"

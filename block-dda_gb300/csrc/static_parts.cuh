@@ -57,17 +57,32 @@ bool dispatch_z_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz, const dfz
 
 template <int PART>
 bool dispatch_tile(int pass, const TileArgs& a, cudaError_t* err) {
-  const int n = (pass == kTileA || pass == kTileE) ? a.g->Px : a.g->Py;
-  switch (n) {
+  if (pass == kTileA || pass == kTileE) {
+    switch (a.g->Px) {
 #define BDDA_TPLAN(I, N, S, LW, ...)                                                     \
   case N:                                                                                \
     if constexpr ((I) % kParts == PART) {                                                \
-      *err = tstatic::launch<sfft::Plan<N, S, LW, __VA_ARGS__>>(pass, a);                \
+      *err = tstatic::launch_x<sfft::Plan<N, S, LW, __VA_ARGS__>>(pass, a);              \
       return true;                                                                       \
     }                                                                                    \
     return false;
 #include "tplans.inc"
 #undef BDDA_TPLAN
+      default:
+        break;
+    }
+    return false;
+  }
+  switch (a.g->Py) {
+#define BDDA_YPLAN(I, N, S, LW, ...)                                                     \
+  case N:                                                                                \
+    if constexpr ((I) % kParts == PART) {                                                \
+      *err = tstatic::launch_y<sfft::Plan<N, S, LW, __VA_ARGS__>>(pass, a);              \
+      return true;                                                                       \
+    }                                                                                    \
+    return false;
+#include "yplans.inc"
+#undef BDDA_YPLAN
     default:
       break;
   }

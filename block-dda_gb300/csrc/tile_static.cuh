@@ -1,6 +1,6 @@
-// Strided passes (A, B, D, E) for complex FP32 with compile-time axis plans
-// (tplans.inc): the two-line kernels of tile_passes.cuh instantiated for the
-// plan of their axis length.
+// Strided passes (A, B, D, E) for complex FP32 with compile-time axis plans:
+// the column-pair kernels of tile_passes.cuh instantiated for the plan of
+// their axis length (x: tplans.inc, y: yplans.inc).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -21,41 +21,49 @@ cudaError_t set_smem(K kernel, int bytes, std::once_flag& once, cudaError_t& cfg
   return cfg;
 }
 
+// x passes (A, E) with the plan of Px (tplans.inc)
 template <class P>
-cudaError_t launch(int pass, const TileArgs& a) {
+cudaError_t launch_x(int pass, const TileArgs& a) {
   const MvpGeom& g = *a.g;
   const int max_nx = kMaxLine / 2;
-  // x passes: [2 buffers][8 columns][2 fields] lines + the occupancy of the tile
+  // [2 buffers][8 columns][2 fields] lines + the occupancy of the tile
   auto smem_x2 = [](int nx) { return 4 * kTZ * P::LW * (int)sizeof(float2) + nx * kTZ * 4; };
   const int smem_ae = smem_x2(max_nx);
-  const int smem_bd = 2 * tile::kTZ2 * P::LW * (int)sizeof(float2);  // y passes: 16 columns per task
+  static std::once_flag oa, oe;
+  static cudaError_t ca = cudaSuccess, ce = cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  if (pass == kTileA) {
+    if ((e = set_smem(tile::k_pass_a2i<P>, smem_ae, oa, ca)) != cudaSuccess) return e;
+    tile::k_pass_a2i<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
+        a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.t1, a.done);
+  } else {
+    if ((e = set_smem(tile::k_pass_e2i<P>, smem_ae, oe, ce)) != cudaSuccess) return e;
+    tile::k_pass_e2i<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
+        a.t1, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
+        a.done);
+  }
+  return cudaGetLastError();
+}
+
+// y passes (B, D) with the plan of Py (yplans.inc: the radix sequence of
+// tplans.inc, a layout for interleaved pairs and rows of eight pairs)
+template <class P>
+cudaError_t launch_y(int pass, const TileArgs& a) {
+  const MvpGeom& g = *a.g;
+  const int smem_bd = 2 * tile::kTZ2 * P::LW * (int)sizeof(float2);  // 16 columns per task
   const int ntask2 = a.nfield * g.Px * ((g.nz + tile::kTZ2 - 1) / tile::kTZ2);
   const int grid2 = std::min(ntask2, a.grid_y);
-  static std::once_flag oa, ob, od, oe;
-  static cudaError_t ca = cudaSuccess, cb = cudaSuccess, cd = cudaSuccess, ce = cudaSuccess;
+  static std::once_flag ob, od;
+  static cudaError_t cb = cudaSuccess, cd = cudaSuccess;
   cudaError_t e = cudaSuccess;
-  switch (pass) {
-    case kTileA:
-      if ((e = set_smem(tile::k_pass_a2i<P>, smem_ae, oa, ca)) != cudaSuccess) return e;
-      tile::k_pass_a2i<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
-          a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.t1, a.done);
-      break;
-    case kTileB:
-      if ((e = set_smem(tile::k_pass_y2i<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
-      tile::k_pass_y2i<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
-                                                                        ntask2, a.twy, a.done);
-      break;
-    case kTileD:
-      if ((e = set_smem(tile::k_pass_y2i<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
-      tile::k_pass_y2i<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
-                                                                       ntask2, a.twy, a.done);
-      break;
-    default:
-      if ((e = set_smem(tile::k_pass_e2i<P>, smem_ae, oe, ce)) != cudaSuccess) return e;
-      tile::k_pass_e2i<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
-          a.t1, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
-          a.done);
-      break;
+  if (pass == kTileB) {
+    if ((e = set_smem(tile::k_pass_y2i<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
+    tile::k_pass_y2i<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
+                                                                      ntask2, a.twy, a.done);
+  } else {
+    if ((e = set_smem(tile::k_pass_y2i<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
+    tile::k_pass_y2i<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
+                                                                     ntask2, a.twy, a.done);
   }
   return cudaGetLastError();
 }
