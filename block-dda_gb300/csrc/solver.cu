@@ -39,11 +39,12 @@ struct CycleGraph {
     const void *op, *X, *Bp, *Q, *diag, *jpre;
     cudaStream_t st;
     unsigned long long dip_epoch, op_bufs, work_bufs;
-    int n, L, full, cycle;
+    int solver, n, L, full, cycle;
     unsigned timing;
   };
   Key key;
   cudaGraphExec_t exec = nullptr;
+  int mvps = 0;  // block MVPs one replay runs
   TimerRec rec;  // launch counts and timed pairs of one replay
   CycleGraph() { std::memset(&key, 0, sizeof key); }
   CycleGraph(const CycleGraph&) = delete;
@@ -52,6 +53,7 @@ struct CycleGraph {
   void reset() {
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
+    mvps = 0;
     rec.clear();
     std::memset(&key, 0, sizeof key);
   }
@@ -424,17 +426,19 @@ __global__ void k_small_zeta(const double2* __restrict__ p1, const double2* __re
 }
 
 // err = sqrt(sum of column-norm partials) / bnorm ; stopping test.  256 threads.
-__global__ void __launch_bounds__(256) k_small_err(const double* __restrict__ vpart, int nparts, int L, SolverCtl* ctl, double tol,
-                                                   double* hist, int k) {
+// The iteration index and tolerance come from the control block (captured cycles).
+__global__ void __launch_bounds__(256) k_small_err(const double* __restrict__ vpart, int nparts, int L, SolverCtl* ctl,
+                                                   double* hist) {
   if (ctl_skip(ctl)) return;
   const double s = block_sum_256(vpart, nparts * L);
   if (threadIdx.x == 0) {
+    const int k = ctl->iter;
     const double err = sqrt(s) / ctl->bnorm;
     ctl->err = err;
     if (hist) hist[k] = err;
     ctl->iter = k + 1;
     if (!isfinite(err)) { ctl->status = BDDA_ERR_BREAKDOWN; ctl->done = 1; }
-    else if (err < tol) ctl->done = 1;
+    else if (err < ctl->tol) ctl->done = 1;
   }
 }
 
@@ -587,11 +591,13 @@ struct Krylov {
            std::getenv("BDDA_NO_GRAPH") == nullptr;
   }
 
-  // Launches one poll cycle (check_every iterations, none of them the first)
-  // as a graph, captured now if the cached one was captured with other
-  // arguments.  *ran = false when the stream could not be captured: nothing
-  // was launched then, and the caller runs the cycle launch by launch.
-  int cycle_graph(C* Q, C* Qn, C* S, C* AS, C* W, C* X, const C* Bp, bool full, bool* ran) {
+  // Launches one poll cycle as a graph: `cycle` issues its check_every
+  // iterations (none of them the first) and runs only under capture, when the
+  // cached graph was captured with other arguments.  *ran = false when the
+  // stream could not be captured: nothing was launched then, and the caller
+  // runs the cycle launch by launch.
+  template <class Cycle>
+  int cycle_graph(int solver, const C* X, const C* Bp, const C* first, bool full, Cycle cycle, bool* ran) {
     *ran = false;
     CycleGraph& cg = w->cycle[std::is_same<T, double>::value ? 0 : 1];
     CycleGraph::Key key;
@@ -599,13 +605,14 @@ struct Krylov {
     key.op = op;
     key.X = X;
     key.Bp = Bp;
-    key.Q = Q;
+    key.Q = first;
     key.diag = diag;
     key.jpre = jpre;
     key.st = st;
     key.dip_epoch = op->dip_epoch;
     key.op_bufs = op->buffer_sig();
     key.work_bufs = w->buffer_sig();
+    key.solver = solver;
     key.n = n;
     key.L = L;
     key.full = full ? 1 : 0;
@@ -619,13 +626,8 @@ struct Krylov {
       }
       op->timer.rec = &cg.rec;
       const int mvps_before = mvps;
-      int rc = BDDA_OK;
-      C* q = Q;
-      C* qn = Qn;
-      for (int i = 0; i < check_every && rc == BDDA_OK; ++i) {
-        rc = cocg_iteration(false, q, qn, S, AS, W, X, full);
-        std::swap(q, qn);
-      }
+      const int rc = cycle();
+      const int cycle_mvps = mvps - mvps_before;
       mvps = mvps_before;
       op->timer.rec = nullptr;
       cudaGraph_t graph = nullptr;
@@ -640,31 +642,34 @@ struct Krylov {
         return rc;  // an argument error of the iteration itself, else OK with *ran false
       }
       cg.key = key;
+      cg.mvps = cycle_mvps;
     }
     BDDA_CUDA(cudaGraphLaunch(cg.exec, st));
-    mvps += check_every;
+    mvps += cg.mvps;
     *ran = true;
     return BDDA_OK;
   }
 
-  // Block COCG-RQ (bl_cocg_rq_mvp_fft.cpp:22-71 / bl_cocg_rq_jacobi_mvp_fft.cpp:22-78).
-  // The host reads the control block every check_every iterations; the
-  // cycles after the first run as one captured graph each.
-  int cocg_rq(const C* Bp, C* X, bool full, double tol, int itermax, int* iters, double* err, int* status) {
-    C* Q = blk(0); C* Qn = blk(1); C* S = blk(2); C* AS = blk(3); C* W = blk(4);
-    BDDA_CUDA(cudaMemsetAsync(X, 0, sizeof(C) * (size_t)n * L, st));
-    BDDA_TRY(init(Bp, tol));
-    cholqr2(Bp, W, Q, 0);
-    BDDA_CUDA(cudaMemcpyAsync(S, Q, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+  // The iteration loop of the solvers.  iter(first) issues one iteration; the
+  // host reads the control block every check_every iterations, and every
+  // cycle after the first runs as one captured graph (the buffers an
+  // iteration swaps are back in place after an even number of iterations).
+  // first_blk names the block the cycle starts from (COCG-RQ's Q), else null.
+  template <class Iter>
+  int iterate(int solver, const C* X, const C* Bp, const C* const* first_blk, bool full, int itermax, Iter iter) {
     bool done = false;
     bool graphs = graphs_allowed();
     int k = 0;
     while (k < itermax) {
       if (graphs && k >= check_every && k % check_every == 0 && k + check_every <= itermax) {
         bool ran = false;
-        BDDA_TRY(cycle_graph(Q, Qn, S, AS, W, X, Bp, full, &ran));
+        auto cycle = [&]() -> int {
+          for (int i = 0; i < check_every; ++i) BDDA_TRY(iter(false));
+          return BDDA_OK;
+        };
+        BDDA_TRY(cycle_graph(solver, X, Bp, first_blk ? *first_blk : nullptr, full, cycle, &ran));
         if (ran) {
-          k += check_every;  // an even number of swaps: Q and Qn are where they were
+          k += check_every;
           BDDA_TRY(poll(&done));
           op->timer.replayed(w->cycle[std::is_same<T, double>::value ? 0 : 1].rec);
           if (done) break;
@@ -672,8 +677,7 @@ struct Krylov {
         }
         graphs = false;
       }
-      BDDA_TRY(cocg_iteration(k == 0, Q, Qn, S, AS, W, X, full));
-      std::swap(Q, Qn);
+      BDDA_TRY(iter(k == 0));
       ++k;
       if (k % check_every == 0 || k == itermax) {
         BDDA_TRY(poll(&done));
@@ -681,6 +685,21 @@ struct Krylov {
       }
     }
     if (!done) BDDA_TRY(poll(&done));
+    return BDDA_OK;
+  }
+
+  // Block COCG-RQ (bl_cocg_rq_mvp_fft.cpp:22-71 / bl_cocg_rq_jacobi_mvp_fft.cpp:22-78)
+  int cocg_rq(const C* Bp, C* X, bool full, double tol, int itermax, int* iters, double* err, int* status) {
+    C* Q = blk(0); C* Qn = blk(1); C* S = blk(2); C* AS = blk(3); C* W = blk(4);
+    BDDA_CUDA(cudaMemsetAsync(X, 0, sizeof(C) * (size_t)n * L, st));
+    BDDA_TRY(init(Bp, tol));
+    cholqr2(Bp, W, Q, 0);
+    BDDA_CUDA(cudaMemcpyAsync(S, Q, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
+    BDDA_TRY(iterate(0, X, Bp, &Q, full, itermax, [&](bool first) -> int {
+      BDDA_TRY(cocg_iteration(first, Q, Qn, S, AS, W, X, full));
+      std::swap(Q, Qn);
+      return BDDA_OK;
+    }));
     *iters = w->ctl_host->iter;
     *err = w->ctl_host->err;
     *status = w->ctl_host->status;
@@ -700,9 +719,7 @@ struct Krylov {
     BDDA_CUDA(cudaMemcpyAsync(P, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
     BDDA_CUDA(cudaMemcpyAsync(R0, Bp, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
     const int gv = vec_grid((size_t)n * L);
-    bool done = false;
-    int k = 0;
-    for (; k < itermax; ++k) {
+    BDDA_TRY(iterate(1, X, Bp, nullptr, false, itermax, [&](bool) -> int {
       BDDA_TRY(mvp(P, V));                                   // V = A P
       gram<true>(R0, V, p);
       gram<true>(R0, R, p2);
@@ -719,19 +736,15 @@ struct Krylov {
       axpby(nullptr, Tm, scal + 1, Z, R);                    // R = T - zeta Z
       colnorm(R, w->vpart.as<double>());
       op->timer.begin(kSmall, st);
-      k_small_err<<<1, 256, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
+      k_small_err<<<1, 256, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), w->hist.as<double>());
       op->timer.end(kSmall, st);
       gram<true>(R0, Z, p);
       small_launch(k_small_solve<double>, (const double2*)nullptr, (const double2*)p, 1, L, small(), ctl(), (int)kM, -1, -1.0,
                    (const double2*)nullptr, (int)kBeta, -1);  // beta = M^-1 (-R0^H Z)
       axpby(nullptr, P, scal + 1, V, Pt);                    // Pt = P - zeta V
       rowmm(Pt, sl(kBeta), nullptr, nullptr, R, P);          // P = R + Pt beta
-      if ((k + 1) % check_every == 0 || k + 1 == itermax) {
-        BDDA_TRY(poll(&done));
-        if (done) break;
-      }
-    }
-    if (!done) BDDA_TRY(poll(&done));
+      return BDDA_OK;
+    }));
     *iters = w->ctl_host->iter;
     *err = w->ctl_host->err;
     *status = w->ctl_host->status;
@@ -753,9 +766,7 @@ struct Krylov {
     BDDA_TRY(mvp(R, V));                                     // V = A R
     BDDA_CUDA(cudaMemcpyAsync(Wm, V, sizeof(C) * (size_t)n * L, cudaMemcpyDeviceToDevice, st));
     const int gv = vec_grid((size_t)n * L);
-    bool done = false;
-    int k = 0;
-    for (; k < itermax; ++k) {
+    BDDA_TRY(iterate(2, X, Bp, &R, false, itermax, [&](bool) -> int {
       gram<true>(R0, V, p);
       gram<true>(R0, R, p2);
       small_launch(k_small_solve<double>, (const double2*)p, (const double2*)p2, 1, L, small(), ctl(), 0, -1, 1.0,
@@ -774,7 +785,7 @@ struct Krylov {
       rowmm(Wm, sl(kNZetaI), Y, sl(kNIdent), R, Rn);         // Rn = R - zeta W - Y
       colnorm(Rn, w->vpart.as<double>());
       op->timer.begin(kSmall, st);
-      k_small_err<<<1, 256, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), tol, w->hist.as<double>(), k);
+      k_small_err<<<1, 256, 0, st>>>(w->vpart.as<double>(), gv, L, ctl(), w->hist.as<double>());
       op->timer.end(kSmall, st);
       BDDA_TRY(mvp(Rn, Wm));                                 // W = A Rnew
       gram<true>(R0, Rn, p);
@@ -783,12 +794,8 @@ struct Krylov {
       std::swap(R, Rn);
       rowmm(U, sl(kBeta), nullptr, nullptr, R, P);           // P = R + U gamma
       rowmm(Y, sl(kBeta), nullptr, nullptr, Wm, V);          // V = W + Y gamma
-      if ((k + 1) % check_every == 0 || k + 1 == itermax) {
-        BDDA_TRY(poll(&done));
-        if (done) break;
-      }
-    }
-    if (!done) BDDA_TRY(poll(&done));
+      return BDDA_OK;
+    }));
     // R/Rn swapping above only changes which buffer holds the residual; X is final.
     *iters = w->ctl_host->iter;
     *err = w->ctl_host->err;

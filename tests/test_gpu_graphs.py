@@ -1,6 +1,6 @@
-"""Poll cycles of block COCG-RQ as captured CUDA graphs (-m gpu).
+"""Poll cycles of the block Krylov solvers as captured CUDA graphs (-m gpu).
 
-Every COCG-RQ solve runs its first poll cycle launch by launch and each later
+Every solve runs its first poll cycle launch by launch and each later
 cycle (check_every iterations between two reads of the control block) as one
 launch of a captured graph; BDDA_NO_GRAPH=1 turns the graphs off.  A graph
 holds the same kernels in the same order with the same arguments, so a solve
@@ -32,21 +32,22 @@ def _solve(op, diag, B, opts, graphs):
         os.environ.pop("BDDA_NO_GRAPH", None)
 
 
+@pytest.mark.parametrize("solver", ["cocg_rq", "bicgstab", "bicggr"])
 @pytest.mark.parametrize("precision", [bdda.SOLVE_FP64, bdda.SOLVE_MIXED])
 @pytest.mark.parametrize("timing", [0, 2])
-def test_graph_cycles_match_direct_launches(precision, timing):
+def test_graph_cycles_match_direct_launches(solver, precision, timing):
     prob = bdda.make_problem(1024, 1.95 + 0.79j, seed=1, n_dirs=2)
     op = bdda.Operator(prob.n, prob.lf, prob.k)
     op.set_dipoles(prob.address)
     op.set_timing(timing)
-    opts = bdda.solve_opts("cocg_rq", jacobi=True, precision=precision, true_tol=1e-8, itermax=1000)
+    opts = bdda.solve_opts(solver, jacobi=True, precision=precision, true_tol=1e-8, itermax=1000)
     Xd, sd, kd = _solve(op, prob.diag, prob.B, opts, graphs=False)
     Xg, sg, kg = _solve(op, prob.diag, prob.B, opts, graphs=True)   # captures the cycle
     Xr, sr, kr = _solve(op, prob.diag, prob.B, opts, graphs=True)   # replays the cached one
     assert sd["iterations"] > 8  # at least one cycle ran as a graph
     for s in (sg, sr):
         assert s["iterations"] == sd["iterations"] and s["status"] == 0
-        assert s["true_res_max"] == sd["true_res_max"]
+        assert s["true_res_max"] == sd["true_res_max"] and s["mvps"] == sd["mvps"]
     assert np.array_equal(Xg, Xd) and np.array_equal(Xr, Xd)
     for name in kd:
         assert kg[name]["launches"] == kd[name]["launches"] == kr[name]["launches"], name
