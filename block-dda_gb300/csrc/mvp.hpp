@@ -174,10 +174,23 @@ struct TileArgs {
   const float2* twx;
   const float2* twy;
   int grid_y, ntask_y;  // persistent grid and tasks of passes B / D
+  int sms;              // multiprocessors of the device
   cudaStream_t st;
   const int* done;
 };
 enum TilePass { kTileA = 0, kTileB, kTileD, kTileE };
+
+// Fields per CTA of the x passes (A, E), an even number: a tile's fields are
+// split over groups of CTAs so that a launch has about two waves of five CTAs
+// per multiprocessor (one CTA per tile left most of the GPU idle: 301 tiles
+// at N=8192).  Returns the number of groups.
+inline int x_field_groups(int nfield, int ntiles, int sms, int* fpg) {
+  const int pairs = (nfield + 1) / 2;
+  const int want = (10 * sms + ntiles - 1) / ntiles;
+  const int groups = want < 1 ? 1 : (want < pairs ? want : pairs);
+  *fpg = 2 * ((pairs + groups - 1) / groups);
+  return (nfield + *fpg - 1) / *fpg;
+}
 
 // Strided pass `pass` for complex FP32 with the compile-time plan of its axis
 // (tplans.inc: Px for A / E; yplans.inc: Py for B / D); false (nothing launched) when the

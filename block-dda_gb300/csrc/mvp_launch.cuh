@@ -118,12 +118,14 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   const int ntask_y = nfield * g.Px * g.nzt;
   const int grid_y = std::min(ntask_y, num_sms() * 8);
   const tile::RtLine<C> lx{g.px}, ly{g.py};
+  int xfpg = 0;  // x passes: fields per CTA
+  const dim3 xgrid(g.ntiles, x_field_groups(nfield, g.ntiles, num_sms(), &xfpg));
   // Strided pass `pass` with the compile-time plan of its axis (complex FP32);
   // false when it was not launched that way.
   cudaError_t serr = cudaSuccess;
   auto static_tile = [&](int pass) -> bool {
     if constexpr (std::is_same<T, float>::value) {
-      const TileArgs a{&g, x, ldx, y, ldy, nfield, diag, jpre, t1, t2, p.twx, p.twy, grid_y, ntask_y, st, done};
+      const TileArgs a{&g, x, ldx, y, ldy, nfield, diag, jpre, t1, t2, p.twx, p.twy, grid_y, ntask_y, num_sms(), st, done};
       cudaError_t e = cudaSuccess;
       const bool ok = launch_tile_static(pass, a, &e);
       if (ok && e != cudaSuccess) serr = e;
@@ -136,8 +138,8 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   // A
   if (timer) timer->begin(kPassA + pbase, st);
   if (!static_tile(kTileA))
-    tile::k_pass_a<T><<<g.ntiles, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
-        x, ldx, nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, t1, done);
+    tile::k_pass_a<T><<<xgrid, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
+        x, ldx, nfield, xfpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, t1, done);
   if (timer) timer->end(kPassA + pbase, st);
   if (serr != cudaSuccess) return serr;
   // B
@@ -179,8 +181,8 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   // E
   if (timer) timer->begin(kPassE + pbase, st);
   if (!static_tile(kTileE))
-    tile::k_pass_e<T><<<g.ntiles, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
-        t1, nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, done);
+    tile::k_pass_e<T><<<xgrid, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
+        t1, nfield, xfpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, done);
   if (timer) timer->end(kPassE + pbase, st);
   if (serr != cudaSuccess) return serr;
   return cudaGetLastError();

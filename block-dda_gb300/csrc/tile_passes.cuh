@@ -58,7 +58,7 @@ constexpr int kRowStep = kTileThreads / kTZ;
 // One CTA per listed (y, z-tile): warp w owns z = z0 + w; loops over fields.
 template <typename T, class Line>
 __global__ void __launch_bounds__(kTileThreads)
-k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int fc, const int* __restrict__ occ,
+k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int fpg, int fc, const int* __restrict__ occ,
          const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, Line lay,
          const typename cplx<T>::type* __restrict__ twx, typename cplx<T>::type* __restrict__ t1, const int* done) {
   using C = typename cplx<T>::type;
@@ -79,8 +79,9 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int 
   }
   __syncthreads();
   const size_t rowstride = (size_t)ny * nzp;  // T1 stride between x rows
-  int l = 0, c = 0;
-  for (int f = 0; f < nfield; ++f) {
+  const int f0 = blockIdx.y * fpg, fend = min(nfield, f0 + fpg);  // this CTA's fields (f0 even)
+  int l = f0 / fc, c = f0 - (f0 / fc) * fc;
+  for (int f = f0; f < fend; ++f) {
     C* line = lines + ((f & 1) * kTZ + warp) * lw;
     const C* xc = x + (size_t)l * ldx + c;
     for (int xi = lane; xi < nx; xi += 32) {
@@ -244,7 +245,7 @@ k_pass_y2i(const float2* __restrict__ src, float2* __restrict__ dst, const unsig
 
 template <typename T, class Line>
 __global__ void __launch_bounds__(kTileThreads)
-k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, const int* __restrict__ occ,
+k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fpg, int fc, const int* __restrict__ occ,
          const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, Line lay,
          const typename cplx<T>::type* __restrict__ twx, const typename cplx<T>::type* __restrict__ x, int ldx,
          const typename cplx<T>::type* __restrict__ diag, const typename cplx<T>::type* __restrict__ jpre,
@@ -274,11 +275,12 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fc, cons
       cp_async<sizeof(C)>(lb + lay.addr(q), zval ? g : t1, zval);
     cp_commit();
   };
-  issue(0, 0);
-  int l = 0, c = 0;
-  for (int f = 0; f < nfield; ++f) {
+  const int f0 = blockIdx.y * fpg, fend = min(nfield, f0 + fpg);  // this CTA's fields (f0 even)
+  issue(f0, 0);
+  int l = f0 / fc, c = f0 - (f0 / fc) * fc;
+  for (int f = f0; f < fend; ++f) {
     const int buf = f & 1;
-    if (f + 1 < nfield) {
+    if (f + 1 < fend) {
       issue(f + 1, buf ^ 1);
       cp_wait<1>();
     } else {
@@ -317,7 +319,7 @@ __device__ __forceinline__ float2* x2i_block(float2* lines, int buf, int h, int 
 
 template <class P>
 __global__ void __launch_bounds__(kTileThreads)
-k_pass_a2i(const float2* __restrict__ x, int ldx, int nfield, int fc, const int* __restrict__ occ,
+k_pass_a2i(const float2* __restrict__ x, int ldx, int nfield, int fpg, int fc, const int* __restrict__ occ,
            const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, const float2* __restrict__ twx,
            float2* __restrict__ t1, const int* done) {
   if (skip(done)) return;
@@ -337,9 +339,10 @@ k_pass_a2i(const float2* __restrict__ x, int ldx, int nfield, int fc, const int*
   }
   __syncthreads();
   const size_t rowstride = (size_t)ny * nzp;
-  for (int f = 0, it = 0; f < nfield; f += 2, ++it) {
+  const int fend = min(nfield, (blockIdx.y + 1) * fpg);  // this CTA's fields: [blockIdx.y fpg, fend)
+  for (int f = blockIdx.y * fpg, it = 0; f < fend; f += 2, ++it) {
     const int buf = it & 1;
-    const int nh = f + 1 < nfield ? 2 : 1;
+    const int nh = f + 1 < fend ? 2 : 1;
     if (wh < nh) {
       const int fh = f + wh, l = fh / fc, c = fh - l * fc;
       const float2* xc = x + (size_t)l * ldx + c;
@@ -366,7 +369,7 @@ k_pass_a2i(const float2* __restrict__ x, int ldx, int nfield, int fc, const int*
 
 template <class P>
 __global__ void __launch_bounds__(kTileThreads)
-k_pass_e2i(const float2* __restrict__ t1, int nfield, int fc, const int* __restrict__ occ,
+k_pass_e2i(const float2* __restrict__ t1, int nfield, int fpg, int fc, const int* __restrict__ occ,
            const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, const float2* __restrict__ twx,
            const float2* __restrict__ x, int ldx, const float2* __restrict__ diag, const float2* __restrict__ jpre,
            float2* __restrict__ y, int ldy, const int* done) {
@@ -386,9 +389,10 @@ k_pass_e2i(const float2* __restrict__ t1, int nfield, int fc, const int* __restr
     const int xi = idx >> 3, w = idx & 7, z = z0 + w;
     socc[idx] = z < nz ? occ[((size_t)xi * ny + yy) * nz + z] : -1;
   }
+  const int f0 = blockIdx.y * fpg, fend = min(nfield, f0 + fpg);  // this CTA's fields
   // fill fields f, f + 1 (if any): column pair tp, rows tq + 64 k
   auto issue = [&](int f, int buf) {
-    const int nh = f + 1 < nfield ? 2 : 1;
+    const int nh = f + 1 < fend ? 2 : 1;
     for (int h = 0; h < nh; ++h) {
       const float2* g = t1 + (size_t)(f + h) * Px * rowstride + (size_t)yy * nzp + z0 + 2 * tp + (size_t)tq * rowstride;
       float2* lb = x2i_block<P>(lines, buf, h, tp);
@@ -397,11 +401,11 @@ k_pass_e2i(const float2* __restrict__ t1, int nfield, int fc, const int* __restr
     }
     cp_commit();
   };
-  issue(0, 0);
-  for (int f = 0, it = 0; f < nfield; f += 2, ++it) {
+  issue(f0, 0);
+  for (int f = f0, it = 0; f < fend; f += 2, ++it) {
     const int buf = it & 1;
-    const int nh = f + 1 < nfield ? 2 : 1;
-    if (f + 2 < nfield) {
+    const int nh = f + 1 < fend ? 2 : 1;
+    if (f + 2 < fend) {
       issue(f + 2, buf ^ 1);
       cp_wait<1>();
     } else {

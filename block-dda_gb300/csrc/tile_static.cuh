@@ -29,18 +29,20 @@ cudaError_t launch_x(int pass, const TileArgs& a) {
   // [2 buffers][8 columns][2 fields] lines + the occupancy of the tile
   auto smem_x2 = [](int nx) { return 4 * kTZ * P::LW * (int)sizeof(float2) + nx * kTZ * 4; };
   const int smem_ae = smem_x2(max_nx);
+  int fpg = 0;
+  const dim3 grid(g.ntiles, x_field_groups(a.nfield, g.ntiles, a.sms, &fpg));
   static std::once_flag oa, oe;
   static cudaError_t ca = cudaSuccess, ce = cudaSuccess;
   cudaError_t e = cudaSuccess;
   if (pass == kTileA) {
     if ((e = set_smem(tile::k_pass_a2i<P>, smem_ae, oa, ca)) != cudaSuccess) return e;
-    tile::k_pass_a2i<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
-        a.x, a.ldx, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.t1, a.done);
+    tile::k_pass_a2i<P><<<grid, kTileThreads, smem_x2(g.nx), a.st>>>(
+        a.x, a.ldx, a.nfield, fpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.t1, a.done);
   } else {
     if ((e = set_smem(tile::k_pass_e2i<P>, smem_ae, oe, ce)) != cudaSuccess) return e;
-    tile::k_pass_e2i<P><<<g.ntiles, kTileThreads, smem_x2(g.nx), a.st>>>(
-        a.t1, a.nfield, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y, a.ldy,
-        a.done);
+    tile::k_pass_e2i<P><<<grid, kTileThreads, smem_x2(g.nx), a.st>>>(
+        a.t1, a.nfield, fpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, a.twx, a.x, a.ldx, a.diag, a.jpre, a.y,
+        a.ldy, a.done);
   }
   return cudaGetLastError();
 }
