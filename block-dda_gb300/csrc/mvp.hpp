@@ -173,12 +173,19 @@ struct TileArgs {
   float2* t2;
   const float2* twx;
   const float2* twy;
-  int grid_y, ntask_y;  // persistent grid and tasks of passes B / D
   int sms;              // multiprocessors of the device
   cudaStream_t st;
   const int* done;
 };
 enum TilePass { kTileA = 0, kTileB, kTileD, kTileE };
+
+// Grid of the y passes (B, D), whose CTAs take tasks (field, x, z tile) in a
+// fixed stride: four waves of the CTAs resident per SM.  Measured on the
+// column-pair passes (N=16384 / 8192, tasks of uneven cost: empty rows are
+// skipped): one exact wave 0.244 / 0.146 ms (forward), two 0.239 / 0.138,
+// four 0.233 / 0.135; the earlier fixed 8 CTAs per SM (1.1-1.6 waves) 0.239 /
+// 0.159.
+constexpr int kYWaves = 4;
 
 // Fields per CTA of the x passes (A, E), an even number: a tile's fields are
 // split over groups of CTAs so that a launch has about two waves of five CTAs

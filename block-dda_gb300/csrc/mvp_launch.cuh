@@ -116,7 +116,12 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   const int pbase = sizeof(T) == sizeof(double) ? (kPassA64 - kPassA) : 0;
   if (g.ntiles == 0) return cudaSuccess;  // no dipoles
   const int ntask_y = nfield * g.Px * g.nzt;
-  const int grid_y = std::min(ntask_y, num_sms() * 8);
+  // runtime-plan y passes: kYWaves waves of the CTAs resident per SM
+  auto grid_y = [&](auto kernel, int smem) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kTileThreads, smem) != cudaSuccess || nb < 1) nb = 1;
+    return std::min(ntask_y, kYWaves * nb * num_sms());
+  };
   const tile::RtLine<C> lx{g.px}, ly{g.py};
   int xfpg = 0;  // x passes: fields per CTA
   const dim3 xgrid(g.ntiles, x_field_groups(nfield, g.ntiles, num_sms(), &xfpg));
@@ -125,7 +130,7 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   cudaError_t serr = cudaSuccess;
   auto static_tile = [&](int pass) -> bool {
     if constexpr (std::is_same<T, float>::value) {
-      const TileArgs a{&g, x, ldx, y, ldy, nfield, diag, jpre, t1, t2, p.twx, p.twy, grid_y, ntask_y, num_sms(), st, done};
+      const TileArgs a{&g, x, ldx, y, ldy, nfield, diag, jpre, t1, t2, p.twx, p.twy, num_sms(), st, done};
       cudaError_t e = cudaSuccess;
       const bool ok = launch_tile_static(pass, a, &e);
       if (ok && e != cudaSuccess) serr = e;
@@ -145,7 +150,8 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   // B
   if (timer) timer->begin(kPassB + pbase, st);
   if (!static_tile(kTileB))
-    tile::k_pass_y<T, false><<<grid_y, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
+    tile::k_pass_y<T, false><<<grid_y(tile::k_pass_y<T, false, tile::RtLine<C>>, tile::smem_tile<T>(plan_lw<C>(g.py), 0)),
+                               kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
         t1, t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, done);
   if (timer) timer->end(kPassB + pbase, st);
   if (serr != cudaSuccess) return serr;
@@ -174,7 +180,8 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   // D
   if (timer) timer->begin(kPassD + pbase, st);
   if (!static_tile(kTileD))
-    tile::k_pass_y<T, true><<<grid_y, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
+    tile::k_pass_y<T, true><<<grid_y(tile::k_pass_y<T, true, tile::RtLine<C>>, tile::smem_tile<T>(plan_lw<C>(g.py), 0)),
+                              kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
         t2, t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, done);
   if (timer) timer->end(kPassD + pbase, st);
   if (serr != cudaSuccess) return serr;

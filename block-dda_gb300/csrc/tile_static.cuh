@@ -54,18 +54,28 @@ cudaError_t launch_y(int pass, const TileArgs& a) {
   const MvpGeom& g = *a.g;
   const int smem_bd = 2 * tile::kTZ2 * P::LW * (int)sizeof(float2);  // 16 columns per task
   const int ntask2 = a.nfield * g.Px * ((g.nz + tile::kTZ2 - 1) / tile::kTZ2);
-  const int grid2 = std::min(ntask2, a.grid_y);
   static std::once_flag ob, od;
   static cudaError_t cb = cudaSuccess, cd = cudaSuccess;
+  static int resident[2] = {0, 0};  // CTAs of each kernel that fit on one SM
   cudaError_t e = cudaSuccess;
+  // The grid is a whole number of waves of the CTAs resident at once (see
+  // kYWaves): a fixed 8 per SM left a partial last wave (1.1-1.6 waves).
+  auto grid_of = [&](auto kernel, int inv) {
+    if (resident[inv] == 0) {
+      int nb = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kTileThreads, smem_bd) != cudaSuccess || nb < 1) nb = 1;
+      resident[inv] = nb;
+    }
+    return std::min(ntask2, kYWaves * resident[inv] * a.sms);
+  };
   if (pass == kTileB) {
     if ((e = set_smem(tile::k_pass_y2i<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
-    tile::k_pass_y2i<false, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
-                                                                      ntask2, a.twy, a.done);
+    tile::k_pass_y2i<false, P><<<grid_of(tile::k_pass_y2i<false, P>, 0), kTileThreads, smem_bd, a.st>>>(
+        a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask2, a.twy, a.done);
   } else {
     if ((e = set_smem(tile::k_pass_y2i<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
-    tile::k_pass_y2i<true, P><<<grid2, kTileThreads, smem_bd, a.st>>>(a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt,
-                                                                     ntask2, a.twy, a.done);
+    tile::k_pass_y2i<true, P><<<grid_of(tile::k_pass_y2i<true, P>, 1), kTileThreads, smem_bd, a.st>>>(
+        a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask2, a.twy, a.done);
   }
   return cudaGetLastError();
 }
