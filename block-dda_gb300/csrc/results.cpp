@@ -4,7 +4,7 @@
 // particle or core/coat properties, Csca = Cext - Cabs, SSA, MAC),
 // Basic_Stats (Basic_Stats.hpp: mean, sample standard deviation from the mean
 // of squares), the section writer operator<< (Result_manager.cpp:178-245) and
-// the volume-equivalent Mie MAC line the driver appends
+// the volume-equivalent Mie MAC line the reference's main program appends
 // (Result_manager.cpp:137-176, block_DDA_main.cpp:169-183).  Numbers go
 // through std::ostream with its default formatting, as the reference's do.
 #include <algorithm>

@@ -369,7 +369,7 @@ typedef struct {
   const double* cabs;
   int f, nx, ny, nz, num_element_occupy;
   double solver_time;                  /* seconds */
-  int append_mac_mie;                  /* add the volume-equivalent Mie MAC line the driver writes */
+  int append_mac_mie;                  /* add the volume-equivalent Mie MAC line (block_DDA_main.cpp:169-183) */
 } bdda_result_record;
 
 /*

@@ -2,7 +2,7 @@
 
 Nothing in the product imports this package.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py`` (its ``cpu_baseline`` leg and the
-``--impl reference`` arm) use it, and there only as the checker or as the timed
+``--impl reference`` arm) use it, and there only to check results or as the timed
 CPU restatement of the reference algorithm, never as the thing measured on the
 GPU.
 
