@@ -583,12 +583,21 @@ struct Krylov {
     return BDDA_OK;
   }
 
-  // Poll cycles run as graphs on a stream that can be captured, with an even
-  // cycle length (Q and Qn are back in place after it); BDDA_NO_GRAPH turns
-  // them off (diagnostics).
+  // Poll cycles run as graphs with an even cycle length (Q and Qn are back in
+  // place after it), on a non-blocking stream: while a blocking stream is
+  // captured, work another thread puts on the legacy default stream would
+  // fail.  The operators' own streams are non-blocking.  BDDA_NO_GRAPH turns
+  // the graphs off (diagnostics).
   bool graphs_allowed() const {
-    return op->graphs && check_every >= 2 && check_every % 2 == 0 && st != nullptr && st != cudaStreamLegacy &&
-           std::getenv("BDDA_NO_GRAPH") == nullptr;
+    if (!op->graphs || check_every < 2 || check_every % 2 != 0 || st == nullptr || st == cudaStreamLegacy ||
+        st == cudaStreamPerThread || std::getenv("BDDA_NO_GRAPH") != nullptr)
+      return false;
+    unsigned int flags = 0;
+    if (cudaStreamGetFlags(st, &flags) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    return (flags & cudaStreamNonBlocking) != 0;
   }
 
   // Launches one poll cycle as a graph: `cycle` issues its check_every
