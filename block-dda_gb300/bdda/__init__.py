@@ -33,7 +33,7 @@ EXPORTS = [
     "bdda_op_create", "bdda_op_destroy", "bdda_op_set_dipoles", "bdda_op_info", "bdda_mbt_fft_mvp",
     "bdda_op_mvp_device", "bdda_solve_opts_default", "bdda_solve_device", "bdda_solve", "bdda_qr_reduced",
     "bdda_mie_a1b1", "bdda_aggregate", "bdda_incident_fields", "bdda_cross_sections", "bdda_op_set_timing",
-    "bdda_op_kernel_stats", "bdda_last_error", "bdda_op_mvp_bytes", "bdda_host_fft_line",
+    "bdda_op_set_graphs", "bdda_op_kernel_stats", "bdda_last_error", "bdda_op_mvp_bytes", "bdda_host_fft_line",
     "bdda_op_mvp_device_noalloc", "bdda_request_footprint", "bdda_server_create", "bdda_server_submit",
     "bdda_server_wait", "bdda_server_stats", "bdda_server_destroy", "bdda_batch_solve",
     "bdda_incident_fields_eh", "bdda_cross_sections_eh", "bdda_read_target_file", "bdda_shape_target",
@@ -167,6 +167,7 @@ def lib(build_if_missing: bool = False):
     L.bdda_format_result.argtypes = [ct.POINTER(ResultRecord), ct.c_char_p, ct.c_int, ip]
     L.bdda_op_mvp_bytes.argtypes = [vp, ct.c_int, ct.c_int, ct.c_int, ct.c_int, dp]
     L.bdda_op_set_timing.argtypes = [vp, ct.c_int]
+    L.bdda_op_set_graphs.argtypes = [vp, ct.c_int]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
     L.bdda_last_error.restype = ct.c_char_p
     L.bdda_request_footprint.argtypes = [ip, ct.c_int, ct.c_int, ct.c_int]
@@ -285,6 +286,10 @@ class Operator:
     def set_timing(self, on=True):
         """True / 1: time every kernel class; 2: the fused z pass only; False / 0: off."""
         _check(lib().bdda_op_set_timing(self._h, int(on) if not isinstance(on, bool) else (1 if on else 0)))
+
+    def set_graphs(self, on=True):
+        """Captured CUDA graphs for the solvers' poll cycles (default on); off: launch by launch."""
+        _check(lib().bdda_op_set_graphs(self._h, 1 if on else 0))
 
     def kernel_stats(self, reset=False):
         n = len(KERNEL_NAMES)

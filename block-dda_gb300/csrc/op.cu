@@ -175,10 +175,6 @@ template int op_block_mvp<dfl>(Op*, const Occupancy&, const dfc*, int, dfc*, int
 
 }  // namespace bdda
 
-void bdda::op_set_graphs(bdda_op* op, bool on) {
-  if (op) op->graphs = on;
-}
-
 using namespace bdda;
 
 // Green spectra of the operator's box, spacing and f at wavenumber k (FP64
@@ -381,6 +377,13 @@ int bdda_op_mvp_bytes(const bdda_op* op, int prec, int L, int with_diag, int wit
   bytes[2] = 2.0 * t2 + ghat;
   bytes[3] = t2 + t1;
   bytes[4] = t1 + occ + vec + (with_diag ? vec + op->f * nocc * s : 0.0) + (with_jpre ? op->f * nocc * s : 0.0);
+  return BDDA_OK;
+}
+
+int bdda_op_set_graphs(bdda_op* op, int on) {
+  if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(op->mu);
+  op->graphs = on != 0;
   return BDDA_OK;
 }
 

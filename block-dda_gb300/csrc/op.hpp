@@ -97,7 +97,7 @@ struct Op {
   KernelTimer timer;
   std::mutex mu;
   std::shared_ptr<SolverWork> solver;   // cached Krylov workspace (solver.cu)
-  bool graphs = true;  // COCG-RQ poll cycles as captured graphs (off under the request scheduler)
+  bool graphs = true;  // solvers' poll cycles as captured graphs (bdda_op_set_graphs)
 
   // signature of every buffer a block MVP's kernels are launched with
   unsigned long long buffer_sig() const {
@@ -169,8 +169,3 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
 
 // The opaque handle of the C ABI.
 struct bdda_op : public bdda::Op {};
-
-namespace bdda {
-// COCG-RQ poll cycles as captured graphs for solves on op (default on).
-void op_set_graphs(bdda_op* op, bool on);
-}  // namespace bdda

@@ -31,10 +31,6 @@
 #include "../../include/bdda.h"
 
 namespace bdda {
-void op_set_graphs(bdda_op* op, bool on);  // op.cu: COCG-RQ poll cycles as captured graphs
-}
-
-namespace bdda {
 void set_error(const std::string& msg);
 }
 
@@ -124,7 +120,7 @@ struct bdda_server {
     // concurrent requests keep the GPU busy between one stream's launches, so
     // captured poll cycles save nothing here and cost their capture (batched
     // workload: 245 vs 251 RHS-solves/s with and without them)
-    if (rc == BDDA_OK) bdda::op_set_graphs(op, false);
+    if (rc == BDDA_OK) rc = bdda_op_set_graphs(op, 0);
     if (rc == BDDA_OK) rc = bdda_op_set_dipoles(op, r.address, r.nocc);
     bdda_solve_stats st{};
     if (rc == BDDA_OK) rc = bdda_solve(op, &opts, r.diag, r.B, 3 * r.nocc, r.X, 3 * r.nocc, r.L, &st);

@@ -444,6 +444,15 @@ int bdda_op_mvp_bytes(const bdda_op* op, int prec, int L, int with_diag, int wit
  * MVP, for timing a whole solve with little overhead). */
 int bdda_op_set_timing(bdda_op* op, int enable);
 
+/* Block Krylov solves on op run every poll cycle after the first (the
+ * check_every iterations between two reads of the control block) as one
+ * launch of a captured CUDA graph (on = 1, the default) or launch by launch
+ * (on = 0; results are bitwise the same).  Graphs pay where one solve's
+ * launches leave the GPU idle (small systems); with many solves in flight on
+ * other streams they only add their capture, and the request scheduler
+ * (bdda_batch_solve, bdda_server_*) turns them off for its operators. */
+int bdda_op_set_graphs(bdda_op* op, int on);
+
 /*
  * Per-kernel totals since the last reset: ms[i], launches[i] for
  * i = 0..n-1 in the order passA..passE of the complex FP32 MVP, passA..passE

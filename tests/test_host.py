@@ -41,6 +41,8 @@ def test_errors_are_reported_not_fatal(lib):
     assert b"f value" in lib.bdda_last_error()
     n = (ct.c_int * 3)(4, 300, 4)
     assert lib.bdda_op_create(ct.byref(h), n, 3, 1.0, 1.0, 0.0, 1) == bdda.ERR_INVALID
+    assert lib.bdda_op_set_graphs(None, 1) == bdda.ERR_INVALID
+    assert b"null operator" in lib.bdda_last_error()
 
 
 def _smooth(v):
