@@ -6,7 +6,8 @@ launch of a captured graph; BDDA_NO_GRAPH=1 turns the graphs off.  A graph
 holds the same kernels in the same order with the same arguments, so a solve
 gives bitwise the same solution, iteration count and per-class launch counts
 either way, and the timed fused z pass keeps its CUDA-event time inside the
-graph.  A cached graph is not replayed after the operator's dipoles changed.
+graph.  A cached graph is not replayed after the operator's dipoles changed,
+and bdda_op_set_graphs switches the graphs per operator.
 """
 import os
 
@@ -81,3 +82,22 @@ def test_graph_not_replayed_after_dipoles_change():
     gh, P = mbt.green_hat(prob.n, 3, prob.lf, prob.k)
     amul = lambda S: mbt.block_mvp(prob.n, 3, gh, P, other, prob.diag, S)  # noqa: E731
     assert np.all(krylov.true_residual(amul, prob.B, Xu) < 2e-8)
+
+
+def test_set_graphs_switch():
+    """bdda_op_set_graphs(op, 0) runs the same solve launch by launch: bitwise
+    the same solution and the same launch counts as with the graphs."""
+    prob = bdda.make_problem(1024, 1.95 + 0.79j, seed=2, n_dirs=2)
+    op = bdda.Operator(prob.n, prob.lf, prob.k)
+    op.set_dipoles(prob.address)
+    opts = bdda.solve_opts("cocg_rq", jacobi=True, precision=bdda.SOLVE_MIXED, true_tol=1e-8, itermax=1000)
+    out = {}
+    for on in (False, True, False):
+        op.set_graphs(on)
+        op.kernel_stats(reset=True)
+        X, st = bdda.solve(op, prob.diag, prob.B, opts, allow_not_converged=False)
+        out.setdefault(on, []).append((X, st, op.kernel_stats()))
+    Xd, sd, kd = out[False][0]
+    for X, st, k in out[True] + out[False][1:]:
+        assert np.array_equal(X, Xd) and st["iterations"] == sd["iterations"] and st["mvps"] == sd["mvps"]
+        assert all(k[name]["launches"] == kd[name]["launches"] for name in kd)
