@@ -587,6 +587,26 @@ def make_problem(nocc, m, wl0=0.55, kf=1.0, Df=2.8, seed=1, n_dirs=1, mkd=0.5):
     return Problem(n=n, lf=d, address=addr, k=k, alpha=alpha, diag=diag, B=B)
 
 
+def target_problem(n, lf, address, vol, m, wl0=0.55, seed=1, n_dirs=1, mkd=0.5):
+    """Problem on a target read from a file (``read_target_file``): the file's
+    lattice spacing ``lf`` and site volume ``vol`` (same length unit, e.g. the
+    monomer radius r_pp of the reference's aggregates) are scaled so that
+    |m| k d = mkd; every site is one dipole of the volume-equivalent radius of
+    ``vol`` (``Target.cpp:13-19``) and one material."""
+    k = 2 * np.pi / wl0
+    m = complex(m)
+    d = mkd / (abs(m) * k)
+    scale = d / float(lf)
+    r_eq = (3.0 * float(vol) / (4.0 * np.pi)) ** (1.0 / 3.0) * scale
+    address = np.ascontiguousarray(address, dtype=np.int32)
+    alpha0 = polarizability(wl0, r_eq, m * m, k)
+    alpha = np.full(address.size, alpha0, dtype=np.complex128)
+    u, e = directions(n_dirs, seed + 1000)
+    B = incident_fields(n, d, address, k, u, e)
+    return Problem(n=tuple(int(v) for v in n), lf=d, address=address, k=k, alpha=alpha,
+                   diag=np.repeat(1.0 / alpha, 3), B=B)
+
+
 # ---------------------------------------------------------------------------
 # batched solves and the request server
 # ---------------------------------------------------------------------------

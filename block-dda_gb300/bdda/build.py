@@ -3,7 +3,10 @@
 Each translation unit under ``block-dda_gb300/csrc`` is compiled in parallel
 with ``nvcc -gencode arch=compute_103a,code=sm_103a`` and linked into
 ``block-dda_gb300/_lib/libbdda.so``.  Objects are rebuilt only when a source or
-header is newer than the library.
+header is newer than the library.  Host code is compiled with
+``-ffp-contract=off``: an aarch64 host compiler would otherwise fuse
+multiply-adds that an x86-64 one keeps apart, and the seeded generators
+(aggregates, directions) must give the same targets on both machines.
 """
 from __future__ import annotations
 
@@ -47,7 +50,7 @@ def up_to_date() -> bool:
 
 def _compile(nvcc, src, obj, verbose_ptxas):
     cmd = [nvcc, "-c", src, "-o", obj, "-O3", "-std=c++17", "-lineinfo", *ARCH,
-           "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-I", os.path.join(REPO, "include"),
+           "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(REPO, "include"),
            "--expt-relaxed-constexpr"]
     if verbose_ptxas and src.endswith(".cu"):
         cmd += ["-Xptxas", "-v"]

@@ -6,13 +6,17 @@
 // own pool or arena, and latency-critical serving loops that must never enter
 // the CUDA allocator (cudaMalloc/cudaFree can synchronise the device).  This
 // variant runs the same five kernels with their two workspace buffers carved
-// out of one file-scope __device__ array of kNoAllocScratchBytes.  Every GPU
-// that loads this library reserves that array until the process exits.
+// out of one file-scope __device__ array of kNoAllocScratchBytes.  A GPU
+// reserves that array when this file's device code is loaded on it -- under
+// CUDA's default lazy module loading, at the first call of the entry point
+// there -- and keeps it until the process exits.  Only complex FP64 and FP32
+// are offered (the double-float MVP is not).
 //
 // The array's host-side name is only a stand-in for the device symbol, so the
 // device address is looked up once per device with cudaGetSymbolAddress, with
-// that device current, the first time the entry point runs on it.  Make that
-// first call before any stream capture begins.  All calls share the one array
+// that device current, the first time the entry point runs on it, and kept for
+// the life of the process (a cudaDeviceReset after that is not supported).
+// Make that first call at set-up, before any stream capture begins.  All calls share the one array
 // and it keeps the last call's contents: calls whose work overlaps on the GPU
 // (different streams, or different operators at the same time) race on it and
 // must be ordered by the caller.  Nothing needs clearing between calls: every

@@ -114,13 +114,19 @@ int bdda_op_mvp_device(bdda_op* op, int prec, const void* x, int ldx, void* y, i
  * reference: it exists for callers that cannot let a library call cudaMalloc
  * -- frameworks that own all device memory through their own pool, and
  * serving loops that must never enter the CUDA allocator (which can
- * synchronise the device).  Same arguments and result as bdda_op_mvp_device,
- * but the two FFT workspaces come from a fixed 64 MiB __device__ array that
- * every GPU loading the library reserves until exit; boxes and nrhs whose
- * workspace exceeds it are rejected with BDDA_ERR_INVALID and a message.
- * The first call on a device looks up the array's device address (make it
- * before any stream capture).  All calls share the array: calls that overlap
- * on the GPU race and must be ordered by the caller.
+ * synchronise the device).  Same arguments and result as bdda_op_mvp_device
+ * for prec BDDA_PREC_FP64 and BDDA_PREC_FP32 (BDDA_PREC_DF64 is rejected with
+ * BDDA_ERR_INVALID), but the two FFT workspaces come from a fixed 64 MiB
+ * __device__ array; boxes and nrhs whose workspace exceeds it are rejected with
+ * BDDA_ERR_INVALID and a message.  The array is reserved on a device when the
+ * library's code holding it is loaded there -- with CUDA's default lazy module
+ * loading, at the first call of this entry point on that device -- and kept
+ * until the process exits; that first call also looks up the array's device
+ * address.  Make the first call at set-up, before any stream capture and
+ * while the device still has 64 MiB free.  The address is kept for the life
+ * of the process: a cudaDeviceReset after the first call is not supported.
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * ordered by the caller.
  */
 int bdda_op_mvp_device_noalloc(bdda_op* op, int prec, const void* x, int ldx, void* y, int ldy, int L,
                                const void* diag, const void* jpre, void* stream);

@@ -83,11 +83,20 @@ class MbtCpu:
     def mvp_cuboid(self, p_hat):
         z = np.zeros(self.M, dtype=np.complex128)
         z[self.pmap] = p_hat
-        q = sfft.ifft(self.au_til * sfft.fft(z, workers=1), workers=1)
-        return q[self.rmap]
+        z = sfft.fft(z, workers=1, overwrite_x=True)
+        z *= self.au_til
+        z = sfft.ifft(z, workers=1, overwrite_x=True)
+        return z[self.rmap]
 
-    def block_mvp(self, S):
-        """AS = DIAG o S + gather(MBT_fft_mvp(scatter(S))) over all columns, threaded over columns."""
+    def bytes_per_column(self):
+        """Host memory one column of ``block_mvp`` holds at its peak: the padded
+        vector, the transform's output and its working copy (16-byte complex)."""
+        return 3 * self.M * 16 + 2 * int(np.prod(self.n)) * 3 * 16
+
+    def block_mvp(self, S, cols=None):
+        """AS = DIAG o S + gather(MBT_fft_mvp(scatter(S))) over the columns
+        ``cols`` (all by default), threaded over columns; other columns of
+        the result are left unset."""
         ncub = int(np.prod(self.n)) * 3
         out = np.empty_like(S)
 
@@ -96,6 +105,7 @@ class MbtCpu:
             p[self.rows] = S[:, l]
             out[:, l] = self.diag * S[:, l] + self.mvp_cuboid(p)[self.rows]
 
+        cols = range(S.shape[1]) if cols is None else cols
         with ThreadPoolExecutor(max_workers=self.threads) as ex:
-            list(ex.map(col, range(S.shape[1])))
+            list(ex.map(col, cols))
         return out

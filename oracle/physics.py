@@ -75,6 +75,54 @@ def reference_incident_waves(n_inc: int, eper_m=1.0 + 0j, mper_m=1.0 + 0j):
 
 
 # --------------------------------------------------------------------------
+# Mie coefficients of the volume-equivalent sphere (polarizability)
+# --------------------------------------------------------------------------
+
+def mie_a1b1(wl0, r_p, eper_p, mper_p=1.0 + 0j, eper_m=1.0 + 0j, mper_m=1.0 + 0j):
+    """First Mie coefficients (a_1, b_1) as ``gmie/gmie_coeff.cpp:33-97`` computes
+    them (BH83 eqs. 4.88 with the Kerker et al. 1983 permeability factors).
+
+    D_n(y) by downward recurrence from 0 at nmx (``:43-46``); psi_n(x) from the
+    downward ratio recurrence R_n = psi_n / psi_{n-1} started at x / (2 nmx + 1)
+    with psi_0 = R_0 cos x (``:51-59``); chi_n(x) upward from chi_0 = -cos x,
+    chi_1 = chi_0 / x - sin x (``:68-72``); xi = psi + i chi.
+    """
+    k0 = 2.0 * math.pi / wl0
+    m_m = np.sqrt(complex(eper_m) * complex(mper_m))
+    m_p = np.sqrt(complex(eper_p) * complex(mper_p))
+    x = m_m * k0 * r_p
+    m_r = m_p / m_m
+    y = x * m_r
+    nstop = int(math.floor(abs(x) + 4.0 * np.cbrt(abs(x)) + 2.0))
+    nmx = max(nstop, int(math.ceil(abs(y)))) + 15
+    dd = [0j] * nmx
+    for n in range(nmx - 1, 1, -1):
+        dd[n - 2] = n / y - 1.0 / (dd[n - 1] + n / y)
+    rr = [0j] * (nmx + 1)
+    rr[nmx] = x / (2.0 * nmx + 1.0)
+    for n in range(nmx - 1, -1, -1):
+        rr[n] = 1.0 / ((2.0 * n + 1.0) / x - rr[n + 1])
+    psi0 = rr[0] * np.cos(x)
+    psi1 = rr[1] * psi0
+    chi0 = -np.cos(x)
+    chi1 = (1.0 / x) * chi0 - np.sin(x)
+    xi0, xi1 = psi0 + 1j * chi0, psi1 + 1j * chi1
+    mp, mm = complex(mper_p), complex(mper_m)
+    fa = mp / (mm * m_r) * dd[0] + 1.0 / x
+    fb = mm * m_r / mp * dd[0] + 1.0 / x
+    a1 = (fa * psi1 - psi0) / (fa * xi1 - xi0)
+    b1 = (fb * psi1 - psi0) / (fb * xi1 - xi0)
+    return complex(a1), complex(b1)
+
+
+def polarizability(wl0, r_p, eper_p, k, mper_p=1.0 + 0j):
+    """alpha_E = 3 i a_1 / (2 k^3) of a dipole of volume-equivalent radius r_p in
+    vacuum (``Target_manager.cpp:232``)."""
+    a1, _ = mie_a1b1(wl0, r_p, eper_p, mper_p)
+    return 3j * a1 / (2.0 * k ** 3)
+
+
+# --------------------------------------------------------------------------
 # targets
 # --------------------------------------------------------------------------
 

@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures under tests/golden/.
 
-Run in a container where the nmoteki/block-DDA sources are mounted (default
-``/root/reference``, or ``--ref PATH``).  It reads the reference's own test
+Run in a container where the nmoteki/block-DDA sources are mounted, with
+``--ref PATH`` naming that source tree (required).  It reads the reference's own test
 program, data files and recorded results as text, builds the reference's Mie
 code with ``oracle/Makefile`` and writes small JSON fixtures.  The GPU machines
 never run this; they only read the JSON it wrote.
@@ -24,6 +24,11 @@ Fixtures:
   BiCGSTAB-Jacobi runs of ``DDA_result_BC_rpp20nm.dat`` for the N8..N64
   targets at eleven wavelengths, their target files, and the oracle's
   reproduction of each.
+* ``target_N65536.npz`` -- the reference's largest aggregate,
+  ``DDA_target_0_agg_N65536_kf1.0_Df2.8.out`` (box 137 x 135 x 176, 60,077
+  monomer sites): box, lattice spacing, site volume and material, and the
+  addresses in file order, delta-encoded (``address = cumsum(address_delta)``).
+  The benchmark's ``--target-file`` workload reads it.
 * ``materials_ref.json`` -- the four material tables and the eper the recorded
   runs used at each wavelength (interpolation pins).
 """
@@ -134,6 +139,16 @@ def target_fixture(ref, name, scale):
     n, lf, addr, vol, mat = physics.read_target_file(os.path.join(ref, name), 1.0)
     return {"source": name, "n": list(n), "lf": lf, "address": addr.tolist(),
             "vol": vol.tolist(), "material": mat.tolist(), "scale_factor_used_in_run": scale}
+
+
+def target_npz(ref, name, path):
+    n, lf, addr, vol, mat = physics.read_target_file(os.path.join(ref, name), 1.0)
+    uv, um = np.unique(vol), np.unique(mat)
+    if uv.size != 1 or um.size != 1:
+        raise ValueError(f"{name}: expected one site volume and one material")
+    delta = np.diff(addr.astype(np.int64), prepend=0).astype(np.int32)
+    np.savez_compressed(path, source=np.array(name), n=np.array(n, dtype=np.int32), lf=np.float64(lf),
+                        vol=np.float64(uv[0]), material=np.int32(um[0]), address_delta=delta)
 
 
 def result_dat(ref, lib):
@@ -253,7 +268,7 @@ def materials_ref(ref):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="nmoteki/block-DDA source tree")
     ap.add_argument("--only", nargs="*", help="write only these fixture files")
     args = ap.parse_args()
     ref = args.ref
@@ -268,6 +283,11 @@ def main():
         "result_f6_BC_rpp20nm.json": lambda: result_f6(ref, lib),
         "materials_ref.json": lambda: materials_ref(ref),
     }
+    npz = {"target_N65536.npz": "DDA_target_0_agg_N65536_kf1.0_Df2.8.out"}
+    for name, src in npz.items():
+        if not args.only or name in args.only:
+            target_npz(ref, src, os.path.join(HERE, name))
+            print("wrote", name)
     out = {name: make() for name, make in makers.items() if not args.only or name in args.only}
     for name, obj in out.items():
         with open(os.path.join(HERE, name), "w") as fh:

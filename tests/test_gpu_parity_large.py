@@ -1,0 +1,80 @@
+"""Parity at the benchmark's own configurations (-m gpu).
+
+The large single-target workloads are beyond the numpy oracle's reach, so two
+independent checks stand in for it:
+
+* the mixed-precision solve (complex FP32 Krylov + FFT-MVP inside FP64
+  refinement) against the plain FP64 solve of the same problem: Cext, Cabs and
+  Csca of every incident wave within 1e-6 relative, the polarisation within
+  1e-6 relative L2;
+* the true residual ||b - (DIAG o x + A_off x)|| / ||b|| of both solutions,
+  recomputed with the second oracle (``oracle.torch3d``: the same Green
+  tensor embedded and transformed with torch.fft in complex128, sharing no
+  code with the CUDA kernels), <= 2e-8 for every column (the solves stop at
+  1e-8 with their own residual MVP).
+
+Configurations: N=16384, nrhs=16, m=2.3+0.6i; N=65536, nrhs=32 with m=1.78 and
+m=1.33+1e-8i (seeded aggregates), and the reference's own N65536 aggregate file
+(box 137 x 135 x 176, padded 288 x 270 x 360) at m=1.78.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import bdda
+from conftest import GOLDEN
+from oracle import torch3d
+
+pytestmark = pytest.mark.gpu
+
+XS_TOL = 1e-6      # cross sections and polarisation, mixed vs FP64
+RES_TOL = 2e-8     # independent true residual
+
+
+def _target_file_problem(m, nrhs):
+    d = np.load(os.path.join(GOLDEN, "target_N65536.npz"))
+    addr = np.cumsum(d["address_delta"].astype(np.int64)).astype(np.int32)
+    return bdda.target_problem(tuple(int(v) for v in d["n"]), float(d["lf"]), addr, float(d["vol"]), m,
+                               wl0=0.55, seed=1, n_dirs=nrhs // 2)
+
+
+CASES = {
+    "N16384_L16_m2.3+0.6i": lambda: bdda.make_problem(16384, 2.3 + 0.6j, seed=1, n_dirs=8),
+    "N65536_L32_m1.78": lambda: bdda.make_problem(65536, 1.78, seed=1, n_dirs=16),
+    "N65536_L32_m1.33+1e-8i": lambda: bdda.make_problem(65536, 1.33 + 1e-8j, seed=1, n_dirs=16),
+    "file_N65536_L32_m1.78": lambda: _target_file_problem(1.78, 32),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_mixed_vs_fp64_and_independent_residual(case):
+    import torch
+    prob = CASES[case]()
+    op = bdda.Operator(prob.n, prob.lf, prob.k)
+    op.set_dipoles(prob.address)
+    o32 = bdda.solve_opts("cocg_rq", jacobi=True, precision=bdda.SOLVE_MIXED, true_tol=1e-8, itermax=3000)
+    o64 = bdda.solve_opts("cocg_rq", jacobi=True, precision=bdda.SOLVE_FP64, true_tol=1e-8, itermax=3000)
+    X32, s32 = bdda.solve(op, prob.diag, prob.B, o32, allow_not_converged=False)
+    X64, s64 = bdda.solve(op, prob.diag, prob.B, o64, allow_not_converged=False)
+    op.close()
+    torch.cuda.synchronize()
+    assert s32["true_res_max"] <= 1e-8 and s64["true_res_max"] <= 1e-8
+    c32 = bdda.cross_sections(prob.k, prob.alpha[0], prob.B, X32)
+    c64 = bdda.cross_sections(prob.k, prob.alpha[0], prob.B, X64)
+    for name, a, b in zip(("Cext", "Cabs", "Csca"), c32, c64):
+        if name == "Cabs" and np.max(np.abs(b)) < 1e-9 * np.max(np.abs(c64[0])):
+            # real m: the absorption weight Im(conj(1/alpha)) - 2k^3/3 vanishes (Re(1/a1) = 1) and
+            # Cabs is rounding noise; compare it on the extinction scale
+            assert np.max(np.abs(a - b)) <= XS_TOL * np.max(np.abs(c64[0])), name
+            continue
+        assert np.max(np.abs(a - b) / np.abs(b)) <= XS_TOL, (name, np.max(np.abs(a - b) / np.abs(b)))
+    assert np.linalg.norm(X32 - X64) / np.linalg.norm(X64) <= XS_TOL
+    ind = torch3d.GreenOperator(prob.n, prob.lf, prob.k, prob.address, device="cuda")
+    r32 = ind.true_residual(prob.diag, prob.B, X32)
+    r64 = ind.true_residual(prob.diag, prob.B, X64)
+    del ind
+    torch.cuda.empty_cache()
+    assert np.all(r32 <= RES_TOL), r32.max()
+    assert np.all(r64 <= RES_TOL), r64.max()
+

@@ -193,3 +193,62 @@ def test_vectorised_reference_algorithm_matches_literal(n):
     gh, P = mbt.green_hat(n, 3, lf, k)
     ref = mbt.block_mvp(n, 3, gh, P, addr, diag, S)
     assert np.linalg.norm(cpu.block_mvp(S) - ref) / np.linalg.norm(ref) < 1e-13
+
+
+# --------------------------------------------------------------------------
+# workload restatements used by the benchmark's CPU reference arm, and the
+# second (torch complex128) oracle of the large parity tests
+# --------------------------------------------------------------------------
+
+@pytest.mark.parametrize("nocc,seed,kf,Df", [(1, 1, 1.0, 2.8), (64, 2, 1.0, 2.8), (1024, 1, 1.0, 2.8),
+                                             (2500, 7, 1.2, 1.9)])
+def test_aggregate_restatement_matches_library(nocc, seed, kf, Df):
+    import bdda
+    from oracle import aggregate
+    n1, a1 = bdda.aggregate(nocc, kf, Df, seed)
+    n2, a2 = aggregate.aggregate(nocc, kf, Df, seed)
+    assert n1 == n2 and np.array_equal(a1, a2)
+
+
+def test_directions_restatement_matches_library():
+    import bdda
+    from oracle import aggregate
+    for nd, seed in ((1, 1001), (8, 1001), (16, 1002)):
+        u1, e1 = bdda.directions(nd, seed)
+        u2, e2 = aggregate.directions(nd, seed)
+        assert np.array_equal(u1, u2) and np.array_equal(e1, e2)
+
+
+def test_mie_restatement_pinned_to_reference_gmie():
+    worst = 0.0
+    for c in golden("mie_ref.json"):
+        a1, b1 = physics.mie_a1b1(c["wl0"], c["rp"], complex(*c["eper"]), complex(*c["mper"]))
+        ra, rb = complex(*c["a1"]), complex(*c["b1"])
+        worst = max(worst, abs(a1 - ra) / abs(ra), abs(b1 - rb) / abs(rb))
+    assert worst < 1e-11, worst
+
+
+@pytest.mark.parametrize("nocc,seed,k", [(200, 3, 11.4 + 0.2j), (700, 5, 11.42)])
+def test_torch_operator_matches_numpy_oracle(nocc, seed, k):
+    from oracle import aggregate, torch3d
+    n, addr = aggregate.aggregate(nocc, 1.0, 2.8, seed)
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((3 * nocc, 3)) + 1j * rng.standard_normal((3 * nocc, 3))
+    gh, P = mbt.green_hat(n, 3, 0.02, k)
+    want = mbt.mvp3d(n, 3, gh, P, x, addr)
+    got = torch3d.GreenOperator(n, 0.02, k, addr).apply(x).numpy()
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-14
+
+
+def test_reference_N65536_target_fixture():
+    """The reference's N65536 aggregate as committed: 60,077 distinct sites of a
+    137 x 135 x 176 box, monomer volume 4 pi / 3 (file units), one material."""
+    import os
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "target_N65536.npz"))
+    addr = np.cumsum(d["address_delta"].astype(np.int64))
+    n = tuple(int(v) for v in d["n"])
+    assert n == (137, 135, 176) and addr.size == 60077
+    assert np.unique(addr).size == addr.size and addr.min() >= 0 and addr.max() < np.prod(n)
+    assert abs(float(d["vol"]) - 4.18879) < 1e-9 and float(d["lf"]) == 1.0
+    assert str(d["source"]) == "DDA_target_0_agg_N65536_kf1.0_Df2.8.out"

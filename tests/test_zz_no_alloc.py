@@ -62,3 +62,51 @@ def test_no_alloc_mvp_rejects_workspace_beyond_fixed_scratch():
         op.mvp_device_noalloc(x.data_ptr(), x.data_ptr(), L, 3 * nocc, 3 * nocc, prec=bdda.PREC_FP32)
     assert ei.value.code == bdda.ERR_INVALID
     assert "scratch" in str(ei.value)
+
+
+def test_no_alloc_mvp_allocates_nothing_and_needs_no_cleared_scratch():
+    """A fresh operator's no-allocation MVPs leave the device's free memory as
+    it was, and a scratch left full of NaN by a larger box's call does not
+    reach the next call's result."""
+    import torch
+    nocc, L = 300, 4
+    n, addr = bdda.aggregate(nocc, 1.0, 2.8, 23)
+    rng = np.random.default_rng(23)
+    x = rng.standard_normal((3 * nocc, L)) + 1j * rng.standard_normal((3 * nocc, L))
+    k = 2 * np.pi / 0.55
+    xd = torch.from_numpy(np.ascontiguousarray(x.T)).cuda()
+    # an earlier operator on the same box loads the code that holds the scratch
+    warm = bdda.Operator(n, 0.02, k)
+    warm.set_dipoles(addr)
+    tmp = torch.empty_like(xd)
+    warm.mvp_device_noalloc(xd.data_ptr(), tmp.data_ptr(), L, 3 * nocc, 3 * nocc, prec=bdda.PREC_FP64)
+    torch.cuda.synchronize()
+    # a larger box with NaN input fills the scratch with NaN
+    nb, ab = bdda.aggregate(2000, 1.0, 2.8, 5)
+    big = bdda.Operator(nb, 0.02, k)
+    big.set_dipoles(ab)
+    xn = torch.full((2, 3 * ab.size), float("nan"), dtype=torch.complex128, device="cuda")
+    yn = torch.empty_like(xn)
+    big.mvp_device_noalloc(xn.data_ptr(), yn.data_ptr(), 2, 3 * ab.size, 3 * ab.size, prec=bdda.PREC_FP64)
+    torch.cuda.synchronize()
+    assert torch.isnan(yn).all()
+    # a fresh operator: only no-allocation calls, and no change of free device memory
+    fresh = bdda.Operator(n, 0.02, k)
+    fresh.set_dipoles(addr)
+    outs = [torch.empty_like(xd) for _ in range(2)]
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for out in outs:
+        fresh.mvp_device_noalloc(xd.data_ptr(), out.data_ptr(), L, 3 * nocc, 3 * nocc, prec=bdda.PREC_FP64)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    # the allocating entry point on another operator of the same box is the reference
+    ref = torch.empty_like(xd)
+    warm.mvp_device(xd.data_ptr(), ref.data_ptr(), L, 3 * nocc, 3 * nocc, prec=bdda.PREC_FP64)
+    torch.cuda.synchronize()
+    want = ref.cpu().numpy()
+    for out in outs:
+        got = out.cpu().numpy()
+        assert np.all(np.isfinite(got))
+        assert _rel(got, want) <= TOL[bdda.PREC_FP64]
