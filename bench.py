@@ -74,6 +74,9 @@ def parse(argv=None):
     ap.add_argument("--target-file", default=None, nargs="?", const=REF_TARGET,
                     help="aggregate from a target fixture (.npz written by tests/golden/make_golden.py) instead of "
                          "the seeded generator; without a value, the reference's N65536 aggregate")
+    ap.add_argument("--file-volumes", action="store_true",
+                    help="with --target-file: each dipole takes the file's site volume (the reference's "
+                         "convention, 4 pi / 3 lf^3 for its aggregates) instead of one lattice cell d^3")
     ap.add_argument("--solver", default="cocg_rq")
     ap.add_argument("--no-jacobi", action="store_true", help="unpreconditioned solver (default: Jacobi-preconditioned)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison solve")
@@ -131,13 +134,16 @@ def target_geometry(a, seed, use_oracle):
     """(n, address, lf_phys, r_eq) of the workload's target.
 
     Seeded aggregate: spacing d, dipole volume d^3.  Target file: the file's
-    spacing lf (in units of the monomer radius r_pp) scaled to d, each site of
-    the file's volume (4 pi / 3 r_pp^3 for the reference's aggregates)."""
+    spacing lf (in units of the monomer radius r_pp) scaled to d, each dipole of
+    volume d^3 -- or, with --file-volumes, of the file's site volume (4 pi / 3
+    r_pp^3 for the reference's aggregates: spheres of radius d on a lattice of
+    spacing d, 4.2 times the cell volume, a far stiffer system)."""
     k, d, _eps = physical(a)
     if a.target_file:
         n, lf, address, vol, _src = load_target_file(a.target_file)
         r_pp = d / lf
-        return n, address, d, (3.0 * vol / (4.0 * math.pi)) ** (1.0 / 3.0) * r_pp
+        v = vol if a.file_volumes else lf ** 3
+        return n, address, d, (3.0 * v / (4.0 * math.pi)) ** (1.0 / 3.0) * r_pp
     if use_oracle:
         from oracle import aggregate as agg
         n, address = agg.aggregate(a.nocc, 1.0, 2.8, seed)
@@ -151,7 +157,8 @@ def problem_ours(a, seed):
     import bdda
     if a.target_file:
         n, lf, address, vol, _src = load_target_file(a.target_file)
-        return bdda.target_problem(n, lf, address, vol, complex(a.m), a.wl0, seed=seed, n_dirs=a.nrhs // 2)
+        v = vol if a.file_volumes else lf ** 3
+        return bdda.target_problem(n, lf, address, v, complex(a.m), a.wl0, seed=seed, n_dirs=a.nrhs // 2)
     return bdda.make_problem(a.nocc, complex(a.m), wl0=a.wl0, seed=seed, n_dirs=a.nrhs // 2)
 
 
@@ -173,7 +180,8 @@ def workload_config(a, n, P, nocc):
     name = SOLVER_NAMES.get(a.solver, a.solver)
     if a.target_file:
         _n, _lf, _ad, _v, src = load_target_file(a.target_file)
-        what = f"reference target file {src} ({nocc} occupied sites)"
+        vols = "file site volumes" if a.file_volumes else "dipole volume d^3"
+        what = f"reference target file {src} ({nocc} occupied sites, {vols})"
     else:
         what = f"N={nocc} dipole lattice aggregate (kf=1.0, Df=2.8, seed=1+rank)"
     ws = 3 * a.nrhs * P[0] * P[1] * ((n[2] + 3) & ~3) * 8
@@ -269,7 +277,7 @@ class CpuReference:
     """The reference's 1-D MBT FFT block matvec on the host cores (oracle.mbt_fast,
     scipy's pocketfft standing in for FFTW), one right-hand side per thread as the
     reference's OpenMP loop over columns.  Threads are capped by the host memory
-    one column needs (a third of what is available)."""
+    one column needs (half of what is available)."""
 
     def __init__(self, n, lf, k, address, diag):
         from oracle.mbt_fast import MbtCpu
@@ -278,7 +286,7 @@ class CpuReference:
         self.cpu = MbtCpu(n, lf, k, address, diag, threads=1)
         self.t_init = time.perf_counter() - t0
         per_col = self.cpu.bytes_per_column()
-        self.threads = int(max(1, min(cores, mem_available() // 3 // per_col)))
+        self.threads = int(max(1, min(cores, mem_available() // 2 // per_col)))
         self.cpu.threads = self.threads
         self.cores = cores
 

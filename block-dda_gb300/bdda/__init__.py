@@ -39,7 +39,7 @@ EXPORTS = [
     "bdda_incident_fields_eh", "bdda_cross_sections_eh", "bdda_read_target_file", "bdda_shape_target",
     "bdda_material_load", "bdda_material_constant", "bdda_material_eval", "bdda_material_destroy",
     "bdda_polarizabilities", "bdda_diag_a", "bdda_op_set_wavenumber", "bdda_sweep", "bdda_mie_q",
-    "bdda_format_result",
+    "bdda_format_result", "bdda_request_footprint_f",
 ]
 
 SHAPES = {"sphere": 0, "cube": 1, "ellipsoid": 2, "cuboid": 3, "cylinder": 4, "rounded_cylinder": 5}
@@ -96,7 +96,7 @@ class ResultRecord(ct.Structure):
 class Request(ct.Structure):
     _fields_ = [("n", ct.c_int * 3), ("lf", ct.c_double), ("k_re", ct.c_double), ("k_im", ct.c_double),
                 ("address", ct.POINTER(ct.c_int)), ("nocc", ct.c_int), ("diag", ct.POINTER(ct.c_double)),
-                ("B", ct.POINTER(ct.c_double)), ("L", ct.c_int), ("X", ct.POINTER(ct.c_double))]
+                ("B", ct.POINTER(ct.c_double)), ("L", ct.c_int), ("X", ct.POINTER(ct.c_double)), ("f", ct.c_int)]
 
 
 class RequestResult(ct.Structure):
@@ -110,7 +110,8 @@ class RequestResult(ct.Structure):
 
 class SolveStats(ct.Structure):
     _fields_ = [("status", ct.c_int), ("iterations", ct.c_int), ("refinements", ct.c_int), ("mvps", ct.c_int),
-                ("final_err", ct.c_double), ("true_res_max", ct.c_double), ("ms_solve", ct.c_double)]
+                ("final_err", ct.c_double), ("true_res_max", ct.c_double), ("ms_solve", ct.c_double),
+                ("fp64_inner_steps", ct.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -172,6 +173,8 @@ def lib(build_if_missing: bool = False):
     L.bdda_last_error.restype = ct.c_char_p
     L.bdda_request_footprint.argtypes = [ip, ct.c_int, ct.c_int, ct.c_int]
     L.bdda_request_footprint.restype = ct.c_double
+    L.bdda_request_footprint_f.argtypes = [ip, ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+    L.bdda_request_footprint_f.restype = ct.c_double
     L.bdda_server_create.argtypes = [ct.POINTER(vp), ct.c_int, ct.c_double, ct.POINTER(SolveOpts), ct.c_int]
     L.bdda_server_submit.argtypes = [vp, ct.POINTER(Request), ct.POINTER(ct.c_longlong)]
     L.bdda_server_wait.argtypes = [vp, ct.c_longlong, ct.POINTER(RequestResult)]
@@ -611,9 +614,9 @@ def target_problem(n, lf, address, vol, m, wl0=0.55, seed=1, n_dirs=1, mkd=0.5):
 # batched solves and the request server
 # ---------------------------------------------------------------------------
 
-def footprint(n, nocc, L, precision=SOLVE_MIXED):
+def footprint(n, nocc, L, precision=SOLVE_MIXED, f=3):
     n3 = (ct.c_int * 3)(*[int(v) for v in n])
-    return float(lib().bdda_request_footprint(n3, int(nocc), int(L), int(precision)))
+    return float(lib().bdda_request_footprint_f(n3, int(nocc), int(L), int(precision), int(f)))
 
 
 class _Held:
@@ -636,6 +639,7 @@ class _Held:
         self.req.B = _dptr(self.B)
         self.req.L = int(self.B.shape[1])
         self.req.X = _dptr(self.X)
+        self.req.f = int(self.B.shape[0] // max(1, self.address.size))  # 3 or 6 rows per dipole
 
 
 class Server:

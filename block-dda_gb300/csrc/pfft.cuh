@@ -351,6 +351,78 @@ __device__ __forceinline__ void stage0_to_global(const ulonglong2* __restrict__ 
   __syncwarp();
 }
 
+// Forward stages s .. end - 1.
+template <class P, int NP, int s, int end>
+__device__ __forceinline__ void forward_to(ulonglong2* sm, const float4* tw, int lane, int nv) {
+  if constexpr (s < end) {
+    stage<P, s, false, NP>(sm, tw, lane, nv);
+    forward_to<P, NP, s + 1, end>(sm, tw, lane, nv);
+  }
+}
+
+// Largest last-stage radix of the fused middle step: 3 R pair elements, 12 R registers.
+constexpr int kFusedMaxRadix = 5;
+
+// Last forward stage, Green product and first inverse stage of a task's three
+// line pairs in one sweep (the packed form of sfft::middle3): butterfly b of
+// the last stage (M = 1, no twiddles) in all three component pairs, the
+// symmetric 3 x 3 spectrum of each of its R frequencies applied in registers,
+// the inverse DFT, one store.
+template <class P>
+__device__ __forceinline__ void middle3(ulonglong2* __restrict__ sm, const float2* __restrict__ gl, int lane) {
+  constexpr int R = P::Rl;
+  constexpr int B = P::N / R;
+  constexpr int m[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  for (int b = lane; b < B; b += 32) {
+    const int idx0 = b * R;
+    ulonglong2* p = sm + P::addr(idx0);
+    cp e[3][R];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+      for (int i = 0; i < R; ++i) e[c][i] = lds(p + c * P::LW + i);
+      dft<R, false>(e[c]);
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      u64 gr[6], gi[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const float2 g = ldg_c(gl + c * P::N + idx0 + i);
+        gr[c] = dup(g.x);
+        gi[c] = dup(g.y);
+      }
+      cp o3[3];
+#pragma unroll
+      for (int o = 0; o < 3; ++o) {
+        // re' = sum re_d gr - sum im_d gi ; im' = sum im_d gr + re_d gi
+        u64 ar = mul(e[0][i].re, gr[m[o][0]]);
+        ar = fma(e[1][i].re, gr[m[o][1]], ar);
+        ar = fma(e[2][i].re, gr[m[o][2]], ar);
+        u64 ai = mul(e[0][i].im, gi[m[o][0]]);
+        ai = fma(e[1][i].im, gi[m[o][1]], ai);
+        ai = fma(e[2][i].im, gi[m[o][2]], ai);
+        u64 bi = mul(e[0][i].im, gr[m[o][0]]);
+        bi = fma(e[1][i].im, gr[m[o][1]], bi);
+        bi = fma(e[2][i].im, gr[m[o][2]], bi);
+        bi = fma(e[0][i].re, gi[m[o][0]], bi);
+        bi = fma(e[1][i].re, gi[m[o][1]], bi);
+        bi = fma(e[2][i].re, gi[m[o][2]], bi);
+        o3[o] = cp{sub(ar, ai), bi};
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) e[c][i] = o3[c];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      dft<R, true>(e[c]);
+#pragma unroll
+      for (int i = 0; i < R; ++i) sts(p + c * P::LW + i, e[c][i]);
+    }
+  }
+  __syncwarp();
+}
+
 template <class P, int NP, int s = 0>
 __device__ __forceinline__ void forward(ulonglong2* sm, const float4* tw, int lane, int nv) {
   if constexpr (s < P::nst) {

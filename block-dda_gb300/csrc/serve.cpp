@@ -47,17 +47,22 @@ int smooth235(int v) {
   }
 }
 
-double footprint_bytes(const int n[3], int nocc, int L, int precision) {
+// Device bytes of one request of f components per dipole: Green spectra (6
+// or 9 components; FP64 or FP32 + double-float), the initialisation's FP64
+// work grid, occupancy, MVP workspace of both precisions, Krylov blocks.
+double footprint_bytes(const int n[3], int nocc, int L, int precision, int f) {
   const double Px = smooth235(2 * n[0]), Py = smooth235(2 * n[1]), Pz = smooth235(2 * n[2]);
   const double Ng = Px * Py * Pz;
   const double nc = (double)n[0] * n[1] * n[2];
   const bool mixed = precision == BDDA_SOLVE_MIXED;
-  const double tables = 6.0 * Ng * (16.0 + (mixed ? 8.0 : 0.0));
-  const double init_work = 6.0 * Ng * 16.0;
+  const double ncomp = f == 6 ? 9.0 : 6.0;
+  const double tables = ncomp * Ng * (16.0 + (mixed ? 8.0 : 0.0));
+  const double init_work = ncomp * Ng * 16.0;
   const double occ = nc * 4.0 + (double)n[1] * ((n[2] + 7) / 8) * 5.0;
-  const double t1 = 3.0 * L * Px * n[1] * n[2], t2 = 3.0 * L * Px * Py * n[2];
+  const double nzp = (double)((n[2] + 3) & ~3);
+  const double t1 = (double)f * L * Px * n[1] * nzp, t2 = (double)f * L * Px * Py * nzp;
   const double mvp = (t1 + t2) * (16.0 + (mixed ? 8.0 : 0.0));
-  const double nu = 3.0 * nocc, LL = (double)L * L;
+  const double nu = (double)f * nocc, LL = (double)L * L;
   const double blocks = 10.0 * nu * L * (mixed ? 8.0 : 16.0) + 3.0 * nu * L * 16.0 + nu * 32.0;
   const double small = 2.0 * LL * 152.0 * 16.0 + 2.0 * std::max(608.0 * L, 1216.0) * 16.0 + LL * 16.0 * 20.0 + 8.0 * 4096;
   const double io = nu * 16.0 + 2.0 * nu * L * 16.0;
@@ -116,14 +121,15 @@ struct bdda_server {
     bdda_op* op = nullptr;
     // mixed: FP32 inner solves + double-float residuals; otherwise plain FP64
     const int prec = opts.precision == BDDA_SOLVE_MIXED ? (BDDA_PREC_FP32 | BDDA_PREC_DF64) : BDDA_PREC_FP64;
-    int rc = bdda_op_create(&op, r.n, 3, r.lf, r.k_re, r.k_im, prec);
+    const int f = r.f == 6 ? 6 : 3;
+    int rc = bdda_op_create(&op, r.n, f, r.lf, r.k_re, r.k_im, prec);
     // concurrent requests keep the GPU busy between one stream's launches, so
     // captured poll cycles save nothing here and cost their capture (batched
     // workload: 245 vs 251 RHS-solves/s with and without them)
     if (rc == BDDA_OK) rc = bdda_op_set_graphs(op, 0);
     if (rc == BDDA_OK) rc = bdda_op_set_dipoles(op, r.address, r.nocc);
     bdda_solve_stats st{};
-    if (rc == BDDA_OK) rc = bdda_solve(op, &opts, r.diag, r.B, 3 * r.nocc, r.X, 3 * r.nocc, r.L, &st);
+    if (rc == BDDA_OK) rc = bdda_solve(op, &opts, r.diag, r.B, f * r.nocc, r.X, f * r.nocc, r.L, &st);
     if (op) bdda_op_destroy(op);
     res->status = rc;
     res->iterations = st.iterations;
@@ -165,8 +171,12 @@ struct bdda_server {
 extern "C" {
 
 double bdda_request_footprint(const int n[3], int nocc, int L, int precision) {
-  if (!n || nocc < 1 || L < 1) return -1.0;
-  return footprint_bytes(n, nocc, L, precision);
+  return bdda_request_footprint_f(n, nocc, L, precision, 3);
+}
+
+double bdda_request_footprint_f(const int n[3], int nocc, int L, int precision, int f) {
+  if (!n || nocc < 1 || L < 1 || (f != 3 && f != 6)) return -1.0;
+  return footprint_bytes(n, nocc, L, precision, f);
 }
 
 int bdda_server_create(bdda_server** out, int slots, double mem_budget_bytes, const bdda_solve_opts* opts, int dry_run) {
@@ -189,7 +199,8 @@ int bdda_server_create(bdda_server** out, int slots, double mem_budget_bytes, co
 }
 
 int bdda_server_submit(bdda_server* s, const bdda_request* r, long long* ticket) {
-  if (!s || !r || !ticket || r->nocc < 1 || r->L < 1 || r->L > 32 || !r->address || !r->diag || !r->B || !r->X) {
+  if (!s || !r || !ticket || r->nocc < 1 || r->L < 1 || r->L > 32 || !r->address || !r->diag || !r->B || !r->X ||
+      (r->f != 0 && r->f != 3 && r->f != 6)) {
     bdda::set_error("bad request");
     return BDDA_ERR_INVALID;
   }
@@ -198,7 +209,7 @@ int bdda_server_submit(bdda_server* s, const bdda_request* r, long long* ticket)
       bdda::set_error("lattice box dimension outside 1..256 (padded FFT lines are limited to 512 points)");
       return BDDA_ERR_INVALID;
     }
-  const double fp = footprint_bytes(r->n, r->nocc, r->L, s->opts.precision);
+  const double fp = footprint_bytes(r->n, r->nocc, r->L, s->opts.precision, r->f == 6 ? 6 : 3);
   if (fp > s->budget) {
     bdda::set_error("request footprint " + std::to_string((long long)fp) + " bytes exceeds the server memory budget");
     return BDDA_ERR_NOMEM;

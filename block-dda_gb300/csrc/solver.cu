@@ -977,8 +977,11 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
 
   Krylov<double> k64{op, w, st, n, L, diag, jpre64, check_every};
   Krylov<float> k32{op, w, st, n, L, w->diag32.as<float2>(), jpre32, check_every};
-  int total_iters = 0, refinements = 0, status = BDDA_OK, mvps = 0;
+  int total_iters = 0, refinements = 0, status = BDDA_OK, mvps = 0, fp64_steps = 0;
   double last_err = 0.0, resmax = -1.0;
+  // precision of the inner solves: FP32 for a mixed solve until a refinement
+  // step shows that FP32 Krylov cannot make progress on this system (below)
+  bool inner64 = !mixed;
 
   // inner solve on RHS R (FP64, leading dim ldr): the correction D is solved in
   // the inner precision into block 9 (right-hand side in block 8), then added
@@ -1006,7 +1009,8 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
       cf = w->colf.as<double>();
       cfi = cf + L;
     }
-    if (!mixed) {
+    if (inner64) {
+      if (mixed) ++fp64_steps;
       double2* Bp = w->blk64[8].as<double2>();
       double2* D = w->blk64[9].as<double2>();
       if (o->jacobi) k_rowscale<double, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n, cf);
@@ -1090,6 +1094,18 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
       R = w->R64.as<double2>();
       ldr = n;
       if (resmax <= o->true_tol) { converged = true; break; }
+      // A mixed solve whose FP32 inner step broke down or cut the true
+      // residual less than tenfold (a system so ill-conditioned that FP32
+      // Krylov stagnates: an FP32 step normally gains three to four digits)
+      // runs its remaining steps with FP64 inner solves, when the operator
+      // holds FP64 tables.  The FP64 Krylov blocks are allocated then.
+      if (!inner64 && (broke || !(resmax < 0.1 * before)) && (op->prec & BDDA_PREC_FP64)) {
+        if (st != op->stream) BDDA_CUDA(order_after(op->stream, st));
+        BDDA_TRY(ensure_work(op, n, L, itermax, true, true));
+        if (st != op->stream) BDDA_CUDA(order_after(st, op->stream));
+        inner64 = true;
+        continue;
+      }
       if (broke && !(resmax < before)) { status = BDDA_ERR_BREAKDOWN; break; }
     }
     if (converged) status = BDDA_OK;  // an inner solve that hit itermax does not matter once the residual is met
@@ -1109,6 +1125,7 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
     stats->final_err = last_err;
     stats->true_res_max = resmax;
     stats->ms_solve = ms;
+    stats->fp64_inner_steps = fp64_steps;
   }
   BDDA_CUDA(cudaGetLastError());
   if (status == BDDA_ERR_BREAKDOWN) set_error("breakdown: singular L x L system, failed Cholesky or non-finite value");

@@ -163,6 +163,69 @@ __device__ __forceinline__ void forward_from_global(C* sm, const C* tw, int lane
   forward<P, NL, 1, C>(sm, tw, lane, nv);
 }
 
+// Forward stages s .. end - 1 of NL lines.
+template <class P, int NL, int s, int end, typename C = float2>
+__device__ __forceinline__ void forward_to(C* sm, const C* tw, int lane, int nv) {
+  if constexpr (s < end) {
+    stage<P, s, false, NL, C>(sm, tw, lane, nv);
+    forward_to<P, NL, s + 1, end, C>(sm, tw, lane, nv);
+  }
+}
+
+// Largest last-stage radix the fused middle step (middle3) runs with: its
+// thread holds the three lines' R elements, 6 R registers for complex FP32.
+template <typename C> constexpr int fused_max_radix() { return sizeof(C) == 8 ? 6 : 5; }
+
+// Last forward stage, Green product and first inverse stage of the three
+// component lines of a z task in one sweep over shared memory.  The last
+// forward stage has M = 1: butterfly b holds the R adjacent elements b R ..
+// b R + R - 1 (at P::addr(b R) + i) and takes no twiddles, and so does the
+// first inverse stage on the same elements; in between, each of the R
+// frequencies is multiplied by the symmetric 3 x 3 Green spectrum (gl[c Pz +
+// idx], components xx xy xz yy yz zz, A = -G of
+// mvp_fft/application_function.cpp:36-40).  A thread does all three lines of
+// its butterfly, so the spectrum is applied in registers: one shared-memory
+// load and store per element instead of the separate stages' three of each.
+template <class P, typename C>
+__device__ __forceinline__ void middle3(C* __restrict__ sm, const C* __restrict__ gl, int lane) {
+  constexpr int R = P::Rl;
+  constexpr int B = P::N / R;
+  for (int b = lane; b < B; b += 32) {
+    const int idx0 = b * R;
+    C* p = sm + P::addr(idx0);
+    C e0[R], e1[R], e2[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      e0[i] = p[i];
+      e1[i] = p[P::LW + i];
+      e2[i] = p[2 * P::LW + i];
+    }
+    dft<R, false>(e0);
+    dft<R, false>(e1);
+    dft<R, false>(e2);
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const C* g = gl + idx0 + i;
+      const C gxx = ldg_c(g), gxy = ldg_c(g + P::N), gxz = ldg_c(g + 2 * P::N);
+      const C gyy = ldg_c(g + 3 * P::N), gyz = ldg_c(g + 4 * P::N), gzz = ldg_c(g + 5 * P::N);
+      const C x = e0[i], y = e1[i], z = e2[i];
+      e0[i] = cadd(cadd(cmul(gxx, x), cmul(gxy, y)), cmul(gxz, z));
+      e1[i] = cadd(cadd(cmul(gxy, x), cmul(gyy, y)), cmul(gyz, z));
+      e2[i] = cadd(cadd(cmul(gxz, x), cmul(gyz, y)), cmul(gzz, z));
+    }
+    dft<R, true>(e0);
+    dft<R, true>(e1);
+    dft<R, true>(e2);
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      p[i] = e0[i];
+      p[P::LW + i] = e1[i];
+      p[2 * P::LW + i] = e2[i];
+    }
+  }
+  __syncwarp();
+}
+
 // Inverse transform (unnormalised): digit-reversed in, natural order out,
 // only the first nv outputs written.
 template <class P, int NL, int s = P::nst - 1, int last = 0, typename C = float2>

@@ -73,11 +73,18 @@ k_pass_c_packed(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp,
   float2* g0 = t2 + (size_t)(3 * la) * fstride + (size_t)line * nzp;
   const ptrdiff_t boff = has_b ? (ptrdiff_t)(3 * fstride) : 0;  // right-hand side la + 1
   pk::stage0_from_global<P, 3>(s0, twz, lane, nz, g0, fstride, boff);
-  pk::forward<P, 3, 1>(s0, twz, lane, nz);
   const float2* gl = ghat + (size_t)line * 6 * Pz;
-  for (int p = lane; p < Pz; p += 32) z_product_pair(s0, LW, P::addr(p), gl, Pz, p);
-  __syncwarp();
-  pk::inverse<P, 3, P::nst - 1, 1>(s0, twz, lane, nz);
+  if constexpr (P::nst >= 2 && P::Rl <= pk::kFusedMaxRadix) {
+    // last forward stage, product and first inverse stage fused (pk::middle3)
+    pk::forward_to<P, 3, 1, P::nst - 1>(s0, twz, lane, nz);
+    pk::middle3<P>(s0, gl, lane);
+    pk::inverse<P, 3, P::nst - 2, 1>(s0, twz, lane, nz);
+  } else {
+    pk::forward<P, 3, 1>(s0, twz, lane, nz);
+    for (int p = lane; p < Pz; p += 32) z_product_pair(s0, LW, P::addr(p), gl, Pz, p);
+    __syncwarp();
+    pk::inverse<P, 3, P::nst - 1, 1>(s0, twz, lane, nz);
+  }
   pk::stage0_to_global<P, 3>(s0, twz, lane, nz, g0, fstride, boff, has_b);
 }
 

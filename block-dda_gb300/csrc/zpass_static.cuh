@@ -39,10 +39,19 @@ k_pass_c_static(C* __restrict__ t2, int L, int Px, int Py, int nz, int nzp, cons
   C* g0 = t2 + (size_t)(fc * l) * fstride + (size_t)line * nzp;
   constexpr bool six = SIX;
   constexpr int halves = six ? 2 : 1;  // line triples: E, then M
+  const C* gl = ghat + (size_t)line * (six ? 9 : 6) * Pz;
+  if constexpr (!SIX && P::nst >= 2 && P::Rl <= sfft::fused_max_radix<C>()) {
+    // last forward stage, product and first inverse stage fused (middle3)
+    sfft::stage0_from_global<P, 3, C>(s0, twz, lane, nz, g0, fstride);
+    sfft::forward_to<P, 3, 1, P::nst - 1, C>(s0, twz, lane, nz);
+    sfft::middle3<P, C>(s0, gl, lane);
+    sfft::inverse<P, 3, P::nst - 2, 1, C>(s0, twz, lane, nz);
+    sfft::stage0_to_global<P, 3, C>(s0, twz, lane, nz, g0, fstride);
+    return;
+  }
   // the first forward stage reads the lines straight from T2 (no staging loop)
   for (int h = 0; h < halves; ++h)
     sfft::forward_from_global<P, 3>(s0 + 3 * h * LW, twz, lane, nz, g0 + 3 * h * fstride, fstride);
-  const C* gl = ghat + (size_t)line * (six ? 9 : 6) * Pz;
   for (int p = lane; p < Pz; p += 32) z_product(s0, LW, P::addr(p), gl, Pz, p, six);
   __syncwarp();
   // the last inverse stage writes the lines straight back to T2 (rows past nz dropped)

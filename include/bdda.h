@@ -135,7 +135,9 @@ int bdda_op_mvp_device_noalloc(bdda_op* op, int prec, const void* x, int ldx, vo
 typedef struct {
   int solver;         /* BDDA_SOLVER_* */
   int jacobi;         /* 1: left Jacobi scaling by 1/DIAG_A (the *_jacobi_mvp_fft variants) */
-  int precision;      /* BDDA_SOLVE_FP64 or BDDA_SOLVE_MIXED */
+  int precision;      /* BDDA_SOLVE_FP64 or BDDA_SOLVE_MIXED (a mixed refinement whose FP32 inner step breaks
+                         down or gains less than a digit continues with FP64 inner solves when the
+                         operator holds FP64 tables; stats->fp64_inner_steps counts them) */
   double tol;         /* reference stopping test on the recurrence error (Solver.hpp:27 default 1e-2) */
   int itermax;        /* reference iteration limit per Krylov solve (Solver.hpp:28 default 300) */
   double true_tol;    /* >0: iterate until every column's true residual ||b-Ax||/||b|| <= true_tol
@@ -157,6 +159,8 @@ typedef struct {
   double final_err;       /* last recurrence error (the reference's printed value) */
   double true_res_max;    /* max over columns of ||b_l - A x_l|| / ||b_l|| (FP64), -1 if not computed */
   double ms_solve;        /* device time of the whole solve (CUDA events) */
+  int fp64_inner_steps;   /* mixed solves: refinement steps run with FP64 inner solves after FP32 Krylov
+                             stagnated or broke down on the system (0 normally) */
 } bdda_solve_stats;
 
 /* Fill opts with the reference defaults (COCG-RQ-Jacobi, FP64, tol 1e-2, itermax 300). */
@@ -199,11 +203,12 @@ typedef struct {
   double k_re, k_im;
   const int* address;
   int nocc;
-  const double* diag;   /* 3*nocc complex */
-  const double* B;      /* 3*nocc x L complex, column-major, ld 3*nocc */
+  const double* diag;   /* f*nocc complex */
+  const double* B;      /* f*nocc x L complex, column-major, ld f*nocc */
   int L;                /* 1..32 */
-  double* X;            /* 3*nocc x L complex output */
-} bdda_request;         /* requests are f = 3 (electric dipoles) */
+  double* X;            /* f*nocc x L complex output */
+  int f;                /* 3 (electric dipoles; 0 means 3) or 6 (electric + magnetic, CEMD) */
+} bdda_request;
 
 typedef struct {
   int status;             /* BDDA_OK or the solve's error code */
@@ -214,8 +219,10 @@ typedef struct {
   double footprint_bytes;             /* device memory reserved for the request */
 } bdda_request_result;
 
-/* Device-memory footprint the server reserves for one request (bytes). */
+/* Device-memory footprint the server reserves for one f = 3 request (bytes). */
 double bdda_request_footprint(const int n[3], int nocc, int L, int precision);
+/* The same for f = 3 or 6 components per dipole. */
+double bdda_request_footprint_f(const int n[3], int nocc, int L, int precision, int f);
 
 typedef struct bdda_server bdda_server;
 

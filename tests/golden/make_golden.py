@@ -28,7 +28,8 @@ Fixtures:
   ``DDA_target_0_agg_N65536_kf1.0_Df2.8.out`` (box 137 x 135 x 176, 60,077
   monomer sites): box, lattice spacing, site volume and material, and the
   addresses in file order, delta-encoded (``address = cumsum(address_delta)``).
-  The benchmark's ``--target-file`` workload reads it.
+  The benchmark's ``--target-file`` workload reads it.  ``target_N1024.npz`` and
+  ``target_N4096.npz`` hold the N1024 and N4096 aggregates the same way.
 * ``materials_ref.json`` -- the four material tables and the eper the recorded
   runs used at each wavelength (interpolation pins).
 """
@@ -283,7 +284,9 @@ def main():
         "result_f6_BC_rpp20nm.json": lambda: result_f6(ref, lib),
         "materials_ref.json": lambda: materials_ref(ref),
     }
-    npz = {"target_N65536.npz": "DDA_target_0_agg_N65536_kf1.0_Df2.8.out"}
+    npz = {"target_N65536.npz": "DDA_target_0_agg_N65536_kf1.0_Df2.8.out",
+           "target_N1024.npz": "DDA_target_0_agg_N1024_kf1.0_Df2.8.out",
+           "target_N4096.npz": "DDA_target_0_agg_N4096_kf1.0_Df2.8.out"}
     for name, src in npz.items():
         if not args.only or name in args.only:
             target_npz(ref, src, os.path.join(HERE, name))

@@ -55,3 +55,37 @@ def test_server_result_same_alone_and_in_the_mix():
     assert r["status"] == 0
     assert np.array_equal(X_mix, X_alone)
     assert st["completed"] == len(probs) and st["peak_running"] >= 2
+
+
+def test_server_takes_f6_requests():
+    """An f = 6 (electric + magnetic dipole) request through the server equals
+    the direct solve on an f = 6 operator with the server's tables (FP32 +
+    double-float) bitwise, next to f = 3 requests in the same mix."""
+    import math
+    from oracle import physics
+    nocc, L = 700, 4
+    n, addr = bdda.aggregate(nocc, 1.0, 2.8, 29)
+    wl0, m = 0.55, 1.9 + 0.4j
+    k = 2 * math.pi / wl0
+    lf = 0.5 / (abs(m) * k)
+    ae, ah = bdda.polarizabilities(wl0, lf * (3 / (4 * math.pi)) ** (1 / 3), m * m, k)
+    diag = bdda.diag_a(np.full(nocc, ae), np.full(nocc, ah))
+    u, e, h = physics.reference_incident_waves(L)
+    B = bdda.incident_fields(n, lf, addr, k, u, e, h)
+    p6 = bdda.Problem(n=n, lf=lf, address=addr, k=k, alpha=np.full(nocc, ae), diag=diag, B=B)
+    opts = _mixed_opts()
+    op = bdda.Operator(n, lf, k, prec=bdda.PREC_FP32 | bdda.PREC_DF64, f=6)
+    op.set_dipoles(addr)
+    op.set_graphs(False)
+    X_direct, st = bdda.solve(op, diag, B, opts, allow_not_converged=False)
+    op.close()
+    assert bdda.footprint(n, nocc, L, f=6) > bdda.footprint(n, nocc, L, f=3)
+    srv = bdda.Server(slots=3, mem_budget_bytes=20e9, opts=opts)
+    others = _problems(3, 31)
+    tickets = [srv.submit(others[0]), srv.submit(p6)] + [srv.submit(p) for p in others[1:]]
+    outs = {t: srv.wait(t) for t in tickets}
+    srv.close()
+    X6, r6 = outs[tickets[1]]
+    assert r6["status"] == 0 and r6["true_res_max"] <= 1e-8
+    assert X6.shape == (6 * nocc, L) and np.array_equal(X6, X_direct)
+    assert all(outs[t][1]["status"] == 0 for t in tickets)

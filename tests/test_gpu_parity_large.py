@@ -15,7 +15,8 @@ independent checks stand in for it:
 
 Configurations: N=16384, nrhs=16, m=2.3+0.6i; N=65536, nrhs=32 with m=1.78 and
 m=1.33+1e-8i (seeded aggregates), and the reference's own N65536 aggregate file
-(box 137 x 135 x 176, padded 288 x 270 x 360) at m=1.78.
+(box 137 x 135 x 176, padded 288 x 270 x 360, one dipole of volume d^3 per
+site) at m=1.78.
 """
 import os
 
@@ -33,10 +34,12 @@ RES_TOL = 2e-8     # independent true residual
 
 
 def _target_file_problem(m, nrhs):
+    """The reference's N65536 aggregate, one dipole of volume d^3 per site."""
     d = np.load(os.path.join(GOLDEN, "target_N65536.npz"))
     addr = np.cumsum(d["address_delta"].astype(np.int64)).astype(np.int32)
-    return bdda.target_problem(tuple(int(v) for v in d["n"]), float(d["lf"]), addr, float(d["vol"]), m,
-                               wl0=0.55, seed=1, n_dirs=nrhs // 2)
+    lf = float(d["lf"])
+    return bdda.target_problem(tuple(int(v) for v in d["n"]), lf, addr, lf ** 3, m, wl0=0.55, seed=1,
+                               n_dirs=nrhs // 2)
 
 
 CASES = {

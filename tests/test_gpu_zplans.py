@@ -69,6 +69,40 @@ def test_every_z_plan_fp32_vs_fp64():
         assert rel < TOL32, (Pz, nz, rel)
 
 
+def _to_df(a):  # complex128 -> float32 [..., 4] = (re_hi, re_lo, im_hi, im_lo)
+    hi_r = a.real.astype(np.float32)
+    hi_i = a.imag.astype(np.float32)
+    lo_r = (a.real - hi_r.astype(np.float64)).astype(np.float32)
+    lo_i = (a.imag - hi_i.astype(np.float64)).astype(np.float32)
+    return np.stack([hi_r, lo_r, hi_i, lo_i], axis=-1)
+
+
+def test_every_z_plan_double_float_vs_fp64():
+    """The double-float z pass (residual MVPs of mixed solves) runs the same
+    compile-time plans; it must give FP64-level results on every length."""
+    import torch
+    rng = np.random.default_rng(9)
+    for i, (Pz, nz) in enumerate(_nz_per_pz()):
+        n = (2, 3, nz)
+        N = int(np.prod(n))
+        nocc = max(2, (2 * N) // 3)
+        addr = np.sort(rng.choice(N, size=nocc, replace=False)).astype(np.int32)
+        L = 1 + i % 2
+        x = rng.standard_normal((3 * nocc, L)) + 1j * rng.standard_normal((3 * nocc, L))
+        op = bdda.Operator(n, 0.03, 2 * np.pi / 0.55)
+        op.set_dipoles(addr)
+        y64 = _mvp(op, x, L, 3 * nocc, bdda.PREC_FP64, torch.complex128)
+        xd = torch.from_numpy(np.ascontiguousarray(_to_df(x.T))).cuda()
+        yd = torch.zeros_like(xd)
+        torch.cuda.synchronize()
+        op.mvp_device(xd.data_ptr(), yd.data_ptr(), L, 3 * nocc, 3 * nocc, prec=bdda.PREC_DF64)
+        torch.cuda.synchronize()
+        y = yd.cpu().numpy().astype(np.float64)
+        ydf = ((y[..., 0] + y[..., 1]) + 1j * (y[..., 2] + y[..., 3])).T
+        rel = np.linalg.norm(ydf - y64) / np.linalg.norm(y64)
+        assert rel < 1e-12, (Pz, nz, rel)
+
+
 @pytest.mark.parametrize("n", [(4, 3, 60), (2, 5, 75), (3, 3, 128), (2, 2, 256)])
 def test_z_plan_fp32_vs_oracle(n):
     import torch
