@@ -51,7 +51,8 @@ REF_TARGET = os.path.join(ROOT, "tests", "golden", "target_N65536.npz")
 # (FP64 recurrence error <= 1e-8) on the single-target workloads, measured on
 # GB300 with the FP64 path; they scale the CPU sample of one matvec to a
 # solve.  The GPU arm re-measures the count and reports it beside.
-REF_ITERS = {(16384, 16, "2.3+0.6j", "synthetic"): 30, (65536, 32, "1.78", "synthetic"): 30}
+REF_ITERS = {(16384, 16, "2.3+0.6j", "synthetic"): 30, (65536, 32, "1.78", "synthetic"): 28,
+             (65536, 32, "1.78", "file"): 22}
 REF_ITERS_FALLBACK = 30
 # DRAM traffic of the complex FP32 MVP passes over their byte model:
 # ncu dram__bytes_read.sum + dram__bytes_write.sum per launch on the N=8192,
@@ -591,23 +592,17 @@ def run_batched(a):
     return 0 if ok == count else 1
 
 
-def run_serving(a):
-    """Config: Poisson arrivals (seeded, default 200 req/s) of aggregate solves,
-    N log-uniform 128-32768, Df 1.8-2.8, lambda U[0.3,1.0] um, m as batched,
-    nrhs uniform in 2-32; admission by memory footprint, concurrent solves;
-    latency = submit -> result on host."""
+def _serve_stream(a, probs, rate, seed):
+    """Submit probs as a seeded Poisson stream at `rate` requests/s; returns the
+    served requests' results, wall time, rejections and server stats."""
     import torch
     import bdda
-    count = a.count or 400
-    rng = np.random.default_rng(7)
-    probs = [bdda.random_problem(rng, n_range=(128, 32768), wl_range=(0.3, 1.0), L_range=(2, 32))
-             for _ in range(count)]
-    gaps = rng.exponential(1.0 / a.rate, size=count)
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=len(probs))
     arrivals = np.cumsum(gaps) - gaps[0]
     opts = bdda.solve_opts("cocg_rq", jacobi=True, precision=bdda.SOLVE_MIXED, true_tol=1e-8, itermax=3000)
-    budget = free_budget()
-    srv = bdda.Server(a.slots, budget, opts)
-    for p in probs[:4]:                       # warm-up
+    srv = bdda.Server(a.slots, free_budget(), opts)
+    for p in probs[:4]:                       # warm-up (module load, pools)
         srv.wait(srv.submit(p))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -629,23 +624,44 @@ def run_serving(a):
     lat = np.array([r["t_done"] - r["t_submit"] for r in res])
     ok = sum(1 for r in res if r["status"] == 0 and r["true_res_max"] <= 1e-8)
     rhs = sum(p.B.shape[1] for p in served)
-    count_served = len(served)
-    line = {"metric": "p99 latency (s) of aggregate solves to 1e-8 under a Poisson request stream",
-            "value": float(np.percentile(lat, 99)), "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 4,
-            "ms_per_step": wall * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c64 (FFT-MVP, Krylov) + c128 (refinement)", "data": "synthetic (seeded lattice aggregates)",
-            "config": {"workload": f"serving: {count} requests, Poisson {a.rate} req/s (seeded), N log-uniform "
-                                   f"128-32768, lambda 0.3-1.0 um, m 1.3-2.4 + 0-0.9i, nrhs 2-32, true residual <= 1e-8",
-                       "slots": a.slots, "memory_budget_GB": budget / 1e9},
+    return {"offered_requests_per_s": rate,
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
                           "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
-            "throughput": {"requests_per_s": count_served / wall, "rhs_solves_per_s": rhs / wall,
-                           "offered_requests_per_s": a.rate},
-            "requests_converged": ok, "requests_served": count_served, "requests": count,
-            "rejected_at_admission": rejected, "peak_concurrent": st["peak_running"],
-            "peak_reserved_GB": st["peak_inflight_bytes"] / 1e9}
+            "throughput": {"requests_per_s": len(served) / wall, "rhs_solves_per_s": rhs / wall},
+            "requests_converged": ok, "requests_served": len(served), "rejected_at_admission": rejected,
+            "peak_concurrent": st["peak_running"], "peak_reserved_GB": st["peak_inflight_bytes"] / 1e9,
+            "spectra_reused": st["spectra_reused"], "wall_s": wall}
+
+
+def run_serving(a):
+    """Config: Poisson arrivals (seeded) of aggregate solves, N log-uniform
+    128-32768, Df 1.8-2.8, lambda U[0.3,1.0] um, m as batched, nrhs uniform in
+    2-32; admission by memory footprint, concurrent solves; latency = submit ->
+    result on host.  Two streams of the same requests: the offered rate (200
+    requests/s, far beyond capacity: its p99 is the queue's drain time and its
+    throughput the capacity), then 0.7 x that measured capacity, whose p50 / p99
+    are the latency of a sustainable load (the line's value)."""
+    import bdda
+    count = a.count or 400
+    rng = np.random.default_rng(7)
+    probs = [bdda.random_problem(rng, n_range=(128, 32768), wl_range=(0.3, 1.0), L_range=(2, 32))
+             for _ in range(count)]
+    over = _serve_stream(a, probs, a.rate, 7)
+    sustain_rate = 0.7 * over["throughput"]["requests_per_s"]
+    sus = _serve_stream(a, probs, sustain_rate, 8)
+    ok = over["requests_converged"] == over["requests_served"] and sus["requests_converged"] == sus["requests_served"]
+    line = {"metric": "p99 latency (s) of aggregate solves to 1e-8 under a Poisson request stream at 0.7 x capacity",
+            "value": sus["latency_s"]["p99"], "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 4,
+            "ms_per_step": sus["wall_s"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64 (FFT-MVP, Krylov) + c128 (refinement)", "data": "synthetic (seeded lattice aggregates)",
+            "config": {"workload": f"serving: {count} requests, Poisson (seeded) at 0.7 x the capacity measured "
+                                   f"under {a.rate} req/s, N log-uniform 128-32768, lambda 0.3-1.0 um, "
+                                   f"m 1.3-2.4 + 0-0.9i, nrhs 2-32, true residual <= 1e-8",
+                       "slots": a.slots, "memory_budget_GB": free_budget() / 1e9},
+            "latency_s": sus["latency_s"], "throughput": sus["throughput"], "sustainable": sus,
+            "overload": over}
     print(json.dumps(line), flush=True)
-    return 0 if ok == count_served else 1
+    return 0 if ok else 1
 
 
 def main():

@@ -39,7 +39,7 @@ EXPORTS = [
     "bdda_incident_fields_eh", "bdda_cross_sections_eh", "bdda_read_target_file", "bdda_shape_target",
     "bdda_material_load", "bdda_material_constant", "bdda_material_eval", "bdda_material_destroy",
     "bdda_polarizabilities", "bdda_diag_a", "bdda_op_set_wavenumber", "bdda_sweep", "bdda_mie_q",
-    "bdda_format_result", "bdda_request_footprint_f",
+    "bdda_format_result", "bdda_request_footprint_f", "bdda_server_set_spectrum_cache", "bdda_server_cache_stats",
 ]
 
 SHAPES = {"sphere": 0, "cube": 1, "ellipsoid": 2, "cuboid": 3, "cylinder": 4, "rounded_cylinder": 5}
@@ -180,6 +180,9 @@ def lib(build_if_missing: bool = False):
     L.bdda_server_wait.argtypes = [vp, ct.c_longlong, ct.POINTER(RequestResult)]
     L.bdda_server_stats.argtypes = [vp, dp, ip, ct.POINTER(ct.c_longlong)]
     L.bdda_server_destroy.argtypes = [vp]
+    L.bdda_server_set_spectrum_cache.argtypes = [vp, ct.c_double]
+    L.bdda_server_cache_stats.argtypes = [vp, ct.POINTER(ct.c_longlong), ct.POINTER(ct.c_longlong),
+                                          ct.POINTER(ct.c_double)]
     L.bdda_batch_solve.argtypes = [ct.POINTER(Request), ct.c_int, ct.c_int, ct.c_double, ct.POINTER(SolveOpts),
                                    ct.POINTER(RequestResult)]
     L.bdda_host_fft_line.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int, dp, ip]
@@ -670,7 +673,14 @@ class Server:
     def stats(self):
         pb, pr, done = ct.c_double(), ct.c_int(), ct.c_longlong()
         _check(lib().bdda_server_stats(self._h, ct.byref(pb), ct.byref(pr), ct.byref(done)))
-        return {"peak_inflight_bytes": pb.value, "peak_running": pr.value, "completed": done.value}
+        ru, bu, cb = ct.c_longlong(), ct.c_longlong(), ct.c_double()
+        _check(lib().bdda_server_cache_stats(self._h, ct.byref(ru), ct.byref(bu), ct.byref(cb)))
+        return {"peak_inflight_bytes": pb.value, "peak_running": pr.value, "completed": done.value,
+                "spectra_reused": ru.value, "spectra_built": bu.value, "cached_bytes": cb.value}
+
+    def set_spectrum_cache(self, max_bytes):
+        """Device bytes of idle operators (Green spectra) kept for later requests; 0 disables."""
+        _check(lib().bdda_server_set_spectrum_cache(self._h, float(max_bytes)))
 
     def close(self):
         if self._h:

@@ -126,10 +126,11 @@ k_fft_strided(double2* __restrict__ data, size_t Cc, AxisPlan p, const double2* 
   }
 }
 
-// g[comp][qx][qy][qz] / Ng  ->  ghat[qx][qy][comp][qz], nc components
+// g[comp][qx][qy][qz] / Ng  ->  ghat[qx][qy][comp][green_pos(qz)], nc components
+// (rl = 0: natural order along z; else last-radix-major, see green_perm_radix)
 template <typename C>
 __global__ void k_green_pack(const double2* __restrict__ g, C* __restrict__ out, int nc, int Px, int Py, int Pz,
-                             double scale) {
+                             double scale, int rl) {
   const size_t ng = (size_t)Px * Py * Pz;
   const size_t total = (size_t)nc * ng;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
@@ -138,7 +139,7 @@ __global__ void k_green_pack(const double2* __restrict__ g, C* __restrict__ out,
     const int comp = (int)(t % nc);
     const size_t line = t / nc;  // qx * Py + qy
     double2 v = g[(size_t)comp * ng + line * Pz + qz];
-    out[idx] = cmake((decltype(C::x))(v.x * scale), (decltype(C::x))(v.y * scale));
+    out[idx - qz + green_pos(qz, Pz, rl)] = cmake((decltype(C::x))(v.x * scale), (decltype(C::x))(v.y * scale));
   }
 }
 
@@ -146,7 +147,7 @@ __global__ void k_green_pack(const double2* __restrict__ g, C* __restrict__ out,
 
 cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_im,
                             const double2* twx, const double2* twy, const double2* twz,
-                            double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, cudaStream_t st) {
+                            double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, int gperm, cudaStream_t st) {
   const int Px = g.Px, Py = g.Py, Pz = g.Pz;
   const size_t ng = (size_t)Px * Py * Pz;
   cudaError_t e;
@@ -180,9 +181,9 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
     k_fft_strided<<<grid, kInitWarps * 32, sm, st>>>(work, cc, g.px, twx);
   }
   const double scale = 1.0 / (double)ng;
-  if (ghat_d) k_green_pack<double2><<<2432, 256, 0, st>>>(work, ghat_d, nc, Px, Py, Pz, scale);
-  if (ghat_f) k_green_pack<float2><<<2432, 256, 0, st>>>(work, ghat_f, nc, Px, Py, Pz, scale);
-  if (ghat_df) k_green_pack<dfc><<<2432, 256, 0, st>>>(work, ghat_df, nc, Px, Py, Pz, scale);
+  if (ghat_d) k_green_pack<double2><<<2432, 256, 0, st>>>(work, ghat_d, nc, Px, Py, Pz, scale, 0);
+  if (ghat_f) k_green_pack<float2><<<2432, 256, 0, st>>>(work, ghat_f, nc, Px, Py, Pz, scale, gperm);
+  if (ghat_df) k_green_pack<dfc><<<2432, 256, 0, st>>>(work, ghat_df, nc, Px, Py, Pz, scale, gperm);
   return cudaGetLastError();
 }
 

@@ -14,6 +14,19 @@ constexpr int kTZ = 8;
 constexpr int kTileThreads = kTZ * 32;
 // Warps per CTA of the fused z pass (one (x, y, rhs) task each), at most.
 constexpr int kZWarps = 8;
+// The fused z pass (f = 3) runs its last forward stage, the Green product and
+// its first inverse stage in one sweep (sfft::middle3 / pk::middle3) when the
+// z plan has two or more stages and a last radix Rl <= kFusedMaxRadix; a
+// thread then takes the Rl adjacent frequencies b Rl .. b Rl + Rl - 1 of a
+// butterfly b, so the FP32 and double-float Green spectra of such operators
+// are stored last-radix-major (frequency b Rl + i at i (Pz / Rl) + b): the
+// lanes' loads of one component are then adjacent (coalesced).
+constexpr int kFusedMaxRadix = 5;
+inline int green_perm_radix(int f, const AxisPlan& pz) {
+  return (f == 3 && pz.nst >= 2 && pz.radix[pz.nst - 1] <= kFusedMaxRadix) ? pz.radix[pz.nst - 1] : 0;
+}
+BDDA_HD int green_pos(int p, int N, int rl) { return rl ? (p % rl) * (N / rl) + p / rl : p; }
+
 // Dynamic shared memory one CTA may take (227 KB).
 constexpr int kZSmemMax = 227 * 1024;
 // Warps per CTA of the z pass when each warp needs per_warp bytes of lines.
@@ -30,6 +43,8 @@ struct MvpGeom {
   int Px, Py, Pz;
   AxisPlan px, py, pz;
   int nzt;                     // ceil(nz / kTZ)
+  int gperm;                   // Green spectrum layout along z: 0 natural (ghat[.][c][p]); else the z plan's
+                               // last radix Rl, ghat[.][c][(p % Rl) (Pz / Rl) + p / Rl] (see kFusedMaxRadix)
   int ntiles;                  // (y, z-tile) pairs holding >= 1 dipole
   long long tile_rows;         // sum over those tiles of their valid z count
   const int* occ;              // [nx*ny*nz] dipole index or -1
@@ -45,6 +60,12 @@ template <typename T> struct MvpPrec {
   const C* twz;
   const C* ghat;  // [Px][Py][6 or 9][Pz] (digit-reversed frequencies), divided by Px*Py*Pz
   const float4* twzp = nullptr;  // complex FP32: z twiddle pairs {wx, wx, wy, wy} (packed z pass)
+  // staged tables (stage_twiddles) of the compile-time-plan kernels: x, y, z
+  // (complex FP32), z pairs (packed z pass), z (double-float z pass)
+  const C* twxs = nullptr;
+  const C* twys = nullptr;
+  const C* twzs = nullptr;
+  const float4* twzps = nullptr;
 };
 
 // Timed kernel classes: the five MVP passes per precision (FP32 first), then
@@ -218,10 +239,11 @@ bool launch_pass_c_static_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz,
 
 // Green tensor: build Ghat (FP64 evaluation + FP64 3-D FFT), layout
 // [Px][Py][nc][Pz] with nc = 6 (g.f = 3) or 9 (g.f = 6), for any of the
-// precisions (null pointers skipped).  work: c128 [nc*Px*Py*Pz].
+// precisions (null pointers skipped); the FP32 and double-float outputs in the
+// z layout gperm (green_pos).  work: c128 [nc*Px*Py*Pz].
 cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_im,
                             const double2* twx, const double2* twy, const double2* twz,
-                            double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, cudaStream_t st);
+                            double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, int gperm, cudaStream_t st);
 
 // Radix schedule and shared-memory layout for a 5-smooth 2 <= N <= kMaxLine.
 // three: the fused z pass (three lines per warp), else the single-line tile
@@ -234,5 +256,11 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
 bool make_axis_plan(int N, AxisPlan* p, bool three, bool wide);
 // FP64 twiddle table exp(-2 pi i t / N), t < N.
 void make_twiddles(int N, std::vector<double2>* out);
+// Staged twiddle table of a plan, for the compile-time-plan kernels: stage s
+// (butterfly span M_s, radix R_s, table stride N / (M_s R_s)) holds
+// w^(k n1 N / (M_s R_s)) at offset_s + (k - 1) M_s + n1 for k = 1 .. R_s - 1,
+// n1 < M_s, offset_s = sum over t < s of (R_t - 1) M_t (sfft::Plan::TWO).
+// k-major, so adjacent butterflies of a stage read adjacent entries.
+void stage_twiddles(const AxisPlan& p, std::vector<double2>* out);
 
 }  // namespace bdda

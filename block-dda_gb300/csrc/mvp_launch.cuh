@@ -57,7 +57,7 @@ __device__ __forceinline__ bool skip(const int* done) { return done && *(volatil
 template <typename T>
 __global__ void __launch_bounds__(kZWarps * 32)
 k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int fc, int Px, int Py, int nz, int nzp, AxisPlan pz,
-         const typename cplx<T>::type* __restrict__ twz, const typename cplx<T>::type* __restrict__ ghat,
+         const typename cplx<T>::type* __restrict__ twz, const typename cplx<T>::type* __restrict__ ghat, int gperm,
          const int* done) {
   using C = typename cplx<T>::type;
   if (skip(done)) return;
@@ -82,7 +82,7 @@ k_pass_c(typename cplx<T>::type* __restrict__ t2, int L, int fc, int Px, int Py,
   const int halves = six ? 2 : 1;  // line triples: E, then M
   for (int h = 0; h < halves; ++h) warp_fft_lines<false, 3>(s0 + 3 * h * lw, lw, twz, pz, lane, 32, nz);
   const C* gl = ghat + (size_t)line * (six ? 9 : 6) * Pz;
-  for (int p = lane; p < Pz; p += 32) z_product(s0, lw, skw(p, sh), gl, Pz, p, six);
+  for (int p = lane; p < Pz; p += 32) z_product(s0, lw, skw(p, sh), gl, Pz, green_pos(p, Pz, gperm), six);
   __syncwarp();
   for (int h = 0; h < halves; ++h) warp_fft_lines<true, 3>(s0 + 3 * h * lw, lw, twz, pz, lane);
   for (int z = lane; z < nz; z += 32) {
@@ -130,7 +130,7 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   cudaError_t serr = cudaSuccess;
   auto static_tile = [&](int pass) -> bool {
     if constexpr (std::is_same<T, float>::value) {
-      const TileArgs a{&g, x, ldx, y, ldy, nfield, diag, jpre, t1, t2, p.twx, p.twy, num_sms(), st, done};
+      const TileArgs a{&g, x, ldx, y, ldy, nfield, diag, jpre, t1, t2, p.twxs, p.twys, num_sms(), st, done};
       cudaError_t e = cudaSuccess;
       const bool ok = launch_tile_static(pass, a, &e);
       if (ok && e != cudaSuccess) serr = e;
@@ -162,18 +162,19 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
     bool launched = false;
     if constexpr (std::is_same<T, float>::value) {
       cudaError_t e = cudaSuccess;
-      launched = launch_pass_c_static(g, t2, L, p.twz, p.twzp, p.ghat, st, done, &e);
+      launched = launch_pass_c_static(g, t2, L, p.twzs, p.twzps, p.ghat, st, done, &e);
       if (launched && e != cudaSuccess) return e;
     } else if constexpr (std::is_same<T, dfz>::value) {
       cudaError_t e = cudaSuccess;
-      launched = launch_pass_c_static_df(g, t2, L, p.twz, p.ghat, st, done, &e);
+      launched = launch_pass_c_static_df(g, t2, L, p.twzs, p.ghat, st, done, &e);
       if (launched && e != cudaSuccess) return e;
     }
     if (!launched) {
       const int per_warp = g.f * plan_lw<C>(g.pz) * (int)sizeof(C);
       const int wpc = z_warps_per_cta(per_warp);
       const unsigned grid = (unsigned)((ntask + wpc - 1) / wpc);
-      k_pass_c<T><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.f, g.Px, g.Py, g.nz, g.nzp, g.pz, p.twz, p.ghat, done);
+      k_pass_c<T><<<grid, wpc * 32, wpc * per_warp, st>>>(t2, L, g.f, g.Px, g.Py, g.nz, g.nzp, g.pz, p.twz, p.ghat,
+                                                           g.gperm, done);
     }
     if (timer) timer->end(kPassC + pbase, st);
   }

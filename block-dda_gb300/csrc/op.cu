@@ -159,7 +159,8 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
   using CA = typename cplx<A>::type;
   static_assert(sizeof(CA) == sizeof(C), "storage layouts agree");
   const MvpPrec<T> tb = op->tables<T>();
-  MvpPrec<A> ta{(const CA*)tb.twx, (const CA*)tb.twy, (const CA*)tb.twz, (const CA*)tb.ghat, tb.twzp};
+  MvpPrec<A> ta{(const CA*)tb.twx, (const CA*)tb.twy, (const CA*)tb.twz, (const CA*)tb.ghat, tb.twzp,
+                (const CA*)tb.twxs, (const CA*)tb.twys, (const CA*)tb.twzs, tb.twzps};
   cudaError_t e = launch_block_mvp<A>(g, ta, (const CA*)x, ldx, (CA*)y, ldy, L, (const CA*)diag, (const CA*)jpre,
                                       op->t1[pi].as<CA>(), op->t2[pi].as<CA>(), st, &op->timer, done);
   if (e != cudaSuccess) return cuda_fail(e, "block MVP launch");
@@ -197,12 +198,13 @@ static int build_spectrum(Op* op, double k_re, double k_im) {
     same = same && a.nst == b.nst && std::equal(a.radix, a.radix + a.nst, b.radix);
   }
   const double2 *tx = op->tw64[0].as<double2>(), *ty = op->tw64[1].as<double2>(), *tz = op->tw64[2].as<double2>();
+  const int gperm = green_perm_radix(f, op->plan[0][2]);  // FP32 / double-float spectra for the fused z pass
   BDDA_CUDA(build_green_hat(op->geom(op->dip, 1), lf, k_re, k_im, tx, ty, tz, work.as<double2>(),
                             op->ghat64.as<double2>(), same ? op->ghat32.as<float2>() : nullptr,
-                            op->ghatdf.as<dfc>(), op->stream));
+                            op->ghatdf.as<dfc>(), gperm, op->stream));
   if (!same && op->ghat32.p)
     BDDA_CUDA(build_green_hat(op->geom(op->dip, 0), lf, k_re, k_im, tx, ty, tz, work.as<double2>(), nullptr,
-                              op->ghat32.as<float2>(), nullptr, op->stream));
+                              op->ghat32.as<float2>(), nullptr, gperm, op->stream));
   BDDA_CUDA(wait_stream(op->stream));
   op->kr = k_re;
   op->ki = k_im;
@@ -265,7 +267,27 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     for (size_t t = 0; t < tw.size(); ++t) td[t] = cmake(dfl(tw[t].x), dfl(tw[t].y));
     BDDA_CUDA(op->twdf[i].ensure(td.size() * sizeof(dfc), op->stream));
     BDDA_CUDA(cudaMemcpyAsync(op->twdf[i].p, td.data(), td.size() * sizeof(dfc), cudaMemcpyHostToDevice, op->stream));
-    BDDA_CUDA(wait_stream(op->stream));  // tw / tf die at the end of this iteration
+    // staged tables of the compile-time-plan kernels (radix sequences of plan set 0)
+    std::vector<double2> ts;
+    stage_twiddles(op->plan[0][i], &ts);
+    const size_t nts = std::max<size_t>(ts.size(), 1);
+    std::vector<float2> tsf(nts, make_float2(1.f, 0.f));
+    std::vector<float4> tsp(nts, make_float4(1.f, 1.f, 0.f, 0.f));
+    std::vector<dfc> tsd(nts, cmake(dfl(1.0), dfl(0.0)));
+    for (size_t t = 0; t < ts.size(); ++t) {
+      tsf[t] = make_float2((float)ts[t].x, (float)ts[t].y);
+      tsp[t] = make_float4(tsf[t].x, tsf[t].x, tsf[t].y, tsf[t].y);
+      tsd[t] = cmake(dfl(ts[t].x), dfl(ts[t].y));
+    }
+    BDDA_CUDA(op->tws32[i].ensure(nts * sizeof(float2), op->stream));
+    BDDA_CUDA(cudaMemcpyAsync(op->tws32[i].p, tsf.data(), nts * sizeof(float2), cudaMemcpyHostToDevice, op->stream));
+    if (i == 2) {
+      BDDA_CUDA(op->tws32p.ensure(nts * sizeof(float4), op->stream));
+      BDDA_CUDA(cudaMemcpyAsync(op->tws32p.p, tsp.data(), nts * sizeof(float4), cudaMemcpyHostToDevice, op->stream));
+      BDDA_CUDA(op->twsdf.ensure(nts * sizeof(dfc), op->stream));
+      BDDA_CUDA(cudaMemcpyAsync(op->twsdf.p, tsd.data(), nts * sizeof(dfc), cudaMemcpyHostToDevice, op->stream));
+    }
+    BDDA_CUDA(wait_stream(op->stream));  // tw / tf / ts die at the end of this iteration
   }
   {
     // kernel attributes sized for the largest line, so every live operator fits; once per process

@@ -88,6 +88,9 @@ struct Op {
   AxisPlan plan[2][3];
   DevBuf tw64[3], tw32[3], twdf[3];
   DevBuf tw32p[3];  // complex FP32 twiddle pairs {wx, wx, wy, wy} of the packed z pass ([2] only)
+  // staged twiddles (stage_twiddles) of the compile-time-plan kernels: complex
+  // FP32 per axis, the packed z pass's pairs, the double-float z pass
+  DevBuf tws32[3], tws32p, twsdf;
   DevBuf ghat64, ghat32, ghatdf;
   Occupancy dip;    // dipole occupancy (set_dipoles)
   unsigned long long dip_epoch = 0;  // bumped whenever dip is rebuilt (captured MVPs hold its sizes)
@@ -103,9 +106,10 @@ struct Op {
   unsigned long long buffer_sig() const {
     unsigned long long h = 0;
     for (int i = 0; i < 3; ++i) {
-      for (const DevBuf* b : {&tw64[i], &tw32[i], &twdf[i], &tw32p[i], &t1[i], &t2[i]}) h = sig_add(h, *b);
+      for (const DevBuf* b : {&tw64[i], &tw32[i], &twdf[i], &tw32p[i], &tws32[i], &t1[i], &t2[i]}) h = sig_add(h, *b);
     }
-    for (const DevBuf* b : {&ghat64, &ghat32, &ghatdf, &dip.occ, &dip.tiles, &dip.tmask}) h = sig_add(h, *b);
+    for (const DevBuf* b : {&ghat64, &ghat32, &ghatdf, &tws32p, &twsdf, &dip.occ, &dip.tiles, &dip.tmask})
+      h = sig_add(h, *b);
     return h;
   }
 
@@ -117,6 +121,7 @@ struct Op {
     g.Px = P[0]; g.Py = P[1]; g.Pz = P[2];
     g.px = plan[set][0]; g.py = plan[set][1]; g.pz = plan[set][2];
     g.nzt = (n[2] + kTZ - 1) / kTZ;
+    g.gperm = 0;
     g.ntiles = o.ntiles;
     g.tile_rows = o.tile_rows;
     g.occ = o.occ.as<int>();
@@ -124,7 +129,13 @@ struct Op {
     g.tmask = o.tmask.as<unsigned char>();
     return g;
   }
-  template <typename T> MvpGeom geom(const Occupancy& o) const { return geom(o, sizeof(T) == sizeof(float) ? 0 : 1); }
+  // FP32 and double-float tables: the Green spectra are in the fused z pass's
+  // layout (green_perm_radix); FP64 keeps the natural one
+  template <typename T> MvpGeom geom(const Occupancy& o) const {
+    MvpGeom g = geom(o, sizeof(T) == sizeof(float) ? 0 : 1);
+    g.gperm = sizeof(T) == sizeof(double) ? 0 : green_perm_radix(f, plan[0][2]);
+    return g;
+  }
   template <typename T> MvpPrec<T> tables() const;
   ~Op();
 };
@@ -133,10 +144,12 @@ template <> inline MvpPrec<double> Op::tables<double>() const {
   return {tw64[0].as<double2>(), tw64[1].as<double2>(), tw64[2].as<double2>(), ghat64.as<double2>()};
 }
 template <> inline MvpPrec<float> Op::tables<float>() const {
-  return {tw32[0].as<float2>(), tw32[1].as<float2>(), tw32[2].as<float2>(), ghat32.as<float2>(), tw32p[2].as<float4>()};
+  return {tw32[0].as<float2>(), tw32[1].as<float2>(), tw32[2].as<float2>(), ghat32.as<float2>(), tw32p[2].as<float4>(),
+          tws32[0].as<float2>(), tws32[1].as<float2>(), tws32[2].as<float2>(), tws32p.as<float4>()};
 }
 template <> inline MvpPrec<dfl> Op::tables<dfl>() const {
-  return {twdf[0].as<dfc>(), twdf[1].as<dfc>(), twdf[2].as<dfc>(), ghatdf.as<dfc>()};
+  return {twdf[0].as<dfc>(), twdf[1].as<dfc>(), twdf[2].as<dfc>(), ghatdf.as<dfc>(), nullptr,
+          nullptr, nullptr, twsdf.as<dfc>(), nullptr};
 }
 
 // Arithmetic of the block-MVP kernels for each table precision.

@@ -212,7 +212,8 @@ template <int R, bool INV> __device__ __forceinline__ void dft(cp* v) {
 
 // ---- stages on 16-byte shared-memory elements (compile-time plan P) -------------
 // NP line pairs per warp; pair j's element idx at sm[j * P::LW + P::addr(idx)].
-// tw: twiddle pair table {wx, wx, wy, wy} of exp(-2 pi i t / N), t < N.
+// tw: staged twiddle pair table ({wx, wx, wy, wy} entries, same layout as
+// sfft's staged table: stage s at P::TWO(s), entry (k - 1) M_s + n1).
 template <class P, int s, bool INV, int NP>
 __device__ __forceinline__ void stage(ulonglong2* __restrict__ sm, const float4* __restrict__ tw, int lane, int nv) {
   constexpr int R = P::rad[s];
@@ -220,7 +221,6 @@ __device__ __forceinline__ void stage(ulonglong2* __restrict__ sm, const float4*
   constexpr int Ls = M * R;
   constexpr int B = P::N / R;
   constexpr int T = NP * B;
-  constexpr int ts = P::N / Ls;
   constexpr int off = (s == P::nst - 1) ? 1 : (M / P::Rl) * P::S;
   constexpr bool prune_in = !INV && s == 0;
   constexpr bool prune_out = INV && s == 0;
@@ -239,21 +239,21 @@ __device__ __forceinline__ void stage(ulonglong2* __restrict__ sm, const float4*
     if (!INV) {
       dft<R, false>(v);
       if (M > 1 && n1 != 0) {
-        const int step = n1 * ts;
+        const float4* tws = tw + P::TWO(s) + n1;
 #pragma unroll
         for (int k = 1; k < R; ++k) {
           u64 c, sn;
-          ld_tw(tw + k * step, c, sn);
+          ld_tw(tws + (k - 1) * M, c, sn);
           v[k] = tw_mul(v[k], c, sn);
         }
       }
     } else {
       if (M > 1 && n1 != 0) {
-        const int step = n1 * ts;
+        const float4* tws = tw + P::TWO(s) + n1;
 #pragma unroll
         for (int k = 1; k < R; ++k) {
           u64 c, sn;
-          ld_tw(tw + k * step, c, sn);
+          ld_tw(tws + (k - 1) * M, c, sn);
           v[k] = tw_mulc(v[k], c, sn);
         }
       }
@@ -300,7 +300,7 @@ __device__ __forceinline__ void stage0_from_global(ulonglong2* __restrict__ sm, 
 #pragma unroll
       for (int k = 1; k < R; ++k) {
         u64 c, sn;
-        ld_tw(tw + k * n1, c, sn);
+        ld_tw(tw + (k - 1) * M + n1, c, sn);
         v[k] = tw_mul(v[k], c, sn);
       }
     }
@@ -332,7 +332,7 @@ __device__ __forceinline__ void stage0_to_global(const ulonglong2* __restrict__ 
 #pragma unroll
       for (int k = 1; k < R; ++k) {
         u64 c, sn;
-        ld_tw(tw + k * n1, c, sn);
+        ld_tw(tw + (k - 1) * M + n1, c, sn);
         v[k] = tw_mulc(v[k], c, sn);
       }
     }
@@ -360,14 +360,12 @@ __device__ __forceinline__ void forward_to(ulonglong2* sm, const float4* tw, int
   }
 }
 
-// Largest last-stage radix of the fused middle step: 3 R pair elements, 12 R registers.
-constexpr int kFusedMaxRadix = 5;
-
 // Last forward stage, Green product and first inverse stage of a task's three
 // line pairs in one sweep (the packed form of sfft::middle3): butterfly b of
 // the last stage (M = 1, no twiddles) in all three component pairs, the
-// symmetric 3 x 3 spectrum of each of its R frequencies applied in registers,
-// the inverse DFT, one store.
+// symmetric 3 x 3 spectrum (last-radix-major, green_pos) of each of its R
+// frequencies applied in registers, the inverse DFT, one store.  Used for
+// R <= kFusedMaxRadix (3 R pair elements, 12 R registers).
 template <class P>
 __device__ __forceinline__ void middle3(ulonglong2* __restrict__ sm, const float2* __restrict__ gl, int lane) {
   constexpr int R = P::Rl;
@@ -388,7 +386,7 @@ __device__ __forceinline__ void middle3(ulonglong2* __restrict__ sm, const float
       u64 gr[6], gi[6];
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        const float2 g = ldg_c(gl + c * P::N + idx0 + i);
+        const float2 g = ldg_c(gl + c * P::N + i * B + b);
         gr[c] = dup(g.x);
         gi[c] = dup(g.y);
       }

@@ -272,6 +272,19 @@ void make_twiddles(int N, std::vector<double2>* out) {
   }
 }
 
+void stage_twiddles(const AxisPlan& p, std::vector<double2>* out) {
+  std::vector<double2> w;
+  make_twiddles(p.N, &w);
+  out->clear();
+  int Ls = p.N;
+  for (int s = 0; s < p.nst; ++s) {
+    const int R = p.radix[s], M = Ls / R, ts = p.N / Ls;
+    for (int k = 1; k < R; ++k)
+      for (int n1 = 0; n1 < M; ++n1) out->push_back(w[(size_t)k * n1 * ts]);  // k n1 ts < N
+    Ls = M;
+  }
+}
+
 }  // namespace bdda
 
 extern "C" {

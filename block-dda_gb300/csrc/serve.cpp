@@ -17,6 +17,14 @@
 // Results do not depend on the mix: every solve uses only its own buffers and
 // fixed-order reductions, so a request computes bitwise the same X alone or
 // among others.
+//
+// Spectrum cache: a finished request's operator -- its Green spectra, plans and
+// workspaces, resident in HBM -- is kept idle, keyed by (box, f, lattice
+// spacing, wavenumber, precision), and the next request with the same key
+// takes it instead of rebuilding the spectrum (only its dipoles are set
+// again).  Idle operators count against the memory budget and against a
+// cache limit (a quarter of the budget unless set); the least recently used
+// are destroyed when an admission needs their memory.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -77,6 +85,21 @@ double now_s(std::chrono::steady_clock::time_point t0) {
 }  // namespace
 
 struct bdda_server {
+  // Operator kept idle after its request, with the device bytes it holds.
+  struct OpKey {
+    int n[3], f, prec;
+    double lf, kr, ki;
+    bool operator==(const OpKey& o) const {
+      return n[0] == o.n[0] && n[1] == o.n[1] && n[2] == o.n[2] && f == o.f && prec == o.prec && lf == o.lf &&
+             kr == o.kr && ki == o.ki;
+    }
+  };
+  struct Cached {
+    OpKey key;
+    bdda_op* op;
+    double bytes;
+    unsigned long long tick;
+  };
   struct Item {
     bdda_request req;
     long long ticket;
@@ -99,6 +122,44 @@ struct bdda_server {
   long long completed = 0, next_ticket = 1;
   bool stopping = false;
   std::vector<std::thread> threads;
+  std::vector<Cached> idle;            // idle operators (spectrum cache)
+  double cache_limit = 0, cache_bytes = 0;
+  unsigned long long tick = 0;
+  long long spectra_reused = 0, spectra_built = 0;
+
+  // Take an idle operator with this key out of the cache (caller holds mu).
+  bool take_cached(const OpKey& k, Cached* out) {
+    for (size_t i = 0; i < idle.size(); ++i)
+      if (idle[i].key == k) {
+        *out = idle[i];
+        idle.erase(idle.begin() + i);
+        cache_bytes -= out->bytes;
+        in_use -= out->bytes;
+        return true;
+      }
+    return false;
+  }
+  // Remove the least recently used idle operator (caller holds mu; the caller
+  // destroys it after releasing mu).
+  bdda_op* evict_lru() {
+    size_t j = 0;
+    for (size_t i = 1; i < idle.size(); ++i)
+      if (idle[i].tick < idle[j].tick) j = i;
+    bdda_op* op = idle[j].op;
+    cache_bytes -= idle[j].bytes;
+    in_use -= idle[j].bytes;
+    idle.erase(idle.begin() + j);
+    return op;
+  }
+  // pick(), destroying idle operators (into *ev) while the head of the queue
+  // does not fit (caller holds mu).
+  int pick_evicting(std::vector<bdda_op*>* ev) {
+    for (;;) {
+      const int i = pick();
+      if (i >= 0 || idle.empty() || pending.empty()) return i;
+      ev->push_back(evict_lru());
+    }
+  }
 
   // index of the request to admit now, or -1 (caller holds mu)
   int pick() const {
@@ -110,37 +171,65 @@ struct bdda_server {
     return -1;
   }
 
-  void execute(const Item& it, bdda_request_result* res) {
+  // Runs one admitted request; *reserved is the memory it holds while it runs
+  // (its footprint, or more when it takes a cached operator grown by an
+  // earlier, larger request).  Returns the operator to keep idle, or null.
+  bdda_op* execute(const Item& it, bdda_request_result* res, const OpKey& key, double* reserved) {
     const bdda_request& r = it.req;
     if (dry) {
       // no device work: hold the slot for a time proportional to the footprint
       std::this_thread::sleep_for(std::chrono::microseconds((long long)(it.footprint / 1e6 * 200.0) + 200));
       res->status = BDDA_OK;
-      return;
+      return nullptr;
     }
     bdda_op* op = nullptr;
-    // mixed: FP32 inner solves + double-float residuals; otherwise plain FP64
-    const int prec = opts.precision == BDDA_SOLVE_MIXED ? (BDDA_PREC_FP32 | BDDA_PREC_DF64) : BDDA_PREC_FP64;
-    const int f = r.f == 6 ? 6 : 3;
-    int rc = bdda_op_create(&op, r.n, f, r.lf, r.k_re, r.k_im, prec);
-    // concurrent requests keep the GPU busy between one stream's launches, so
-    // captured poll cycles save nothing here and cost their capture (batched
-    // workload: 245 vs 251 RHS-solves/s with and without them)
-    if (rc == BDDA_OK) rc = bdda_op_set_graphs(op, 0);
+    Cached c{};
+    bool reused = false;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      if (take_cached(key, &c)) {
+        reused = true;
+        op = c.op;
+        const double extra = std::max(0.0, c.bytes - *reserved);  // the operator may hold more than this request needs
+        in_use += extra;
+        peak_in_use = std::max(peak_in_use, in_use);
+        *reserved += extra;
+        ++spectra_reused;
+      } else {
+        ++spectra_built;
+      }
+    }
+    const int f = key.f;
+    int rc = BDDA_OK;
+    if (!reused) {
+      rc = bdda_op_create(&op, r.n, f, r.lf, r.k_re, r.k_im, key.prec);
+      // concurrent requests keep the GPU busy between one stream's launches, so
+      // captured poll cycles save nothing here and cost their capture (batched
+      // workload: 245 vs 251 RHS-solves/s with and without them)
+      if (rc == BDDA_OK) rc = bdda_op_set_graphs(op, 0);
+    }
     if (rc == BDDA_OK) rc = bdda_op_set_dipoles(op, r.address, r.nocc);
     bdda_solve_stats st{};
     if (rc == BDDA_OK) rc = bdda_solve(op, &opts, r.diag, r.B, f * r.nocc, r.X, f * r.nocc, r.L, &st);
-    if (op) bdda_op_destroy(op);
     res->status = rc;
     res->iterations = st.iterations;
     res->refinements = st.refinements;
     res->true_res_max = st.true_res_max;
+    if (op && (rc == BDDA_OK || rc == BDDA_ERR_NOT_CONVERGED) && *reserved <= cache_limit) return op;
+    if (op) bdda_op_destroy(op);
+    return nullptr;
   }
 
   void worker() {
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
-      cv_work.wait(lk, [&] { return (stopping && pending.empty()) || pick() >= 0; });
+      std::vector<bdda_op*> evicted;
+      cv_work.wait(lk, [&] { return (stopping && pending.empty()) || pick_evicting(&evicted) >= 0; });
+      if (!evicted.empty()) {
+        lk.unlock();
+        for (bdda_op* op : evicted) bdda_op_destroy(op);
+        lk.lock();
+      }
       if (stopping && pending.empty()) return;
       const int i = pick();
       if (i < 0) continue;
@@ -155,10 +244,32 @@ struct bdda_server {
       res.t_start = now_s(t0);
       res.footprint_bytes = it.footprint;
       lk.unlock();
-      execute(it, &res);
+      OpKey key{};
+      for (int d = 0; d < 3; ++d) key.n[d] = it.req.n[d];
+      key.f = it.req.f == 6 ? 6 : 3;
+      // mixed: FP32 inner solves + double-float residuals; otherwise plain FP64
+      key.prec = opts.precision == BDDA_SOLVE_MIXED ? (BDDA_PREC_FP32 | BDDA_PREC_DF64) : BDDA_PREC_FP64;
+      key.lf = it.req.lf;
+      key.kr = it.req.k_re;
+      key.ki = it.req.k_im;
+      double reserved = it.footprint;
+      bdda_op* keep = execute(it, &res, key, &reserved);
       res.t_done = now_s(t0);
       lk.lock();
-      in_use -= it.footprint;
+      in_use -= reserved;
+      if (keep) {
+        // keep the operator idle, within the cache limit (oldest first out)
+        std::vector<bdda_op*> out;
+        while (!idle.empty() && cache_bytes + reserved > cache_limit) out.push_back(evict_lru());
+        idle.push_back({key, keep, reserved, ++tick});
+        cache_bytes += reserved;
+        in_use += reserved;
+        if (!out.empty()) {
+          lk.unlock();
+          for (bdda_op* op : out) bdda_op_destroy(op);
+          lk.lock();
+        }
+      }
       --running;
       ++completed;
       done[it.ticket] = res;
@@ -191,6 +302,7 @@ int bdda_server_create(bdda_server** out, int slots, double mem_budget_bytes, co
   bdda_server* s = new bdda_server();
   s->slots = slots;
   s->budget = mem_budget_bytes;
+  s->cache_limit = 0.25 * mem_budget_bytes;
   s->opts = *opts;
   s->dry = dry_run != 0;
   for (int i = 0; i < slots; ++i) s->threads.emplace_back([s] { s->worker(); });
@@ -259,6 +371,34 @@ int bdda_server_stats(bdda_server* s, double* peak_inflight_bytes, int* peak_run
   return BDDA_OK;
 }
 
+int bdda_server_set_spectrum_cache(bdda_server* s, double max_bytes) {
+  if (!s || max_bytes < 0) {
+    bdda::set_error("bad spectrum-cache arguments");
+    return BDDA_ERR_INVALID;
+  }
+  std::vector<bdda_op*> out;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->cache_limit = std::min(max_bytes, s->budget);
+    while (!s->idle.empty() && s->cache_bytes > s->cache_limit) out.push_back(s->evict_lru());
+    s->cv_work.notify_all();
+  }
+  for (bdda_op* op : out) bdda_op_destroy(op);
+  return BDDA_OK;
+}
+
+int bdda_server_cache_stats(bdda_server* s, long long* spectra_reused, long long* spectra_built, double* cached_bytes) {
+  if (!s) {
+    bdda::set_error("null server");
+    return BDDA_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (spectra_reused) *spectra_reused = s->spectra_reused;
+  if (spectra_built) *spectra_built = s->spectra_built;
+  if (cached_bytes) *cached_bytes = s->cache_bytes;
+  return BDDA_OK;
+}
+
 int bdda_server_destroy(bdda_server* s) {
   if (!s) return BDDA_OK;
   {
@@ -267,6 +407,8 @@ int bdda_server_destroy(bdda_server* s) {
     s->cv_work.notify_all();
   }
   for (auto& t : s->threads) t.join();
+  for (auto& c : s->idle) bdda_op_destroy(c.op);
+  s->idle.clear();
   delete s;
   return BDDA_OK;
 }

@@ -7,6 +7,10 @@
 // butterfly element is a per-butterfly base address plus an immediate offset
 // and the index arithmetic divides by constants.
 //
+// Twiddles come from a staged table (stage_twiddles, built on the host from
+// the plan's radices): for each stage its factors, k-major, so that the lanes
+// of a butterfly loop -- adjacent n1 -- load adjacent entries for each k.
+//
 // Layout: element idx = q * R_last + r of a line lives at q * S + r.  Every
 // stage s before the last steps through its butterfly in multiples of R_last
 // (M_s is a multiple of it), so its elements are (M_s / R_last) * S apart; the
@@ -31,6 +35,13 @@ struct Plan {
     return m;
   }
   __device__ static __forceinline__ int addr(int idx) { return (idx / Rl) * S + idx % Rl; }
+  // Offset of stage s in the staged twiddle table (stage_twiddles): stage s
+  // holds w^(k n1 N / (M_s R_s)) at (k - 1) M_s + n1, k = 1 .. R_s - 1, n1 < M_s.
+  static constexpr int TWO(int s) {
+    int o = 0;
+    for (int t = 0; t < s; ++t) o += (rad[t] - 1) * M(t);
+    return o;
+  }
 };
 
 // One stage over NL lines of a warp.  Forward (DIF): DFT then twiddle;
@@ -44,7 +55,6 @@ __device__ __forceinline__ void stage(C* __restrict__ sm, const C* __restrict__ 
   constexpr int Ls = M * R;
   constexpr int B = P::N / R;    // butterflies per line
   constexpr int T = NL * B;      // butterflies of the warp
-  constexpr int ts = P::N / Ls;  // twiddle table stride
   constexpr int off = (s == P::nst - 1) ? 1 : (M / P::Rl) * P::S;
   constexpr bool prune_in = !INV && s == 0;
   constexpr bool prune_out = INV && s == 0;
@@ -63,15 +73,15 @@ __device__ __forceinline__ void stage(C* __restrict__ sm, const C* __restrict__ 
     if (!INV) {
       dft<R, false>(v);
       if (M > 1 && n1 != 0) {
-        const int step = n1 * ts;
+        const C* tws = tw + P::TWO(s) + n1;
 #pragma unroll
-        for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tw + k * step));
+        for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tws + (k - 1) * M));
       }
     } else {
       if (M > 1 && n1 != 0) {
-        const int step = n1 * ts;
+        const C* tws = tw + P::TWO(s) + n1;
 #pragma unroll
-        for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tw + k * step));
+        for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tws + (k - 1) * M));
       }
       dft<R, true>(v);
     }
@@ -108,7 +118,7 @@ __device__ __forceinline__ void stage0_from_global(C* __restrict__ sm, const C* 
     dft<R, false>(v);
     if (M > 1 && n1 != 0) {
 #pragma unroll
-      for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tw + k * n1));
+      for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tw + (k - 1) * M + n1));
     }
     C* p = sm + j * P::LW + P::addr(n1);
 #pragma unroll
@@ -135,7 +145,7 @@ __device__ __forceinline__ void stage0_to_global(const C* __restrict__ sm, const
     for (int i = 0; i < R; ++i) v[i] = p[i * off];
     if (M > 1 && n1 != 0) {
 #pragma unroll
-      for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tw + k * n1));
+      for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tw + (k - 1) * M + n1));
     }
     dft<R, true>(v);
     C* g = gdst + (size_t)j * gstride + n1;
@@ -172,20 +182,18 @@ __device__ __forceinline__ void forward_to(C* sm, const C* tw, int lane, int nv)
   }
 }
 
-// Largest last-stage radix the fused middle step (middle3) runs with: its
-// thread holds the three lines' R elements, 6 R registers for complex FP32.
-template <typename C> constexpr int fused_max_radix() { return sizeof(C) == 8 ? 6 : 5; }
-
 // Last forward stage, Green product and first inverse stage of the three
 // component lines of a z task in one sweep over shared memory.  The last
 // forward stage has M = 1: butterfly b holds the R adjacent elements b R ..
 // b R + R - 1 (at P::addr(b R) + i) and takes no twiddles, and so does the
 // first inverse stage on the same elements; in between, each of the R
-// frequencies is multiplied by the symmetric 3 x 3 Green spectrum (gl[c Pz +
-// idx], components xx xy xz yy yz zz, A = -G of
-// mvp_fft/application_function.cpp:36-40).  A thread does all three lines of
-// its butterfly, so the spectrum is applied in registers: one shared-memory
-// load and store per element instead of the separate stages' three of each.
+// frequencies is multiplied by the symmetric 3 x 3 Green spectrum (components
+// xx xy xz yy yz zz, A = -G of mvp_fft/application_function.cpp:36-40), stored
+// last-radix-major (frequency b R + i of component c at gl[c Pz + i (Pz / R) +
+// b], green_pos), so for each (c, i) the lanes' loads are adjacent.  A thread
+// does all three lines of its butterfly, so the spectrum is applied in
+// registers: one shared-memory load and store per element instead of the
+// separate stages' three of each.
 template <class P, typename C>
 __device__ __forceinline__ void middle3(C* __restrict__ sm, const C* __restrict__ gl, int lane) {
   constexpr int R = P::Rl;
@@ -205,7 +213,7 @@ __device__ __forceinline__ void middle3(C* __restrict__ sm, const C* __restrict_
     dft<R, false>(e2);
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const C* g = gl + idx0 + i;
+      const C* g = gl + i * B + b;
       const C gxx = ldg_c(g), gxy = ldg_c(g + P::N), gxz = ldg_c(g + 2 * P::N);
       const C gyy = ldg_c(g + 3 * P::N), gyz = ldg_c(g + 4 * P::N), gzz = ldg_c(g + 5 * P::N);
       const C x = e0[i], y = e1[i], z = e2[i];
@@ -255,7 +263,6 @@ __device__ __forceinline__ void stage_il(float2* __restrict__ sm, const float2* 
   constexpr int Ls = M * R;
   constexpr int B = P::N / R;
   constexpr int T = 2 * B;
-  constexpr int ts = P::N / Ls;
   constexpr int off = 2 * ((s == P::nst - 1) ? 1 : (M / P::Rl) * P::S);
   constexpr bool prune_in = !INV && s == 0;
   constexpr bool prune_out = INV && s == 0;
@@ -274,15 +281,15 @@ __device__ __forceinline__ void stage_il(float2* __restrict__ sm, const float2* 
     if (!INV) {
       dft<R, false>(v);
       if (M > 1 && n1 != 0) {
-        const int step = n1 * ts;
+        const float2* tws = tw + P::TWO(s) + n1;
 #pragma unroll
-        for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tw + k * step));
+        for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tws + (k - 1) * M));
       }
     } else {
       if (M > 1 && n1 != 0) {
-        const int step = n1 * ts;
+        const float2* tws = tw + P::TWO(s) + n1;
 #pragma unroll
-        for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tw + k * step));
+        for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tws + (k - 1) * M));
       }
       dft<R, true>(v);
     }

@@ -74,7 +74,7 @@ k_pass_c_packed(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp,
   const ptrdiff_t boff = has_b ? (ptrdiff_t)(3 * fstride) : 0;  // right-hand side la + 1
   pk::stage0_from_global<P, 3>(s0, twz, lane, nz, g0, fstride, boff);
   const float2* gl = ghat + (size_t)line * 6 * Pz;
-  if constexpr (P::nst >= 2 && P::Rl <= pk::kFusedMaxRadix) {
+  if constexpr (P::nst >= 2 && P::Rl <= kFusedMaxRadix) {  // the spectrum is last-radix-major
     // last forward stage, product and first inverse stage fused (pk::middle3)
     pk::forward_to<P, 3, 1, P::nst - 1>(s0, twz, lane, nz);
     pk::middle3<P>(s0, gl, lane);

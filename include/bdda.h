@@ -241,7 +241,20 @@ int bdda_server_submit(bdda_server* s, const bdda_request* r, long long* ticket)
 int bdda_server_wait(bdda_server* s, long long ticket, bdda_request_result* res);
 /* Peak reserved memory, peak concurrent requests, completed requests. */
 int bdda_server_stats(bdda_server* s, double* peak_inflight_bytes, int* peak_running, long long* completed);
-/* Drain the queue, join the workers, free the server. */
+/*
+ * Spectrum cache: a finished request's operator (Green spectra, plans and
+ * workspaces, resident in HBM) is kept idle, and a later request with the same
+ * box, f, lattice spacing, wavenumber and precision takes it instead of
+ * rebuilding the spectrum.  Idle operators count against the memory budget
+ * and against max_bytes (default: a quarter of the budget; 0 disables the
+ * cache); the least recently used go first when an admission needs memory.
+ * No counterpart in the reference, which rebuilds everything per target and
+ * wavelength (block_DDA_main.cpp:138-163).
+ */
+int bdda_server_set_spectrum_cache(bdda_server* s, double max_bytes);
+/* Requests that reused a cached operator, operators built, device bytes held idle. */
+int bdda_server_cache_stats(bdda_server* s, long long* spectra_reused, long long* spectra_built, double* cached_bytes);
+/* Drain the queue, join the workers, free the server (and its idle operators). */
 int bdda_server_destroy(bdda_server* s);
 /* Solve `count` requests concurrently (a server submitted all at once). */
 int bdda_batch_solve(const bdda_request* reqs, int count, int slots, double mem_budget_bytes,

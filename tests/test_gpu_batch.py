@@ -89,3 +89,29 @@ def test_server_takes_f6_requests():
     assert r6["status"] == 0 and r6["true_res_max"] <= 1e-8
     assert X6.shape == (6 * nocc, L) and np.array_equal(X6, X_direct)
     assert all(outs[t][1]["status"] == 0 for t in tickets)
+
+
+def test_server_reuses_cached_spectrum_bitwise():
+    """A request with the box, spacing and wavenumber of a finished one takes
+    its idle operator (Green spectra kept in HBM) instead of rebuilding it; the
+    solution is bitwise the one of a fresh operator.  A different wavelength
+    builds a new spectrum; with the cache off nothing is reused."""
+    import dataclasses
+    p = bdda.make_problem(900, 1.9 + 0.3j, seed=41, n_dirs=2)
+    q = bdda.make_problem(900, 1.9 + 0.3j, wl0=0.6, seed=41, n_dirs=2)
+    p2 = dataclasses.replace(p, B=np.asfortranarray(p.B[:, ::-1]))  # same target, other right-hand sides
+    opts = _mixed_opts()
+    srv = bdda.Server(slots=1, mem_budget_bytes=20e9, opts=opts)
+    outs = [srv.wait(srv.submit(x)) for x in (p, q, p2, p)]
+    st = srv.stats()
+    srv.close()
+    assert all(r["status"] == 0 for _, r in outs)
+    assert st["spectra_built"] == 2 and st["spectra_reused"] == 2
+    assert np.array_equal(outs[3][0], outs[0][0])
+    fresh = bdda.Server(slots=1, mem_budget_bytes=20e9, opts=opts)
+    fresh.set_spectrum_cache(0)
+    X2, _ = fresh.wait(fresh.submit(p2))
+    st0 = fresh.stats()
+    fresh.close()
+    assert st0["spectra_reused"] == 0 and st0["cached_bytes"] == 0
+    assert np.array_equal(outs[2][0], X2)
