@@ -81,7 +81,10 @@ Op::~Op() {
   // release every stream-ordered buffer on the operator's stream before it goes away
   solver.reset();
   for (auto* o : {&dip, &cub}) { o->occ.release(); o->tiles.release(); o->tmask.release(); }
-  for (int i = 0; i < 3; ++i) { tw64[i].release(); tw32[i].release(); twdf[i].release(); tw32p[i].release(); }
+  for (int i = 0; i < 3; ++i) {
+    tw64[i].release(); tw32[i].release(); twdf[i].release(); tw32p[i].release(); tws32[i].release();
+  }
+  tws32p.release(); twsdf.release();
   ghat64.release(); ghat32.release(); ghatdf.release();
   for (int i = 0; i < 3; ++i) { t1[i].release(); t2[i].release(); }
   if (stream) {

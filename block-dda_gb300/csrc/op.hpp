@@ -89,7 +89,8 @@ struct Op {
   DevBuf tw64[3], tw32[3], twdf[3];
   DevBuf tw32p[3];  // complex FP32 twiddle pairs {wx, wx, wy, wy} of the packed z pass ([2] only)
   // staged twiddles (stage_twiddles) of the compile-time-plan kernels: complex
-  // FP32 per axis, the packed z pass's pairs, the double-float z pass
+  // FP32 per axis, the packed z pass's pairs, the double-float z pass.  Every
+  // DevBuf of the operator is released in ~Op, before its stream is destroyed.
   DevBuf tws32[3], tws32p, twsdf;
   DevBuf ghat64, ghat32, ghatdf;
   Occupancy dip;    // dipole occupancy (set_dipoles)
