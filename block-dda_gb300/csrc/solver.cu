@@ -21,6 +21,10 @@
 
 namespace bdda {
 
+// Iteration cap of an FP32 inner solve of a mixed refinement whose operator
+// holds FP64 tables (the FP64 fallback of the refinement loop).
+constexpr int kMixedInnerCap = 400;
+
 // ---------------------------------------------------------------------------
 // small-state slots (each L x L complex FP64, column-major)
 // ---------------------------------------------------------------------------
@@ -1026,7 +1030,11 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
       if (o->jacobi) k_rowscale<float, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n, cf);
       else k_convert<float, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n, cf);
       op->timer.count(kOther);
-      BDDA_TRY(k32.run(o->solver, Bp, D, full, tol, itermax, &it, &er, &stt));
+      // with FP64 tables to fall back on, an FP32 inner solve that has not met
+      // its tolerance after kMixedInnerCap iterations (well-posed systems need
+      // tens) ends there, and the refinement decides whether to switch
+      const int imax = (refine && (op->prec & BDDA_PREC_FP64)) ? std::min(itermax, kMixedInnerCap) : itermax;
+      BDDA_TRY(k32.run(o->solver, Bp, D, full, tol, imax, &it, &er, &stt));
       if (accumulate) k_accumulate<float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd, cfi);
       else k_convert<double, float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd, cfi);
       op->timer.count(kOther);

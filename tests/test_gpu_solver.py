@@ -176,3 +176,31 @@ def test_solve_status_codes():
     assert ei.value.code == bdda.ERR_INVALID
     with pytest.raises(bdda.BddaError):
         bdda.solve(op, prob.diag, np.zeros((3 * prob.nocc, 33)), bdda.solve_opts())
+
+
+def test_mixed_solve_falls_back_to_fp64_inner_solves():
+    """The reference's N1024 aggregate with its own site volumes (spheres of
+    radius d on a lattice of spacing d) at m = 1.78 is so ill-conditioned that
+    FP32 Krylov stagnates (FP64 COCG-RQ needs ~350 iterations); the mixed
+    refinement must switch to FP64 inner solves and still reach the true
+    residual, with the FP64 solve's cross sections."""
+    import os
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "target_N1024.npz"))
+    addr = np.cumsum(d["address_delta"].astype(np.int64)).astype(np.int32)
+    n = tuple(int(v) for v in d["n"])
+    prob = bdda.target_problem(n, float(d["lf"]), addr, float(d["vol"]), 1.78, wl0=0.55, seed=1, n_dirs=4)
+    op = bdda.Operator(prob.n, prob.lf, prob.k)
+    op.set_dipoles(prob.address)
+    X64, s64 = bdda.solve(op, prob.diag, prob.B, bdda.solve_opts("cocg_rq", precision=bdda.SOLVE_FP64, true_tol=1e-8,
+                                                                  itermax=3000), allow_not_converged=False)
+    Xm, sm = bdda.solve(op, prob.diag, prob.B, bdda.solve_opts("cocg_rq", precision=bdda.SOLVE_MIXED, true_tol=1e-8,
+                                                                itermax=3000), allow_not_converged=False)
+    assert s64["iterations"] > 200
+    assert sm["status"] == 0 and sm["true_res_max"] <= 1e-8 and sm["fp64_inner_steps"] >= 1
+    res = krylov.true_residual(_oracle_amul(prob), prob.B, Xm)
+    assert np.all(res < 2e-8), res
+    cm = bdda.cross_sections(prob.k, prob.alpha[0], prob.B, Xm)
+    c64 = bdda.cross_sections(prob.k, prob.alpha[0], prob.B, X64)
+    for a, b in (cm[0], c64[0]), (cm[2], c64[2]):  # Cext, Csca (real m: Cabs is rounding noise)
+        assert np.max(np.abs(a - b) / np.abs(b)) < 1e-6
