@@ -40,6 +40,7 @@ EXPORTS = [
     "bdda_material_load", "bdda_material_constant", "bdda_material_eval", "bdda_material_destroy",
     "bdda_polarizabilities", "bdda_diag_a", "bdda_op_set_wavenumber", "bdda_sweep", "bdda_mie_q",
     "bdda_format_result", "bdda_request_footprint_f", "bdda_server_set_spectrum_cache", "bdda_server_cache_stats",
+    "bdda_op_set_autotune", "bdda_op_get_tuning",
 ]
 
 SHAPES = {"sphere": 0, "cube": 1, "ellipsoid": 2, "cuboid": 3, "cylinder": 4, "rounded_cylinder": 5}
@@ -169,6 +170,8 @@ def lib(build_if_missing: bool = False):
     L.bdda_op_mvp_bytes.argtypes = [vp, ct.c_int, ct.c_int, ct.c_int, ct.c_int, dp]
     L.bdda_op_set_timing.argtypes = [vp, ct.c_int]
     L.bdda_op_set_graphs.argtypes = [vp, ct.c_int]
+    L.bdda_op_set_autotune.argtypes = [vp, ct.c_int]
+    L.bdda_op_get_tuning.argtypes = [vp, ct.c_int, ip, ct.POINTER(ct.c_float)]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
     L.bdda_last_error.restype = ct.c_char_p
     L.bdda_request_footprint.argtypes = [ip, ct.c_int, ct.c_int, ct.c_int]
@@ -262,6 +265,13 @@ class Operator:
         _check(lib().bdda_op_info(self._h, _iptr(P), ct.byref(nocc), ct.byref(nl)))
         return tuple(int(v) for v in P), nocc.value, nl.value
 
+    def plans(self):
+        """Radix sequences of the complex FP32 FFT plans per axis (x, y: the
+        tile passes' tables; z: the fused z pass's table)."""
+        P, _, _ = self.info()
+        return {ax: host_fft_line(np.zeros(P[i]), prec=PREC_FP32, max_radix=16 if i == 2 else 8)[1]
+                for i, ax in enumerate("xyz")}
+
     def mbt_fft_mvp(self, p_hat):
         """Reference ``MBT_fft_mvp`` on a full cuboid vector (host, complex128)."""
         x = np.ascontiguousarray(p_hat, dtype=np.complex128)
@@ -296,6 +306,23 @@ class Operator:
     def set_graphs(self, on=True):
         """Captured CUDA graphs for the solvers' poll cycles (default on); off: launch by launch."""
         _check(lib().bdda_op_set_graphs(self._h, 1 if on else 0))
+
+    def set_autotune(self, on=True):
+        """Measured FFT launch schedule for the complex FP32 MVP (default on)."""
+        _check(lib().bdda_op_set_autotune(self._h, 1 if on else 0))
+
+    def tuning(self, L):
+        """(schedule dict, candidate ms dict, measured?) for nrhs L (bdda_op_get_tuning)."""
+        sch = np.zeros(4, np.int32)
+        ms = (ct.c_float * 13)()
+        rc = lib().bdda_op_get_tuning(self._h, int(L), _iptr(sch), ms)
+        _check(rc, (ERR_NOT_CONVERGED,))
+        cand = {"y": {f"buf{1 + i // 4}_waves{(1, 2, 4, 8)[i % 4]}": ms[i] for i in range(8)},
+                "z_pass": {"scalar": ms[8], "packed": ms[9]},
+                "x_cta_per_sm": {str(v): ms[10 + i] for i, v in enumerate((5, 10, 20))}}
+        return ({"y_waves": int(sch[0]), "y_buffers": int(sch[1]),
+                 "z_pass": {-1: "default", 0: "scalar", 1: "packed"}[int(sch[2])], "x_cta_per_sm": int(sch[3])},
+                cand, rc == OK)
 
     def kernel_stats(self, reset=False):
         n = len(KERNEL_NAMES)

@@ -183,7 +183,7 @@ cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_i
   const double scale = 1.0 / (double)ng;
   if (ghat_d) k_green_pack<double2><<<2432, 256, 0, st>>>(work, ghat_d, nc, Px, Py, Pz, scale, 0);
   if (ghat_f) k_green_pack<float2><<<2432, 256, 0, st>>>(work, ghat_f, nc, Px, Py, Pz, scale, gperm);
-  if (ghat_df) k_green_pack<dfc><<<2432, 256, 0, st>>>(work, ghat_df, nc, Px, Py, Pz, scale, gperm);
+  if (ghat_df) k_green_pack<dfc><<<2432, 256, 0, st>>>(work, ghat_df, nc, Px, Py, Pz, scale, 0);
   return cudaGetLastError();
 }
 

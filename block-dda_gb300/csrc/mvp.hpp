@@ -18,10 +18,12 @@ constexpr int kZWarps = 8;
 // its first inverse stage in one sweep (sfft::middle3 / pk::middle3) when the
 // z plan has two or more stages and a last radix Rl <= kFusedMaxRadix; a
 // thread then takes the Rl adjacent frequencies b Rl .. b Rl + Rl - 1 of a
-// butterfly b, so the FP32 and double-float Green spectra of such operators
-// are stored last-radix-major (frequency b Rl + i at i (Pz / Rl) + b): the
-// lanes' loads of one component are then adjacent (coalesced).
+// butterfly b, so the complex FP32 Green spectrum of such operators is stored
+// last-radix-major (frequency b Rl + i at i (Pz / Rl) + b): the lanes' loads
+// of one component are then adjacent (coalesced).
 constexpr int kFusedMaxRadix = 5;
+// (complex FP32 only: the double-float fused step needs 168 registers and ran
+// slower than the separate stages, 54.9 vs 41.6 ms per N=65536, L=32 pass.)
 inline int green_perm_radix(int f, const AxisPlan& pz) {
   return (f == 3 && pz.nst >= 2 && pz.radix[pz.nst - 1] <= kFusedMaxRadix) ? pz.radix[pz.nst - 1] : 0;
 }
@@ -35,6 +37,16 @@ inline int z_warps_per_cta(int per_warp) {
   return w < 1 ? 1 : (w > kZWarps ? kZWarps : w);
 }
 
+// Launch schedule of a block MVP's tile passes, chosen per operator and nrhs
+// by the autotuner (op.cu: candidates timed with CUDA events on the operator's
+// own buffers) or left at the defaults.
+struct MvpTune {
+  int zpacked = -1;  // pass C: -1 the default rule (packed where three 8-warp CTAs fit), 0 scalar, 1 packed
+  int ywaves = 4;    // passes B, D: grid of this many waves of the CTAs resident per SM
+  int ybuf = 2;      // passes B, D: tile buffers per CTA (2: prefetch the next task; 1: twice the CTAs)
+  int xcta = 10;     // passes A, E: aim at this many CTAs per SM (fields split into groups)
+};
+
 // Geometry shared by both precisions (device pointers).
 struct MvpGeom {
   int f;                       // components per dipole: 3 (E) or 6 (E, M)
@@ -45,6 +57,8 @@ struct MvpGeom {
   int nzt;                     // ceil(nz / kTZ)
   int gperm;                   // Green spectrum layout along z: 0 natural (ghat[.][c][p]); else the z plan's
                                // last radix Rl, ghat[.][c][(p % Rl) (Pz / Rl) + p / Rl] (see kFusedMaxRadix)
+  MvpTune tune;                // launch schedule of the tile passes
+  unsigned passes = 0x1fu;     // passes launched (bit 0 = A .. bit 4 = E); the autotuner times them one by one
   int ntiles;                  // (y, z-tile) pairs holding >= 1 dipole
   long long tile_rows;         // sum over those tiles of their valid z count
   const int* occ;              // [nx*ny*nz] dipole index or -1
@@ -201,7 +215,8 @@ struct TileArgs {
 enum TilePass { kTileA = 0, kTileB, kTileD, kTileE };
 
 // Grid of the y passes (B, D), whose CTAs take tasks (field, x, z tile) in a
-// fixed stride: four waves of the CTAs resident per SM.  Measured on the
+// fixed stride: by default four waves of the CTAs resident per SM
+// (MvpTune::ywaves).  Measured on the
 // column-pair passes (N=16384 / 8192, tasks of uneven cost: empty rows are
 // skipped): one exact wave 0.244 / 0.146 ms (forward), two 0.239 / 0.138,
 // four 0.233 / 0.135; the earlier fixed 8 CTAs per SM (1.1-1.6 waves) 0.239 /
@@ -209,12 +224,12 @@ enum TilePass { kTileA = 0, kTileB, kTileD, kTileE };
 constexpr int kYWaves = 4;
 
 // Fields per CTA of the x passes (A, E), an even number: a tile's fields are
-// split over groups of CTAs so that a launch has about two waves of five CTAs
-// per multiprocessor (one CTA per tile left most of the GPU idle: 301 tiles
-// at N=8192).  Returns the number of groups.
-inline int x_field_groups(int nfield, int ntiles, int sms, int* fpg) {
+// split over groups of CTAs so that a launch has about xcta CTAs per
+// multiprocessor (default 10: two waves of five; one CTA per tile left most
+// of the GPU idle: 301 tiles at N=8192).  Returns the number of groups.
+inline int x_field_groups(int nfield, int ntiles, int sms, int* fpg, int xcta = 10) {
   const int pairs = (nfield + 1) / 2;
-  const int want = (10 * sms + ntiles - 1) / ntiles;
+  const int want = (xcta * sms + ntiles - 1) / ntiles;
   const int groups = want < 1 ? 1 : (want < pairs ? want : pairs);
   *fpg = 2 * ((pairs + groups - 1) / groups);
   return (nfield + *fpg - 1) / *fpg;
@@ -232,6 +247,10 @@ bool launch_tile_static(int pass, const TileArgs& a, cudaError_t* err);
 bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz, const float4* twzp, const float2* ghat,
                           cudaStream_t st, const int* done, cudaError_t* err);
 
+// Whether the packed-pair pass C can run for z length Pz and f (an autotuner
+// candidate besides the scalar kernel).
+bool packed_z_available(int Pz, int f);
+
 // Pass C of a double-float block MVP (f = 3) with the compile-time z plan of
 // g.Pz; false (nothing launched) when g.Pz has none or f = 6.
 bool launch_pass_c_static_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz, const dfzc* ghat, cudaStream_t st,
@@ -239,8 +258,8 @@ bool launch_pass_c_static_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz,
 
 // Green tensor: build Ghat (FP64 evaluation + FP64 3-D FFT), layout
 // [Px][Py][nc][Pz] with nc = 6 (g.f = 3) or 9 (g.f = 6), for any of the
-// precisions (null pointers skipped); the FP32 and double-float outputs in the
-// z layout gperm (green_pos).  work: c128 [nc*Px*Py*Pz].
+// precisions (null pointers skipped); the complex FP32 output in the z layout
+// gperm (green_pos), the others natural.  work: c128 [nc*Px*Py*Pz].
 cudaError_t build_green_hat(const MvpGeom& g, double lf, double k_re, double k_im,
                             const double2* twx, const double2* twy, const double2* twz,
                             double2* work, double2* ghat_d, float2* ghat_f, dfc* ghat_df, int gperm, cudaStream_t st);

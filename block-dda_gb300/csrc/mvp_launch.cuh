@@ -120,11 +120,13 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   auto grid_y = [&](auto kernel, int smem) {
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kTileThreads, smem) != cudaSuccess || nb < 1) nb = 1;
-    return std::min(ntask_y, kYWaves * nb * num_sms());
+    return std::min(ntask_y, g.tune.ywaves * nb * num_sms());
   };
   const tile::RtLine<C> lx{g.px}, ly{g.py};
   int xfpg = 0;  // x passes: fields per CTA
-  const dim3 xgrid(g.ntiles, x_field_groups(nfield, g.ntiles, num_sms(), &xfpg));
+  const dim3 xgrid(g.ntiles, x_field_groups(nfield, g.ntiles, num_sms(), &xfpg, g.tune.xcta));
+  const bool runA = g.passes & 1u, runB = g.passes & 2u, runC = g.passes & 4u, runD = g.passes & 8u,
+             runE = g.passes & 16u;
   // Strided pass `pass` with the compile-time plan of its axis (complex FP32);
   // false when it was not launched that way.
   cudaError_t serr = cudaSuccess;
@@ -141,22 +143,22 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
     }
   };
   // A
-  if (timer) timer->begin(kPassA + pbase, st);
-  if (!static_tile(kTileA))
+  if (runA && timer) timer->begin(kPassA + pbase, st);
+  if (runA && !static_tile(kTileA))
     tile::k_pass_a<T><<<xgrid, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
         x, ldx, nfield, xfpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, t1, done);
-  if (timer) timer->end(kPassA + pbase, st);
+  if (runA && timer) timer->end(kPassA + pbase, st);
   if (serr != cudaSuccess) return serr;
   // B
-  if (timer) timer->begin(kPassB + pbase, st);
-  if (!static_tile(kTileB))
+  if (runB && timer) timer->begin(kPassB + pbase, st);
+  if (runB && !static_tile(kTileB))
     tile::k_pass_y<T, false><<<grid_y(tile::k_pass_y<T, false, tile::RtLine<C>>, tile::smem_tile<T>(plan_lw<C>(g.py), 0)),
                                kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
         t1, t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, done);
-  if (timer) timer->end(kPassB + pbase, st);
+  if (runB && timer) timer->end(kPassB + pbase, st);
   if (serr != cudaSuccess) return serr;
   // C
-  {
+  if (runC) {
     const long long ntask = (long long)g.Px * g.Py * L;
     if (timer) timer->begin(kPassC + pbase, st);
     bool launched = false;
@@ -179,19 +181,19 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
     if (timer) timer->end(kPassC + pbase, st);
   }
   // D
-  if (timer) timer->begin(kPassD + pbase, st);
-  if (!static_tile(kTileD))
+  if (runD && timer) timer->begin(kPassD + pbase, st);
+  if (runD && !static_tile(kTileD))
     tile::k_pass_y<T, true><<<grid_y(tile::k_pass_y<T, true, tile::RtLine<C>>, tile::smem_tile<T>(plan_lw<C>(g.py), 0)),
                               kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
         t2, t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, done);
-  if (timer) timer->end(kPassD + pbase, st);
+  if (runD && timer) timer->end(kPassD + pbase, st);
   if (serr != cudaSuccess) return serr;
   // E
-  if (timer) timer->begin(kPassE + pbase, st);
-  if (!static_tile(kTileE))
+  if (runE && timer) timer->begin(kPassE + pbase, st);
+  if (runE && !static_tile(kTileE))
     tile::k_pass_e<T><<<xgrid, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
         t1, nfield, xfpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, done);
-  if (timer) timer->end(kPassE + pbase, st);
+  if (runE && timer) timer->end(kPassE + pbase, st);
   if (serr != cudaSuccess) return serr;
   return cudaGetLastError();
 }

@@ -136,6 +136,93 @@ int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o) {
   return BDDA_OK;
 }
 
+// Measured choice of the tile passes' launch schedule for a complex FP32 block
+// MVP of L columns (the FFT schedules: y-pass grid waves, scalar or packed z
+// pass, x-pass CTAs per SM).  Each candidate is launched alone on the
+// operator's own workspace -- pass A reads x and writes T1, B reads T1 and
+// writes T2, C works in place on T2, so re-running them is harmless -- three
+// times with CUDA events, and the fastest is kept.  Runs once per operator and
+// nrhs, outside stream capture, for workspaces of at least kTuneMinBytes (below
+// that the MVP is bound by launch latency and the defaults are kept); a
+// process-wide table keyed by the geometry lets later operators of the same
+// box, occupancy and nrhs skip the measurement.
+constexpr size_t kTuneMinBytes = 64ull << 20;
+
+static std::mutex g_tune_mu;
+static std::map<std::string, Op::TuneRec> g_tune_cache;
+
+static std::string tune_key(const MvpGeom& g, int L) {
+  return std::to_string(g.f) + ":" + std::to_string(g.nx) + "," + std::to_string(g.ny) + "," + std::to_string(g.nz) +
+         ":" + std::to_string(g.ntiles) + ":" + std::to_string(g.tile_rows) + ":" + std::to_string(L);
+}
+
+static cudaError_t autotune_f32(Op* op, MvpGeom g, const MvpPrec<float>& p, const float2* x, int ldx, int L,
+                                float2* t1, float2* t2, cudaStream_t st, Op::TuneRec* out) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  auto timed = [&](unsigned passes, const MvpTune& t, float* ms) -> cudaError_t {
+    g.tune = t;
+    g.passes = passes;
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaError_t r = cudaEventRecord(a, st);
+      if (r == cudaSuccess) r = launch_block_mvp<float>(g, p, x, ldx, nullptr, ldx, L, nullptr, nullptr, t1, t2, st,
+                                                        nullptr, nullptr);
+      if (r == cudaSuccess) r = cudaEventRecord(b, st);
+      if (r == cudaSuccess) r = cudaEventSynchronize(b);
+      float t_ms = 0.f;
+      if (r == cudaSuccess) r = cudaEventElapsedTime(&t_ms, a, b);
+      if (r != cudaSuccess) return r;
+      best = std::min(best, t_ms);
+    }
+    *ms = best;
+    return cudaSuccess;
+  };
+  Op::TuneRec rec{};
+  for (float& v : rec.ms) v = -1.f;
+  MvpTune t;  // defaults
+  float dummy = 0.f;
+  if (e == cudaSuccess) e = timed(1u, t, &dummy);  // pass A fills T1
+  const int yw[4] = {1, 2, 4, 8};
+  int best = -1;
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i) {  // y pass: buffers 1, 2 x waves 1, 2, 4, 8
+    MvpTune c = t;
+    c.ybuf = 1 + i / 4;
+    c.ywaves = yw[i % 4];
+    e = timed(2u, c, &rec.ms[i]);
+    if (e == cudaSuccess && (best < 0 || rec.ms[i] < rec.ms[best])) best = i;
+  }
+  if (e == cudaSuccess) {
+    t.ybuf = 1 + best / 4;
+    t.ywaves = yw[best % 4];
+  }
+  if (e == cudaSuccess && packed_z_available(g.Pz, g.f) && p.twzps) {
+    MvpTune c = t;
+    c.zpacked = 0;
+    e = timed(4u, c, &rec.ms[8]);
+    c.zpacked = 1;
+    if (e == cudaSuccess) e = timed(4u, c, &rec.ms[9]);
+    if (e == cudaSuccess) t.zpacked = rec.ms[9] < rec.ms[8] ? 1 : 0;
+  }
+  const int xc[3] = {5, 10, 20};
+  best = -1;
+  for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
+    MvpTune c = t;
+    c.xcta = xc[i];
+    e = timed(1u, c, &rec.ms[10 + i]);
+    if (e == cudaSuccess && (best < 0 || rec.ms[10 + i] < rec.ms[10 + best])) best = i;
+  }
+  if (e == cudaSuccess) t.xcta = xc[best];
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  rec.tune = t;
+  rec.measured = e == cudaSuccess;
+  *out = rec;
+  (void)op;
+  return e;
+}
+
 template <typename T>
 int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, int ldx, typename cplx<T>::type* y, int ldy,
                  int L, const typename cplx<T>::type* diag, const typename cplx<T>::type* jpre, cudaStream_t st,
@@ -164,6 +251,32 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
   const MvpPrec<T> tb = op->tables<T>();
   MvpPrec<A> ta{(const CA*)tb.twx, (const CA*)tb.twy, (const CA*)tb.twz, (const CA*)tb.ghat, tb.twzp,
                 (const CA*)tb.twxs, (const CA*)tb.twys, (const CA*)tb.twzs, tb.twzps};
+  if constexpr (std::is_same<T, float>::value) {
+    auto it = op->tuned.find(L);
+    if (it != op->tuned.end()) {
+      g.tune = it->second.tune;
+    } else if (op->autotune && &o == &op->dip && mvp_t2_elems(g, L) * sizeof(C) >= kTuneMinBytes) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      BDDA_CUDA(cudaStreamIsCapturing(st, &cs));
+      if (cs == cudaStreamCaptureStatusNone) {
+        const std::string key = tune_key(g, L);
+        Op::TuneRec rec{};
+        bool have = false;
+        {
+          std::lock_guard<std::mutex> lk(g_tune_mu);
+          auto c = g_tune_cache.find(key);
+          if (c != g_tune_cache.end()) { rec = c->second; have = true; }
+        }
+        if (!have) {
+          BDDA_CUDA(autotune_f32(op, g, ta, x, ldx, L, op->t1[pi].as<float2>(), op->t2[pi].as<float2>(), st, &rec));
+          std::lock_guard<std::mutex> lk(g_tune_mu);
+          g_tune_cache[key] = rec;
+        }
+        op->tuned[L] = rec;
+        g.tune = rec.tune;
+      }
+    }
+  }
   cudaError_t e = launch_block_mvp<A>(g, ta, (const CA*)x, ldx, (CA*)y, ldy, L, (const CA*)diag, (const CA*)jpre,
                                       op->t1[pi].as<CA>(), op->t2[pi].as<CA>(), st, &op->timer, done);
   if (e != cudaSuccess) return cuda_fail(e, "block MVP launch");
@@ -410,6 +523,29 @@ int bdda_op_set_graphs(bdda_op* op, int on) {
   std::lock_guard<std::mutex> lk(op->mu);
   op->graphs = on != 0;
   return BDDA_OK;
+}
+
+int bdda_op_set_autotune(bdda_op* op, int on) {
+  if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(op->mu);
+  op->autotune = on != 0;
+  op->tuned.clear();
+  return BDDA_OK;
+}
+
+int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[13]) {
+  if (!op || !schedule) { set_error("null argument"); return BDDA_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(op->mu);
+  const MvpTune def;
+  auto it = op->tuned.find(L);
+  const MvpTune& t = it != op->tuned.end() ? it->second.tune : def;
+  schedule[0] = t.ywaves;
+  schedule[1] = t.ybuf;
+  schedule[2] = t.zpacked;
+  schedule[3] = t.xcta;
+  if (candidate_ms)
+    for (int i = 0; i < 13; ++i) candidate_ms[i] = it != op->tuned.end() ? it->second.ms[i] : -1.f;
+  return it != op->tuned.end() && it->second.measured ? BDDA_OK : BDDA_ERR_NOT_CONVERGED;
 }
 
 int bdda_op_set_timing(bdda_op* op, int enable) {

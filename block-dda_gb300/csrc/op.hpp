@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -102,6 +103,14 @@ struct Op {
   std::mutex mu;
   std::shared_ptr<SolverWork> solver;   // cached Krylov workspace (solver.cu)
   bool graphs = true;  // solvers' poll cycles as captured graphs (bdda_op_set_graphs)
+  // Autotuned launch schedule of the complex FP32 block MVP, per nrhs
+  // (bdda_op_set_autotune, bdda_op_get_tuning); candidate times in ms:
+  // [0..7] pass B with 1 then 2 buffers x 1, 2, 4, 8 waves, [8..9] pass C
+  // scalar / packed, [10..12] pass A at 5, 10, 20 CTAs per SM; negative: not
+  // a candidate.
+  struct TuneRec { MvpTune tune; float ms[13]; bool measured; };
+  bool autotune = true;
+  std::map<int, TuneRec> tuned;
 
   // signature of every buffer a block MVP's kernels are launched with
   unsigned long long buffer_sig() const {
@@ -130,11 +139,11 @@ struct Op {
     g.tmask = o.tmask.as<unsigned char>();
     return g;
   }
-  // FP32 and double-float tables: the Green spectra are in the fused z pass's
-  // layout (green_perm_radix); FP64 keeps the natural one
+  // complex FP32 tables: the Green spectrum is in the fused z pass's layout
+  // (green_perm_radix); FP64 and double-float keep the natural one
   template <typename T> MvpGeom geom(const Occupancy& o) const {
     MvpGeom g = geom(o, sizeof(T) == sizeof(float) ? 0 : 1);
-    g.gperm = sizeof(T) == sizeof(double) ? 0 : green_perm_radix(f, plan[0][2]);
+    g.gperm = sizeof(T) == sizeof(float) ? green_perm_radix(f, plan[0][2]) : 0;
     return g;
   }
   template <typename T> MvpPrec<T> tables() const;

@@ -207,6 +207,8 @@ struct bdda_server {
       // captured poll cycles save nothing here and cost their capture (batched
       // workload: 245 vs 251 RHS-solves/s with and without them)
       if (rc == BDDA_OK) rc = bdda_op_set_graphs(op, 0);
+      // one solve per operator: measuring its FFT schedule would cost more than it saves
+      if (rc == BDDA_OK) rc = bdda_op_set_autotune(op, 0);
     }
     if (rc == BDDA_OK) rc = bdda_op_set_dipoles(op, r.address, r.nocc);
     bdda_solve_stats st{};

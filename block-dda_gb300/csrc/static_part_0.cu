@@ -41,6 +41,19 @@ bool launch_pass_c_static_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz,
          static_z_df_part2(g, t2, L, twz, ghat, st, done, err) || static_z_df_part3(g, t2, L, twz, ghat, st, done, err);
 }
 
+bool packed_z_available(int Pz, int f) {
+  if (f != 3) return false;
+  switch (Pz) {
+#define BDDA_ZPLAN(I, N, S, LW, ...) \
+  case N:                            \
+    return zpacked::fits<sfft::Plan<N, S, LW, __VA_ARGS__>>();
+#include "zplans.inc"
+#undef BDDA_ZPLAN
+    default:
+      return false;
+  }
+}
+
 bool launch_tile_static(int pass, const TileArgs& a, cudaError_t* err) {
   return static_tile_part0(pass, a, err) || static_tile_part1(pass, a, err) || static_tile_part2(pass, a, err) ||
          static_tile_part3(pass, a, err);

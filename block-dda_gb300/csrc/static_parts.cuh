@@ -20,7 +20,7 @@ bool dispatch_z(const MvpGeom& g, float2* t2, int L, const float2* twz, const fl
   case N:                                                                                \
     if constexpr ((I) % kParts == PART) {                                                \
       using Pl = sfft::Plan<N, S, LW, __VA_ARGS__>;                                      \
-      *err = (twzp && g.f == 3 && zpacked::worth<Pl>()) ? zpacked::launch<Pl>(g, t2, L, twzp, ghat, st, done) \
+      *err = zpacked::chosen<Pl>(g, twzp) ? zpacked::launch<Pl>(g, t2, L, twzp, ghat, st, done) \
                                 : zstatic::launch<Pl>(g, t2, L, twz, ghat, st, done);    \
       return true;                                                                       \
     }                                                                                    \

@@ -182,18 +182,22 @@ constexpr int kTZ2 = 2 * kTZ;
 // staged and stored one column pair -- 16 contiguous bytes, since rows are
 // padded to a multiple of 4 elements -- per copy (a copy per column left the
 // warps stalled on the shared-memory queue).  A pair whose second column is
-// row padding transforms it and never stores it.
+// row padding transforms it and never stores it.  NBUF = 2: the next task's
+// tile is prefetched by cp.async into the second buffer while the current one
+// is transformed; NBUF = 1: one buffer, so twice the CTAs fit on an SM
+// (the autotuner picks; N=65536, Py=270: 3.28 -> 2.57 ms forward with one
+// buffer, Py=160: 0.254 -> 0.267 ms).
 constexpr int kPairsY = kTZ2 / 2;
 constexpr int kRowStepP = kTileThreads / kPairsY;
 
-template <bool INV, class P>
+template <bool INV, class P, int NBUF = 2>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_y2i(const float2* __restrict__ src, float2* __restrict__ dst, const unsigned char* __restrict__ tmask, int ny,
            int nz, int nzp, int nzt, int ntask, const float2* __restrict__ twy, const int* done) {
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int Py = P::N, lw = P::LW;
-  float2* tile = reinterpret_cast<float2*>(smem_raw);  // [2][kPairsY][lw][2]
+  float2* tile = reinterpret_cast<float2*>(smem_raw);  // [NBUF][kPairsY][lw][2]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nin = INV ? Py : ny;
   const int nout = INV ? ny : Py;
@@ -214,11 +218,14 @@ k_pass_y2i(const float2* __restrict__ src, float2* __restrict__ dst, const unsig
     cp_commit();
   };
   int task = blockIdx.x;
-  if (task < ntask) issue(task, 0);
+  if (NBUF == 2 && task < ntask) issue(task, 0);
   for (int it = 0; task < ntask; ++it, task += gridDim.x) {
-    const int buf = it & 1;
+    const int buf = NBUF == 2 ? (it & 1) : 0;
     const int next = task + gridDim.x;
-    if (next < ntask) {
+    if (NBUF == 1) {
+      issue(task, 0);
+      cp_wait<0>();
+    } else if (next < ntask) {
       issue(next, buf ^ 1);
       cp_wait<1>();
     } else {
@@ -239,7 +246,7 @@ k_pass_y2i(const float2* __restrict__ src, float2* __restrict__ dst, const unsig
       for (int yy = ty; yy < nout; yy += kRowStepP, ob += (size_t)kRowStepP * nzp / 2, tm += (size_t)kRowStepP * nzt)
         if (!INV || *tm) *ob = lb[P::addr(yy)];
     }
-    __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task
+    __syncthreads();  // buffer 'buf' is the cp.async target of the next-but-one task (next task, NBUF = 1)
   }
 }
 

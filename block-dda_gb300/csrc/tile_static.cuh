@@ -30,7 +30,7 @@ cudaError_t launch_x(int pass, const TileArgs& a) {
   auto smem_x2 = [](int nx) { return 4 * kTZ * P::LW * (int)sizeof(float2) + nx * kTZ * 4; };
   const int smem_ae = smem_x2(max_nx);
   int fpg = 0;
-  const dim3 grid(g.ntiles, x_field_groups(a.nfield, g.ntiles, a.sms, &fpg));
+  const dim3 grid(g.ntiles, x_field_groups(a.nfield, g.ntiles, a.sms, &fpg, g.tune.xcta));
   static std::once_flag oa, oe;
   static cudaError_t ca = cudaSuccess, ce = cudaSuccess;
   cudaError_t e = cudaSuccess;
@@ -48,36 +48,42 @@ cudaError_t launch_x(int pass, const TileArgs& a) {
 }
 
 // y passes (B, D) with the plan of Py (yplans.inc: the radix sequence of
-// tplans.inc, a layout for interleaved pairs and rows of eight pairs)
-template <class P>
-cudaError_t launch_y(int pass, const TileArgs& a) {
+// tplans.inc, a layout for interleaved pairs and rows of eight pairs),
+// double- or single-buffered (MvpTune::ybuf)
+template <class P, int NBUF>
+cudaError_t launch_y_buf(int pass, const TileArgs& a) {
   const MvpGeom& g = *a.g;
-  const int smem_bd = 2 * tile::kTZ2 * P::LW * (int)sizeof(float2);  // 16 columns per task
+  const int smem_bd = NBUF * tile::kTZ2 * P::LW * (int)sizeof(float2);  // 16 columns per task and buffer
   const int ntask2 = a.nfield * g.Px * ((g.nz + tile::kTZ2 - 1) / tile::kTZ2);
   static std::once_flag ob, od;
   static cudaError_t cb = cudaSuccess, cd = cudaSuccess;
   static int resident[2] = {0, 0};  // CTAs of each kernel that fit on one SM
   cudaError_t e = cudaSuccess;
   // The grid is a whole number of waves of the CTAs resident at once (see
-  // kYWaves): a fixed 8 per SM left a partial last wave (1.1-1.6 waves).
+  // MvpTune::ywaves): a fixed 8 per SM left a partial last wave (1.1-1.6 waves).
   auto grid_of = [&](auto kernel, int inv) {
     if (resident[inv] == 0) {
       int nb = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kTileThreads, smem_bd) != cudaSuccess || nb < 1) nb = 1;
       resident[inv] = nb;
     }
-    return std::min(ntask2, kYWaves * resident[inv] * a.sms);
+    return std::min(ntask2, g.tune.ywaves * resident[inv] * a.sms);
   };
   if (pass == kTileB) {
-    if ((e = set_smem(tile::k_pass_y2i<false, P>, smem_bd, ob, cb)) != cudaSuccess) return e;
-    tile::k_pass_y2i<false, P><<<grid_of(tile::k_pass_y2i<false, P>, 0), kTileThreads, smem_bd, a.st>>>(
+    if ((e = set_smem(tile::k_pass_y2i<false, P, NBUF>, smem_bd, ob, cb)) != cudaSuccess) return e;
+    tile::k_pass_y2i<false, P, NBUF><<<grid_of(tile::k_pass_y2i<false, P, NBUF>, 0), kTileThreads, smem_bd, a.st>>>(
         a.t1, a.t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask2, a.twy, a.done);
   } else {
-    if ((e = set_smem(tile::k_pass_y2i<true, P>, smem_bd, od, cd)) != cudaSuccess) return e;
-    tile::k_pass_y2i<true, P><<<grid_of(tile::k_pass_y2i<true, P>, 1), kTileThreads, smem_bd, a.st>>>(
+    if ((e = set_smem(tile::k_pass_y2i<true, P, NBUF>, smem_bd, od, cd)) != cudaSuccess) return e;
+    tile::k_pass_y2i<true, P, NBUF><<<grid_of(tile::k_pass_y2i<true, P, NBUF>, 1), kTileThreads, smem_bd, a.st>>>(
         a.t2, a.t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask2, a.twy, a.done);
   }
   return cudaGetLastError();
+}
+
+template <class P>
+cudaError_t launch_y(int pass, const TileArgs& a) {
+  return a.g->tune.ybuf == 1 ? launch_y_buf<P, 1>(pass, a) : launch_y_buf<P, 2>(pass, a);
 }
 
 }  // namespace tstatic

@@ -94,6 +94,15 @@ k_pass_c_packed(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp,
 // occupancy is then twice as high (Pz=250: 9.9 ms scalar vs 10.3 ms packed
 // per N=65536, L=32 block MVP; Pz=120: 0.35 vs 0.31 ms at N=8192, L=16).
 template <class P> constexpr bool worth() { return 3 * kZWarps * 3 * P::LW * 16 <= kZSmemMax; }
+// The packed kernel can run where two 8-warp CTAs fit; between that and
+// worth() the autotuner decides (MvpTune::zpacked).
+template <class P> constexpr bool fits() { return 2 * kZWarps * 3 * P::LW * 16 <= kZSmemMax; }
+template <class P> bool chosen(const MvpGeom& g, const float4* twzp) {
+  if (!twzp || g.f != 3 || !fits<P>()) return false;
+  return g.tune.zpacked < 0 ? worth<P>() : g.tune.zpacked == 1;
+}
+// Whether the packed kernel is a candidate for this length (autotuner).
+inline bool packed_fits_lw(int lw) { return 2 * kZWarps * 3 * lw * 16 <= kZSmemMax; }
 
 template <class P>
 cudaError_t launch(const MvpGeom& g, float2* t2, int L, const float4* twz, const float2* ghat, cudaStream_t st,
