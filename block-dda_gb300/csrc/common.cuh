@@ -141,7 +141,12 @@ template <typename C> inline C ldg_c(const C* p) { return *p; }
 #endif
 
 // Transform length limits of the warp-per-line FFT.
-constexpr int kMaxLine = 512;   // longest line one warp transforms
+// Longest line one warp transforms (box sides up to kMaxLine / 2 = 600).  The
+// compile-time plan tables cover lengths up to kMaxStaticLine; longer lines
+// run the runtime-plan kernels (strided passes single-buffered where two tile
+// buffers of 16-byte elements would exceed the shared memory of a CTA).
+constexpr int kMaxLine = 1200;
+constexpr int kMaxStaticLine = 512;
 constexpr int kMaxStages = 16;
 
 // Radix schedule of one axis: N = prod(radix[0..nst)), with the per-stage

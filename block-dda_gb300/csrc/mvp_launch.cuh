@@ -123,6 +123,9 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
     return std::min(ntask_y, g.tune.ywaves * nb * num_sms());
   };
   const tile::RtLine<C> lx{g.px}, ly{g.py};
+  // runtime-plan strided passes: tile buffers and shared memory (one buffer for long 16-byte lines)
+  const int xbuf = tile::tile_buffers<T>(plan_lw<C>(g.px), g.nx), ybuf = tile::tile_buffers<T>(plan_lw<C>(g.py), 0);
+  const int xsm = tile::smem_tile<T>(plan_lw<C>(g.px), g.nx, xbuf), ysm = tile::smem_tile<T>(plan_lw<C>(g.py), 0, ybuf);
   int xfpg = 0;  // x passes: fields per CTA
   const dim3 xgrid(g.ntiles, x_field_groups(nfield, g.ntiles, num_sms(), &xfpg, g.tune.xcta));
   const bool runA = g.passes & 1u, runB = g.passes & 2u, runC = g.passes & 4u, runD = g.passes & 8u,
@@ -145,16 +148,15 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   // A
   if (runA && timer) timer->begin(kPassA + pbase, st);
   if (runA && !static_tile(kTileA))
-    tile::k_pass_a<T><<<xgrid, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
-        x, ldx, nfield, xfpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, t1, done);
+    tile::k_pass_a<T><<<xgrid, kTileThreads, xsm, st>>>(
+        x, ldx, nfield, xfpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, t1, xbuf, done);
   if (runA && timer) timer->end(kPassA + pbase, st);
   if (serr != cudaSuccess) return serr;
   // B
   if (runB && timer) timer->begin(kPassB + pbase, st);
   if (runB && !static_tile(kTileB))
-    tile::k_pass_y<T, false><<<grid_y(tile::k_pass_y<T, false, tile::RtLine<C>>, tile::smem_tile<T>(plan_lw<C>(g.py), 0)),
-                               kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
-        t1, t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, done);
+    tile::k_pass_y<T, false><<<grid_y(tile::k_pass_y<T, false, tile::RtLine<C>>, ysm), kTileThreads, ysm, st>>>(
+        t1, t2, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, ybuf, done);
   if (runB && timer) timer->end(kPassB + pbase, st);
   if (serr != cudaSuccess) return serr;
   // C
@@ -183,16 +185,16 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   // D
   if (runD && timer) timer->begin(kPassD + pbase, st);
   if (runD && !static_tile(kTileD))
-    tile::k_pass_y<T, true><<<grid_y(tile::k_pass_y<T, true, tile::RtLine<C>>, tile::smem_tile<T>(plan_lw<C>(g.py), 0)),
-                              kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.py), 0), st>>>(
-        t2, t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, done);
+    tile::k_pass_y<T, true><<<grid_y(tile::k_pass_y<T, true, tile::RtLine<C>>, ysm), kTileThreads, ysm, st>>>(
+        t2, t1, g.tmask, g.ny, g.nz, g.nzp, g.nzt, ntask_y, ly, p.twy, ybuf, done);
   if (runD && timer) timer->end(kPassD + pbase, st);
   if (serr != cudaSuccess) return serr;
   // E
   if (runE && timer) timer->begin(kPassE + pbase, st);
   if (runE && !static_tile(kTileE))
-    tile::k_pass_e<T><<<xgrid, kTileThreads, tile::smem_tile<T>(plan_lw<C>(g.px), g.nx), st>>>(
-        t1, nfield, xfpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, done);
+    tile::k_pass_e<T><<<xgrid, kTileThreads, xsm, st>>>(
+        t1, nfield, xfpg, g.f, g.occ, g.tiles, g.nx, g.ny, g.nz, g.nzp, g.nzt, lx, p.twx, x, ldx, diag, jpre, y, ldy, xbuf,
+        done);
   if (runE && timer) timer->end(kPassE + pbase, st);
   if (serr != cudaSuccess) return serr;
   return cudaGetLastError();
@@ -202,7 +204,7 @@ template <typename T>
 cudaError_t configure_mvp_kernels() {
   using C = typename cplx<T>::type;
   using Rt = tile::RtLine<C>;
-  const int ts = tile::smem_tile<T>(kMaxLineWords, kMaxLine / 2);
+  const int ts = std::min(tile::smem_tile<T>(kMaxLineWords, kMaxLine / 2), kZSmemMax);
   const int zs = kZSmemMax;
   const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
   cudaError_t e;

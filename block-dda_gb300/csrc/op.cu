@@ -341,7 +341,7 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
   }
   for (int i = 0; i < 3; ++i)
     if (n[i] < 1 || n[i] > kMaxLine / 2) {
-      set_error("lattice box dimension outside 1..256");
+      set_error("lattice box dimension outside 1.." + std::to_string(kMaxLine / 2));
       return BDDA_ERR_INVALID;
     }
   if (!(lf > 0.0)) { set_error("lattice spacing must be positive"); return BDDA_ERR_INVALID; }

@@ -45,6 +45,7 @@ void set_error(const std::string& msg);
 namespace {
 
 constexpr int kMaxBypass = 8;
+constexpr int kMaxBoxSide = 600;  // bdda_op_create's limit: half the longest FFT line (kMaxLine)
 
 int smooth235(int v) {
   for (;; ++v) {
@@ -319,8 +320,9 @@ int bdda_server_submit(bdda_server* s, const bdda_request* r, long long* ticket)
     return BDDA_ERR_INVALID;
   }
   for (int i = 0; i < 3; ++i)
-    if (r->n[i] < 1 || r->n[i] > 256) {
-      bdda::set_error("lattice box dimension outside 1..256 (padded FFT lines are limited to 512 points)");
+    if (r->n[i] < 1 || r->n[i] > kMaxBoxSide) {
+      bdda::set_error("lattice box dimension outside 1.." + std::to_string(kMaxBoxSide) +
+                      " (padded FFT lines are limited to " + std::to_string(2 * kMaxBoxSide) + " points)");
       return BDDA_ERR_INVALID;
     }
   const double fp = footprint_bytes(r->n, r->nocc, r->L, s->opts.precision, r->f == 6 ? 6 : 3);

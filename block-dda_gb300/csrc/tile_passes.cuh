@@ -60,14 +60,15 @@ template <typename T, class Line>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int fpg, int fc, const int* __restrict__ occ,
          const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, Line lay,
-         const typename cplx<T>::type* __restrict__ twx, typename cplx<T>::type* __restrict__ t1, const int* done) {
+         const typename cplx<T>::type* __restrict__ twx, typename cplx<T>::type* __restrict__ t1, int nbuf,
+         const int* done) {
   using C = typename cplx<T>::type;
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Px = lay.n();
   const int lw = lay.lw();
-  C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
-  int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
+  C* lines = reinterpret_cast<C*>(smem_raw);                       // [nbuf][kTZ][lw]
+  int* socc = reinterpret_cast<int*>(lines + nbuf * kTZ * lw);     // [nx][kTZ]
   const int tile = tiles[blockIdx.x];
   const int y = tile / nzt, z0 = (tile - y * nzt) * kTZ;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -82,7 +83,8 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int 
   const int f0 = blockIdx.y * fpg, fend = min(nfield, f0 + fpg);  // this CTA's fields (f0 even)
   int l = f0 / fc, c = f0 - (f0 / fc) * fc;
   for (int f = f0; f < fend; ++f) {
-    C* line = lines + ((f & 1) * kTZ + warp) * lw;
+    const int buf = nbuf == 2 ? (f & 1) : 0;
+    C* line = lines + (buf * kTZ + warp) * lw;
     const C* xc = x + (size_t)l * ldx + c;
     for (int xi = lane; xi < nx; xi += 32) {
       const int m = socc[xi * kTZ + warp];
@@ -93,10 +95,11 @@ k_pass_a(const typename cplx<T>::type* __restrict__ x, int ldx, int nfield, int 
     __syncthreads();
     // drain: thread tid writes column w = tid % 8 of rows q = tid / 8 + 32 k
     if (zval) {
-      const C* lb = lines + ((f & 1) * kTZ + tw8) * lw;
+      const C* lb = lines + (buf * kTZ + tw8) * lw;
       C* out = t1 + (size_t)f * Px * rowstride + (size_t)y * nzp + z0 + tw8 + (size_t)tq * rowstride;
       for (int q = tq; q < Px; q += kRowStep, out += kRowStep * rowstride) *out = lb[lay.addr(q)];
     }
+    if (nbuf == 1) __syncthreads();  // the next field's gather overwrites the drained buffer
     if (++c == fc) { c = 0; ++l; }
   }
 }
@@ -109,13 +112,13 @@ template <typename T, bool INV, class Line>
 __global__ void __launch_bounds__(kTileThreads)
 k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type* __restrict__ dst,
          const unsigned char* __restrict__ tmask, int ny, int nz, int nzp, int nzt, int ntask, Line lay,
-         const typename cplx<T>::type* __restrict__ twy, const int* done) {
+         const typename cplx<T>::type* __restrict__ twy, int nbuf, const int* done) {
   using C = typename cplx<T>::type;
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Py = lay.n();
   const int lw = lay.lw();
-  C* lines = reinterpret_cast<C*>(smem_raw);  // [2][kTZ][lw]
+  C* lines = reinterpret_cast<C*>(smem_raw);  // [nbuf][kTZ][lw]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nin = INV ? Py : ny;    // rows read
   const int nout = INV ? ny : Py;   // rows written
@@ -139,11 +142,14 @@ k_pass_y(const typename cplx<T>::type* __restrict__ src, typename cplx<T>::type*
   };
 
   int task = blockIdx.x;
-  if (task < ntask) issue(task, 0);
+  if (nbuf == 2 && task < ntask) issue(task, 0);
   for (int it = 0; task < ntask; ++it, task += gridDim.x) {
-    const int buf = it & 1;
+    const int buf = nbuf == 2 ? (it & 1) : 0;
     const int next = task + gridDim.x;
-    if (next < ntask) {
+    if (nbuf == 1) {
+      issue(task, 0);
+      cp_wait<0>();
+    } else if (next < ntask) {
       issue(next, buf ^ 1);
       cp_wait<1>();
     } else {
@@ -256,14 +262,14 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fpg, int
          const int* __restrict__ tiles, int nx, int ny, int nz, int nzp, int nzt, Line lay,
          const typename cplx<T>::type* __restrict__ twx, const typename cplx<T>::type* __restrict__ x, int ldx,
          const typename cplx<T>::type* __restrict__ diag, const typename cplx<T>::type* __restrict__ jpre,
-         typename cplx<T>::type* __restrict__ y, int ldy, const int* done) {
+         typename cplx<T>::type* __restrict__ y, int ldy, int nbuf, const int* done) {
   using C = typename cplx<T>::type;
   if (skip(done)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Px = lay.n();
   const int lw = lay.lw();
-  C* lines = reinterpret_cast<C*>(smem_raw);                       // [2][kTZ][lw]
-  int* socc = reinterpret_cast<int*>(lines + 2 * kTZ * lw);        // [nx][kTZ]
+  C* lines = reinterpret_cast<C*>(smem_raw);                       // [nbuf][kTZ][lw]
+  int* socc = reinterpret_cast<int*>(lines + nbuf * kTZ * lw);     // [nx][kTZ]
   const int tile = tiles[blockIdx.x];
   const int yy = tile / nzt, z0 = (tile - yy * nzt) * kTZ;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -283,11 +289,14 @@ k_pass_e(const typename cplx<T>::type* __restrict__ t1, int nfield, int fpg, int
     cp_commit();
   };
   const int f0 = blockIdx.y * fpg, fend = min(nfield, f0 + fpg);  // this CTA's fields (f0 even)
-  issue(f0, 0);
+  if (nbuf == 2) issue(f0, 0);
   int l = f0 / fc, c = f0 - (f0 / fc) * fc;
   for (int f = f0; f < fend; ++f) {
-    const int buf = f & 1;
-    if (f + 1 < fend) {
+    const int buf = nbuf == 2 ? (f & 1) : 0;
+    if (nbuf == 1) {
+      issue(f, 0);
+      cp_wait<0>();
+    } else if (f + 1 < fend) {
       issue(f + 1, buf ^ 1);
       cp_wait<1>();
     } else {
@@ -438,9 +447,13 @@ k_pass_e2i(const float2* __restrict__ t1, int nfield, int fpg, int fc, const int
   }
 }
 
-template <typename T> int smem_tile(int lw, int nx) {
-  return 2 * kTZ * lw * (int)sizeof(typename cplx<T>::type) + nx * kTZ * 4;
+// Dynamic shared memory of a runtime-plan strided pass with nbuf tile buffers
+// (nx > 0: the x passes' occupancy table of the tile).
+template <typename T> int smem_tile(int lw, int nx, int nbuf = 2) {
+  return nbuf * kTZ * lw * (int)sizeof(typename cplx<T>::type) + nx * kTZ * 4;
 }
+// Two tile buffers where they fit in a CTA's shared memory, else one.
+template <typename T> int tile_buffers(int lw, int nx) { return smem_tile<T>(lw, nx, 2) <= kZSmemMax ? 2 : 1; }
 
 }  // namespace tile
 }  // namespace bdda

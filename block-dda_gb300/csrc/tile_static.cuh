@@ -25,7 +25,7 @@ cudaError_t set_smem(K kernel, int bytes, std::once_flag& once, cudaError_t& cfg
 template <class P>
 cudaError_t launch_x(int pass, const TileArgs& a) {
   const MvpGeom& g = *a.g;
-  const int max_nx = kMaxLine / 2;
+  const int max_nx = kMaxStaticLine / 2;
   // [2 buffers][8 columns][2 fields] lines + the occupancy of the tile
   auto smem_x2 = [](int nx) { return 4 * kTZ * P::LW * (int)sizeof(float2) + nx * kTZ * 4; };
   const int smem_ae = smem_x2(max_nx);

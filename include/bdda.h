@@ -54,7 +54,7 @@ typedef struct bdda_op bdda_op;
  * declared in MBT_utils.hpp:5): instead of returning the FFT of the 1-D MBT
  * projection Au_til, the Green-tensor spectrum on the 2x-padded 5-smooth grid
  * is built on the device and kept in the handle.
- *   n[3]        lattice box (nx, ny, nz), each 1..256
+ *   n[3]        lattice box (nx, ny, nz), each 1..600 (padded FFT lines up to 1200 points)
  *   f           3 (electric dipoles, the reference's CED) or 6 (electric and
  *               magnetic dipoles, its default CEMD mode): rows f*m + c of every
  *               vector, c < 3 electric, c >= 3 magnetic

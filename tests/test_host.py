@@ -39,7 +39,7 @@ def test_errors_are_reported_not_fatal(lib):
     n = (ct.c_int * 3)(4, 4, 4)
     assert lib.bdda_op_create(ct.byref(h), n, 4, 1.0, 1.0, 0.0, 1) == bdda.ERR_INVALID
     assert b"f value" in lib.bdda_last_error()
-    n = (ct.c_int * 3)(4, 300, 4)
+    n = (ct.c_int * 3)(4, 601, 4)   # box sides up to 600: padded lines up to 1200 points
     assert lib.bdda_op_create(ct.byref(h), n, 3, 1.0, 1.0, 0.0, 1) == bdda.ERR_INVALID
     assert lib.bdda_op_set_graphs(None, 1) == bdda.ERR_INVALID
     assert b"null operator" in lib.bdda_last_error()
@@ -52,8 +52,10 @@ def _smooth(v):
     return v == 1
 
 
-@pytest.mark.parametrize("N", [v for v in range(2, 513) if _smooth(v)])
+@pytest.mark.parametrize("N", [v for v in range(2, 1201) if _smooth(v)])
 def test_device_fft_core_on_cpu(N):
+    """Every 5-smooth length a box side up to 600 pads to (lengths past 512 run
+    only the runtime-plan kernels)."""
     rng = np.random.default_rng(N)
     a = rng.standard_normal(N) + 1j * rng.standard_normal(N)
     b = rng.standard_normal(N) + 1j * rng.standard_normal(N)
