@@ -627,13 +627,21 @@ def _serve_stream(a, probs, rate, seed, budget):
     lat = np.array([r["t_done"] - r["t_submit"] for r in res])
     ok = sum(1 for r in res if r["status"] == 0 and r["true_res_max"] <= 1e-8)
     rhs = sum(p.B.shape[1] for p in served)
+    desc = [{"nocc": p.nocc, "box": list(p.n), "nrhs": int(p.B.shape[1]), "status": r["status"],
+             "iterations": r["iterations"], "true_res_max": r["true_res_max"], "retried_fp64": r["retried_fp64"],
+             "service_s": r["t_done"] - r["t_start"], "latency_s": r["t_done"] - r["t_submit"]}
+            for p, r in zip(served, res)]
     return {"offered_requests_per_s": rate,
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
                           "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
             "throughput": {"requests_per_s": len(served) / wall, "rhs_solves_per_s": rhs / wall},
             "requests_converged": ok, "requests_served": len(served), "rejected_at_admission": rejected,
             "peak_concurrent": st["peak_running"], "peak_reserved_GB": st["peak_inflight_bytes"] / 1e9,
-            "spectra_reused": st["spectra_reused"], "wall_s": wall}
+            "spectra_reused": st["spectra_reused"], "wall_s": wall,
+            "retried_fp64": sum(d["retried_fp64"] for d in desc),
+            "failed": [d for d in desc if d["status"] != 0 or d["true_res_max"] > 1e-8],
+            "slowest": sorted(desc, key=lambda d: -d["service_s"])[:8],
+            "service_s_sum": float(sum(d["service_s"] for d in desc))}
 
 
 def run_serving(a):

@@ -103,7 +103,7 @@ class Request(ct.Structure):
 class RequestResult(ct.Structure):
     _fields_ = [("status", ct.c_int), ("iterations", ct.c_int), ("refinements", ct.c_int),
                 ("true_res_max", ct.c_double), ("t_submit", ct.c_double), ("t_start", ct.c_double),
-                ("t_done", ct.c_double), ("footprint_bytes", ct.c_double)]
+                ("t_done", ct.c_double), ("footprint_bytes", ct.c_double), ("retried_fp64", ct.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
