@@ -222,9 +222,6 @@ enum TilePass { kTileA = 0, kTileB, kTileD, kTileE };
 // four 0.233 / 0.135; the earlier fixed 8 CTAs per SM (1.1-1.6 waves) 0.239 /
 // 0.159.
 constexpr int kYWaves = 4;
-// Runtime-plan strided passes with 16-byte elements (FP64, double-float) use
-// one tile buffer when two would take more than this (see mvp_launch.cuh).
-constexpr int kRtSingleBufferBytes = 48 * 1024;
 
 // Fields per CTA of the x passes (A, E), an even number: a tile's fields are
 // split over groups of CTAs so that a launch has about xcta CTAs per

@@ -124,14 +124,10 @@ cudaError_t launch_block_mvp(const MvpGeom& g, const MvpPrec<T>& p, const typena
   };
   const tile::RtLine<C> lx{g.px}, ly{g.py};
   // runtime-plan strided passes: tile buffers and shared memory -- one buffer
-  // where two would not fit, and for 16-byte elements wherever two buffers
-  // take more than kRtSingleBufferBytes (prefetching the next tile is then
-  // worth less than the CTAs the second buffer keeps off the SM)
-  auto rt_buffers = [&](int lw, int nx) {
-    if (tile::tile_buffers<T>(lw, nx) == 1) return 1;
-    return (sizeof(C) == 16 && tile::smem_tile<T>(lw, nx, 2) > kRtSingleBufferBytes) ? 1 : 2;
-  };
-  const int xbuf = rt_buffers(plan_lw<C>(g.px), g.nx), ybuf = rt_buffers(plan_lw<C>(g.py), 0);
+  // where two would not fit (long lines of 16-byte elements).  Single
+  // buffering where two fit was measured no faster for the double-float y
+  // passes (N=65536, Py=270: 14.6 / 14.3 vs 14.3 / 14.0 ms).
+  const int xbuf = tile::tile_buffers<T>(plan_lw<C>(g.px), g.nx), ybuf = tile::tile_buffers<T>(plan_lw<C>(g.py), 0);
   const int xsm = tile::smem_tile<T>(plan_lw<C>(g.px), g.nx, xbuf), ysm = tile::smem_tile<T>(plan_lw<C>(g.py), 0, ybuf);
   int xfpg = 0;  // x passes: fields per CTA
   const dim3 xgrid(g.ntiles, x_field_groups(nfield, g.ntiles, num_sms(), &xfpg, g.tune.xcta));

@@ -162,6 +162,21 @@ struct bdda_server {
     }
   }
 
+  // Express slots: extra workers that take only small requests (footprint up
+  // to kExpressBytes), so that a queue held up by long solves of large
+  // targets still serves the many small ones.
+  static constexpr double kExpressBytes = 2e9;
+  // index of the first small request that fits, or -1 (caller holds mu)
+  int pick_express() const {
+    for (size_t i = 0; i < pending.size(); ++i)
+      if (pending[i].footprint <= kExpressBytes && in_use + pending[i].footprint <= budget) {
+        // passing a head that waits for memory counts as a bypass, and is limited likewise
+        const bool head_waits = i > 0 && in_use + pending.front().footprint > budget;
+        return (head_waits && pending.front().bypassed >= kMaxBypass) ? -1 : (int)i;
+      }
+    return -1;
+  }
+
   // index of the request to admit now, or -1 (caller holds mu)
   int pick() const {
     if (pending.empty()) return -1;
@@ -245,20 +260,22 @@ struct bdda_server {
     return nullptr;
   }
 
-  void worker() {
+  void worker(bool express) {
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
       std::vector<bdda_op*> evicted;
-      cv_work.wait(lk, [&] { return (stopping && pending.empty()) || pick_evicting(&evicted) >= 0; });
+      cv_work.wait(lk, [&] {
+        return (stopping && pending.empty()) || (express ? pick_express() >= 0 : pick_evicting(&evicted) >= 0);
+      });
       if (!evicted.empty()) {
         lk.unlock();
         for (bdda_op* op : evicted) bdda_op_destroy(op);
         lk.lock();
       }
       if (stopping && pending.empty()) return;
-      const int i = pick();
+      const int i = express ? pick_express() : pick();
       if (i < 0) continue;
-      if (i > 0) pending.front().bypassed++;
+      if (i > 0 && (!express || in_use + pending.front().footprint > budget)) pending.front().bypassed++;
       Item it = pending[i];
       pending.erase(pending.begin() + i);
       in_use += it.footprint;
@@ -330,7 +347,10 @@ int bdda_server_create(bdda_server** out, int slots, double mem_budget_bytes, co
   s->cache_limit = 0.25 * mem_budget_bytes;
   s->opts = *opts;
   s->dry = dry_run != 0;
-  for (int i = 0; i < slots; ++i) s->threads.emplace_back([s] { s->worker(); });
+  for (int i = 0; i < slots; ++i) s->threads.emplace_back([s] { s->worker(false); });
+  // express slots for small requests: a quarter of the slots, at least one
+  const int express = dry_run ? 0 : std::max(1, slots / 4);
+  for (int i = 0; i < express; ++i) s->threads.emplace_back([s] { s->worker(true); });
   *out = s;
   return BDDA_OK;
 }

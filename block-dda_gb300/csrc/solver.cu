@@ -21,8 +21,8 @@
 
 namespace bdda {
 
-// Iteration cap of an FP32 inner solve of a mixed refinement whose operator
-// holds FP64 tables (the FP64 fallback of the refinement loop).
+// Iteration cap of an FP32 inner solve of a mixed refinement (the FP64
+// fallback of the refinement loop takes over where FP32 Krylov stalls).
 constexpr int kMixedInnerCap = 400;
 
 // ---------------------------------------------------------------------------
@@ -1030,10 +1030,12 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
       if (o->jacobi) k_rowscale<float, double><<<gv, 256, 0, st>>>(n, L, w->jpre64.as<double2>(), R, ldr, Bp, n, cf);
       else k_convert<float, double><<<gv, 256, 0, st>>>(n, L, R, ldr, Bp, n, cf);
       op->timer.count(kOther);
-      // with FP64 tables to fall back on, an FP32 inner solve that has not met
-      // its tolerance after kMixedInnerCap iterations (well-posed systems need
-      // tens) ends there, and the refinement decides whether to switch
-      const int imax = (refine && (op->prec & BDDA_PREC_FP64)) ? std::min(itermax, kMixedInnerCap) : itermax;
+      // an FP32 inner solve of a refinement that has not met its tolerance after
+      // kMixedInnerCap iterations (well-posed systems need tens) ends there, and
+      // the refinement decides whether to continue, to switch to FP64 inner
+      // solves (FP64 tables) or to report the stall (the request server then
+      // solves again with FP64 tables)
+      const int imax = refine ? std::min(itermax, kMixedInnerCap) : itermax;
       BDDA_TRY(k32.run(o->solver, Bp, D, full, tol, imax, &it, &er, &stt));
       if (accumulate) k_accumulate<float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd, cfi);
       else k_convert<double, float><<<gv, 256, 0, st>>>(n, L, D, n, Dst, ldd, cfi);
