@@ -115,3 +115,24 @@ def test_server_reuses_cached_spectrum_bitwise():
     fresh.close()
     assert st0["spectra_reused"] == 0 and st0["cached_bytes"] == 0
     assert np.array_equal(outs[2][0], X2)
+
+
+def test_server_express_slot_serves_small_request_past_large_ones():
+    """With the one regular slot busy with large requests (footprint > 2 GB),
+    a small request submitted after them runs on an express slot and finishes
+    first; every result still converges."""
+    big = [bdda.make_problem(16384, 2.0 + 0.3j, seed=s, n_dirs=8) for s in (3, 4, 5)]
+    small = bdda.make_problem(300, 1.5 + 0.1j, seed=3, n_dirs=1)
+    assert all(bdda.footprint(p.n, p.nocc, 16) > 2e9 for p in big)
+    assert bdda.footprint(small.n, small.nocc, 2) < 2e9
+    srv = bdda.Server(slots=1, mem_budget_bytes=60e9, opts=_mixed_opts())
+    tb = [srv.submit(p) for p in big]
+    ts = srv.submit(small)
+    rs = srv.wait(ts)[1]
+    rb = [srv.wait(t)[1] for t in tb]
+    st = srv.stats()
+    srv.close()
+    assert rs["status"] == 0 and all(r["status"] == 0 for r in rb)
+    assert rs["t_done"] < max(r["t_done"] for r in rb)
+    assert rs["t_done"] < rb[1]["t_start"] or rs["t_done"] < rb[0]["t_done"]
+    assert st["peak_running"] >= 2
