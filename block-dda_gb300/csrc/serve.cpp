@@ -36,6 +36,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "../../include/bdda.h"
 
 namespace bdda {
@@ -107,6 +109,7 @@ struct bdda_server {
     double footprint;
     double t_submit;
     int bypassed = 0;
+    bool exclusive = false;  // ran out of device memory once: runs again with nothing else on the GPU
   };
 
   int slots;
@@ -127,6 +130,7 @@ struct bdda_server {
   double cache_limit = 0, cache_bytes = 0;
   unsigned long long tick = 0;
   long long spectra_reused = 0, spectra_built = 0;
+  bool solo = false;  // an exclusive request is running: nothing else is admitted
 
   // Take an idle operator with this key out of the cache (caller holds mu).
   bool take_cached(const OpKey& k, Cached* out) {
@@ -155,6 +159,8 @@ struct bdda_server {
   // pick(), destroying idle operators (into *ev) while the head of the queue
   // does not fit (caller holds mu).
   int pick_evicting(std::vector<bdda_op*>* ev) {
+    if (!pending.empty() && pending.front().exclusive && running == 0)
+      while (!idle.empty()) ev->push_back(evict_lru());  // all of the device for it
     for (;;) {
       const int i = pick();
       if (i >= 0 || idle.empty() || pending.empty()) return i;
@@ -168,6 +174,7 @@ struct bdda_server {
   static constexpr double kExpressBytes = 2e9;
   // index of the first small request that fits, or -1 (caller holds mu)
   int pick_express() const {
+    if (solo || (!pending.empty() && pending.front().exclusive)) return -1;
     for (size_t i = 0; i < pending.size(); ++i)
       if (pending[i].footprint <= kExpressBytes && in_use + pending[i].footprint <= budget) {
         // passing a head that waits for memory counts as a bypass, and is limited likewise
@@ -179,7 +186,9 @@ struct bdda_server {
 
   // index of the request to admit now, or -1 (caller holds mu)
   int pick() const {
-    if (pending.empty()) return -1;
+    if (pending.empty() || solo) return -1;
+    if (pending.front().exclusive)  // waits for every running request to finish, then runs alone
+      return (running == 0 && in_use + pending.front().footprint <= budget) ? 0 : -1;
     if (in_use + pending.front().footprint <= budget) return 0;
     if (pending.front().bypassed >= kMaxBypass) return -1;
     for (size_t i = 1; i < pending.size(); ++i)
@@ -201,6 +210,16 @@ struct bdda_server {
     bdda_op* op = nullptr;
     Cached c{};
     bool reused = false;
+    if (it.exclusive) {
+      // return the stream-ordered pool's cached free memory to the device, so
+      // that the request's large buffers are not refused for fragmentation
+      int dev = 0;
+      cudaMemPool_t pool;
+      if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        cudaDeviceSynchronize();  // nothing else runs: an exclusive request waits for the others
+        cudaMemPoolTrimTo(pool, 0);
+      }
+    }
     {
       std::lock_guard<std::mutex> lk(mu);
       if (take_cached(key, &c)) {
@@ -278,6 +297,7 @@ struct bdda_server {
       if (i > 0 && (!express || in_use + pending.front().footprint > budget)) pending.front().bypassed++;
       Item it = pending[i];
       pending.erase(pending.begin() + i);
+      if (it.exclusive) solo = true;
       in_use += it.footprint;
       peak_in_use = std::max(peak_in_use, in_use);
       peak_running = std::max(peak_running, ++running);
@@ -299,6 +319,23 @@ struct bdda_server {
       res.t_done = now_s(t0);
       lk.lock();
       in_use -= reserved;
+      if (it.exclusive) solo = false;
+      if (res.status == BDDA_ERR_NOMEM && !it.exclusive && !dry) {
+        // the device refused memory that the footprint allowed (other requests'
+        // buffers, pool fragmentation): queue the request again at the head,
+        // to run alone once the running ones are done
+        if (keep) {
+          lk.unlock();
+          bdda_op_destroy(keep);
+          lk.lock();
+        }
+        Item again = it;
+        again.exclusive = true;
+        pending.push_front(again);
+        --running;
+        cv_work.notify_all();
+        continue;
+      }
       if (keep) {
         // keep the operator idle, within the cache limit (oldest first out)
         std::vector<bdda_op*> out;
