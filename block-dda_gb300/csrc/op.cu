@@ -156,8 +156,8 @@ static std::string tune_key(const MvpGeom& g, int L) {
          ":" + std::to_string(g.ntiles) + ":" + std::to_string(g.tile_rows) + ":" + std::to_string(L);
 }
 
-static cudaError_t autotune_f32(Op* op, MvpGeom g, const MvpPrec<float>& p, const float2* x, int ldx, int L,
-                                float2* t1, float2* t2, cudaStream_t st, Op::TuneRec* out) {
+static cudaError_t autotune_f32(MvpGeom g, const MvpPrec<float>& p, const float2* x, int ldx, int L, float2* t1,
+                                float2* t2, cudaStream_t st, Op::TuneRec* out) {
   cudaEvent_t a = nullptr, b = nullptr;
   cudaError_t e = cudaEventCreate(&a);
   if (e == cudaSuccess) e = cudaEventCreate(&b);
@@ -219,7 +219,6 @@ static cudaError_t autotune_f32(Op* op, MvpGeom g, const MvpPrec<float>& p, cons
   rec.tune = t;
   rec.measured = e == cudaSuccess;
   *out = rec;
-  (void)op;
   return e;
 }
 
@@ -268,7 +267,7 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
           if (c != g_tune_cache.end()) { rec = c->second; have = true; }
         }
         if (!have) {
-          BDDA_CUDA(autotune_f32(op, g, ta, x, ldx, L, op->t1[pi].as<float2>(), op->t2[pi].as<float2>(), st, &rec));
+          BDDA_CUDA(autotune_f32(g, ta, x, ldx, L, op->t1[pi].as<float2>(), op->t2[pi].as<float2>(), st, &rec));
           std::lock_guard<std::mutex> lk(g_tune_mu);
           g_tune_cache[key] = rec;
         }
