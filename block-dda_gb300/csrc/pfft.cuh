@@ -233,7 +233,7 @@ __device__ __forceinline__ void stage(ulonglong2* __restrict__ sm, const float4*
     cp v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      if (prune_in) v[i] = (idx0 + i * M < nv) ? lds(p + i * off) : cp{0ull, 0ull};
+      if (prune_in) v[i] = (2 * i < R && idx0 + i * M < nv) ? lds(p + i * off) : cp{0ull, 0ull};
       else v[i] = lds(p + i * off);
     }
     if (!INV) {
@@ -262,7 +262,7 @@ __device__ __forceinline__ void stage(ulonglong2* __restrict__ sm, const float4*
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       if (prune_out) {
-        if (idx0 + i * M < nv) sts(p + i * off, v[i]);
+        if (2 * i < R && idx0 + i * M < nv) sts(p + i * off, v[i]);
       } else {
         sts(p + i * off, v[i]);
       }
@@ -288,7 +288,7 @@ __device__ __forceinline__ void stage0_from_global(ulonglong2* __restrict__ sm, 
     cp v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      if (n1 + i * M < nv) {
+      if (2 * i < R && n1 + i * M < nv) {  // nv <= N / 2, as in sfft::stage
         const float2 x = g[i * M], y = g[i * M + boff];
         v[i] = {p2(x.x, y.x), p2(x.y, y.y)};
       } else {
@@ -340,7 +340,7 @@ __device__ __forceinline__ void stage0_to_global(const ulonglong2* __restrict__ 
     float2* g = ga + (size_t)j * gstride + n1;
 #pragma unroll
     for (int i = 0; i < R; ++i)
-      if (n1 + i * M < nv) {
+      if (2 * i < R && n1 + i * M < nv) {
         float ra, rb, ia, ib;
         unp(v[i].re, ra, rb);
         unp(v[i].im, ia, ib);

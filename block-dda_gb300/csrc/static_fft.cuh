@@ -48,6 +48,10 @@ struct Plan {
 // inverse (DIT, the adjoint): conjugate twiddle then inverse DFT.  The forward
 // first stage reads only inputs idx < nv (the rest are zero padding); the
 // inverse last stage writes only outputs idx < nv (the rest are discarded).
+// Every caller has nv <= N / 2 (a padded line is at least twice the box
+// side), so in those stages (span M = N / R) the butterfly elements i with
+// 2 i >= R are padding in every butterfly: compile-time zero inputs and dead
+// outputs, whose DFT arithmetic the compiler folds away.
 template <class P, int s, bool INV, int NL, typename C = float2>
 __device__ __forceinline__ void stage(C* __restrict__ sm, const C* __restrict__ tw, int lane, int nv) {
   constexpr int R = P::rad[s];
@@ -67,7 +71,7 @@ __device__ __forceinline__ void stage(C* __restrict__ sm, const C* __restrict__ 
     C v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      if (prune_in) v[i] = (idx0 + i * M < nv) ? p[i * off] : czero<C>();
+      if (prune_in) v[i] = (2 * i < R && idx0 + i * M < nv) ? p[i * off] : czero<C>();
       else v[i] = p[i * off];
     }
     if (!INV) {
@@ -88,7 +92,7 @@ __device__ __forceinline__ void stage(C* __restrict__ sm, const C* __restrict__ 
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       if (prune_out) {
-        if (idx0 + i * M < nv) p[i * off] = v[i];
+        if (2 * i < R && idx0 + i * M < nv) p[i * off] = v[i];
       } else {
         p[i * off] = v[i];
       }
@@ -114,7 +118,7 @@ __device__ __forceinline__ void stage0_from_global(C* __restrict__ sm, const C* 
     const C* g = gsrc + (size_t)j * gstride + n1;
     C v[R];
 #pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = (n1 + i * M < nv) ? g[i * M] : czero<C>();
+    for (int i = 0; i < R; ++i) v[i] = (2 * i < R && n1 + i * M < nv) ? g[i * M] : czero<C>();
     dft<R, false>(v);
     if (M > 1 && n1 != 0) {
 #pragma unroll
@@ -151,7 +155,7 @@ __device__ __forceinline__ void stage0_to_global(const C* __restrict__ sm, const
     C* g = gdst + (size_t)j * gstride + n1;
 #pragma unroll
     for (int i = 0; i < R; ++i)
-      if (n1 + i * M < nv) g[i * M] = v[i];
+      if (2 * i < R && n1 + i * M < nv) g[i * M] = v[i];
   }
   __syncwarp();
 }
@@ -275,7 +279,7 @@ __device__ __forceinline__ void stage_il(float2* __restrict__ sm, const float2* 
     float2 v[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      if (prune_in) v[i] = (idx0 + i * M < nv) ? p[i * off] : make_float2(0.f, 0.f);
+      if (prune_in) v[i] = (2 * i < R && idx0 + i * M < nv) ? p[i * off] : make_float2(0.f, 0.f);
       else v[i] = p[i * off];
     }
     if (!INV) {
@@ -296,7 +300,7 @@ __device__ __forceinline__ void stage_il(float2* __restrict__ sm, const float2* 
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       if (prune_out) {
-        if (idx0 + i * M < nv) p[i * off] = v[i];
+        if (2 * i < R && idx0 + i * M < nv) p[i * off] = v[i];
       } else {
         p[i * off] = v[i];
       }
