@@ -40,7 +40,7 @@ EXPORTS = [
     "bdda_material_load", "bdda_material_constant", "bdda_material_eval", "bdda_material_destroy",
     "bdda_polarizabilities", "bdda_diag_a", "bdda_op_set_wavenumber", "bdda_sweep", "bdda_mie_q",
     "bdda_format_result", "bdda_request_footprint_f", "bdda_server_set_spectrum_cache", "bdda_server_cache_stats",
-    "bdda_op_set_autotune", "bdda_op_get_tuning",
+    "bdda_op_set_autotune", "bdda_op_get_tuning", "bdda_op_check_status",
 ]
 
 SHAPES = {"sphere": 0, "cube": 1, "ellipsoid": 2, "cuboid": 3, "cylinder": 4, "rounded_cylinder": 5}
@@ -172,6 +172,7 @@ def lib(build_if_missing: bool = False):
     L.bdda_op_set_graphs.argtypes = [vp, ct.c_int]
     L.bdda_op_set_autotune.argtypes = [vp, ct.c_int]
     L.bdda_op_get_tuning.argtypes = [vp, ct.c_int, ip, ct.POINTER(ct.c_float)]
+    L.bdda_op_check_status.argtypes = [vp]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
     L.bdda_last_error.restype = ct.c_char_p
     L.bdda_request_footprint.argtypes = [ip, ct.c_int, ct.c_int, ct.c_int]
@@ -314,15 +315,20 @@ class Operator:
     def tuning(self, L):
         """(schedule dict, candidate ms dict, measured?) for nrhs L (bdda_op_get_tuning)."""
         sch = np.zeros(4, np.int32)
-        ms = (ct.c_float * 13)()
+        ms = (ct.c_float * 14)()
         rc = lib().bdda_op_get_tuning(self._h, int(L), _iptr(sch), ms)
         _check(rc, (ERR_NOT_CONVERGED,))
         cand = {"y": {f"buf{1 + i // 4}_waves{(1, 2, 4, 8)[i % 4]}": ms[i] for i in range(8)},
-                "z_pass": {"scalar": ms[8], "packed": ms[9]},
+                "z_pass": {"scalar": ms[8], "packed": ms[9], "pipelined": ms[13]},
                 "x_cta_per_sm": {str(v): ms[10 + i] for i, v in enumerate((5, 10, 20))}}
         return ({"y_waves": int(sch[0]), "y_buffers": int(sch[1]),
-                 "z_pass": {-1: "default", 0: "scalar", 1: "packed"}[int(sch[2])], "x_cta_per_sm": int(sch[3])},
+                 "z_pass": {-1: "default", 0: "scalar", 1: "packed", 2: "pipelined"}[int(sch[2])],
+                 "x_cta_per_sm": int(sch[3])},
                 cand, rc == OK)
+
+    def check_status(self):
+        """Raise if a kernel of this operator reported a failed bounded wait (bdda_op_check_status)."""
+        _check(lib().bdda_op_check_status(self._h))
 
     def kernel_stats(self, reset=False):
         n = len(KERNEL_NAMES)
@@ -558,7 +564,8 @@ def host_fft_line(x, inverse=False, prec=1, nvalid=0, max_radix=8):
 
     The schedule is the operator's for an axis of this length and the element
     width of prec: max_radix > 8 selects the z axis (three-line fused pass),
-    otherwise the x / y axes."""
+    otherwise the x / y axes; max_radix = 32 the complex FP32 z schedule
+    (first-stage radices up to 32) in any arithmetic."""
     a = np.ascontiguousarray(x, dtype=np.complex128).copy()
     rad = np.zeros(16, np.int32)
     rad[0] = int(max_radix)

@@ -70,11 +70,13 @@ def main(argv=None):
         kd = op.kernel_stats(reset=True)
         ks.update({k: v for k, v in kd.items() if k.endswith("c128") and v["launches"]})
     op.set_timing(False)
-    sched, _cand, measured = op.tuning(L)
+    sched, cand, measured = op.tuning(L)
+    op.check_status()
     out = {"nocc": a.nocc, "nrhs": L, "box": list(prob.n), "grid": list(op.info()[0]), "plans": op.plans(),
            "ms_per_launch": {k: round(v["ms"] / max(1, v["launches"]), 4) for k, v in ks.items() if v["launches"]},
            "bytes": dict(zip("ABCDE", [float(v) for v in op.mvp_bytes(L, bdda.PREC_FP32, True, True)])),
-           "schedule": sched, "autotuned": measured}
+           "schedule": sched, "autotuned": measured,
+           "z_pass_candidates_ms": {k: round(v, 4) for k, v in cand["z_pass"].items() if v > 0}}
     op.close()
     print(json.dumps(out), flush=True)
     return 0

@@ -228,7 +228,18 @@ template <int R, bool INV, typename C> BDDA_FFT_FN void dft(C* v) {
   else if constexpr (R == 10) dft_ct<2, 5, INV>(v);
   else if constexpr (R == 12) dft_ct<4, 3, INV>(v);
   else if constexpr (R == 15) dft_ct<3, 5, INV>(v);
-  else dft_ct<4, 4, INV>(v);  // 16
+  else if constexpr (R == 16) dft_ct<4, 4, INV>(v);
+  // the first-stage radices of the complex FP32 z plans
+  else if constexpr (R == 18) dft_ct<2, 9, INV>(v);
+  else if constexpr (R == 20) dft_ct<4, 5, INV>(v);
+  else if constexpr (R == 24) dft_ct<8, 3, INV>(v);
+  else if constexpr (R == 25) dft_ct<5, 5, INV>(v);
+  else if constexpr (R == 27) dft_ct<3, 9, INV>(v);
+  else if constexpr (R == 30) dft_ct<2, 15, INV>(v);
+  else {
+    static_assert(R == 32, "register radix");
+    dft_ct<4, 8, INV>(v);
+  }
 }
 
 // ---- shared-memory line layout ---------------------------------------------
@@ -286,9 +297,15 @@ BDDA_FFT_FN void warp_stage_lines(C* __restrict__ s, int lw, int sh, const C* __
   BDDA_SYNCWARP();
 }
 
-// Stage dispatch over every register radix of the plans (2, 3, 4, 5, 8 and
-// the composite 6, 9, 10, 12, 15, 16).
-template <bool INV, int NL, typename C>
+// Stage dispatch over the register radices of the plans: 2, 3, 4, 5, 8 and
+// the composite 6, 9, 10, 12, 15, 16; with BIG also 18, 20, 24, 25, 27, 30
+// and 32, which only the complex FP32 z plans take (their first stage).  The
+// kernels that can meet a complex FP32 z plan on this path -- the Green
+// spectrum's z transform and the host line transform -- instantiate BIG; the
+// MVP's runtime-plan kernels never do (pass C of complex FP32 runs the
+// compile-time kernels for every tabled z length, and the other plans hold
+// radices <= 16).
+template <bool INV, int NL, typename C, bool BIG = false>
 BDDA_FFT_FN void warp_stage_lines_dispatch(const AxisPlan& p, int st, C* s, int lw, const C* tw, int lane, int lanes,
                                            int nvalid) {
   const int M = p.M[st], ts = p.tstride[st], sh = plan_sk<C>(p);
@@ -304,22 +321,35 @@ BDDA_FFT_FN void warp_stage_lines_dispatch(const AxisPlan& p, int st, C* s, int 
     case 10: warp_stage_lines<10, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
     case 12: warp_stage_lines<12, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
     case 15: warp_stage_lines<15, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
-    default: warp_stage_lines<16, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    case 16: warp_stage_lines<16, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+    default:
+      if constexpr (BIG) {
+        switch (p.radix[st]) {
+          case 18: warp_stage_lines<18, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+          case 20: warp_stage_lines<20, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+          case 24: warp_stage_lines<24, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+          case 25: warp_stage_lines<25, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+          case 27: warp_stage_lines<27, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+          case 30: warp_stage_lines<30, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+          default: warp_stage_lines<32, INV, NL>(s, lw, sh, tw, M, ts, iM, p.N, lane, lanes, nvalid); break;
+        }
+      }
+      break;
   }
 }
 
 // NL lines of one warp transformed together (forward pruned to nvalid inputs):
 // forward natural -> digit-reversed (DIF), inverse digit-reversed -> natural
 // (DIT, unnormalised).
-template <bool INV, int NL, typename C>
+template <bool INV, int NL, typename C, bool BIG = false>
 BDDA_FFT_FN void warp_fft_lines(C* __restrict__ s, int lw, const C* __restrict__ tw, const AxisPlan& p, int lane,
                                 int lanes = 32, int nvalid = 1 << 30) {
   if (!INV) {
     for (int st = 0; st < p.nst; ++st)
-      warp_stage_lines_dispatch<false, NL>(p, st, s, lw, tw, lane, lanes, st == 0 ? nvalid : p.N);
+      warp_stage_lines_dispatch<false, NL, C, BIG>(p, st, s, lw, tw, lane, lanes, st == 0 ? nvalid : p.N);
   } else {
     for (int st = p.nst - 1; st >= 0; --st)
-      warp_stage_lines_dispatch<true, NL>(p, st, s, lw, tw, lane, lanes, p.N);
+      warp_stage_lines_dispatch<true, NL, C, BIG>(p, st, s, lw, tw, lane, lanes, p.N);
   }
 }
 

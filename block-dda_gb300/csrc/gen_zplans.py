@@ -1,14 +1,22 @@
-"""Generates the compile-time FFT plans of the complex FP32 block-MVP passes.
+"""Generates the compile-time FFT plans of the block-MVP passes.
 
-  zplans.inc  three-line plans of the fused z pass (one warp transforms the
-              three component lines of an (x, y, rhs) task)
+  zplans.inc  three-line plans of the complex FP32 fused z pass (one warp
+              transforms the three component lines of an (x, y, rhs) task);
+              the first stage may take a radix up to 32, and a last radix
+              <= FUSED_MAX lets the last forward stage, the Green product and
+              the first inverse stage run as one step (sfft::middle3), so
+              that a 2-stage plan makes two shared-memory round trips per
+              line triple instead of four or more
+  zwplans.inc three-line plans of the 16-byte z passes (FP64 / double-float:
+              register radices <= 16, no fused step)
   tplans.inc  single-line plans of the strided x / y passes (one warp per
               line, eight lines per CTA filled and drained as a tile)
 
 For every 5-smooth line length 2 <= N <= 512 it picks, among the radix
 sequences with the fewest or one more than the fewest stages (register
-radices 2..16), the sequence and the padded layout that minimise a cost of
-shared-memory wavefronts plus issued instructions per line.
+radices 2..16, and the first-stage radices of zplans.inc), the sequence and
+the padded layout that minimise a cost of shared-memory wavefronts plus
+issued instructions per line.
 
 Layout: element idx = q * R_last + r of a line lives at q * S + r (S >= R_last),
 so every butterfly of every stage reads its R elements at one base address plus
@@ -23,13 +31,16 @@ bank (this reproduces the shared-memory wavefront counts ncu reports).
               padded layout chosen for the interleaved pairs and the 16-byte
               tile fill / drain of eight column pairs
 
-Usage: python gen_zplans.py [z] [t] [il]   (writes the tables beside it;
+Usage: python gen_zplans.py [z] [zw] [t] [il]   (writes the tables beside it;
        il reads the radix sequences from tplans.inc)
 """
 import os
 import sys
 
 RADICES = (16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2)
+FIRST_RADICES = (32, 30, 27, 25, 24, 20, 18) + RADICES   # first stage of the complex FP32 z plans
+FUSED_MAX = 10  # largest last radix of the fused middle step (kFusedMaxRadix)
+Z_MAX_PAD = 1.2  # line pitch of the complex FP32 z plans at most 1.2 N + 2
 ESIZE = 8       # complex FP32
 
 
@@ -40,8 +51,9 @@ def smooth(n):
     return n == 1
 
 
-def sequences(n):
-    """Radix sequences with the fewest stages and with one more."""
+def sequences(n, first=RADICES):
+    """Radix sequences with the fewest stages and with one more (first: the
+    radices the first stage may take)."""
     out = {}
 
     def rec(rem, cur, depth):
@@ -50,7 +62,7 @@ def sequences(n):
             return
         if depth == 0:
             return
-        for r in RADICES:
+        for r in (first if not cur else RADICES):
             if rem % r == 0:
                 rec(rem // r, cur + [r], depth - 1)
     for depth in range(1, 12):
@@ -81,7 +93,8 @@ def dft_cost(r):
     base = {2: 4, 3: 12, 4: 16, 5: 34, 8: 52}
     if r in base:
         return base[r]
-    a, b = {6: (2, 3), 9: (3, 3), 10: (2, 5), 12: (4, 3), 15: (3, 5), 16: (4, 4)}[r]
+    a, b = {6: (2, 3), 9: (3, 3), 10: (2, 5), 12: (4, 3), 15: (3, 5), 16: (4, 4), 18: (2, 9), 20: (4, 5),
+            24: (8, 3), 25: (5, 5), 27: (3, 9), 30: (2, 15), 32: (4, 8)}[r]
     return a * dft_cost(b) + b * dft_cost(a) + 4 * (a - 1) * (b - 1)
 
 
@@ -120,6 +133,60 @@ def cost_z(n, rad, S, LW):
     for j in range(3):                                            # load, product (2), store
         for z0 in range(0, n, 32):
             wf += 4 * wavefronts([j * LW + (z // rl) * S + z % rl for z in range(z0, min(n, z0 + 32))])
+    return wf + instr / 4.0
+
+
+def stage_pass(n, rad, S, LW, s, NL, load, store):
+    """Wavefronts and warp instructions of stage s of NL lines (one warp)."""
+    rl = rad[-1]
+    Ls = n
+    for R in rad[:s]:
+        Ls //= R
+    R = rad[s]
+    M = Ls // R
+    B = n // R
+    T = NL * B
+    wf = instr = 0
+    for t0 in range(0, T, 32):
+        chunk = range(t0, min(T, t0 + 32))
+        for i in range(R):
+            a = []
+            for t in chunk:
+                j, u = divmod(t, B)
+                b, n1 = divmod(u, M)
+                idx = b * Ls + n1 + i * M
+                a.append(j * LW + (idx // rl) * S + idx % rl)
+            wf += (load + store) * wavefronts(a)
+        instr += (load + store) * R + dft_cost(R) + (5 * (R - 1) if M > 1 else 0) + 16
+    return wf, instr
+
+
+def cost_zf(n, rad, S, LW):
+    """One three-line task of the complex FP32 z pass: the first forward
+    stage reads global memory and the last inverse stage writes it (shared
+    memory stores / loads only); with nst >= 2 and a last radix <= FUSED_MAX
+    the last forward stage, the product and the first inverse stage are one
+    step in which a thread takes one butterfly of all three lines."""
+    rl, nst = rad[-1], len(rad)
+    fused = nst >= 2 and rl <= FUSED_MAX
+    wf = instr = 0
+    for s in range(nst - 1 if fused else nst):
+        w, i = stage_pass(n, rad, S, LW, s, 3, 0 if s == 0 else 1, 1)   # forward
+        wf, instr = wf + w, instr + i
+        w, i = stage_pass(n, rad, S, LW, s, 3, 1, 0 if s == 0 else 1)   # inverse
+        wf, instr = wf + w, instr + i
+    if fused:
+        B = n // rl
+        for b0 in range(0, B, 32):
+            for j in range(3):
+                for i in range(rl):
+                    wf += 2 * wavefronts([j * LW + b * S + i for b in range(b0, min(B, b0 + 32))])
+            instr += 6 * rl + 2 * dft_cost(rl) * 3 + rl * (12 + 36) + 16
+    else:
+        for j in range(3):                                            # product: load, store
+            for z0 in range(0, n, 32):
+                wf += 2 * wavefronts([j * LW + (z // rl) * S + z % rl for z in range(z0, min(n, z0 + 32))])
+        instr += ((n + 31) // 32) * (6 + 12 + 36)
     return wf + instr / 4.0
 
 
@@ -198,28 +265,33 @@ def choose_layout(n, rad, cost):
     return best[1], best[2]
 
 
-def choose(n, cost):
+def choose(n, cost, first=RADICES, max_pad=None):
+    """Radix sequence and layout of least cost; max_pad caps the line pitch
+    at n * max_pad + 2 elements (shared memory per warp sets the occupancy,
+    which the per-task cost does not see)."""
     best = None
-    for rad in sequences(n):
+    for rad in sequences(n, first):
         rl = rad[-1]
         for S in range(rl, rl + 4):
             top = (n // rl - 1) * S + rl
             for d in range(16):
                 LW = top + d
+                if max_pad is not None and LW > n * max_pad + 2:
+                    continue
                 key = (cost(n, rad, S, LW), LW, S)
                 if best is None or key < best[0]:
                     best = (key, rad, S, LW)
     return best[1], best[2], best[3]
 
 
-def write(path, macro, what, cost):
+def write(path, macro, what, cost, first=RADICES, max_pad=None):
     lines = ["// Generated by gen_zplans.py: compile-time plans of the %s." % what,
              "// %s(index, N, S, LW, radices...): element q*R_last + r at q*S + r, lines LW apart." % macro]
     idx = 0
     for n in range(2, 513):
         if not smooth(n):
             continue
-        rad, S, LW = choose(n, cost)
+        rad, S, LW = choose(n, cost, first, max_pad)
         lines.append("%s(%d, %d, %d, %d, %s)" % (macro, idx, n, S, LW, ", ".join(str(r) for r in rad)))
         idx += 1
         print(macro, n, rad, S, LW, file=sys.stderr, flush=True)
@@ -266,7 +338,11 @@ def main():
                  "column-pair y passes (line pairs interleaved, eight pairs per task)", cost_y_il, rad)
         return
     if "z" in which:
-        write(os.path.join(here, "zplans.inc"), "BDDA_ZPLAN", "fused z pass (three lines per warp)", cost_z)
+        write(os.path.join(here, "zplans.inc"), "BDDA_ZPLAN", "complex FP32 fused z pass (three lines per warp)",
+              cost_zf, FIRST_RADICES, Z_MAX_PAD)
+    if "zw" in which:
+        write(os.path.join(here, "zwplans.inc"), "BDDA_ZWPLAN",
+              "16-byte (FP64 / double-float) z passes (three lines per warp)", cost_z)
     if "t" in which:
         write(os.path.join(here, "tplans.inc"), "BDDA_TPLAN", "strided x / y passes (one line per warp)",
               cost_tile)

@@ -97,7 +97,7 @@ k_fft_contig(double2* __restrict__ data, size_t nlines, AxisPlan p, const double
   double2* d = data + line * p.N;
   for (int i = lane; i < p.N; i += 32) s[skw(i, sh)] = d[i];
   __syncwarp();
-  warp_fft_lines<false, 1>(s, 0, tw, p, lane);  // any schedule (the z axis uses composite radices)
+  warp_fft_lines<false, 1, double2, true>(s, 0, tw, p, lane);  // any schedule (z: composite and first-stage radices)
   for (int i = lane; i < p.N; i += 32) d[i] = s[skw(i, sh)];
 }
 

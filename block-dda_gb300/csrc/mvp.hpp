@@ -20,8 +20,13 @@ constexpr int kZWarps = 8;
 // thread then takes the Rl adjacent frequencies b Rl .. b Rl + Rl - 1 of a
 // butterfly b, so the complex FP32 Green spectrum of such operators is stored
 // last-radix-major (frequency b Rl + i at i (Pz / Rl) + b): the lanes' loads
-// of one component are then adjacent (coalesced).
-constexpr int kFusedMaxRadix = 5;
+// of one component are then adjacent (coalesced).  With the complex FP32 z
+// table's first-stage radices up to 32, most lengths are two stages with a
+// fused last radix (250 = 25 x 10, 243 = 27 x 9, 270 = 27 x 10): the first
+// stage reads T2 and writes shared memory, the fused step reads and writes it
+// once, the last inverse stage reads it and writes T2.  The packed kernel
+// fuses only up to radix 5 (zpacked::supported).
+constexpr int kFusedMaxRadix = 10;
 // (complex FP32 only: the double-float fused step needs 168 registers and ran
 // slower than the separate stages, 54.9 vs 41.6 ms per N=65536, L=32 pass.)
 inline int green_perm_radix(int f, const AxisPlan& pz) {
@@ -41,7 +46,9 @@ inline int z_warps_per_cta(int per_warp) {
 // by the autotuner (op.cu: candidates timed with CUDA events on the operator's
 // own buffers) or left at the defaults.
 struct MvpTune {
-  int zpacked = -1;  // pass C: -1 the default rule (packed where three 8-warp CTAs fit), 0 scalar, 1 packed
+  // pass C kernel: -1 the default rule (pipelined where the plan and shared memory allow, else packed where
+  // three 8-warp CTAs fit, else scalar), 0 scalar, 1 packed, 2 pipelined (zpass_pipe.cuh)
+  int zkern = -1;
   int ywaves = 4;    // passes B, D: grid of this many waves of the CTAs resident per SM
   int ybuf = 2;      // passes B, D: tile buffers per CTA (2: prefetch the next task; 1: twice the CTAs)
   int xcta = 10;     // passes A, E: aim at this many CTAs per SM (fields split into groups)
@@ -61,6 +68,7 @@ struct MvpGeom {
   unsigned passes = 0x1fu;     // passes launched (bit 0 = A .. bit 4 = E); the autotuner times them one by one
   int ntiles;                  // (y, z-tile) pairs holding >= 1 dipole
   long long tile_rows;         // sum over those tiles of their valid z count
+  int* kstat = nullptr;        // status word of the pipelined z pass (1: a bounded copy wait gave up)
   const int* occ;              // [nx*ny*nz] dipole index or -1
   const int* tiles;            // [ntiles]  y*nzt + zt
   const unsigned char* tmask;  // [ny*nzt]  1 for those tiles
@@ -250,6 +258,8 @@ bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz
 // Whether the packed-pair pass C can run for z length Pz and f (an autotuner
 // candidate besides the scalar kernel).
 bool packed_z_available(int Pz, int f);
+// Whether the pipelined z pass (zpass_pipe.cuh) runs this geometry at nrhs L.
+bool pipe_z_available(int Pz, int f, int nzp, int L);
 
 // Pass C of a double-float block MVP (f = 3) with the compile-time z plan of
 // g.Pz; false (nothing launched) when g.Pz has none or f = 6.

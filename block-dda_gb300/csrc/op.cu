@@ -86,11 +86,24 @@ Op::~Op() {
   }
   tws32p.release(); twsdf.release();
   ghat64.release(); ghat32.release(); ghatdf.release();
+  kstat.release();
   for (int i = 0; i < 3; ++i) { t1[i].release(); t2[i].release(); }
   if (stream) {
     wait_stream(stream);
     cudaStreamDestroy(stream);
   }
+}
+
+int take_kernel_status(Op* op, cudaStream_t st) {
+  if (!op->kstat.p) return BDDA_OK;
+  int h = 0;
+  BDDA_CUDA(cudaMemcpyAsync(&h, op->kstat.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BDDA_CUDA(wait_stream(st));
+  if (h == 0) return BDDA_OK;
+  BDDA_CUDA(cudaMemsetAsync(op->kstat.p, 0, sizeof(int), st));
+  BDDA_CUDA(wait_stream(st));
+  set_error("z pass: a wait on a bulk copy to shared memory gave up after 2 s (results invalid)");
+  return BDDA_ERR_CUDA;
 }
 
 int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o) {
@@ -197,13 +210,27 @@ static cudaError_t autotune_f32(MvpGeom g, const MvpPrec<float>& p, const float2
     t.ybuf = 1 + best / 4;
     t.ywaves = yw[best % 4];
   }
-  if (e == cudaSuccess && packed_z_available(g.Pz, g.f) && p.twzps) {
-    MvpTune c = t;
-    c.zpacked = 0;
-    e = timed(4u, c, &rec.ms[8]);
-    c.zpacked = 1;
-    if (e == cudaSuccess) e = timed(4u, c, &rec.ms[9]);
-    if (e == cudaSuccess) t.zpacked = rec.ms[9] < rec.ms[8] ? 1 : 0;
+  {  // pass C: scalar, packed and pipelined kernels where they run this geometry
+    const bool packed = packed_z_available(g.Pz, g.f) && p.twzps;
+    const bool pipe = pipe_z_available(g.Pz, g.f, g.nzp, L);
+    if (e == cudaSuccess && (packed || pipe)) {
+      MvpTune c = t;
+      c.zkern = 0;
+      e = timed(4u, c, &rec.ms[8]);
+      int kbest = 0;
+      float mbest = rec.ms[8];
+      if (e == cudaSuccess && packed) {
+        c.zkern = 1;
+        e = timed(4u, c, &rec.ms[9]);
+        if (e == cudaSuccess && rec.ms[9] < mbest) { kbest = 1; mbest = rec.ms[9]; }
+      }
+      if (e == cudaSuccess && pipe) {
+        c.zkern = 2;
+        e = timed(4u, c, &rec.ms[13]);
+        if (e == cudaSuccess && rec.ms[13] < mbest) { kbest = 2; mbest = rec.ms[13]; }
+      }
+      if (e == cudaSuccess) t.zkern = kbest;
+    }
   }
   const int xc[3] = {5, 10, 20};
   best = -1;
@@ -361,6 +388,8 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     }
   }
   BDDA_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  BDDA_CUDA(op->kstat.ensure(sizeof(int), op->stream));
+  BDDA_CUDA(cudaMemsetAsync(op->kstat.p, 0, sizeof(int), op->stream));
   keep_pool_memory();
   // twiddles
   for (int i = 0; i < 3; ++i) {
@@ -382,25 +411,29 @@ int bdda_op_create(bdda_op** out, const int n[3], int f, double lf, double k_re,
     for (size_t t = 0; t < tw.size(); ++t) td[t] = cmake(dfl(tw[t].x), dfl(tw[t].y));
     BDDA_CUDA(op->twdf[i].ensure(td.size() * sizeof(dfc), op->stream));
     BDDA_CUDA(cudaMemcpyAsync(op->twdf[i].p, td.data(), td.size() * sizeof(dfc), cudaMemcpyHostToDevice, op->stream));
-    // staged tables of the compile-time-plan kernels (radix sequences of plan set 0)
+    // staged tables of the complex FP32 compile-time-plan kernels (plan set 0)
     std::vector<double2> ts;
     stage_twiddles(op->plan[0][i], &ts);
     const size_t nts = std::max<size_t>(ts.size(), 1);
     std::vector<float2> tsf(nts, make_float2(1.f, 0.f));
     std::vector<float4> tsp(nts, make_float4(1.f, 1.f, 0.f, 0.f));
-    std::vector<dfc> tsd(nts, cmake(dfl(1.0), dfl(0.0)));
     for (size_t t = 0; t < ts.size(); ++t) {
       tsf[t] = make_float2((float)ts[t].x, (float)ts[t].y);
       tsp[t] = make_float4(tsf[t].x, tsf[t].x, tsf[t].y, tsf[t].y);
-      tsd[t] = cmake(dfl(ts[t].x), dfl(ts[t].y));
     }
+    // the double-float z pass runs the 16-byte z table's plan (plan set 1)
+    std::vector<double2> tsw;
+    stage_twiddles(op->plan[1][i], &tsw);
+    const size_t ntw = std::max<size_t>(tsw.size(), 1);
+    std::vector<dfc> tsd(ntw, cmake(dfl(1.0), dfl(0.0)));
+    for (size_t t = 0; t < tsw.size(); ++t) tsd[t] = cmake(dfl(tsw[t].x), dfl(tsw[t].y));
     BDDA_CUDA(op->tws32[i].ensure(nts * sizeof(float2), op->stream));
     BDDA_CUDA(cudaMemcpyAsync(op->tws32[i].p, tsf.data(), nts * sizeof(float2), cudaMemcpyHostToDevice, op->stream));
     if (i == 2) {
       BDDA_CUDA(op->tws32p.ensure(nts * sizeof(float4), op->stream));
       BDDA_CUDA(cudaMemcpyAsync(op->tws32p.p, tsp.data(), nts * sizeof(float4), cudaMemcpyHostToDevice, op->stream));
-      BDDA_CUDA(op->twsdf.ensure(nts * sizeof(dfc), op->stream));
-      BDDA_CUDA(cudaMemcpyAsync(op->twsdf.p, tsd.data(), nts * sizeof(dfc), cudaMemcpyHostToDevice, op->stream));
+      BDDA_CUDA(op->twsdf.ensure(ntw * sizeof(dfc), op->stream));
+      BDDA_CUDA(cudaMemcpyAsync(op->twsdf.p, tsd.data(), ntw * sizeof(dfc), cudaMemcpyHostToDevice, op->stream));
     }
     BDDA_CUDA(wait_stream(op->stream));  // tw / tf / ts die at the end of this iteration
   }
@@ -532,7 +565,7 @@ int bdda_op_set_autotune(bdda_op* op, int on) {
   return BDDA_OK;
 }
 
-int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[13]) {
+int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[14]) {
   if (!op || !schedule) { set_error("null argument"); return BDDA_ERR_INVALID; }
   std::lock_guard<std::mutex> lk(op->mu);
   const MvpTune def;
@@ -540,10 +573,10 @@ int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[1
   const MvpTune& t = it != op->tuned.end() ? it->second.tune : def;
   schedule[0] = t.ywaves;
   schedule[1] = t.ybuf;
-  schedule[2] = t.zpacked;
+  schedule[2] = t.zkern;
   schedule[3] = t.xcta;
   if (candidate_ms)
-    for (int i = 0; i < 13; ++i) candidate_ms[i] = it != op->tuned.end() ? it->second.ms[i] : -1.f;
+    for (int i = 0; i < 14; ++i) candidate_ms[i] = it != op->tuned.end() ? it->second.ms[i] : -1.f;
   return it != op->tuned.end() && it->second.measured ? BDDA_OK : BDDA_ERR_NOT_CONVERGED;
 }
 
@@ -553,6 +586,12 @@ int bdda_op_set_timing(bdda_op* op, int enable) {
   op->timer.enabled = enable != 0;
   op->timer.mask = enable == 2 ? (1u << kPassC) | (1u << kPassC64) : ~0u;
   return BDDA_OK;
+}
+
+int bdda_op_check_status(bdda_op* op) {
+  if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(op->mu);
+  return take_kernel_status(op, op->stream);
 }
 
 int bdda_op_kernel_stats(bdda_op* op, double* ms, long long* launches, int n, int reset) {

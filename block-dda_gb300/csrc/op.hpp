@@ -84,8 +84,9 @@ struct Op {
   double lf = 0, kr = 0, ki = 0;
   int prec = 0;  // bit mask BDDA_PREC_FP64 | BDDA_PREC_FP32
   // Axis plans per element width: [0] complex FP32 (the compile-time plan
-  // tables' radix sequences), [1] 16-byte FP64 / double-float (radices <= 8 on
-  // the single-line x / y axes).  Each set has its own Green spectrum order.
+  // tables' radix sequences, first-stage radices up to 32 along z), [1]
+  // 16-byte FP64 / double-float (the 16-byte z table, radices <= 8 on the
+  // single-line x / y axes).  Each set has its own Green spectrum order.
   AxisPlan plan[2][3];
   DevBuf tw64[3], tw32[3], twdf[3];
   DevBuf tw32p[3];  // complex FP32 twiddle pairs {wx, wx, wy, wy} of the packed z pass ([2] only)
@@ -94,6 +95,7 @@ struct Op {
   // DevBuf of the operator is released in ~Op, before its stream is destroyed.
   DevBuf tws32[3], tws32p, twsdf;
   DevBuf ghat64, ghat32, ghatdf;
+  DevBuf kstat;     // int: status word of the pipelined z pass (take_kernel_status)
   Occupancy dip;    // dipole occupancy (set_dipoles)
   unsigned long long dip_epoch = 0;  // bumped whenever dip is rebuilt (captured MVPs hold its sizes)
   Occupancy cub;    // every cuboid site (the reference's MBT_fft_mvp vector)
@@ -106,9 +108,9 @@ struct Op {
   // Autotuned launch schedule of the complex FP32 block MVP, per nrhs
   // (bdda_op_set_autotune, bdda_op_get_tuning); candidate times in ms:
   // [0..7] pass B with 1 then 2 buffers x 1, 2, 4, 8 waves, [8..9] pass C
-  // scalar / packed, [10..12] pass A at 5, 10, 20 CTAs per SM; negative: not
-  // a candidate.
-  struct TuneRec { MvpTune tune; float ms[13]; bool measured; };
+  // scalar / packed, [10..12] pass A at 5, 10, 20 CTAs per SM, [13] pass C
+  // pipelined; negative: not a candidate.
+  struct TuneRec { MvpTune tune; float ms[14]; bool measured; };
   bool autotune = true;
   std::map<int, TuneRec> tuned;
 
@@ -118,7 +120,7 @@ struct Op {
     for (int i = 0; i < 3; ++i) {
       for (const DevBuf* b : {&tw64[i], &tw32[i], &twdf[i], &tw32p[i], &tws32[i], &t1[i], &t2[i]}) h = sig_add(h, *b);
     }
-    for (const DevBuf* b : {&ghat64, &ghat32, &ghatdf, &tws32p, &twsdf, &dip.occ, &dip.tiles, &dip.tmask})
+    for (const DevBuf* b : {&ghat64, &ghat32, &ghatdf, &tws32p, &twsdf, &kstat, &dip.occ, &dip.tiles, &dip.tmask})
       h = sig_add(h, *b);
     return h;
   }
@@ -132,6 +134,7 @@ struct Op {
     g.px = plan[set][0]; g.py = plan[set][1]; g.pz = plan[set][2];
     g.nzt = (n[2] + kTZ - 1) / kTZ;
     g.gperm = 0;
+    g.kstat = kstat.as<int>();
     g.ntiles = o.ntiles;
     g.tile_rows = o.tile_rows;
     g.occ = o.occ.as<int>();
@@ -181,6 +184,10 @@ cudaError_t wait_stream(cudaStream_t st);
 
 // Build the occupancy tables from a host list of lattice addresses (null -> all sites).
 int build_occupancy(Op* op, const int* address, int nocc, Occupancy* o);
+// Reads and clears the operator's kernel status word (the pipelined z pass
+// sets it when a bounded wait on a bulk copy gave up) once the work of stream
+// st is done: BDDA_OK, or BDDA_ERR_CUDA with a message.
+int take_kernel_status(Op* op, cudaStream_t st);
 
 // y = [diag o x +] A_off x [o jpre] for L columns (device pointers, op->stream or st).
 template <typename T>

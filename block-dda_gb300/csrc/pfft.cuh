@@ -365,7 +365,7 @@ __device__ __forceinline__ void forward_to(ulonglong2* sm, const float4* tw, int
 // the last stage (M = 1, no twiddles) in all three component pairs, the
 // symmetric 3 x 3 spectrum (last-radix-major, green_pos) of each of its R
 // frequencies applied in registers, the inverse DFT, one store.  Used for
-// R <= kFusedMaxRadix (3 R pair elements, 12 R registers).
+// R <= 5 (3 R pair elements, 12 R registers; zpacked::supported).
 template <class P>
 __device__ __forceinline__ void middle3(ulonglong2* __restrict__ sm, const float2* __restrict__ gl, int lane) {
   constexpr int R = P::Rl;

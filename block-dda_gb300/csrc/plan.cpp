@@ -145,15 +145,19 @@ Layout best_layout(int N, const std::vector<int>& rad, bool three, int esize) {
 
 struct PlanChoice { std::vector<int> rad; Layout l8, l16; };
 
-// Radix sequences of the compile-time plans of complex FP32: the fused z pass
-// (three-line plans) ...  Every operator's axes use the same sequences, so
-// the runtime-plan kernels of the other precisions and the Green spectrum
-// share the digit order of the compile-time ones.
+// Radix sequences of the compile-time plans: the complex FP32 fused z pass
+// (three-line plans, first-stage radices up to 32) ...
 struct PlanRow { int N, S, LW; int rad[kMaxStages]; };
 constexpr PlanRow kZPlans[] = {
 #define BDDA_ZPLAN(I, N, S, LW, ...) {N, S, LW, {__VA_ARGS__}},
 #include "zplans.inc"
 #undef BDDA_ZPLAN
+};
+// ... the 16-byte (FP64 / double-float) z passes (radices <= 16) ...
+constexpr PlanRow kZWPlans[] = {
+#define BDDA_ZWPLAN(I, N, S, LW, ...) {N, S, LW, {__VA_ARGS__}},
+#include "zwplans.inc"
+#undef BDDA_ZWPLAN
 };
 // ... and of the strided x / y passes (single-line plans).
 constexpr PlanRow kTPlans[] = {
@@ -177,12 +181,14 @@ bool table_radices(const PlanRow (&tab)[K], int N, std::vector<int>* rad) {
 // sequences, the one whose best 8-byte layout takes the fewest wavefronts
 // (complex FP32 is the hot precision); the 16-byte layout is then fitted to it.
 // Radix sequence: the compile-time tables' for complex FP32 and for every
-// z axis; otherwise (16-byte tile passes) the fewest-stage sequence of radices
+// z axis (each element width its own z table, and so its own Green spectrum
+// order); otherwise (16-byte tile passes) the fewest-stage sequence of radices
 // <= 8 whose best 16-byte layout takes the fewest wavefronts.  Then the best
 // layout of each element width for that sequence.
 PlanChoice choose_plan(int N, bool three, bool wide) {
   PlanChoice best;
-  const bool tabled = three ? table_radices(kZPlans, N, &best.rad) : (!wide && table_radices(kTPlans, N, &best.rad));
+  const bool tabled = three ? table_radices(wide ? kZWPlans : kZPlans, N, &best.rad)
+                            : (!wide && table_radices(kTPlans, N, &best.rad));
   if (!tabled) {
     const std::vector<int> allowed = three ? std::vector<int>{16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2}
                                            : std::vector<int>{8, 5, 4, 3, 2};
@@ -295,13 +301,15 @@ extern "C" {
 // (values are rounded to float and back).  nvalid in (0, N): the forward
 // transform reads only the first nvalid inputs and takes the rest as zero
 // (the pad slots hold poison values to prove it).  radix[0] > 8 on input: the
-// z-axis schedule, else the x / y one, each for the element width of prec.
-// Returns the number of stages, or a negative value for an unsupported N.
-// Radices are written to radix (<= 16).
+// z-axis schedule, else the x / y one, each for the element width of prec;
+// radix[0] = 32: the complex FP32 z schedule in any arithmetic (its Green
+// spectrum is transformed in FP64).  Returns the number of stages, or a
+// negative value for an unsupported N.  Radices are written to radix (<= 32).
 int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, int* radix) {
   bdda::AxisPlan p;
   const bool three = radix && radix[0] > 8;
-  if (!bdda::make_axis_plan(N, &p, three, prec != 2)) return -1;
+  const bool wide = (radix && radix[0] == 32) ? false : prec != 2;
+  if (!bdda::make_axis_plan(N, &p, three, wide)) return -1;
   std::vector<double2> tw;
   bdda::make_twiddles(N, &tw);
   // nvalid: forward transforms read only the first nvalid inputs (zero padding)
@@ -310,8 +318,8 @@ int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, i
     const int sh = bdda::plan_sk<double2>(p);
     std::vector<double2> s(bdda::plan_lw<double2>(p), make_double2(1e300, 1e300));
     for (int i = 0; i < N; ++i) s[bdda::skw(i, sh)] = make_double2(data[2 * i], data[2 * i + 1]);
-    if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, tw.data(), p, 0, 1);
-    else bdda::warp_fft_lines<false, 1>(s.data(), 0, tw.data(), p, 0, 1, nv);
+    if (inverse) bdda::warp_fft_lines<true, 1, double2, true>(s.data(), 0, tw.data(), p, 0, 1);
+    else bdda::warp_fft_lines<false, 1, double2, true>(s.data(), 0, tw.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
       const double2 v = s[bdda::skw(i, sh)];
       data[2 * i] = v.x; data[2 * i + 1] = v.y;
@@ -323,8 +331,8 @@ int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, i
       s[bdda::skw(i, sh)] = bdda::cmake(bdda::dfz(data[2 * i]), bdda::dfz(data[2 * i + 1]));
       t[i] = bdda::cmake(bdda::dfz(tw[i].x), bdda::dfz(tw[i].y));
     }
-    if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, t.data(), p, 0, 1);
-    else bdda::warp_fft_lines<false, 1>(s.data(), 0, t.data(), p, 0, 1, nv);
+    if (inverse) bdda::warp_fft_lines<true, 1, bdda::dfzc, true>(s.data(), 0, t.data(), p, 0, 1);
+    else bdda::warp_fft_lines<false, 1, bdda::dfzc, true>(s.data(), 0, t.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
       const bdda::dfzc v = s[bdda::skw(i, sh)];
       data[2 * i] = (double)v.x.hi + (double)v.x.lo; data[2 * i + 1] = (double)v.y.hi + (double)v.y.lo;
@@ -336,8 +344,8 @@ int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, i
       s[bdda::skw(i, sh)] = make_float2((float)data[2 * i], (float)data[2 * i + 1]);
       t[i] = make_float2((float)tw[i].x, (float)tw[i].y);
     }
-    if (inverse) bdda::warp_fft_lines<true, 1>(s.data(), 0, t.data(), p, 0, 1);
-    else bdda::warp_fft_lines<false, 1>(s.data(), 0, t.data(), p, 0, 1, nv);
+    if (inverse) bdda::warp_fft_lines<true, 1, float2, true>(s.data(), 0, t.data(), p, 0, 1);
+    else bdda::warp_fft_lines<false, 1, float2, true>(s.data(), 0, t.data(), p, 0, 1, nv);
     for (int i = 0; i < N; ++i) {
       const float2 v = s[bdda::skw(i, sh)];
       data[2 * i] = v.x; data[2 * i + 1] = v.y;

@@ -1127,6 +1127,13 @@ static int solve_impl(Op* op, const bdda_solve_opts* o, const double2* diag, con
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  {
+    const int ks = take_kernel_status(op, st);  // a pipelined z pass whose copy wait gave up
+    if (ks != BDDA_OK) {
+      if (stats) stats->status = ks;
+      return ks;
+    }
+  }
   if (stats) {
     stats->status = status;
     stats->iterations = total_iters;

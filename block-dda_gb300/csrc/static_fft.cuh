@@ -15,13 +15,20 @@
 // stage s before the last steps through its butterfly in multiples of R_last
 // (M_s is a multiple of it), so its elements are (M_s / R_last) * S apart; the
 // last stage's are adjacent.  Lines are LW elements apart.  The plans come
-// from zplans.inc / tplans.inc / yplans.inc (gen_zplans.py).
+// from zplans.inc / zwplans.inc / tplans.inc / yplans.inc (gen_zplans.py).
 #pragma once
 
 #include "fft_core.cuh"
 
 namespace bdda {
 namespace sfft {
+
+// Twiddle / spectrum load: TS = the table was staged in shared memory (a
+// plain load), else an L1-cached global load.
+template <bool TS, typename C> __device__ __forceinline__ C ldt(const C* p) {
+  if constexpr (TS) return *p;
+  else return ldg_c(p);
+}
 
 template <int N_, int S_, int LW_, int... R>
 struct Plan {
@@ -52,7 +59,7 @@ struct Plan {
 // side), so in those stages (span M = N / R) the butterfly elements i with
 // 2 i >= R are padding in every butterfly: compile-time zero inputs and dead
 // outputs, whose DFT arithmetic the compiler folds away.
-template <class P, int s, bool INV, int NL, typename C = float2>
+template <class P, int s, bool INV, int NL, typename C = float2, bool TS = false>
 __device__ __forceinline__ void stage(C* __restrict__ sm, const C* __restrict__ tw, int lane, int nv) {
   constexpr int R = P::rad[s];
   constexpr int M = P::M(s);
@@ -79,13 +86,13 @@ __device__ __forceinline__ void stage(C* __restrict__ sm, const C* __restrict__ 
       if (M > 1 && n1 != 0) {
         const C* tws = tw + P::TWO(s) + n1;
 #pragma unroll
-        for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tws + (k - 1) * M));
+        for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldt<TS>(tws + (k - 1) * M));
       }
     } else {
       if (M > 1 && n1 != 0) {
         const C* tws = tw + P::TWO(s) + n1;
 #pragma unroll
-        for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tws + (k - 1) * M));
+        for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldt<TS>(tws + (k - 1) * M));
       }
       dft<R, true>(v);
     }
@@ -105,7 +112,7 @@ __device__ __forceinline__ void stage(C* __restrict__ sm, const C* __restrict__ 
 // shared memory: line j's element idx < nv at gsrc[j * gstride + idx] (the
 // zero padding past nv is never read), results stored to the padded shared
 // line as stage<P, 0, false, NL> stores them.
-template <class P, int NL, typename C = float2>
+template <class P, int NL, typename C = float2, bool TS = false>
 __device__ __forceinline__ void stage0_from_global(C* __restrict__ sm, const C* __restrict__ tw, int lane,
                                                    int nv, const C* __restrict__ gsrc, size_t gstride) {
   constexpr int R = P::rad[0];
@@ -122,7 +129,7 @@ __device__ __forceinline__ void stage0_from_global(C* __restrict__ sm, const C* 
     dft<R, false>(v);
     if (M > 1 && n1 != 0) {
 #pragma unroll
-      for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldg_c(tw + (k - 1) * M + n1));
+      for (int k = 1; k < R; ++k) v[k] = cmul(v[k], ldt<TS>(tw + (k - 1) * M + n1));
     }
     C* p = sm + j * P::LW + P::addr(n1);
 #pragma unroll
@@ -133,7 +140,7 @@ __device__ __forceinline__ void stage0_from_global(C* __restrict__ sm, const C* 
 
 // Last inverse stage with its outputs written to global memory: line j's
 // element idx < nv to gdst[j * gstride + idx] (the rest are discarded).
-template <class P, int NL, typename C = float2>
+template <class P, int NL, typename C = float2, bool TS = false>
 __device__ __forceinline__ void stage0_to_global(const C* __restrict__ sm, const C* __restrict__ tw,
                                                  int lane, int nv, C* __restrict__ gdst, size_t gstride) {
   constexpr int R = P::rad[0];
@@ -149,7 +156,7 @@ __device__ __forceinline__ void stage0_to_global(const C* __restrict__ sm, const
     for (int i = 0; i < R; ++i) v[i] = p[i * off];
     if (M > 1 && n1 != 0) {
 #pragma unroll
-      for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldg_c(tw + (k - 1) * M + n1));
+      for (int k = 1; k < R; ++k) v[k] = cmulc(v[k], ldt<TS>(tw + (k - 1) * M + n1));
     }
     dft<R, true>(v);
     C* g = gdst + (size_t)j * gstride + n1;
@@ -178,11 +185,11 @@ __device__ __forceinline__ void forward_from_global(C* sm, const C* tw, int lane
 }
 
 // Forward stages s .. end - 1 of NL lines.
-template <class P, int NL, int s, int end, typename C = float2>
+template <class P, int NL, int s, int end, typename C = float2, bool TS = false>
 __device__ __forceinline__ void forward_to(C* sm, const C* tw, int lane, int nv) {
   if constexpr (s < end) {
-    stage<P, s, false, NL, C>(sm, tw, lane, nv);
-    forward_to<P, NL, s + 1, end, C>(sm, tw, lane, nv);
+    stage<P, s, false, NL, C, TS>(sm, tw, lane, nv);
+    forward_to<P, NL, s + 1, end, C, TS>(sm, tw, lane, nv);
   }
 }
 
@@ -198,7 +205,7 @@ __device__ __forceinline__ void forward_to(C* sm, const C* tw, int lane, int nv)
 // does all three lines of its butterfly, so the spectrum is applied in
 // registers: one shared-memory load and store per element instead of the
 // separate stages' three of each.
-template <class P, typename C>
+template <class P, typename C, bool GS = false>
 __device__ __forceinline__ void middle3(C* __restrict__ sm, const C* __restrict__ gl, int lane) {
   constexpr int R = P::Rl;
   constexpr int B = P::N / R;
@@ -218,8 +225,8 @@ __device__ __forceinline__ void middle3(C* __restrict__ sm, const C* __restrict_
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const C* g = gl + i * B + b;
-      const C gxx = ldg_c(g), gxy = ldg_c(g + P::N), gxz = ldg_c(g + 2 * P::N);
-      const C gyy = ldg_c(g + 3 * P::N), gyz = ldg_c(g + 4 * P::N), gzz = ldg_c(g + 5 * P::N);
+      const C gxx = ldt<GS>(g), gxy = ldt<GS>(g + P::N), gxz = ldt<GS>(g + 2 * P::N);
+      const C gyy = ldt<GS>(g + 3 * P::N), gyz = ldt<GS>(g + 4 * P::N), gzz = ldt<GS>(g + 5 * P::N);
       const C x = e0[i], y = e1[i], z = e2[i];
       e0[i] = cadd(cadd(cmul(gxx, x), cmul(gxy, y)), cmul(gxz, z));
       e1[i] = cadd(cadd(cmul(gxy, x), cmul(gyy, y)), cmul(gyz, z));
@@ -240,11 +247,11 @@ __device__ __forceinline__ void middle3(C* __restrict__ sm, const C* __restrict_
 
 // Inverse transform (unnormalised): digit-reversed in, natural order out,
 // only the first nv outputs written.
-template <class P, int NL, int s = P::nst - 1, int last = 0, typename C = float2>
+template <class P, int NL, int s = P::nst - 1, int last = 0, typename C = float2, bool TS = false>
 __device__ __forceinline__ void inverse(C* sm, const C* tw, int lane, int nv) {
   if constexpr (s >= last) {
-    stage<P, s, true, NL, C>(sm, tw, lane, nv);
-    inverse<P, NL, s - 1, last, C>(sm, tw, lane, nv);
+    stage<P, s, true, NL, C, TS>(sm, tw, lane, nv);
+    inverse<P, NL, s - 1, last, C, TS>(sm, tw, lane, nv);
   }
 }
 

@@ -41,12 +41,27 @@ bool launch_pass_c_static_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz,
          static_z_df_part2(g, t2, L, twz, ghat, st, done, err) || static_z_df_part3(g, t2, L, twz, ghat, st, done, err);
 }
 
+bool pipe_z_available(int Pz, int f, int nzp, int L) {
+  if (f != 3) return false;
+  const int nw = L < kZWarps ? L : kZWarps;
+  switch (Pz) {
+#define BDDA_ZPLAN(I, N, S, LW, ...)                                                      \
+  case N:                                                                                 \
+    return zpipe::supported<sfft::Plan<N, S, LW, __VA_ARGS__>>() &&                       \
+           zpipe::smem_bytes<sfft::Plan<N, S, LW, __VA_ARGS__>>(nw, nzp) <= (size_t)kZSmemMax / 2;
+#include "zplans.inc"
+#undef BDDA_ZPLAN
+    default:
+      return false;
+  }
+}
+
 bool packed_z_available(int Pz, int f) {
   if (f != 3) return false;
   switch (Pz) {
 #define BDDA_ZPLAN(I, N, S, LW, ...) \
   case N:                            \
-    return zpacked::fits<sfft::Plan<N, S, LW, __VA_ARGS__>>();
+    return zpacked::supported<sfft::Plan<N, S, LW, __VA_ARGS__>>() && zpacked::fits<sfft::Plan<N, S, LW, __VA_ARGS__>>();
 #include "zplans.inc"
 #undef BDDA_ZPLAN
     default:

@@ -5,6 +5,7 @@
 
 #include "tile_static.cuh"
 #include "zpass_packed.cuh"
+#include "zpass_pipe.cuh"
 #include "zpass_static.cuh"
 
 namespace bdda {
@@ -20,8 +21,15 @@ bool dispatch_z(const MvpGeom& g, float2* t2, int L, const float2* twz, const fl
   case N:                                                                                \
     if constexpr ((I) % kParts == PART) {                                                \
       using Pl = sfft::Plan<N, S, LW, __VA_ARGS__>;                                      \
-      *err = zpacked::chosen<Pl>(g, twzp) ? zpacked::launch<Pl>(g, t2, L, twzp, ghat, st, done) \
-                                : zstatic::launch<Pl>(g, t2, L, twz, ghat, st, done);    \
+      if constexpr (zpacked::supported<Pl>())                                            \
+        if (zpacked::chosen<Pl>(g, twzp)) {                                              \
+          *err = zpacked::launch<Pl>(g, t2, L, twzp, ghat, st, done);                    \
+          return true;                                                                   \
+        }                                                                                \
+      if ((g.tune.zkern < 0 || g.tune.zkern == 2) &&                                     \
+          zpipe::launch<Pl>(g, t2, L, twz, ghat, st, done, err))                         \
+        return true;                                                                     \
+      *err = zstatic::launch<Pl>(g, t2, L, twz, ghat, st, done);                         \
       return true;                                                                       \
     }                                                                                    \
     return false;
@@ -33,22 +41,22 @@ bool dispatch_z(const MvpGeom& g, float2* t2, int L, const float2* twz, const fl
   return false;
 }
 
-// The double-float z pass of f = 3 operators with the same compile-time plans
-// (the double-float Green spectrum uses the z table's radix order too).
+// The double-float z pass of f = 3 operators with the 16-byte z table's
+// compile-time plans (the double-float Green spectrum is in their digit order).
 template <int PART>
 bool dispatch_z_df(const MvpGeom& g, dfzc* t2, int L, const dfzc* twz, const dfzc* ghat, cudaStream_t st,
                    const int* done, cudaError_t* err) {
   if (g.f != 3) return false;
   switch (g.Pz) {
-#define BDDA_ZPLAN(I, N, S, LW, ...)                                                                  \
+#define BDDA_ZWPLAN(I, N, S, LW, ...)                                                                 \
   case N:                                                                                             \
     if constexpr ((I) % kParts == PART) {                                                             \
       *err = zstatic::launch_f<sfft::Plan<N, S, LW, __VA_ARGS__>, false, dfzc>(g, t2, L, twz, ghat, st, done); \
       return true;                                                                                    \
     }                                                                                                 \
     return false;
-#include "zplans.inc"
-#undef BDDA_ZPLAN
+#include "zwplans.inc"
+#undef BDDA_ZWPLAN
     default:
       break;
   }

@@ -95,11 +95,22 @@ k_pass_c_packed(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp,
 // per N=65536, L=32 block MVP; Pz=120: 0.35 vs 0.31 ms at N=8192, L=16).
 template <class P> constexpr bool worth() { return 3 * kZWarps * 3 * P::LW * 16 <= kZSmemMax; }
 // The packed kernel can run where two 8-warp CTAs fit; between that and
-// worth() the autotuner decides (MvpTune::zpacked).
+// worth() the autotuner decides (MvpTune::zkern).
 template <class P> constexpr bool fits() { return 2 * kZWarps * 3 * P::LW * 16 <= kZSmemMax; }
+// Plans the packed kernel is built for: register radices <= 16 (a pair
+// element takes four registers), and a fused step only up to radix 5 (three
+// lines of 2 R registers of pairs); a plan with a last radix 6..kFusedMaxRadix
+// has the last-radix-major spectrum of the scalar kernel's fused step, which
+// the packed kernel's separate product would read in the wrong order.
+template <class P> constexpr bool supported() {
+  for (int s = 0; s < P::nst; ++s)
+    if (P::rad[s] > 16) return false;
+  return P::nst < 2 || P::Rl <= 5 || P::Rl > kFusedMaxRadix;
+}
 template <class P> bool chosen(const MvpGeom& g, const float4* twzp) {
+  if constexpr (!supported<P>()) return false;
   if (!twzp || g.f != 3 || !fits<P>()) return false;
-  return g.tune.zpacked < 0 ? worth<P>() : g.tune.zpacked == 1;
+  return g.tune.zkern < 0 ? worth<P>() && !(P::nst >= 2 && P::Rl <= kFusedMaxRadix) : g.tune.zkern == 1;
 }
 // Whether the packed kernel is a candidate for this length (autotuner).
 inline bool packed_fits_lw(int lw) { return 2 * kZWarps * 3 * lw * 16 <= kZSmemMax; }

@@ -486,21 +486,30 @@ int bdda_op_set_graphs(bdda_op* op, int on);
  * MVP of an nrhs whose FFT workspace is at least 64 MiB times, with CUDA
  * events on the operator's own buffers, the candidates of each tile pass's
  * launch schedule -- y passes double- or single-buffered with a grid of 1, 2,
- * 4 or 8 waves of the resident CTAs, scalar or packed-pair z pass where both
- * fit, x passes aiming at 5, 10 or 20
- * CTAs per SM -- and keeps the fastest (also for later operators of the same
- * box, occupancy and nrhs in this process).  Not inside stream capture.  The
- * schedules only reorder work: results equal the default schedule's bitwise,
- * except that the packed and scalar z passes round differently (FP32 MVP
- * tolerance).  on = 0 restores the defaults and forgets the choices. */
+ * 4 or 8 waves of the resident CTAs, the scalar, packed-pair or pipelined z
+ * pass where they run the geometry, x passes aiming at 5, 10 or 20 CTAs per
+ * SM -- and keeps the fastest (also for later operators of the same box,
+ * occupancy and nrhs in this process).  Not inside stream capture.  The
+ * schedules only reorder work: results equal the default schedule's bitwise
+ * (the pipelined and scalar z passes too), except that the packed z pass
+ * rounds differently (FP32 MVP tolerance).  on = 0 restores the defaults and
+ * forgets the choices. */
 int bdda_op_set_autotune(bdda_op* op, int on);
 /* The schedule in use for nrhs L: schedule = {y waves, y buffers, z pass (-1
- * default rule, 0 scalar, 1 packed), x CTAs per SM}; candidate_ms (may be
- * null): measured ms of pass B with 1 then 2 buffers x waves 1, 2, 4, 8
- * ([0..7]), pass C scalar / packed ([8..9]), pass A at 5, 10, 20 CTAs per SM
- * ([10..12]), -1 where not measured.  BDDA_ERR_NOT_CONVERGED when L was not
- * tuned (defaults returned). */
-int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[13]);
+ * default rule, 0 scalar, 1 packed, 2 pipelined), x CTAs per SM};
+ * candidate_ms (may be null): measured ms of pass B with 1 then 2 buffers x
+ * waves 1, 2, 4, 8 ([0..7]), pass C scalar / packed ([8..9]), pass A at 5,
+ * 10, 20 CTAs per SM ([10..12]), pass C pipelined ([13]), -1 where not
+ * measured.  BDDA_ERR_NOT_CONVERGED when L was not tuned (defaults
+ * returned). */
+int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[14]);
+/* Reads and clears the operator's kernel status word.  The pipelined z pass
+ * (complex FP32) waits on its bulk copies for at most 2 s; a wait that gives
+ * up (never expected) sets the word and the MVP's results are invalid.
+ * bdda_solve / bdda_solve_device read it at their end; after
+ * bdda_op_mvp_device, synchronise its stream and call this.  BDDA_OK, or
+ * BDDA_ERR_CUDA with a message. */
+int bdda_op_check_status(bdda_op* op);
 
 /*
  * Per-kernel totals since the last reset: ms[i], launches[i] for

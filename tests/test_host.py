@@ -87,10 +87,19 @@ def test_device_fft_core_on_cpu(N):
     assert int(np.prod(r16)) == N and max(r16) <= 16
     assert np.allclose(np.sort_complex(np.round(f16, 8)), np.sort_complex(np.round(ref, 8)))
     assert np.max(np.abs(c16 / N - cref)) / np.max(np.abs(cref)) < 2e-15
-    f16s, _ = bdda.host_fft_line(a, prec=2, max_radix=16)
-    g16s, _ = bdda.host_fft_line(b, prec=2, max_radix=16)
-    c16s, _ = bdda.host_fft_line(f16s * g16s, inverse=True, prec=2, max_radix=16)
-    assert np.max(np.abs(c16s / N - cref)) / np.max(np.abs(cref)) < 1e-6
+    # the complex FP32 z schedule (first-stage radices up to 32): FP32 arithmetic, and FP64 as the
+    # Green spectrum's transform runs it, in the same digit order
+    f32s, r32 = bdda.host_fft_line(a, prec=2, max_radix=16)
+    g32s, _ = bdda.host_fft_line(b, prec=2, max_radix=16)
+    c32s, _ = bdda.host_fft_line(f32s * g32s, inverse=True, prec=2, max_radix=16)
+    assert int(np.prod(r32)) == N and max(r32) <= 32 and all(r <= 16 for r in r32[1:])
+    assert np.max(np.abs(c32s / N - cref)) / np.max(np.abs(cref)) < 1e-6
+    f32d, r32d = bdda.host_fft_line(a, prec=1, max_radix=32)
+    g32d, _ = bdda.host_fft_line(b, prec=1, max_radix=32)
+    c32d, _ = bdda.host_fft_line(f32d * g32d, inverse=True, prec=1, max_radix=32)
+    assert r32d == r32
+    assert np.max(np.abs(f32d - f32s)) <= 1e-5 * np.max(np.abs(f32d))
+    assert np.max(np.abs(c32d / N - cref)) / np.max(np.abs(cref)) < 2e-15
     # pruned input: only the first nv values are read (the rest are poisoned in the hook)
     nv = max(1, N // 2)
     ap = a.copy()

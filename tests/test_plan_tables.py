@@ -6,7 +6,11 @@
   take their sequences from tplans.inc;
 * every layout holds its line: element q R_last + r at q S + r with
   S >= R_last, so the last element sits below the pitch LW;
-* the generator reproduces the committed yplans.inc.
+* the generator reproduces the committed yplans.inc, and the complex FP32 z
+  table's entries for the default workload's lengths;
+* only the first stage of a complex FP32 z plan takes a radix above 16 (the
+  register radices of every other kernel), the 16-byte z table none, and both
+  z tables list the same lengths.
 """
 import importlib.util
 import os
@@ -41,8 +45,8 @@ def test_y_table_keeps_the_radix_sequences():
         assert t[n][2] == y[n][2], n
 
 
-@pytest.mark.parametrize("name,macro", [("zplans.inc", "BDDA_ZPLAN"), ("tplans.inc", "BDDA_TPLAN"),
-                                        ("yplans.inc", "BDDA_YPLAN")])
+@pytest.mark.parametrize("name,macro", [("zplans.inc", "BDDA_ZPLAN"), ("zwplans.inc", "BDDA_ZWPLAN"),
+                                        ("tplans.inc", "BDDA_TPLAN"), ("yplans.inc", "BDDA_YPLAN")])
 def test_layouts_hold_their_lines(name, macro):
     tab = _table(name, macro)
     assert tab
@@ -65,3 +69,22 @@ def test_generator_reproduces_the_y_table(tmp_path):
                g.cost_y_il, rad)
     with open(os.path.join(CSRC, "yplans.inc")) as f:
         assert out.read_text() == f.read()
+
+
+def test_z_tables_radix_limits():
+    z = _table("zplans.inc", "BDDA_ZPLAN")
+    zw = _table("zwplans.inc", "BDDA_ZWPLAN")
+    assert sorted(z) == sorted(zw)
+    for n, (_, _, rad) in z.items():
+        assert rad[0] <= 32 and all(r <= 16 for r in rad[1:]), (n, rad)
+    for n, (_, _, rad) in zw.items():
+        assert all(r <= 16 for r in rad), (n, rad)
+    # the default workload's z length: two stages, fused last radix
+    assert z[250][2] == (25, 10) and z[243][2] == (27, 9)
+
+
+@pytest.mark.parametrize("n", [125, 243, 250])
+def test_generator_reproduces_z_entries(n):
+    g = _gen()
+    rad, S, LW = g.choose(n, g.cost_zf, g.FIRST_RADICES, g.Z_MAX_PAD)
+    assert _table("zplans.inc", "BDDA_ZPLAN")[n] == (S, LW, tuple(rad))
