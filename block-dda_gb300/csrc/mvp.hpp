@@ -258,7 +258,8 @@ bool launch_pass_c_static(const MvpGeom& g, float2* t2, int L, const float2* twz
 // Whether the packed-pair pass C can run for z length Pz and f (an autotuner
 // candidate besides the scalar kernel).
 bool packed_z_available(int Pz, int f);
-// Whether the pipelined z pass (zpass_pipe.cuh) runs this geometry at nrhs L.
+// Whether the pipelined z pass (zpass_pipe.cuh) can run this geometry at nrhs
+// L (an autotuner candidate; the default rule also wants two CTAs per SM).
 bool pipe_z_available(int Pz, int f, int nzp, int L);
 
 // Pass C of a double-float block MVP (f = 3) with the compile-time z plan of

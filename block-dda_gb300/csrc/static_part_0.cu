@@ -47,8 +47,7 @@ bool pipe_z_available(int Pz, int f, int nzp, int L) {
   switch (Pz) {
 #define BDDA_ZPLAN(I, N, S, LW, ...)                                                      \
   case N:                                                                                 \
-    return zpipe::supported<sfft::Plan<N, S, LW, __VA_ARGS__>>() &&                       \
-           zpipe::smem_bytes<sfft::Plan<N, S, LW, __VA_ARGS__>>(nw, nzp) <= (size_t)kZSmemMax / 2;
+    return zpipe::smem_bytes<sfft::Plan<N, S, LW, __VA_ARGS__>>(nw, nzp) <= (size_t)kZSmemMax;
 #include "zplans.inc"
 #undef BDDA_ZPLAN
     default:

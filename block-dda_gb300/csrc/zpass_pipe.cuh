@@ -1,8 +1,9 @@
-// Pipelined fused z pass (pass C) for complex FP32, f = 3, fused plans.
+// Pipelined fused z pass (pass C) for complex FP32, f = 3.
 //
-// The same arithmetic as zstatic::k_pass_c_static's fused path (first forward
-// stage, stages up to the last, fused last stage / Green product / first
-// inverse stage, inverse stages, last inverse stage; static_fft.cuh), run by
+// The same arithmetic as zstatic::k_pass_c_static (first forward stage, the
+// other forward stages, the Green product -- fused with the last forward and
+// first inverse stage where the plan allows, sfft::middle3 -- the inverse
+// stages, the last inverse stage; static_fft.cuh, zproduct.cuh), run by
 // persistent CTAs that keep every load of the compute phases in shared
 // memory:
 //
@@ -32,11 +33,14 @@
 #include "async_copy.cuh"
 #include "mvp.hpp"
 #include "static_fft.cuh"
+#include "zproduct.cuh"
 
 namespace bdda {
 namespace zpipe {
 
-template <class P> constexpr bool supported() { return P::nst >= 2 && P::Rl <= kFusedMaxRadix; }
+// Plans whose last stage, product and first inverse stage are one step (the
+// complex FP32 spectrum is then last-radix-major, green_perm_radix).
+template <class P> constexpr bool fused() { return P::nst >= 2 && P::Rl <= kFusedMaxRadix; }
 
 // Staging row pitch (complex values): even (16-byte rows for the bulk copies)
 // and congruent to the first stage's span M0 (or M0 + 1) modulo 16, so the
@@ -134,12 +138,20 @@ k_pass_c_pipe(float2* __restrict__ t2, int L, int nlines, int nz, int nzp, const
       }
       xpend = true;
     }
-    sfft::forward_to<P, 3, 1, P::nst - 1, float2, true>(wl, tws, lane, nz);
+    sfft::forward_to<P, 3, 1, fused<P>() ? P::nst - 1 : P::nst, float2, true>(wl, tws, lane, nz);
     ok = __all_sync(0xffffffffu, !*abort_flag && acp::wait(&gbar[k & 1], (uint32_t)((k >> 1) & 1)));
     if (!ok) break;
-    sfft::middle3<P, float2, true>(wl, gs + (k & 1) * 6 * Pz, lane);
+    const float2* gl = gs + (k & 1) * 6 * Pz;
+    if constexpr (fused<P>()) {
+      sfft::middle3<P, float2, true>(wl, gl, lane);
+    } else {
+      for (int p = lane; p < Pz; p += 32) z_product<float2, true>(wl, LW, P::addr(p), gl, Pz, p, false);
+      __syncwarp();
+    }
     if (l + nw >= L && lane == 0) {  // this warp's last Green step of line k
+      __threadfence_block();         // its reads of the spectrum buffer before the count
       if (atomicAdd(&gdone[k & 1], 1) == nw - 1) {
+        __threadfence_block();       // every warp's reads before the refill
         gdone[k & 1] = 0;
         if (k + 2 < nk && !*abort_flag) {
           acp::fence_proxy_async();
@@ -147,7 +159,7 @@ k_pass_c_pipe(float2* __restrict__ t2, int L, int nlines, int nz, int nzp, const
         }
       }
     }
-    sfft::inverse<P, 3, P::nst - 2, 1, float2, true>(wl, tws, lane, nz);
+    sfft::inverse<P, 3, fused<P>() ? P::nst - 2 : P::nst - 1, 1, float2, true>(wl, tws, lane, nz);
     sfft::stage0_to_global<P, 3, float2, true>(wl, tws, lane, nz, rows(k, l), fstride);
     k = k2;
     l = l2;
@@ -168,42 +180,40 @@ k_pass_c_pipe(float2* __restrict__ t2, int L, int nlines, int nz, int nzp, const
 }
 
 // Launches the pipelined kernel; false (nothing launched) where it does not
-// apply: plan not fused, no status word, or less than two CTAs per SM.
+// apply: f = 6, no status word, a CTA's shared memory above the limit, or --
+// under the default rule (MvpTune::zkern < 0) -- less than two CTAs per SM
+// (the autotuner may still pick it with one).
 template <class P>
 bool launch(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2* ghat, cudaStream_t st,
             const int* done, cudaError_t* err) {
-  if constexpr (!supported<P>()) {
-    return false;
-  } else {
-    if (g.f != 3 || !g.kstat || g.gperm != P::Rl) return false;
-    const int nw = L < kZWarps ? L : kZWarps;
-    const size_t bytes = smem_bytes<P>(nw, g.nzp);
-    if (bytes > (size_t)kZSmemMax / 2) return false;
-    static std::once_flag once;
-    static cudaError_t cfg = cudaSuccess;
-    static int nsm = 0;
-    std::call_once(once, [] {
-      cfg = cudaFuncSetAttribute(k_pass_c_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, kZSmemMax);
-      int dev = 0;
-      if (cfg == cudaSuccess) cfg = cudaGetDevice(&dev);
-      if (cfg == cudaSuccess) cfg = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    });
-    if (cfg != cudaSuccess) {
-      *err = cfg;
-      return true;
-    }
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass_c_pipe<P>, nw * 32, bytes);
-    if (e != cudaSuccess || per_sm < 1) {
-      *err = e != cudaSuccess ? e : cudaErrorInvalidConfiguration;
-      return true;
-    }
-    const long long nlines = (long long)g.Px * g.Py;
-    const long long grid = std::min<long long>(nlines, (long long)per_sm * nsm);
-    k_pass_c_pipe<P><<<(unsigned)grid, nw * 32, bytes, st>>>(t2, L, (int)nlines, g.nz, g.nzp, twz, ghat, done, g.kstat);
-    *err = cudaGetLastError();
+  if (g.f != 3 || !g.kstat || g.gperm != (fused<P>() ? P::Rl : 0)) return false;
+  const int nw = L < kZWarps ? L : kZWarps;
+  const size_t bytes = smem_bytes<P>(nw, g.nzp);
+  if (bytes > (size_t)(g.tune.zkern == 2 ? kZSmemMax : kZSmemMax / 2)) return false;
+  static std::once_flag once;
+  static cudaError_t cfg = cudaSuccess;
+  static int nsm = 0;
+  std::call_once(once, [] {
+    cfg = cudaFuncSetAttribute(k_pass_c_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, kZSmemMax);
+    int dev = 0;
+    if (cfg == cudaSuccess) cfg = cudaGetDevice(&dev);
+    if (cfg == cudaSuccess) cfg = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  });
+  if (cfg != cudaSuccess) {
+    *err = cfg;
     return true;
   }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass_c_pipe<P>, nw * 32, bytes);
+  if (e != cudaSuccess || per_sm < 1) {
+    *err = e != cudaSuccess ? e : cudaErrorInvalidConfiguration;
+    return true;
+  }
+  const long long nlines = (long long)g.Px * g.Py;
+  const long long grid = std::min<long long>(nlines, (long long)per_sm * nsm);
+  k_pass_c_pipe<P><<<(unsigned)grid, nw * 32, bytes, st>>>(t2, L, (int)nlines, g.nz, g.nzp, twz, ghat, done, g.kstat);
+  *err = cudaGetLastError();
+  return true;
 }
 
 }  // namespace zpipe

@@ -13,18 +13,24 @@
 
 namespace bdda {
 
-template <typename C>
+// GS: the spectrum was staged in shared memory (plain loads), else L1-cached
+// global loads.
+template <typename C, bool GS = false>
 __device__ __forceinline__ void z_product(C* __restrict__ s, int lw, int a, const C* __restrict__ gl, int Pz, int p,
                                           bool six) {
+  auto ld = [](const C* q) -> C {
+    if constexpr (GS) return *q;
+    else return ldg_c(q);
+  };
   const C e0 = s[a], e1 = s[lw + a], e2 = s[2 * lw + a];
-  const C gxx = ldg_c(gl + p), gxy = ldg_c(gl + Pz + p), gxz = ldg_c(gl + 2 * Pz + p);
-  const C gyy = ldg_c(gl + 3 * Pz + p), gyz = ldg_c(gl + 4 * Pz + p), gzz = ldg_c(gl + 5 * Pz + p);
+  const C gxx = ld(gl + p), gxy = ld(gl + Pz + p), gxz = ld(gl + 2 * Pz + p);
+  const C gyy = ld(gl + 3 * Pz + p), gyz = ld(gl + 4 * Pz + p), gzz = ld(gl + 5 * Pz + p);
   C ox = cadd(cadd(cmul(gxx, e0), cmul(gxy, e1)), cmul(gxz, e2));
   C oy = cadd(cadd(cmul(gxy, e0), cmul(gyy, e1)), cmul(gyz, e2));
   C oz = cadd(cadd(cmul(gxz, e0), cmul(gyz, e1)), cmul(gzz, e2));
   if (six) {
     const C m0 = s[3 * lw + a], m1 = s[4 * lw + a], m2 = s[5 * lw + a];
-    const C bxy = ldg_c(gl + 6 * Pz + p), bxz = ldg_c(gl + 7 * Pz + p), byz = ldg_c(gl + 8 * Pz + p);
+    const C bxy = ld(gl + 6 * Pz + p), bxz = ld(gl + 7 * Pz + p), byz = ld(gl + 8 * Pz + p);
     // E' = A E + B M
     ox = cadd(ox, cadd(cmul(bxy, m1), cmul(bxz, m2)));
     oy = cadd(oy, csub(cmul(byz, m2), cmul(bxy, m0)));
