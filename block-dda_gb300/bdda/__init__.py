@@ -559,16 +559,17 @@ def cross_sections(k, alpha0, E, P, alpha_h0=None):
     return out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy()
 
 
-def host_fft_line(x, inverse=False, prec=1, nvalid=0, max_radix=8):
+def host_fft_line(x, inverse=False, prec=1, nvalid=0, max_radix=8, c64_schedule=False):
     """Run the device FFT core on the CPU (unit tests).  Returns (y, radices).
 
     The schedule is the operator's for an axis of this length and the element
     width of prec: max_radix > 8 selects the z axis (three-line fused pass),
-    otherwise the x / y axes; max_radix = 32 the complex FP32 z schedule
-    (first-stage radices up to 32) in any arithmetic."""
+    otherwise the x / y axes; c64_schedule the complex FP32 schedule (first-
+    stage radices up to 32) in any arithmetic."""
     a = np.ascontiguousarray(x, dtype=np.complex128).copy()
     rad = np.zeros(16, np.int32)
     rad[0] = int(max_radix)
+    rad[1] = 1 if c64_schedule else 0
     nst = lib().bdda_host_fft_line(int(a.size), 1 if inverse else 0, int(prec), int(nvalid), _dptr(a), _iptr(rad))
     if nst < 0:
         raise BddaError(ERR_INVALID, "unsupported FFT length")

@@ -117,7 +117,7 @@ k_fft_strided(double2* __restrict__ data, size_t Cc, AxisPlan p, const double2* 
     smem[w * lw + skw(i, sh)] = (c < Cc) ? base[(size_t)i * Cc + c] : make_double2(0.0, 0.0);
   }
   __syncthreads();
-  warp_fft_lines<false, 1>(smem + (tid >> 5) * lw, 0, tw, p, tid & 31);
+  warp_fft_lines<false, 1, double2, true>(smem + (tid >> 5) * lw, 0, tw, p, tid & 31);
   __syncthreads();
   for (int idx = tid; idx < N * kInitWarps; idx += kInitWarps * 32) {
     const int w = idx % kInitWarps, i = idx / kInitWarps;

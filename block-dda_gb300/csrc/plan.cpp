@@ -302,13 +302,13 @@ extern "C" {
 // transform reads only the first nvalid inputs and takes the rest as zero
 // (the pad slots hold poison values to prove it).  radix[0] > 8 on input: the
 // z-axis schedule, else the x / y one, each for the element width of prec;
-// radix[0] = 32: the complex FP32 z schedule in any arithmetic (its Green
-// spectrum is transformed in FP64).  Returns the number of stages, or a
+// radix[1] = 1 on input: the complex FP32 schedule in any arithmetic (its
+// Green spectrum is transformed in FP64).  Returns the number of stages, or a
 // negative value for an unsupported N.  Radices are written to radix (<= 32).
 int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, int* radix) {
   bdda::AxisPlan p;
   const bool three = radix && radix[0] > 8;
-  const bool wide = (radix && radix[0] == 32) ? false : prec != 2;
+  const bool wide = (radix && radix[1] == 1) ? false : prec != 2;
   if (!bdda::make_axis_plan(N, &p, three, wide)) return -1;
   std::vector<double2> tw;
   bdda::make_twiddles(N, &tw);

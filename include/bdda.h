@@ -533,9 +533,11 @@ const char* bdda_last_error(void);
  * rest count as zero); 0 reads all.  data holds N interleaved complex doubles,
  * overwritten.  The schedule is the one the operator gives an axis of that
  * length for the element width of prec: radix[0] on input > 8 selects the z
- * axis (fused three-line pass), otherwise the x / y axes (single-line tile
- * passes).  Radices are written to radix[0..16) on return.  Returns the
- * number of radix stages or -1 for an unsupported N.
+ * axis (fused three-line pass), otherwise the x / y axes (tile passes);
+ * radix[1] = 1 on input selects the complex FP32 schedule whatever prec (the
+ * one its Green spectrum is transformed with in FP64).  Radices are written
+ * to radix[0..16) on return.  Returns the number of radix stages or -1 for
+ * an unsupported N.
  */
 int bdda_host_fft_line(int N, int inverse, int prec, int nvalid, double* data, int* radix);
 

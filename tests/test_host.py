@@ -94,12 +94,13 @@ def test_device_fft_core_on_cpu(N):
     c32s, _ = bdda.host_fft_line(f32s * g32s, inverse=True, prec=2, max_radix=16)
     assert int(np.prod(r32)) == N and max(r32) <= 32 and all(r <= 16 for r in r32[1:])
     assert np.max(np.abs(c32s / N - cref)) / np.max(np.abs(cref)) < 1e-6
-    f32d, r32d = bdda.host_fft_line(a, prec=1, max_radix=32)
-    g32d, _ = bdda.host_fft_line(b, prec=1, max_radix=32)
-    c32d, _ = bdda.host_fft_line(f32d * g32d, inverse=True, prec=1, max_radix=32)
-    assert r32d == r32
-    assert np.max(np.abs(f32d - f32s)) <= 1e-5 * np.max(np.abs(f32d))
-    assert np.max(np.abs(c32d / N - cref)) / np.max(np.abs(cref)) < 2e-15
+    for mr, f32, r32x in ((16, f32s, r32), (8, fa32, None)):   # z, then the x / y schedule
+        f32d, r32d = bdda.host_fft_line(a, prec=1, max_radix=mr, c64_schedule=True)
+        g32d, _ = bdda.host_fft_line(b, prec=1, max_radix=mr, c64_schedule=True)
+        c32d, _ = bdda.host_fft_line(f32d * g32d, inverse=True, prec=1, max_radix=mr, c64_schedule=True)
+        assert r32x is None or r32d == r32x
+        assert np.max(np.abs(f32d - f32)) <= 1e-5 * np.max(np.abs(f32d))
+        assert np.max(np.abs(c32d / N - cref)) / np.max(np.abs(cref)) < 2e-15
     # pruned input: only the first nv values are read (the rest are poisoned in the hook)
     nv = max(1, N // 2)
     ap = a.copy()
