@@ -250,18 +250,21 @@ struct bdda_server {
     if (rc == BDDA_OK) rc = bdda_solve(op, &opts, r.diag, r.B, f * r.nocc, r.X, f * r.nocc, r.L, &st);
     if ((rc == BDDA_ERR_BREAKDOWN || rc == BDDA_ERR_NOT_CONVERGED) && opts.precision == BDDA_SOLVE_MIXED &&
         !(key.prec & BDDA_PREC_FP64)) {
-      // A mixed solve that broke down or stagnated on FP32 Krylov: solve again on
-      // an operator that also holds FP64 tables, so that the refinement can
-      // continue with FP64 inner solves (the operator is not cached: its key
-      // would not match later requests')
+      // A mixed solve that broke down or stagnated on FP32 Krylov: solve again
+      // in FP64 on an operator with FP64 tables, starting from the mixed
+      // solve's iterate (the solver restarts from zero if that is no better;
+      // the operator is not cached: its key would not match later requests')
       bdda_op_destroy(op);
       op = nullptr;
-      rc = bdda_op_create(&op, r.n, f, r.lf, r.k_re, r.k_im, BDDA_PREC_FP64 | BDDA_PREC_FP32 | BDDA_PREC_DF64);
+      rc = bdda_op_create(&op, r.n, f, r.lf, r.k_re, r.k_im, BDDA_PREC_FP64);
       if (rc == BDDA_OK) rc = bdda_op_set_graphs(op, 0);
       if (rc == BDDA_OK) rc = bdda_op_set_autotune(op, 0);
       if (rc == BDDA_OK) rc = bdda_op_set_dipoles(op, r.address, r.nocc);
+      bdda_solve_opts o64 = opts;
+      o64.precision = BDDA_SOLVE_FP64;
+      o64.warm_start = 1;
       bdda_solve_stats st2{};
-      if (rc == BDDA_OK) rc = bdda_solve(op, &opts, r.diag, r.B, f * r.nocc, r.X, f * r.nocc, r.L, &st2);
+      if (rc == BDDA_OK) rc = bdda_solve(op, &o64, r.diag, r.B, f * r.nocc, r.X, f * r.nocc, r.L, &st2);
       st2.iterations += st.iterations;
       st2.refinements += st.refinements;
       st = st2;

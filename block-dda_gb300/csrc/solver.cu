@@ -23,7 +23,7 @@ namespace bdda {
 
 // Iteration cap of an FP32 inner solve of a mixed refinement (the FP64
 // fallback of the refinement loop takes over where FP32 Krylov stalls).
-constexpr int kMixedInnerCap = 400;
+constexpr int kMixedInnerCap = 200;
 
 // ---------------------------------------------------------------------------
 // small-state slots (each L x L complex FP64, column-major)

@@ -217,8 +217,8 @@ typedef struct {
   double true_res_max;
   double t_submit, t_start, t_done;   /* seconds since the server started (steady clock) */
   double footprint_bytes;             /* device memory reserved for the request */
-  int retried_fp64;                   /* 1: the mixed solve broke down or stagnated and was solved again on an
-                                         operator with FP64 tables (FP64 inner solves where FP32 stalls) */
+  int retried_fp64;                   /* 1: the mixed solve broke down or stagnated and was solved again in
+                                         FP64, starting from the mixed solve's iterate */
 } bdda_request_result;
 
 /* Device-memory footprint the server reserves for one f = 3 request (bytes). */
