@@ -356,19 +356,34 @@ k_pass_a2i(const float2* __restrict__ x, int ldx, int nfield, int fpg, int fc, c
   __syncthreads();
   const size_t rowstride = (size_t)ny * nzp;
   const int fend = min(nfield, (blockIdx.y + 1) * fpg);  // this CTA's fields: [blockIdx.y fpg, fend)
+  // The gathered sites of a warp's column pair (element t = 2 xi + column,
+  // t < 2 nx <= Px) are loaded into registers one field pair ahead: the loads
+  // of field f + 2 are in flight while field f is transformed and drained.
+  constexpr int kPre = (Px + 31) / 32;
+  float2 pre[kPre];
+  auto gather = [&](int fh) {
+    const int l = fh / fc, c = fh - l * fc;
+    const float2* xc = x + (size_t)l * ldx + c;
+#pragma unroll
+    for (int j = 0; j < kPre; ++j) {
+      const int t = lane + 32 * j;
+      const int m = t < 2 * nx ? socc[(t >> 1) * kTZ + 2 * wp + (t & 1)] : -1;
+      pre[j] = m >= 0 ? xc[fc * (size_t)m] : make_float2(0.f, 0.f);
+    }
+  };
+  if (blockIdx.y * fpg + wh < fend) gather(blockIdx.y * fpg + wh);
   for (int f = blockIdx.y * fpg, it = 0; f < fend; f += 2, ++it) {
     const int buf = it & 1;
     const int nh = f + 1 < fend ? 2 : 1;
     if (wh < nh) {
-      const int fh = f + wh, l = fh / fc, c = fh - l * fc;
-      const float2* xc = x + (size_t)l * ldx + c;
       float2* blk = x2i_block<P>(lines, buf, wh, wp);
-      for (int t = lane; t < 2 * nx; t += 32) {
-        const int xi = t >> 1, hc = t & 1;
-        const int m = socc[xi * kTZ + 2 * wp + hc];
-        blk[2 * P::addr(xi) + hc] = m >= 0 ? xc[fc * (size_t)m] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < kPre; ++j) {
+        const int t = lane + 32 * j;
+        if (t < 2 * nx) blk[2 * P::addr(t >> 1) + (t & 1)] = pre[j];
       }
       __syncwarp();
+      if (f + 2 + wh < fend) gather(f + 2 + wh);
       sfft::forward_il<P>(blk, twx, lane, nx);
     }
     __syncthreads();
