@@ -40,7 +40,7 @@ EXPORTS = [
     "bdda_material_load", "bdda_material_constant", "bdda_material_eval", "bdda_material_destroy",
     "bdda_polarizabilities", "bdda_diag_a", "bdda_op_set_wavenumber", "bdda_sweep", "bdda_mie_q",
     "bdda_format_result", "bdda_request_footprint_f", "bdda_server_set_spectrum_cache", "bdda_server_cache_stats",
-    "bdda_op_set_autotune", "bdda_op_get_tuning", "bdda_op_check_status",
+    "bdda_op_set_autotune", "bdda_op_get_tuning", "bdda_op_check_status", "bdda_op_set_z_kernel",
 ]
 
 SHAPES = {"sphere": 0, "cube": 1, "ellipsoid": 2, "cuboid": 3, "cylinder": 4, "rounded_cylinder": 5}
@@ -173,6 +173,7 @@ def lib(build_if_missing: bool = False):
     L.bdda_op_set_autotune.argtypes = [vp, ct.c_int]
     L.bdda_op_get_tuning.argtypes = [vp, ct.c_int, ip, ct.POINTER(ct.c_float)]
     L.bdda_op_check_status.argtypes = [vp]
+    L.bdda_op_set_z_kernel.argtypes = [vp, ct.c_int]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
     L.bdda_last_error.restype = ct.c_char_p
     L.bdda_request_footprint.argtypes = [ip, ct.c_int, ct.c_int, ct.c_int]
@@ -318,13 +319,17 @@ class Operator:
         ms = (ct.c_float * 14)()
         rc = lib().bdda_op_get_tuning(self._h, int(L), _iptr(sch), ms)
         _check(rc, (ERR_NOT_CONVERGED,))
-        cand = {"y": {f"buf{1 + i // 4}_waves{(1, 2, 4, 8)[i % 4]}": ms[i] for i in range(8)},
+        cand = {"y": {f"buf{1 + i // 4}_waves{(2, 4, 8, 16)[i % 4]}": ms[i] for i in range(8)},
                 "z_pass": {"scalar": ms[8], "packed": ms[9], "pipelined": ms[13]},
                 "x_cta_per_sm": {str(v): ms[10 + i] for i, v in enumerate((5, 10, 20))}}
         return ({"y_waves": int(sch[0]), "y_buffers": int(sch[1]),
                  "z_pass": {-1: "default", 0: "scalar", 1: "packed", 2: "pipelined"}[int(sch[2])],
                  "x_cta_per_sm": int(sch[3])},
                 cand, rc == OK)
+
+    def set_z_kernel(self, kind="default"):
+        """Force the complex FP32 pass C kernel: "default", "scalar", "packed" or "pipelined"."""
+        _check(lib().bdda_op_set_z_kernel(self._h, {"default": -1, "scalar": 0, "packed": 1, "pipelined": 2}[kind]))
 
     def check_status(self):
         """Raise if a kernel of this operator reported a failed bounded wait (bdda_op_check_status)."""

@@ -284,14 +284,30 @@ def choose(n, cost, first=RADICES, max_pad=None):
     return best[1], best[2], best[3]
 
 
-def write(path, macro, what, cost, first=RADICES, max_pad=None):
+FUSED_WIDE_MIN_N = 181  # kFusedWideMinN: shorter z lines keep the packed-pair kernel's plans
+
+
+def z_entry(n):
+    """Plan of the complex FP32 z table.  Lines shorter than FUSED_WIDE_MIN_N
+    (the packed-pair z pass's range: three 8-warp CTAs of it fit up to a
+    pitch of ~200) keep the 16-byte table's plan (cost_z, radices <= 16, a
+    fused step only up to radix 5), on which the packed kernel was measured
+    faster than the two-stage fused plans (N=16384, Pz=150: packed 10 x 15
+    0.64 ms, pipelined 15 x 10 0.76 ms); longer lines take the two-stage fused
+    model (cost_zf, first-stage radices up to 32)."""
+    if n < FUSED_WIDE_MIN_N:
+        return choose(n, cost_z)
+    return choose(n, cost_zf, FIRST_RADICES, Z_MAX_PAD)
+
+
+def write(path, macro, what, cost, first=RADICES, max_pad=None, entry=None):
     lines = ["// Generated by gen_zplans.py: compile-time plans of the %s." % what,
              "// %s(index, N, S, LW, radices...): element q*R_last + r at q*S + r, lines LW apart." % macro]
     idx = 0
     for n in range(2, 513):
         if not smooth(n):
             continue
-        rad, S, LW = choose(n, cost, first, max_pad)
+        rad, S, LW = entry(n) if entry else choose(n, cost, first, max_pad)
         lines.append("%s(%d, %d, %d, %d, %s)" % (macro, idx, n, S, LW, ", ".join(str(r) for r in rad)))
         idx += 1
         print(macro, n, rad, S, LW, file=sys.stderr, flush=True)
@@ -339,7 +355,7 @@ def main():
         return
     if "z" in which:
         write(os.path.join(here, "zplans.inc"), "BDDA_ZPLAN", "complex FP32 fused z pass (three lines per warp)",
-              cost_zf, FIRST_RADICES, Z_MAX_PAD)
+              cost_zf, entry=z_entry)
     if "zw" in which:
         write(os.path.join(here, "zwplans.inc"), "BDDA_ZWPLAN",
               "16-byte (FP64 / double-float) z passes (three lines per warp)", cost_z)

@@ -16,7 +16,7 @@ constexpr int kTileThreads = kTZ * 32;
 constexpr int kZWarps = 8;
 // The fused z pass (f = 3) runs its last forward stage, the Green product and
 // its first inverse stage in one sweep (sfft::middle3 / pk::middle3) when the
-// z plan has two or more stages and a last radix Rl <= kFusedMaxRadix; a
+// z plan has two or more stages and a last radix Rl <= kFusedMaxRadix (fused_z); a
 // thread then takes the Rl adjacent frequencies b Rl .. b Rl + Rl - 1 of a
 // butterfly b, so the complex FP32 Green spectrum of such operators is stored
 // last-radix-major (frequency b Rl + i at i (Pz / Rl) + b): the lanes' loads
@@ -24,13 +24,20 @@ constexpr int kZWarps = 8;
 // table's first-stage radices up to 32, most lengths are two stages with a
 // fused last radix (250 = 25 x 10, 243 = 27 x 9, 270 = 27 x 10): the first
 // stage reads T2 and writes shared memory, the fused step reads and writes it
-// once, the last inverse stage reads it and writes T2.  The packed kernel
-// fuses only up to radix 5 (zpacked::supported).
+// once, the last inverse stage reads it and writes T2.  Shorter lines (below
+// kFusedWideMinN points, the packed-pair kernel's range) keep plans of radices
+// <= 16 and fuse only up to radix 5, the packed kernel's limit
+// (zpacked::supported).
 constexpr int kFusedMaxRadix = 10;
+constexpr int kFusedMaxRadixShort = 5;
+constexpr int kFusedWideMinN = 181;
+BDDA_HD constexpr bool fused_z(int N, int nst, int rl) {
+  return nst >= 2 && (rl <= kFusedMaxRadixShort || (rl <= kFusedMaxRadix && N >= kFusedWideMinN));
+}
 // (complex FP32 only: the double-float fused step needs 168 registers and ran
 // slower than the separate stages, 54.9 vs 41.6 ms per N=65536, L=32 pass.)
 inline int green_perm_radix(int f, const AxisPlan& pz) {
-  return (f == 3 && pz.nst >= 2 && pz.radix[pz.nst - 1] <= kFusedMaxRadix) ? pz.radix[pz.nst - 1] : 0;
+  return (f == 3 && fused_z(pz.N, pz.nst, pz.radix[pz.nst - 1])) ? pz.radix[pz.nst - 1] : 0;
 }
 BDDA_HD int green_pos(int p, int N, int rl) { return rl ? (p % rl) * (N / rl) + p / rl : p; }
 
@@ -63,7 +70,7 @@ struct MvpGeom {
   AxisPlan px, py, pz;
   int nzt;                     // ceil(nz / kTZ)
   int gperm;                   // Green spectrum layout along z: 0 natural (ghat[.][c][p]); else the z plan's
-                               // last radix Rl, ghat[.][c][(p % Rl) (Pz / Rl) + p / Rl] (see kFusedMaxRadix)
+                               // last radix Rl, ghat[.][c][(p % Rl) (Pz / Rl) + p / Rl] (see fused_z)
   MvpTune tune;                // launch schedule of the tile passes
   unsigned passes = 0x1fu;     // passes launched (bit 0 = A .. bit 4 = E); the autotuner times them one by one
   int ntiles;                  // (y, z-tile) pairs holding >= 1 dipole

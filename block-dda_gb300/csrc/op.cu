@@ -197,9 +197,9 @@ static cudaError_t autotune_f32(MvpGeom g, const MvpPrec<float>& p, const float2
   MvpTune t;  // defaults
   float dummy = 0.f;
   if (e == cudaSuccess) e = timed(1u, t, &dummy);  // pass A fills T1
-  const int yw[4] = {1, 2, 4, 8};
+  const int yw[4] = {2, 4, 8, 16};
   int best = -1;
-  for (int i = 0; i < 8 && e == cudaSuccess; ++i) {  // y pass: buffers 1, 2 x waves 1, 2, 4, 8
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i) {  // y pass: buffers 1, 2 x waves 2, 4, 8, 16
     MvpTune c = t;
     c.ybuf = 1 + i / 4;
     c.ywaves = yw[i % 4];
@@ -302,6 +302,7 @@ int op_block_mvp(Op* op, const Occupancy& o, const typename cplx<T>::type* x, in
         g.tune = rec.tune;
       }
     }
+    if (op->zkern_force >= 0) g.tune.zkern = op->zkern_force;
   }
   cudaError_t e = launch_block_mvp<A>(g, ta, (const CA*)x, ldx, (CA*)y, ldy, L, (const CA*)diag, (const CA*)jpre,
                                       op->t1[pi].as<CA>(), op->t2[pi].as<CA>(), st, &op->timer, done);
@@ -585,6 +586,14 @@ int bdda_op_set_timing(bdda_op* op, int enable) {
   std::lock_guard<std::mutex> lk(op->mu);
   op->timer.enabled = enable != 0;
   op->timer.mask = enable == 2 ? (1u << kPassC) | (1u << kPassC64) : ~0u;
+  return BDDA_OK;
+}
+
+int bdda_op_set_z_kernel(bdda_op* op, int kind) {
+  if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
+  if (kind < -1 || kind > 2) { set_error("z kernel must be -1 (default), 0 scalar, 1 packed or 2 pipelined"); return BDDA_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(op->mu);
+  op->zkern_force = kind;
   return BDDA_OK;
 }
 

@@ -74,7 +74,7 @@ k_pass_c_packed(float2* __restrict__ t2, int L, int Px, int Py, int nz, int nzp,
   const ptrdiff_t boff = has_b ? (ptrdiff_t)(3 * fstride) : 0;  // right-hand side la + 1
   pk::stage0_from_global<P, 3>(s0, twz, lane, nz, g0, fstride, boff);
   const float2* gl = ghat + (size_t)line * 6 * Pz;
-  if constexpr (P::nst >= 2 && P::Rl <= kFusedMaxRadix) {  // the spectrum is last-radix-major
+  if constexpr (fused_z(P::N, P::nst, P::Rl)) {  // the spectrum is last-radix-major
     // last forward stage, product and first inverse stage fused (pk::middle3)
     pk::forward_to<P, 3, 1, P::nst - 1>(s0, twz, lane, nz);
     pk::middle3<P>(s0, gl, lane);
@@ -105,12 +105,13 @@ template <class P> constexpr bool fits() { return 2 * kZWarps * 3 * P::LW * 16 <
 template <class P> constexpr bool supported() {
   for (int s = 0; s < P::nst; ++s)
     if (P::rad[s] > 16) return false;
-  return P::nst < 2 || P::Rl <= 5 || P::Rl > kFusedMaxRadix;
+  return !fused_z(P::N, P::nst, P::Rl) || P::Rl <= kFusedMaxRadixShort;
 }
 template <class P> bool chosen(const MvpGeom& g, const float4* twzp) {
   if constexpr (!supported<P>()) return false;
   if (!twzp || g.f != 3 || !fits<P>()) return false;
-  return g.tune.zkern < 0 ? worth<P>() && !(P::nst >= 2 && P::Rl <= kFusedMaxRadix) : g.tune.zkern == 1;
+  return g.tune.zkern < 0 ? worth<P>() && !(fused_z(P::N, P::nst, P::Rl) && P::N >= kFusedWideMinN)
+                          : g.tune.zkern == 1;
 }
 // Whether the packed kernel is a candidate for this length (autotuner).
 inline bool packed_fits_lw(int lw) { return 2 * kZWarps * 3 * lw * 16 <= kZSmemMax; }

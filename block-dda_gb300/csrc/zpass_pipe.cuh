@@ -40,7 +40,7 @@ namespace zpipe {
 
 // Plans whose last stage, product and first inverse stage are one step (the
 // complex FP32 spectrum is then last-radix-major, green_perm_radix).
-template <class P> constexpr bool fused() { return P::nst >= 2 && P::Rl <= kFusedMaxRadix; }
+template <class P> constexpr bool fused() { return fused_z(P::N, P::nst, P::Rl); }
 
 // Staging row pitch (complex values): even (16-byte rows for the bulk copies)
 // and congruent to the first stage's span M0 (or M0 + 1) modulo 16, so the

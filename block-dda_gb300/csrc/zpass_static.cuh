@@ -40,7 +40,7 @@ k_pass_c_static(C* __restrict__ t2, int L, int Px, int Py, int nz, int nzp, cons
   constexpr bool six = SIX;
   constexpr int halves = six ? 2 : 1;  // line triples: E, then M
   const C* gl = ghat + (size_t)line * (six ? 9 : 6) * Pz;
-  if constexpr (!SIX && sizeof(C) == sizeof(float2) && P::nst >= 2 && P::Rl <= kFusedMaxRadix) {
+  if constexpr (!SIX && sizeof(C) == sizeof(float2) && fused_z(P::N, P::nst, P::Rl)) {
     // complex FP32 (its spectrum is last-radix-major)
     // last forward stage, product and first inverse stage fused (middle3)
     sfft::stage0_from_global<P, 3, C>(s0, twz, lane, nz, g0, fstride);

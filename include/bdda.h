@@ -485,8 +485,8 @@ int bdda_op_set_graphs(bdda_op* op, int on);
  * are FFTW_ESTIMATE).  With on = 1 (the default) the first complex FP32 block
  * MVP of an nrhs whose FFT workspace is at least 64 MiB times, with CUDA
  * events on the operator's own buffers, the candidates of each tile pass's
- * launch schedule -- y passes double- or single-buffered with a grid of 1, 2,
- * 4 or 8 waves of the resident CTAs, the scalar, packed-pair or pipelined z
+ * launch schedule -- y passes double- or single-buffered with a grid of 2, 4,
+ * 8 or 16 waves of the resident CTAs, the scalar, packed-pair or pipelined z
  * pass where they run the geometry, x passes aiming at 5, 10 or 20 CTAs per
  * SM -- and keeps the fastest (also for later operators of the same box,
  * occupancy and nrhs in this process).  Not inside stream capture.  The
@@ -498,11 +498,19 @@ int bdda_op_set_autotune(bdda_op* op, int on);
 /* The schedule in use for nrhs L: schedule = {y waves, y buffers, z pass (-1
  * default rule, 0 scalar, 1 packed, 2 pipelined), x CTAs per SM};
  * candidate_ms (may be null): measured ms of pass B with 1 then 2 buffers x
- * waves 1, 2, 4, 8 ([0..7]), pass C scalar / packed ([8..9]), pass A at 5,
+ * waves 2, 4, 8, 16 ([0..7]), pass C scalar / packed ([8..9]), pass A at 5,
  * 10, 20 CTAs per SM ([10..12]), pass C pipelined ([13]), -1 where not
  * measured.  BDDA_ERR_NOT_CONVERGED when L was not tuned (defaults
  * returned). */
 int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[14]);
+/* Forces the complex FP32 pass C kernel for every nrhs: -1 the autotuned /
+ * default choice, 0 scalar, 1 packed-pair, 2 pipelined.  Where the forced
+ * kernel cannot run the operator's z plan (packed: radices above 16 or a fused
+ * last radix above 5, or more shared memory than two CTAs per SM; pipelined:
+ * f = 6 or more shared memory than a CTA may take) the scalar kernel runs.
+ * The kernels compute the same transform; the packed one rounds its pair
+ * arithmetic differently (FP32 MVP tolerance). */
+int bdda_op_set_z_kernel(bdda_op* op, int kind);
 /* Reads and clears the operator's kernel status word.  The pipelined z pass
  * (complex FP32) waits on its bulk copies for at most 2 s; a wait that gives
  * up (never expected) sets the word and the MVP's results are invalid.

@@ -46,13 +46,15 @@ def test_autotuner_keeps_fastest_candidate_and_results():
     xs = cand["x_cta_per_sm"]
     assert str(sched["x_cta_per_sm"]) == min(xs, key=xs.get)
     z = {k: v for k, v in cand["z_pass"].items() if v > 0}
-    # Pz = 150, plan 15 x 10 with the fused Green step: the scalar and pipelined kernels are the candidates
-    # (the packed kernel fuses only up to radix 5), and the default rule runs the pipelined one
-    assert op.info()[0][2] == 150 and op.plans()["z"] == [15, 10]
-    assert sorted(z) == ["pipelined", "scalar"]
+    # Pz = 150, plan 10 x 15 (no fused step): scalar, packed and pipelined kernels are the candidates, and the
+    # default rule runs the packed one (three 8-warp CTAs of it fit)
+    assert op.info()[0][2] == 150 and op.plans()["z"] == [10, 15]
+    assert sorted(z) == ["packed", "pipelined", "scalar"]
     assert sched["z_pass"] == min(z, key=z.get)
-    # same arithmetic in both kernels (the pipelined one stages rows, spectrum and twiddles in shared memory)
-    assert np.linalg.norm(y_tuned - y_def) / np.linalg.norm(y_def) < 1e-6
+    if sched["z_pass"] == "packed":
+        assert np.array_equal(y_tuned, y_def)
+    else:   # the packed kernel rounds its pair arithmetic differently
+        assert np.linalg.norm(y_tuned - y_def) / np.linalg.norm(y_def) < 5e-6
     # the tuned schedule is kept: a second call gives the same bits
     assert np.array_equal(_mvp(op, x, L, n, prob.diag), y_tuned)
     # and a solve on the tuned operator still meets its true residual

@@ -69,6 +69,36 @@ def test_every_z_plan_fp32_vs_fp64():
         assert rel < TOL32, (Pz, nz, rel)
 
 
+@pytest.mark.parametrize("L", [3, 8])
+def test_every_z_plan_pipelined_and_scalar_kernels(L):
+    """The pipelined z pass (bulk copies of rows, spectrum and twiddles into
+    shared memory, persistent CTAs) against the scalar kernel on every z
+    length, fused and unfused plans: the same arithmetic (agreement to FP32
+    rounding), and both against the FP64 MVP.  L = 3 leaves CTA warps of the
+    pipelined kernel without a task in the last round of a line; L = 8 fills
+    them."""
+    import torch
+    rng = np.random.default_rng(11 + L)
+    for i, (Pz, nz) in enumerate(_nz_per_pz()):
+        n = (4, 3, nz)
+        N = int(np.prod(n))
+        nocc = max(2, (2 * N) // 3)
+        addr = np.sort(rng.choice(N, size=nocc, replace=False)).astype(np.int32)
+        x = rng.standard_normal((3 * nocc, L)) + 1j * rng.standard_normal((3 * nocc, L))
+        op = bdda.Operator(n, 0.03, 2 * np.pi / 0.55)
+        op.set_dipoles(addr)
+        op.set_autotune(False)
+        y64 = _mvp(op, x, L, 3 * nocc, bdda.PREC_FP64, torch.complex128)
+        op.set_z_kernel("pipelined")
+        yp = _mvp(op, x, L, 3 * nocc, bdda.PREC_FP32, torch.complex64)
+        op.set_z_kernel("scalar")
+        ys = _mvp(op, x, L, 3 * nocc, bdda.PREC_FP32, torch.complex64)
+        op.check_status()
+        ref = np.linalg.norm(y64)
+        assert np.linalg.norm(yp - y64) / ref < TOL32, (Pz, nz)
+        assert np.linalg.norm(yp - ys) / ref < 1e-6, (Pz, nz)
+
+
 def _to_df(a):  # complex128 -> float32 [..., 4] = (re_hi, re_lo, im_hi, im_lo)
     hi_r = a.real.astype(np.float32)
     hi_i = a.imag.astype(np.float32)

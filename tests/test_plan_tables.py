@@ -83,8 +83,10 @@ def test_z_tables_radix_limits():
     assert z[250][2] == (25, 10) and z[243][2] == (27, 9)
 
 
-@pytest.mark.parametrize("n", [125, 243, 250])
+@pytest.mark.parametrize("n", [125, 150, 243, 250])
 def test_generator_reproduces_z_entries(n):
     g = _gen()
-    rad, S, LW = g.choose(n, g.cost_zf, g.FIRST_RADICES, g.Z_MAX_PAD)
+    rad, S, LW = g.z_entry(n)
     assert _table("zplans.inc", "BDDA_ZPLAN")[n] == (S, LW, tuple(rad))
+    if n <= 150:   # packed-pass lengths keep the 16-byte table's plan
+        assert _table("zwplans.inc", "BDDA_ZWPLAN")[n] == (S, LW, tuple(rad))
