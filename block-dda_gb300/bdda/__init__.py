@@ -41,6 +41,7 @@ EXPORTS = [
     "bdda_polarizabilities", "bdda_diag_a", "bdda_op_set_wavenumber", "bdda_sweep", "bdda_mie_q",
     "bdda_format_result", "bdda_request_footprint_f", "bdda_server_set_spectrum_cache", "bdda_server_cache_stats",
     "bdda_op_set_autotune", "bdda_op_get_tuning", "bdda_op_check_status", "bdda_op_set_z_kernel",
+    "bdda_op_test_z_stall",
 ]
 
 SHAPES = {"sphere": 0, "cube": 1, "ellipsoid": 2, "cuboid": 3, "cylinder": 4, "rounded_cylinder": 5}
@@ -174,6 +175,7 @@ def lib(build_if_missing: bool = False):
     L.bdda_op_get_tuning.argtypes = [vp, ct.c_int, ip, ct.POINTER(ct.c_float)]
     L.bdda_op_check_status.argtypes = [vp]
     L.bdda_op_set_z_kernel.argtypes = [vp, ct.c_int]
+    L.bdda_op_test_z_stall.argtypes = [vp, ct.c_int]
     L.bdda_op_kernel_stats.argtypes = [vp, dp, ct.POINTER(ct.c_longlong), ct.c_int, ct.c_int]
     L.bdda_last_error.restype = ct.c_char_p
     L.bdda_request_footprint.argtypes = [ip, ct.c_int, ct.c_int, ct.c_int]
@@ -330,6 +332,10 @@ class Operator:
     def set_z_kernel(self, kind="default"):
         """Force the complex FP32 pass C kernel: "default", "scalar", "packed" or "pipelined"."""
         _check(lib().bdda_op_set_z_kernel(self._h, {"default": -1, "scalar": 0, "packed": 1, "pipelined": 2}[kind]))
+
+    def test_z_stall(self, on=True):
+        """Test hook: the pipelined z pass gives up one bounded wait (bdda_op_test_z_stall)."""
+        _check(lib().bdda_op_test_z_stall(self._h, 1 if on else 0))
 
     def check_status(self):
         """Raise if a kernel of this operator reported a failed bounded wait (bdda_op_check_status)."""

@@ -76,6 +76,7 @@ struct MvpGeom {
   int ntiles;                  // (y, z-tile) pairs holding >= 1 dipole
   long long tile_rows;         // sum over those tiles of their valid z count
   int* kstat = nullptr;        // status word of the pipelined z pass (1: a bounded copy wait gave up)
+  int zstall = 0;              // test hook: the pipelined z pass gives up one wait (bdda_op_test_z_stall)
   const int* occ;              // [nx*ny*nz] dipole index or -1
   const int* tiles;            // [ntiles]  y*nzt + zt
   const unsigned char* tmask;  // [ny*nzt]  1 for those tiles

@@ -597,6 +597,13 @@ int bdda_op_set_z_kernel(bdda_op* op, int kind) {
   return BDDA_OK;
 }
 
+int bdda_op_test_z_stall(bdda_op* op, int on) {
+  if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
+  std::lock_guard<std::mutex> lk(op->mu);
+  op->zstall = on != 0;
+  return BDDA_OK;
+}
+
 int bdda_op_check_status(bdda_op* op) {
   if (!op) { set_error("null operator"); return BDDA_ERR_INVALID; }
   std::lock_guard<std::mutex> lk(op->mu);

@@ -114,6 +114,7 @@ struct Op {
   bool autotune = true;
   std::map<int, TuneRec> tuned;
   int zkern_force = -1;  // pass C kernel forced for every nrhs (bdda_op_set_z_kernel), -1: tuned / default
+  int zstall = 0;        // test hook (bdda_op_test_z_stall)
 
   // signature of every buffer a block MVP's kernels are launched with
   unsigned long long buffer_sig() const {
@@ -136,6 +137,7 @@ struct Op {
     g.nzt = (n[2] + kTZ - 1) / kTZ;
     g.gperm = 0;
     g.kstat = kstat.as<int>();
+    g.zstall = zstall;
     g.ntiles = o.ntiles;
     g.tile_rows = o.tile_rows;
     g.occ = o.occ.as<int>();

@@ -23,7 +23,9 @@
 // writes global memory directly).  Every wait on a copy is bounded
 // (async_copy.cuh); a wait that gives up sets *status = 1, the warp stops
 // computing, waits (bounded) for the copies it issued and returns, and the
-// host reports the error.
+// host reports the error.  stall != 0 (test hook, bdda_op_test_z_stall):
+// warp 0 of CTA 0 first waits on a barrier that nothing arrives on, so that
+// path runs without a fault.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -52,7 +54,7 @@ template <class P> __host__ __device__ inline int stage_pitch(int nzp) {
   return nzp + (((Me - nzp) % 16) + 16) % 16;
 }
 
-constexpr int kHeader = 128;  // barriers (kZWarps + 2) x 8 B, counters
+constexpr int kHeader = 128;  // barriers (kZWarps + 2) x 8 B, counters, the test barrier
 
 template <class P> __host__ __device__ inline int tw_elems() { return (P::TWO(P::nst) + 1) & ~1; }
 
@@ -65,7 +67,7 @@ template <class P> __host__ __device__ inline size_t smem_bytes(int nw, int nzp)
 template <class P>
 __global__ void __launch_bounds__(kZWarps * 32)
 k_pass_c_pipe(float2* __restrict__ t2, int L, int nlines, int nz, int nzp, const float2* __restrict__ twz,
-              const float2* __restrict__ ghat, const int* done, int* status) {
+              const float2* __restrict__ ghat, const int* done, int* status, int stall) {
   if (done && *(volatile const int*)done) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   constexpr int Pz = P::N, LW = P::LW;
@@ -77,6 +79,7 @@ k_pass_c_pipe(float2* __restrict__ t2, int L, int nlines, int nz, int nzp, const
   int* gdone = reinterpret_cast<int*>(gbar + 2);  // [2] warps done with the spectrum buffer
   int* glast = gdone + 2;                         // [2] line whose spectrum was last issued into the buffer
   volatile int* abort_flag = glast + 2;
+  uint64_t* tbar = reinterpret_cast<uint64_t*>(smem_raw + 104);  // never arrived on (test hook)
   float2* tws = reinterpret_cast<float2*>(smem_raw + kHeader);
   float2* gs = tws + tw_elems<P>();
   float2* stg = gs + 2 * 6 * Pz;
@@ -103,6 +106,7 @@ k_pass_c_pipe(float2* __restrict__ t2, int L, int nlines, int nz, int nzp, const
     for (int w = 0; w < kZWarps; ++w) acp::bar_init(&xbar[w], 1);
     acp::bar_init(&gbar[0], 1);
     acp::bar_init(&gbar[1], 1);
+    acp::bar_init(tbar, 1);
     gdone[0] = gdone[1] = 0;
     glast[0] = glast[1] = -1;
     *abort_flag = 0;
@@ -120,7 +124,8 @@ k_pass_c_pipe(float2* __restrict__ t2, int L, int nlines, int nz, int nzp, const
   bool xpend = true;
   if (lane == 0) issue_x(0, warp);
   bool ok = true;
-  while (k < nk) {
+  if (stall && blockIdx.x == 0 && warp == 0) ok = __all_sync(0xffffffffu, acp::wait(tbar, 0));  // gives up
+  while (ok && k < nk) {
     ok = __all_sync(0xffffffffu, !*abort_flag && acp::wait(&xbar[warp], xpar));
     if (!ok) break;
     xpend = false;
@@ -211,7 +216,8 @@ bool launch(const MvpGeom& g, float2* t2, int L, const float2* twz, const float2
   }
   const long long nlines = (long long)g.Px * g.Py;
   const long long grid = std::min<long long>(nlines, (long long)per_sm * nsm);
-  k_pass_c_pipe<P><<<(unsigned)grid, nw * 32, bytes, st>>>(t2, L, (int)nlines, g.nz, g.nzp, twz, ghat, done, g.kstat);
+  k_pass_c_pipe<P><<<(unsigned)grid, nw * 32, bytes, st>>>(t2, L, (int)nlines, g.nz, g.nzp, twz, ghat, done, g.kstat,
+                                                             g.zstall);
   *err = cudaGetLastError();
   return true;
 }

@@ -518,6 +518,11 @@ int bdda_op_set_z_kernel(bdda_op* op, int kind);
  * bdda_op_mvp_device, synchronise its stream and call this.  BDDA_OK, or
  * BDDA_ERR_CUDA with a message. */
 int bdda_op_check_status(bdda_op* op);
+/* Test hook of that path: while on, warp 0 of the first CTA of every
+ * pipelined z pass first waits on a barrier that nothing arrives on, gives up
+ * after the 2 s limit and sets the status word; the launch's results are then
+ * invalid, the context stays usable. */
+int bdda_op_test_z_stall(bdda_op* op, int on);
 
 /*
  * Per-kernel totals since the last reset: ms[i], launches[i] for
