@@ -105,6 +105,55 @@ BDDA_HD dfzc cmake(dfz a, dfz b) { dfzc c; c.x = a; c.y = b; return c; }
 
 template <typename C> BDDA_HD C cadd(C a, C b) { return cmake(a.x + b.x, a.y + b.y); }
 template <typename C> BDDA_HD C csub(C a, C b) { return cmake(a.x - b.x, a.y - b.y); }
+
+#if defined(__CUDA_ARCH__)
+// Complex FP32 values as one two-lane f32x2 operand (sm_100-family
+// add/sub/mul/fma.rn.f32x2: both parts in one issue slot, each part rounded as
+// the scalar instruction rounds it).  Device code only; the host build and the
+// other element types keep the scalar templates above.
+namespace f2 {
+__device__ __forceinline__ unsigned long long pk(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 up(unsigned long long r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+__device__ __forceinline__ unsigned long long dup(float c) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(c));
+  return r;
+}
+__device__ __forceinline__ float2 add(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
+  return up(d);
+}
+__device__ __forceinline__ float2 sub(float2 a, float2 b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
+  return up(d);
+}
+// c a (real c)
+__device__ __forceinline__ float2 scale(float c, float2 a) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(dup(c)), "l"(pk(a)));
+  return up(d);
+}
+// c a + b (real c), one rounding per part
+__device__ __forceinline__ float2 scale_add(float c, float2 a, float2 b) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(dup(c)), "l"(pk(a)), "l"(pk(b)));
+  return up(d);
+}
+}  // namespace f2
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return f2::add(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return f2::sub(a, b); }
+#endif
+
 template <typename C> BDDA_HD C cmul(C a, C b) {
   return cmake(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }

@@ -45,6 +45,14 @@ namespace bdda {
 
 template <typename C> BDDA_FFT_FN C mul_i(C a) { return cmake(-a.y, a.x); }     // i a
 template <typename C> BDDA_FFT_FN C mul_mi(C a) { return cmake(a.y, -a.x); }    // -i a
+// a + w b and a - w b with w = i (INV) or -i, part by part: no swapped copy of
+// b is formed (a two-lane f32x2 add would need one in a register pair)
+template <bool INV, typename C> BDDA_FFT_FN C add_ib(C a, C b) {
+  return INV ? cmake(a.x - b.y, a.y + b.x) : cmake(a.x + b.y, a.y - b.x);
+}
+template <bool INV, typename C> BDDA_FFT_FN C sub_ib(C a, C b) {
+  return INV ? cmake(a.x + b.y, a.y - b.x) : cmake(a.x - b.y, a.y + b.x);
+}
 
 template <bool INV, typename C> BDDA_FFT_FN void dft2(C* v) {
   C a = v[0], b = v[1];
@@ -56,23 +64,30 @@ template <bool INV, typename C> BDDA_FFT_FN void dft3(C* v) {
   using T = decltype(C::x);
   const T s = T(0.86602540378443864676);  // sin(2 pi / 3)
   C t1 = cadd(v[1], v[2]);
-  C t2 = cmake(v[0].x - T(0.5) * t1.x, v[0].y - T(0.5) * t1.y);
   C d = csub(v[1], v[2]);
-  C t3 = cmake(s * d.x, s * d.y);
+  C t2, t3;
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(C) == sizeof(float2) && sizeof(T) == sizeof(float)) {  // two-lane f32x2
+    t2 = f2::scale_add(-0.5f, t1, v[0]);
+    t3 = f2::scale(s, d);
+  } else
+#endif
+  {
+    t2 = cmake(v[0].x - T(0.5) * t1.x, v[0].y - T(0.5) * t1.y);
+    t3 = cmake(s * d.x, s * d.y);
+  }
   v[0] = cadd(v[0], t1);
-  C it3 = INV ? mul_i(t3) : mul_mi(t3);
-  v[1] = cadd(t2, it3);
-  v[2] = csub(t2, it3);
+  v[1] = add_ib<INV>(t2, t3);
+  v[2] = sub_ib<INV>(t2, t3);
 }
 
 template <bool INV, typename C> BDDA_FFT_FN void dft4(C* v) {
   C a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
   C b0 = cadd(v[1], v[3]), b1 = csub(v[1], v[3]);
-  C ib1 = INV ? mul_i(b1) : mul_mi(b1);
   v[0] = cadd(a0, b0);
   v[2] = csub(a0, b0);
-  v[1] = cadd(a1, ib1);
-  v[3] = csub(a1, ib1);
+  v[1] = add_ib<INV>(a1, b1);
+  v[3] = sub_ib<INV>(a1, b1);
 }
 
 template <bool INV, typename C> BDDA_FFT_FN void dft5(C* v) {
@@ -83,17 +98,26 @@ template <bool INV, typename C> BDDA_FFT_FN void dft5(C* v) {
   const T s2 = T(0.58778525229247312917);   // sin(4 pi / 5)
   C t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
   C t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
-  C a1 = cmake(v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y);
-  C a2 = cmake(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
-  C b1 = cmake(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
-  C b2 = cmake(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
-  C ib1 = INV ? mul_i(b1) : mul_mi(b1);
-  C ib2 = INV ? mul_i(b2) : mul_mi(b2);
+  C a1, a2, b1, b2;
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(C) == sizeof(float2) && sizeof(T) == sizeof(float)) {  // two-lane f32x2
+    a1 = f2::scale_add(c2, t2, f2::scale_add(c1, t1, v[0]));
+    a2 = f2::scale_add(c1, t2, f2::scale_add(c2, t1, v[0]));
+    b1 = f2::scale_add(s2, t4, f2::scale(s1, t3));
+    b2 = f2::scale_add(-s1, t4, f2::scale(s2, t3));
+  } else
+#endif
+  {
+    a1 = cmake(v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y);
+    a2 = cmake(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
+    b1 = cmake(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+    b2 = cmake(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+  }
   v[0] = cadd(v[0], cadd(t1, t2));
-  v[1] = cadd(a1, ib1);
-  v[4] = csub(a1, ib1);
-  v[2] = cadd(a2, ib2);
-  v[3] = csub(a2, ib2);
+  v[1] = add_ib<INV>(a1, b1);
+  v[4] = sub_ib<INV>(a1, b1);
+  v[2] = add_ib<INV>(a2, b2);
+  v[3] = sub_ib<INV>(a2, b2);
 }
 
 template <bool INV, typename C> BDDA_FFT_FN void dft8(C* v) {
