@@ -45,14 +45,6 @@ namespace bdda {
 
 template <typename C> BDDA_FFT_FN C mul_i(C a) { return cmake(-a.y, a.x); }     // i a
 template <typename C> BDDA_FFT_FN C mul_mi(C a) { return cmake(a.y, -a.x); }    // -i a
-// a + w b and a - w b with w = i (INV) or -i, part by part: no swapped copy of
-// b is formed (a two-lane f32x2 add would need one in a register pair)
-template <bool INV, typename C> BDDA_FFT_FN C add_ib(C a, C b) {
-  return INV ? cmake(a.x - b.y, a.y + b.x) : cmake(a.x + b.y, a.y - b.x);
-}
-template <bool INV, typename C> BDDA_FFT_FN C sub_ib(C a, C b) {
-  return INV ? cmake(a.x + b.y, a.y - b.x) : cmake(a.x - b.y, a.y + b.x);
-}
 
 template <bool INV, typename C> BDDA_FFT_FN void dft2(C* v) {
   C a = v[0], b = v[1];
@@ -77,17 +69,19 @@ template <bool INV, typename C> BDDA_FFT_FN void dft3(C* v) {
     t3 = cmake(s * d.x, s * d.y);
   }
   v[0] = cadd(v[0], t1);
-  v[1] = add_ib<INV>(t2, t3);
-  v[2] = sub_ib<INV>(t2, t3);
+  C it3 = INV ? mul_i(t3) : mul_mi(t3);
+  v[1] = cadd(t2, it3);
+  v[2] = csub(t2, it3);
 }
 
 template <bool INV, typename C> BDDA_FFT_FN void dft4(C* v) {
   C a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
   C b0 = cadd(v[1], v[3]), b1 = csub(v[1], v[3]);
+  C ib1 = INV ? mul_i(b1) : mul_mi(b1);
   v[0] = cadd(a0, b0);
   v[2] = csub(a0, b0);
-  v[1] = add_ib<INV>(a1, b1);
-  v[3] = sub_ib<INV>(a1, b1);
+  v[1] = cadd(a1, ib1);
+  v[3] = csub(a1, ib1);
 }
 
 template <bool INV, typename C> BDDA_FFT_FN void dft5(C* v) {
@@ -113,11 +107,13 @@ template <bool INV, typename C> BDDA_FFT_FN void dft5(C* v) {
     b1 = cmake(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
     b2 = cmake(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
   }
+  C ib1 = INV ? mul_i(b1) : mul_mi(b1);
+  C ib2 = INV ? mul_i(b2) : mul_mi(b2);
   v[0] = cadd(v[0], cadd(t1, t2));
-  v[1] = add_ib<INV>(a1, b1);
-  v[4] = sub_ib<INV>(a1, b1);
-  v[2] = add_ib<INV>(a2, b2);
-  v[3] = sub_ib<INV>(a2, b2);
+  v[1] = cadd(a1, ib1);
+  v[4] = csub(a1, ib1);
+  v[2] = cadd(a2, ib2);
+  v[3] = csub(a2, ib2);
 }
 
 template <bool INV, typename C> BDDA_FFT_FN void dft8(C* v) {
