@@ -81,6 +81,11 @@ def test_z_tables_radix_limits():
         assert all(r <= 16 for r in rad), (n, rad)
     # the default workload's z length: two stages, fused last radix
     assert z[250][2] == (25, 10) and z[243][2] == (27, 9)
+    # lines shorter than the two-stage threshold (the packed-pair kernel's range) keep the 16-byte plans
+    g = _gen()
+    for n in z:
+        if n < g.FUSED_WIDE_MIN_N:
+            assert z[n] == zw[n], n
 
 
 @pytest.mark.parametrize("n", [125, 150, 243, 250])
@@ -90,3 +95,13 @@ def test_generator_reproduces_z_entries(n):
     assert _table("zplans.inc", "BDDA_ZPLAN")[n] == (S, LW, tuple(rad))
     if n <= 150:   # packed-pass lengths keep the 16-byte table's plan
         assert _table("zwplans.inc", "BDDA_ZWPLAN")[n] == (S, LW, tuple(rad))
+
+
+def test_generator_constants_match_the_kernels():
+    """The generator's fused-step rule is the kernels' (fused_z, mvp.hpp)."""
+    import re
+    g = _gen()
+    src = open(os.path.join(CSRC, "mvp.hpp")).read()
+    const = {k: int(v) for k, v in re.findall(r"constexpr int (k\w+) = (\d+);", src)}
+    assert const["kFusedMaxRadix"] == g.FUSED_MAX
+    assert const["kFusedWideMinN"] == g.FUSED_WIDE_MIN_N
