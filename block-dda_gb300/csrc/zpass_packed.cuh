@@ -113,8 +113,6 @@ template <class P> bool chosen(const MvpGeom& g, const float4* twzp) {
   return g.tune.zkern < 0 ? worth<P>() && !(fused_z(P::N, P::nst, P::Rl) && P::N >= kFusedWideMinN)
                           : g.tune.zkern == 1;
 }
-// Whether the packed kernel is a candidate for this length (autotuner).
-inline bool packed_fits_lw(int lw) { return 2 * kZWarps * 3 * lw * 16 <= kZSmemMax; }
 
 template <class P>
 cudaError_t launch(const MvpGeom& g, float2* t2, int L, const float4* twz, const float2* ghat, cudaStream_t st,
