@@ -317,16 +317,17 @@ class Operator:
 
     def tuning(self, L):
         """(schedule dict, candidate ms dict, measured?) for nrhs L (bdda_op_get_tuning)."""
-        sch = np.zeros(4, np.int32)
-        ms = (ct.c_float * 14)()
+        sch = np.zeros(6, np.int32)
+        ms = (ct.c_float * 22)()
         rc = lib().bdda_op_get_tuning(self._h, int(L), _iptr(sch), ms)
         _check(rc, (ERR_NOT_CONVERGED,))
         cand = {"y": {f"buf{1 + i // 4}_waves{(2, 4, 8, 16)[i % 4]}": ms[i] for i in range(8)},
+                "y_inverse": {f"buf{1 + i // 4}_waves{(2, 4, 8, 16)[i % 4]}": ms[14 + i] for i in range(8)},
                 "z_pass": {"scalar": ms[8], "packed": ms[9], "pipelined": ms[13]},
                 "x_cta_per_sm": {str(v): ms[10 + i] for i, v in enumerate((5, 10, 20))}}
         return ({"y_waves": int(sch[0]), "y_buffers": int(sch[1]),
                  "z_pass": {-1: "default", 0: "scalar", 1: "packed", 2: "pipelined"}[int(sch[2])],
-                 "x_cta_per_sm": int(sch[3])},
+                 "x_cta_per_sm": int(sch[3]), "y_inverse_waves": int(sch[4]), "y_inverse_buffers": int(sch[5])},
                 cand, rc == OK)
 
     def set_z_kernel(self, kind="default"):

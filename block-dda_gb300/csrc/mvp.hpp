@@ -58,6 +58,8 @@ struct MvpTune {
   int zkern = -1;
   int ywaves = 4;    // passes B, D: grid of this many waves of the CTAs resident per SM
   int ybuf = 2;      // passes B, D: tile buffers per CTA (2: prefetch the next task; 1: twice the CTAs)
+  int ybufd = 0;     // pass D's own buffers and waves when > 0 (the autotuner times it separately)
+  int ywavesd = 0;
   int xcta = 10;     // passes A, E: aim at this many CTAs per SM (fields split into groups)
 };
 

@@ -232,6 +232,18 @@ static cudaError_t autotune_f32(MvpGeom g, const MvpPrec<float>& p, const float2
       if (e == cudaSuccess) t.zkern = kbest;
     }
   }
+  best = -1;
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i) {  // inverse y pass (D, reads T2): its own buffers and waves
+    MvpTune c = t;
+    c.ybufd = 1 + i / 4;
+    c.ywavesd = yw[i % 4];
+    e = timed(8u, c, &rec.ms[14 + i]);
+    if (e == cudaSuccess && (best < 0 || rec.ms[14 + i] < rec.ms[14 + best])) best = i;
+  }
+  if (e == cudaSuccess) {
+    t.ybufd = 1 + best / 4;
+    t.ywavesd = yw[best % 4];
+  }
   const int xc[3] = {5, 10, 20};
   best = -1;
   for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
@@ -566,7 +578,7 @@ int bdda_op_set_autotune(bdda_op* op, int on) {
   return BDDA_OK;
 }
 
-int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[14]) {
+int bdda_op_get_tuning(bdda_op* op, int L, int schedule[6], float candidate_ms[22]) {
   if (!op || !schedule) { set_error("null argument"); return BDDA_ERR_INVALID; }
   std::lock_guard<std::mutex> lk(op->mu);
   const MvpTune def;
@@ -576,8 +588,10 @@ int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[1
   schedule[1] = t.ybuf;
   schedule[2] = t.zkern;
   schedule[3] = t.xcta;
+  schedule[4] = t.ywavesd > 0 ? t.ywavesd : t.ywaves;
+  schedule[5] = t.ybufd > 0 ? t.ybufd : t.ybuf;
   if (candidate_ms)
-    for (int i = 0; i < 14; ++i) candidate_ms[i] = it != op->tuned.end() ? it->second.ms[i] : -1.f;
+    for (int i = 0; i < 22; ++i) candidate_ms[i] = it != op->tuned.end() ? it->second.ms[i] : -1.f;
   return it != op->tuned.end() && it->second.measured ? BDDA_OK : BDDA_ERR_NOT_CONVERGED;
 }
 

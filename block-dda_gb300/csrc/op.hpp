@@ -109,8 +109,8 @@ struct Op {
   // (bdda_op_set_autotune, bdda_op_get_tuning); candidate times in ms:
   // [0..7] pass B with 1 then 2 buffers x 2, 4, 8, 16 waves, [8..9] pass C
   // scalar / packed, [10..12] pass A at 5, 10, 20 CTAs per SM, [13] pass C
-  // pipelined; negative: not a candidate.
-  struct TuneRec { MvpTune tune; float ms[14]; bool measured; };
+  // pipelined, [14..21] pass D as [0..7]; negative: not a candidate.
+  struct TuneRec { MvpTune tune; float ms[22]; bool measured; };
   bool autotune = true;
   std::map<int, TuneRec> tuned;
   int zkern_force = -1;  // pass C kernel forced for every nrhs (bdda_op_set_z_kernel), -1: tuned / default

@@ -67,7 +67,8 @@ cudaError_t launch_y_buf(int pass, const TileArgs& a) {
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kTileThreads, smem_bd) != cudaSuccess || nb < 1) nb = 1;
       resident[inv] = nb;
     }
-    return std::min(ntask2, g.tune.ywaves * resident[inv] * a.sms);
+    const int waves = (inv && g.tune.ywavesd > 0) ? g.tune.ywavesd : g.tune.ywaves;
+    return std::min(ntask2, waves * resident[inv] * a.sms);
   };
   if (pass == kTileB) {
     if ((e = set_smem(tile::k_pass_y2i<false, P, NBUF>, smem_bd, ob, cb)) != cudaSuccess) return e;
@@ -83,7 +84,8 @@ cudaError_t launch_y_buf(int pass, const TileArgs& a) {
 
 template <class P>
 cudaError_t launch_y(int pass, const TileArgs& a) {
-  return a.g->tune.ybuf == 1 ? launch_y_buf<P, 1>(pass, a) : launch_y_buf<P, 2>(pass, a);
+  const int nbuf = (pass == kTileD && a.g->tune.ybufd > 0) ? a.g->tune.ybufd : a.g->tune.ybuf;
+  return nbuf == 1 ? launch_y_buf<P, 1>(pass, a) : launch_y_buf<P, 2>(pass, a);
 }
 
 }  // namespace tstatic

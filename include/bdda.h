@@ -496,13 +496,13 @@ int bdda_op_set_graphs(bdda_op* op, int on);
  * forgets the choices. */
 int bdda_op_set_autotune(bdda_op* op, int on);
 /* The schedule in use for nrhs L: schedule = {y waves, y buffers, z pass (-1
- * default rule, 0 scalar, 1 packed, 2 pipelined), x CTAs per SM};
- * candidate_ms (may be null): measured ms of pass B with 1 then 2 buffers x
- * waves 2, 4, 8, 16 ([0..7]), pass C scalar / packed ([8..9]), pass A at 5,
- * 10, 20 CTAs per SM ([10..12]), pass C pipelined ([13]), -1 where not
- * measured.  BDDA_ERR_NOT_CONVERGED when L was not tuned (defaults
- * returned). */
-int bdda_op_get_tuning(bdda_op* op, int L, int schedule[4], float candidate_ms[14]);
+ * default rule, 0 scalar, 1 packed, 2 pipelined), x CTAs per SM, inverse y
+ * (pass D) waves, inverse y buffers}; candidate_ms (may be null): measured ms
+ * of pass B with 1 then 2 buffers x waves 2, 4, 8, 16 ([0..7]), pass C
+ * scalar / packed ([8..9]), pass A at 5, 10, 20 CTAs per SM ([10..12]), pass
+ * C pipelined ([13]), pass D as pass B ([14..21]), -1 where not measured.
+ * BDDA_ERR_NOT_CONVERGED when L was not tuned (defaults returned). */
+int bdda_op_get_tuning(bdda_op* op, int L, int schedule[6], float candidate_ms[22]);
 /* Forces the complex FP32 pass C kernel for every nrhs: -1 the autotuned /
  * default choice, 0 scalar, 1 packed-pair, 2 pipelined.  Where the forced
  * kernel cannot run the operator's z plan (packed: radices above 16 or a fused

@@ -43,6 +43,9 @@ def test_autotuner_keeps_fastest_candidate_and_results():
     assert all(v > 0 for v in ys.values())
     best = min(ys, key=ys.get)
     assert best == f"buf{sched['y_buffers']}_waves{sched['y_waves']}"
+    yd = cand["y_inverse"]
+    assert all(v > 0 for v in yd.values())
+    assert min(yd, key=yd.get) == f"buf{sched['y_inverse_buffers']}_waves{sched['y_inverse_waves']}"
     xs = cand["x_cta_per_sm"]
     assert str(sched["x_cta_per_sm"]) == min(xs, key=xs.get)
     z = {k: v for k, v in cand["z_pass"].items() if v > 0}
